@@ -1,0 +1,376 @@
+"""Synthetic cases in the reference layout (the inputs of the RHS path).
+
+The reference reads Gambit/ICEM meshes that are not shipped, so the cases its
+benchmark configurations describe are generated here, deterministically:
+
+* ``isentropic_vortex`` -- periodic Cartesian box [0, L)^3, inviscid
+  isentropic vortex advected in x (uniform in z).
+* ``taylor_green``      -- periodic [0, 2 pi)^3 with sinusoidally perturbed
+  node positions x_i = xi_i + A sin(xi_j) sin(xi_k) (cyclic), analytic
+  metrics, Taylor-Green vortex initial condition.
+* ``ghost_box``         -- a non-periodic box surrounded by three layers of
+  ghost nodes (loc = 100) with boundary codes on the faces, edges and corners,
+  used to exercise the one-sided stencil branches keyed on ``loc``.
+
+Every generator fills the arrays the reference's host hands to its kernels:
+GRID (neighbour table, loc codes), det, TRANSFORMED (node metrics and the
+half-point metrics of Main.cpp:2369-2440), DETERM, and FLOW.  Row 0 is the
+reference's dummy row; it is given a benign state whose neighbours point to
+itself so that computing it (the reference's NDRange includes it) stays finite.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+from . import layout as L
+
+
+@dataclasses.dataclass
+class Params:
+    """Physical and numerical constants of the RHS path.
+
+    The reference hard-codes mach/reynolds/prandtl/t_inf in Viscous.cl:30-33
+    (1.5, 500, 0.72, 273) and weno_eps in Weno.cl:59 (10e-8); Weno takes Mach
+    as an argument (Weno.cl:36).  ``viscous=0`` zeroes Fv/Ev/Gv (inviscid
+    runs); ``les=0`` drops the mixed-time-scale SGS terms.
+    """
+    mach: float = 1.5
+    reynolds: float = 500.0
+    prandtl: float = 0.72
+    t_inf: float = 273.0
+    weno_eps: float = 1e-7
+    viscous: int = 1
+    les: int = 1
+
+
+@dataclasses.dataclass
+class Case:
+    name: str
+    shape: tuple            # (ni, nj, nk) of owned nodes for structured cases
+    periodic: bool
+    sd_node: int            # owned nodes 1..sd_node
+    g_node: int             # owned + ghost nodes 1..g_node
+    arrays: dict            # layout.empty_arrays(g_node + 1) filled
+    params: Params
+    dt: float
+
+    @property
+    def n_rows(self) -> int:
+        return self.g_node + 1
+
+    def copy(self) -> "Case":
+        return dataclasses.replace(self, arrays={k: v.copy() for k, v in self.arrays.items()},
+                                   params=dataclasses.replace(self.params))
+
+
+# --------------------------------------------------------------- helpers ---
+
+def _flow_from_primitives(flow, rho, u, v, w, p, mach):
+    f = L.FLOW
+    flow[:, f["rho"]] = rho
+    flow[:, f["u"]] = u
+    flow[:, f["v"]] = v
+    flow[:, f["w"]] = w
+    flow[:, f["p"]] = p
+    flow[:, f["t"]] = (1.4 * mach * mach) * (p / rho)
+    flow[:, f["a"]] = np.sqrt(1.4 * p / rho)
+    flow[:, f["e"]] = p / (0.4 * rho)
+    flow[:, f["mu"]] = 0.0
+
+
+def _set_dummy_row(a):
+    """Row 0: neighbours to itself, unit metrics, quiescent unit state."""
+    g = a["grid"][0]
+    for k in ("N0", "N1", "N2", "N3", "N4", "N5", "ID", "loc"):
+        g[k] = 0
+    a["det"][0] = 1.0
+    a["deter"][0, :] = 1.0
+    m = np.zeros(63)
+    for b in range(7):
+        m[9 * b + 0] = m[9 * b + 4] = m[9 * b + 8] = 1.0
+    a["metric"][0] = m
+    a["flow"][0] = 0.0
+    _flow_from_primitives(a["flow"][0:1], 1.0, 0.0, 0.0, 0.0, 1.0, 1.0)
+
+
+def _periodic_index(ni, nj, nk):
+    """Row number (1-based) of node (i, j, k), i fastest."""
+    i, j, k = np.meshgrid(np.arange(ni), np.arange(nj), np.arange(nk), indexing="ij")
+    return (1 + i + ni * (j + nj * k)), i, j, k
+
+
+def _fill_periodic_grid(a, ni, nj, nk, x, y, z):
+    """Wrap-around neighbour table; arrays x,y,z are (ni,nj,nk)."""
+    row, i, j, k = _periodic_index(ni, nj, nk)
+    rows = row.transpose(2, 1, 0).ravel()  # i fastest -> rows 1..n in order
+    assert np.array_equal(rows, np.arange(1, ni * nj * nk + 1))
+
+    def rid(ii, jj, kk):
+        return (1 + (ii % ni) + ni * ((jj % nj) + nj * (kk % nk))).transpose(2, 1, 0).ravel()
+
+    g = a["grid"][1:]
+    g["x"] = x.transpose(2, 1, 0).ravel()
+    g["y"] = y.transpose(2, 1, 0).ravel()
+    g["z"] = z.transpose(2, 1, 0).ravel()
+    g["N0"] = rid(i, j + 1, k)
+    g["N1"] = rid(i + 1, j, k)
+    g["N2"] = rid(i, j - 1, k)
+    g["N3"] = rid(i - 1, j, k)
+    g["N4"] = rid(i, j, k + 1)
+    g["N5"] = rid(i, j, k - 1)
+    g["ID"] = rows
+    g["loc"] = 0
+
+
+def _node_metrics(jac):
+    """jac[..., a, b] = d x_a / d zeta_b (index coordinates).  Returns the
+    9 node metrics (zeta_x, zeta_y, zeta_z, eta_x, ..., xi_z) and det."""
+    inv = np.linalg.inv(jac)          # inv[..., b, a] = d zeta_b / d x_a
+    det = np.linalg.det(jac)
+    m9 = inv.reshape(inv.shape[:-2] + (9,))
+    return m9, det
+
+
+def half_point_metrics(a, n_rows_owned: int):
+    """Face metrics and face determinants by the six-point midpoint rule
+    (3, -25, 150, 150, -25, 3)/256 of node values along each direction,
+    Main.cpp:2369-2440, for rows 1..n_rows_owned.  Uses the neighbour table,
+    so it works for any layout whose neighbours of owned nodes exist."""
+    g = a["grid"]
+    rows = np.arange(1, n_rows_owned + 1)
+    node_m = a["metric"][:, 0:9]
+    det = a["det"]
+    plus = [g[n] for n in L.PLUS]
+    minus = [g[n] for n in L.MINUS]
+    for d in range(3):
+        P, M = plus[d], minus[d]
+        im1 = M[rows]
+        im2 = M[im1]
+        im3 = M[im2]
+        ip1 = P[rows]
+        ip2 = P[ip1]
+        ip3 = P[ip2]
+
+        def interp(v, s0, s1, s2, s3, s4, s5):
+            return (1.0 / 256.0) * (3.0 * (v[s0]) - 25.0 * (v[s1]) + 150.0 * (v[s2]) + 150.0 * (v[s3])
+                                    - 25.0 * (v[s4]) + 3.0 * (v[s5]))
+
+        bp = 1 + 2 * d
+        bm = 2 + 2 * d
+        a["metric"][rows, 9 * bp:9 * bp + 9] = interp(node_m, im2, im1, rows, ip1, ip2, ip3)
+        a["metric"][rows, 9 * bm:9 * bm + 9] = interp(node_m, im3, im2, im1, rows, ip1, ip2)
+        a["deter"][rows, 2 * d] = interp(det, im2, im1, rows, ip1, ip2, ip3)
+        a["deter"][rows, 2 * d + 1] = interp(det, im3, im2, im1, rows, ip1, ip2)
+
+
+def cfl_dt(a, rows, cfl: float) -> float:
+    """Builder-defined time step: cfl / max over nodes and directions of
+    |U . grad zeta_d| + c |grad zeta_d| (unit computational spacing).  The
+    reference itself uses a fixed del_t (Main.cpp:47)."""
+    f = a["flow"][rows]
+    m = a["metric"][rows, 0:9].reshape(-1, 3, 3)
+    u = f[:, [L.FLOW["u"], L.FLOW["v"], L.FLOW["w"]]]
+    c = np.sqrt(1.4 * f[:, L.FLOW["p"]] / f[:, L.FLOW["rho"]])
+    un = np.abs(np.einsum("nda,na->nd", m, u))
+    gn = np.linalg.norm(m, axis=2)
+    lam = (un + c[:, None] * gn).max()
+    return float(cfl / lam)
+
+
+# ------------------------------------------------------------- generators --
+
+def isentropic_vortex(n=64, length=10.0, beta=5.0, u_inf=0.5, center=(5.0, 5.0),
+                      weno_eps=1e-7, cfl=0.5, shape=None) -> Case:
+    """Inviscid isentropic vortex on a periodic Cartesian grid.
+
+    Nodes x_i = i*D, D = length/n, identity-direction metrics zeta_x = eta_y =
+    xi_z = 1/D in all seven metric blocks and det = D^3 (the reference's flux
+    difference has unit computational spacing, Weno.cl:3060-3082).  gamma=1.4,
+    rho_inf = p_inf = 1, vortex of strength beta centred at ``center`` in x-y,
+    uniform in z.  ``viscous=0``: Fv, Ev, Gv are zeroed.
+    """
+    ni, nj, nk = shape if shape is not None else (n, n, n)
+    D = length / ni
+    a = L.empty_arrays(ni * nj * nk + 1)
+    _set_dummy_row(a)
+    xs = np.arange(ni) * D
+    ys = np.arange(nj) * (length / nj)
+    zs = np.arange(nk) * (length / nk)
+    X, Y, Z = np.meshgrid(xs, ys, zs, indexing="ij")
+    _fill_periodic_grid(a, ni, nj, nk, X, Y, Z)
+    Dy, Dz = length / nj, length / nk
+    m = np.zeros(63)
+    for b in range(7):
+        m[9 * b + 0] = 1.0 / D
+        m[9 * b + 4] = 1.0 / Dy
+        m[9 * b + 8] = 1.0 / Dz
+    a["metric"][1:] = m
+    a["det"][1:] = D * Dy * Dz
+    a["deter"][1:] = D * Dy * Dz
+
+    gam = 1.4
+    xr = a["grid"]["x"][1:] - center[0]
+    yr = a["grid"]["y"][1:] - center[1]
+    r2 = xr * xr + yr * yr
+    ex = np.exp(0.5 * (1.0 - r2))
+    du = -beta / (2 * math.pi) * ex * yr
+    dv = beta / (2 * math.pi) * ex * xr
+    T = 1.0 - (gam - 1.0) * beta * beta / (8.0 * gam * math.pi ** 2) * np.exp(1.0 - r2)
+    rho = T ** (1.0 / (gam - 1.0))
+    p = rho ** gam
+    mach = u_inf / math.sqrt(gam)
+    _flow_from_primitives(a["flow"][1:], rho, u_inf + du, dv, np.zeros_like(rho), p, mach)
+    rows = np.arange(1, ni * nj * nk + 1)
+    prm = Params(mach=mach, weno_eps=weno_eps, viscous=0, les=0)
+    return Case("isentropic_vortex", (ni, nj, nk), True, ni * nj * nk, ni * nj * nk, a, prm,
+                cfl_dt(a, rows, cfl))
+
+
+def taylor_green(n=128, amp=0.05, mach=0.1, reynolds=1600.0, prandtl=0.72, t_inf=273.0,
+                 weno_eps=1e-7, cfl=0.5, les=1, shape=None) -> Case:
+    """Taylor-Green vortex on a periodic [0, 2 pi)^3 grid with perturbed nodes
+    x = xi1 + A sin xi2 sin xi3, y = xi2 + A sin xi3 sin xi1,
+    z = xi3 + A sin xi1 sin xi2.  Node metrics and det come from the analytic
+    Jacobian (index coordinates, spacing h = 2 pi / n); face metrics and face
+    determinants by the reference's six-point midpoint rule.  Initial state
+    u = sin x cos y cos z, v = -cos x sin y cos z, w = 0, rho = 1,
+    p = 1/(gamma M^2) + (cos 2x + cos 2y)(cos 2z + 2)/16."""
+    ni, nj, nk = shape if shape is not None else (n, n, n)
+    hs = (2 * math.pi / ni, 2 * math.pi / nj, 2 * math.pi / nk)
+    x1, x2, x3 = np.meshgrid(np.arange(ni) * hs[0], np.arange(nj) * hs[1], np.arange(nk) * hs[2],
+                             indexing="ij")
+    A = amp
+    X = x1 + A * np.sin(x2) * np.sin(x3)
+    Y = x2 + A * np.sin(x3) * np.sin(x1)
+    Z = x3 + A * np.sin(x1) * np.sin(x2)
+    a = L.empty_arrays(ni * nj * nk + 1)
+    _set_dummy_row(a)
+    _fill_periodic_grid(a, ni, nj, nk, X, Y, Z)
+    jac = np.empty(x1.shape + (3, 3))
+    jac[..., 0, 0] = 1.0
+    jac[..., 0, 1] = A * np.cos(x2) * np.sin(x3)
+    jac[..., 0, 2] = A * np.sin(x2) * np.cos(x3)
+    jac[..., 1, 0] = A * np.sin(x3) * np.cos(x1)
+    jac[..., 1, 1] = 1.0
+    jac[..., 1, 2] = A * np.cos(x3) * np.sin(x1)
+    jac[..., 2, 0] = A * np.cos(x1) * np.sin(x2)
+    jac[..., 2, 1] = A * np.sin(x1) * np.cos(x2)
+    jac[..., 2, 2] = 1.0
+    jac = jac * np.array(hs)[None, None, None, None, :]
+    m9, det = _node_metrics(jac)
+    a["metric"][1:, 0:9] = m9.transpose(2, 1, 0, 3).reshape(-1, 9)
+    a["det"][1:] = det.transpose(2, 1, 0).ravel()
+    half_point_metrics(a, ni * nj * nk)
+
+    gam = 1.4
+    xx, yy, zz = a["grid"]["x"][1:], a["grid"]["y"][1:], a["grid"]["z"][1:]
+    u = np.sin(xx) * np.cos(yy) * np.cos(zz)
+    v = -np.cos(xx) * np.sin(yy) * np.cos(zz)
+    w = np.zeros_like(u)
+    rho = np.ones_like(u)
+    p = 1.0 / (gam * mach * mach) + (np.cos(2 * xx) + np.cos(2 * yy)) * (np.cos(2 * zz) + 2.0) / 16.0
+    _flow_from_primitives(a["flow"][1:], rho, u, v, w, p, mach)
+    rows = np.arange(1, ni * nj * nk + 1)
+    prm = Params(mach=mach, reynolds=reynolds, prandtl=prandtl, t_inf=t_inf, weno_eps=weno_eps,
+                 viscous=1, les=les)
+    return Case("taylor_green", (ni, nj, nk), True, ni * nj * nk, ni * nj * nk, a, prm,
+                cfl_dt(a, rows, cfl))
+
+
+def ghost_box(shape=(10, 9, 8), seed=0, mach=1.5, amp=0.05) -> Case:
+    """Non-periodic box of owned nodes with three ghost layers on every side.
+
+    Owned nodes carry ``loc`` = 0 in the interior and a code in 1..26 on the
+    boundary (faces, edges, corners), ghosts carry 100, as in
+    node_locations.cpp and Main.cpp:1426-2300.  Ghost neighbour chains that
+    would leave the padded box point back to the ghost itself.  The flow is
+    a smooth perturbation of a uniform state (seeded), the geometry a mildly
+    perturbed Cartesian grid with analytic metrics."""
+    ni, nj, nk = shape
+    G = 3
+    pi_, pj, pk = ni + 2 * G, nj + 2 * G, nk + 2 * G
+    ii, jj, kk = np.meshgrid(np.arange(pi_), np.arange(pj), np.arange(pk), indexing="ij")
+    owned = (ii >= G) & (ii < G + ni) & (jj >= G) & (jj < G + nj) & (kk >= G) & (kk < G + nk)
+    n_owned = int(owned.sum())
+    n_all = pi_ * pj * pk
+    # row numbers: owned first (i fastest), then ghosts
+    order = np.zeros((pi_, pj, pk), dtype=np.int64)
+    own_idx = np.argwhere(owned.transpose(2, 1, 0))[:, ::-1]  # (i,j,k) with i fastest
+    order[own_idx[:, 0], own_idx[:, 1], own_idx[:, 2]] = np.arange(1, n_owned + 1)
+    gh_idx = np.argwhere((~owned).transpose(2, 1, 0))[:, ::-1]
+    order[gh_idx[:, 0], gh_idx[:, 1], gh_idx[:, 2]] = np.arange(n_owned + 1, n_all + 1)
+
+    a = L.empty_arrays(n_all + 1)
+    _set_dummy_row(a)
+    h = 1.0 / max(ni, nj, nk)
+    x1, x2, x3 = ii * h, jj * h, kk * h
+    A = amp * h * 4
+    X = x1 + A * np.sin(7 * x2) * np.sin(5 * x3)
+    Y = x2 + A * np.sin(6 * x3) * np.sin(5 * x1)
+    Z = x3 + A * np.sin(5 * x1) * np.sin(6 * x2)
+
+    def nb(di, dj, dk):
+        ti, tj, tk = ii + di, jj + dj, kk + dk
+        inside = (ti >= 0) & (ti < pi_) & (tj >= 0) & (tj < pj) & (tk >= 0) & (tk < pk)
+        ti = np.where(inside, ti, ii)
+        tj = np.where(inside, tj, jj)
+        tk = np.where(inside, tk, kk)
+        return order[ti, tj, tk]
+
+    def put(field, vals):
+        a["grid"][field][order.ravel()] = vals.ravel()
+
+    put("x", X)
+    put("y", Y)
+    put("z", Z)
+    put("N0", nb(0, 1, 0))
+    put("N1", nb(1, 0, 0))
+    put("N2", nb(0, -1, 0))
+    put("N3", nb(-1, 0, 0))
+    put("N4", nb(0, 0, 1))
+    put("N5", nb(0, 0, -1))
+    put("ID", order)
+    # boundary codes: count of box faces a node lies on -> distinct codes
+    on = [(ii == G) | (ii == G + ni - 1), (jj == G) | (jj == G + nj - 1), (kk == G) | (kk == G + nk - 1)]
+    face_code = (1 * (ii == G) + 2 * (ii == G + ni - 1) + 3 * (jj == G) + 4 * (jj == G + nj - 1)
+                 + 5 * (kk == G) + 6 * (kk == G + nk - 1))
+    nfaces = on[0].astype(int) + on[1].astype(int) + on[2].astype(int)
+    loc = np.where(nfaces == 0, 0, np.where(nfaces == 1, face_code, np.where(nfaces == 2, 6 + face_code, 14 + face_code)))
+    loc = np.where(owned, loc, 100)
+    put("loc", loc)
+
+    jac = np.zeros(ii.shape + (3, 3))
+    jac[..., 0, 0] = h
+    jac[..., 0, 1] = A * 7 * h * np.cos(7 * x2) * np.sin(5 * x3)
+    jac[..., 0, 2] = A * 5 * h * np.sin(7 * x2) * np.cos(5 * x3)
+    jac[..., 1, 0] = A * 5 * h * np.sin(6 * x3) * np.cos(5 * x1)
+    jac[..., 1, 1] = h
+    jac[..., 1, 2] = A * 6 * h * np.cos(6 * x3) * np.sin(5 * x1)
+    jac[..., 2, 0] = A * 5 * h * np.cos(5 * x1) * np.sin(6 * x2)
+    jac[..., 2, 1] = A * 6 * h * np.sin(5 * x1) * np.cos(6 * x2)
+    jac[..., 2, 2] = h
+    m9, det = _node_metrics(jac)
+    a["metric"][order.ravel(), 0:9] = m9.reshape(-1, 9)
+    a["det"][order.ravel()] = det.ravel()
+    # ghosts carry their own node metrics in every half-point block
+    for b in range(1, 7):
+        a["metric"][1:, 9 * b:9 * b + 9] = a["metric"][1:, 0:9]
+    a["deter"][1:, :] = a["det"][1:, None]
+    half_point_metrics(a, n_owned)
+
+    rng = np.random.default_rng(seed)
+    ph = rng.uniform(0, 2 * math.pi, size=6)
+    rho = 1.0 + 0.1 * np.sin(2 * math.pi * x1 + ph[0]) * np.cos(2 * math.pi * x2 + ph[1])
+    u = 0.6 + 0.1 * np.sin(2 * math.pi * x2 + ph[2])
+    v = 0.1 * np.cos(2 * math.pi * x3 + ph[3])
+    w = 0.05 * np.sin(2 * math.pi * x1 + ph[4])
+    p = 1.0 / (1.4 * mach * mach) * (1.0 + 0.05 * np.cos(2 * math.pi * (x1 + x2 + x3) + ph[5]))
+    flow = np.zeros((n_all, 9))
+    _flow_from_primitives(flow, rho.ravel(), u.ravel(), v.ravel(), w.ravel(), p.ravel(), mach)
+    a["flow"][order.ravel()] = flow
+    rows = np.arange(1, n_owned + 1)
+    prm = Params(mach=mach)
+    return Case("ghost_box", (ni, nj, nk), False, n_owned, n_all, a, prm, cfl_dt(a, rows, 0.3))

@@ -1,0 +1,299 @@
+// dropin.cu -- the three reference kernels on the reference's own layout.
+//
+// One thread per row (work-item), exactly the NDRange of the reference
+// (Solver.cpp:31-38, local size 1 there).  Buffers are the packed AoS structs
+// of include/cfd_rhs.h; device code reads them through aligned double/int
+// views (every struct size is a multiple of 8 bytes) rather than through the
+// packed types, which would force byte-wise loads.  Neighbour chains are
+// bounds-checked: a row whose stencil leaves [0, n_rows) is skipped and the
+// context's error word gets CFD_FLAG_BAD_INDEX.
+#include "internal.h"
+
+namespace cfd {
+
+// ---- aligned views of the packed reference structs ----
+// GRID: 56 B = 7 doubles = 14 ints; x,y,z at doubles 0..2, N0..N5 at ints
+// 6..11, ID at 12, loc at 13.
+__device__ __forceinline__ int grid_nb(const int *g, int row, int which) { return g[14 * row + 6 + which]; }
+__device__ __forceinline__ int grid_loc(const int *g, int row) { return g[14 * row + 13]; }
+// neighbour slot of (+d) and (-d): d=0 -> N1/N3, d=1 -> N0/N2, d=2 -> N4/N5
+__device__ __forceinline__ int plus_slot(int d) { return d == 0 ? 1 : (d == 1 ? 0 : 4); }
+__device__ __forceinline__ int minus_slot(int d) { return d == 0 ? 3 : (d == 1 ? 2 : 5); }
+
+// Chained neighbour gather (Weno.cl:159-226): idx[d][o+3], o = -3..3.
+// Returns false if any index leaves [0, n_rows).
+__device__ __forceinline__ bool gather_star(const int *grid, int gid, int n_rows, int idx[3][7])
+{
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        idx[d][3] = gid;
+        int p = gid, m = gid;
+#pragma unroll
+        for (int o = 1; o <= 3; ++o) {
+            p = grid_nb(grid, p, plus_slot(d));
+            m = grid_nb(grid, m, minus_slot(d));
+            if ((unsigned)p >= (unsigned)n_rows || (unsigned)m >= (unsigned)n_rows) return false;
+            idx[d][3 + o] = p;
+            idx[d][3 - o] = m;
+        }
+    }
+    return true;
+}
+
+// FLOW field offsets inside the 9-double row
+enum { FU = 0, FV = 1, FW = 2, FP = 3, FT = 4, FRHO = 5, FMU = 6, FA = 7, FE = 8 };
+
+// ------------------------------------------------------------------ U_Q --
+// U_Q.cl:36-125.
+__global__ void __launch_bounds__(128) k_uq(double *__restrict__ U, double *__restrict__ Q,
+                                            const int *__restrict__ grid, const double *__restrict__ det,
+                                            const double *__restrict__ flow, double *__restrict__ roe, int n_items,
+                                            int n_rows, unsigned *flags)
+{
+    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= n_items) return;
+    int nb[6];
+#pragma unroll
+    for (int s = 0; s < 6; ++s) {
+        nb[s] = grid_nb(grid, gid, s);
+        if ((unsigned)nb[s] >= (unsigned)n_rows) {
+            atomicOr(flags, CFD_FLAG_BAD_INDEX);
+            return;
+        }
+    }
+    const double *fi = flow + 9 * (size_t)gid;
+    const double rho = fi[FRHO], u = fi[FU], v = fi[FV], w = fi[FW], p = fi[FP];
+    const double si = sqrt(rho);
+    const double hi = total_enthalpy(rho, u, v, w, p);
+    // ROE block order ip, jp, kp, im, jm, km; neighbour slots N1, N0, N4, N3, N2, N5
+    const int slot_of_block[6] = {1, 0, 4, 3, 2, 5};
+    double *r = roe + 36 * (size_t)gid;
+#pragma unroll
+    for (int b = 0; b < 6; ++b) {
+        const double *fn = flow + 9 * (size_t)nb[slot_of_block[b]];
+        const double rb = fn[FRHO], ub = fn[FU], vb = fn[FV], wb = fn[FW], pb = fn[FP];
+        const double sb = sqrt(rb);
+        double ra[5];
+        roe_average(sb, ub, vb, wb, total_enthalpy(rb, ub, vb, wb, pb), si, u, v, w, hi, ra);
+        r[6 * b + 0] = ra[0];
+        r[6 * b + 1] = ra[1];
+        r[6 * b + 2] = ra[2];
+        r[6 * b + 4] = ra[3];
+        r[6 * b + 5] = ra[4];
+    }
+    const double D = det[gid];
+    const double ke = 0.5 * rho * (u * u + v * v + w * w);
+    double *Ur = U + 5 * (size_t)gid, *Qr = Q + 5 * (size_t)gid;
+    Ur[0] = D * rho;
+    Ur[1] = D * rho * u;
+    Ur[2] = D * rho * v;
+    Ur[3] = D * rho * w;
+    Ur[4] = D * ((p / 0.4) + ke);
+    Qr[0] = rho;
+    Qr[1] = rho * u;
+    Qr[2] = rho * v;
+    Qr[3] = rho * w;
+    Qr[4] = ((p / 0.4) + ke);
+}
+
+// -------------------------------------------------------------- Viscous --
+// Viscous.cl:23-643.
+__global__ void __launch_bounds__(128) k_viscous(Phys P, const double *__restrict__ U, double *__restrict__ F,
+                                                 double *__restrict__ E, double *__restrict__ G,
+                                                 double *__restrict__ Fv, double *__restrict__ Ev,
+                                                 double *__restrict__ Gv, const int *__restrict__ grid,
+                                                 const double *__restrict__ metric, const double *__restrict__ det,
+                                                 double *__restrict__ flow, int n_items, int n_rows, unsigned *flags)
+{
+    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= n_items) return;
+    int idx[3][7];
+    if (!gather_star(grid, gid, n_rows, idx)) {
+        atomicOr(flags, CFD_FLAG_BAD_INDEX);
+        return;
+    }
+    double m[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) m[k] = metric[63 * (size_t)gid + k];
+    const double D = det[gid];
+    const double *fr = flow + 9 * (size_t)gid;
+    const double prim[5] = {fr[FRHO], fr[FU], fr[FV], fr[FW], fr[FP]};
+    double Fn[5], En[5], Gn[5];
+    node_inviscid_flux(prim, m, D, Fn, En, Gn);
+    double Fvn[5] = {0, 0, 0, 0, 0}, Evn[5] = {0, 0, 0, 0, 0}, Gvn[5] = {0, 0, 0, 0, 0};
+    double mu;
+    {
+        double dU[3][5];
+#pragma unroll 1
+        for (int d = 0; d < 3; ++d) {
+            int L[7];
+#pragma unroll
+            for (int o = 0; o < 7; ++o) L[o] = grid_loc(grid, idx[d][o]);
+#pragma unroll
+            for (int c = 0; c < 5; ++c) {
+                double f[7];
+#pragma unroll
+                for (int o = 0; o < 7; ++o) f[o] = U[5 * (size_t)idx[d][o] + c];
+                dU[d][c] = visc_deriv_ref(f, L);
+            }
+        }
+        double Ui[5];
+#pragma unroll
+        for (int c = 0; c < 5; ++c) Ui[c] = U[5 * (size_t)gid + c];
+        // MTS test-filter velocity differences (Viscous.cl:493-495)
+        double KS[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const int c = d + 1;
+            const double *um = U + 5 * (size_t)idx[d][2], *up = U + 5 * (size_t)idx[d][4];
+            KS[d] = sqr((Ui[c] / Ui[0]) - ((0.25 * um[c] + 0.5 * Ui[c] + 0.25 * up[c]) / (0.25 * um[0] + 0.5 * Ui[0] + 0.25 * up[0])));
+        }
+        viscous_node_flux(dU, Ui, m, D, prim, KS, P, Fvn, Evn, Gvn, mu);
+    }
+    double *o;
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+        o = F + 5 * (size_t)gid; o[c] = Fn[c];
+        o = E + 5 * (size_t)gid; o[c] = En[c];
+        o = G + 5 * (size_t)gid; o[c] = Gn[c];
+        o = Fv + 5 * (size_t)gid; o[c] = P.viscous ? Fvn[c] : 0.0;
+        o = Ev + 5 * (size_t)gid; o[c] = P.viscous ? Evn[c] : 0.0;
+        o = Gv + 5 * (size_t)gid; o[c] = P.viscous ? Gvn[c] : 0.0;
+    }
+    flow[9 * (size_t)gid + FMU] = mu;
+}
+
+// ----------------------------------------------------------------- Weno --
+// Weno.cl:36-3137: per row, both faces of each direction from the row's own
+// face data (metric blocks, DETERM, ROE_AVERAGING), as the reference does.
+__global__ void __launch_bounds__(128) k_weno(Phys P, int j, double mach, double dt, const double *__restrict__ deter,
+                                              const double *__restrict__ det, double *__restrict__ U0,
+                                              double *__restrict__ U1, double *__restrict__ U2,
+                                              const int *__restrict__ grid, const double *__restrict__ Q,
+                                              const double *__restrict__ metric, const double *__restrict__ roe,
+                                              const double *__restrict__ Fv, const double *__restrict__ Ev,
+                                              const double *__restrict__ Gv, const double *__restrict__ F,
+                                              const double *__restrict__ E, const double *__restrict__ G,
+                                              double *__restrict__ flow, int n_items, int n_rows, unsigned *flags,
+                                              double *__restrict__ L_out)
+{
+    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= n_items) return;
+    int idx[3][7];
+    if (!gather_star(grid, gid, n_rows, idx)) {
+        atomicOr(flags, CFD_FLAG_BAD_INDEX);
+        return;
+    }
+    double L[5] = {0, 0, 0, 0, 0};
+    double Ldiss[5] = {0, 0, 0, 0, 0};
+#pragma unroll 1
+    for (int d = 0; d < 3; ++d) {
+        const double *NF = d == 0 ? F : (d == 1 ? E : G);
+        const double *VF = d == 0 ? Fv : (d == 1 ? Ev : Gv);
+        double Fh[2][5];
+#pragma unroll 1
+        for (int s = 0; s < 2; ++s) {
+            // face metric block 1+2d+s, components of direction d
+            const double *fm = metric + 63 * (size_t)gid + 9 * (1 + 2 * d + s) + 3 * d;
+            const double det_f = deter[6 * (size_t)gid + 2 * d + s];
+            const double *ra = roe + 36 * (size_t)gid + 6 * (d + 3 * s);
+            const double rstate[5] = {ra[0], ra[1], ra[2], ra[4], ra[5]};
+            const int base = s == 0 ? 1 : 0;   // stencil rows: offsets -2..3 (plus) or -3..2 (minus)
+            double pts[6][5], nfv[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k)
+#pragma unroll
+                for (int c = 0; c < 5; ++c) pts[k][c] = Q[5 * (size_t)idx[d][base + k] + c];
+            llf_face_flux(pts, fm[0], fm[1], fm[2], det_f, rstate, P.eps, Fh[s]);
+#pragma unroll
+            for (int c = 0; c < 5; ++c) {
+#pragma unroll
+                for (int k = 0; k < 6; ++k) nfv[k] = NF[5 * (size_t)idx[d][base + k] + c];
+                Fh[s][c] += face_correction(nfv);
+            }
+        }
+        int Lc[7];
+#pragma unroll
+        for (int o = 0; o < 7; ++o) Lc[o] = grid_loc(grid, idx[d][o]);
+#pragma unroll
+        for (int c = 0; c < 5; ++c) {
+            L[c] += Fh[0][c] - Fh[1][c];
+            double f[7];
+#pragma unroll
+            for (int o = 0; o < 7; ++o) f[o] = VF[5 * (size_t)idx[d][o] + c];
+            Ldiss[c] += weno_visc_deriv_ref(f, Lc);
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 5; ++c) L[c] = -(L[c] + Ldiss[c]);
+    if (L_out) {
+#pragma unroll
+        for (int c = 0; c < 5; ++c) L_out[5 * (size_t)gid + c] = L[c];
+    }
+    // SSP-RK3 stage (Weno.cl:3084-3126)
+    double Un[5];
+    const size_t r5 = 5 * (size_t)gid;
+    if (j == 0) {
+#pragma unroll
+        for (int c = 0; c < 5; ++c) { Un[c] = U0[r5 + c] + dt * L[c]; U1[r5 + c] = Un[c]; }
+    } else if (j == 1) {
+#pragma unroll
+        for (int c = 0; c < 5; ++c) {
+            Un[c] = (3.0 / 4.0) * U0[r5 + c] + (1.0 / 4.0) * U1[r5 + c] + 0.25 * dt * L[c];
+            U2[r5 + c] = Un[c];
+        }
+    } else {
+#pragma unroll
+        for (int c = 0; c < 5; ++c) {
+            Un[c] = (U0[r5 + c] / 3.0) + ((2.0 / 3.0) * U2[r5 + c]) + (2.0 / 3.0) * (dt * L[c]);
+            U0[r5 + c] = Un[c];
+        }
+    }
+    // primitive recovery (Weno.cl:3128-3135)
+    const double idet = 1.0 / det[gid];
+    double fu[5];
+#pragma unroll
+    for (int c = 0; c < 5; ++c) fu[c] = idet * Un[c];
+    const double rho = fu[0];
+    const double ir = 1.0 / rho;
+    const double u = fu[1] * ir, v = fu[2] * ir, w = fu[3] * ir;
+    const double e = (fu[4] * ir) - 0.5 * (u * u + v * v + w * w);
+    const double p = e * rho * 0.4;
+    double *fo = flow + 9 * (size_t)gid;
+    fo[FRHO] = rho;
+    fo[FU] = u;
+    fo[FV] = v;
+    fo[FW] = w;
+    fo[FE] = e;
+    fo[FP] = p;
+    fo[FT] = (1.4 * mach * mach) * (p * ir);
+    fo[FA] = sqrt(1.4 * p * ir);
+    if (gid > 0 && !(isfinite(rho) && isfinite(u) && isfinite(v) && isfinite(w) && isfinite(p)))
+        atomicOr(flags, CFD_FLAG_NONFINITE);
+}
+
+void launch_uq(cudaStream_t st, double *U, double *Q, const int *grid, const double *det, const double *flow,
+               double *roe, int n_items, int n_rows, unsigned *flags)
+{
+    k_uq<<<blocks_for(n_items, 128), 128, 0, st>>>(U, Q, grid, det, flow, roe, n_items, n_rows, flags);
+}
+
+void launch_viscous(cudaStream_t st, const Phys &P, const double *U, double *F, double *E, double *G, double *Fv,
+                    double *Ev, double *Gv, const int *grid, const double *metric, const double *det, double *flow,
+                    int n_items, int n_rows, unsigned *flags)
+{
+    k_viscous<<<blocks_for(n_items, 128), 128, 0, st>>>(P, U, F, E, G, Fv, Ev, Gv, grid, metric, det, flow, n_items,
+                                                        n_rows, flags);
+}
+
+void launch_weno(cudaStream_t st, const Phys &P, int j, double mach, double dt, const double *deter,
+                 const double *det, double *U0, double *U1, double *U2, const int *grid, const double *Q,
+                 const double *metric, const double *roe, const double *Fv, const double *Ev, const double *Gv,
+                 const double *F, const double *E, const double *G, double *flow, int n_items, int n_rows,
+                 unsigned *flags, double *L_out)
+{
+    k_weno<<<blocks_for(n_items, 128), 128, 0, st>>>(P, j, mach, dt, deter, det, U0, U1, U2, grid, Q, metric, roe, Fv,
+                                                     Ev, Gv, F, E, G, flow, n_items, n_rows, flags, L_out);
+}
+
+}  // namespace cfd

@@ -1,0 +1,64 @@
+// internal.h -- host-side objects behind the C ABI (context, solver) and the
+// launch helpers shared by the .cu translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "cfd_rhs.h"
+#include "physics.cuh"
+
+// Device error-flag bits (one 32-bit word per context, or per instance in
+// the batched solver).
+enum : unsigned {
+    CFD_FLAG_BAD_INDEX = 1u,   // a neighbour index outside [0, n_rows)
+    CFD_FLAG_NONFINITE = 2u,   // NaN/Inf in an advanced state
+    CFD_FLAG_TIMEOUT = 4u      // a bounded wait gave up
+};
+
+struct cfd_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    bool async = false;
+    int32_t n_rows = 0;
+    unsigned *d_flags = nullptr;   // device error word
+    unsigned *h_flags = nullptr;   // pinned mirror
+    uint64_t launches = 0;
+    std::string last_error;
+};
+
+namespace cfd {
+
+// Records a CUDA error on the context; returns the status to hand back.
+cfd_status_t cuda_fail(cfd_ctx *ctx, cudaError_t e, const char *what);
+cfd_status_t fail(cfd_ctx *ctx, cfd_status_t s, const std::string &msg);
+// Makes ctx->device current on this host thread.
+cfd_status_t use_device(cfd_ctx *ctx);
+// After a launch: checks the launch, and in synchronous mode waits and
+// converts device flags into a status (clearing them).
+cfd_status_t after_launch(cfd_ctx *ctx, const char *what);
+// Waits for the stream and converts/clears device flags.
+cfd_status_t drain(cfd_ctx *ctx);
+cfd_status_t flags_to_status(cfd_ctx *ctx, unsigned flags);
+bool is_device_pointer(const void *p);
+Phys make_phys(const cfd_params_t *p);
+
+inline unsigned blocks_for(long long n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+// Drop-in kernel launchers (dropin.cu).  All pointers are device pointers.
+void launch_uq(cudaStream_t st, double *U, double *Q, const int *grid, const double *det, const double *flow,
+               double *roe, int n_items, int n_rows, unsigned *flags);
+void launch_viscous(cudaStream_t st, const Phys &P, const double *U, double *F, double *E, double *G, double *Fv,
+                    double *Ev, double *Gv, const int *grid, const double *metric, const double *det, double *flow,
+                    int n_items, int n_rows, unsigned *flags);
+void launch_weno(cudaStream_t st, const Phys &P, int j, double mach, double dt, const double *deter,
+                 const double *det, double *U0, double *U1, double *U2, const int *grid, const double *Q,
+                 const double *metric, const double *roe, const double *Fv, const double *Ev, const double *Gv,
+                 const double *F, const double *E, const double *G, double *flow, int n_items, int n_rows,
+                 unsigned *flags, double *L_out);
+
+}  // namespace cfd

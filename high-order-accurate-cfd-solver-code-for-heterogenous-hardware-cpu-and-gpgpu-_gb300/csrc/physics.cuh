@@ -1,0 +1,381 @@
+// physics.cuh -- device arithmetic of the RHS path, shared by the drop-in
+// (reference-layout) kernels and the structured face-based kernels.
+//
+// Every function follows the reference kernels' formulas (cited per
+// function) with gamma = 1.4 written as the reference writes it (0.4, 1.4,
+// 0.2).  Functions are templated on the compute type T: double for the FP64
+// path, float for the parts the mixed-precision path runs in FP32.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+
+namespace cfd {
+
+template <class T> __device__ __forceinline__ T sqr(T x) { return x * x; }
+
+// Total enthalpy per unit mass, U_Q.cl:64-65.
+template <class T>
+__device__ __forceinline__ T total_enthalpy(T rho, T u, T v, T w, T p)
+{
+    return ((p / T(0.4)) + T(0.5) * rho * (u * u + v * v + w * w) + p) / rho;
+}
+
+// Roe-averaged face state from the two adjacent nodes (U_Q.cl:60-109):
+// out = {u, v, w, h, rho}.  sb/hb belong to the neighbour, si/hi to the node.
+template <class T>
+__device__ __forceinline__ void roe_average(T sb, T ub, T vb, T wb, T hb, T si, T ui, T vi, T wi, T hi,
+                                            T out[5])
+{
+    const T den = sb + si;
+    out[4] = sb * si;
+    out[0] = (sb * ub + si * ui) / den;
+    out[1] = (sb * vb + si * vi) / den;
+    out[2] = (sb * wb + si * wi) / den;
+    out[3] = (sb * hb + si * hi) / den;
+}
+
+// Roe eigen-system of one face (Weno.cl:337-413): k_bar = grad(zeta)/|grad(zeta)|
+// from the face metric, sound speed from the Roe state, left (Lm) and right
+// (R) eigenvector matrices of the Euler flux Jacobian along k_bar.
+template <class T>
+struct FaceEigen {
+    T kx, ky, kz, a, alpha, beta, theta, phi, ru, rv, rw, rr;
+
+    __device__ __forceinline__ void init(T mx, T my, T mz, const T roe[5])
+    {
+        ru = roe[0];
+        rv = roe[1];
+        rw = roe[2];
+        const T rh = roe[3];
+        rr = roe[4];
+        const T kk = sqrt(mx * mx + my * my + mz * mz);
+        a = sqrt(T(0.4) * (rh - T(0.5) * (ru * ru + rv * rv + rw * rw)));
+        kx = mx / kk;
+        ky = my / kk;
+        kz = mz / kk;
+        theta = kx * ru + ky * rv + kz * rw;
+        phi = T(0.5) * T(0.4) * (ru * ru + rv * rv + rw * rw);
+        const T s2 = T(1.4142135623730951);  // sqrt(2.0)
+        alpha = rr / (s2 * a);
+        beta = T(1.0) / (s2 * rr * a);
+    }
+
+    // Left eigenvectors, rows of l_eigen_Q (Weno.cl:384-412).
+    __device__ __forceinline__ void left(T Lm[5][5]) const
+    {
+        const T a2 = a * a;
+        const T ph = phi / a2;
+        Lm[0][0] = kx * (T(1.0) - ph) - ((kz * rv - ky * rw) / rr);
+        Lm[0][1] = kx * T(0.4) * ru / a2;
+        Lm[0][2] = (kx * T(0.4) * rv / a2) + (kz / rr);
+        Lm[0][3] = (kx * T(0.4) * rw / a2) - (ky / rr);
+        Lm[0][4] = -kx * T(0.4) / a2;
+        Lm[1][0] = ky * (T(1.0) - ph) - ((kx * rw - kz * ru) / rr);
+        Lm[1][1] = (ky * T(0.4) * ru / a2) - kz / rr;
+        Lm[1][2] = ky * T(0.4) * rv / a2;
+        Lm[1][3] = (ky * T(0.4) * rw / a2) + (kx / rr);
+        Lm[1][4] = -ky * T(0.4) / a2;
+        Lm[2][0] = kz * (T(1.0) - ph) - ((ky * ru - kx * rv) / rr);
+        Lm[2][1] = kz * T(0.4) * ru / a2 + (ky / rr);
+        Lm[2][2] = kz * T(0.4) * rv / a2 - (kx / rr);
+        Lm[2][3] = kz * T(0.4) * rw / a2;
+        Lm[2][4] = -kz * T(0.4) / a2;
+        Lm[3][0] = beta * (phi - theta * a);
+        Lm[3][1] = -beta * (T(0.4) * ru - kx * a);
+        Lm[3][2] = -beta * (T(0.4) * rv - ky * a);
+        Lm[3][3] = -beta * (T(0.4) * rw - kz * a);
+        Lm[3][4] = beta * T(0.4);
+        Lm[4][0] = beta * (phi + theta * a);
+        Lm[4][1] = -beta * (T(0.4) * ru + kx * a);
+        Lm[4][2] = -beta * (T(0.4) * rv + ky * a);
+        Lm[4][3] = -beta * (T(0.4) * rw + kz * a);
+        Lm[4][4] = beta * T(0.4);
+    }
+
+    // Right eigenvectors times a characteristic vector c (Weno.cl:349-380 and
+    // the back-projection 2188-2289): q = R c.
+    __device__ __forceinline__ void right_times(const T c[5], T q[5]) const
+    {
+        const T e0 = ((phi + a * a) / T(0.4));
+        q[0] = kx * c[0] + ky * c[1] + kz * c[2] + alpha * c[3] + alpha * c[4];
+        q[1] = (kx * ru) * c[0] + (ky * ru - kz * rr) * c[1] + (kz * ru + ky * rr) * c[2]
+               + (alpha * (ru + kx * a)) * c[3] + (alpha * (ru - kx * a)) * c[4];
+        q[2] = (kx * rv + kz * rr) * c[0] + (ky * rv) * c[1] + (kz * rv - kx * rr) * c[2]
+               + (alpha * (rv + ky * a)) * c[3] + (alpha * (rv - ky * a)) * c[4];
+        q[3] = (kx * rw - ky * rr) * c[0] + (ky * rw + kx * rr) * c[1] + (kz * rw) * c[2]
+               + (alpha * (rw + kz * a)) * c[3] + (alpha * (rw - kz * a)) * c[4];
+        q[4] = (((kx * phi) / T(0.4)) + rr * (kz * rv - ky * rw)) * c[0]
+               + (((ky * phi) / T(0.4)) + rr * (kx * rw - kz * ru)) * c[1]
+               + (((kz * phi) / T(0.4)) + rr * (ky * ru - kx * rv)) * c[2]
+               + (alpha * (e0 + theta * a)) * c[3] + (alpha * (e0 - theta * a)) * c[4];
+    }
+};
+
+// WENO5 nonlinear interpolation of one characteristic variable to the face
+// between c[2] (left node) and c[3] (right node); c[0..5] are the six nodes
+// left-2 .. right+2.  Right-biased ("pos", linear weights 1/16, 5/8, 5/16)
+// and left-biased ("neg", 5/16, 5/8, 1/16) values, Jiang-Shu smoothness
+// indicators and weights d_k/(eps+IS_k)^2 (Weno.cl:1056-1280).
+template <class T>
+__device__ __forceinline__ void weno_pair(const T c[6], T eps, T &pos, T &neg)
+{
+    const T cm2 = c[0], cm1 = c[1], c0 = c[2], c1 = c[3], c2 = c[4], c3 = c[5];
+    const T p0 = (T(15.0) / T(8.0)) * c1 - (T(5.0) / T(4.0)) * c2 + (T(3.0) / T(8.0)) * c3;
+    const T p1 = (T(3.0) / T(8.0)) * c0 + (T(3.0) / T(4.0)) * c1 - (T(1.0) / T(8.0)) * c2;
+    const T p2 = (T(-1.0) / T(8.0)) * cm1 + (T(3.0) / T(4.0)) * c0 + (T(3.0) / T(8.0)) * c1;
+    const T m2 = (T(3.0) / T(8.0)) * cm2 - (T(5.0) / T(4.0)) * cm1 + (T(15.0) / T(8.0)) * c0;
+    // candidates m0 == p1 and m1 == p2 (same stencils, same arithmetic)
+    const T k13 = T(13.0) / T(12.0), k14 = T(1.0) / T(4.0);
+    const T ISm2 = k13 * sqr(cm2 - T(2.0) * cm1 + c0) + k14 * sqr(cm2 - T(4.0) * cm1 + T(3.0) * c0);
+    const T ISm1 = k13 * sqr(cm1 - T(2.0) * c0 + c1) + k14 * sqr(cm1 - c1);
+    const T ISm0 = k13 * sqr(c0 - T(2.0) * c1 + c2) + k14 * sqr(T(3.0) * c0 - T(4.0) * c1 + c2);
+    const T ISp2 = k13 * sqr(cm1 - T(2.0) * c0 + c1) + k14 * sqr(cm1 - T(4.0) * c0 + T(3.0) * c1);
+    const T ISp1 = k13 * sqr(c0 - T(2.0) * c1 + c2) + k14 * sqr(c0 - c2);
+    const T ISp0 = k13 * sqr(c1 - T(2.0) * c2 + c3) + k14 * sqr(T(3.0) * c1 - T(4.0) * c2 + c3);
+    const T d16 = T(1.0) / T(16.0), d58 = T(5.0) / T(8.0), d516 = T(5.0) / T(16.0);
+    // w_k = d_k / s_k with s_k = (eps + IS_k)^2; the normalised combination
+    // sum(w_k x_k)/sum(w_k) is evaluated with a single division as
+    // sum(d_k x_k prod_{j!=k} s_j) / sum(d_k prod_{j!=k} s_j).
+    {
+        const T s0 = sqr(eps + ISp0), s1 = sqr(eps + ISp1), s2 = sqr(eps + ISp2);
+        const T w0 = d16 * (s1 * s2), w1 = d58 * (s0 * s2), w2 = d516 * (s0 * s1);
+        pos = (w0 * p0 + w1 * p1 + w2 * p2) / (w0 + w1 + w2);
+    }
+    {
+        const T s0 = sqr(eps + ISm0), s1 = sqr(eps + ISm1), s2 = sqr(eps + ISm2);
+        const T w0 = d516 * (s1 * s2), w1 = d58 * (s0 * s2), w2 = d16 * (s0 * s1);
+        neg = (w0 * p1 + w1 * p2 + w2 * m2) / (w0 + w1 + w2);
+    }
+}
+
+// Contravariant Euler flux of a face state q (conserved, per unit volume)
+// through the face metric (mx,my,mz): mx*F + my*E + mz*G with the Cartesian
+// fluxes of Weno.cl:2291-2507 (p = 0.4 (E - |m|^2/(2 rho)), E + p =
+// 1.4 E - 0.2 |m|^2/rho).  Also returns lambda_5 = U.m + c|m| of
+// Weno.cl:2511-2583 (element [4]).
+template <class T>
+__device__ __forceinline__ T contravariant_flux(const T q[5], T mx, T my, T mz, T f[5])
+{
+    const T ir = T(1.0) / q[0];
+    const T u = q[1] * ir, v = q[2] * ir, w = q[3] * ir;
+    const T ke2 = q[1] * u + q[2] * v + q[3] * w;        // |m|^2 / rho
+    const T pr = T(0.4) * (q[4] - T(0.5) * ke2);
+    const T hq = (T(1.4) * q[4] - T(0.2) * ke2);
+    const T un = mx * u + my * v + mz * w;
+    f[0] = q[0] * un;
+    f[1] = q[1] * un + mx * pr;
+    f[2] = q[2] * un + my * pr;
+    f[3] = q[3] * un + mz * pr;
+    f[4] = hq * un;
+    const T e = q[4] * ir - T(0.5) * (u * u + v * v + w * w);
+    const T c2k = T(1.4) * T(0.4) * e * (mx * mx + my * my + mz * mz);
+    return un + sqrt(c2k);
+}
+
+// Full LLF face flux of one face: Roe eigenvectors, characteristic
+// projection of the six stencil points, WENO5 both sides, back-projection,
+// contravariant fluxes x face det, lambda_5 based LLF (Weno.cl:2859-2947):
+// Fhat = 0.5 (Fp + Fn - alpha (det qp - det qn)),  alpha = max |lambda_5|.
+// pts[k][c]: conserved Q of nodes left-2 .. right+2.
+template <class T>
+__device__ __forceinline__ void llf_face_flux(const T pts[6][5], T mx, T my, T mz, T det_f, const T roe[5],
+                                              T eps, T Fhat[5])
+{
+    FaceEigen<T> eg;
+    eg.init(mx, my, mz, roe);
+    T cpos[5], cneg[5];
+    {
+        T Lm[5][5];
+        eg.left(Lm);
+#pragma unroll
+        for (int r = 0; r < 5; ++r) {
+            T cv[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k)
+                cv[k] = Lm[r][0] * pts[k][0] + Lm[r][1] * pts[k][1] + Lm[r][2] * pts[k][2] + Lm[r][3] * pts[k][3]
+                        + Lm[r][4] * pts[k][4];
+            weno_pair(cv, eps, cpos[r], cneg[r]);
+        }
+    }
+    T qp[5], qn[5];
+    eg.right_times(cpos, qp);
+    eg.right_times(cneg, qn);
+    T fp[5], fn[5];
+    const T lp = contravariant_flux(qp, mx, my, mz, fp);
+    const T ln = contravariant_flux(qn, mx, my, mz, fn);
+    const T alpha = fmax(fabs(lp), fabs(ln));
+#pragma unroll
+    for (int c = 0; c < 5; ++c)
+        Fhat[c] = T(0.5) * (det_f * fp[c] + det_f * fn[c] - alpha * (det_f * qp[c] - det_f * qn[c]));
+}
+
+// Sixth-order midpoint-and-node correction of a face flux (Weno.cl:2950-3058):
+// Fh = Fhat - d2/24 + 7 d4/5760 with d2 = (-5,39,-34,-34,39,-5)/48 and
+// d4 = (1,-3,2,2,-3,1)/2 of the node fluxes f[0..5] = left-2 .. right+2.
+template <class T>
+__device__ __forceinline__ T face_correction(const T f[6])
+{
+    const T d2 = (T(1.0) / T(48.0)) * (T(-5.0) * f[0] + T(39.0) * f[1] - T(34.0) * f[2] - T(34.0) * f[3]
+                                       + T(39.0) * f[4] - T(5.0) * f[5]);
+    const T d4 = (T(1.0) / T(2.0)) * (f[0] - T(3.0) * f[1] + T(2.0) * f[2] + T(2.0) * f[3] - T(3.0) * f[4] + f[5]);
+    return -(T(1.0) / T(24.0)) * d2 + (T(7.0) / T(5760.0)) * d4;
+}
+
+// Location-code-driven first derivative of the Viscous kernel
+// (Viscous.cl:285-332; the same branch set for eta and xi).  f[0..6] are the
+// values at offsets -3..3, L[0..6] their loc codes.  Branches the reference
+// leaves undefined give 0.
+__device__ __forceinline__ double visc_deriv_ref(const double f[7], const int L[7])
+{
+    const int L0 = L[3];
+    double D = 0.0;
+    if (L0 > 0 && L0 <= 52 && L[4] == 100) D = (1.0 / 6.0) * (11.0 * f[3] - 18.0 * f[2] + 9.0 * f[1] - 2.0 * f[0]);
+    if (L0 > 0 && L0 <= 52 && L[2] == 100) D = (1.0 / 6.0) * (-11.0 * f[3] + 18.0 * f[4] - 9.0 * f[5] + 2.0 * f[6]);
+    if (L0 == 0 && L[4] > 0 && L[4] <= 52 && L[5] == 100) D = (1.0 / 6.0) * (2.0 * f[4] + 3.0 * f[3] - 6.0 * f[2] + f[1]);
+    if (L0 == 0 && L[2] > 0 && L[1] == 100) D = (1.0 / 6.0) * ((-2.0) * f[2] - 3.0 * f[3] + 6.0 * f[4] - f[5]);
+    if (L0 == 0 && L[1] != 100 && L[2] != 100 && L[5] != 100 && L[4] != 100)
+        D = (1.0 / 12.0) * (8.0 * (f[4] - f[2]) - (f[5] - f[1]));
+    if (L0 > 0 && L[1] != 100 && L[2] != 100 && L[5] != 100 && L[4] != 100)
+        D = (1.0 / 12.0) * (8.0 * (f[4] - f[2]) - (f[5] - f[1]));
+    return D;
+}
+
+// Viscous-flux derivative branches of the Weno kernel (Weno.cl:2732-2856).
+// The reference has no branch for a boundary node away from ghosts in this
+// direction (its value is uninitialised there); the central form is used.
+__device__ __forceinline__ double weno_visc_deriv_ref(const double f[7], const int L[7])
+{
+    const int L0 = L[3];
+    double D = (1.0 / 12.0) * (8.0 * (f[4] - f[2]) - (f[5] - f[1]));
+    if (L0 > 0 && L0 <= 52 && L[4] == 100) D = (1.0 / 6.0) * (11.0 * f[3] - 18.0 * f[2] + 9.0 * f[1] - 2.0 * f[0]);
+    if (L0 > 0 && L0 <= 52 && L[2] == 100) D = (1.0 / 6.0) * (-11.0 * f[3] + 18.0 * f[4] - 9.0 * f[5] + 2.0 * f[6]);
+    if (L0 == 0 && L[4] > 0 && L[4] <= 52 && L[5] == 100) D = (1.0 / 6.0) * ((2.0) * f[4] + 3.0 * f[3] - 6.0 * f[2] + f[1]);
+    if (L0 == 0 && L[2] > 0 && L[2] <= 52 && L[1] == 100) D = (1.0 / 6.0) * ((-2.0) * f[2] - 3.0 * f[3] + 6.0 * f[4] - f[5]);
+    return D;
+}
+
+// Physical constants of one run.
+struct Phys {
+    double mach, reynolds, prandtl, t_inf, eps;
+    int viscous, les;
+};
+
+// Viscous and SGS fluxes at one node from the derivatives of U along the
+// three directions (Viscous.cl:439-631).  dU[d][c]: derivative of U_c along
+// direction d; Ui: U at the node; m: node metrics (9); det: node det;
+// prim: rho,u,v,w,p of FLOW at the node; KS: the three MTS test-filter
+// velocity-difference squares.  Writes contravariant Fv/Ev/Gv (x det) and mu.
+__device__ __forceinline__ void viscous_node_flux(const double dU[3][5], const double Ui[5], const double m[9],
+                                                  double det, const double prim[5], const double KS[3],
+                                                  const Phys &P, double Fv[5], double Ev[5], double Gv[5],
+                                                  double &mu_out)
+{
+    const double Mach = P.mach, Reyl = P.reynolds, Pr = P.prandtl, Free_t = P.t_inf;
+    const double U0 = Ui[0], U1 = Ui[1], U2 = Ui[2], U3 = Ui[3], U4 = Ui[4];
+    const double iU0 = 1.0 / U0;
+    const double iU00 = 1.0 / (U0 * U0);
+    double uc[3], vc[3], wc[3], tc[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        uc[d] = iU0 * dU[d][1] - (U1 * iU00) * dU[d][0];
+        vc[d] = iU0 * dU[d][2] - (U2 * iU00) * dU[d][0];
+        wc[d] = iU0 * dU[d][3] - (U3 * iU00) * dU[d][0];
+    }
+    const double uu = U1 * iU0, vv = U2 * iU0, ww = U3 * iU0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+        tc[d] = iU0 * dU[d][4] - (U4 * iU00) * dU[d][0] - uu * uc[d] - vv * vc[d] - ww * wc[d];
+
+    // Sutherland's law with T = gamma M^2 (gamma-1) e (Viscous.cl:451-458)
+    const double d_temp = (1.4 * Mach * Mach * 0.4 * ((U4 * iU0) - 0.5 * (uu * uu + vv * vv + ww * ww)));
+    const double sd = sqrt(d_temp);
+    const double S = 110.4 / Free_t;
+    const double mu = (sd * sd * sd) * ((1.0 + S) / (d_temp + S));
+    mu_out = mu;
+
+    const double zx = m[0], zy = m[1], zz = m[2], ex = m[3], ey = m[4], ez = m[5], xx = m[6], xy = m[7], xz = m[8];
+    const double dudx = uc[0] * zx + uc[1] * ex + uc[2] * xx, dudy = uc[0] * zy + uc[1] * ey + uc[2] * xy,
+                 dudz = uc[0] * zz + uc[1] * ez + uc[2] * xz;
+    const double dvdx = vc[0] * zx + vc[1] * ex + vc[2] * xx, dvdy = vc[0] * zy + vc[1] * ey + vc[2] * xy,
+                 dvdz = vc[0] * zz + vc[1] * ez + vc[2] * xz;
+    const double dwdx = wc[0] * zx + wc[1] * ex + wc[2] * xx, dwdy = wc[0] * zy + wc[1] * ey + wc[2] * xy,
+                 dwdz = wc[0] * zz + wc[1] * ez + wc[2] * xz;
+    const double dtdx = tc[0] * zx + tc[1] * ex + tc[2] * xx, dtdy = tc[0] * zy + tc[1] * ey + tc[2] * xy,
+                 dtdz = tc[0] * zz + tc[1] * ez + tc[2] * xz;
+
+    const double kq = -(mu * 1.4 / (Pr * Reyl));
+    const double qx_ = kq * dtdx, qy_ = kq * dtdy, qz_ = kq * dtdz;   // Viscous.cl:461-463
+    const double mr = mu / Reyl;                                        // Viscous.cl:466-476
+    const double txx = mr * ((4.0 / 3.0) * dudx - (2.0 / 3.0) * dvdy - (2.0 / 3.0) * dwdz);
+    const double tyy = mr * ((4.0 / 3.0) * dvdy - (2.0 / 3.0) * dudx - (2.0 / 3.0) * dwdz);
+    const double tzz = mr * ((4.0 / 3.0) * dwdz - (2.0 / 3.0) * dudx - (2.0 / 3.0) * dvdy);
+    const double sxy = dudy + dvdx, sxz = dudz + dwdx, syz = dvdz + dwdy;
+    const double txy = mr * sxy, txz = mr * sxz, tyz = mr * syz;
+
+    double TXY = 0, TYZ = 0, TXZ = 0, TXX = 0, TYY = 0, TZZ = 0, HX = 0, HY = 0, HZ = 0, DX = 0, DY = 0, DZ = 0;
+    if (P.les) {  // mixed-time-scale SGS model, Viscous.cl:490-558
+        const double C_MTS = 0.03, C_T = 10.0;
+        const double s_xy = 0.5 * sxy, s_yz = 0.5 * syz, s_xz = 0.5 * sxz;
+        const double mod = sqrt(2.0 * ((s_xy * s_xy + s_yz * s_yz + s_xz * s_xz)
+                                       + (2.0 / 3.0) * (dudx * dudx + dvdy * dvdy + dwdz * dwdz)));
+        const double DEL = 1.0 / cbrt(det);
+        double ed[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const double sk = sqrt(KS[d]);
+            if (mod != 0.0) {
+                const double R = (DEL * mod) / sk;
+                ed[d] = (C_MTS / (1.0 + R / C_T)) * DEL * sk;
+            } else {
+                ed[d] = C_MTS * DEL * sk;
+            }
+        }
+        const double r2 = -2.0 * U0;
+        TXY = r2 * ed[0] * s_xy;
+        TYZ = r2 * ed[1] * s_yz;
+        TXZ = r2 * ed[2] * s_xz;
+        TXX = r2 * ed[0] * dudx;
+        TYY = r2 * ed[1] * dvdy;
+        TZZ = r2 * ed[2] * dwdz;
+        const double kQ = -(1.0 / (1.4 * 0.4 * Mach * Mach));
+        const double Qx = kQ * ed[0] * dtdx, Qy = kQ * ed[1] * dtdy, Qz = kQ * ed[2] * dtdz;
+        HX = Qx + (TXX + TXY + TXZ) * prim[1];
+        HY = Qy + (TXY + TYY + TYZ) * prim[2];
+        HZ = Qz + (TXZ + TYZ + TZZ) * prim[3];
+        DX = 0.4 * Qx;
+        DY = 0.4 * Qy;
+        DZ = 0.4 * Qz;
+    }
+    const double u = prim[1], v = prim[2], w = prim[3];
+    // Cartesian viscous fluxes, Viscous.cl:580-596
+    const double tFv[5] = {0.0, -txx + TXX, -txy + TXY, -txz + TXZ, ((-u * txx - v * txy - w * txz) + qx_ + HX + DX)};
+    const double tEv[5] = {0.0, -txy + TXY, -tyy + TYY, -tyz + TYZ, ((-u * txy - v * tyy - w * tyz) + qy_ + HY + DY)};
+    const double tGv[5] = {0.0, -txz + TXZ, -tyz + TYZ, -tzz + TZZ, ((-u * txz - v * tyz - w * tzz) + qz_ + HZ + DZ)};
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+        Fv[c] = det * (zx * tFv[c] + zy * tEv[c] + zz * tGv[c]);
+        Ev[c] = det * (ex * tFv[c] + ey * tEv[c] + ez * tGv[c]);
+        Gv[c] = det * (xx * tFv[c] + xy * tEv[c] + xz * tGv[c]);
+    }
+}
+
+// Contravariant node inviscid fluxes F, E, G (x det) from the primitives,
+// Viscous.cl:560-578 and 615-631.
+__device__ __forceinline__ void node_inviscid_flux(const double prim[5], const double m[9], double det, double F[5],
+                                                   double E[5], double G[5])
+{
+    const double rho = prim[0], u = prim[1], v = prim[2], w = prim[3], p = prim[4];
+    const double Et = (((p / 0.4) + 0.5 * rho * (u * u + v * v + w * w)) + p);
+    const double tF[5] = {rho * u, rho * u * u + p, rho * v * u, rho * u * w, Et * u};
+    const double tE[5] = {rho * v, rho * v * u, rho * v * v + p, rho * v * w, Et * v};
+    const double tG[5] = {rho * w, rho * u * w, rho * v * w, rho * w * w + p, Et * w};
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+        F[c] = det * (m[0] * tF[c] + m[1] * tE[c] + m[2] * tG[c]);
+        E[c] = det * (m[3] * tF[c] + m[4] * tE[c] + m[5] * tG[c]);
+        G[c] = det * (m[6] * tF[c] + m[7] * tE[c] + m[8] * tG[c]);
+    }
+}
+
+}  // namespace cfd

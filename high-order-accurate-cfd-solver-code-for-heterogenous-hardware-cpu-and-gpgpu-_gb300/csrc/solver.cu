@@ -1,0 +1,399 @@
+// solver.cu -- resident solver object: the reference host loop
+// (Solver.cpp:356-658, stages U_Q -> Viscous -> Weno(j)) run on the device
+// with the state kept in device memory between stages and steps.
+//
+// Path selection at create time:
+//   CFD_PATH_STRUCTURED  the neighbour table is a periodic (i,j,k) lattice
+//                        with loc == 0 everywhere and single-valued face data
+//                        -> face-based SoA kernels (structured.cu)
+//   CFD_PATH_GATHER      anything else -> the drop-in kernels on the
+//                        reference layout (dropin.cu), the same code the
+//                        cfd_uq/cfd_viscous/cfd_weno entry points run
+// Ghost rows are not refilled between stages (the reference's boundary
+// routine intialise(), Flow_Initialisation.cpp, is outside this library).
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "internal.h"
+#include "structured.h"
+
+struct cfd_solver {
+    cfd_ctx *ctx = nullptr;
+    cfd_params_t prm{};
+    cfd::Phys P{};
+    int path = CFD_PATH_GATHER;
+    int32_t g_node = 0, sd_node = 0, n_rows = 0;
+    int ni = 0, nj = 0, nk = 0;
+    bool mixed = false;
+    std::vector<void *> allocs;
+    uint64_t bytes = 0;
+    // gather path (reference layout, device)
+    int *grid = nullptr;
+    double *det = nullptr, *deter = nullptr, *metric = nullptr, *flow = nullptr;
+    double *U[3] = {nullptr, nullptr, nullptr};
+    double *Q = nullptr, *F = nullptr, *E = nullptr, *G = nullptr, *Fv = nullptr, *Ev = nullptr, *Gv = nullptr;
+    double *roe = nullptr, *L = nullptr;
+    // structured path
+    cfd::StructuredLaunch S{};
+    double *stage9 = nullptr;   // AoS staging, rows 0..N, 9 doubles
+    double *stage5 = nullptr;   // AoS staging, rows 0..N, 5 doubles
+    double *Lsoa = nullptr;
+};
+
+namespace {
+
+using namespace cfd;
+
+cfd_status_t dalloc(cfd_solver *s, size_t bytes, void **p)
+{
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) return cuda_fail(s->ctx, e, "cudaMalloc (solver)");
+    s->allocs.push_back(*p);
+    s->bytes += bytes;
+    return CFD_OK;
+}
+
+template <class T>
+cfd_status_t dalloc_t(cfd_solver *s, size_t count, T **p)
+{
+    return dalloc(s, count * sizeof(T), (void **)p);
+}
+
+cfd_status_t upload(cfd_solver *s, void *dst, const void *src, size_t bytes)
+{
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s->ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(s->ctx, e, "cudaMemcpyAsync H2D (solver)");
+    return CFD_OK;
+}
+
+int nb_of(const cfd_grid_t &g, int slot)
+{
+    switch (slot) {
+    case 0: return g.N0;
+    case 1: return g.N1;
+    case 2: return g.N2;
+    case 3: return g.N3;
+    case 4: return g.N4;
+    default: return g.N5;
+    }
+}
+
+// Lattice detection: rows 1..N, row(i,j,k) = 1 + i + ni*(j + nj*k) with
+// N1/N3 = +-i, N0/N2 = +-j, N4/N5 = +-k, periodic wrap, loc == 0.
+bool detect_lattice(const cfd_geometry_t *g, int &ni, int &nj, int &nk)
+{
+    const int N = g->sd_node;
+    if (g->g_node != N || N < 1) return false;
+    auto cycle = [&](int slot) {
+        int r = 1, len = 0;
+        do {
+            r = nb_of(g->grid[r], slot);
+            ++len;
+            if (r < 1 || r > N || len > N) return -1;
+        } while (r != 1);
+        return len;
+    };
+    ni = cycle(1);
+    if (ni <= 0) return false;
+    const int cj = cycle(0), ck = cycle(4);
+    if (cj <= 0 || ck <= 0) return false;
+    nj = cj;
+    nk = ck;
+    if ((long long)ni * nj * nk != N) return false;
+    for (int k = 0; k < nk; ++k)
+        for (int j = 0; j < nj; ++j)
+            for (int i = 0; i < ni; ++i) {
+                auto row = [&](int a, int b, int c) {
+                    a = (a % ni + ni) % ni;
+                    b = (b % nj + nj) % nj;
+                    c = (c % nk + nk) % nk;
+                    return 1 + a + ni * (b + nj * c);
+                };
+                const cfd_grid_t &r = g->grid[row(i, j, k)];
+                if (r.loc != 0) return false;
+                if (r.N1 != row(i + 1, j, k) || r.N3 != row(i - 1, j, k) || r.N0 != row(i, j + 1, k)
+                    || r.N2 != row(i, j - 1, k) || r.N4 != row(i, j, k + 1) || r.N5 != row(i, j, k - 1))
+                    return false;
+            }
+    return true;
+}
+
+// The face-based path evaluates face n+1/2 from node n's +d data; the
+// reference evaluates it again from node n+1's -d data.  Both must agree.
+bool faces_single_valued(const cfd_geometry_t *g)
+{
+    const int N = g->sd_node;
+    const double tol = 1e-13;
+    auto close = [&](double a, double b, double scale) { return std::fabs(a - b) <= tol * scale; };
+    for (int r = 1; r <= N; ++r) {
+        const double *m = (const double *)&g->metric[r];
+        const double *dd = (const double *)&g->deter[r];
+        const int slots[3] = {1, 0, 4};
+        for (int d = 0; d < 3; ++d) {
+            const int nbr = nb_of(g->grid[r], slots[d]);
+            const double *mn = (const double *)&g->metric[nbr];
+            const double *dn = (const double *)&g->deter[nbr];
+            double scale = 0;
+            for (int c = 0; c < 3; ++c) scale = std::fmax(scale, std::fabs(m[9 * (1 + 2 * d) + 3 * d + c]));
+            for (int c = 0; c < 3; ++c)
+                if (!close(m[9 * (1 + 2 * d) + 3 * d + c], mn[9 * (2 + 2 * d) + 3 * d + c], scale)) return false;
+            if (!close(dd[2 * d], dn[2 * d + 1], std::fabs(dd[2 * d]))) return false;
+        }
+    }
+    return true;
+}
+
+cfd_status_t create_gather(cfd_solver *s, const cfd_geometry_t *g)
+{
+    const size_t R = (size_t)s->n_rows;
+    cfd_status_t st;
+    if ((st = dalloc_t(s, R * 14, &s->grid)) || (st = dalloc_t(s, R, &s->det)) || (st = dalloc_t(s, R * 6, &s->deter))
+        || (st = dalloc_t(s, R * 63, &s->metric)) || (st = dalloc_t(s, R * 9, &s->flow)))
+        return st;
+    for (int q = 0; q < 3; ++q)
+        if ((st = dalloc_t(s, R * 5, &s->U[q]))) return st;
+    double **c5[] = {&s->Q, &s->F, &s->E, &s->G, &s->Fv, &s->Ev, &s->Gv, &s->L};
+    for (double **p : c5)
+        if ((st = dalloc_t(s, R * 5, p))) return st;
+    if ((st = dalloc_t(s, R * 36, &s->roe))) return st;
+    for (int q = 0; q < 3; ++q) cudaMemsetAsync(s->U[q], 0, R * 5 * sizeof(double), s->ctx->stream);
+    for (double **p : c5) cudaMemsetAsync(*p, 0, R * 5 * sizeof(double), s->ctx->stream);
+    cudaMemsetAsync(s->roe, 0, R * 36 * sizeof(double), s->ctx->stream);
+    if ((st = upload(s, s->grid, g->grid, R * sizeof(cfd_grid_t))) || (st = upload(s, s->det, g->det, R * 8))
+        || (st = upload(s, s->deter, g->deter, R * 48)) || (st = upload(s, s->metric, g->metric, R * 504)))
+        return st;
+    cudaError_t e = cudaStreamSynchronize(s->ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(s->ctx, e, "solver create sync");
+    return CFD_OK;
+}
+
+cfd_status_t create_structured(cfd_solver *s, const cfd_geometry_t *g)
+{
+    const size_t N = (size_t)s->ni * s->nj * s->nk;
+    StructuredLaunch &S = s->S;
+    S.ni = s->ni;
+    S.nj = s->nj;
+    S.nk = s->nk;
+    S.stream = s->ctx->stream;
+    S.P = s->P;
+    S.mixed = s->mixed ? 1 : 0;
+    S.flags = s->ctx->d_flags;
+    double *m9, *det, *fm, *fdet;
+    cfd_status_t st;
+    if ((st = dalloc_t(s, 9 * N, &m9)) || (st = dalloc_t(s, N, &det)) || (st = dalloc_t(s, 9 * N, &fm))
+        || (st = dalloc_t(s, 3 * N, &fdet)) || (st = dalloc_t(s, 9 * N, &S.prim9)) || (st = dalloc_t(s, 5 * N, &S.Q))
+        || (st = dalloc_t(s, 15 * N, &S.FEG)) || (st = dalloc_t(s, 15 * N, &S.V)) || (st = dalloc_t(s, 2 * N, &S.sh))
+        || (st = dalloc_t(s, 15 * N, &S.Fh)) || (st = dalloc_t(s, 9 * (N + 1), &s->stage9))
+        || (st = dalloc_t(s, 5 * (N + 1), &s->stage5)) || (st = dalloc_t(s, 5 * N, &s->Lsoa)))
+        return st;
+    for (int q = 0; q < 3; ++q)
+        if ((st = dalloc_t(s, 5 * N, &S.U[q]))) return st;
+    for (int q = 0; q < 3; ++q) cudaMemsetAsync(S.U[q], 0, 5 * N * sizeof(double), S.stream);
+    cudaMemsetAsync(S.V, 0, 15 * N * sizeof(double), S.stream);
+    cudaMemsetAsync(s->stage5, 0, 5 * (N + 1) * sizeof(double), S.stream);
+    cudaMemsetAsync(s->stage9, 0, 9 * (N + 1) * sizeof(double), S.stream);
+    // geometry AoS -> SoA on the host (one-off)
+    std::vector<double> h(9 * N), hd(N), hf(9 * N), hfd(3 * N);
+    for (size_t n = 0; n < N; ++n) {
+        const double *m = (const double *)&g->metric[n + 1];
+        const double *dd = (const double *)&g->deter[n + 1];
+        for (int q = 0; q < 9; ++q) h[q * N + n] = m[q];
+        hd[n] = g->det[n + 1];
+        for (int d = 0; d < 3; ++d) {
+            for (int c = 0; c < 3; ++c) hf[(d * 3 + c) * N + n] = m[9 * (1 + 2 * d) + 3 * d + c];
+            hfd[d * N + n] = dd[2 * d];
+        }
+    }
+    if ((st = upload(s, m9, h.data(), 9 * N * 8)) || (st = upload(s, det, hd.data(), N * 8))
+        || (st = upload(s, fm, hf.data(), 9 * N * 8)) || (st = upload(s, fdet, hfd.data(), 3 * N * 8)))
+        return st;
+    cudaError_t e = cudaStreamSynchronize(S.stream);   // host vectors go out of scope
+    if (e != cudaSuccess) return cuda_fail(s->ctx, e, "solver create sync");
+    S.m9 = m9;
+    S.det = det;
+    S.fm = fm;
+    S.fdet = fdet;
+    return CFD_OK;
+}
+
+cfd_status_t run_stage(cfd_solver *s, int j, double dt, bool want_L)
+{
+    cfd_ctx *ctx = s->ctx;
+    if (s->path == CFD_PATH_STRUCTURED) {
+        structured_stage(s->S, j, dt, want_L ? s->Lsoa : nullptr);
+        ctx->launches += structured_launches_per_stage();
+    } else {
+        double *Uj = s->U[j];
+        launch_uq(ctx->stream, Uj, s->Q, s->grid, s->det, s->flow, s->roe, s->g_node + 1, s->n_rows, ctx->d_flags);
+        launch_viscous(ctx->stream, s->P, Uj, s->F, s->E, s->G, s->Fv, s->Ev, s->Gv, s->grid, s->metric, s->det,
+                       s->flow, s->g_node + 1, s->n_rows, ctx->d_flags);
+        launch_weno(ctx->stream, s->P, j, s->P.mach, dt, s->deter, s->det, s->U[0], s->U[1], s->U[2], s->grid, s->Q,
+                    s->metric, s->roe, s->Fv, s->Ev, s->Gv, s->F, s->E, s->G, s->flow, s->sd_node + 1, s->n_rows,
+                    ctx->d_flags, want_L ? s->L : nullptr);
+        ctx->launches += 3;
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "stage launch");
+    return CFD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+cfd_status_t cfd_solver_create(cfd_ctx_t *ctx, const cfd_geometry_t *geom, const cfd_params_t *params,
+                               int32_t force_path, cfd_solver_t **out)
+{
+    if (!ctx || !geom || !out) return CFD_EINVAL;
+    *out = nullptr;
+    if (!geom->grid || !geom->det || !geom->deter || !geom->metric)
+        return fail(ctx, CFD_EINVAL, "cfd_solver_create: null geometry array");
+    if (geom->g_node < 1 || geom->sd_node < 1 || geom->sd_node > geom->g_node)
+        return fail(ctx, CFD_EINVAL, "cfd_solver_create: need 1 <= sd_node <= g_node");
+    if (force_path < -1 || force_path > 1) return fail(ctx, CFD_EINVAL, "cfd_solver_create: bad force_path");
+    const int32_t n_rows = geom->g_node + 1;
+    for (int32_t r = 0; r < n_rows; ++r)
+        for (int slot = 0; slot < 6; ++slot) {
+            const int v = nb_of(geom->grid[r], slot);
+            if (v < 0 || v >= n_rows)
+                return fail(ctx, CFD_EINVAL, "cfd_solver_create: neighbour index outside [0, g_node]");
+        }
+    cfd_status_t st = use_device(ctx);
+    if (st != CFD_OK) return st;
+    cfd_solver *s = new cfd_solver();
+    s->ctx = ctx;
+    cfd_params_default(&s->prm);
+    if (params) s->prm = *params;
+    s->P = make_phys(&s->prm);
+    s->mixed = s->prm.precision == CFD_PREC_MIXED;
+    s->g_node = geom->g_node;
+    s->sd_node = geom->sd_node;
+    s->n_rows = n_rows;
+    int ni = 0, nj = 0, nk = 0;
+    const bool lattice = force_path != CFD_PATH_GATHER && detect_lattice(geom, ni, nj, nk) && faces_single_valued(geom);
+    if (force_path == CFD_PATH_STRUCTURED && !lattice) {
+        delete s;
+        return fail(ctx, CFD_EINVAL, "cfd_solver_create: table is not a periodic lattice with single-valued faces");
+    }
+    s->path = lattice ? CFD_PATH_STRUCTURED : CFD_PATH_GATHER;
+    if (s->mixed && s->path != CFD_PATH_STRUCTURED) {
+        delete s;
+        return fail(ctx, CFD_EUNSUPPORTED, "cfd_solver_create: mixed precision needs the structured path");
+    }
+    s->ni = ni;
+    s->nj = nj;
+    s->nk = nk;
+    st = s->path == CFD_PATH_STRUCTURED ? create_structured(s, geom) : create_gather(s, geom);
+    if (st != CFD_OK) {
+        cfd_solver_destroy(s);
+        return st;
+    }
+    *out = s;
+    return CFD_OK;
+}
+
+cfd_status_t cfd_solver_destroy(cfd_solver_t *s)
+{
+    if (!s) return CFD_EINVAL;
+    use_device(s->ctx);
+    cudaStreamSynchronize(s->ctx->stream);
+    for (void *p : s->allocs) cudaFree(p);
+    delete s;
+    return CFD_OK;
+}
+
+cfd_status_t cfd_solver_info(const cfd_solver_t *s, cfd_solver_info_t *info)
+{
+    if (!s || !info) return CFD_EINVAL;
+    std::memset(info, 0, sizeof *info);
+    info->path = s->path;
+    info->ni = s->ni;
+    info->nj = s->nj;
+    info->nk = s->nk;
+    info->precision = s->mixed ? CFD_PREC_MIXED : CFD_PREC_FP64;
+    info->device_bytes = s->bytes;
+    return CFD_OK;
+}
+
+cfd_status_t cfd_solver_set_flow(cfd_solver_t *s, const cfd_flow_t *flow_host)
+{
+    if (!s || !flow_host) return CFD_EINVAL;
+    cfd_status_t st = use_device(s->ctx);
+    if (st != CFD_OK) return st;
+    const size_t R = (size_t)s->n_rows;
+    if (s->path == CFD_PATH_GATHER) {
+        st = upload(s, s->flow, flow_host, R * sizeof(cfd_flow_t));
+    } else {
+        const long long N = (long long)s->ni * s->nj * s->nk;
+        st = upload(s, s->stage9, flow_host, R * sizeof(cfd_flow_t));
+        if (st == CFD_OK) aos_to_soa(s->ctx->stream, s->stage9, 9, 9, N, s->S.prim9);
+    }
+    if (st != CFD_OK) return st;
+    return drain(s->ctx);
+}
+
+cfd_status_t cfd_solver_get_flow(cfd_solver_t *s, cfd_flow_t *flow_host)
+{
+    if (!s || !flow_host) return CFD_EINVAL;
+    cfd_status_t st = use_device(s->ctx);
+    if (st != CFD_OK) return st;
+    const size_t R = (size_t)s->n_rows;
+    const double *src = s->flow;
+    if (s->path == CFD_PATH_STRUCTURED) {
+        soa_to_aos(s->ctx->stream, s->S.prim9, 9, 9, (long long)s->ni * s->nj * s->nk, s->stage9);
+        src = s->stage9;
+    }
+    cudaError_t e = cudaMemcpyAsync(flow_host, src, R * sizeof(cfd_flow_t), cudaMemcpyDeviceToHost, s->ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(s->ctx, e, "cudaMemcpyAsync D2H (flow)");
+    return drain(s->ctx);
+}
+
+cfd_status_t cfd_solver_get_u0(cfd_solver_t *s, cfd_column_t *u0_host)
+{
+    if (!s || !u0_host) return CFD_EINVAL;
+    cfd_status_t st = use_device(s->ctx);
+    if (st != CFD_OK) return st;
+    const size_t R = (size_t)s->n_rows;
+    const double *src = s->U[0];
+    if (s->path == CFD_PATH_STRUCTURED) {
+        soa_to_aos(s->ctx->stream, s->S.U[0], 5, 5, (long long)s->ni * s->nj * s->nk, s->stage5);
+        src = s->stage5;
+    }
+    cudaError_t e = cudaMemcpyAsync(u0_host, src, R * sizeof(cfd_column_t), cudaMemcpyDeviceToHost, s->ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(s->ctx, e, "cudaMemcpyAsync D2H (U0)");
+    return drain(s->ctx);
+}
+
+cfd_status_t cfd_solver_step(cfd_solver_t *s, double del_t, int32_t nsteps)
+{
+    if (!s || nsteps < 0 || !std::isfinite(del_t)) return CFD_EINVAL;
+    cfd_status_t st = use_device(s->ctx);
+    if (st != CFD_OK) return st;
+    for (int n = 0; n < nsteps; ++n)
+        for (int j = 0; j < 3; ++j)
+            if ((st = run_stage(s, j, del_t, false)) != CFD_OK) return st;
+    if (s->ctx->async) return CFD_OK;
+    return drain(s->ctx);
+}
+
+cfd_status_t cfd_solver_stage(cfd_solver_t *s, int32_t j, double del_t, cfd_column_t *L_host)
+{
+    if (!s || j < 0 || j > 2) return CFD_EINVAL;
+    cfd_status_t st = use_device(s->ctx);
+    if (st != CFD_OK) return st;
+    if ((st = run_stage(s, j, del_t, L_host != nullptr)) != CFD_OK) return st;
+    if (L_host) {
+        const size_t R = (size_t)s->n_rows;
+        const double *src = s->L;
+        if (s->path == CFD_PATH_STRUCTURED) {
+            soa_to_aos(s->ctx->stream, s->Lsoa, 5, 5, (long long)s->ni * s->nj * s->nk, s->stage5);
+            src = s->stage5;
+        }
+        cudaError_t e = cudaMemcpyAsync(L_host, src, R * sizeof(cfd_column_t), cudaMemcpyDeviceToHost, s->ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(s->ctx, e, "cudaMemcpyAsync D2H (L)");
+    }
+    return drain(s->ctx);
+}
+
+}  // extern "C"

@@ -1,0 +1,36 @@
+// structured.h -- launch interface of the face-based lattice kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "physics.cuh"
+
+namespace cfd {
+
+// Device pointers of one lattice (SoA, [component][N]).
+struct StructuredLaunch {
+    int ni, nj, nk;
+    cudaStream_t stream;
+    Phys P;
+    int mixed;                 // 1: characteristic/WENO/LLF in FP32
+    const double *m9;          // [9][N]   node metrics
+    const double *det;         // [N]
+    const double *fm;          // [3 dir][3 comp][N] metric of face n+1/2
+    const double *fdet;        // [3][N]   det of face n+1/2
+    double *prim9;             // [9][N]   FLOW fields u,v,w,p,t,rho,mu,a,e
+    double *U[3];              // [5][N]   U0, U1, U2
+    double *Q;                 // [5][N]
+    double *FEG;               // [3][5][N] contravariant node fluxes
+    double *V;                 // [3][5][N] viscous fluxes
+    double *sh;                // [2][N]   sqrt(rho), H
+    double *Fh;                // [3][5][N] corrected face fluxes
+    unsigned *flags;
+};
+
+// One RK stage j of the host loop; Lout (device [5][N]) may be null.
+void structured_stage(const StructuredLaunch &S, int j, double dt, double *Lout);
+int structured_launches_per_stage();
+void aos_to_soa(cudaStream_t st, const double *aos, int stride, int ncomp, long long N, double *soa);
+void soa_to_aos(cudaStream_t st, const double *soa, int stride, int ncomp, long long N, double *aos);
+
+}  // namespace cfd

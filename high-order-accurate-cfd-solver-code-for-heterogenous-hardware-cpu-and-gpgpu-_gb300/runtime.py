@@ -1,0 +1,218 @@
+"""Host-side mirror of the reference's RHS interface over the C ABI.
+
+``Context`` mirrors the reference's OpenCL objects: device buffers
+(``cl::Buffer``, Solver.cpp:232-273), copies (``cl::copy``) and the three
+kernel launches with the reference's argument order (``uq``, ``viscous``,
+``weno``; Solver.cpp:277-315, 377, 440, 521).  ``Solver`` is the resident
+form of the reference host loop (Solver.cpp:356-658): the state stays on the
+device and whole SSP-RK3 steps run without host round trips.
+
+Errors surface as ``CfdError`` carrying the library's status code, instead of
+the reference's print-and-exit.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+
+import numpy as np
+
+from . import abi
+from . import layout as L
+
+# per-row sizes (bytes) of every reference buffer
+ROW_BYTES = {"grid": 56, "det": 8, "deter": 48, "metric": 504, "flow": 72, "U0": 40, "U1": 40, "U2": 40,
+             "Q": 40, "F": 40, "E": 40, "G": 40, "Fv": 40, "Ev": 40, "Gv": 40, "roe": 288, "L": 40}
+
+
+def to_params(p) -> abi.Params:
+    out = abi.Params()
+    abi.load().cfd_params_default(C.byref(out))
+    if p is None:
+        return out
+    out.mach, out.reynolds, out.prandtl, out.t_inf = p.mach, p.reynolds, p.prandtl, p.t_inf
+    out.weno_eps = p.weno_eps
+    out.viscous, out.les = int(p.viscous), int(p.les)
+    out.precision = int(getattr(p, "precision", 0))
+    return out
+
+
+def _ptr(a: np.ndarray) -> int:
+    assert a.flags["C_CONTIGUOUS"], "arrays must be C-contiguous"
+    return a.ctypes.data
+
+
+class Context:
+    """One CUDA device + stream; owns the error state of its launches."""
+
+    def __init__(self, device: int = 0):
+        self.lib = abi.load()
+        h = C.c_void_p()
+        s = self.lib.cfd_ctx_create(C.byref(h), int(device))
+        if s != abi.OK:
+            raise abi.CfdError(s, "cfd_ctx_create")
+        self.h = h
+        self._buffers = []
+
+    # -- errors --
+    def check(self, status: int, where: str):
+        if status != abi.OK:
+            detail = self.lib.cfd_last_error(self.h)
+            raise abi.CfdError(status, where, detail.decode() if detail else "")
+
+    def close(self):
+        if self.h:
+            for p in self._buffers:
+                self.lib.cfd_buffer_free(self.h, p)
+            self._buffers = []
+            self.lib.cfd_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_rows(self, n_rows: int):
+        self.check(self.lib.cfd_ctx_set_rows(self.h, int(n_rows)), "cfd_ctx_set_rows")
+
+    def set_async(self, on: bool):
+        self.check(self.lib.cfd_ctx_set_async(self.h, 1 if on else 0), "cfd_ctx_set_async")
+
+    def synchronize(self):
+        self.check(self.lib.cfd_ctx_synchronize(self.h), "cfd_ctx_synchronize")
+
+    @property
+    def launch_count(self) -> int:
+        return int(self.lib.cfd_ctx_launch_count(self.h))
+
+    # -- buffers (cl::Buffer / cl::copy) --
+    def alloc(self, nbytes: int) -> int:
+        p = C.c_void_p()
+        self.check(self.lib.cfd_buffer_alloc(self.h, int(nbytes), C.byref(p)), "cfd_buffer_alloc")
+        self._buffers.append(p.value)
+        return p.value
+
+    def free(self, ptr: int):
+        self.check(self.lib.cfd_buffer_free(self.h, C.c_void_p(ptr)), "cfd_buffer_free")
+        self._buffers.remove(ptr)
+
+    def write(self, dev: int, host: np.ndarray):
+        self.check(self.lib.cfd_buffer_write(self.h, C.c_void_p(dev), C.c_void_p(_ptr(host)), host.nbytes),
+                   "cfd_buffer_write")
+
+    def read(self, host: np.ndarray, dev: int):
+        self.check(self.lib.cfd_buffer_read(self.h, C.c_void_p(_ptr(host)), C.c_void_p(dev), host.nbytes),
+                   "cfd_buffer_read")
+
+    def upload_case(self, arrays: dict, names=None) -> dict:
+        """Device copies of the reference buffers of a case (plus L)."""
+        names = names or list(arrays) + ["L"]
+        n_rows = arrays["det"].shape[0]
+        dev = {}
+        for k in names:
+            dev[k] = self.alloc(ROW_BYTES[k] * n_rows)
+            if k in arrays:
+                self.write(dev[k], np.ascontiguousarray(arrays[k]))
+        self.set_rows(n_rows)
+        return dev
+
+    def download(self, dev: dict, name: str, like: np.ndarray) -> np.ndarray:
+        out = np.empty_like(like)
+        self.read(out, dev[name])
+        return out
+
+    # -- the three reference kernels (device pointers, reference arg order) --
+    def uq(self, U_C, Q_C, Grid_P, det, FLOW, ROE_AVER, n_items: int):
+        self.check(self.lib.cfd_uq(self.h, U_C, Q_C, Grid_P, det, FLOW, ROE_AVER, int(n_items)), "cfd_uq")
+
+    def viscous(self, U_C, F_C, E_C, G_C, Fv_C, Ev_C, Gv_C, Grid_P, metric, det, FLOW, n_items: int, params=None):
+        pr = to_params(params)
+        self.check(self.lib.cfd_viscous(self.h, U_C, F_C, E_C, G_C, Fv_C, Ev_C, Gv_C, Grid_P, metric, det, FLOW,
+                                        int(n_items), C.byref(pr)), "cfd_viscous")
+
+    def weno(self, j, Mach, del_t, deter, det, U0, U1, U2, Grid_P, Q_C, metric, ROE_AVER, Fv, Ev, Gv, F, E, G,
+             FLOW, n_items: int, params=None, L_out=None):
+        pr = to_params(params)
+        self.check(self.lib.cfd_weno(self.h, int(j), float(Mach), float(del_t), deter, det, U0, U1, U2, Grid_P, Q_C,
+                                     metric, ROE_AVER, Fv, Ev, Gv, F, E, G, FLOW, int(n_items), C.byref(pr), L_out),
+                   "cfd_weno")
+
+    def stage(self, dev: dict, g_node: int, sd_node: int, params, j: int, dt: float, want_L: bool = False):
+        """One stage of the reference host loop (Solver.cpp:365-541) through
+        the three drop-in entry points; U_Q writes U_j, Viscous reads U_j."""
+        Uj = dev[("U0", "U1", "U2")[j]]
+        self.uq(Uj, dev["Q"], dev["grid"], dev["det"], dev["flow"], dev["roe"], g_node + 1)
+        self.viscous(Uj, dev["F"], dev["E"], dev["G"], dev["Fv"], dev["Ev"], dev["Gv"], dev["grid"], dev["metric"],
+                     dev["det"], dev["flow"], g_node + 1, params)
+        self.weno(j, params.mach, dt, dev["deter"], dev["det"], dev["U0"], dev["U1"], dev["U2"], dev["grid"],
+                  dev["Q"], dev["metric"], dev["roe"], dev["Fv"], dev["Ev"], dev["Gv"], dev["F"], dev["E"], dev["G"],
+                  dev["flow"], sd_node + 1, params, dev["L"] if want_L else None)
+
+
+@dataclasses.dataclass
+class SolverInfo:
+    path: str
+    shape: tuple
+    precision: str
+    device_bytes: int
+
+
+class Solver:
+    """Resident RHS solver for one grid (cfd_solver_*)."""
+
+    def __init__(self, ctx: Context, case, params=None, force_path: int = -1, precision: int = 0):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        a = case.arrays
+        self._geom_arrays = (a["grid"], a["det"], a["deter"], a["metric"])
+        self.g_node, self.sd_node = case.g_node, case.sd_node
+        geom = abi.Geometry(case.g_node, case.sd_node, _ptr(a["grid"]), _ptr(a["det"]), _ptr(a["deter"]),
+                            _ptr(a["metric"]))
+        pr = to_params(params if params is not None else case.params)
+        pr.precision = int(precision)
+        h = C.c_void_p()
+        ctx.check(self.lib.cfd_solver_create(ctx.h, C.byref(geom), C.byref(pr), int(force_path), C.byref(h)),
+                  "cfd_solver_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.cfd_solver_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self) -> SolverInfo:
+        i = abi.SolverInfo()
+        self.ctx.check(self.lib.cfd_solver_info(self.h, C.byref(i)), "cfd_solver_info")
+        return SolverInfo("structured" if i.path == abi.PATH_STRUCTURED else "gather", (i.ni, i.nj, i.nk),
+                          "mixed" if i.precision == abi.PREC_MIXED else "fp64", int(i.device_bytes))
+
+    def set_flow(self, flow: np.ndarray):
+        assert flow.shape == (self.g_node + 1, L.NFLOW) and flow.dtype == np.float64
+        self.ctx.check(self.lib.cfd_solver_set_flow(self.h, C.c_void_p(_ptr(flow))), "cfd_solver_set_flow")
+
+    def get_flow(self, out: np.ndarray | None = None) -> np.ndarray:
+        out = np.empty((self.g_node + 1, L.NFLOW)) if out is None else out
+        self.ctx.check(self.lib.cfd_solver_get_flow(self.h, C.c_void_p(_ptr(out))), "cfd_solver_get_flow")
+        return out
+
+    def get_u0(self) -> np.ndarray:
+        out = np.empty((self.g_node + 1, L.NCOL))
+        self.ctx.check(self.lib.cfd_solver_get_u0(self.h, C.c_void_p(_ptr(out))), "cfd_solver_get_u0")
+        return out
+
+    def step(self, dt: float, nsteps: int = 1):
+        self.ctx.check(self.lib.cfd_solver_step(self.h, float(dt), int(nsteps)), "cfd_solver_step")
+
+    def stage(self, j: int, dt: float, want_L: bool = True):
+        out = np.zeros((self.g_node + 1, L.NCOL)) if want_L else None
+        self.ctx.check(self.lib.cfd_solver_stage(self.h, int(j), float(dt), C.c_void_p(_ptr(out)) if want_L else None),
+                       "cfd_solver_stage")
+        return out

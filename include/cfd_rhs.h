@@ -1,0 +1,226 @@
+/*
+ * cfd_rhs.h -- C ABI of the GB300 right-hand-side path (libcfd_gb300.so).
+ *
+ * Drop-in replacement for the three OpenCL kernel launches of the reference
+ * solver's host loop (Solver.cpp:365-541):
+ *
+ *   reference launch                                   replacement
+ *   -------------------------------------------------  -----------------
+ *   queue.enqueueNDRangeKernel(kernel_U_Q, ...)        cfd_uq
+ *        Solver.cpp:377, kernel args Solver.cpp:277-282, U_Q.cl:36-38
+ *   queue_viscous.enqueueNDRangeKernel(kernel_viscous) cfd_viscous
+ *        Solver.cpp:440, args Solver.cpp:284-294, Viscous.cl:23-26
+ *   queue_weno.enqueueNDRangeKernel(kernel_weno, ...)  cfd_weno
+ *        Solver.cpp:521, args Solver.cpp:296-314, Weno.cl:36-40
+ *   cl::Buffer(...) / cl::copy(...)                    cfd_buffer_*
+ *        Solver.cpp:232-273 and the copies around each launch
+ *
+ * The buffers use the reference's packed array-of-structs layout
+ * (functions.h:49-113), reproduced below with the same field names and
+ * sizes.  Row 0 is the reference's dummy row; the NDRange of U_Q and Viscous
+ * is g_node+1 rows, that of Weno sd_node+1 rows (Solver.cpp:31-38).
+ *
+ * Beyond the drop-in, the library offers a resident solver object that runs
+ * whole SSP-RK3 steps on the device (cfd_solver_*), selecting a face-based
+ * structured-grid path when the neighbour table is a periodic lattice, and a
+ * batched solver for many grids in one launch per stage (cfd_batch_*).
+ *
+ * Error handling: every entry point returns a cfd_status_t; none exits the
+ * process (the reference prints and calls exit(1), Solver.cpp:378-381).
+ * Threading: a context is used by one host thread at a time; separate
+ * contexts may be used concurrently.
+ */
+#ifndef CFD_RHS_H
+#define CFD_RHS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CFD_ABI_VERSION 1
+
+typedef enum {
+    CFD_OK = 0,
+    CFD_EINVAL = 1,        /* bad argument, pointer kind, neighbour index or size */
+    CFD_ENONFINITE = 2,    /* a NaN/Inf appeared in the advanced state            */
+    CFD_ETIMEOUT = 3,      /* a bounded device wait gave up                       */
+    CFD_ECUDA = 4,         /* a CUDA runtime call failed (see cfd_last_error)     */
+    CFD_ENOMEM = 5,        /* device allocation failed                            */
+    CFD_EUNSUPPORTED = 6   /* request outside what this build supports            */
+} cfd_status_t;
+
+/* ------------------------------------------------ reference data layout -- */
+#pragma pack(push, 1)
+/* GRID (functions.h:57-61): coordinates, neighbours N0=+j N1=+i N2=-j N3=-i
+ * N4=+k N5=-k (U_Q.cl:51-56), node ID and location code (0 interior,
+ * 1..56 boundary, 100 ghost). */
+typedef struct {
+    double x, y, z;
+    int32_t N0, N1, N2, N3, N4, N5;
+    int32_t ID, loc;
+} cfd_grid_t;
+
+/* FLOW_VARIABLES (functions.h:49-51). */
+typedef struct {
+    double u, v, w, p, t, rho, mu, a, e;
+} cfd_flow_t;
+
+/* Solver_Column_matrix (functions.h:53-55): rho, rho u, rho v, rho w, E. */
+typedef struct {
+    double N0, N1, N2, N3, N4;
+} cfd_column_t;
+
+/* TRANSFORMED (functions.h:93-98): node metrics, then the half-point metrics
+ * of the six faces. */
+typedef struct {
+    double zeta_x, zeta_y, zeta_z, eta_x, eta_y, eta_z, xi_x, xi_y, xi_z;
+    double zeta_xip, zeta_yip, zeta_zip, eta_xip, eta_yip, eta_zip, xi_xip, xi_yip, xi_zip;
+    double zeta_xim, zeta_yim, zeta_zim, eta_xim, eta_yim, eta_zim, xi_xim, xi_yim, xi_zim;
+    double zeta_xjp, zeta_yjp, zeta_zjp, eta_xjp, eta_yjp, eta_zjp, xi_xjp, xi_yjp, xi_zjp;
+    double zeta_xjm, zeta_yjm, zeta_zjm, eta_xjm, eta_yjm, eta_zjm, xi_xjm, xi_yjm, xi_zjm;
+    double zeta_xkp, zeta_ykp, zeta_zkp, eta_xkp, eta_ykp, eta_zkp, xi_xkp, xi_ykp, xi_zkp;
+    double zeta_xkm, zeta_ykm, zeta_zkm, eta_xkm, eta_ykm, eta_zkm, xi_xkm, xi_ykm, xi_zkm;
+} cfd_metric_t;
+
+/* DETERM (functions.h:110-112): face Jacobian determinants. */
+typedef struct {
+    double ip, im, jp, jm, kp, km;
+} cfd_determ_t;
+
+/* ROE_AVERAGING (functions.h:63-70): Roe states of the six faces. */
+typedef struct {
+    double roe_u_ip, roe_v_ip, roe_w_ip, roe_p_ip, roe_h_ip, roe_rho_ip;
+    double roe_u_jp, roe_v_jp, roe_w_jp, roe_p_jp, roe_h_jp, roe_rho_jp;
+    double roe_u_kp, roe_v_kp, roe_w_kp, roe_p_kp, roe_h_kp, roe_rho_kp;
+    double roe_u_im, roe_v_im, roe_w_im, roe_p_im, roe_h_im, roe_rho_im;
+    double roe_u_jm, roe_v_jm, roe_w_jm, roe_p_jm, roe_h_jm, roe_rho_jm;
+    double roe_u_km, roe_v_km, roe_w_km, roe_p_km, roe_h_km, roe_rho_km;
+} cfd_roe_t;
+#pragma pack(pop)
+
+/* -------------------------------------------------------- parameters ---- */
+typedef enum { CFD_PREC_FP64 = 0, CFD_PREC_MIXED = 1 } cfd_precision_t;
+
+/* The constants the reference hard-codes (Viscous.cl:30-33 Mach 1.5,
+ * Reyl 500, Pr 0.72, Free_t 273; Weno.cl:59 Epsilon 10e-8).  A NULL params
+ * pointer anywhere below means exactly these values with viscous and LES on
+ * and FP64 arithmetic.  gamma is 1.4 throughout, as in the reference. */
+typedef struct {
+    double mach;
+    double reynolds;
+    double prandtl;
+    double t_inf;
+    double weno_eps;
+    int32_t viscous;     /* 0: Fv = Ev = Gv = 0 (inviscid)                    */
+    int32_t les;         /* 0: drop the mixed-time-scale SGS terms            */
+    int32_t precision;   /* cfd_precision_t (solver objects only)             */
+    int32_t reserved;
+} cfd_params_t;
+
+void cfd_params_default(cfd_params_t *p);
+
+/* ----------------------------------------------------------- context ---- */
+typedef struct cfd_ctx cfd_ctx_t;
+
+/* Creates a context on CUDA device `device` with its own stream. */
+cfd_status_t cfd_ctx_create(cfd_ctx_t **ctx, int device);
+cfd_status_t cfd_ctx_destroy(cfd_ctx_t *ctx);
+/* Use a caller-owned cudaStream_t (as void*) instead of the context's. */
+cfd_status_t cfd_ctx_set_stream(cfd_ctx_t *ctx, void *cuda_stream);
+/* async = 0 (default): each kernel entry point waits for its launch and
+ * reports device-side errors, like the reference's event.wait(); finish().
+ * async = 1: entry points only enqueue; errors surface at synchronize. */
+cfd_status_t cfd_ctx_set_async(cfd_ctx_t *ctx, int async);
+cfd_status_t cfd_ctx_synchronize(cfd_ctx_t *ctx);
+/* Number of rows of every buffer (g_node + 1).  Neighbour indices outside
+ * [0, n_rows) make a kernel skip the row and report CFD_EINVAL. */
+cfd_status_t cfd_ctx_set_rows(cfd_ctx_t *ctx, int32_t n_rows);
+/* Kernels this context launched since creation (for accounting). */
+uint64_t cfd_ctx_launch_count(const cfd_ctx_t *ctx);
+const char *cfd_status_string(cfd_status_t s);
+const char *cfd_last_error(const cfd_ctx_t *ctx);
+
+/* ------------------------------------------- buffers (cl::Buffer/copy) -- */
+cfd_status_t cfd_buffer_alloc(cfd_ctx_t *ctx, size_t bytes, void **device_ptr);
+cfd_status_t cfd_buffer_free(cfd_ctx_t *ctx, void *device_ptr);
+cfd_status_t cfd_buffer_write(cfd_ctx_t *ctx, void *device_dst, const void *host_src, size_t bytes);
+cfd_status_t cfd_buffer_read(cfd_ctx_t *ctx, void *host_dst, const void *device_src, size_t bytes);
+
+/* ------------------------------------------- drop-in kernel entry points -- */
+/* All buffer arguments are device pointers (cfd_buffer_alloc or any
+ * cudaMalloc'd memory).  Argument order follows the reference kernels; the
+ * trailing params pointer (NULL = reference constants) carries the constants
+ * the reference hard-codes. */
+
+/* U_Q.cl:36-125: Roe averages of the six faces, U_C = det*Q, Q_C. */
+cfd_status_t cfd_uq(cfd_ctx_t *ctx, cfd_column_t *U_C, cfd_column_t *Q_C, const cfd_grid_t *Grid_P,
+                    const double *det, cfd_flow_t *FLOW, cfd_roe_t *ROE_AVER, int32_t n_items);
+
+/* Viscous.cl:23-643: node fluxes F,E,G and viscous + SGS fluxes Fv,Ev,Gv
+ * (contravariant, times det); writes FLOW.mu. */
+cfd_status_t cfd_viscous(cfd_ctx_t *ctx, cfd_column_t *U_C, cfd_column_t *F_C, cfd_column_t *E_C,
+                         cfd_column_t *G_C, cfd_column_t *Fv_C, cfd_column_t *Ev_C, cfd_column_t *Gv_C,
+                         const cfd_grid_t *Grid_P, const cfd_metric_t *metric, const double *det,
+                         cfd_flow_t *FLOW, int32_t n_items, const cfd_params_t *params);
+
+/* Weno.cl:36-3137: characteristic WENO5 + LLF + 6th-order flux correction +
+ * viscous divergence, RHS L, SSP-RK3 stage j (0,1,2) and primitive update.
+ * L_out (device, may be NULL) receives L per row. */
+cfd_status_t cfd_weno(cfd_ctx_t *ctx, int32_t j, double Mach, double del_t, const cfd_determ_t *deter,
+                      const double *det, cfd_column_t *U0, cfd_column_t *U1, cfd_column_t *U2,
+                      const cfd_grid_t *Grid_P, cfd_column_t *Q_C, const cfd_metric_t *metric,
+                      cfd_roe_t *ROE_AVER, cfd_column_t *Fv, cfd_column_t *Ev, cfd_column_t *Gv,
+                      cfd_column_t *F, cfd_column_t *E, cfd_column_t *G, cfd_flow_t *FLOW, int32_t n_items,
+                      const cfd_params_t *params, cfd_column_t *L_out);
+
+/* ---------------------------------------------- resident solver object -- */
+/* Host-side description of one grid in the reference layout (all host
+ * pointers, rows 0..g_node).  Copied at create time. */
+typedef struct {
+    int32_t g_node;     /* rows 1..g_node hold owned + ghost nodes   */
+    int32_t sd_node;    /* rows 1..sd_node are owned (advanced) rows  */
+    const cfd_grid_t *grid;
+    const double *det;
+    const cfd_determ_t *deter;
+    const cfd_metric_t *metric;
+} cfd_geometry_t;
+
+typedef enum {
+    CFD_PATH_GATHER = 0,       /* drop-in kernels on the reference layout       */
+    CFD_PATH_STRUCTURED = 1    /* face-based kernels on a periodic lattice (SoA) */
+} cfd_path_t;
+
+typedef struct {
+    int32_t path;              /* cfd_path_t chosen at create time           */
+    int32_t ni, nj, nk;        /* lattice shape for the structured path      */
+    int32_t precision;         /* cfd_precision_t                            */
+    int32_t reserved;
+    uint64_t device_bytes;     /* device memory held by the solver           */
+} cfd_solver_info_t;
+
+typedef struct cfd_solver cfd_solver_t;
+
+/* `force_path` = -1 chooses automatically; 0/1 forces a path (forcing the
+ * structured path on a table that is not a periodic lattice -> CFD_EINVAL). */
+cfd_status_t cfd_solver_create(cfd_ctx_t *ctx, const cfd_geometry_t *geom, const cfd_params_t *params,
+                               int32_t force_path, cfd_solver_t **solver);
+cfd_status_t cfd_solver_destroy(cfd_solver_t *s);
+cfd_status_t cfd_solver_info(const cfd_solver_t *s, cfd_solver_info_t *info);
+/* State in/out as FLOW rows 0..g_node (host pointers). */
+cfd_status_t cfd_solver_set_flow(cfd_solver_t *s, const cfd_flow_t *flow_host);
+cfd_status_t cfd_solver_get_flow(cfd_solver_t *s, cfd_flow_t *flow_host);
+/* Conserved state U0 (= det*Q at the last step boundary), rows 0..g_node. */
+cfd_status_t cfd_solver_get_u0(cfd_solver_t *s, cfd_column_t *u0_host);
+/* nsteps SSP-RK3 steps of size del_t, entirely on the device. */
+cfd_status_t cfd_solver_step(cfd_solver_t *s, double del_t, int32_t nsteps);
+/* One stage j of the host loop; copies L (rows 0..g_node, owned rows set)
+ * to L_host when non-NULL. */
+cfd_status_t cfd_solver_stage(cfd_solver_t *s, int32_t j, double del_t, cfd_column_t *L_host);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CFD_RHS_H */

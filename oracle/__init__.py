@@ -1,0 +1,190 @@
+"""CPU oracle for the RHS path -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+bench.py may import this package; the product never does.  It wraps two
+shared libraries through ctypes:
+
+* ``liboracle.so`` -- the C restatement in cfd_oracle.c (always built;
+  plain C + OpenMP, portable to the Arm GPU host);
+* ``_ref/libcfd_ref.so`` -- the reference's own kernel sources compiled as
+  host C++ (build_ref.sh; only where the reference checkout exists).  It pins
+  the restatement; golden vectors committed under tests/golden/ were made
+  with it.
+
+Arrays follow the reference layout documented in the product's layout module
+(float64 row-major, row 0 = dummy row).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import pathlib
+import subprocess
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+LIB = HERE / "liboracle.so"
+REF_LIB = HERE / "_ref" / "libcfd_ref.so"
+
+_dp = C.POINTER(C.c_double)
+_vp = C.c_void_p
+
+
+class OrParams(C.Structure):
+    _fields_ = [("mach", C.c_double), ("reynolds", C.c_double), ("prandtl", C.c_double),
+                ("t_inf", C.c_double), ("weno_eps", C.c_double), ("viscous", C.c_int),
+                ("les", C.c_int)]
+
+
+class OrCase(C.Structure):
+    _fields_ = [("g_node", C.c_int), ("sd_node", C.c_int)] + [
+        (n, _vp) for n in ("grid", "det", "deter", "metric", "flow", "U0", "U1", "U2", "Q",
+                           "F", "E", "G", "Fv", "Ev", "Gv", "roe")]
+
+
+def build(force: bool = False) -> None:
+    """Compile the restatement (and the reference pin where possible)."""
+    src = HERE / "cfd_oracle.c"
+    if force or not LIB.exists() or LIB.stat().st_mtime < max(src.stat().st_mtime,
+                                                               (HERE / "cfd_oracle.h").stat().st_mtime):
+        subprocess.run(["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
+                        str(src), "-o", str(LIB), "-lm"], check=True)
+    ref_dir = pathlib.Path(os.environ.get("CFD_REFERENCE_DIR", "/root/reference"))
+    if (ref_dir / "Weno.cl").exists() and (force or not REF_LIB.exists()):
+        subprocess.run(["bash", str(HERE / "build_ref.sh")], check=True)
+
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            build()
+        _lib = C.CDLL(str(LIB))
+        _lib.oracle_stage.argtypes = [C.POINTER(OrCase), C.POINTER(OrParams), C.c_int, C.c_double, _vp]
+        _lib.oracle_rk3_steps.argtypes = [C.POINTER(OrCase), C.POINTER(OrParams), C.c_double, C.c_int]
+        _lib.oracle_uq.argtypes = [C.c_int] + [_vp] * 6
+        _lib.oracle_viscous.argtypes = [C.c_int, C.POINTER(OrParams)] + [_vp] * 11
+        _lib.oracle_weno.argtypes = ([C.c_int, C.c_int, C.c_double, C.c_double, C.POINTER(OrParams)]
+                                     + [_vp] * 17)
+        _lib.oracle_set_threads.argtypes = [C.c_int]
+        _lib.oracle_set_poison.argtypes = [C.c_int]
+        _lib.oracle_get_threads.restype = C.c_int
+    return _lib
+
+
+def ref_available() -> bool:
+    return REF_LIB.exists()
+
+
+def ref():
+    global _ref
+    if _ref is None:
+        _ref = C.CDLL(str(REF_LIB))
+        _ref.ref_uq.argtypes = [C.c_int] + [_vp] * 6
+        _ref.ref_viscous.argtypes = [C.c_int] + [_vp] * 11
+        _ref.ref_viscous_param.argtypes = [C.c_int] + [C.c_double] * 4 + [_vp] * 11
+        _ref.ref_weno.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double] + [_vp] * 16
+    return _ref
+
+
+def _p(a: np.ndarray):
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_vp)
+
+
+def make_params(p) -> OrParams:
+    return OrParams(p.mach, p.reynolds, p.prandtl, p.t_inf, p.weno_eps, int(p.viscous), int(p.les))
+
+
+def make_case(arrays: dict, g_node: int, sd_node: int) -> OrCase:
+    c = OrCase()
+    c.g_node = g_node
+    c.sd_node = sd_node
+    for name, _ in OrCase._fields_[2:]:
+        setattr(c, name, _p(arrays[name]))
+    return c
+
+
+def set_poison(on: bool) -> None:
+    lib().oracle_set_poison(1 if on else 0)
+
+
+def set_threads(n: int) -> None:
+    lib().oracle_set_threads(int(n))
+
+
+# ------------------------------------------------------------ restatement --
+
+def stage(arrays: dict, g_node: int, sd_node: int, params, j: int, dt: float, want_L: bool = False):
+    """One RK stage (U_Q, Viscous, Weno(j)) in place; returns L (rows x 5)."""
+    Lout = np.zeros((g_node + 1, 5)) if want_L else None
+    c = make_case(arrays, g_node, sd_node)
+    pr = make_params(params)
+    lib().oracle_stage(C.byref(c), C.byref(pr), int(j), float(dt), _p(Lout) if want_L else None)
+    return Lout
+
+
+def rk3_steps(arrays: dict, g_node: int, sd_node: int, params, dt: float, nsteps: int) -> None:
+    c = make_case(arrays, g_node, sd_node)
+    pr = make_params(params)
+    lib().oracle_rk3_steps(C.byref(c), C.byref(pr), float(dt), int(nsteps))
+
+
+def uq(a: dict, n_items: int, U_out: np.ndarray) -> None:
+    lib().oracle_uq(n_items, _p(U_out), _p(a["Q"]), _p(a["grid"]), _p(a["det"]), _p(a["flow"]), _p(a["roe"]))
+
+
+def viscous(a: dict, n_items: int, params, U_in: np.ndarray) -> None:
+    pr = make_params(params)
+    lib().oracle_viscous(n_items, C.byref(pr), _p(U_in), _p(a["F"]), _p(a["E"]), _p(a["G"]), _p(a["Fv"]),
+                         _p(a["Ev"]), _p(a["Gv"]), _p(a["grid"]), _p(a["metric"]), _p(a["det"]), _p(a["flow"]))
+
+
+def weno(a: dict, n_items: int, params, j: int, dt: float, want_L: bool = False):
+    Lout = np.zeros((a["det"].shape[0], 5)) if want_L else None
+    pr = make_params(params)
+    lib().oracle_weno(n_items, int(j), params.mach, float(dt), C.byref(pr), _p(a["deter"]), _p(a["det"]),
+                      _p(a["U0"]), _p(a["U1"]), _p(a["U2"]), _p(a["grid"]), _p(a["Q"]), _p(a["metric"]),
+                      _p(a["roe"]), _p(a["Fv"]), _p(a["Ev"]), _p(a["Gv"]), _p(a["F"]), _p(a["E"]), _p(a["G"]),
+                      _p(a["flow"]), _p(Lout) if want_L else None)
+    return Lout
+
+
+# ------------------------------------------------- reference (pin) build --
+
+def ref_uq(a: dict, n_items: int, U_out: np.ndarray) -> None:
+    ref().ref_uq(n_items, _p(U_out), _p(a["Q"]), _p(a["grid"]), _p(a["det"]), _p(a["flow"]), _p(a["roe"]))
+
+
+def ref_viscous(a: dict, n_items: int, params, U_in: np.ndarray) -> None:
+    """The reference Viscous kernel; with its own constants when ``params``
+    carries them (1.5, 500, 0.72, 273), else the constant-substituted copy."""
+    args = (_p(U_in), _p(a["F"]), _p(a["E"]), _p(a["G"]), _p(a["Fv"]), _p(a["Ev"]), _p(a["Gv"]),
+            _p(a["grid"]), _p(a["metric"]), _p(a["det"]), _p(a["flow"]))
+    if (params.mach, params.reynolds, params.prandtl, params.t_inf) == (1.5, 500.0, 0.72, 273.0):
+        ref().ref_viscous(n_items, *args)
+    else:
+        ref().ref_viscous_param(n_items, params.mach, params.reynolds, params.prandtl, params.t_inf, *args)
+    if not params.viscous:
+        for k in ("Fv", "Ev", "Gv"):
+            a[k][:n_items] = 0.0
+
+
+def ref_weno(a: dict, n_items: int, mach: float, j: int, dt: float) -> None:
+    ref().ref_weno(n_items, int(j), float(mach), float(dt), _p(a["deter"]), _p(a["det"]), _p(a["U0"]),
+                   _p(a["U1"]), _p(a["U2"]), _p(a["grid"]), _p(a["Q"]), _p(a["metric"]), _p(a["roe"]),
+                   _p(a["Fv"]), _p(a["Ev"]), _p(a["Gv"]), _p(a["F"]), _p(a["E"]), _p(a["G"]), _p(a["flow"]))
+
+
+def ref_stage(a: dict, g_node: int, sd_node: int, params, j: int, dt: float) -> None:
+    """Solver.cpp:365-541 sequencing with the reference kernels themselves.
+    The reference kernels use eps = 1e-7 (Weno.cl:59) and always run MTS."""
+    Uj = a[("U0", "U1", "U2")[j]]
+    ref_uq(a, g_node + 1, Uj)
+    ref_viscous(a, g_node + 1, params, Uj)
+    ref_weno(a, sd_node + 1, params.mach, j, dt)

@@ -1,0 +1,29 @@
+#!/usr/bin/env bash
+# Builds the parity pin: the reference's own kernel sources (U_Q.cl,
+# Viscous.cl, Weno.cl), compiled where they lie as host C++ through
+# oracle/ref_shim.h, into oracle/_ref/libcfd_ref.so.  Outputs go only to
+# oracle/_ref/ (git-ignored).  The one generated file is a copy of Viscous.cl
+# whose four hard-coded constants (Mach, Reyl, Pr, Free_t) read globals, so
+# the pin also covers other flow parameters.  Needs the reference checkout;
+# exits 0 without building when it is absent.
+set -euo pipefail
+HERE="$(cd "$(dirname "$0")" && pwd)"
+REF_DIR="${CFD_REFERENCE_DIR:-/root/reference}"
+OUT="$HERE/_ref"
+if [ ! -f "$REF_DIR/Weno.cl" ]; then
+    echo "build_ref: reference sources not found at $REF_DIR; skipping" >&2
+    exit 0
+fi
+mkdir -p "$OUT"
+sed -e 's/const double Mach = 1\.5;/const double Mach = ::ref_visc_mach;/' \
+    -e 's/const double Reyl = 500\.0;/const double Reyl = ::ref_visc_reyl;/' \
+    -e 's/const double Pr = 0\.72;/const double Pr = ::ref_visc_pr;/' \
+    -e 's/const double Free_t = 273\.0;/const double Free_t = ::ref_visc_tinf;/' \
+    "$REF_DIR/Viscous.cl" > "$OUT/Viscous_param.cl"
+for c in ref_visc_mach ref_visc_reyl ref_visc_pr ref_visc_tinf; do
+    grep -q "= ::$c;" "$OUT/Viscous_param.cl" || { echo "build_ref: substitution of $c failed" >&2; exit 1; }
+done
+g++ -std=c++17 -O2 -ffp-contract=off -fopenmp -fPIC -shared -w \
+    -I"$HERE" -I"$OUT" -I"$REF_DIR" \
+    "$HERE/ref_kernels.cpp" -o "$OUT/libcfd_ref.so"
+echo "build_ref: built $OUT/libcfd_ref.so"

@@ -1,0 +1,137 @@
+"""Drop-in entry points (cfd_uq, cfd_viscous, cfd_weno) on the GPU against
+the reference's golden vectors and the oracle.  Tolerance: relative L2
+<= 1e-12 (FP64; the GPU contracts a*b+c into FMA and its libm differs from
+the host's in the last ulp, so bitwise equality is not expected)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from helpers import copy_arrays, rel_l2
+from test_oracle_golden import FIXTURES, load_fixture, stage_keys
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+def run_dropin(ctx, arrays, g_node, sd_node, params, dt, stages, want=None):
+    dev = ctx.upload_case(arrays)
+    out = []
+    for j in range(stages):
+        ctx.stage(dev, g_node, sd_node, params, j, dt, want_L=True)
+        snap = {}
+        for k in (want or stage_keys(j)) + ("L",):
+            like = arrays[k] if k in arrays else np.zeros((g_node + 1, 5))
+            snap[k] = ctx.download(dev, k, like)
+        out.append(snap)
+    for p in dev.values():
+        ctx.free(p)
+    return out
+
+
+@pytest.mark.parametrize("name", FIXTURES)
+def test_dropin_matches_reference_golden(ctx, name):
+    z, a, g_node, sd_node, stages, params, dt = load_fixture(name)
+    res = run_dropin(ctx, a, g_node, sd_node, params, dt, stages)
+    rows = np.arange(1, sd_node + 1)
+    for j in range(stages):
+        for k in stage_keys(j):
+            want = z[f"s{j}_{k}"]
+            got = res[j][k]
+            r = rows
+            if f"mask_s{j}_{k}" in z:
+                r = rows[z[f"mask_s{j}_{k}"][rows]]
+            if k == "roe":
+                cols = [c for c in range(36) if c % 6 != 3]
+                got, want = got[:, cols], want[:, cols]
+            err = rel_l2(got[r], want[r])
+            assert err <= TOL, f"{name} stage {j} {k}: {err:.3e}"
+
+
+@pytest.mark.parametrize("maker", ["vortex", "tgv", "tgv_inviscid", "box"])
+def test_dropin_matches_oracle(ctx, oracle_mod, maker):
+    from cfd_gb300 import cases
+    if maker == "vortex":
+        c, stages = cases.isentropic_vortex(n=20, shape=(20, 16, 12)), 3
+    elif maker == "tgv":
+        c, stages = cases.taylor_green(n=14, shape=(14, 12, 10)), 3
+    elif maker == "tgv_inviscid":
+        c, stages = cases.taylor_green(n=12), 3
+        c.params.viscous, c.params.les = 0, 0
+    else:
+        c, stages = cases.ghost_box(shape=(9, 8, 7), seed=5), 1
+    a = copy_arrays(c.arrays)
+    res = run_dropin(ctx, c.arrays, c.g_node, c.sd_node, c.params, c.dt, stages,
+                     want=("F", "E", "G", "Fv", "Ev", "Gv", "U0", "U1", "U2", "flow"))
+    own = np.arange(1, c.sd_node + 1)
+    if maker == "box":
+        P = copy_arrays(c.arrays)
+        oracle_mod.set_poison(True)
+        try:
+            oracle_mod.stage(P, c.g_node, c.sd_node, c.params, 0, c.dt)
+        finally:
+            oracle_mod.set_poison(False)
+    for j in range(stages):
+        L = oracle_mod.stage(a, c.g_node, c.sd_node, c.params, j, c.dt, want_L=True)
+        for k in ("F", "E", "G", "Fv", "Ev", "Gv", ("U1", "U2", "U0")[j], "flow", "L"):
+            want = L if k == "L" else a[k]
+            r = own
+            if maker == "box" and k != "L":
+                r = own[np.isfinite(P[k][own]).all(axis=1)]
+            elif maker == "box":
+                r = own[np.isfinite(P["U1"][own]).all(axis=1)]
+            err = rel_l2(res[j][k][r], want[r])
+            assert err <= TOL, f"{maker} stage {j} {k}: {err:.3e}"
+
+
+def test_bad_neighbour_index_is_rejected(ctx):
+    from cfd_gb300 import abi, cases
+    c = cases.isentropic_vortex(n=6)
+    a = copy_arrays(c.arrays)
+    a["grid"]["N1"][5] = c.g_node + 7       # outside [0, n_rows)
+    dev = ctx.upload_case(a)
+    with pytest.raises(abi.CfdError) as e:
+        ctx.uq(dev["U0"], dev["Q"], dev["grid"], dev["det"], dev["flow"], dev["roe"], c.g_node + 1)
+    assert e.value.status == abi.EINVAL
+    with pytest.raises(abi.CfdError) as e:
+        ctx.stage(dev, c.g_node, c.sd_node, c.params, 0, c.dt)
+    assert e.value.status == abi.EINVAL
+    # the context stays usable after the rejected launch
+    b = copy_arrays(c.arrays)
+    ctx.write(dev["grid"], b["grid"])
+    ctx.stage(dev, c.g_node, c.sd_node, c.params, 0, c.dt)
+    for p in dev.values():
+        ctx.free(p)
+
+
+def test_nonfinite_state_is_reported(ctx):
+    from cfd_gb300 import abi, cases
+    c = cases.isentropic_vortex(n=8)
+    a = copy_arrays(c.arrays)
+    a["flow"][17, 5] = np.nan                # density of one node
+    dev = ctx.upload_case(a)
+    with pytest.raises(abi.CfdError) as e:
+        ctx.stage(dev, c.g_node, c.sd_node, c.params, 0, c.dt)
+    assert e.value.status == abi.ENONFINITE
+    for p in dev.values():
+        ctx.free(p)
+
+
+def test_argument_validation(ctx):
+    from cfd_gb300 import abi, cases
+    c = cases.isentropic_vortex(n=6)
+    dev = ctx.upload_case(c.arrays)
+    with pytest.raises(abi.CfdError) as e:       # more items than rows
+        ctx.uq(dev["U0"], dev["Q"], dev["grid"], dev["det"], dev["flow"], dev["roe"], c.g_node + 2)
+    assert e.value.status == abi.EINVAL
+    host = np.zeros((c.g_node + 1, 5))
+    with pytest.raises(abi.CfdError) as e:       # host pointer where a device buffer is required
+        ctx.uq(host.ctypes.data, dev["Q"], dev["grid"], dev["det"], dev["flow"], dev["roe"], c.g_node + 1)
+    assert e.value.status == abi.EINVAL
+    with pytest.raises(abi.CfdError) as e:
+        ctx.weno(3, 1.5, 0.01, dev["deter"], dev["det"], dev["U0"], dev["U1"], dev["U2"], dev["grid"], dev["Q"],
+                 dev["metric"], dev["roe"], dev["Fv"], dev["Ev"], dev["Gv"], dev["F"], dev["E"], dev["G"],
+                 dev["flow"], c.sd_node + 1)
+    assert e.value.status == abi.EINVAL
+    for p in dev.values():
+        ctx.free(p)
