@@ -31,6 +31,11 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libcfd_gb300.so")
 
 
+# Translation units whose FP64 arithmetic must follow the reference's
+# evaluation order: no contraction of a*b+c into FMA.
+EXACT_FP64 = {"dropin.cu", "structured.cu"}
+
+
 def sources() -> list[pathlib.Path]:
     return sorted(CSRC.glob("*.cu"))
 
@@ -52,7 +57,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
 
     def compile_one(src: pathlib.Path):
         obj = OBJ_DIR / (src.stem + ".o")
-        cmd = [cc, *ARCH, *NVCC_FLAGS, *extra, "-c", str(src), "-o", str(obj)]
+        fmad = ["--fmad=false"] if src.name in EXACT_FP64 else []
+        cmd = [cc, *ARCH, *NVCC_FLAGS, *fmad, *extra, "-c", str(src), "-o", str(obj)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         return src, obj, r
 

@@ -7,7 +7,12 @@
 // packed types, which would force byte-wise loads.  Neighbour chains are
 // bounds-checked: a row whose stencil leaves [0, n_rows) is skipped and the
 // context's error word gets CFD_FLAG_BAD_INDEX.
+//
+// Arithmetic: the exact FP64 layer (physics_exact.cuh); this file is
+// compiled with --fmad=false so that results follow the reference's
+// evaluation order.
 #include "internal.h"
+#include "physics_exact.cuh"
 
 namespace cfd {
 
@@ -64,7 +69,7 @@ __global__ void __launch_bounds__(128) k_uq(double *__restrict__ U, double *__re
     const double *fi = flow + 9 * (size_t)gid;
     const double rho = fi[FRHO], u = fi[FU], v = fi[FV], w = fi[FW], p = fi[FP];
     const double si = sqrt(rho);
-    const double hi = total_enthalpy(rho, u, v, w, p);
+    const double hi = ex::enthalpy(rho, u, v, w, p);
     // ROE block order ip, jp, kp, im, jm, km; neighbour slots N1, N0, N4, N3, N2, N5
     const int slot_of_block[6] = {1, 0, 4, 3, 2, 5};
     double *r = roe + 36 * (size_t)gid;
@@ -74,7 +79,7 @@ __global__ void __launch_bounds__(128) k_uq(double *__restrict__ U, double *__re
         const double rb = fn[FRHO], ub = fn[FU], vb = fn[FV], wb = fn[FW], pb = fn[FP];
         const double sb = sqrt(rb);
         double ra[5];
-        roe_average(sb, ub, vb, wb, total_enthalpy(rb, ub, vb, wb, pb), si, u, v, w, hi, ra);
+        ex::roe(sb, ub, vb, wb, ex::enthalpy(rb, ub, vb, wb, pb), si, u, v, w, hi, ra);
         r[6 * b + 0] = ra[0];
         r[6 * b + 1] = ra[1];
         r[6 * b + 2] = ra[2];
@@ -119,8 +124,8 @@ __global__ void __launch_bounds__(128) k_viscous(Phys P, const double *__restric
     const double *fr = flow + 9 * (size_t)gid;
     const double prim[5] = {fr[FRHO], fr[FU], fr[FV], fr[FW], fr[FP]};
     double Fn[5], En[5], Gn[5];
-    node_inviscid_flux(prim, m, D, Fn, En, Gn);
-    double Fvn[5] = {0, 0, 0, 0, 0}, Evn[5] = {0, 0, 0, 0, 0}, Gvn[5] = {0, 0, 0, 0, 0};
+    ex::node_flux(prim, m, D, Fn, En, Gn);
+    double Fvn[5], Evn[5], Gvn[5];
     double mu;
     {
         double dU[3][5];
@@ -140,15 +145,15 @@ __global__ void __launch_bounds__(128) k_viscous(Phys P, const double *__restric
         double Ui[5];
 #pragma unroll
         for (int c = 0; c < 5; ++c) Ui[c] = U[5 * (size_t)gid + c];
-        // MTS test-filter velocity differences (Viscous.cl:493-495)
-        double KS[3];
+        double KS[3];   // MTS test filter (Viscous.cl:493-495)
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             const int c = d + 1;
             const double *um = U + 5 * (size_t)idx[d][2], *up = U + 5 * (size_t)idx[d][4];
-            KS[d] = sqr((Ui[c] / Ui[0]) - ((0.25 * um[c] + 0.5 * Ui[c] + 0.25 * up[c]) / (0.25 * um[0] + 0.5 * Ui[0] + 0.25 * up[0])));
+            KS[d] = ex::ks(Ui[c], Ui[0], um[c], um[0], up[c], up[0]);
         }
-        viscous_node_flux(dU, Ui, m, D, prim, KS, P, Fvn, Evn, Gvn, mu);
+        const ex::Visc V{P.mach, P.reynolds, P.prandtl, P.t_inf, P.les};
+        ex::viscous_node(dU, Ui, m, D, prim, KS, V, Fvn, Evn, Gvn, mu);
     }
     double *o;
 #pragma unroll
@@ -184,8 +189,7 @@ __global__ void __launch_bounds__(128) k_weno(Phys P, int j, double mach, double
         atomicOr(flags, CFD_FLAG_BAD_INDEX);
         return;
     }
-    double L[5] = {0, 0, 0, 0, 0};
-    double Ldiss[5] = {0, 0, 0, 0, 0};
+    double dflux[3][5], dvis[3][5];
 #pragma unroll 1
     for (int d = 0; d < 3; ++d) {
         const double *NF = d == 0 ? F : (d == 1 ? E : G);
@@ -204,12 +208,13 @@ __global__ void __launch_bounds__(128) k_weno(Phys P, int j, double mach, double
             for (int k = 0; k < 6; ++k)
 #pragma unroll
                 for (int c = 0; c < 5; ++c) pts[k][c] = Q[5 * (size_t)idx[d][base + k] + c];
-            llf_face_flux(pts, fm[0], fm[1], fm[2], det_f, rstate, P.eps, Fh[s]);
+            double Fhat[5];
+            ex::face_flux(pts, fm[0], fm[1], fm[2], det_f, rstate, P.eps, Fhat);
 #pragma unroll
             for (int c = 0; c < 5; ++c) {
 #pragma unroll
                 for (int k = 0; k < 6; ++k) nfv[k] = NF[5 * (size_t)idx[d][base + k] + c];
-                Fh[s][c] += face_correction(nfv);
+                Fh[s][c] = ex::corrected(Fhat[c], nfv);
             }
         }
         int Lc[7];
@@ -217,48 +222,31 @@ __global__ void __launch_bounds__(128) k_weno(Phys P, int j, double mach, double
         for (int o = 0; o < 7; ++o) Lc[o] = grid_loc(grid, idx[d][o]);
 #pragma unroll
         for (int c = 0; c < 5; ++c) {
-            L[c] += Fh[0][c] - Fh[1][c];
+            dflux[d][c] = Fh[0][c] - Fh[1][c];
             double f[7];
 #pragma unroll
             for (int o = 0; o < 7; ++o) f[o] = VF[5 * (size_t)idx[d][o] + c];
-            Ldiss[c] += weno_visc_deriv_ref(f, Lc);
+            dvis[d][c] = weno_visc_deriv_ref(f, Lc);
         }
     }
+    double L[5];
 #pragma unroll
-    for (int c = 0; c < 5; ++c) L[c] = -(L[c] + Ldiss[c]);
+    for (int c = 0; c < 5; ++c)
+        L[c] = (-1.0) * (dflux[0][c] + dflux[1][c] + dflux[2][c] + dvis[0][c] + dvis[1][c] + dvis[2][c]);
     if (L_out) {
 #pragma unroll
         for (int c = 0; c < 5; ++c) L_out[5 * (size_t)gid + c] = L[c];
     }
-    // SSP-RK3 stage (Weno.cl:3084-3126)
-    double Un[5];
+    // SSP-RK3 stage and primitive recovery (Weno.cl:3084-3135)
     const size_t r5 = 5 * (size_t)gid;
-    if (j == 0) {
+    double u0[5], u1[5], u2[5], Un[5];
 #pragma unroll
-        for (int c = 0; c < 5; ++c) { Un[c] = U0[r5 + c] + dt * L[c]; U1[r5 + c] = Un[c]; }
-    } else if (j == 1) {
+    for (int c = 0; c < 5; ++c) { u0[c] = U0[r5 + c]; u1[c] = U1[r5 + c]; u2[c] = U2[r5 + c]; }
+    double rho, u, v, w, e, p, t, a;
+    ex::rk_and_primitives(j, dt, mach, det[gid], u0, u1, u2, L, Un, rho, u, v, w, e, p, t, a);
+    double *Uo = j == 0 ? U1 : (j == 1 ? U2 : U0);
 #pragma unroll
-        for (int c = 0; c < 5; ++c) {
-            Un[c] = (3.0 / 4.0) * U0[r5 + c] + (1.0 / 4.0) * U1[r5 + c] + 0.25 * dt * L[c];
-            U2[r5 + c] = Un[c];
-        }
-    } else {
-#pragma unroll
-        for (int c = 0; c < 5; ++c) {
-            Un[c] = (U0[r5 + c] / 3.0) + ((2.0 / 3.0) * U2[r5 + c]) + (2.0 / 3.0) * (dt * L[c]);
-            U0[r5 + c] = Un[c];
-        }
-    }
-    // primitive recovery (Weno.cl:3128-3135)
-    const double idet = 1.0 / det[gid];
-    double fu[5];
-#pragma unroll
-    for (int c = 0; c < 5; ++c) fu[c] = idet * Un[c];
-    const double rho = fu[0];
-    const double ir = 1.0 / rho;
-    const double u = fu[1] * ir, v = fu[2] * ir, w = fu[3] * ir;
-    const double e = (fu[4] * ir) - 0.5 * (u * u + v * v + w * w);
-    const double p = e * rho * 0.4;
+    for (int c = 0; c < 5; ++c) Uo[r5 + c] = Un[c];
     double *fo = flow + 9 * (size_t)gid;
     fo[FRHO] = rho;
     fo[FU] = u;
@@ -266,8 +254,8 @@ __global__ void __launch_bounds__(128) k_weno(Phys P, int j, double mach, double
     fo[FW] = w;
     fo[FE] = e;
     fo[FP] = p;
-    fo[FT] = (1.4 * mach * mach) * (p * ir);
-    fo[FA] = sqrt(1.4 * p * ir);
+    fo[FT] = t;
+    fo[FA] = a;
     if (gid > 0 && !(isfinite(rho) && isfinite(u) && isfinite(v) && isfinite(w) && isfinite(p)))
         atomicOr(flags, CFD_FLAG_NONFINITE);
 }

@@ -17,7 +17,13 @@
 //   k_update  pointwise + radius-2: L = -(flux differences + viscous
 //             divergence), SSP-RK3 stage j, primitive recovery
 // Layout: every field is [component][N] with n = i + ni*(j + nj*k).
+//
+// The FP64 kernels use the exact arithmetic layer (physics_exact.cuh) and
+// this file is compiled with --fmad=false: the face flux of face i+1/2 is
+// bit-identical to what the reference computes for it (twice).  The FP32
+// face kernel of the mixed-precision form lives in mixed.cu.
 #include "internal.h"
+#include "physics_exact.cuh"
 #include "structured.h"
 
 namespace cfd {
@@ -80,7 +86,7 @@ __global__ void __launch_bounds__(128) k_prep(Lat g, const double *__restrict__ 
     for (int k = 0; k < 9; ++k) m[k] = m9[k * N + n];
     const double prim[5] = {rho, u, v, w, p};
     double F[5], Ec[5], G[5];
-    node_inviscid_flux(prim, m, D, F, Ec, G);
+    ex::node_flux(prim, m, D, F, Ec, G);
 #pragma unroll
     for (int c = 0; c < 5; ++c) {
         FEG[(0 * 5 + c) * N + n] = F[c];
@@ -88,7 +94,7 @@ __global__ void __launch_bounds__(128) k_prep(Lat g, const double *__restrict__ 
         FEG[(2 * 5 + c) * N + n] = G[c];
     }
     sh[n] = sqrt(rho);
-    sh[N + n] = total_enthalpy(rho, u, v, w, p);
+    sh[N + n] = ex::enthalpy(rho, u, v, w, p);
 }
 
 // ------------------------------------------------------------- viscous --
@@ -111,10 +117,9 @@ __global__ void __launch_bounds__(128) k_visc(Lat g, Phys P, const double *__res
                         p2 = g.step(i, j, k, d, 2);
 #pragma unroll
         for (int c = 0; c < 5; ++c)
-            dU[d][c] = (1.0 / 12.0) * (8.0 * (Uj[c * N + p1] - Uj[c * N + m1]) - (Uj[c * N + p2] - Uj[c * N + m2]));
+            dU[d][c] = ex::central4(Uj[c * N + m2], Uj[c * N + m1], Uj[c * N + p1], Uj[c * N + p2]);
         const int c = d + 1;
-        KS[d] = sqr((Ui[c] / Ui[0]) - ((0.25 * Uj[c * N + m1] + 0.5 * Ui[c] + 0.25 * Uj[c * N + p1])
-                                       / (0.25 * Uj[m1] + 0.5 * Ui[0] + 0.25 * Uj[p1])));
+        KS[d] = ex::ks(Ui[c], Ui[0], Uj[c * N + m1], Uj[m1], Uj[c * N + p1], Uj[p1]);
     }
     double m[9];
 #pragma unroll
@@ -122,7 +127,8 @@ __global__ void __launch_bounds__(128) k_visc(Lat g, Phys P, const double *__res
     const double prim[5] = {prim9[FRHO * N + n], prim9[FU * N + n], prim9[FV * N + n], prim9[FW * N + n],
                             prim9[FP * N + n]};
     double Fv[5], Ev[5], Gv[5], mu;
-    viscous_node_flux(dU, Ui, m, det[n], prim, KS, P, Fv, Ev, Gv, mu);
+    const ex::Visc Vp{P.mach, P.reynolds, P.prandtl, P.t_inf, P.les};
+    ex::viscous_node(dU, Ui, m, det[n], prim, KS, Vp, Fv, Ev, Gv, mu);
 #pragma unroll
     for (int c = 0; c < 5; ++c) {
         V[(0 * 5 + c) * N + n] = Fv[c];
@@ -138,21 +144,15 @@ __global__ void __launch_bounds__(128) k_mu_only(Lat g, Phys P, const double *__
     const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= g.N) return;
     const long long N = g.N;
-    const double U0 = Uj[n], U1 = Uj[N + n], U2 = Uj[2 * N + n], U3 = Uj[3 * N + n], U4 = Uj[4 * N + n];
-    const double iU0 = 1.0 / U0;
-    const double uu = U1 * iU0, vv = U2 * iU0, ww = U3 * iU0;
-    const double d_temp = (1.4 * P.mach * P.mach * 0.4 * ((U4 * iU0) - 0.5 * (uu * uu + vv * vv + ww * ww)));
-    const double sd = sqrt(d_temp);
-    const double S = 110.4 / P.t_inf;
-    prim9[FMU * N + n] = (sd * sd * sd) * ((1.0 + S) / (d_temp + S));
+    const double Ui[5] = {Uj[n], Uj[N + n], Uj[2 * N + n], Uj[3 * N + n], Uj[4 * N + n]};
+    prim9[FMU * N + n] = ex::mu_of(Ui, P.mach, P.t_inf);
 }
 
 // ---------------------------------------------------------------- faces --
-// One thread per face n+1/2 along D.  T: arithmetic type of the
-// characteristic/WENO/LLF part (double, or float in the mixed form); the
-// inputs, the face metric/det product and the correction stay FP64.
-template <int D, class T>
-__global__ void __launch_bounds__(128) k_face(Lat g, T eps, const double *__restrict__ Q,
+// One thread per face n+1/2 along D (FP64, exact arithmetic): Roe average of
+// the two adjacent nodes, LLF face flux and the 6th-order correction.
+template <int D>
+__global__ void __launch_bounds__(128) k_face(Lat g, double eps, const double *__restrict__ Q,
                                               const double *__restrict__ prim9, const double *__restrict__ sh,
                                               const double *__restrict__ fm, const double *__restrict__ fdet,
                                               const double *__restrict__ FEG, double *__restrict__ Fh)
@@ -165,30 +165,27 @@ __global__ void __launch_bounds__(128) k_face(Lat g, T eps, const double *__rest
     long long s[6];
 #pragma unroll
     for (int o = 0; o < 6; ++o) s[o] = g.step(i, j, k, D, o - 2);
-    T pts[6][5];
+    double pts[6][5];
 #pragma unroll
     for (int o = 0; o < 6; ++o)
 #pragma unroll
-        for (int c = 0; c < 5; ++c) pts[o][c] = (T)Q[c * N + s[o]];
-    // Roe average of the face: neighbour (right, s[3]) and node (left, s[2])
-    T roe[5];
+        for (int c = 0; c < 5; ++c) pts[o][c] = Q[c * N + s[o]];
+    double roe[5];
     {
-        const long long l = s[2], r = s[3];
-        roe_average<T>((T)sh[r], (T)prim9[FU * N + r], (T)prim9[FV * N + r], (T)prim9[FW * N + r], (T)sh[N + r],
-                       (T)sh[l], (T)prim9[FU * N + l], (T)prim9[FV * N + l], (T)prim9[FW * N + l], (T)sh[N + l],
-                       roe);
+        const long long l = s[2], r = s[3];   // node (left) and its +D neighbour
+        ex::roe(sh[r], prim9[FU * N + r], prim9[FV * N + r], prim9[FW * N + r], sh[N + r], sh[l], prim9[FU * N + l],
+                prim9[FV * N + l], prim9[FW * N + l], sh[N + l], roe);
     }
-    const T mx = (T)fm[(D * 3 + 0) * N + n], my = (T)fm[(D * 3 + 1) * N + n], mz = (T)fm[(D * 3 + 2) * N + n];
-    const T df = (T)fdet[D * N + n];
-    T Fhat[5];
-    llf_face_flux<T>(pts, mx, my, mz, df, roe, eps, Fhat);
+    double Fhat[5];
+    ex::face_flux(pts, fm[(D * 3 + 0) * N + n], fm[(D * 3 + 1) * N + n], fm[(D * 3 + 2) * N + n], fdet[D * N + n], roe,
+                  eps, Fhat);
     const double *NF = FEG + (size_t)D * 5 * N;
 #pragma unroll
     for (int c = 0; c < 5; ++c) {
         double f[6];
 #pragma unroll
         for (int o = 0; o < 6; ++o) f[o] = NF[c * N + s[o]];
-        Fh[(D * 5 + c) * N + n] = (double)Fhat[c] + face_correction(f);
+        Fh[(D * 5 + c) * N + n] = ex::corrected(Fhat[c], f);
     }
 }
 
@@ -204,57 +201,46 @@ __global__ void __launch_bounds__(128) k_update(Lat g, int viscous, int jst, dou
     const long long N = g.N;
     int i, j, k;
     g.ijk(n, i, j, k);
-    double L[5] = {0, 0, 0, 0, 0}, Lv[5] = {0, 0, 0, 0, 0};
+    double dflux[3][5], dvis[3][5];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const long long m1 = g.step(i, j, k, d, -1);
 #pragma unroll
-        for (int c = 0; c < 5; ++c) L[c] += Fh[(d * 5 + c) * N + n] - Fh[(d * 5 + c) * N + m1];
+        for (int c = 0; c < 5; ++c) dflux[d][c] = Fh[(d * 5 + c) * N + n] - Fh[(d * 5 + c) * N + m1];
         if (viscous) {
             const long long m2 = g.step(i, j, k, d, -2), p1 = g.step(i, j, k, d, 1), p2 = g.step(i, j, k, d, 2);
             const double *Vd = V + (size_t)d * 5 * N;
 #pragma unroll
-            for (int c = 0; c < 5; ++c)
-                Lv[c] += (1.0 / 12.0) * (8.0 * (Vd[c * N + p1] - Vd[c * N + m1]) - (Vd[c * N + p2] - Vd[c * N + m2]));
+            for (int c = 0; c < 5; ++c) dvis[d][c] = ex::central4(Vd[c * N + m2], Vd[c * N + m1], Vd[c * N + p1], Vd[c * N + p2]);
+        } else {
+#pragma unroll
+            for (int c = 0; c < 5; ++c) dvis[d][c] = 0.0;
         }
     }
+    double L[5];
 #pragma unroll
-    for (int c = 0; c < 5; ++c) L[c] = -(L[c] + Lv[c]);
+    for (int c = 0; c < 5; ++c)
+        L[c] = (-1.0) * (dflux[0][c] + dflux[1][c] + dflux[2][c] + dvis[0][c] + dvis[1][c] + dvis[2][c]);
     if (Lout) {
 #pragma unroll
         for (int c = 0; c < 5; ++c) Lout[c * N + n] = L[c];
     }
-    double Un[5];
-    if (jst == 0) {
+    double u0[5], u1[5], u2[5], Un[5];
 #pragma unroll
-        for (int c = 0; c < 5; ++c) { Un[c] = U0[c * N + n] + dt * L[c]; U1[c * N + n] = Un[c]; }
-    } else if (jst == 1) {
+    for (int c = 0; c < 5; ++c) { u0[c] = U0[c * N + n]; u1[c] = U1[c * N + n]; u2[c] = U2[c * N + n]; }
+    double rho, u, v, w, e, p, t, a;
+    ex::rk_and_primitives(jst, dt, mach, det[n], u0, u1, u2, L, Un, rho, u, v, w, e, p, t, a);
+    double *Uo = jst == 0 ? U1 : (jst == 1 ? U2 : U0);
 #pragma unroll
-        for (int c = 0; c < 5; ++c) {
-            Un[c] = (3.0 / 4.0) * U0[c * N + n] + (1.0 / 4.0) * U1[c * N + n] + 0.25 * dt * L[c];
-            U2[c * N + n] = Un[c];
-        }
-    } else {
-#pragma unroll
-        for (int c = 0; c < 5; ++c) {
-            Un[c] = (U0[c * N + n] / 3.0) + ((2.0 / 3.0) * U2[c * N + n]) + (2.0 / 3.0) * (dt * L[c]);
-            U0[c * N + n] = Un[c];
-        }
-    }
-    const double idet = 1.0 / det[n];
-    const double rho = idet * Un[0];
-    const double ir = 1.0 / rho;
-    const double u = (idet * Un[1]) * ir, v = (idet * Un[2]) * ir, w = (idet * Un[3]) * ir;
-    const double e = ((idet * Un[4]) * ir) - 0.5 * (u * u + v * v + w * w);
-    const double p = e * rho * 0.4;
+    for (int c = 0; c < 5; ++c) Uo[c * N + n] = Un[c];
     prim9[FRHO * N + n] = rho;
     prim9[FU * N + n] = u;
     prim9[FV * N + n] = v;
     prim9[FW * N + n] = w;
     prim9[FE * N + n] = e;
     prim9[FP * N + n] = p;
-    prim9[FT * N + n] = (1.4 * mach * mach) * (p * ir);
-    prim9[FA * N + n] = sqrt(1.4 * p * ir);
+    prim9[FT * N + n] = t;
+    prim9[FA * N + n] = a;
     if (!(isfinite(rho) && isfinite(u) && isfinite(v) && isfinite(w) && isfinite(p))) atomicOr(flags, CFD_FLAG_NONFINITE);
 }
 
@@ -293,14 +279,11 @@ void structured_stage(const StructuredLaunch &S, int jst, double dt, double *Lou
     else
         k_mu_only<<<nb, 128, 0, st>>>(g, S.P, Uj, S.prim9);
     if (S.mixed) {
-        const float e = (float)S.P.eps;
-        k_face<0, float><<<nb, 128, 0, st>>>(g, e, S.Q, S.prim9, S.sh, S.fm, S.fdet, S.FEG, S.Fh);
-        k_face<1, float><<<nb, 128, 0, st>>>(g, e, S.Q, S.prim9, S.sh, S.fm, S.fdet, S.FEG, S.Fh);
-        k_face<2, float><<<nb, 128, 0, st>>>(g, e, S.Q, S.prim9, S.sh, S.fm, S.fdet, S.FEG, S.Fh);
+        launch_faces_mixed(S);
     } else {
-        k_face<0, double><<<nb, 128, 0, st>>>(g, S.P.eps, S.Q, S.prim9, S.sh, S.fm, S.fdet, S.FEG, S.Fh);
-        k_face<1, double><<<nb, 128, 0, st>>>(g, S.P.eps, S.Q, S.prim9, S.sh, S.fm, S.fdet, S.FEG, S.Fh);
-        k_face<2, double><<<nb, 128, 0, st>>>(g, S.P.eps, S.Q, S.prim9, S.sh, S.fm, S.fdet, S.FEG, S.Fh);
+        k_face<0><<<nb, 128, 0, st>>>(g, S.P.eps, S.Q, S.prim9, S.sh, S.fm, S.fdet, S.FEG, S.Fh);
+        k_face<1><<<nb, 128, 0, st>>>(g, S.P.eps, S.Q, S.prim9, S.sh, S.fm, S.fdet, S.FEG, S.Fh);
+        k_face<2><<<nb, 128, 0, st>>>(g, S.P.eps, S.Q, S.prim9, S.sh, S.fm, S.fdet, S.FEG, S.Fh);
     }
     k_update<<<nb, 128, 0, st>>>(g, S.P.viscous, jst, S.P.mach, dt, S.det, S.Fh, S.V, S.U[0], S.U[1], S.U[2], S.prim9,
                                  S.flags, Lout);

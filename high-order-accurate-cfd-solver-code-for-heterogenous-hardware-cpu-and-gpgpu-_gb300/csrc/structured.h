@@ -27,6 +27,9 @@ struct StructuredLaunch {
     unsigned *flags;
 };
 
+// The three face-flux launches of the mixed-precision form (mixed.cu).
+void launch_faces_mixed(const StructuredLaunch &S);
+
 // One RK stage j of the host loop; Lout (device [5][N]) may be null.
 void structured_stage(const StructuredLaunch &S, int j, double dt, double *Lout);
 int structured_launches_per_stage();
