@@ -1,0 +1,387 @@
+"""Benchmark of the RHS path: cell-updates/s (nodes x full SSP-RK3 steps / s).
+
+Workload (default): Taylor-Green vortex on a 128^3 periodic grid with
+sinusoidally perturbed node positions (curvilinear metrics), Re 1600,
+Mach 0.1, Pr 0.72, reference mixed-time-scale LES, synthetic inputs generated
+in-process.  One "step" = one full SSP-RK3 step (three stages of U_Q ->
+Viscous -> Weno) over the whole grid.
+
+Arms:
+  --impl gb300      (default) the CUDA library.  ``value``: FP64 form, state
+                    resident in HBM, CUDA events on the launching stream;
+                    ``e2e``: the same through the public solver API with the
+                    FLOW buffer copied from / to pinned host memory every
+                    step; ``mixed``: the mixed-precision form, with its
+                    relative L2 error against the FP64 form on the same run.
+  --impl reference  the reference algorithm on the host cores (the CPU
+                    restatement in oracle/, all threads), same workload.
+
+Multi-GPU: the path does not exchange data between instances; N ranks run
+N independent replicas (weak scaling), timed between barriers, max over
+ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import __graft_entry__  # noqa: E402
+
+METRIC = "cell-updates/s FP64 vs mixed at <=1e-6 rel L2 vs FP64; p50/p99 solve latency"
+UNIT = "cell-updates/s"
+
+# Algorithmic (compulsory) bytes of an ideal fused face-based FP64 SSP-RK3
+# step per cell: 5 state reads + 3 state writes of 40 B, plus 22 doubles of
+# geometry per stage (node metrics 9, det 1, three face metrics 3x3, three
+# face dets 3), x3 stages.
+ALGO_BYTES_PER_CELL_UPDATE = 5 * 40 + 3 * 40 + 3 * 22 * 8          # 848
+# Per-launch compulsory bytes per node of each structured kernel (every
+# input and output element once): see the design doc, kernel table.
+KERNEL_BYTES_PER_NODE = {
+    "prep": (5 + 9 + 1 + 5 + 5 + 15 + 2) * 8,          # prims, metrics, det -> Q, U_j, F/E/G, sqrt(rho), H
+    "viscous": (5 + 9 + 1 + 4 + 15 + 1) * 8,           # U_j, metrics, det, prims -> Fv/Ev/Gv, mu
+    "mu_only": (5 + 1) * 8,
+    "face_i": (5 + 3 + 2 + 3 + 1 + 5 + 5) * 8,         # Q, u/v/w, sqrt(rho)/H, face metric, face det, F -> Fh
+    "face_j": (5 + 3 + 2 + 3 + 1 + 5 + 5) * 8,
+    "face_k": (5 + 3 + 2 + 3 + 1 + 5 + 5) * 8,
+    "update": (15 + 15 + 10 + 1 + 5 + 8) * 8,          # Fh, Fv/Ev/Gv, two U, det -> U, 8 FLOW fields
+}
+# FP64 operations per launch-unit of the structured FP64 kernels, counted by
+# ncu (sm__sass_thread_inst_executed_op_d{fma,mul,add}_pred_on.sum, FMA = 2)
+# on the 64^3 Taylor-Green case; profiles/structured_fp64_tgv.md.
+FP64_FLOP_PER_NODE = {}
+
+
+def parse_args(argv=None):
+    p = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
+    p.add_argument("--config", choices=("tgv128", "tgv64", "vortex64"), default="tgv128")
+    p.add_argument("--cpu-steps", type=int, default=1, help="full steps timed for the CPU baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-mixed", action="store_true")
+    return p.parse_args(argv)
+
+
+def make_case(config: str):
+    from cfd_gb300 import cases
+    if config in ("tgv128", "tgv64"):
+        n = 128 if config == "tgv128" else 64
+        return cases.taylor_green(n=n), {"workload": f"taylor_green_{n}^3_curvilinear_les", "grid": [n, n, n],
+                                         "re": 1600, "mach": 0.1, "les": "mts"}
+    return cases.isentropic_vortex(n=64), {"workload": "isentropic_vortex_64^3_periodic_inviscid",
+                                           "grid": [64, 64, 64]}
+
+
+# ------------------------------------------------------------ distributed --
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def dist_init(world: int, backend: str):
+    if world > 1:
+        import torch.distributed as dist
+        if not dist.is_initialized():
+            dist.init_process_group(backend=backend)
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def aggregate(seconds: float, units: float, world: int, device=None):
+    """Whole-job throughput: units summed over ranks / max time over ranks."""
+    if world == 1:
+        return units / seconds, seconds
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    u = torch.tensor([units], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(u.item()) / float(t.item()), float(t.item())
+
+
+# ----------------------------------------------------------------- clocks --
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock, power and throttle reasons while the
+    timed region runs."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                                          "-lms", "100", "-i", str(self.device)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+        return False
+
+    def summary(self):
+        if not getattr(self, "lines", None):
+            return None
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------- CPU legs ---
+
+def cpu_oracle_rate(case, nsteps: int, threads: int | None = None):
+    """Times the CPU restatement of the reference algorithm (oracle/) on the
+    host cores: nsteps full SSP-RK3 steps of the whole case."""
+    import oracle
+    oracle.build()
+    if threads:
+        oracle.set_threads(threads)
+    cores = oracle.lib().oracle_get_threads()
+    a = {k: v.copy() for k, v in case.arrays.items()}
+    t0 = time.perf_counter()
+    oracle.rk3_steps(a, case.g_node, case.sd_node, case.params, case.dt, nsteps)
+    dt = time.perf_counter() - t0
+    return case.sd_node * nsteps / dt, cores, dt
+
+
+def reference_arm(args):
+    world, rank, local = dist_env()
+    if rank != 0:
+        return 0
+    case, cfg = make_case(args.config)
+    import oracle
+    oracle.build()
+    cores = oracle.lib().oracle_get_threads()
+    a = {k: v.copy() for k, v in case.arrays.items()}
+    for _ in range(args.warmup):
+        oracle.rk3_steps(a, case.g_node, case.sd_node, case.params, case.dt, 1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.rk3_steps(a, case.g_node, case.sd_node, case.params, case.dt, 1)
+    secs = time.perf_counter() - t0
+    value = case.sd_node * args.steps / secs
+    cfg = dict(cfg, parallelism="host cores (OpenMP)", l2="n/a (CPU)")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": cfg,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} full SSP-RK3 steps of the whole {cfg['workload']} grid; "
+                                   "the reference's own OpenCL/MPI build cannot run on this host (no OpenCL ICD, "
+                                   "no MPI), so its kernel arithmetic runs through the bit-exact C restatement"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------- GPU arm ----
+
+def gpu_arm(args):
+    import numpy as np
+    import torch
+
+    world, rank, local = dist_env()
+    dist_init(world, "nccl")
+    torch.cuda.set_device(local)
+    __graft_entry__.load_package()
+    from cfd_gb300 import abi, runtime
+
+    case, cfg = make_case(args.config)
+    N = case.sd_node
+    ctx = runtime.Context(local)
+    stream = torch.cuda.Stream(device=local)
+    ctx.set_stream(stream.cuda_stream)
+
+    def time_resident(precision: int, steps: int, warmup: int):
+        s = runtime.Solver(ctx, case, precision=precision)
+        assert s.info().path == "structured"
+        s.set_flow(case.arrays["flow"])
+        s.step(case.dt, warmup)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier(world)
+        torch.cuda.synchronize()
+        launches0 = ctx.launch_count
+        with ClockSampler(local) as clk:
+            with torch.cuda.stream(stream):
+                e0.record(stream)
+            s.step(case.dt, steps)
+            with torch.cuda.stream(stream):
+                e1.record(stream)
+            torch.cuda.synchronize()
+        barrier(world)
+        secs = e0.elapsed_time(e1) / 1e3
+        return s, secs, ctx.launch_count - launches0, clk.summary()
+
+    # --- FP64 form, resident ---
+    s64, secs64, launches64, clocks = time_resident(0, args.steps, args.warmup)
+    value, tmax = aggregate(secs64, N * args.steps, world, device=f"cuda:{local}")
+    prof = [s64.profile_stage(j, case.dt) for j in range(3)]   # advances 1 step (3 stages) after timing
+    u64 = s64.get_u0()
+
+    # --- mixed form, resident, same number of steps from the same state ---
+    mixed = None
+    if not args.no_mixed:
+        sm, secsm, launchesm, clocks_m = time_resident(1, args.steps, args.warmup)
+        vm, _ = aggregate(secsm, N * args.steps, world, device=f"cuda:{local}")
+        prof_m = [sm.profile_stage(j, case.dt) for j in range(3)]
+        um = sm.get_u0()
+        err = float(np.linalg.norm(um[1:] - u64[1:]) / np.linalg.norm(u64[1:]))
+        mixed = {"value": vm, "unit": UNIT, "ms_per_step": 1e3 * secsm / args.steps, "speedup_vs_fp64": vm / value,
+                 "rel_l2_vs_fp64": err, "steps_compared": args.warmup + args.steps + 1,
+                 "dtype": "f32 characteristic/WENO/LLF + f64 state/RK/metrics", "gpu_launches": launchesm,
+                 "kernels_ms_per_stage": _kernel_table(prof_m)}
+        sm.close()
+
+    # --- end to end through the public API with host buffers ---
+    host_in = torch.empty((case.g_node + 1, 9), dtype=torch.float64, pin_memory=True).numpy()
+    host_out = torch.empty((case.g_node + 1, 9), dtype=torch.float64, pin_memory=True).numpy()
+    host_in[...] = case.arrays["flow"]
+    se = runtime.Solver(ctx, case)
+    for _ in range(min(args.warmup, 2)):
+        se.set_flow(host_in)
+        se.step(case.dt, 1)
+        se.get_flow(host_out)
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        se.set_flow(host_in)
+        se.step(case.dt, 1)
+        se.get_flow(host_out)
+        host_in, host_out = host_out, host_in
+    e2e_secs = time.perf_counter() - t0
+    barrier(world)
+    e2e_value, _ = aggregate(e2e_secs, N * args.steps, world, device=f"cuda:{local}")
+    se.close()
+
+    # --- roofline of the dominant kernel ---
+    table = _kernel_table(prof)
+    dom = max(table, key=lambda k: table[k])
+    peaks = load_peaks()
+    hbm_peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if hbm_peak else "fallback"
+    hbm_peak = hbm_peak or 6800.0
+    dom_bytes = KERNEL_BYTES_PER_NODE.get(dom, 0) * N
+    achieved = dom_bytes / (table[dom] * 1e-3) / 1e9
+    fp64_peak = ctx.probe_flops(True)
+    fp32_peak = ctx.probe_flops(False)
+    fp64_roof = None
+    if dom in FP64_FLOP_PER_NODE:
+        f = FP64_FLOP_PER_NODE[dom] * N / (table[dom] * 1e-3)
+        fp64_roof = {"achieved": f / 1e12, "peak": fp64_peak / 1e12, "unit": "TFLOP/s", "frac": f / fp64_peak}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * tmax / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": dict(cfg, parallelism=f"replicas x{world}" if world > 1 else "single GPU",
+                       l2="inputs larger than L2 (resident working set %.2f GB)" % (s64.info().device_bytes / 1e9),
+                       path="structured face-based, exact FP64 evaluation order"),
+        "gpu_launches": launches64,
+        "clocks": clocks,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(host_in.nbytes),
+                "d2h_bytes_per_step": int(host_out.nbytes)},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_src,
+                     "note": "FP64-pipe bound; see roofline_fp64"},
+        "roofline_fp64": fp64_roof,
+        "step_algorithmic_gbs": ALGO_BYTES_PER_CELL_UPDATE * value / world / 1e9,
+        "peaks_probed": {"fp64_tflops": fp64_peak / 1e12, "fp32_tflops": fp32_peak / 1e12},
+        "kernels_ms_per_stage": table,
+        "mixed": mixed,
+    }
+    s64.close()
+
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        rate, cores, secs = cpu_oracle_rate(case, args.cpu_steps)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": f"{args.cpu_steps} full SSP-RK3 step(s) of the whole grid "
+                                          f"({secs:.1f} s on {cores} threads), CPU restatement of the reference "
+                                          "kernels (bit-exact against their sources on x86)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def load_peaks() -> dict:
+    """Measured peaks of this machine's GPUs (HBM copy GB/s, bf16)."""
+    try:
+        return json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except (OSError, ValueError):
+        return {}
+
+
+def _kernel_table(prof) -> dict:
+    """Mean device ms per stage of each kernel name over the three stages."""
+    acc = {}
+    for stage in prof:
+        for name, ms in stage:
+            acc.setdefault(name, []).append(ms)
+    return {k: sum(v) / len(v) for k, v in acc.items()}
+
+
+def main(argv=None):
+    args = parse_args(argv)
+    __graft_entry__.load_package()
+    if args.impl == "reference":
+        return reference_arm(args)
+    return gpu_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

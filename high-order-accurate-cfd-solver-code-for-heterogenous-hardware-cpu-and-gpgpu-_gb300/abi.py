@@ -38,6 +38,10 @@ class Geometry(C.Structure):
                 ("deter", C.c_void_p), ("metric", C.c_void_p)]
 
 
+class KernelTime(C.Structure):
+    _fields_ = [("name", C.c_char * 24), ("ms", C.c_double)]
+
+
 class SolverInfo(C.Structure):
     _fields_ = [("path", C.c_int32), ("ni", C.c_int32), ("nj", C.c_int32), ("nk", C.c_int32),
                 ("precision", C.c_int32), ("reserved", C.c_int32), ("device_bytes", C.c_uint64)]
@@ -74,6 +78,8 @@ PROTOTYPES = {
     "cfd_solver_get_u0": (C.c_int, [_vp, _vp]),
     "cfd_solver_step": (C.c_int, [_vp, _d, _i32]),
     "cfd_solver_stage": (C.c_int, [_vp, _i32, _d, _vp]),
+    "cfd_solver_profile_stage": (C.c_int, [_vp, _i32, _d, _vp, _i32, C.POINTER(_i32)]),
+    "cfd_probe_flops": (C.c_int, [_vp, _i32, C.POINTER(_d)]),
 }
 
 _lib = None

@@ -68,14 +68,17 @@ __global__ void __launch_bounds__(128) k_face_mixed(int ni, int nj, int nk, floa
 
 }  // namespace
 
-void launch_faces_mixed(const StructuredLaunch &S)
+void launch_faces_mixed(const StructuredLaunch &S, cudaEvent_t *ev)
 {
     const long long N = (long long)S.ni * S.nj * S.nk;
     const unsigned nb = blocks_for(N, 128);
     const float e = (float)S.P.eps;
     k_face_mixed<0><<<nb, 128, 0, S.stream>>>(S.ni, S.nj, S.nk, e, S.Q, S.prim9, S.sh, S.fm, S.fdet, S.FEG, S.Fh);
+    if (ev) cudaEventRecord(ev[0], S.stream);
     k_face_mixed<1><<<nb, 128, 0, S.stream>>>(S.ni, S.nj, S.nk, e, S.Q, S.prim9, S.sh, S.fm, S.fdet, S.FEG, S.Fh);
+    if (ev) cudaEventRecord(ev[1], S.stream);
     k_face_mixed<2><<<nb, 128, 0, S.stream>>>(S.ni, S.nj, S.nk, e, S.Q, S.prim9, S.sh, S.fm, S.fdet, S.FEG, S.Fh);
+    if (ev) cudaEventRecord(ev[2], S.stream);
 }
 
 }  // namespace cfd

@@ -220,6 +220,7 @@ cfd_status_t create_structured(cfd_solver *s, const cfd_geometry_t *g)
 cfd_status_t run_stage(cfd_solver *s, int j, double dt, bool want_L)
 {
     cfd_ctx *ctx = s->ctx;
+    s->S.stream = ctx->stream;   // the context's stream may have been replaced
     if (s->path == CFD_PATH_STRUCTURED) {
         structured_stage(s->S, j, dt, want_L ? s->Lsoa : nullptr);
         ctx->launches += structured_launches_per_stage();
@@ -326,6 +327,7 @@ cfd_status_t cfd_solver_set_flow(cfd_solver_t *s, const cfd_flow_t *flow_host)
         st = upload(s, s->flow, flow_host, R * sizeof(cfd_flow_t));
     } else {
         const long long N = (long long)s->ni * s->nj * s->nk;
+        s->S.stream = s->ctx->stream;
         st = upload(s, s->stage9, flow_host, R * sizeof(cfd_flow_t));
         if (st == CFD_OK) aos_to_soa(s->ctx->stream, s->stage9, 9, 9, N, s->S.prim9);
     }
@@ -393,6 +395,52 @@ cfd_status_t cfd_solver_stage(cfd_solver_t *s, int32_t j, double del_t, cfd_colu
         cudaError_t e = cudaMemcpyAsync(L_host, src, R * sizeof(cfd_column_t), cudaMemcpyDeviceToHost, s->ctx->stream);
         if (e != cudaSuccess) return cuda_fail(s->ctx, e, "cudaMemcpyAsync D2H (L)");
     }
+    return drain(s->ctx);
+}
+
+cfd_status_t cfd_solver_profile_stage(cfd_solver_t *s, int32_t j, double del_t, cfd_kernel_time_t *out,
+                                      int32_t max_out, int32_t *n_out)
+{
+    if (!s || !out || !n_out || j < 0 || j > 2 || max_out <= 0) return CFD_EINVAL;
+    cfd_status_t st = use_device(s->ctx);
+    if (st != CFD_OK) return st;
+    cudaStream_t stream = s->ctx->stream;
+    s->S.stream = stream;
+    const int nk = s->path == CFD_PATH_STRUCTURED ? structured_launches_per_stage() : 3;
+    std::vector<cudaEvent_t> ev(nk + 1);
+    for (auto &e : ev) cudaEventCreate(&e);
+    if (s->path == CFD_PATH_STRUCTURED) {
+        structured_stage(s->S, j, del_t, nullptr, ev.data());
+    } else {
+        cudaEventRecord(ev[0], stream);
+        double *Uj = s->U[j];
+        launch_uq(stream, Uj, s->Q, s->grid, s->det, s->flow, s->roe, s->g_node + 1, s->n_rows, s->ctx->d_flags);
+        cudaEventRecord(ev[1], stream);
+        launch_viscous(stream, s->P, Uj, s->F, s->E, s->G, s->Fv, s->Ev, s->Gv, s->grid, s->metric, s->det, s->flow,
+                       s->g_node + 1, s->n_rows, s->ctx->d_flags);
+        cudaEventRecord(ev[2], stream);
+        launch_weno(stream, s->P, j, s->P.mach, del_t, s->deter, s->det, s->U[0], s->U[1], s->U[2], s->grid, s->Q,
+                    s->metric, s->roe, s->Fv, s->Ev, s->Gv, s->F, s->E, s->G, s->flow, s->sd_node + 1, s->n_rows,
+                    s->ctx->d_flags, nullptr);
+        cudaEventRecord(ev[3], stream);
+    }
+    s->ctx->launches += nk;
+    cudaError_t e = cudaEventSynchronize(ev[nk]);
+    if (e == cudaSuccess) {
+        const char *gnames[3] = {"uq", "viscous", "weno"};
+        const int n = nk < max_out ? nk : max_out;
+        for (int i = 0; i < n; ++i) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, ev[i], ev[i + 1]);
+            const char *nm = s->path == CFD_PATH_STRUCTURED ? structured_kernel_name(i, s->P.viscous != 0) : gnames[i];
+            std::strncpy(out[i].name, nm, sizeof out[i].name - 1);
+            out[i].name[sizeof out[i].name - 1] = 0;
+            out[i].ms = ms;
+        }
+        *n_out = n;
+    }
+    for (auto &x : ev) cudaEventDestroy(x);
+    if (e != cudaSuccess) return cuda_fail(s->ctx, e, "profile stage");
     return drain(s->ctx);
 }
 

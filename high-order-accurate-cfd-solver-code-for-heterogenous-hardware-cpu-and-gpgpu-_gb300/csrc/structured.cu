@@ -267,26 +267,45 @@ __global__ void k_soa_to_aos(const double *__restrict__ soa, int stride, int nco
 // ------------------------------------------------------------- launchers --
 static Lat lat(const StructuredLaunch &S) { return Lat{S.ni, S.nj, S.nk, (long long)S.ni * S.nj * S.nk}; }
 
-void structured_stage(const StructuredLaunch &S, int jst, double dt, double *Lout)
+void structured_stage(const StructuredLaunch &S, int jst, double dt, double *Lout, cudaEvent_t *ev)
 {
     const Lat g = lat(S);
     const unsigned nb = blocks_for(g.N, 128);
     cudaStream_t st = S.stream;
     double *Uj = S.U[jst];
+    int e = 0;
+    auto mark = [&]() {
+        if (ev) cudaEventRecord(ev[e++], st);
+    };
+    mark();
     k_prep<<<nb, 128, 0, st>>>(g, S.m9, S.det, S.prim9, Uj, S.Q, S.FEG, S.sh);
+    mark();
     if (S.P.viscous)
         k_visc<<<nb, 128, 0, st>>>(g, S.P, S.m9, S.det, Uj, S.prim9, S.V);
     else
         k_mu_only<<<nb, 128, 0, st>>>(g, S.P, Uj, S.prim9);
+    mark();
     if (S.mixed) {
-        launch_faces_mixed(S);
+        launch_faces_mixed(S, ev ? ev + e : nullptr);
+        e += 3;
     } else {
         k_face<0><<<nb, 128, 0, st>>>(g, S.P.eps, S.Q, S.prim9, S.sh, S.fm, S.fdet, S.FEG, S.Fh);
+        mark();
         k_face<1><<<nb, 128, 0, st>>>(g, S.P.eps, S.Q, S.prim9, S.sh, S.fm, S.fdet, S.FEG, S.Fh);
+        mark();
         k_face<2><<<nb, 128, 0, st>>>(g, S.P.eps, S.Q, S.prim9, S.sh, S.fm, S.fdet, S.FEG, S.Fh);
+        mark();
     }
     k_update<<<nb, 128, 0, st>>>(g, S.P.viscous, jst, S.P.mach, dt, S.det, S.Fh, S.V, S.U[0], S.U[1], S.U[2], S.prim9,
                                  S.flags, Lout);
+    mark();
+}
+
+const char *structured_kernel_name(int i, bool viscous)
+{
+    static const char *names[6] = {"prep", "viscous", "face_i", "face_j", "face_k", "update"};
+    if (i == 1 && !viscous) return "mu_only";
+    return (i >= 0 && i < 6) ? names[i] : "?";
 }
 
 int structured_launches_per_stage() { return 6; }

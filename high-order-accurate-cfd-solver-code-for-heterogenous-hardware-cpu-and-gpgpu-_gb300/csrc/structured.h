@@ -28,10 +28,14 @@ struct StructuredLaunch {
 };
 
 // The three face-flux launches of the mixed-precision form (mixed.cu).
-void launch_faces_mixed(const StructuredLaunch &S);
+// ev (optional): three events recorded after the three launches.
+void launch_faces_mixed(const StructuredLaunch &S, cudaEvent_t *ev = nullptr);
 
 // One RK stage j of the host loop; Lout (device [5][N]) may be null.
-void structured_stage(const StructuredLaunch &S, int j, double dt, double *Lout);
+// ev (optional) receives structured_launches_per_stage()+1 recorded events
+// bracketing the launches, for per-kernel timing.
+void structured_stage(const StructuredLaunch &S, int j, double dt, double *Lout, cudaEvent_t *ev = nullptr);
+const char *structured_kernel_name(int i, bool viscous);
 int structured_launches_per_stage();
 void aos_to_soa(cudaStream_t st, const double *aos, int stride, int ncomp, long long N, double *soa);
 void soa_to_aos(cudaStream_t st, const double *soa, int stride, int ncomp, long long N, double *aos);

@@ -74,6 +74,15 @@ class Context:
         except Exception:
             pass
 
+    def set_stream(self, cuda_stream: int):
+        """Launch on a caller-owned cudaStream_t (e.g. a torch stream)."""
+        self.check(self.lib.cfd_ctx_set_stream(self.h, C.c_void_p(cuda_stream)), "cfd_ctx_set_stream")
+
+    def probe_flops(self, fp64: bool) -> float:
+        out = C.c_double()
+        self.check(self.lib.cfd_probe_flops(self.h, 1 if fp64 else 0, C.byref(out)), "cfd_probe_flops")
+        return out.value
+
     def set_rows(self, n_rows: int):
         self.check(self.lib.cfd_ctx_set_rows(self.h, int(n_rows)), "cfd_ctx_set_rows")
 
@@ -210,6 +219,14 @@ class Solver:
 
     def step(self, dt: float, nsteps: int = 1):
         self.ctx.check(self.lib.cfd_solver_step(self.h, float(dt), int(nsteps)), "cfd_solver_step")
+
+    def profile_stage(self, j: int, dt: float) -> list:
+        """One stage with per-launch device times: [(name, ms), ...]."""
+        buf = (abi.KernelTime * 16)()
+        n = C.c_int32()
+        self.ctx.check(self.lib.cfd_solver_profile_stage(self.h, int(j), float(dt), buf, 16, C.byref(n)),
+                       "cfd_solver_profile_stage")
+        return [(buf[i].name.decode(), buf[i].ms) for i in range(n.value)]
 
     def stage(self, j: int, dt: float, want_L: bool = True):
         out = np.zeros((self.g_node + 1, L.NCOL)) if want_L else None

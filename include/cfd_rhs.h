@@ -220,6 +220,21 @@ cfd_status_t cfd_solver_step(cfd_solver_t *s, double del_t, int32_t nsteps);
  * to L_host when non-NULL. */
 cfd_status_t cfd_solver_stage(cfd_solver_t *s, int32_t j, double del_t, cfd_column_t *L_host);
 
+/* One stage j of the host loop with a CUDA event around every kernel
+ * launch; out[i] receives each launch's name and device time.  The stage
+ * advances the state like cfd_solver_stage. */
+typedef struct {
+    char name[24];
+    double ms;
+} cfd_kernel_time_t;
+cfd_status_t cfd_solver_profile_stage(cfd_solver_t *s, int32_t j, double del_t, cfd_kernel_time_t *out,
+                                      int32_t max_out, int32_t *n_out);
+
+/* ------------------------------------------------------------ probes ---- */
+/* Measured FMA throughput of this device (FLOP/s, FMA = 2 FLOP): fp64 != 0
+ * for double, 0 for float.  Denominator of the FP64/FP32 rooflines. */
+cfd_status_t cfd_probe_flops(cfd_ctx_t *ctx, int32_t fp64, double *flops_per_s);
+
 #ifdef __cplusplus
 }
 #endif
