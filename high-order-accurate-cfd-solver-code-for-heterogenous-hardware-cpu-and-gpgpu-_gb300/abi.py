@@ -80,7 +80,9 @@ PROTOTYPES = {
     "cfd_solver_stage": (C.c_int, [_vp, _i32, _d, _vp]),
     "cfd_solver_profile_stage": (C.c_int, [_vp, _i32, _d, _vp, _i32, C.POINTER(_i32)]),
     "cfd_probe_flops": (C.c_int, [_vp, _i32, C.POINTER(_d)]),
+    "cfd_lattice_stage_static": (C.c_int, [_vp, _i32, _i32, _i32, _i32, _d, C.POINTER(Params)] + [_vp] * 8),
 }
+STATIC_MAX_NODES = 32768
 
 _lib = None
 

@@ -235,6 +235,29 @@ cfd_status_t cfd_solver_profile_stage(cfd_solver_t *s, int32_t j, double del_t, 
  * for double, 0 for float.  Denominator of the FP64/FP32 rooflines. */
 cfd_status_t cfd_probe_flops(cfd_ctx_t *ctx, int32_t fp64, double *flops_per_s);
 
+/* ------------------------------------------- allocation-free RK3 stage -- */
+/* No counterpart in the reference.  For callers that must not allocate
+ * device memory while they advance a solution (a host framework that owns a
+ * fixed memory pool, a real-time loop that forbids the allocation and the
+ * device synchronisation cudaMalloc/cudaFree can cause, a plugin that is
+ * only handed buffers): one SSP-RK3 stage j on a periodic ni x nj x nk
+ * lattice, the same kernels as the resident solver's structured path, with
+ * every intermediate kept in a library-owned device array sized for
+ * CFD_STATIC_MAX_NODES nodes (about 27 MB per GPU that loads the library,
+ * held until the process exits).  The caller passes the reference-layout
+ * device buffers, rows 1..ni*nj*nk in lattice order (i fastest); det, deter
+ * and metric are read; FLOW, U_j, the U the stage advances and L_out (may be
+ * NULL) are written.  Larger lattices are rejected with CFD_EINVAL.  The
+ * first call on each device looks up the array's device address; make it
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU race and must be serialised by the caller.  The call waits for
+ * the stage to finish on `cuda_stream` and returns its status. */
+#define CFD_STATIC_MAX_NODES 32768
+cfd_status_t cfd_lattice_stage_static(void *cuda_stream, int32_t ni, int32_t nj, int32_t nk, int32_t j,
+                                      double del_t, const cfd_params_t *params, const double *det,
+                                      const cfd_determ_t *deter, const cfd_metric_t *metric, cfd_column_t *U0,
+                                      cfd_column_t *U1, cfd_column_t *U2, cfd_flow_t *FLOW, cfd_column_t *L_out);
+
 #ifdef __cplusplus
 }
 #endif
