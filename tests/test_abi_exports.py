@@ -52,3 +52,26 @@ def test_struct_sizes_match_reference(pkg):
     assert layout.GRID_DTYPE.itemsize == 56
     assert layout.BYTES_PER_NODE_REFERENCE == 1376
     assert ctypes.sizeof(abi.Params) == 56
+
+
+@pytest.mark.parametrize("lang,compiler", [("c", "gcc"), ("c++", "g++")])
+def test_header_compiles_standalone(tmp_path, lang, compiler):
+    """include/cfd_rhs.h is self-contained C (no CUDA or torch types)."""
+    import shutil
+    import subprocess
+    if shutil.which(compiler) is None:
+        pytest.skip(f"{compiler} not available")
+    src = tmp_path / ("t.c" if lang == "c" else "t.cpp")
+    src.write_text('#include "cfd_rhs.h"\n'
+                   '_Static_assert(sizeof(cfd_grid_t) == 56, "GRID");\n' if lang == "c" else
+                   '#include "cfd_rhs.h"\n'
+                   'static_assert(sizeof(cfd_grid_t) == 56, "GRID");\n'
+                   'static_assert(sizeof(cfd_flow_t) == 72, "FLOW");\n'
+                   'static_assert(sizeof(cfd_column_t) == 40, "column");\n'
+                   'static_assert(sizeof(cfd_metric_t) == 504, "metric");\n'
+                   'static_assert(sizeof(cfd_determ_t) == 48, "determ");\n'
+                   'static_assert(sizeof(cfd_roe_t) == 288, "roe");\n'
+                   'int main() { cfd_params_t p; cfd_params_default(&p); return 0; }\n')
+    r = subprocess.run([compiler, "-fsyntax-only", "-Wall", "-Werror", f"-I{ROOT / 'include'}", str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
