@@ -34,6 +34,9 @@ def nvcc() -> str:
 # Translation units whose FP64 arithmetic must follow the reference's
 # evaluation order: no contraction of a*b+c into FMA.
 EXACT_FP64 = {"dropin.cu", "structured.cu"}
+# Translation units of the mixed-precision form: approximate FP32 division and
+# square root (single-precision only; FP64 arithmetic is unaffected).
+FAST_FP32 = {"mixed.cu"}
 
 
 def sources() -> list[pathlib.Path]:
@@ -58,6 +61,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     def compile_one(src: pathlib.Path):
         obj = OBJ_DIR / (src.stem + ".o")
         fmad = ["--fmad=false"] if src.name in EXACT_FP64 else []
+        if src.name in FAST_FP32:
+            fmad += ["--prec-div=false", "--prec-sqrt=false"]
         cmd = [cc, *ARCH, *NVCC_FLAGS, *fmad, *extra, "-c", str(src), "-o", str(obj)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         return src, obj, r

@@ -134,17 +134,13 @@ __device__ __forceinline__ void weno_pair(const T c[6], T eps, T &pos, T &neg)
     const T ISp1 = k13 * sqr(c0 - T(2.0) * c1 + c2) + k14 * sqr(c0 - c2);
     const T ISp0 = k13 * sqr(c1 - T(2.0) * c2 + c3) + k14 * sqr(T(3.0) * c1 - T(4.0) * c2 + c3);
     const T d16 = T(1.0) / T(16.0), d58 = T(5.0) / T(8.0), d516 = T(5.0) / T(16.0);
-    // w_k = d_k / s_k with s_k = (eps + IS_k)^2; the normalised combination
-    // sum(w_k x_k)/sum(w_k) is evaluated with a single division as
-    // sum(d_k x_k prod_{j!=k} s_j) / sum(d_k prod_{j!=k} s_j).
+    // w_k = d_k / (eps + IS_k)^2, normalised once: sum(w_k x_k) / sum(w_k)
     {
-        const T s0 = sqr(eps + ISp0), s1 = sqr(eps + ISp1), s2 = sqr(eps + ISp2);
-        const T w0 = d16 * (s1 * s2), w1 = d58 * (s0 * s2), w2 = d516 * (s0 * s1);
+        const T w0 = d16 / sqr(eps + ISp0), w1 = d58 / sqr(eps + ISp1), w2 = d516 / sqr(eps + ISp2);
         pos = (w0 * p0 + w1 * p1 + w2 * p2) / (w0 + w1 + w2);
     }
     {
-        const T s0 = sqr(eps + ISm0), s1 = sqr(eps + ISm1), s2 = sqr(eps + ISm2);
-        const T w0 = d516 * (s1 * s2), w1 = d58 * (s0 * s2), w2 = d16 * (s0 * s1);
+        const T w0 = d516 / sqr(eps + ISm0), w1 = d58 / sqr(eps + ISm1), w2 = d16 / sqr(eps + ISm2);
         neg = (w0 * p1 + w1 * p2 + w2 * m2) / (w0 + w1 + w2);
     }
 }
@@ -262,96 +258,97 @@ struct Phys {
 };
 
 // Viscous and SGS fluxes at one node from the derivatives of U along the
-// three directions (Viscous.cl:439-631).  dU[d][c]: derivative of U_c along
+// three directions (Viscous.cl:439-631), FMA-friendly rewrite for the
+// mixed-precision form (T = float there).  dU[d][c]: derivative of U_c along
 // direction d; Ui: U at the node; m: node metrics (9); det: node det;
 // prim: rho,u,v,w,p of FLOW at the node; KS: the three MTS test-filter
 // velocity-difference squares.  Writes contravariant Fv/Ev/Gv (x det) and mu.
-__device__ __forceinline__ void viscous_node_flux(const double dU[3][5], const double Ui[5], const double m[9],
-                                                  double det, const double prim[5], const double KS[3],
-                                                  const Phys &P, double Fv[5], double Ev[5], double Gv[5],
-                                                  double &mu_out)
+template <class T>
+__device__ __forceinline__ void viscous_node_flux(const T dU[3][5], const T Ui[5], const T m[9], T det,
+                                                  const T prim[5], const T KS[3], const Phys &P, T Fv[5], T Ev[5],
+                                                  T Gv[5], T &mu_out)
 {
-    const double Mach = P.mach, Reyl = P.reynolds, Pr = P.prandtl, Free_t = P.t_inf;
-    const double U0 = Ui[0], U1 = Ui[1], U2 = Ui[2], U3 = Ui[3], U4 = Ui[4];
-    const double iU0 = 1.0 / U0;
-    const double iU00 = 1.0 / (U0 * U0);
-    double uc[3], vc[3], wc[3], tc[3];
+    const T Mach = (T)P.mach, Reyl = (T)P.reynolds, Pr = (T)P.prandtl, Free_t = (T)P.t_inf;
+    const T U0 = Ui[0], U1 = Ui[1], U2 = Ui[2], U3 = Ui[3], U4 = Ui[4];
+    const T iU0 = T(1.0) / U0;
+    const T iU00 = iU0 * iU0;
+    T uc[3], vc[3], wc[3], tc[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         uc[d] = iU0 * dU[d][1] - (U1 * iU00) * dU[d][0];
         vc[d] = iU0 * dU[d][2] - (U2 * iU00) * dU[d][0];
         wc[d] = iU0 * dU[d][3] - (U3 * iU00) * dU[d][0];
     }
-    const double uu = U1 * iU0, vv = U2 * iU0, ww = U3 * iU0;
+    const T uu = U1 * iU0, vv = U2 * iU0, ww = U3 * iU0;
 #pragma unroll
     for (int d = 0; d < 3; ++d)
         tc[d] = iU0 * dU[d][4] - (U4 * iU00) * dU[d][0] - uu * uc[d] - vv * vc[d] - ww * wc[d];
 
     // Sutherland's law with T = gamma M^2 (gamma-1) e (Viscous.cl:451-458)
-    const double d_temp = (1.4 * Mach * Mach * 0.4 * ((U4 * iU0) - 0.5 * (uu * uu + vv * vv + ww * ww)));
-    const double sd = sqrt(d_temp);
-    const double S = 110.4 / Free_t;
-    const double mu = (sd * sd * sd) * ((1.0 + S) / (d_temp + S));
+    const T d_temp = (T(1.4) * Mach * Mach * T(0.4) * ((U4 * iU0) - T(0.5) * (uu * uu + vv * vv + ww * ww)));
+    const T sd = sqrt(d_temp);
+    const T S = T(110.4) / Free_t;
+    const T mu = (sd * sd * sd) * ((T(1.0) + S) / (d_temp + S));
     mu_out = mu;
 
-    const double zx = m[0], zy = m[1], zz = m[2], ex = m[3], ey = m[4], ez = m[5], xx = m[6], xy = m[7], xz = m[8];
-    const double dudx = uc[0] * zx + uc[1] * ex + uc[2] * xx, dudy = uc[0] * zy + uc[1] * ey + uc[2] * xy,
-                 dudz = uc[0] * zz + uc[1] * ez + uc[2] * xz;
-    const double dvdx = vc[0] * zx + vc[1] * ex + vc[2] * xx, dvdy = vc[0] * zy + vc[1] * ey + vc[2] * xy,
-                 dvdz = vc[0] * zz + vc[1] * ez + vc[2] * xz;
-    const double dwdx = wc[0] * zx + wc[1] * ex + wc[2] * xx, dwdy = wc[0] * zy + wc[1] * ey + wc[2] * xy,
-                 dwdz = wc[0] * zz + wc[1] * ez + wc[2] * xz;
-    const double dtdx = tc[0] * zx + tc[1] * ex + tc[2] * xx, dtdy = tc[0] * zy + tc[1] * ey + tc[2] * xy,
-                 dtdz = tc[0] * zz + tc[1] * ez + tc[2] * xz;
+    const T zx = m[0], zy = m[1], zz = m[2], ex = m[3], ey = m[4], ez = m[5], xx = m[6], xy = m[7], xz = m[8];
+    const T dudx = uc[0] * zx + uc[1] * ex + uc[2] * xx, dudy = uc[0] * zy + uc[1] * ey + uc[2] * xy,
+            dudz = uc[0] * zz + uc[1] * ez + uc[2] * xz;
+    const T dvdx = vc[0] * zx + vc[1] * ex + vc[2] * xx, dvdy = vc[0] * zy + vc[1] * ey + vc[2] * xy,
+            dvdz = vc[0] * zz + vc[1] * ez + vc[2] * xz;
+    const T dwdx = wc[0] * zx + wc[1] * ex + wc[2] * xx, dwdy = wc[0] * zy + wc[1] * ey + wc[2] * xy,
+            dwdz = wc[0] * zz + wc[1] * ez + wc[2] * xz;
+    const T dtdx = tc[0] * zx + tc[1] * ex + tc[2] * xx, dtdy = tc[0] * zy + tc[1] * ey + tc[2] * xy,
+            dtdz = tc[0] * zz + tc[1] * ez + tc[2] * xz;
 
-    const double kq = -(mu * 1.4 / (Pr * Reyl));
-    const double qx_ = kq * dtdx, qy_ = kq * dtdy, qz_ = kq * dtdz;   // Viscous.cl:461-463
-    const double mr = mu / Reyl;                                        // Viscous.cl:466-476
-    const double txx = mr * ((4.0 / 3.0) * dudx - (2.0 / 3.0) * dvdy - (2.0 / 3.0) * dwdz);
-    const double tyy = mr * ((4.0 / 3.0) * dvdy - (2.0 / 3.0) * dudx - (2.0 / 3.0) * dwdz);
-    const double tzz = mr * ((4.0 / 3.0) * dwdz - (2.0 / 3.0) * dudx - (2.0 / 3.0) * dvdy);
-    const double sxy = dudy + dvdx, sxz = dudz + dwdx, syz = dvdz + dwdy;
-    const double txy = mr * sxy, txz = mr * sxz, tyz = mr * syz;
+    const T kq = -(mu * T(1.4) / (Pr * Reyl));
+    const T qx_ = kq * dtdx, qy_ = kq * dtdy, qz_ = kq * dtdz;   // Viscous.cl:461-463
+    const T mr = mu / Reyl;                                       // Viscous.cl:466-476
+    const T txx = mr * (T(4.0 / 3.0) * dudx - T(2.0 / 3.0) * dvdy - T(2.0 / 3.0) * dwdz);
+    const T tyy = mr * (T(4.0 / 3.0) * dvdy - T(2.0 / 3.0) * dudx - T(2.0 / 3.0) * dwdz);
+    const T tzz = mr * (T(4.0 / 3.0) * dwdz - T(2.0 / 3.0) * dudx - T(2.0 / 3.0) * dvdy);
+    const T sxy = dudy + dvdx, sxz = dudz + dwdx, syz = dvdz + dwdy;
+    const T txy = mr * sxy, txz = mr * sxz, tyz = mr * syz;
 
-    double TXY = 0, TYZ = 0, TXZ = 0, TXX = 0, TYY = 0, TZZ = 0, HX = 0, HY = 0, HZ = 0, DX = 0, DY = 0, DZ = 0;
+    T TXY = 0, TYZ = 0, TXZ = 0, TXX = 0, TYY = 0, TZZ = 0, HX = 0, HY = 0, HZ = 0, DX = 0, DY = 0, DZ = 0;
     if (P.les) {  // mixed-time-scale SGS model, Viscous.cl:490-558
-        const double C_MTS = 0.03, C_T = 10.0;
-        const double s_xy = 0.5 * sxy, s_yz = 0.5 * syz, s_xz = 0.5 * sxz;
-        const double mod = sqrt(2.0 * ((s_xy * s_xy + s_yz * s_yz + s_xz * s_xz)
-                                       + (2.0 / 3.0) * (dudx * dudx + dvdy * dvdy + dwdz * dwdz)));
-        const double DEL = 1.0 / cbrt(det);
-        double ed[3];
+        const T C_MTS = T(0.03), C_T = T(10.0);
+        const T s_xy = T(0.5) * sxy, s_yz = T(0.5) * syz, s_xz = T(0.5) * sxz;
+        const T mod = sqrt(T(2.0) * ((s_xy * s_xy + s_yz * s_yz + s_xz * s_xz)
+                                     + T(2.0 / 3.0) * (dudx * dudx + dvdy * dvdy + dwdz * dwdz)));
+        const T DEL = T(1.0) / cbrt(det);
+        T ed[3];
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            const double sk = sqrt(KS[d]);
-            if (mod != 0.0) {
-                const double R = (DEL * mod) / sk;
-                ed[d] = (C_MTS / (1.0 + R / C_T)) * DEL * sk;
+            const T sk = sqrt(KS[d]);
+            if (mod != T(0.0)) {
+                const T R = (DEL * mod) / sk;
+                ed[d] = (C_MTS / (T(1.0) + R / C_T)) * DEL * sk;
             } else {
                 ed[d] = C_MTS * DEL * sk;
             }
         }
-        const double r2 = -2.0 * U0;
+        const T r2 = T(-2.0) * U0;
         TXY = r2 * ed[0] * s_xy;
         TYZ = r2 * ed[1] * s_yz;
         TXZ = r2 * ed[2] * s_xz;
         TXX = r2 * ed[0] * dudx;
         TYY = r2 * ed[1] * dvdy;
         TZZ = r2 * ed[2] * dwdz;
-        const double kQ = -(1.0 / (1.4 * 0.4 * Mach * Mach));
-        const double Qx = kQ * ed[0] * dtdx, Qy = kQ * ed[1] * dtdy, Qz = kQ * ed[2] * dtdz;
+        const T kQ = -(T(1.0) / (T(1.4) * T(0.4) * Mach * Mach));
+        const T Qx = kQ * ed[0] * dtdx, Qy = kQ * ed[1] * dtdy, Qz = kQ * ed[2] * dtdz;
         HX = Qx + (TXX + TXY + TXZ) * prim[1];
         HY = Qy + (TXY + TYY + TYZ) * prim[2];
         HZ = Qz + (TXZ + TYZ + TZZ) * prim[3];
-        DX = 0.4 * Qx;
-        DY = 0.4 * Qy;
-        DZ = 0.4 * Qz;
+        DX = T(0.4) * Qx;
+        DY = T(0.4) * Qy;
+        DZ = T(0.4) * Qz;
     }
-    const double u = prim[1], v = prim[2], w = prim[3];
+    const T u = prim[1], v = prim[2], w = prim[3];
     // Cartesian viscous fluxes, Viscous.cl:580-596
-    const double tFv[5] = {0.0, -txx + TXX, -txy + TXY, -txz + TXZ, ((-u * txx - v * txy - w * txz) + qx_ + HX + DX)};
-    const double tEv[5] = {0.0, -txy + TXY, -tyy + TYY, -tyz + TYZ, ((-u * txy - v * tyy - w * tyz) + qy_ + HY + DY)};
-    const double tGv[5] = {0.0, -txz + TXZ, -tyz + TYZ, -tzz + TZZ, ((-u * txz - v * tyz - w * tzz) + qz_ + HZ + DZ)};
+    const T tFv[5] = {T(0), -txx + TXX, -txy + TXY, -txz + TXZ, ((-u * txx - v * txy - w * txz) + qx_ + HX + DX)};
+    const T tEv[5] = {T(0), -txy + TXY, -tyy + TYY, -tyz + TYZ, ((-u * txy - v * tyy - w * tyz) + qy_ + HY + DY)};
+    const T tGv[5] = {T(0), -txz + TXZ, -tyz + TYZ, -tzz + TZZ, ((-u * txz - v * tyz - w * tzz) + qz_ + HZ + DZ)};
 #pragma unroll
     for (int c = 0; c < 5; ++c) {
         Fv[c] = det * (zx * tFv[c] + zy * tEv[c] + zz * tGv[c]);
@@ -361,15 +358,15 @@ __device__ __forceinline__ void viscous_node_flux(const double dU[3][5], const d
 }
 
 // Contravariant node inviscid fluxes F, E, G (x det) from the primitives,
-// Viscous.cl:560-578 and 615-631.
-__device__ __forceinline__ void node_inviscid_flux(const double prim[5], const double m[9], double det, double F[5],
-                                                   double E[5], double G[5])
+// Viscous.cl:560-578 and 615-631 (FMA-friendly, mixed form).
+template <class T>
+__device__ __forceinline__ void node_inviscid_flux(const T prim[5], const T m[9], T det, T F[5], T E[5], T G[5])
 {
-    const double rho = prim[0], u = prim[1], v = prim[2], w = prim[3], p = prim[4];
-    const double Et = (((p / 0.4) + 0.5 * rho * (u * u + v * v + w * w)) + p);
-    const double tF[5] = {rho * u, rho * u * u + p, rho * v * u, rho * u * w, Et * u};
-    const double tE[5] = {rho * v, rho * v * u, rho * v * v + p, rho * v * w, Et * v};
-    const double tG[5] = {rho * w, rho * u * w, rho * v * w, rho * w * w + p, Et * w};
+    const T rho = prim[0], u = prim[1], v = prim[2], w = prim[3], p = prim[4];
+    const T Et = (p * T(2.5) + T(0.5) * rho * (u * u + v * v + w * w)) + p;
+    const T tF[5] = {rho * u, rho * u * u + p, rho * v * u, rho * u * w, Et * u};
+    const T tE[5] = {rho * v, rho * v * u, rho * v * v + p, rho * v * w, Et * v};
+    const T tG[5] = {rho * w, rho * u * w, rho * v * w, rho * w * w + p, Et * w};
 #pragma unroll
     for (int c = 0; c < 5; ++c) {
         F[c] = det * (m[0] * tF[c] + m[1] * tE[c] + m[2] * tG[c]);

@@ -182,15 +182,25 @@ cfd_status_t create_structured(cfd_solver *s, const cfd_geometry_t *g)
     double *m9, *det, *fm, *fdet;
     cfd_status_t st;
     if ((st = dalloc_t(s, 9 * N, &m9)) || (st = dalloc_t(s, N, &det)) || (st = dalloc_t(s, 9 * N, &fm))
-        || (st = dalloc_t(s, 3 * N, &fdet)) || (st = dalloc_t(s, 9 * N, &S.prim9)) || (st = dalloc_t(s, 5 * N, &S.Q))
-        || (st = dalloc_t(s, 15 * N, &S.FEG)) || (st = dalloc_t(s, 15 * N, &S.V)) || (st = dalloc_t(s, 2 * N, &S.sh))
-        || (st = dalloc_t(s, 15 * N, &S.Fh)) || (st = dalloc_t(s, 9 * (N + 1), &s->stage9))
-        || (st = dalloc_t(s, 5 * (N + 1), &s->stage5)) || (st = dalloc_t(s, 5 * N, &s->Lsoa)))
+        || (st = dalloc_t(s, 3 * N, &fdet)) || (st = dalloc_t(s, 9 * N, &S.prim9))
+        || (st = dalloc_t(s, 9 * (N + 1), &s->stage9)) || (st = dalloc_t(s, 5 * (N + 1), &s->stage5))
+        || (st = dalloc_t(s, 5 * N, &s->Lsoa)))
         return st;
     for (int q = 0; q < 3; ++q)
         if ((st = dalloc_t(s, 5 * N, &S.U[q]))) return st;
+    if (s->mixed) {   // FP32 stage intermediates
+        if ((st = dalloc_t(s, 5 * N, &S.Q32)) || (st = dalloc_t(s, 5 * N, &S.R32)) || (st = dalloc_t(s, 15 * N, &S.FEG32))
+            || (st = dalloc_t(s, 15 * N, &S.V32)) || (st = dalloc_t(s, 15 * N, &S.Fh32))
+            || (st = dalloc_t(s, 9 * N, &S.fm32)) || (st = dalloc_t(s, 3 * N, &S.fdet32)))
+            return st;
+        cudaMemsetAsync(S.V32, 0, 15 * N * sizeof(float), S.stream);
+    } else {          // FP64 stage intermediates
+        if ((st = dalloc_t(s, 5 * N, &S.Q)) || (st = dalloc_t(s, 15 * N, &S.FEG)) || (st = dalloc_t(s, 15 * N, &S.V))
+            || (st = dalloc_t(s, 2 * N, &S.sh)) || (st = dalloc_t(s, 15 * N, &S.Fh)))
+            return st;
+        cudaMemsetAsync(S.V, 0, 15 * N * sizeof(double), S.stream);
+    }
     for (int q = 0; q < 3; ++q) cudaMemsetAsync(S.U[q], 0, 5 * N * sizeof(double), S.stream);
-    cudaMemsetAsync(S.V, 0, 15 * N * sizeof(double), S.stream);
     cudaMemsetAsync(s->stage5, 0, 5 * (N + 1) * sizeof(double), S.stream);
     cudaMemsetAsync(s->stage9, 0, 9 * (N + 1) * sizeof(double), S.stream);
     // geometry AoS -> SoA on the host (one-off)
@@ -208,12 +218,13 @@ cfd_status_t create_structured(cfd_solver *s, const cfd_geometry_t *g)
     if ((st = upload(s, m9, h.data(), 9 * N * 8)) || (st = upload(s, det, hd.data(), N * 8))
         || (st = upload(s, fm, hf.data(), 9 * N * 8)) || (st = upload(s, fdet, hfd.data(), 3 * N * 8)))
         return st;
-    cudaError_t e = cudaStreamSynchronize(S.stream);   // host vectors go out of scope
-    if (e != cudaSuccess) return cuda_fail(s->ctx, e, "solver create sync");
     S.m9 = m9;
     S.det = det;
     S.fm = fm;
     S.fdet = fdet;
+    if (s->mixed) mixed_geometry(S);
+    cudaError_t e = cudaStreamSynchronize(S.stream);   // host vectors go out of scope
+    if (e != cudaSuccess) return cuda_fail(s->ctx, e, "solver create sync");
     return CFD_OK;
 }
 

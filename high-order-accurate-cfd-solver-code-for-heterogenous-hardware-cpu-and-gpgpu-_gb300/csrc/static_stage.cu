@@ -106,6 +106,7 @@ extern "C" cfd_status_t cfd_lattice_stage_static(void *cuda_stream, int32_t ni, 
     const long long N = (long long)ni * nj * nk;
     if (N > CFD_STATIC_MAX_NODES) return CFD_EINVAL;   // beyond the static scratch array
     if (!det || !deter || !metric || !U0 || !U1 || !U2 || !FLOW) return CFD_EINVAL;
+    if (params && params->precision == CFD_PREC_MIXED) return CFD_EUNSUPPORTED;   // FP64 form only
     double *base = nullptr;
     cfd_status_t s = scratch_address(&base);
     if (s != CFD_OK) return s;
@@ -124,7 +125,7 @@ extern "C" cfd_status_t cfd_lattice_stage_static(void *cuda_stream, int32_t ni, 
     S.nk = nk;
     S.stream = st;
     S.P = make_phys(params);
-    S.mixed = (params && params->precision == CFD_PREC_MIXED) ? 1 : 0;
+    S.mixed = 0;
     double *m9 = take(9), *dt_ = take(1), *fm = take(9), *fdet = take(3);
     S.m9 = m9;
     S.det = dt_;

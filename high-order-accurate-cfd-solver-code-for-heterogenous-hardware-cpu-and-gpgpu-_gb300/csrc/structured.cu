@@ -269,6 +269,10 @@ static Lat lat(const StructuredLaunch &S) { return Lat{S.ni, S.nj, S.nk, (long l
 
 void structured_stage(const StructuredLaunch &S, int jst, double dt, double *Lout, cudaEvent_t *ev)
 {
+    if (S.mixed) {
+        mixed_stage(S, jst, dt, Lout, ev);
+        return;
+    }
     const Lat g = lat(S);
     const unsigned nb = blocks_for(g.N, 128);
     cudaStream_t st = S.stream;
@@ -285,17 +289,12 @@ void structured_stage(const StructuredLaunch &S, int jst, double dt, double *Lou
     else
         k_mu_only<<<nb, 128, 0, st>>>(g, S.P, Uj, S.prim9);
     mark();
-    if (S.mixed) {
-        launch_faces_mixed(S, ev ? ev + e : nullptr);
-        e += 3;
-    } else {
-        k_face<0><<<nb, 128, 0, st>>>(g, S.P.eps, S.Q, S.prim9, S.sh, S.fm, S.fdet, S.FEG, S.Fh);
-        mark();
-        k_face<1><<<nb, 128, 0, st>>>(g, S.P.eps, S.Q, S.prim9, S.sh, S.fm, S.fdet, S.FEG, S.Fh);
-        mark();
-        k_face<2><<<nb, 128, 0, st>>>(g, S.P.eps, S.Q, S.prim9, S.sh, S.fm, S.fdet, S.FEG, S.Fh);
-        mark();
-    }
+    k_face<0><<<nb, 128, 0, st>>>(g, S.P.eps, S.Q, S.prim9, S.sh, S.fm, S.fdet, S.FEG, S.Fh);
+    mark();
+    k_face<1><<<nb, 128, 0, st>>>(g, S.P.eps, S.Q, S.prim9, S.sh, S.fm, S.fdet, S.FEG, S.Fh);
+    mark();
+    k_face<2><<<nb, 128, 0, st>>>(g, S.P.eps, S.Q, S.prim9, S.sh, S.fm, S.fdet, S.FEG, S.Fh);
+    mark();
     k_update<<<nb, 128, 0, st>>>(g, S.P.viscous, jst, S.P.mach, dt, S.det, S.Fh, S.V, S.U[0], S.U[1], S.U[2], S.prim9,
                                  S.flags, Lout);
     mark();

@@ -25,11 +25,22 @@ struct StructuredLaunch {
     double *sh;                // [2][N]   sqrt(rho), H
     double *Fh;                // [3][5][N] corrected face fluxes
     unsigned *flags;
+    // mixed-precision form (FP32 stage intermediates, mixed.cu)
+    float *Q32 = nullptr;      // [5][N]
+    float *R32 = nullptr;      // [5][N] u, v, w, sqrt(rho), H
+    float *FEG32 = nullptr;    // [3][5][N]
+    float *V32 = nullptr;      // [3][5][N]
+    float *Fh32 = nullptr;     // [3][5][N]
+    float *fm32 = nullptr;     // [3][3][N]
+    float *fdet32 = nullptr;   // [3][N]
 };
 
 // The three face-flux launches of the mixed-precision form (mixed.cu).
-// ev (optional): three events recorded after the three launches.
-void launch_faces_mixed(const StructuredLaunch &S, cudaEvent_t *ev = nullptr);
+// Mixed-precision stage (mixed.cu): same launch count and order as the FP64
+// stage; ev as for structured_stage.
+void mixed_stage(const StructuredLaunch &S, int j, double dt, double *Lout, cudaEvent_t *ev);
+// FP32 copies of the face metrics and face dets (once, after upload).
+void mixed_geometry(const StructuredLaunch &S);
 
 // One RK stage j of the host loop; Lout (device [5][N]) may be null.
 // ev (optional) receives structured_launches_per_stage()+1 recorded events

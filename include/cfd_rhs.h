@@ -247,7 +247,8 @@ cfd_status_t cfd_probe_flops(cfd_ctx_t *ctx, int32_t fp64, double *flops_per_s);
  * held until the process exits).  The caller passes the reference-layout
  * device buffers, rows 1..ni*nj*nk in lattice order (i fastest); det, deter
  * and metric are read; FLOW, U_j, the U the stage advances and L_out (may be
- * NULL) are written.  Larger lattices are rejected with CFD_EINVAL.  The
+ * NULL) are written; FP64 form only (CFD_PREC_MIXED -> CFD_EUNSUPPORTED).
+ * Larger lattices are rejected with CFD_EINVAL.  The
  * first call on each device looks up the array's device address; make it
  * before any stream capture.  All calls share the array: calls that overlap
  * on the GPU race and must be serialised by the caller.  The call waits for
