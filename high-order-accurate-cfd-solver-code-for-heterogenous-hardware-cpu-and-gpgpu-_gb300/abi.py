@@ -47,6 +47,12 @@ class SolverInfo(C.Structure):
                 ("precision", C.c_int32), ("reserved", C.c_int32), ("device_bytes", C.c_uint64)]
 
 
+class BatchInfo(C.Structure):
+    _fields_ = [("n_active", C.c_int32), ("tile_nodes", C.c_int32), ("blocks", C.c_int32), ("graph", C.c_int32),
+                ("precision", C.c_int32), ("reserved", C.c_int32), ("nodes_total", C.c_uint64),
+                ("device_bytes", C.c_uint64), ("capacity_bytes", C.c_uint64)]
+
+
 _vp = C.c_void_p
 _i32 = C.c_int32
 _d = C.c_double
@@ -80,6 +86,18 @@ PROTOTYPES = {
     "cfd_solver_stage": (C.c_int, [_vp, _i32, _d, _vp]),
     "cfd_solver_profile_stage": (C.c_int, [_vp, _i32, _d, _vp, _i32, C.POINTER(_i32)]),
     "cfd_probe_flops": (C.c_int, [_vp, _i32, C.POINTER(_d)]),
+    "cfd_batch_create": (C.c_int, [_vp, _i32, C.c_uint64, C.POINTER(_vp)]),
+    "cfd_batch_destroy": (C.c_int, [_vp]),
+    "cfd_batch_instance_bytes": (C.c_uint64, [_i32, C.c_int64]),
+    "cfd_batch_add": (C.c_int, [_vp, C.POINTER(Geometry), C.POINTER(Params), _vp, _d, C.POINTER(_i32)]),
+    "cfd_batch_remove": (C.c_int, [_vp, _i32]),
+    "cfd_batch_step": (C.c_int, [_vp, _i32]),
+    "cfd_batch_get_flow": (C.c_int, [_vp, _i32, _vp]),
+    "cfd_batch_get_u0": (C.c_int, [_vp, _i32, _vp]),
+    "cfd_batch_slot_status": (C.c_int, [_vp, _i32]),
+    "cfd_batch_set_tiling": (C.c_int, [_vp, _i32, _i32, _i32]),
+    "cfd_batch_tune": (C.c_int, [_vp, _i32]),
+    "cfd_batch_info": (C.c_int, [_vp, C.POINTER(BatchInfo)]),
     "cfd_lattice_stage_static": (C.c_int, [_vp, _i32, _i32, _i32, _i32, _d, C.POINTER(Params)] + [_vp] * 8),
 }
 STATIC_MAX_NODES = 32768

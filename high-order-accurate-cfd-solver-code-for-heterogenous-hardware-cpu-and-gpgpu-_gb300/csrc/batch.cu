@@ -1,0 +1,576 @@
+// batch.cu -- many independent lattices advanced together: one persistent,
+// cooperative launch per RK stage over a tile table of all instances
+// (batch_kernel.cuh), one RK step captured as a CUDA graph, and a tuner that
+// times tile sizes on the live batch (state saved and restored around the
+// trials).  Instances are admitted against a device-memory budget, keep
+// their state resident, and can be added and removed between steps; this is
+// the engine under the serving loop.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "batch_kernel.cuh"
+#include "batch_ops.h"
+#include "internal.h"
+#include "lattice_host.h"
+#include "structured.h"
+
+namespace {
+
+using namespace cfd;
+
+constexpr int kMaxSlots = 4096;
+
+struct BatchInst {
+    bool active = false;
+    int32_t g_node = 0;
+    int ni = 0, nj = 0, nk = 0, N = 0;
+    cfd_params_t prm{};
+    double dt = 0.0;
+    std::vector<void *> allocs;
+    uint64_t bytes = 0;
+    LatView view{};
+    double *stage9 = nullptr;   // AoS FLOW staging rows 0..N
+    double *stage5 = nullptr;   // AoS column staging rows 0..N
+};
+
+}  // namespace
+
+struct cfd_batch {
+    cfd_ctx *ctx = nullptr;
+    int precision = CFD_PREC_FP64;
+    uint64_t capacity = 0, used = 0;
+    std::vector<BatchInst> slots;
+    LatView *d_views = nullptr;
+    size_t views_cap = 0;
+    BatchTile *d_tiles = nullptr;
+    size_t tiles_cap = 0;
+    int ntiles = 0;
+    int n_views = 0;
+    unsigned *d_words = nullptr;          // [0..1] barrier, [2] batch flags, [4..] per-slot flags
+    int threads = 128;
+    int blocks_override = 0;
+    int blocks = 0;
+    bool dirty = true;
+    bool use_graph = true;
+    bool graph_ok = false;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    uint64_t total_nodes = 0;
+};
+
+namespace {
+
+unsigned *bar_words(cfd_batch *b) { return b->d_words; }
+unsigned *batch_flags(cfd_batch *b) { return b->d_words + 2; }
+unsigned *slot_flags(cfd_batch *b, int slot) { return b->d_words + 4 + slot; }
+
+uint64_t instance_bytes(int precision, int64_t N)
+{
+    const uint64_t doubles = (22 + 9 + 15) * (uint64_t)N + 14 * (uint64_t)(N + 1);
+    if (precision == CFD_PREC_MIXED) return doubles * 8 + (12 + 55) * (uint64_t)N * 4;
+    return (doubles + 52 * (uint64_t)N) * 8;
+}
+
+void drop_graph(cfd_batch *b)
+{
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->gexec = nullptr;
+    b->graph = nullptr;
+    b->graph_ok = false;
+}
+
+void free_instance(BatchInst &I)
+{
+    for (void *p : I.allocs) cudaFree(p);
+    I.allocs.clear();
+    I = BatchInst();
+}
+
+template <class T>
+cfd_status_t ialloc(cfd_batch *b, BatchInst &I, size_t count, T **p)
+{
+    cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+    if (e != cudaSuccess) return cuda_fail(b->ctx, e, "cudaMalloc (batch instance)");
+    I.allocs.push_back(*p);
+    I.bytes += count * sizeof(T);
+    return CFD_OK;
+}
+
+cfd_status_t rebuild(cfd_batch *b)
+{
+    std::vector<LatView> views;
+    std::vector<BatchTile> tiles;
+    const int T = b->threads;
+    uint64_t nodes = 0;
+    for (size_t s = 0; s < b->slots.size(); ++s) {
+        const BatchInst &I = b->slots[s];
+        if (!I.active) continue;
+        const int v = (int)views.size();
+        views.push_back(I.view);
+        for (int n0 = 0; n0 < I.N; n0 += T) tiles.push_back(BatchTile{v, n0, std::min(T, I.N - n0), 0});
+        nodes += (uint64_t)I.N;
+    }
+    cudaStream_t st = b->ctx->stream;
+    cudaError_t e = cudaSuccess;
+    if (views.size() > b->views_cap) {
+        if (b->d_views) cudaFree(b->d_views);
+        b->views_cap = std::max<size_t>(views.size(), 2 * b->views_cap);
+        e = cudaMalloc(&b->d_views, b->views_cap * sizeof(LatView));
+        if (e != cudaSuccess) return cuda_fail(b->ctx, e, "batch view table");
+    }
+    if (tiles.size() > b->tiles_cap) {
+        if (b->d_tiles) cudaFree(b->d_tiles);
+        b->tiles_cap = std::max<size_t>(tiles.size(), 2 * b->tiles_cap);
+        e = cudaMalloc(&b->d_tiles, b->tiles_cap * sizeof(BatchTile));
+        if (e != cudaSuccess) return cuda_fail(b->ctx, e, "batch tile table");
+    }
+    if (!views.empty()) e = cudaMemcpyAsync(b->d_views, views.data(), views.size() * sizeof(LatView), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && !tiles.empty())
+        e = cudaMemcpyAsync(b->d_tiles, tiles.data(), tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(b->ctx, e, "batch table upload");
+    b->ntiles = (int)tiles.size();
+    b->n_views = (int)views.size();
+    b->total_nodes = nodes;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int occ = b->precision == CFD_PREC_MIXED ? batch_occupancy_mixed(T) : batch_occupancy_fp64(T);
+    if (occ <= 0) return fail(b->ctx, CFD_EUNSUPPORTED, "batch: stage kernel does not fit at this tile size");
+    int blocks = occ * sms;
+    if (b->blocks_override > 0) blocks = std::min(blocks, b->blocks_override);
+    blocks = std::max(1, std::min(blocks, 4 * std::max(b->ntiles, 1)));
+    b->blocks = blocks;
+    drop_graph(b);
+    b->dirty = false;
+    return CFD_OK;
+}
+
+BatchLaunch launch_of(cfd_batch *b)
+{
+    BatchLaunch L{};
+    L.views = b->d_views;
+    L.tiles = b->d_tiles;
+    L.ntiles = b->ntiles;
+    L.threads = b->threads;
+    L.blocks = b->blocks;
+    L.bar = bar_words(b);
+    L.gflags = batch_flags(b);
+    // generous deadline for the barrier: 5 s + 50 ns per node of the batch
+    L.limit_ns = 5000000000ULL + 50ULL * b->total_nodes;
+    L.stream = b->ctx->stream;
+    return L;
+}
+
+cudaError_t launch_step(cfd_batch *b)
+{
+    const BatchLaunch L = launch_of(b);
+    for (int j = 0; j < 3; ++j) {
+        cudaError_t e = b->precision == CFD_PREC_MIXED ? batch_stage_mixed(L, j) : batch_stage_fp64(L, j);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+void try_capture(cfd_batch *b)
+{
+    cudaStream_t st = b->ctx->stream;
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        b->use_graph = false;
+        return;
+    }
+    cudaError_t le = launch_step(b);
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(st, &g);
+    if (le != cudaSuccess || ce != cudaSuccess || !g) {
+        cudaGetLastError();
+        if (g) cudaGraphDestroy(g);
+        b->use_graph = false;
+        return;
+    }
+    cudaGraphExec_t ge = nullptr;
+    if (cudaGraphInstantiate(&ge, g, 0) != cudaSuccess) {
+        cudaGetLastError();
+        cudaGraphDestroy(g);
+        b->use_graph = false;
+        return;
+    }
+    b->graph = g;
+    b->gexec = ge;
+    b->graph_ok = true;
+}
+
+// Waits for the stream; batch-level flags become the status, per-slot flags
+// stay readable through cfd_batch_slot_status.
+cfd_status_t finish(cfd_batch *b)
+{
+    std::vector<unsigned> w(4 + b->slots.size());
+    cudaError_t e = cudaMemcpyAsync(w.data(), b->d_words, w.size() * sizeof(unsigned), cudaMemcpyDeviceToHost,
+                                    b->ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(b->ctx, e, "batch finish");
+    if (w[2] & CFD_FLAG_TIMEOUT) return fail(b->ctx, CFD_ETIMEOUT, "batch: grid barrier deadline expired");
+    for (size_t s = 0; s < b->slots.size(); ++s)
+        if (b->slots[s].active && (w[4 + s] & CFD_FLAG_NONFINITE))
+            return fail(b->ctx, CFD_ENONFINITE, "batch: non-finite state in slot " + std::to_string(s));
+    return CFD_OK;
+}
+
+// Per-instance arrays that a step changes, for the tuner's save/restore.
+std::vector<std::pair<void *, size_t>> mutable_arrays(const BatchInst &I, int precision)
+{
+    const size_t N = (size_t)I.N;
+    std::vector<std::pair<void *, size_t>> v = {{I.view.prim9, 9 * N * 8}, {I.view.U0, 5 * N * 8},
+                                                {I.view.U1, 5 * N * 8}, {I.view.U2, 5 * N * 8}};
+    if (precision == CFD_PREC_MIXED) {
+        v.push_back({I.view.Q32, 5 * N * 4});
+        v.push_back({I.view.R32, 5 * N * 4});
+        v.push_back({I.view.FEG32, 15 * N * 4});
+    } else {
+        v.push_back({I.view.Q, 5 * N * 8});
+        v.push_back({I.view.FEG, 15 * N * 8});
+        v.push_back({I.view.sh, 2 * N * 8});
+    }
+    return v;
+}
+
+}  // namespace
+
+extern "C" {
+
+uint64_t cfd_batch_instance_bytes(int32_t precision, int64_t nodes) { return instance_bytes(precision, nodes); }
+
+cfd_status_t cfd_batch_create(cfd_ctx_t *ctx, int32_t precision, uint64_t capacity_bytes, cfd_batch_t **out)
+{
+    if (!ctx || !out || (precision != CFD_PREC_FP64 && precision != CFD_PREC_MIXED)) return CFD_EINVAL;
+    *out = nullptr;
+    cfd_status_t s = use_device(ctx);
+    if (s != CFD_OK) return s;
+    cfd_batch *b = new cfd_batch();
+    b->ctx = ctx;
+    b->precision = precision;
+    if (capacity_bytes == 0) {
+        size_t fr = 0, tot = 0;
+        cudaMemGetInfo(&fr, &tot);
+        capacity_bytes = (uint64_t)(0.85 * (double)fr);
+    }
+    b->capacity = capacity_bytes;
+    cudaError_t e = cudaMalloc(&b->d_words, (4 + kMaxSlots) * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(b->d_words, 0, (4 + kMaxSlots) * sizeof(unsigned));
+    if (e != cudaSuccess) {
+        delete b;
+        return cuda_fail(ctx, e, "batch create");
+    }
+    *out = b;
+    return CFD_OK;
+}
+
+cfd_status_t cfd_batch_destroy(cfd_batch_t *b)
+{
+    if (!b) return CFD_EINVAL;
+    use_device(b->ctx);
+    cudaStreamSynchronize(b->ctx->stream);
+    drop_graph(b);
+    for (auto &I : b->slots) free_instance(I);
+    if (b->d_views) cudaFree(b->d_views);
+    if (b->d_tiles) cudaFree(b->d_tiles);
+    if (b->d_words) cudaFree(b->d_words);
+    delete b;
+    return CFD_OK;
+}
+
+cfd_status_t cfd_batch_add(cfd_batch_t *b, const cfd_geometry_t *geom, const cfd_params_t *params,
+                           const cfd_flow_t *flow, double del_t, int32_t *slot_out)
+{
+    if (!b || !geom || !flow || !slot_out || !std::isfinite(del_t)) return CFD_EINVAL;
+    *slot_out = -1;
+    cfd_ctx *ctx = b->ctx;
+    cfd_status_t st = use_device(ctx);
+    if (st != CFD_OK) return st;
+    if (!geom->grid || !geom->det || !geom->deter || !geom->metric || geom->g_node < 1)
+        return fail(ctx, CFD_EINVAL, "cfd_batch_add: bad geometry");
+    for (int32_t r = 0; r <= geom->g_node; ++r)
+        for (int slot = 0; slot < 6; ++slot) {
+            const int v = nb_of(geom->grid[r], slot);
+            if (v < 0 || v > geom->g_node) return fail(ctx, CFD_EINVAL, "cfd_batch_add: neighbour index out of range");
+        }
+    int ni = 0, nj = 0, nk = 0;
+    if (!detect_lattice(geom, ni, nj, nk) || !faces_single_valued(geom))
+        return fail(ctx, CFD_EUNSUPPORTED, "cfd_batch_add: batched instances must be periodic lattices");
+    const int N = ni * nj * nk;
+    const uint64_t need = instance_bytes(b->precision, N);
+    if (b->used + need > b->capacity) return fail(ctx, CFD_ENOMEM, "cfd_batch_add: device-memory budget exhausted");
+    int slot = -1;
+    for (size_t s = 0; s < b->slots.size(); ++s)
+        if (!b->slots[s].active) {
+            slot = (int)s;
+            break;
+        }
+    if (slot < 0) {
+        if ((int)b->slots.size() >= kMaxSlots) return fail(ctx, CFD_ENOMEM, "cfd_batch_add: too many instances");
+        b->slots.emplace_back();
+        slot = (int)b->slots.size() - 1;
+    }
+    BatchInst &I = b->slots[slot];
+    I.g_node = geom->g_node;
+    I.ni = ni;
+    I.nj = nj;
+    I.nk = nk;
+    I.N = N;
+    cfd_params_default(&I.prm);
+    if (params) I.prm = *params;
+    I.dt = del_t;
+    const size_t Nz = (size_t)N;
+    double *m9, *det, *fm, *fdet, *prim9, *U0, *U1, *U2;
+    if ((st = ialloc(b, I, 9 * Nz, &m9)) || (st = ialloc(b, I, Nz, &det)) || (st = ialloc(b, I, 9 * Nz, &fm))
+        || (st = ialloc(b, I, 3 * Nz, &fdet)) || (st = ialloc(b, I, 9 * Nz, &prim9)) || (st = ialloc(b, I, 5 * Nz, &U0))
+        || (st = ialloc(b, I, 5 * Nz, &U1)) || (st = ialloc(b, I, 5 * Nz, &U2))
+        || (st = ialloc(b, I, 9 * (Nz + 1), &I.stage9)) || (st = ialloc(b, I, 5 * (Nz + 1), &I.stage5))) {
+        free_instance(I);
+        return st;
+    }
+    LatView &v = I.view;
+    v.ni = ni;
+    v.nj = nj;
+    v.nk = nk;
+    v.N = N;
+    v.P = make_phys(&I.prm);
+    v.dt = del_t;
+    v.m9 = m9;
+    v.det = det;
+    v.fm = fm;
+    v.fdet = fdet;
+    v.prim9 = prim9;
+    v.U0 = U0;
+    v.U1 = U1;
+    v.U2 = U2;
+    v.flags = slot_flags(b, slot);
+    v.Lout = nullptr;
+    if (b->precision == CFD_PREC_MIXED) {
+        float *fm32, *fdet32;
+        if ((st = ialloc(b, I, 9 * Nz, &fm32)) || (st = ialloc(b, I, 3 * Nz, &fdet32)) || (st = ialloc(b, I, 5 * Nz, &v.Q32))
+            || (st = ialloc(b, I, 5 * Nz, &v.R32)) || (st = ialloc(b, I, 15 * Nz, &v.FEG32))
+            || (st = ialloc(b, I, 15 * Nz, &v.V32)) || (st = ialloc(b, I, 15 * Nz, &v.Fh32))) {
+            free_instance(I);
+            return st;
+        }
+        v.fm32 = fm32;
+        v.fdet32 = fdet32;
+    } else {
+        if ((st = ialloc(b, I, 5 * Nz, &v.Q)) || (st = ialloc(b, I, 15 * Nz, &v.FEG)) || (st = ialloc(b, I, 15 * Nz, &v.V))
+            || (st = ialloc(b, I, 2 * Nz, &v.sh)) || (st = ialloc(b, I, 15 * Nz, &v.Fh))) {
+            free_instance(I);
+            return st;
+        }
+    }
+    cudaStream_t sm = ctx->stream;
+    std::vector<double> h, hd, hf, hfd;
+    lattice_geometry_soa(geom, Nz, h, hd, hf, hfd);
+    cudaError_t e = cudaMemcpyAsync(m9, h.data(), 9 * Nz * 8, cudaMemcpyHostToDevice, sm);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(det, hd.data(), Nz * 8, cudaMemcpyHostToDevice, sm);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(fm, hf.data(), 9 * Nz * 8, cudaMemcpyHostToDevice, sm);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(fdet, hfd.data(), 3 * Nz * 8, cudaMemcpyHostToDevice, sm);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(I.stage9, flow, 9 * (Nz + 1) * 8, cudaMemcpyHostToDevice, sm);
+    if (e == cudaSuccess) e = cudaMemsetAsync(I.stage5, 0, 5 * (Nz + 1) * 8, sm);
+    if (e == cudaSuccess) e = cudaMemsetAsync(v.flags, 0, sizeof(unsigned), sm);
+    for (double *u : {U0, U1, U2})
+        if (e == cudaSuccess) e = cudaMemsetAsync(u, 0, 5 * Nz * 8, sm);
+    if (e == cudaSuccess) e = b->precision == CFD_PREC_MIXED ? cudaMemsetAsync(v.V32, 0, 15 * Nz * 4, sm)
+                                                              : cudaMemsetAsync(v.V, 0, 15 * Nz * 8, sm);
+    if (e != cudaSuccess) {
+        cudaStreamSynchronize(sm);
+        free_instance(I);
+        return cuda_fail(ctx, e, "cfd_batch_add upload");
+    }
+    aos_to_soa(sm, I.stage9, 9, 9, N, prim9);
+    if (b->precision == CFD_PREC_MIXED) {
+        StructuredLaunch S{};
+        S.ni = ni;
+        S.nj = nj;
+        S.nk = nk;
+        S.stream = sm;
+        S.fm = fm;
+        S.fdet = fdet;
+        S.fm32 = const_cast<float *>(v.fm32);
+        S.fdet32 = const_cast<float *>(v.fdet32);
+        mixed_geometry(S);
+        batch_prep_mixed(v, sm);
+    } else {
+        batch_prep_fp64(v, sm);
+    }
+    ctx->launches += 2;
+    e = cudaStreamSynchronize(sm);   // host geometry vectors go out of scope
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        free_instance(I);
+        return cuda_fail(ctx, e, "cfd_batch_add prep");
+    }
+    I.active = true;
+    b->used += I.bytes;
+    b->dirty = true;
+    *slot_out = slot;
+    return CFD_OK;
+}
+
+cfd_status_t cfd_batch_remove(cfd_batch_t *b, int32_t slot)
+{
+    if (!b || slot < 0 || slot >= (int)b->slots.size() || !b->slots[slot].active) return CFD_EINVAL;
+    use_device(b->ctx);
+    cudaStreamSynchronize(b->ctx->stream);
+    b->used -= b->slots[slot].bytes;
+    free_instance(b->slots[slot]);
+    b->dirty = true;
+    return CFD_OK;
+}
+
+cfd_status_t cfd_batch_step(cfd_batch_t *b, int32_t nsteps)
+{
+    if (!b || nsteps < 0) return CFD_EINVAL;
+    cfd_status_t st = use_device(b->ctx);
+    if (st != CFD_OK) return st;
+    if (b->dirty && (st = rebuild(b)) != CFD_OK) return st;
+    if (b->ntiles == 0 || nsteps == 0) return CFD_OK;
+    if (b->use_graph && !b->graph_ok) try_capture(b);
+    cudaStream_t sm = b->ctx->stream;
+    for (int s = 0; s < nsteps; ++s) {
+        cudaError_t e = b->graph_ok ? cudaGraphLaunch(b->gexec, sm) : launch_step(b);
+        if (e != cudaSuccess) return cuda_fail(b->ctx, e, "batch step launch");
+        b->ctx->launches += 3;
+    }
+    return finish(b);
+}
+
+cfd_status_t cfd_batch_get_flow(cfd_batch_t *b, int32_t slot, cfd_flow_t *host)
+{
+    if (!b || !host || slot < 0 || slot >= (int)b->slots.size() || !b->slots[slot].active) return CFD_EINVAL;
+    use_device(b->ctx);
+    BatchInst &I = b->slots[slot];
+    soa_to_aos(b->ctx->stream, I.view.prim9, 9, 9, I.N, I.stage9);
+    cudaError_t e = cudaMemcpyAsync(host, I.stage9, 9 * ((size_t)I.N + 1) * 8, cudaMemcpyDeviceToHost, b->ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(b->ctx, e, "cfd_batch_get_flow");
+    return CFD_OK;
+}
+
+cfd_status_t cfd_batch_get_u0(cfd_batch_t *b, int32_t slot, cfd_column_t *host)
+{
+    if (!b || !host || slot < 0 || slot >= (int)b->slots.size() || !b->slots[slot].active) return CFD_EINVAL;
+    use_device(b->ctx);
+    BatchInst &I = b->slots[slot];
+    soa_to_aos(b->ctx->stream, I.view.U0, 5, 5, I.N, I.stage5);
+    cudaError_t e = cudaMemcpyAsync(host, I.stage5, 5 * ((size_t)I.N + 1) * 8, cudaMemcpyDeviceToHost, b->ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(b->ctx, e, "cfd_batch_get_u0");
+    return CFD_OK;
+}
+
+cfd_status_t cfd_batch_slot_status(cfd_batch_t *b, int32_t slot)
+{
+    if (!b || slot < 0 || slot >= (int)b->slots.size() || !b->slots[slot].active) return CFD_EINVAL;
+    unsigned w = 0;
+    cudaError_t e = cudaMemcpyAsync(&w, slot_flags(b, slot), sizeof w, cudaMemcpyDeviceToHost, b->ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(b->ctx, e, "cfd_batch_slot_status");
+    return (w & CFD_FLAG_NONFINITE) ? CFD_ENONFINITE : CFD_OK;
+}
+
+cfd_status_t cfd_batch_set_tiling(cfd_batch_t *b, int32_t tile_nodes, int32_t max_blocks, int32_t use_graph)
+{
+    if (!b || (tile_nodes != 0 && tile_nodes != 64 && tile_nodes != 128 && tile_nodes != 256) || max_blocks < 0)
+        return CFD_EINVAL;
+    if (tile_nodes) b->threads = tile_nodes;
+    b->blocks_override = max_blocks;
+    b->use_graph = use_graph != 0;
+    b->dirty = true;
+    drop_graph(b);
+    return CFD_OK;
+}
+
+cfd_status_t cfd_batch_tune(cfd_batch_t *b, int32_t steps_per_trial)
+{
+    if (!b || steps_per_trial < 1) return CFD_EINVAL;
+    cfd_status_t st = use_device(b->ctx);
+    if (st != CFD_OK) return st;
+    cudaStream_t sm = b->ctx->stream;
+    // save the mutable state of every instance
+    std::vector<std::pair<void *, size_t>> arrays;
+    for (auto &I : b->slots)
+        if (I.active)
+            for (auto &a : mutable_arrays(I, b->precision)) arrays.push_back(a);
+    size_t total = 0;
+    for (auto &a : arrays) total += a.second;
+    if (total == 0) return CFD_OK;
+    char *backup = nullptr;
+    cudaError_t e = cudaMalloc(&backup, total);
+    if (e != cudaSuccess) return cuda_fail(b->ctx, e, "cfd_batch_tune backup");
+    auto copy_all = [&](bool save) {
+        size_t off = 0;
+        for (auto &a : arrays) {
+            if (save) cudaMemcpyAsync(backup + off, a.first, a.second, cudaMemcpyDeviceToDevice, sm);
+            else cudaMemcpyAsync(a.first, backup + off, a.second, cudaMemcpyDeviceToDevice, sm);
+            off += a.second;
+        }
+    };
+    copy_all(true);
+    const int candidates[3] = {64, 128, 256};
+    int best = b->threads;
+    float best_ms = 1e30f;
+    cudaEvent_t t0, t1;
+    cudaEventCreate(&t0);
+    cudaEventCreate(&t1);
+    for (int T : candidates) {
+        b->threads = T;
+        b->dirty = true;
+        if ((st = rebuild(b)) != CFD_OK) continue;
+        if (b->use_graph) try_capture(b);
+        auto one = [&]() { return b->graph_ok ? cudaGraphLaunch(b->gexec, sm) : launch_step(b); };
+        if (one() != cudaSuccess) { cudaGetLastError(); continue; }   // warm-up
+        cudaEventRecord(t0, sm);
+        bool ok = true;
+        for (int s = 0; s < steps_per_trial && ok; ++s) ok = one() == cudaSuccess;
+        cudaEventRecord(t1, sm);
+        b->ctx->launches += 3 * (steps_per_trial + 1);
+        if (!ok || cudaEventSynchronize(t1) != cudaSuccess) { cudaGetLastError(); continue; }
+        float ms = 0;
+        cudaEventElapsedTime(&ms, t0, t1);
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = T;
+        }
+    }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    copy_all(false);
+    cudaMemsetAsync(b->d_words, 0, (4 + kMaxSlots) * sizeof(unsigned), sm);
+    e = cudaStreamSynchronize(sm);
+    cudaFree(backup);
+    if (e != cudaSuccess) return cuda_fail(b->ctx, e, "cfd_batch_tune restore");
+    b->threads = best;
+    b->dirty = true;
+    return rebuild(b);
+}
+
+cfd_status_t cfd_batch_info(const cfd_batch_t *b, cfd_batch_info_t *info)
+{
+    if (!b || !info) return CFD_EINVAL;
+    std::memset(info, 0, sizeof *info);
+    int n = 0;
+    for (auto &I : b->slots) n += I.active ? 1 : 0;
+    info->n_active = n;
+    info->tile_nodes = b->threads;
+    info->blocks = b->blocks;
+    info->graph = b->graph_ok ? 1 : 0;
+    info->precision = b->precision;
+    uint64_t nodes = 0;
+    for (auto &I : b->slots)
+        if (I.active) nodes += (uint64_t)I.N;
+    info->nodes_total = nodes;
+    info->device_bytes = b->used;
+    info->capacity_bytes = b->capacity;
+    return CFD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,62 @@
+// lattice.cuh -- one periodic lattice as the device kernels see it: shape,
+// constants, and pointers to its structure-of-arrays fields.  Shared by the
+// single-lattice kernels (structured.cu, mixed.cu) and the batched
+// persistent kernel (batch_*.cu), which holds one LatView per instance.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "physics.cuh"
+
+namespace cfd {
+
+// Field layout: every array is [component][N], n = i + ni*(j + nj*k).
+struct LatView {
+    int ni, nj, nk, N;
+    Phys P;
+    double dt;
+    // geometry (FP64), and FP32 copies of the face terms for the mixed form
+    const double *m9, *det, *fm, *fdet;
+    const float *fm32, *fdet32;
+    // state
+    double *prim9;             // FLOW fields u,v,w,p,t,rho,mu,a,e
+    double *U0, *U1, *U2;
+    // FP64 stage intermediates
+    double *Q, *FEG, *V, *sh, *Fh;
+    // FP32 stage intermediates (mixed form)
+    float *Q32, *R32, *FEG32, *V32, *Fh32;
+    unsigned *flags;           // error word of this lattice
+    double *Lout;              // optional [5][N] right-hand side output
+};
+
+enum { LF_U = 0, LF_V = 1, LF_W = 2, LF_P = 3, LF_T = 4, LF_RHO = 5, LF_MU = 6, LF_A = 7, LF_E = 8 };
+
+// periodic wrap for offsets of any size (|o| may exceed the extent)
+__device__ __forceinline__ int lwrap(int x, int n)
+{
+    while (x < 0) x += n;
+    while (x >= n) x -= n;
+    return x;
+}
+
+__device__ __forceinline__ void lat_ijk(const LatView &g, int n, int &i, int &j, int &k)
+{
+    const unsigned un = (unsigned)n, uni = (unsigned)g.ni, unj = (unsigned)g.nj;
+    const unsigned r = un / uni;
+    i = (int)(un - r * uni);
+    k = (int)(r / unj);
+    j = (int)(r - (unsigned)k * unj);
+}
+
+// node at offset o along direction d from (i,j,k)
+__device__ __forceinline__ int lat_step(const LatView &g, int i, int j, int k, int d, int o)
+{
+    if (d == 0) i = lwrap(i + o, g.ni);
+    else if (d == 1) j = lwrap(j + o, g.nj);
+    else k = lwrap(k + o, g.nk);
+    return i + g.ni * (j + g.nj * k);
+}
+
+__device__ __forceinline__ double *lat_U(const LatView &g, int q) { return q == 0 ? g.U0 : (q == 1 ? g.U1 : g.U2); }
+
+}  // namespace cfd

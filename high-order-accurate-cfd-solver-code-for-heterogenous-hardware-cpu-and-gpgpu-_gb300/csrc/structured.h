@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include "lattice.cuh"
 #include "physics.cuh"
 
 namespace cfd {
@@ -41,6 +42,41 @@ struct StructuredLaunch {
 void mixed_stage(const StructuredLaunch &S, int j, double dt, double *Lout, cudaEvent_t *ev);
 // FP32 copies of the face metrics and face dets (once, after upload).
 void mixed_geometry(const StructuredLaunch &S);
+
+// Device view of a StructuredLaunch for one stage.
+inline LatView make_view(const StructuredLaunch &S, double dt, double *Lout)
+{
+    LatView g{};
+    g.ni = S.ni;
+    g.nj = S.nj;
+    g.nk = S.nk;
+    g.N = S.ni * S.nj * S.nk;
+    g.P = S.P;
+    g.dt = dt;
+    g.m9 = S.m9;
+    g.det = S.det;
+    g.fm = S.fm;
+    g.fdet = S.fdet;
+    g.fm32 = S.fm32;
+    g.fdet32 = S.fdet32;
+    g.prim9 = S.prim9;
+    g.U0 = S.U[0];
+    g.U1 = S.U[1];
+    g.U2 = S.U[2];
+    g.Q = S.Q;
+    g.FEG = S.FEG;
+    g.V = S.V;
+    g.sh = S.sh;
+    g.Fh = S.Fh;
+    g.Q32 = S.Q32;
+    g.R32 = S.R32;
+    g.FEG32 = S.FEG32;
+    g.V32 = S.V32;
+    g.Fh32 = S.Fh32;
+    g.flags = S.flags;
+    g.Lout = Lout;
+    return g;
+}
 
 // One RK stage j of the host loop; Lout (device [5][N]) may be null.
 // ev (optional) receives structured_launches_per_stage()+1 recorded events

@@ -233,3 +233,88 @@ class Solver:
         self.ctx.check(self.lib.cfd_solver_stage(self.h, int(j), float(dt), C.c_void_p(_ptr(out)) if want_L else None),
                        "cfd_solver_stage")
         return out
+
+
+@dataclasses.dataclass
+class BatchInfo:
+    n_active: int
+    tile_nodes: int
+    blocks: int
+    graph: bool
+    precision: str
+    nodes_total: int
+    device_bytes: int
+    capacity_bytes: int
+
+
+class Batch:
+    """Many periodic-lattice instances advanced together (cfd_batch_*): one
+    persistent launch per RK stage over all instances, CUDA-graph replay."""
+
+    def __init__(self, ctx: Context, precision: int = 0, capacity_bytes: int = 0):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        h = C.c_void_p()
+        ctx.check(self.lib.cfd_batch_create(ctx.h, int(precision), int(capacity_bytes), C.byref(h)), "cfd_batch_create")
+        self.h = h
+        self.rows = {}
+
+    @staticmethod
+    def instance_bytes(precision: int, nodes: int) -> int:
+        return int(abi.load().cfd_batch_instance_bytes(int(precision), int(nodes)))
+
+    def close(self):
+        if self.h:
+            self.lib.cfd_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add(self, case, flow=None, dt=None, params=None) -> int:
+        a = case.arrays
+        geom = abi.Geometry(case.g_node, case.sd_node, _ptr(a["grid"]), _ptr(a["det"]), _ptr(a["deter"]),
+                            _ptr(a["metric"]))
+        pr = to_params(params if params is not None else case.params)
+        f = np.ascontiguousarray(a["flow"] if flow is None else flow)
+        slot = C.c_int32()
+        self.ctx.check(self.lib.cfd_batch_add(self.h, C.byref(geom), C.byref(pr), C.c_void_p(_ptr(f)),
+                                              float(case.dt if dt is None else dt), C.byref(slot)), "cfd_batch_add")
+        self.rows[slot.value] = case.g_node + 1
+        return slot.value
+
+    def remove(self, slot: int):
+        self.ctx.check(self.lib.cfd_batch_remove(self.h, int(slot)), "cfd_batch_remove")
+        self.rows.pop(slot, None)
+
+    def step(self, nsteps: int = 1):
+        self.ctx.check(self.lib.cfd_batch_step(self.h, int(nsteps)), "cfd_batch_step")
+
+    def get_flow(self, slot: int) -> np.ndarray:
+        out = np.empty((self.rows[slot], L.NFLOW))
+        self.ctx.check(self.lib.cfd_batch_get_flow(self.h, int(slot), C.c_void_p(_ptr(out))), "cfd_batch_get_flow")
+        return out
+
+    def get_u0(self, slot: int) -> np.ndarray:
+        out = np.empty((self.rows[slot], L.NCOL))
+        self.ctx.check(self.lib.cfd_batch_get_u0(self.h, int(slot), C.c_void_p(_ptr(out))), "cfd_batch_get_u0")
+        return out
+
+    def slot_status(self, slot: int) -> int:
+        return int(self.lib.cfd_batch_slot_status(self.h, int(slot)))
+
+    def set_tiling(self, tile_nodes: int = 0, max_blocks: int = 0, use_graph: bool = True):
+        self.ctx.check(self.lib.cfd_batch_set_tiling(self.h, int(tile_nodes), int(max_blocks), 1 if use_graph else 0),
+                       "cfd_batch_set_tiling")
+
+    def tune(self, steps_per_trial: int = 2):
+        self.ctx.check(self.lib.cfd_batch_tune(self.h, int(steps_per_trial)), "cfd_batch_tune")
+
+    def info(self) -> BatchInfo:
+        i = abi.BatchInfo()
+        self.ctx.check(self.lib.cfd_batch_info(self.h, C.byref(i)), "cfd_batch_info")
+        return BatchInfo(i.n_active, i.tile_nodes, i.blocks, bool(i.graph), "mixed" if i.precision else "fp64",
+                         int(i.nodes_total), int(i.device_bytes), int(i.capacity_bytes))

@@ -230,6 +230,52 @@ typedef struct {
 cfd_status_t cfd_solver_profile_stage(cfd_solver_t *s, int32_t j, double del_t, cfd_kernel_time_t *out,
                                       int32_t max_out, int32_t *n_out);
 
+/* ------------------------------------------------ batched lattices ---- */
+/* Many independent periodic lattices of different sizes advanced together:
+ * one persistent cooperative kernel launch per RK stage covers every
+ * instance through a tile table, and one RK step is captured as a CUDA
+ * graph.  Instances are admitted against a device-memory budget, stay
+ * resident, and may be added or removed between steps (the serving loop's
+ * engine).  Each instance has its own parameters and time step. */
+typedef struct cfd_batch cfd_batch_t;
+
+typedef struct {
+    int32_t n_active;          /* instances in the batch                      */
+    int32_t tile_nodes;        /* nodes per tile = threads per block          */
+    int32_t blocks;            /* persistent grid size                        */
+    int32_t graph;             /* 1 when steps replay a captured CUDA graph   */
+    int32_t precision;         /* cfd_precision_t of the whole batch          */
+    int32_t reserved;
+    uint64_t nodes_total;
+    uint64_t device_bytes;     /* admitted instance memory                    */
+    uint64_t capacity_bytes;   /* admission budget                            */
+} cfd_batch_info_t;
+
+/* capacity_bytes = 0: 85 % of the device memory free at creation. */
+cfd_status_t cfd_batch_create(cfd_ctx_t *ctx, int32_t precision, uint64_t capacity_bytes, cfd_batch_t **batch);
+cfd_status_t cfd_batch_destroy(cfd_batch_t *b);
+/* Device bytes one instance of `nodes` lattice nodes takes (admission). */
+uint64_t cfd_batch_instance_bytes(int32_t precision, int64_t nodes);
+/* Adds a periodic-lattice instance (CFD_EUNSUPPORTED otherwise) with its
+ * initial FLOW rows 0..g_node and time step; CFD_ENOMEM beyond the budget. */
+cfd_status_t cfd_batch_add(cfd_batch_t *b, const cfd_geometry_t *geom, const cfd_params_t *params,
+                           const cfd_flow_t *flow, double del_t, int32_t *slot);
+cfd_status_t cfd_batch_remove(cfd_batch_t *b, int32_t slot);
+/* nsteps SSP-RK3 steps of every instance.  CFD_ENONFINITE names the first
+ * failing slot in cfd_last_error; the other instances advance normally. */
+cfd_status_t cfd_batch_step(cfd_batch_t *b, int32_t nsteps);
+cfd_status_t cfd_batch_get_flow(cfd_batch_t *b, int32_t slot, cfd_flow_t *flow_host);
+/* U0 = det*Q of the current FLOW (the next stage's U_Q output). */
+cfd_status_t cfd_batch_get_u0(cfd_batch_t *b, int32_t slot, cfd_column_t *u0_host);
+cfd_status_t cfd_batch_slot_status(cfd_batch_t *b, int32_t slot);
+/* tile_nodes in {64, 128, 256} (0 = keep), max_blocks (0 = occupancy limit),
+ * use_graph 0/1. */
+cfd_status_t cfd_batch_set_tiling(cfd_batch_t *b, int32_t tile_nodes, int32_t max_blocks, int32_t use_graph);
+/* Times each tile size on the live batch (state saved and restored) and
+ * keeps the fastest. */
+cfd_status_t cfd_batch_tune(cfd_batch_t *b, int32_t steps_per_trial);
+cfd_status_t cfd_batch_info(const cfd_batch_t *b, cfd_batch_info_t *info);
+
 /* ------------------------------------------------------------ probes ---- */
 /* Measured FMA throughput of this device (FLOP/s, FMA = 2 FLOP): fp64 != 0
  * for double, 0 for float.  Denominator of the FP64/FP32 rooflines. */

@@ -1,0 +1,158 @@
+"""Batched lattices (cfd_batch_*): one persistent launch per RK stage over
+instances of different sizes.  Each instance must give the same result in a
+mix as alone (bitwise: the per-node arithmetic does not depend on the batch),
+FP64 instances must match the oracle (relative L2 <= 1e-12), and mixed
+instances the FP64 form (<= 1e-6)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from helpers import copy_arrays, rel_l2
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+def mix_cases():
+    from cfd_gb300 import cases
+    return [
+        cases.isentropic_vortex(n=12, shape=(12, 10, 8)),
+        cases.taylor_green(n=10, shape=(10, 12, 9)),
+        cases.isentropic_vortex(n=9, beta=3.0, u_inf=0.3, shape=(9, 9, 11)),
+        cases.taylor_green(n=8, shape=(8, 8, 8), amp=0.03),
+    ]
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_mix_equals_alone_bitwise(ctx, precision):
+    from cfd_gb300 import runtime
+    cs = mix_cases()
+    mix = runtime.Batch(ctx, precision)
+    slots = [mix.add(c) for c in cs]
+    info = mix.info()
+    assert info.n_active == len(cs) and info.nodes_total == sum(c.sd_node for c in cs)
+    mix.step(3)
+    for c, s in zip(cs, slots):
+        alone = runtime.Batch(ctx, precision)
+        a = alone.add(c)
+        alone.step(3)
+        assert np.array_equal(alone.get_flow(a), mix.get_flow(s))
+        assert np.array_equal(alone.get_u0(a), mix.get_u0(s))
+        alone.close()
+    mix.close()
+
+
+def test_fp64_batch_matches_oracle_and_solver(ctx, oracle_mod):
+    from cfd_gb300 import runtime
+    cs = mix_cases()
+    b = runtime.Batch(ctx, 0)
+    slots = [b.add(c) for c in cs]
+    b.step(4)
+    for c, s in zip(cs, slots):
+        a = copy_arrays(c.arrays)
+        oracle_mod.rk3_steps(a, c.g_node, c.sd_node, c.params, c.dt, 4)
+        own = slice(1, c.sd_node + 1)
+        got = b.get_flow(s)
+        assert rel_l2(got[own], a["flow"][own]) <= TOL
+        sv = runtime.Solver(ctx, c)
+        sv.set_flow(c.arrays["flow"])
+        sv.step(c.dt, 4)
+        assert np.array_equal(sv.get_flow()[own], got[own])   # same per-node arithmetic
+        sv.close()
+    b.close()
+
+
+def test_mixed_batch_error_budget(ctx):
+    from cfd_gb300 import runtime
+    cs = mix_cases()
+    res = []
+    for prec in (0, 1):
+        b = runtime.Batch(ctx, prec)
+        slots = [b.add(c) for c in cs]
+        b.step(6)
+        res.append([b.get_u0(s)[1:] for s in slots])
+        b.close()
+    for u64, um in zip(*res):
+        assert rel_l2(um, u64) <= 1e-6
+
+
+def test_add_remove_between_steps_and_slot_reuse(ctx):
+    from cfd_gb300 import runtime
+    cs = mix_cases()
+    b = runtime.Batch(ctx, 1)
+    s0 = b.add(cs[0])
+    s1 = b.add(cs[1])
+    b.step(2)
+    b.remove(s0)
+    s2 = b.add(cs[2])
+    assert s2 == s0                      # freed slot reused
+    b.step(1)
+    # instance 1 stepped 3 times in a changing batch == alone 3 steps
+    alone = runtime.Batch(ctx, 1)
+    a = alone.add(cs[1])
+    alone.step(3)
+    assert np.array_equal(alone.get_flow(a), b.get_flow(s1))
+    # instance 2 stepped once after joining == alone 1 step
+    alone2 = runtime.Batch(ctx, 1)
+    a2 = alone2.add(cs[2])
+    alone2.step(1)
+    assert np.array_equal(alone2.get_flow(a2), b.get_flow(s2))
+    for x in (b, alone, alone2):
+        x.close()
+
+
+def test_tuning_and_graph_do_not_change_results(ctx):
+    from cfd_gb300 import runtime
+    cs = mix_cases()
+    ref = runtime.Batch(ctx, 1)
+    ref.set_tiling(128, 0, use_graph=False)
+    rs = [ref.add(c) for c in cs]
+    ref.step(2)
+    tuned = runtime.Batch(ctx, 1)
+    ts = [tuned.add(c) for c in cs]
+    tuned.tune(1)                        # trials run on the live batch, state restored
+    tuned.step(2)
+    assert tuned.info().tile_nodes in (64, 128, 256)
+    for r, t in zip(rs, ts):
+        assert np.array_equal(ref.get_flow(r), tuned.get_flow(t))
+    ref.close()
+    tuned.close()
+
+
+def test_admission_budget_and_unsupported_geometry(ctx):
+    from cfd_gb300 import abi, cases, runtime
+    c = cases.isentropic_vortex(n=10)
+    need = runtime.Batch.instance_bytes(0, c.sd_node)
+    b = runtime.Batch(ctx, 0, capacity_bytes=int(1.5 * need))
+    b.add(c)
+    with pytest.raises(abi.CfdError) as e:
+        b.add(c)
+    assert e.value.status == abi.ENOMEM
+    with pytest.raises(abi.CfdError) as e:
+        b.add(cases.ghost_box(shape=(6, 6, 6)))
+    assert e.value.status == abi.EUNSUPPORTED
+    b.close()
+
+
+def test_nonfinite_instance_is_isolated(ctx):
+    """A poisoned instance reports CFD_ENONFINITE for its own slot; the other
+    instances of the batch advance exactly as they would alone."""
+    from cfd_gb300 import abi, runtime
+    cs = mix_cases()
+    bad = copy_arrays(cs[1].arrays)["flow"]
+    bad[7, 5] = np.nan
+    b = runtime.Batch(ctx, 0)
+    s_good = b.add(cs[0])
+    s_bad = b.add(cs[1], flow=bad)
+    with pytest.raises(abi.CfdError) as e:
+        b.step(1)
+    assert e.value.status == abi.ENONFINITE
+    assert b.slot_status(s_bad) == abi.ENONFINITE
+    assert b.slot_status(s_good) == abi.OK
+    alone = runtime.Batch(ctx, 0)
+    a = alone.add(cs[0])
+    alone.step(1)
+    assert np.array_equal(alone.get_flow(a), b.get_flow(s_good))
+    b.close()
+    alone.close()
