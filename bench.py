@@ -72,6 +72,10 @@ def parse_args(argv=None):
     p.add_argument("--cpu-steps", type=int, default=1, help="full steps timed for the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-mixed", action="store_true")
+    p.add_argument("--batch-count", type=int, default=64, help="instances of the batched workload (0 = skip)")
+    p.add_argument("--batch-steps", type=int, default=20)
+    p.add_argument("--serve-requests", type=int, default=24, help="requests of the serving workload (0 = skip)")
+    p.add_argument("--serve-fp64", action="store_true", help="also serve the stream with the FP64 form")
     return p.parse_args(argv)
 
 
@@ -343,6 +347,11 @@ def gpu_arm(args):
     }
     s64.close()
 
+    if args.batch_count > 0:
+        line["batched"] = bench_batched(ctx, torch, stream, args)
+    if args.serve_requests > 0:
+        line["serving"] = bench_serving(ctx, args)
+
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         rate, cores, secs = cpu_oracle_rate(case, args.cpu_steps)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
@@ -364,6 +373,92 @@ def load_peaks() -> dict:
         return json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
     except (OSError, ValueError):
         return {}
+
+
+def batched_cases(count: int, seed: int = 20261203):
+    """Batched workload: `count` isentropic-vortex instances with lattice edge
+    log-uniform in [32, 96], vortex strength uniform in [2, 6] and advection
+    speed uniform in [0.2, 0.8] (seeded)."""
+    import numpy as np
+    from cfd_gb300 import cases
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        n = int(round(math.exp(rng.uniform(math.log(32), math.log(96)))))
+        beta, u_inf = float(rng.uniform(2.0, 6.0)), float(rng.uniform(0.2, 0.8))
+        out.append(cases.isentropic_vortex(n=n, beta=beta, u_inf=u_inf))
+    return out
+
+
+def bench_batched(ctx, torch, stream, args):
+    """One persistent launch per RK stage over all instances; mixed form
+    (tuned tiles) and FP64 form; mixed-vs-FP64 error after the same steps."""
+    import numpy as np
+    from cfd_gb300 import runtime
+    t0 = time.perf_counter()
+    cs = batched_cases(args.batch_count)
+    gen_s = time.perf_counter() - t0
+    nodes = sum(c.sd_node for c in cs)
+    out = {"instances": len(cs), "nodes_total": nodes, "case_generation_s": gen_s,
+           "workload": "isentropic vortices, edge log-uniform [32, 96], beta U[2,6], u_inf U[0.2,0.8], seed 20261203"}
+
+    def timed(b, steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        b.step(steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3
+
+    u_ref = None
+    for prec, steps in ((0, max(1, args.batch_steps // 5)), (1, args.batch_steps)):
+        b = runtime.Batch(ctx, prec)
+        slots = [b.add(c) for c in cs]
+        if prec == 1:
+            b.tune(1)
+        b.step(1)
+        secs = timed(b, steps)
+        info = b.info()
+        key = "mixed" if prec else "fp64"
+        out[key] = {"value": nodes * steps / secs, "unit": UNIT, "ms_per_step": 1e3 * secs / steps, "steps": steps,
+                    "tile_nodes": info.tile_nodes, "blocks": info.blocks, "cuda_graph": info.graph,
+                    "device_gb": info.device_bytes / 1e9}
+        if prec == 0:
+            u_ref = [b.get_u0(s)[1:] for s in slots]
+            ref_steps = 1 + steps
+        b.close()
+    # mixed after the same number of steps as the FP64 reference
+    b = runtime.Batch(ctx, 1)
+    slots = [b.add(c) for c in cs]
+    b.step(ref_steps)
+    num = sum(float(np.sum((b.get_u0(s)[1:] - u) ** 2)) for s, u in zip(slots, u_ref))
+    den = sum(float(np.sum(u ** 2)) for u in u_ref)
+    b.close()
+    out["mixed"]["rel_l2_vs_fp64"] = math.sqrt(num / den)
+    out["mixed"]["speedup_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    return out
+
+
+def bench_serving(ctx, args):
+    """Continuous batching of a seeded Poisson request stream (mean 50/s;
+    vortex or Taylor-Green; edge log-uniform [32, 160]; steps U[50, 400])."""
+    from cfd_gb300 import serving
+    reqs = serving.poisson_requests(args.serve_requests)
+    t0 = time.perf_counter()
+    cache = {r.rid: serving.make_case(r) for r in reqs}
+    gen_s = time.perf_counter() - t0
+    out = {"requests": len(reqs), "arrival_rate_per_s": 50.0, "case_generation_s": gen_s,
+           "workload": "Poisson(50/s) vortex/TGV 50:50, edge log-uniform [32,160], steps U[50,400], seed 20261203"}
+    for prec in ((1, 0) if args.serve_fp64 else (1,)):
+        srv = serving.Server(ctx, precision=prec, tune=True)
+        r = srv.run(reqs, case_cache=cache)
+        srv.close()
+        out["mixed" if prec else "fp64"] = {
+            "cell_updates_per_s": r["cell_updates_per_s"], "latency_p50_s": r["latency_p50_s"],
+            "latency_p99_s": r["latency_p99_s"], "latency_max_s": r["latency_max_s"], "makespan_s": r["makespan_s"],
+            "batch_steps": r["batch_steps"], "completed": r["requests"]}
+    return out
 
 
 def _kernel_table(prof) -> dict:

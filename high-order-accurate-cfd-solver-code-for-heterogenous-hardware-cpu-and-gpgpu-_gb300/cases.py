@@ -127,11 +127,64 @@ def _fill_periodic_grid(a, ni, nj, nk, x, y, z):
 
 def _node_metrics(jac):
     """jac[..., a, b] = d x_a / d zeta_b (index coordinates).  Returns the
-    9 node metrics (zeta_x, zeta_y, zeta_z, eta_x, ..., xi_z) and det."""
-    inv = np.linalg.inv(jac)          # inv[..., b, a] = d zeta_b / d x_a
-    det = np.linalg.det(jac)
+    9 node metrics (zeta_x, zeta_y, zeta_z, eta_x, ..., xi_z) = the inverse
+    Jacobian (cofactors / det, as Grid_Transformation.cpp:1029-1037 forms
+    them) and det."""
+    J = jac
+    c00 = J[..., 1, 1] * J[..., 2, 2] - J[..., 1, 2] * J[..., 2, 1]
+    c01 = J[..., 1, 2] * J[..., 2, 0] - J[..., 1, 0] * J[..., 2, 2]
+    c02 = J[..., 1, 0] * J[..., 2, 1] - J[..., 1, 1] * J[..., 2, 0]
+    det = J[..., 0, 0] * c00 + J[..., 0, 1] * c01 + J[..., 0, 2] * c02
+    inv = np.empty(J.shape)
+    inv[..., 0, 0] = c00
+    inv[..., 1, 0] = c01
+    inv[..., 2, 0] = c02
+    inv[..., 0, 1] = J[..., 0, 2] * J[..., 2, 1] - J[..., 0, 1] * J[..., 2, 2]
+    inv[..., 1, 1] = J[..., 0, 0] * J[..., 2, 2] - J[..., 0, 2] * J[..., 2, 0]
+    inv[..., 2, 1] = J[..., 0, 1] * J[..., 2, 0] - J[..., 0, 0] * J[..., 2, 1]
+    inv[..., 0, 2] = J[..., 0, 1] * J[..., 1, 2] - J[..., 0, 2] * J[..., 1, 1]
+    inv[..., 1, 2] = J[..., 0, 2] * J[..., 1, 0] - J[..., 0, 0] * J[..., 1, 2]
+    inv[..., 2, 2] = J[..., 0, 0] * J[..., 1, 1] - J[..., 0, 1] * J[..., 1, 0]
+    inv /= det[..., None, None]       # inv[..., b, a] = d zeta_b / d x_a
     m9 = inv.reshape(inv.shape[:-2] + (9,))
     return m9, det
+
+
+def _lattice_half_points(a, m9_kji, det_kji):
+    """Half-point metrics and face determinants of a periodic lattice from
+    node values held in row order as [k, j, i, ...] arrays: the six-point
+    midpoint rule (3, -25, 150, 150, -25, 3)/256 of Main.cpp:2369-2440 with
+    the same operand order as half_point_metrics, evaluated on wrap-padded
+    slices instead of neighbour chains."""
+    nk, nj, ni = det_kji.shape
+    for d in range(3):
+        axis = 2 - d                      # i -> axis 2, j -> axis 1, k -> axis 0
+        n = det_kji.shape[axis]
+        for src, dst_cols in ((m9_kji, None), (det_kji, None)):
+            pad = [(0, 0)] * src.ndim
+            pad[axis] = (3, 3)
+            v = np.pad(src, pad, mode="wrap")
+
+            def sl(o):
+                idx = [slice(None)] * src.ndim
+                idx[axis] = slice(3 + o, 3 + o + n)
+                return v[tuple(idx)]
+            for side in (0, 1):            # +1/2 face uses offsets -2..3, -1/2 face -3..2
+                o0 = -2 - side
+                # ((((3 f0 - 25 f1) + 150 f2) + 150 f3) - 25 f4) + 3 f5, then x 1/256,
+                # accumulated in place (same order and rounding as the expression)
+                out = np.multiply(sl(o0), 3.0)
+                tmp = np.empty_like(out)
+                for o, cst, sub in ((1, 25.0, True), (2, 150.0, False), (3, 150.0, False), (4, 25.0, True),
+                                    (5, 3.0, False)):
+                    np.multiply(sl(o0 + o), cst, out=tmp)
+                    (np.subtract if sub else np.add)(out, tmp, out=out)
+                out *= (1.0 / 256.0)
+                if src is m9_kji:
+                    b = 1 + 2 * d + side
+                    a["metric"][1:, 9 * b:9 * b + 9] = out.reshape(-1, 9)
+                else:
+                    a["deter"][1:, 2 * d + side] = out.ravel()
 
 
 def half_point_metrics(a, n_rows_owned: int):
@@ -240,33 +293,35 @@ def taylor_green(n=128, amp=0.05, mach=0.1, reynolds=1600.0, prandtl=0.72, t_inf
     p = 1/(gamma M^2) + (cos 2x + cos 2y)(cos 2z + 2)/16."""
     ni, nj, nk = shape if shape is not None else (n, n, n)
     hs = (2 * math.pi / ni, 2 * math.pi / nj, 2 * math.pi / nk)
-    x1, x2, x3 = np.meshgrid(np.arange(ni) * hs[0], np.arange(nj) * hs[1], np.arange(nk) * hs[2],
-                             indexing="ij")
+    # arrays in row order [k, j, i] (i fastest)
+    x3, x2, x1 = np.meshgrid(np.arange(nk) * hs[2], np.arange(nj) * hs[1], np.arange(ni) * hs[0], indexing="ij")
     A = amp
-    X = x1 + A * np.sin(x2) * np.sin(x3)
-    Y = x2 + A * np.sin(x3) * np.sin(x1)
-    Z = x3 + A * np.sin(x1) * np.sin(x2)
+    s1, c1, s2, c2, s3, c3 = np.sin(x1), np.cos(x1), np.sin(x2), np.cos(x2), np.sin(x3), np.cos(x3)
+    X = x1 + A * s2 * s3
+    Y = x2 + A * s3 * s1
+    Z = x3 + A * s1 * s2
     a = L.empty_arrays(ni * nj * nk + 1)
     _set_dummy_row(a)
-    _fill_periodic_grid(a, ni, nj, nk, X, Y, Z)
+    _fill_periodic_grid(a, ni, nj, nk, X.transpose(2, 1, 0), Y.transpose(2, 1, 0), Z.transpose(2, 1, 0))
     jac = np.empty(x1.shape + (3, 3))
     jac[..., 0, 0] = 1.0
-    jac[..., 0, 1] = A * np.cos(x2) * np.sin(x3)
-    jac[..., 0, 2] = A * np.sin(x2) * np.cos(x3)
-    jac[..., 1, 0] = A * np.sin(x3) * np.cos(x1)
+    jac[..., 0, 1] = A * c2 * s3
+    jac[..., 0, 2] = A * s2 * c3
+    jac[..., 1, 0] = A * s3 * c1
     jac[..., 1, 1] = 1.0
-    jac[..., 1, 2] = A * np.cos(x3) * np.sin(x1)
-    jac[..., 2, 0] = A * np.cos(x1) * np.sin(x2)
-    jac[..., 2, 1] = A * np.sin(x1) * np.cos(x2)
+    jac[..., 1, 2] = A * c3 * s1
+    jac[..., 2, 0] = A * c1 * s2
+    jac[..., 2, 1] = A * s1 * c2
     jac[..., 2, 2] = 1.0
-    jac = jac * np.array(hs)[None, None, None, None, :]
+    jac *= np.array(hs)[None, None, None, None, :]
     m9, det = _node_metrics(jac)
-    a["metric"][1:, 0:9] = m9.transpose(2, 1, 0, 3).reshape(-1, 9)
-    a["det"][1:] = det.transpose(2, 1, 0).ravel()
-    half_point_metrics(a, ni * nj * nk)
+    del jac
+    a["metric"][1:, 0:9] = m9.reshape(-1, 9)
+    a["det"][1:] = det.ravel()
+    _lattice_half_points(a, m9, det)
 
     gam = 1.4
-    xx, yy, zz = a["grid"]["x"][1:], a["grid"]["y"][1:], a["grid"]["z"][1:]
+    xx, yy, zz = X.ravel(), Y.ravel(), Z.ravel()
     u = np.sin(xx) * np.cos(yy) * np.cos(zz)
     v = -np.cos(xx) * np.sin(yy) * np.cos(zz)
     w = np.zeros_like(u)

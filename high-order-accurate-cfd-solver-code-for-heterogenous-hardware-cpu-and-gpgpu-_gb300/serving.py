@@ -1,0 +1,149 @@
+"""Serving loop: continuous batching of independent solves on one GPU.
+
+Requests (an initial-value problem on a periodic lattice plus a number of
+SSP-RK3 steps) arrive over time.  The loop keeps every admitted solve's
+state resident in one batch (``runtime.Batch``: one persistent launch per RK
+stage over all instances) and, between steps:
+
+* admits queued requests in arrival order while their device-memory
+  footprint fits the batch budget (``cfd_batch_instance_bytes``);
+* advances every admitted solve by one step;
+* retires the solves that reached their step count (their FLOW is read back
+  as the result) and frees their memory for the queue.
+
+Requests that arrive while others run join at the next step boundary, so
+their work overlaps on the device with the solves already in flight.  The
+reference has no serving layer; this is the builder's request loop around the
+RHS path.  Latency = completion time - arrival time.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+import time
+
+import numpy as np
+
+from . import cases, runtime
+
+
+@dataclasses.dataclass
+class Request:
+    rid: int
+    arrival: float          # seconds from the start of the run
+    kind: str               # "vortex" or "tgv"
+    n: int                  # lattice edge (n^3 nodes)
+    steps: int
+    seed: int
+
+
+@dataclasses.dataclass
+class Completed:
+    rid: int
+    arrival: float
+    admitted: float
+    finished: float
+    nodes: int
+    steps: int
+    flow: np.ndarray | None
+
+    @property
+    def latency(self) -> float:
+        return self.finished - self.arrival
+
+
+def poisson_requests(count: int, rate: float = 50.0, n_range=(32, 160), steps_range=(50, 400),
+                     seed: int = 20261203) -> list:
+    """Seeded request stream: Poisson arrivals of mean rate `rate` per second,
+    50/50 vortex/Taylor-Green, lattice edge log-uniform in n_range, step count
+    uniform in steps_range."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for r in range(count):
+        t += rng.exponential(1.0 / rate)
+        kind = "vortex" if rng.random() < 0.5 else "tgv"
+        n = int(round(math.exp(rng.uniform(math.log(n_range[0]), math.log(n_range[1])))))
+        steps = int(rng.integers(steps_range[0], steps_range[1] + 1))
+        out.append(Request(r, t, kind, n, steps, int(rng.integers(0, 2**31 - 1))))
+    return out
+
+
+def make_case(req: Request):
+    rng = np.random.default_rng(req.seed)
+    if req.kind == "vortex":
+        return cases.isentropic_vortex(n=req.n, beta=float(rng.uniform(2.0, 6.0)), u_inf=float(rng.uniform(0.2, 0.8)))
+    return cases.taylor_green(n=req.n)
+
+
+class Server:
+    """Continuous-batching request loop over one ``runtime.Batch``."""
+
+    def __init__(self, ctx, precision: int = 1, capacity_bytes: int = 0, keep_results: bool = False,
+                 tune: bool = False):
+        self.batch = runtime.Batch(ctx, precision, capacity_bytes)
+        self.precision = precision
+        self.keep_results = keep_results
+        self.tune = tune
+        self.info0 = self.batch.info()
+
+    def close(self):
+        self.batch.close()
+
+    def run(self, requests: list, case_cache: dict | None = None, clock=time.perf_counter) -> dict:
+        """Serves `requests` (sorted by arrival) in real time; returns the
+        completed solves and summary statistics."""
+        case_cache = {} if case_cache is None else case_cache
+        queue = list(sorted(requests, key=lambda r: r.arrival))
+        active = {}              # slot -> [request, remaining steps, admitted time]
+        done = []
+        budget = self.info0.capacity_bytes
+        t0 = clock()
+        steps_run = 0
+        tuned = not self.tune
+        while queue or active:
+            now = clock() - t0
+            # admission: arrived requests in order while their footprint fits
+            used = self.batch.info().device_bytes
+            while queue and queue[0].arrival <= now:
+                req = queue[0]
+                need = runtime.Batch.instance_bytes(self.precision, req.n ** 3)
+                if used + need > budget:
+                    if not active:
+                        raise RuntimeError(f"request {req.rid} ({req.n}^3) exceeds the device budget")
+                    break
+                c = case_cache.get(req.rid) or make_case(req)
+                slot = self.batch.add(c)
+                used += need
+                active[slot] = [req, req.steps, clock() - t0]
+                queue.pop(0)
+            if not active:
+                time.sleep(max(0.0, min(queue[0].arrival - (clock() - t0), 0.05)))
+                continue
+            if not tuned and len(active) > 1:
+                self.batch.tune(1)
+                tuned = True
+            self.batch.step(1)
+            steps_run += 1
+            finished = [s for s, a in active.items() if a[1] == 1]
+            for s in list(active):
+                active[s][1] -= 1
+            for s in finished:
+                req, _, adm = active.pop(s)
+                flow = self.batch.get_flow(s) if self.keep_results else None
+                self.batch.remove(s)
+                done.append(Completed(req.rid, req.arrival, adm, clock() - t0, req.n ** 3, req.steps, flow))
+        makespan = clock() - t0
+        lat = np.array([c.latency for c in done])
+        work = float(sum(c.nodes * c.steps for c in done))
+        return {
+            "completed": done,
+            "requests": len(done),
+            "makespan_s": makespan,
+            "batch_steps": steps_run,
+            "cell_updates": work,
+            "cell_updates_per_s": work / makespan if makespan > 0 else 0.0,
+            "latency_p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
+            "latency_p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
+            "latency_max_s": float(lat.max()) if len(lat) else None,
+        }

@@ -77,3 +77,17 @@ def test_axis_permutation_symmetry(oracle_mod):
                 s = L1g[i, k, j]
                 exp[k, j, i] = [s[0], s[3], s[1], s[2], s[4]]
     assert rel_l2(L2g, exp) < 1e-12
+
+
+def test_request_stream_is_seeded(pkg):
+    """The serving workload generator is deterministic and follows the
+    configured distributions (Poisson mean 50/s, n in [32, 160], steps in
+    [50, 400])."""
+    from cfd_gb300 import serving
+    a = serving.poisson_requests(40)
+    b = serving.poisson_requests(40)
+    assert [(r.arrival, r.n, r.steps, r.kind) for r in a] == [(r.arrival, r.n, r.steps, r.kind) for r in b]
+    assert all(32 <= r.n <= 160 and 50 <= r.steps <= 400 for r in a)
+    gaps = np.diff([0.0] + [r.arrival for r in a])
+    assert 0.005 < gaps.mean() < 0.06
+    assert {r.kind for r in a} == {"vortex", "tgv"}
