@@ -76,6 +76,8 @@ def parse_args(argv=None):
     p.add_argument("--batch-steps", type=int, default=20)
     p.add_argument("--serve-requests", type=int, default=24, help="requests of the serving workload (0 = skip)")
     p.add_argument("--serve-fp64", action="store_true", help="also serve the stream with the FP64 form")
+    p.add_argument("--diag-steps", type=int, default=200,
+                   help="steps of the kinetic-energy/enstrophy comparison on the main case (0 = skip)")
     return p.parse_args(argv)
 
 
@@ -347,6 +349,8 @@ def gpu_arm(args):
     }
     s64.close()
 
+    if args.diag_steps > 0 and args.config.startswith("tgv"):
+        line["tgv_diagnostics"] = bench_diagnostics(ctx, case, args)
     if args.batch_count > 0:
         line["batched"] = bench_batched(ctx, torch, stream, args)
     if args.serve_requests > 0:
@@ -438,6 +442,34 @@ def bench_batched(ctx, torch, stream, args):
     out["mixed"]["rel_l2_vs_fp64"] = math.sqrt(num / den)
     out["mixed"]["speedup_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
     return out
+
+
+def bench_diagnostics(ctx, case, args):
+    """Kinetic energy and enstrophy of the main case over `diag_steps` steps,
+    mixed form against the FP64 form (which matches the oracle to 1e-12)."""
+    import numpy as np
+    from cfd_gb300 import diagnostics, runtime
+    every = max(1, args.diag_steps // 4)
+    hist = {}
+    for prec in (0, 1):
+        s = runtime.Solver(ctx, case, precision=prec)
+        s.set_flow(case.arrays["flow"])
+        h = [diagnostics.kinetic_energy_enstrophy(case.arrays["flow"], case.arrays["metric"], case.arrays["det"],
+                                                  case.shape)]
+        done = 0
+        while done < args.diag_steps:
+            k = min(every, args.diag_steps - done)
+            s.step(case.dt, k)
+            done += k
+            h.append(diagnostics.kinetic_energy_enstrophy(s.get_flow(), case.arrays["metric"], case.arrays["det"],
+                                                          case.shape))
+        s.close()
+        hist[prec] = np.array(h)
+    err = np.abs(hist[1] - hist[0]) / np.abs(hist[0])
+    return {"steps": args.diag_steps, "samples_every": every,
+            "kinetic_energy_fp64": hist[0][:, 0].tolist(), "enstrophy_fp64": hist[0][:, 1].tolist(),
+            "kinetic_energy_max_rel_err_mixed": float(err[:, 0].max()),
+            "enstrophy_max_rel_err_mixed": float(err[:, 1].max())}
 
 
 def bench_serving(ctx, args):

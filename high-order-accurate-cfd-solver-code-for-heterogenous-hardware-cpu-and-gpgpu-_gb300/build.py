@@ -52,6 +52,8 @@ def _stale() -> bool:
 
 
 def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) -> pathlib.Path:
+    """Compile every csrc/*.cu for sm_103a and link libcfd_gb300.so.  Extra
+    nvcc flags may be passed in the CFD_NVCC_EXTRA environment variable."""
     if not force and not _stale():
         return LIB
     cc = nvcc()
@@ -63,7 +65,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
         fmad = ["--fmad=false"] if src.name in EXACT_FP64 else []
         if src.name in FAST_FP32:
             fmad += ["--prec-div=false", "--prec-sqrt=false"]
-        cmd = [cc, *ARCH, *NVCC_FLAGS, *fmad, *extra, "-c", str(src), "-o", str(obj)]
+        user = os.environ.get("CFD_NVCC_EXTRA", "").split()
+        cmd = [cc, *ARCH, *NVCC_FLAGS, *fmad, *extra, *user, "-c", str(src), "-o", str(obj)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         return src, obj, r
 

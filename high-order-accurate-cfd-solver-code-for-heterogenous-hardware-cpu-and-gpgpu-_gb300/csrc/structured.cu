@@ -27,6 +27,12 @@
 #include "lattice_fp64.cuh"
 #include "structured.h"
 
+// Minimum resident blocks per SM requested for the FP64 face kernel (its
+// register budget); 2 keeps it spill-free at 128 threads per block.
+#ifndef CFD_FACE_MIN_BLOCKS
+#define CFD_FACE_MIN_BLOCKS 2
+#endif
+
 namespace cfd {
 
 namespace {
@@ -52,7 +58,7 @@ __global__ void __launch_bounds__(128) k_mu_only(LatView g, int q)
 }
 
 template <int D>
-__global__ void __launch_bounds__(128) k_face(LatView g)
+__global__ void __launch_bounds__(128, CFD_FACE_MIN_BLOCKS) k_face(LatView g)
 {
     const int n = node_id();
     if (n < g.N) ex::face_node<D>(g, n);

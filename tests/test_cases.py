@@ -91,3 +91,13 @@ def test_request_stream_is_seeded(pkg):
     gaps = np.diff([0.0] + [r.arrival for r in a])
     assert 0.005 < gaps.mean() < 0.06
     assert {r.kind for r in a} == {"vortex", "tgv"}
+
+
+def test_tgv_initial_kinetic_energy(pkg):
+    """At t = 0 the TGV kinetic energy is 1/8 of rho V0^2 (volume average of
+    (sin x cos y cos z)^2 + (cos x sin y cos z)^2 over the box, times 1/2)."""
+    from cfd_gb300 import cases, diagnostics
+    c = cases.taylor_green(n=32, amp=0.0)
+    ke, ens = diagnostics.kinetic_energy_enstrophy(c.arrays["flow"], c.arrays["metric"], c.arrays["det"], c.shape)
+    assert abs(ke - 0.125) < 1e-12
+    assert abs(ens - 0.375) < 2e-3            # 3/8 for the analytic field, 4th-order differences

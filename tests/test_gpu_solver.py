@@ -141,3 +141,50 @@ def test_mixed_precision_rejected_on_gather_path(ctx):
     with pytest.raises(abi.CfdError) as e:
         runtime.Solver(ctx, c, precision=1)
     assert e.value.status == abi.EUNSUPPORTED
+
+
+def test_config1_vortex_64_rhs_and_100_steps(ctx, oracle_mod):
+    """Config 1 at its full size: the RHS of the 64^3 vortex against the
+    oracle, then 100 SSP-RK3 steps of the face-based path against the drop-in
+    (gather) path, an independent GPU implementation of the same kernels."""
+    from cfd_gb300 import runtime
+    c = make("vortex", n=64)
+    s = runtime.Solver(ctx, c)
+    s.set_flow(c.arrays["flow"])
+    Lg = s.stage(0, c.dt)
+    a = copy_arrays(c.arrays)
+    Lo = oracle_mod.stage(a, c.g_node, c.sd_node, c.params, 0, c.dt, want_L=True)
+    own = slice(1, c.sd_node + 1)
+    assert rel_l2(Lg[own], Lo[own]) <= TOL
+    s.close()
+    out = []
+    for force in (1, 0):
+        s = runtime.Solver(ctx, c, force_path=force)
+        s.set_flow(c.arrays["flow"])
+        s.step(c.dt, 100)
+        out.append((s.get_flow()[own], s.get_u0()[own]))
+        s.close()
+    assert rel_l2(out[0][0], out[1][0]) <= TOL
+    assert rel_l2(out[0][1], out[1][1]) <= TOL
+    m0 = c.arrays["det"][own] @ c.arrays["flow"][own][:, 5]
+    assert abs(out[0][1][:, 0].sum() - m0) <= 1e-12 * m0        # mass conserved over 100 steps
+
+
+def test_tgv_kinetic_energy_and_enstrophy_mixed_vs_fp64(ctx):
+    """Config 2's diagnostics on a reduced grid: kinetic energy and enstrophy
+    of the mixed form track the FP64 form to within 1e-6 relative."""
+    from cfd_gb300 import diagnostics, runtime
+    c = make("tgv", n=24)
+    hist = []
+    for prec in (0, 1):
+        s = runtime.Solver(ctx, c, precision=prec)
+        s.set_flow(c.arrays["flow"])
+        h = []
+        for _ in range(4):
+            s.step(c.dt, 5)
+            h.append(diagnostics.kinetic_energy_enstrophy(s.get_flow(), c.arrays["metric"], c.arrays["det"], c.shape))
+        hist.append(np.array(h))
+        s.close()
+    err = np.abs(hist[1] - hist[0]) / np.abs(hist[0])
+    assert err.max() <= 1e-6, err
+    assert hist[0][-1, 0] < hist[0][0, 0]                  # kinetic energy decays (viscous + SGS)
