@@ -68,7 +68,7 @@ unsigned *slot_flags(cfd_batch *b, int slot) { return b->d_words + 4 + slot; }
 uint64_t instance_bytes(int precision, int64_t N)
 {
     const uint64_t doubles = (22 + 9 + 15) * (uint64_t)N + 14 * (uint64_t)(N + 1);
-    if (precision == CFD_PREC_MIXED) return doubles * 8 + (12 + 55) * (uint64_t)N * 4;
+    if (precision == CFD_PREC_MIXED) return (doubles + (uint64_t)N) * 8 + (12 + 9 + 55) * (uint64_t)N * 4;
     return (doubles + 52 * (uint64_t)N) * 8;
 }
 
@@ -350,8 +350,10 @@ cfd_status_t cfd_batch_add(cfd_batch_t *b, const cfd_geometry_t *geom, const cfd
     v.flags = slot_flags(b, slot);
     v.Lout = nullptr;
     if (b->precision == CFD_PREC_MIXED) {
-        float *fm32, *fdet32;
-        if ((st = ialloc(b, I, 9 * Nz, &fm32)) || (st = ialloc(b, I, 3 * Nz, &fdet32)) || (st = ialloc(b, I, 5 * Nz, &v.Q32))
+        float *fm32, *fdet32, *m932;
+        double *idet;
+        if ((st = ialloc(b, I, 9 * Nz, &fm32)) || (st = ialloc(b, I, 3 * Nz, &fdet32)) || (st = ialloc(b, I, 9 * Nz, &m932))
+            || (st = ialloc(b, I, Nz, &idet)) || (st = ialloc(b, I, 5 * Nz, &v.Q32))
             || (st = ialloc(b, I, 5 * Nz, &v.R32)) || (st = ialloc(b, I, 15 * Nz, &v.FEG32))
             || (st = ialloc(b, I, 15 * Nz, &v.V32)) || (st = ialloc(b, I, 15 * Nz, &v.Fh32))) {
             free_instance(I);
@@ -359,6 +361,8 @@ cfd_status_t cfd_batch_add(cfd_batch_t *b, const cfd_geometry_t *geom, const cfd
         }
         v.fm32 = fm32;
         v.fdet32 = fdet32;
+        v.m9_32 = m932;
+        v.idet = idet;
     } else {
         if ((st = ialloc(b, I, 5 * Nz, &v.Q)) || (st = ialloc(b, I, 15 * Nz, &v.FEG)) || (st = ialloc(b, I, 15 * Nz, &v.V))
             || (st = ialloc(b, I, 2 * Nz, &v.sh)) || (st = ialloc(b, I, 15 * Nz, &v.Fh))) {
@@ -394,14 +398,18 @@ cfd_status_t cfd_batch_add(cfd_batch_t *b, const cfd_geometry_t *geom, const cfd
         S.stream = sm;
         S.fm = fm;
         S.fdet = fdet;
+        S.m9 = m9;
+        S.det = det;
         S.fm32 = const_cast<float *>(v.fm32);
         S.fdet32 = const_cast<float *>(v.fdet32);
+        S.m932 = const_cast<float *>(v.m9_32);
+        S.idet = const_cast<double *>(v.idet);
         mixed_geometry(S);
         batch_prep_mixed(v, sm);
     } else {
         batch_prep_fp64(v, sm);
     }
-    ctx->launches += 2;
+    ctx->launches += b->precision == CFD_PREC_MIXED ? 2 + kMixedGeometryLaunches : 2;
     e = cudaStreamSynchronize(sm);   // host geometry vectors go out of scope
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) {

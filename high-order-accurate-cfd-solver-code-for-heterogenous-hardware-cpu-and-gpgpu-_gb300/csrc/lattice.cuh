@@ -18,6 +18,8 @@ struct LatView {
     // geometry (FP64), and FP32 copies of the face terms for the mixed form
     const double *m9, *det, *fm, *fdet;
     const float *fm32, *fdet32;
+    const float *m9_32;        // FP32 node metrics (mixed form)
+    const double *idet;        // 1/det (mixed form)
     // state
     double *prim9;             // FLOW fields u,v,w,p,t,rho,mu,a,e
     double *U0, *U1, *U2;

@@ -20,7 +20,7 @@ __device__ __forceinline__ void prep_values(const LatView &g, int n, int q, doub
     const int N = g.N;
     const double D = g.det[n];
     const double ke = 0.5 * rho * (u * u + v * v + w * w);
-    const double E = (p / 0.4) + ke;
+    const double E = p * 2.5 + ke;
     double *Uq = lat_U(g, q);
     Uq[0 * N + n] = D * rho;
     Uq[1 * N + n] = D * rho * u;
@@ -40,7 +40,7 @@ __device__ __forceinline__ void prep_values(const LatView &g, int n, int q, doub
     g.R32[4 * N + n] = (float)(E + p) / rf;
     float m[9];
 #pragma unroll
-    for (int c = 0; c < 9; ++c) m[c] = (float)g.m9[c * N + n];
+    for (int c = 0; c < 9; ++c) m[c] = g.m9_32[c * N + n];
     const float prim[5] = {rf, (float)u, (float)v, (float)w, (float)p};
     float F[5], Ec[5], G[5];
     node_inviscid_flux<float>(prim, m, (float)D, F, Ec, G);
@@ -84,7 +84,7 @@ __device__ __forceinline__ void visc_node(const LatView &g, int n, int q)
     }
     float m[9];
 #pragma unroll
-    for (int c = 0; c < 9; ++c) m[c] = (float)g.m9[c * N + n];
+    for (int c = 0; c < 9; ++c) m[c] = g.m9_32[c * N + n];
     const float prim[5] = {(float)g.prim9[LF_RHO * N + n], (float)g.prim9[LF_U * N + n], (float)g.prim9[LF_V * N + n],
                            (float)g.prim9[LF_W * N + n], (float)g.prim9[LF_P * N + n]};
     float Fv[5], Ev[5], Gv[5], mu;
@@ -146,29 +146,43 @@ __device__ __forceinline__ void face_node(const LatView &g, int n)
     }
 }
 
-// RHS sum and SSP-RK3 stage in FP64 from the FP32 face and viscous fluxes;
-// with fuse_next, the next stage's prep on the new primitives.
+// 1/x in FP64 from an FP32 seed and two Newton steps (relative error near
+// FP64 rounding; the mixed form does not need the correctly rounded value).
+__device__ __forceinline__ double recip_fast(double x)
+{
+    double r = (double)(1.0f / (float)x);
+    r = r * fma(-x, r, 2.0);
+    r = r * fma(-x, r, 2.0);
+    return r;
+}
+
+// RHS and SSP-RK3 stage from the FP32 face and viscous fluxes.  L is summed
+// in FP32: neighbouring face fluxes are within a factor of two of each other,
+// so their FP32 difference is exact, and L's error is dominated by the FP32
+// face fluxes themselves.  The RK accumulation and the state are FP64.  With
+// fuse_next, the next stage's prep on the new primitives.
 __device__ __forceinline__ void update_node(const LatView &g, int n, int jst, bool fuse_next)
 {
     const int N = g.N;
     int i, j, k;
     lat_ijk(g, n, i, j, k);
-    double L[5] = {0, 0, 0, 0, 0};
+    float Lf[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const int m1 = lat_step(g, i, j, k, d, -1);
 #pragma unroll
-        for (int c = 0; c < 5; ++c) L[c] += (double)g.Fh32[(d * 5 + c) * N + n] - (double)g.Fh32[(d * 5 + c) * N + m1];
+        for (int c = 0; c < 5; ++c) Lf[c] += g.Fh32[(d * 5 + c) * N + n] - g.Fh32[(d * 5 + c) * N + m1];
         if (g.P.viscous) {
             const int m2 = lat_step(g, i, j, k, d, -2), p1 = lat_step(g, i, j, k, d, 1), p2 = lat_step(g, i, j, k, d, 2);
             const float *Vd = g.V32 + (size_t)d * 5 * N;
 #pragma unroll
             for (int c = 0; c < 5; ++c)
-                L[c] += (double)((1.0f / 12.0f) * (8.0f * (Vd[c * N + p1] - Vd[c * N + m1]) - (Vd[c * N + p2] - Vd[c * N + m2])));
+                Lf[c] += (1.0f / 12.0f) * (8.0f * (Vd[c * N + p1] - Vd[c * N + m1]) - (Vd[c * N + p2] - Vd[c * N + m2]));
         }
     }
+    double L[5];
 #pragma unroll
-    for (int c = 0; c < 5; ++c) L[c] = -L[c];
+    for (int c = 0; c < 5; ++c) L[c] = -(double)Lf[c];
     if (g.Lout) {
 #pragma unroll
         for (int c = 0; c < 5; ++c) g.Lout[c * N + n] = L[c];
@@ -191,21 +205,23 @@ __device__ __forceinline__ void update_node(const LatView &g, int n, int jst, bo
 #pragma unroll
         for (int c = 0; c < 5; ++c) Uo[c * N + n] = Un[c];
     }
-    const double idet = 1.0 / g.det[n];
+    const double idet = g.idet[n];
     const double rho = idet * Un[0];
-    const double ir = 1.0 / rho;
-    const double u = (idet * Un[1]) * ir, v = (idet * Un[2]) * ir, w = (idet * Un[3]) * ir;
-    const double e = ((idet * Un[4]) * ir) - 0.5 * (u * u + v * v + w * w);
+    const double ir = recip_fast(rho);
+    const double s = idet * ir;
+    const double u = Un[1] * s, v = Un[2] * s, w = Un[3] * s;
+    const double e = Un[4] * s - 0.5 * (u * u + v * v + w * w);
     const double p = e * rho * 0.4;
     const double mach = g.P.mach;
+    const double pr = p * ir;
     g.prim9[LF_RHO * N + n] = rho;
     g.prim9[LF_U * N + n] = u;
     g.prim9[LF_V * N + n] = v;
     g.prim9[LF_W * N + n] = w;
     g.prim9[LF_E * N + n] = e;
     g.prim9[LF_P * N + n] = p;
-    g.prim9[LF_T * N + n] = (1.4 * mach * mach) * (p * ir);
-    g.prim9[LF_A * N + n] = sqrt(1.4 * p * ir);
+    g.prim9[LF_T * N + n] = (1.4 * mach * mach) * pr;
+    g.prim9[LF_A * N + n] = (double)sqrtf(1.4f * (float)pr);
     if (!(isfinite(rho) && isfinite(u) && isfinite(v) && isfinite(w) && isfinite(p))) atomicOr(g.flags, 2u);
     // the next stage's U_Q overwrites U_{jst+1} (mod 3) with det*Q(FLOW)
     if (fuse_next) prep_values(g, n, jst == 2 ? 0 : jst + 1, rho, u, v, w, p);

@@ -54,6 +54,18 @@ __global__ void __launch_bounds__(256) k_update_m(LatView g, int jst)
     if (n < g.N) mx::update_node(g, n, jst, false);
 }
 
+__global__ void __launch_bounds__(256) k_update_prep_m(LatView g, int jst)
+{
+    const int n = node_id();
+    if (n < g.N) mx::update_node(g, n, jst, true);
+}
+
+__global__ void k_recip(const double *__restrict__ a, double *__restrict__ b, long long n)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) b[t] = 1.0 / a[t];
+}
+
 __global__ void k_to_float(const double *__restrict__ a, float *__restrict__ b, long long n)
 {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -67,33 +79,56 @@ void mixed_geometry(const StructuredLaunch &S)
     const long long N = (long long)S.ni * S.nj * S.nk;
     k_to_float<<<blocks_for(9 * N, 256), 256, 0, S.stream>>>(S.fm, S.fm32, 9 * N);
     k_to_float<<<blocks_for(3 * N, 256), 256, 0, S.stream>>>(S.fdet, S.fdet32, 3 * N);
+    k_to_float<<<blocks_for(9 * N, 256), 256, 0, S.stream>>>(S.m9, S.m932, 9 * N);
+    k_recip<<<blocks_for(N, 256), 256, 0, S.stream>>>(S.det, S.idet, N);
 }
 
-void mixed_stage(const StructuredLaunch &S, int jst, double dt, double *Lout, cudaEvent_t *ev)
+int mixed_stage(const StructuredLaunch &S, int jst, double dt, double *Lout, cudaEvent_t *ev, bool prep, bool fuse,
+                const char **names)
 {
     const LatView g = make_view(S, dt, Lout);
     const unsigned nb256 = blocks_for(g.N, 256), nb128 = blocks_for(g.N, 128);
     cudaStream_t st = S.stream;
-    int e = 0;
+    int e = 0, k = 0;
     auto mark = [&]() {
         if (ev) cudaEventRecord(ev[e++], st);
     };
+    auto name = [&](const char *nm) {
+        if (names) names[k] = nm;
+        ++k;
+    };
     mark();
-    k_prep_m<<<nb256, 256, 0, st>>>(g, jst);
-    mark();
-    if (S.P.viscous)
+    if (prep) {
+        k_prep_m<<<nb256, 256, 0, st>>>(g, jst);
+        name("prep");
+        mark();
+    }
+    if (S.P.viscous) {
         k_visc_m<<<nb256, 256, 0, st>>>(g, jst);
-    else
+        name("viscous");
+    } else {
         k_mu_m<<<nb256, 256, 0, st>>>(g, jst);
+        name("mu_only");
+    }
     mark();
     k_face_m<0><<<nb128, 128, 0, st>>>(g);
+    name("face_i");
     mark();
     k_face_m<1><<<nb128, 128, 0, st>>>(g);
+    name("face_j");
     mark();
     k_face_m<2><<<nb128, 128, 0, st>>>(g);
+    name("face_k");
     mark();
-    k_update_m<<<nb256, 256, 0, st>>>(g, jst);
+    if (fuse) {
+        k_update_prep_m<<<nb256, 256, 0, st>>>(g, jst);
+        name("update+prep");
+    } else {
+        k_update_m<<<nb256, 256, 0, st>>>(g, jst);
+        name("update");
+    }
     mark();
+    return k;
 }
 
 }  // namespace cfd

@@ -40,6 +40,7 @@ struct cfd_solver {
     double *stage9 = nullptr;   // AoS staging, rows 0..N, 9 doubles
     double *stage5 = nullptr;   // AoS staging, rows 0..N, 5 doubles
     double *Lsoa = nullptr;
+    int prep_ready = -1;        // mixed form: stage whose U_Q outputs are current
 };
 
 namespace {
@@ -115,7 +116,8 @@ cfd_status_t create_structured(cfd_solver *s, const cfd_geometry_t *g)
     if (s->mixed) {   // FP32 stage intermediates
         if ((st = dalloc_t(s, 5 * N, &S.Q32)) || (st = dalloc_t(s, 5 * N, &S.R32)) || (st = dalloc_t(s, 15 * N, &S.FEG32))
             || (st = dalloc_t(s, 15 * N, &S.V32)) || (st = dalloc_t(s, 15 * N, &S.Fh32))
-            || (st = dalloc_t(s, 9 * N, &S.fm32)) || (st = dalloc_t(s, 3 * N, &S.fdet32)))
+            || (st = dalloc_t(s, 9 * N, &S.fm32)) || (st = dalloc_t(s, 3 * N, &S.fdet32))
+            || (st = dalloc_t(s, 9 * N, &S.m932)) || (st = dalloc_t(s, N, &S.idet)))
             return st;
         cudaMemsetAsync(S.V32, 0, 15 * N * sizeof(float), S.stream);
     } else {          // FP64 stage intermediates
@@ -137,7 +139,10 @@ cfd_status_t create_structured(cfd_solver *s, const cfd_geometry_t *g)
     S.det = det;
     S.fm = fm;
     S.fdet = fdet;
-    if (s->mixed) mixed_geometry(S);
+    if (s->mixed) {
+        mixed_geometry(S);
+        s->ctx->launches += kMixedGeometryLaunches;
+    }
     cudaError_t e = cudaStreamSynchronize(S.stream);   // host vectors go out of scope
     if (e != cudaSuccess) return cuda_fail(s->ctx, e, "solver create sync");
     return CFD_OK;
@@ -148,8 +153,10 @@ cfd_status_t run_stage(cfd_solver *s, int j, double dt, bool want_L)
     cfd_ctx *ctx = s->ctx;
     s->S.stream = ctx->stream;   // the context's stream may have been replaced
     if (s->path == CFD_PATH_STRUCTURED) {
-        structured_stage(s->S, j, dt, want_L ? s->Lsoa : nullptr);
-        ctx->launches += structured_launches_per_stage();
+        const bool mixed = s->S.mixed != 0;
+        ctx->launches += structured_stage(s->S, j, dt, want_L ? s->Lsoa : nullptr, nullptr, nullptr,
+                                          !mixed || s->prep_ready != j, mixed);
+        if (mixed) s->prep_ready = j == 2 ? 0 : j + 1;
     } else {
         double *Uj = s->U[j];
         launch_uq(ctx->stream, Uj, s->Q, s->grid, s->det, s->flow, s->roe, s->g_node + 1, s->n_rows, ctx->d_flags);
@@ -254,6 +261,7 @@ cfd_status_t cfd_solver_set_flow(cfd_solver_t *s, const cfd_flow_t *flow_host)
     } else {
         const long long N = (long long)s->ni * s->nj * s->nk;
         s->S.stream = s->ctx->stream;
+        s->prep_ready = -1;
         st = upload(s, s->stage9, flow_host, R * sizeof(cfd_flow_t));
         if (st == CFD_OK) aos_to_soa(s->ctx->stream, s->stage9, 9, 9, N, s->S.prim9);
     }
@@ -332,11 +340,14 @@ cfd_status_t cfd_solver_profile_stage(cfd_solver_t *s, int32_t j, double del_t, 
     if (st != CFD_OK) return st;
     cudaStream_t stream = s->ctx->stream;
     s->S.stream = stream;
-    const int nk = s->path == CFD_PATH_STRUCTURED ? structured_launches_per_stage() : 3;
-    std::vector<cudaEvent_t> ev(nk + 1);
+    std::vector<cudaEvent_t> ev(kMaxStageLaunches + 1);
     for (auto &e : ev) cudaEventCreate(&e);
+    const char *snames[kMaxStageLaunches] = {};
+    int nk = 3;
     if (s->path == CFD_PATH_STRUCTURED) {
-        structured_stage(s->S, j, del_t, nullptr, ev.data());
+        const bool mixed = s->S.mixed != 0;
+        nk = structured_stage(s->S, j, del_t, nullptr, ev.data(), snames, !mixed || s->prep_ready != j, mixed);
+        if (mixed) s->prep_ready = j == 2 ? 0 : j + 1;
     } else {
         cudaEventRecord(ev[0], stream);
         double *Uj = s->U[j];
@@ -349,16 +360,18 @@ cfd_status_t cfd_solver_profile_stage(cfd_solver_t *s, int32_t j, double del_t, 
                     s->metric, s->roe, s->Fv, s->Ev, s->Gv, s->F, s->E, s->G, s->flow, s->sd_node + 1, s->n_rows,
                     s->ctx->d_flags, nullptr);
         cudaEventRecord(ev[3], stream);
+        snames[0] = "uq";
+        snames[1] = "viscous";
+        snames[2] = "weno";
     }
     s->ctx->launches += nk;
     cudaError_t e = cudaEventSynchronize(ev[nk]);
     if (e == cudaSuccess) {
-        const char *gnames[3] = {"uq", "viscous", "weno"};
         const int n = nk < max_out ? nk : max_out;
         for (int i = 0; i < n; ++i) {
             float ms = 0;
             cudaEventElapsedTime(&ms, ev[i], ev[i + 1]);
-            const char *nm = s->path == CFD_PATH_STRUCTURED ? structured_kernel_name(i, s->P.viscous != 0) : gnames[i];
+            const char *nm = snames[i] ? snames[i] : "?";
             std::strncpy(out[i].name, nm, sizeof out[i].name - 1);
             out[i].name[sizeof out[i].name - 1] = 0;
             out[i].ms = ms;

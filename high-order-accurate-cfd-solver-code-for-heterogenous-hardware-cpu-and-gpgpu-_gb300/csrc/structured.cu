@@ -91,12 +91,10 @@ __global__ void k_soa_to_aos(const double *__restrict__ soa, int stride, int nco
 
 }  // namespace
 
-void structured_stage(const StructuredLaunch &S, int jst, double dt, double *Lout, cudaEvent_t *ev)
+int structured_stage(const StructuredLaunch &S, int jst, double dt, double *Lout, cudaEvent_t *ev,
+                     const char **names, bool prep, bool fuse)
 {
-    if (S.mixed) {
-        mixed_stage(S, jst, dt, Lout, ev);
-        return;
-    }
+    if (S.mixed) return mixed_stage(S, jst, dt, Lout, ev, prep, fuse, names);
     const LatView g = make_view(S, dt, Lout);
     const unsigned nb = blocks_for(g.N, 128);
     cudaStream_t st = S.stream;
@@ -104,6 +102,10 @@ void structured_stage(const StructuredLaunch &S, int jst, double dt, double *Lou
     auto mark = [&]() {
         if (ev) cudaEventRecord(ev[e++], st);
     };
+    static const char *fp64_names[6] = {"prep", "viscous", "face_i", "face_j", "face_k", "update"};
+    if (names)
+        for (int i = 0; i < 6; ++i) names[i] = fp64_names[i];
+    if (names && !S.P.viscous) names[1] = "mu_only";
     mark();
     k_prep<<<nb, 128, 0, st>>>(g, jst);
     mark();
@@ -120,16 +122,8 @@ void structured_stage(const StructuredLaunch &S, int jst, double dt, double *Lou
     mark();
     k_update<<<nb, 128, 0, st>>>(g, jst);
     mark();
+    return 6;
 }
-
-const char *structured_kernel_name(int i, bool viscous)
-{
-    static const char *names[6] = {"prep", "viscous", "face_i", "face_j", "face_k", "update"};
-    if (i == 1 && !viscous) return "mu_only";
-    return (i >= 0 && i < 6) ? names[i] : "?";
-}
-
-int structured_launches_per_stage() { return 6; }
 
 void aos_to_soa(cudaStream_t st, const double *aos, int stride, int ncomp, long long N, double *soa)
 {

@@ -34,13 +34,22 @@ struct StructuredLaunch {
     float *Fh32 = nullptr;     // [3][5][N]
     float *fm32 = nullptr;     // [3][3][N]
     float *fdet32 = nullptr;   // [3][N]
+    float *m932 = nullptr;     // [9][N] node metrics
+    double *idet = nullptr;    // [N] 1/det
 };
 
 // The three face-flux launches of the mixed-precision form (mixed.cu).
-// Mixed-precision stage (mixed.cu): same launch count and order as the FP64
-// stage; ev as for structured_stage.
-void mixed_stage(const StructuredLaunch &S, int j, double dt, double *Lout, cudaEvent_t *ev);
-// FP32 copies of the face metrics and face dets (once, after upload).
+// Mixed-precision stage (mixed.cu).  With prep = false the stage's U_Q
+// outputs are taken as already produced (by the previous stage's fused
+// update); with fuse = true the update also produces the next stage's.
+// Returns the number of launches; ev (optional) gets one event before and one
+// after each launch (launches + 1 events), names[i] the launch names.
+int mixed_stage(const StructuredLaunch &S, int j, double dt, double *Lout, cudaEvent_t *ev, bool prep, bool fuse,
+                const char **names);
+// FP32 copies of the node metrics, face metrics and face dets, and 1/det
+// (once, after upload).
+// FP32 copies of the face and node metrics and 1/det (kernels launched: 4)
+constexpr int kMixedGeometryLaunches = 4;
 void mixed_geometry(const StructuredLaunch &S);
 
 // Device view of a StructuredLaunch for one stage.
@@ -59,6 +68,8 @@ inline LatView make_view(const StructuredLaunch &S, double dt, double *Lout)
     g.fdet = S.fdet;
     g.fm32 = S.fm32;
     g.fdet32 = S.fdet32;
+    g.m9_32 = S.m932;
+    g.idet = S.idet;
     g.prim9 = S.prim9;
     g.U0 = S.U[0];
     g.U1 = S.U[1];
@@ -79,11 +90,14 @@ inline LatView make_view(const StructuredLaunch &S, double dt, double *Lout)
 }
 
 // One RK stage j of the host loop; Lout (device [5][N]) may be null.
-// ev (optional) receives structured_launches_per_stage()+1 recorded events
-// bracketing the launches, for per-kernel timing.
-void structured_stage(const StructuredLaunch &S, int j, double dt, double *Lout, cudaEvent_t *ev = nullptr);
-const char *structured_kernel_name(int i, bool viscous);
-int structured_launches_per_stage();
+// Returns the number of kernel launches; ev (optional, at least
+// kMaxStageLaunches+1 entries) receives events bracketing every launch and
+// names (optional) the launch names.  prep/fuse as for mixed_stage (the FP64
+// form always runs its own prep and no fused update).
+constexpr int kMaxStageLaunches = 6;
+int structured_stage(const StructuredLaunch &S, int j, double dt, double *Lout, cudaEvent_t *ev = nullptr,
+                     const char **names = nullptr, bool prep = true, bool fuse = false);
+
 void aos_to_soa(cudaStream_t st, const double *aos, int stride, int ncomp, long long N, double *soa);
 void soa_to_aos(cudaStream_t st, const double *soa, int stride, int ncomp, long long N, double *aos);
 
