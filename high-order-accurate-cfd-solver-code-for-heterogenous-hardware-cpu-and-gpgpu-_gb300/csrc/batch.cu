@@ -68,7 +68,8 @@ unsigned *slot_flags(cfd_batch *b, int slot) { return b->d_words + 4 + slot; }
 uint64_t instance_bytes(int precision, int64_t N)
 {
     const uint64_t doubles = (22 + 9 + 15) * (uint64_t)N + 14 * (uint64_t)(N + 1);
-    if (precision == CFD_PREC_MIXED) return (doubles + (uint64_t)N) * 8 + (12 + 9 + 55) * (uint64_t)N * 4;
+    // mixed: FP32 face/node geometry (12 + 10 + 2), prim32 (9), stage intermediates (55)
+    if (precision == CFD_PREC_MIXED) return doubles * 8 + (12 + 10 + 2 + 9 + 55) * (uint64_t)N * 4;
     return (doubles + 52 * (uint64_t)N) * 8;
 }
 
@@ -226,6 +227,7 @@ std::vector<std::pair<void *, size_t>> mutable_arrays(const BatchInst &I, int pr
     std::vector<std::pair<void *, size_t>> v = {{I.view.prim9, 9 * N * 8}, {I.view.U0, 5 * N * 8},
                                                 {I.view.U1, 5 * N * 8}, {I.view.U2, 5 * N * 8}};
     if (precision == CFD_PREC_MIXED) {
+        v.push_back({I.view.prim32, 9 * N * 4});
         v.push_back({I.view.Q32, 5 * N * 4});
         v.push_back({I.view.R32, 5 * N * 4});
         v.push_back({I.view.FEG32, 15 * N * 4});
@@ -339,6 +341,8 @@ cfd_status_t cfd_batch_add(cfd_batch_t *b, const cfd_geometry_t *geom, const cfd
     v.N = N;
     v.P = make_phys(&I.prm);
     v.dt = del_t;
+    v.dt_hi = (float)del_t;
+    v.dt_lo = (float)(del_t - (double)v.dt_hi);
     v.m9 = m9;
     v.det = det;
     v.fm = fm;
@@ -350,10 +354,10 @@ cfd_status_t cfd_batch_add(cfd_batch_t *b, const cfd_geometry_t *geom, const cfd
     v.flags = slot_flags(b, slot);
     v.Lout = nullptr;
     if (b->precision == CFD_PREC_MIXED) {
-        float *fm32, *fdet32, *m932;
-        double *idet;
-        if ((st = ialloc(b, I, 9 * Nz, &fm32)) || (st = ialloc(b, I, 3 * Nz, &fdet32)) || (st = ialloc(b, I, 9 * Nz, &m932))
-            || (st = ialloc(b, I, Nz, &idet)) || (st = ialloc(b, I, 5 * Nz, &v.Q32))
+        float *fm32, *fdet32, *node32, *idet32;
+        if ((st = ialloc(b, I, 9 * Nz, &fm32)) || (st = ialloc(b, I, 3 * Nz, &fdet32))
+            || (st = ialloc(b, I, 10 * Nz, &node32)) || (st = ialloc(b, I, 2 * Nz, &idet32))
+            || (st = ialloc(b, I, 9 * Nz, &v.prim32)) || (st = ialloc(b, I, 5 * Nz, &v.Q32))
             || (st = ialloc(b, I, 5 * Nz, &v.R32)) || (st = ialloc(b, I, 15 * Nz, &v.FEG32))
             || (st = ialloc(b, I, 15 * Nz, &v.V32)) || (st = ialloc(b, I, 15 * Nz, &v.Fh32))) {
             free_instance(I);
@@ -361,8 +365,8 @@ cfd_status_t cfd_batch_add(cfd_batch_t *b, const cfd_geometry_t *geom, const cfd
         }
         v.fm32 = fm32;
         v.fdet32 = fdet32;
-        v.m9_32 = m932;
-        v.idet = idet;
+        v.node32 = node32;
+        v.idet32 = idet32;
     } else {
         if ((st = ialloc(b, I, 5 * Nz, &v.Q)) || (st = ialloc(b, I, 15 * Nz, &v.FEG)) || (st = ialloc(b, I, 15 * Nz, &v.V))
             || (st = ialloc(b, I, 2 * Nz, &v.sh)) || (st = ialloc(b, I, 15 * Nz, &v.Fh))) {
@@ -402,8 +406,8 @@ cfd_status_t cfd_batch_add(cfd_batch_t *b, const cfd_geometry_t *geom, const cfd
         S.det = det;
         S.fm32 = const_cast<float *>(v.fm32);
         S.fdet32 = const_cast<float *>(v.fdet32);
-        S.m932 = const_cast<float *>(v.m9_32);
-        S.idet = const_cast<double *>(v.idet);
+        S.node32 = const_cast<float *>(v.node32);
+        S.idet32 = const_cast<float *>(v.idet32);
         mixed_geometry(S);
         batch_prep_mixed(v, sm);
     } else {
@@ -456,6 +460,8 @@ cfd_status_t cfd_batch_get_flow(cfd_batch_t *b, int32_t slot, cfd_flow_t *host)
     if (!b || !host || slot < 0 || slot >= (int)b->slots.size() || !b->slots[slot].active) return CFD_EINVAL;
     use_device(b->ctx);
     BatchInst &I = b->slots[slot];
+    // mixed: FP64 FLOW of the hi/lo state (after whole steps it is in slot 0)
+    if (b->precision == CFD_PREC_MIXED) mixed_flow_out(I.view, 0, b->ctx->stream);
     soa_to_aos(b->ctx->stream, I.view.prim9, 9, 9, I.N, I.stage9);
     cudaError_t e = cudaMemcpyAsync(host, I.stage9, 9 * ((size_t)I.N + 1) * 8, cudaMemcpyDeviceToHost, b->ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->ctx->stream);
@@ -468,7 +474,10 @@ cfd_status_t cfd_batch_get_u0(cfd_batch_t *b, int32_t slot, cfd_column_t *host)
     if (!b || !host || slot < 0 || slot >= (int)b->slots.size() || !b->slots[slot].active) return CFD_EINVAL;
     use_device(b->ctx);
     BatchInst &I = b->slots[slot];
-    soa_to_aos(b->ctx->stream, I.view.U0, 5, 5, I.N, I.stage5);
+    if (b->precision == CFD_PREC_MIXED)
+        mixed_u_out(I.view, 0, I.stage5, b->ctx->stream);
+    else
+        soa_to_aos(b->ctx->stream, I.view.U0, 5, 5, I.N, I.stage5);
     cudaError_t e = cudaMemcpyAsync(host, I.stage5, 5 * ((size_t)I.N + 1) * 8, cudaMemcpyDeviceToHost, b->ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->ctx->stream);
     if (e != cudaSuccess) return cuda_fail(b->ctx, e, "cfd_batch_get_u0");

@@ -11,17 +11,23 @@
 namespace cfd {
 
 // Field layout: every array is [component][N], n = i + ni*(j + nj*k).
+//
+// Mixed form: U0/U1/U2 hold each conserved value as an unevaluated sum of
+// two FP32 numbers (hi + lo, about 48 significant bits) in the same bytes as
+// the FP64 form's [5][N] doubles: hi at [c][N], lo at [5 + c][N].
 struct LatView {
     int ni, nj, nk, N;
     Phys P;
     double dt;
-    // geometry (FP64), and FP32 copies of the face terms for the mixed form
+    float dt_hi, dt_lo;        // dt as hi + lo (mixed form)
+    // geometry (FP64), and FP32 copies for the mixed form
     const double *m9, *det, *fm, *fdet;
     const float *fm32, *fdet32;
-    const float *m9_32;        // FP32 node metrics (mixed form)
-    const double *idet;        // 1/det (mixed form)
+    const float *node32;       // [10][N] 9 node metrics, then det (mixed form)
+    const float *idet32;       // [2][N] 1/det as hi, lo (mixed form)
     // state
     double *prim9;             // FLOW fields u,v,w,p,t,rho,mu,a,e
+    float *prim32;             // the same fields in FP32 (mixed form)
     double *U0, *U1, *U2;
     // FP64 stage intermediates
     double *Q, *FEG, *V, *sh, *Fh;
@@ -60,5 +66,8 @@ __device__ __forceinline__ int lat_step(const LatView &g, int i, int j, int k, i
 }
 
 __device__ __forceinline__ double *lat_U(const LatView &g, int q) { return q == 0 ? g.U0 : (q == 1 ? g.U1 : g.U2); }
+
+// mixed form: the hi/lo view of U slot q ([10][N] floats)
+__device__ __forceinline__ float *lat_W(const LatView &g, int q) { return reinterpret_cast<float *>(lat_U(g, q)); }
 
 }  // namespace cfd

@@ -1,9 +1,19 @@
 // lattice_mixed.cuh -- per-node operations of the mixed-precision lattice
-// stage.  FP32: characteristic projection, WENO5, LLF, face and node fluxes,
-// viscous/SGS fluxes.  FP64: the state U0/U1/U2 and FLOW, the RHS sum and RK
-// accumulation, the derivatives of U feeding the viscous terms, and the
-// geometry inputs.  Include only from translation units compiled with FMA
-// contraction and approximate FP32 division/square root.
+// stage, written for a part whose FP64 rate is a small fraction of its FP32
+// rate.
+//
+// State: each conserved value of U0/U1/U2 is carried as hi + lo, two FP32
+// numbers (about 48 significant bits; double-float arithmetic after Dekker,
+// "A floating-point technique for extending the available precision", 1971,
+// with the FMA-based exact product).  The RK3 accumulation runs in that
+// arithmetic on the FP32 pipe.
+// FP32: characteristic projection, WENO5, LLF, face and node fluxes, the
+// viscous/SGS fluxes, the right-hand side sum, and the primitives derived
+// from the state each stage (rounded once from hi/lo quotients).
+// FP64 only at the boundary: FLOW in (kPrepFromFlow) and FLOW/U out.
+// Include only from translation units compiled with FMA contraction and
+// approximate FP32 division/square root; the hi/lo routines below use
+// explicit fmaf and plain additions, which contraction leaves exact.
 #pragma once
 
 #include "lattice.cuh"
@@ -11,104 +21,237 @@
 namespace cfd {
 namespace mx {
 
-// U_Q for one node from primitives in registers: U_q = det*Q (FP64) and the
-// FP32 inputs of the face stage: Q, Roe inputs (u, v, w, sqrt(rho), H), node
-// fluxes.
-__device__ __forceinline__ void prep_values(const LatView &g, int n, int q, double rho, double u, double v, double w,
-                                            double p)
+struct dfl {
+    float h, l;
+};
+
+// s + e == a + b exactly (Knuth's two-sum)
+__device__ __forceinline__ dfl two_sum(float a, float b)
+{
+    const float s = a + b;
+    const float bb = s - a;
+    const float e = (a - (s - bb)) + (b - bb);
+    return {s, e};
+}
+
+// s + e == a + b exactly when |a| >= |b| or a == 0 (Dekker's fast two-sum)
+__device__ __forceinline__ dfl quick_two_sum(float a, float b)
+{
+    const float s = a + b;
+    return {s, b - (s - a)};
+}
+
+__device__ __forceinline__ dfl df_add(dfl x, dfl y)
+{
+    const dfl s = two_sum(x.h, y.h);
+    const dfl t = two_sum(x.l, y.l);
+    dfl v = quick_two_sum(s.h, s.l + t.h);
+    return quick_two_sum(v.h, t.l + v.l);
+}
+
+// x * c, c given as hi + lo
+__device__ __forceinline__ dfl df_mul(dfl x, dfl c)
+{
+    const float p = x.h * c.h;
+    float e = fmaf(x.h, c.h, -p);
+    e = fmaf(x.h, c.l, fmaf(x.l, c.h, e));
+    return quick_two_sum(p, e);
+}
+
+// x * c rounded once to FP32
+__device__ __forceinline__ float df_mul_f(dfl x, dfl c)
+{
+    return fmaf(x.h, c.h, fmaf(x.h, c.l, x.l * c.h));
+}
+
+// a / b rounded to FP32 (within about one ulp), r an approximation of 1/b.h
+__device__ __forceinline__ float df_div_f(dfl a, dfl b, float r)
+{
+    const float q = a.h * r;
+    const float rem = fmaf(-q, b.h, a.h) + (a.l - q * b.l);
+    return fmaf(rem, r, q);
+}
+
+// a / b as hi + lo (error near 2^-44 relative)
+__device__ __forceinline__ dfl df_div(dfl a, dfl b, float r)
+{
+    const float q = df_div_f(a, b, r);
+    const float p = q * b.h;
+    const float pe = fmaf(q, b.h, -p);
+    // remainder a - q*b, then one correction step
+    const float rem = ((a.h - p) - pe) + (a.l - q * b.l);
+    return quick_two_sum(q, rem * r);
+}
+
+// 1/3 and 2/3 as hi + lo
+constexpr float kThirdH = (float)(1.0 / 3.0);
+constexpr float kThirdL = (float)(1.0 / 3.0 - (double)(float)(1.0 / 3.0));
+constexpr float kTwoThirdH = (float)(2.0 / 3.0);
+constexpr float kTwoThirdL = (float)(2.0 / 3.0 - (double)(float)(2.0 / 3.0));
+// gamma - 1 = 0.4 as hi + lo
+constexpr float kGm1H = (float)0.4;
+constexpr float kGm1L = (float)(0.4 - (double)(float)0.4);
+
+__device__ __forceinline__ void load_state(const LatView &g, int q, int n, dfl Un[5])
 {
     const int N = g.N;
-    const double D = g.det[n];
-    const double ke = 0.5 * rho * (u * u + v * v + w * w);
-    const double E = p * 2.5 + ke;
-    double *Uq = lat_U(g, q);
-    Uq[0 * N + n] = D * rho;
-    Uq[1 * N + n] = D * rho * u;
-    Uq[2 * N + n] = D * rho * v;
-    Uq[3 * N + n] = D * rho * w;
-    Uq[4 * N + n] = D * E;
-    g.Q32[0 * N + n] = (float)rho;
-    g.Q32[1 * N + n] = (float)(rho * u);
-    g.Q32[2 * N + n] = (float)(rho * v);
-    g.Q32[3 * N + n] = (float)(rho * w);
-    g.Q32[4 * N + n] = (float)E;
-    const float rf = (float)rho;
-    g.R32[0 * N + n] = (float)u;
-    g.R32[1 * N + n] = (float)v;
-    g.R32[2 * N + n] = (float)w;
-    g.R32[3 * N + n] = sqrtf(rf);
-    g.R32[4 * N + n] = (float)(E + p) / rf;
-    float m[9];
+    const float *W = lat_W(g, q);
 #pragma unroll
-    for (int c = 0; c < 9; ++c) m[c] = g.m9_32[c * N + n];
-    const float prim[5] = {rf, (float)u, (float)v, (float)w, (float)p};
-    float F[5], Ec[5], G[5];
-    node_inviscid_flux<float>(prim, m, (float)D, F, Ec, G);
+    for (int c = 0; c < 5; ++c) Un[c] = {W[c * N + n], W[(5 + c) * N + n]};
+}
+
+__device__ __forceinline__ void store_state(const LatView &g, int q, int n, const dfl Un[5])
+{
+    const int N = g.N;
+    float *W = lat_W(g, q);
 #pragma unroll
     for (int c = 0; c < 5; ++c) {
-        g.FEG32[(0 * 5 + c) * N + n] = F[c];
-        g.FEG32[(1 * 5 + c) * N + n] = Ec[c];
-        g.FEG32[(2 * 5 + c) * N + n] = G[c];
+        W[c * N + n] = Un[c].h;
+        W[(5 + c) * N + n] = Un[c].l;
     }
 }
 
-__device__ __forceinline__ void prep_node(const LatView &g, int n, int q)
+// U_Q of the next stage from the state Un (= det * Q): the FP32 primitives
+// (prim32 rho,u,v,w,e,p,t,a), and the inputs of the face stage: Q, the Roe
+// inputs (u, v, w, sqrt(rho), H) and the contravariant node fluxes.
+__device__ __forceinline__ void derive(const LatView &g, int n, const dfl Un[5])
 {
     const int N = g.N;
-    prep_values(g, n, q, g.prim9[LF_RHO * N + n], g.prim9[LF_U * N + n], g.prim9[LF_V * N + n],
-                g.prim9[LF_W * N + n], g.prim9[LF_P * N + n]);
+    const dfl idet = {g.idet32[n], g.idet32[N + n]};
+    const float r0 = 1.0f / Un[0].h;
+    const float rho = df_mul_f(Un[0], idet);
+    const float u = df_div_f(Un[1], Un[0], r0), v = df_div_f(Un[2], Un[0], r0), w = df_div_f(Un[3], Un[0], r0);
+    const float ke = 0.5f * (u * u + v * v + w * w);
+    const dfl q4 = df_div(Un[4], Un[0], r0);   // E / rho
+    const dfl e2 = df_add(q4, {-ke, 0.0f});
+    const float e = e2.h + e2.l;
+    const dfl rho2 = df_mul(Un[0], idet);
+    const float p = df_mul_f(df_mul(rho2, e2), {kGm1H, kGm1L});
+    const float irho = 1.0f / rho;
+    const float pr = p * irho;
+    const float mach = (float)g.P.mach;
+    float *F = g.prim32;
+    F[LF_RHO * N + n] = rho;
+    F[LF_U * N + n] = u;
+    F[LF_V * N + n] = v;
+    F[LF_W * N + n] = w;
+    F[LF_E * N + n] = e;
+    F[LF_P * N + n] = p;
+    F[LF_T * N + n] = (1.4f * mach * mach) * pr;
+    F[LF_A * N + n] = sqrtf(1.4f * pr);
+    if (!(isfinite(rho) && isfinite(u) && isfinite(v) && isfinite(w) && isfinite(p))) atomicOr(g.flags, 2u);
+    const float E = df_mul_f(Un[4], idet);
+    g.Q32[0 * N + n] = rho;
+    g.Q32[1 * N + n] = df_mul_f(Un[1], idet);
+    g.Q32[2 * N + n] = df_mul_f(Un[2], idet);
+    g.Q32[3 * N + n] = df_mul_f(Un[3], idet);
+    g.Q32[4 * N + n] = E;
+    g.R32[0 * N + n] = u;
+    g.R32[1 * N + n] = v;
+    g.R32[2 * N + n] = w;
+    g.R32[3 * N + n] = sqrtf(rho);
+    g.R32[4 * N + n] = q4.h + (q4.l + pr);     // H = E/rho + p/rho
+    float m[9];
+#pragma unroll
+    for (int c = 0; c < 9; ++c) m[c] = g.node32[c * N + n];
+    const float prim[5] = {rho, u, v, w, p};
+    float Fx[5], Ex[5], Gx[5];
+    node_inviscid_flux<float>(prim, m, g.node32[9 * N + n], Fx, Ex, Gx);
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+        g.FEG32[(0 * 5 + c) * N + n] = Fx[c];
+        g.FEG32[(1 * 5 + c) * N + n] = Ex[c];
+        g.FEG32[(2 * 5 + c) * N + n] = Gx[c];
+    }
 }
 
-// Viscous + MTS SGS fluxes: derivatives of U_q in FP64, the rest in FP32.
+// U_Q from the FP64 FLOW (after an upload): U = det * Q(FLOW) in FP64, split
+// into hi + lo in slot q, then derive.
+__device__ __forceinline__ void init_node(const LatView &g, int n, int q)
+{
+    const int N = g.N;
+    const double rho = g.prim9[LF_RHO * N + n], u = g.prim9[LF_U * N + n], v = g.prim9[LF_V * N + n],
+                 w = g.prim9[LF_W * N + n], p = g.prim9[LF_P * N + n];
+    const double D = g.det[n];
+    const double E = p / 0.4 + 0.5 * rho * (u * u + v * v + w * w);
+    const double U[5] = {D * rho, D * rho * u, D * rho * v, D * rho * w, D * E};
+    dfl Un[5];
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+        Un[c].h = (float)U[c];
+        Un[c].l = (float)(U[c] - (double)Un[c].h);
+    }
+    store_state(g, q, n, Un);
+    g.prim32[LF_MU * N + n] = (float)g.prim9[LF_MU * N + n];
+    derive(g, n, Un);
+}
+
+// U_Q from the state in slot src, copied to slot dst (a stage run out of the
+// usual order: U_dst = det * Q(FLOW) with FLOW the current state).
+__device__ __forceinline__ void prep_node(const LatView &g, int n, int src, int dst)
+{
+    dfl Un[5];
+    load_state(g, src, n, Un);
+    if (src != dst) store_state(g, dst, n, Un);
+    derive(g, n, Un);
+}
+
+// Viscous + MTS SGS fluxes from slot q.  Derivatives of U from hi/lo
+// differences (exact hi differences for neighbours within a factor of two);
+// everything else in FP32.
 __device__ __forceinline__ void visc_node(const LatView &g, int n, int q)
 {
     const int N = g.N;
-    const double *Uj = lat_U(g, q);
+    const float *W = lat_W(g, q);
     int i, j, k;
     lat_ijk(g, n, i, j, k);
     float dU[3][5], KS[3], Ui[5];
 #pragma unroll
-    for (int c = 0; c < 5; ++c) Ui[c] = (float)Uj[c * N + n];
+    for (int c = 0; c < 5; ++c) Ui[c] = W[c * N + n];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const int m2 = lat_step(g, i, j, k, d, -2), m1 = lat_step(g, i, j, k, d, -1), p1 = lat_step(g, i, j, k, d, 1),
                   p2 = lat_step(g, i, j, k, d, 2);
 #pragma unroll
-        for (int c = 0; c < 5; ++c)
-            dU[d][c] = (float)((1.0 / 12.0) * (8.0 * (Uj[c * N + p1] - Uj[c * N + m1]) - (Uj[c * N + p2] - Uj[c * N + m2])));
+        for (int c = 0; c < 5; ++c) {
+            const float *H = W + c * N, *L = W + (5 + c) * N;
+            const float d1 = (H[p1] - H[m1]) + (L[p1] - L[m1]);
+            const float d2 = (H[p2] - H[m2]) + (L[p2] - L[m2]);
+            dU[d][c] = (1.0f / 12.0f) * (8.0f * d1 - d2);
+        }
         const int c = d + 1;
-        const float um = (float)Uj[c * N + m1], up = (float)Uj[c * N + p1];
-        const float rm = (float)Uj[m1], rp = (float)Uj[p1];
+        const float um = W[c * N + m1], up = W[c * N + p1];
+        const float rm = W[m1], rp = W[p1];
         const float dlt = (Ui[c] / Ui[0]) - ((0.25f * um + 0.5f * Ui[c] + 0.25f * up) / (0.25f * rm + 0.5f * Ui[0] + 0.25f * rp));
         KS[d] = dlt * dlt;
     }
     float m[9];
 #pragma unroll
-    for (int c = 0; c < 9; ++c) m[c] = g.m9_32[c * N + n];
-    const float prim[5] = {(float)g.prim9[LF_RHO * N + n], (float)g.prim9[LF_U * N + n], (float)g.prim9[LF_V * N + n],
-                           (float)g.prim9[LF_W * N + n], (float)g.prim9[LF_P * N + n]};
+    for (int c = 0; c < 9; ++c) m[c] = g.node32[c * N + n];
+    const float *F = g.prim32;
+    const float prim[5] = {F[LF_RHO * N + n], F[LF_U * N + n], F[LF_V * N + n], F[LF_W * N + n], F[LF_P * N + n]};
     float Fv[5], Ev[5], Gv[5], mu;
-    viscous_node_flux<float>(dU, Ui, m, (float)g.det[n], prim, KS, g.P, Fv, Ev, Gv, mu);
+    viscous_node_flux<float>(dU, Ui, m, g.node32[9 * N + n], prim, KS, g.P, Fv, Ev, Gv, mu);
 #pragma unroll
     for (int c = 0; c < 5; ++c) {
         g.V32[(0 * 5 + c) * N + n] = Fv[c];
         g.V32[(1 * 5 + c) * N + n] = Ev[c];
         g.V32[(2 * 5 + c) * N + n] = Gv[c];
     }
-    g.prim9[LF_MU * N + n] = (double)mu;
+    g.prim32[LF_MU * N + n] = mu;
 }
 
 __device__ __forceinline__ void mu_node(const LatView &g, int n, int q)
 {
     const int N = g.N;
-    const double *Uj = lat_U(g, q);
-    const float U0 = (float)Uj[n], iU0 = 1.0f / U0;
-    const float uu = (float)Uj[N + n] * iU0, vv = (float)Uj[2 * N + n] * iU0, ww = (float)Uj[3 * N + n] * iU0;
+    const float *W = lat_W(g, q);
+    const float U0 = W[n], iU0 = 1.0f / U0;
+    const float uu = W[N + n] * iU0, vv = W[2 * N + n] * iU0, ww = W[3 * N + n] * iU0;
     const float mach = (float)g.P.mach;
-    const float d_temp = 1.4f * mach * mach * 0.4f * ((float)Uj[4 * N + n] * iU0 - 0.5f * (uu * uu + vv * vv + ww * ww));
+    const float d_temp = 1.4f * mach * mach * 0.4f * (W[4 * N + n] * iU0 - 0.5f * (uu * uu + vv * vv + ww * ww));
     const float sd = sqrtf(d_temp);
     const float S = 110.4f / (float)g.P.t_inf;
-    g.prim9[LF_MU * N + n] = (double)((sd * sd * sd) * ((1.0f + S) / (d_temp + S)));
+    g.prim32[LF_MU * N + n] = (sd * sd * sd) * ((1.0f + S) / (d_temp + S));
 }
 
 // Face n+1/2 along D, all FP32.
@@ -146,22 +289,15 @@ __device__ __forceinline__ void face_node(const LatView &g, int n)
     }
 }
 
-// 1/x in FP64 from an FP32 seed and two Newton steps (relative error near
-// FP64 rounding; the mixed form does not need the correctly rounded value).
-__device__ __forceinline__ double recip_fast(double x)
-{
-    double r = (double)(1.0f / (float)x);
-    r = r * fma(-x, r, 2.0);
-    r = r * fma(-x, r, 2.0);
-    return r;
-}
-
-// RHS and SSP-RK3 stage from the FP32 face and viscous fluxes.  L is summed
-// in FP32: neighbouring face fluxes are within a factor of two of each other,
-// so their FP32 difference is exact, and L's error is dominated by the FP32
-// face fluxes themselves.  The RK accumulation and the state are FP64.  With
-// fuse_next, the next stage's prep on the new primitives.
-__device__ __forceinline__ void update_node(const LatView &g, int n, int jst, bool fuse_next)
+// RHS and SSP-RK3 stage jst from the FP32 face and viscous fluxes, then the
+// next stage's U_Q.  L is summed in FP32 (neighbouring face fluxes within a
+// factor of two subtract exactly); the RK accumulation is hi/lo:
+//   jst 0: U1 = U0 + dt L
+//   jst 1: U2 = 3/4 U0 + 1/4 U1 + 1/4 dt L
+//   jst 2: U0 = 1/3 U0 + 2/3 U2 + 2/3 dt L
+// and the new state lands in slot (jst+1) mod 3, which is also the next
+// stage's U_Q slot.
+__device__ __forceinline__ void update_node(const LatView &g, int n, int jst)
 {
     const int N = g.N;
     int i, j, k;
@@ -180,51 +316,65 @@ __device__ __forceinline__ void update_node(const LatView &g, int n, int jst, bo
                 Lf[c] += (1.0f / 12.0f) * (8.0f * (Vd[c * N + p1] - Vd[c * N + m1]) - (Vd[c * N + p2] - Vd[c * N + m2]));
         }
     }
-    double L[5];
-#pragma unroll
-    for (int c = 0; c < 5; ++c) L[c] = -(double)Lf[c];
     if (g.Lout) {
 #pragma unroll
-        for (int c = 0; c < 5; ++c) g.Lout[c * N + n] = L[c];
+        for (int c = 0; c < 5; ++c) g.Lout[c * N + n] = -(double)Lf[c];
     }
-    const double dt = g.dt;
-    double Un[5];
+    const dfl dt = {g.dt_hi, g.dt_lo};
+    dfl U0[5], Un[5];
+    load_state(g, 0, n, U0);
     if (jst == 0) {
 #pragma unroll
-        for (int c = 0; c < 5; ++c) Un[c] = g.U0[c * N + n] + dt * L[c];
+        for (int c = 0; c < 5; ++c) Un[c] = df_add(U0[c], df_mul({-Lf[c], 0.0f}, dt));
     } else if (jst == 1) {
+        dfl U1[5];
+        load_state(g, 1, n, U1);
 #pragma unroll
-        for (int c = 0; c < 5; ++c) Un[c] = 0.75 * g.U0[c * N + n] + 0.25 * g.U1[c * N + n] + 0.25 * dt * L[c];
+        for (int c = 0; c < 5; ++c) {
+            const dfl a = df_mul(U0[c], {0.75f, 0.0f});
+            const dfl b = {0.25f * U1[c].h, 0.25f * U1[c].l};
+            const dfl t = df_mul({-0.25f * Lf[c], 0.0f}, dt);
+            Un[c] = df_add(df_add(a, b), t);
+        }
     } else {
+        dfl U2[5];
+        load_state(g, 2, n, U2);
 #pragma unroll
-        for (int c = 0; c < 5; ++c)
-            Un[c] = (1.0 / 3.0) * g.U0[c * N + n] + (2.0 / 3.0) * g.U2[c * N + n] + (2.0 / 3.0) * (dt * L[c]);
+        for (int c = 0; c < 5; ++c) {
+            const dfl a = df_mul(U0[c], {kThirdH, kThirdL});
+            const dfl b = df_mul(U2[c], {kTwoThirdH, kTwoThirdL});
+            const dfl t = df_mul(df_mul({-Lf[c], 0.0f}, dt), {kTwoThirdH, kTwoThirdL});
+            Un[c] = df_add(df_add(a, b), t);
+        }
     }
-    double *Uo = jst == 0 ? g.U1 : (jst == 1 ? g.U2 : g.U0);
-    if (!fuse_next) {
+    store_state(g, jst == 2 ? 0 : jst + 1, n, Un);
+    derive(g, n, Un);
+}
+
+// FP64 FLOW of the state in slot q (boundary output): the FP64 form's
+// primitive formulas on hi + lo; mu from the last viscous pass.
+__device__ __forceinline__ void flow_out_node(const LatView &g, int n, int q)
+{
+    const int N = g.N;
+    const float *W = lat_W(g, q);
+    double fu[5];
+    const double id = 1.0 / g.det[n];
 #pragma unroll
-        for (int c = 0; c < 5; ++c) Uo[c * N + n] = Un[c];
-    }
-    const double idet = g.idet[n];
-    const double rho = idet * Un[0];
-    const double ir = recip_fast(rho);
-    const double s = idet * ir;
-    const double u = Un[1] * s, v = Un[2] * s, w = Un[3] * s;
-    const double e = Un[4] * s - 0.5 * (u * u + v * v + w * w);
+    for (int c = 0; c < 5; ++c) fu[c] = id * ((double)W[c * N + n] + (double)W[(5 + c) * N + n]);
+    const double rho = fu[0], u = fu[1] / fu[0], v = fu[2] / fu[0], w = fu[3] / fu[0];
+    const double e = (fu[4] / fu[0]) - 0.5 * (u * u + v * v + w * w);
     const double p = e * rho * 0.4;
     const double mach = g.P.mach;
-    const double pr = p * ir;
-    g.prim9[LF_RHO * N + n] = rho;
-    g.prim9[LF_U * N + n] = u;
-    g.prim9[LF_V * N + n] = v;
-    g.prim9[LF_W * N + n] = w;
-    g.prim9[LF_E * N + n] = e;
-    g.prim9[LF_P * N + n] = p;
-    g.prim9[LF_T * N + n] = (1.4 * mach * mach) * pr;
-    g.prim9[LF_A * N + n] = (double)sqrtf(1.4f * (float)pr);
-    if (!(isfinite(rho) && isfinite(u) && isfinite(v) && isfinite(w) && isfinite(p))) atomicOr(g.flags, 2u);
-    // the next stage's U_Q overwrites U_{jst+1} (mod 3) with det*Q(FLOW)
-    if (fuse_next) prep_values(g, n, jst == 2 ? 0 : jst + 1, rho, u, v, w, p);
+    double *F = g.prim9;
+    F[LF_RHO * N + n] = rho;
+    F[LF_U * N + n] = u;
+    F[LF_V * N + n] = v;
+    F[LF_W * N + n] = w;
+    F[LF_E * N + n] = e;
+    F[LF_P * N + n] = p;
+    F[LF_T * N + n] = (1.4 * mach * mach) * (p / rho);
+    F[LF_A * N + n] = sqrt(1.4 * p / rho);
+    F[LF_MU * N + n] = (double)g.prim32[LF_MU * N + n];
 }
 
 }  // namespace mx

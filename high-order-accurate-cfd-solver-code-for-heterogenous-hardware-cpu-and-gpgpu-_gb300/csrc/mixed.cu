@@ -1,18 +1,19 @@
 // mixed.cu -- the mixed-precision form of the structured (lattice) stage.
 //
-// What runs in FP32: the characteristic projection, WENO5 weights and
-// reconstruction, the LLF split and face fluxes, the viscous and SGS fluxes,
-// the node fluxes used by the sixth-order correction.  What stays FP64: the
-// conserved state U0/U1/U2 and FLOW, the RK3 stage accumulation and the
-// right-hand side sum, the derivatives of U that feed the viscous terms, and
-// the metric/Jacobian inputs (rounded to FP32 only where a face flux uses
-// them).  Stage intermediates are stored in FP32 (half the bytes).
+// FP32: the characteristic projection, WENO5 weights and reconstruction, the
+// LLF split and face fluxes, the viscous and SGS fluxes, the node fluxes used
+// by the sixth-order correction, the right-hand side sum.  The conserved
+// state U0/U1/U2 is carried as hi + lo FP32 pairs and the RK3 stage is
+// accumulated in that arithmetic, so no stage kernel issues FP64 work; FP64
+// appears only where FLOW enters (after an upload) and where FLOW/U leave.
+// Stage intermediates are FP32 (half the bytes of the FP64 form).
 //
-// Kernels per stage: k_prep_m (pointwise), k_visc_m (radius-2 star),
-// k_face_m<d> x3 (one thread per face), k_update_m (FP64 RK stage); the
-// per-node operations are in lattice_mixed.cuh.  This file is compiled with
-// FMA contraction on and approximate FP32 division/square root (the mixed
-// form's error budget is 1e-6 relative L2 against the FP64 form).
+// Kernels per stage: k_visc_m (radius-2 star), k_face_m<d> x3 (one thread
+// per face), k_update_m (RK stage + the next stage's U_Q); k_init_m /
+// k_prep_m supply U_Q when no update produced it.  The per-node operations
+// are in lattice_mixed.cuh.  This file is compiled with FMA contraction on
+// and approximate FP32 division/square root (the mixed form's error budget
+// is 1e-6 relative L2 against the FP64 form).
 #include "internal.h"
 #include "lattice_mixed.cuh"
 #include "structured.h"
@@ -23,10 +24,16 @@ namespace {
 
 __device__ __forceinline__ int node_id() { return blockIdx.x * blockDim.x + threadIdx.x; }
 
-__global__ void __launch_bounds__(256) k_prep_m(LatView g, int q)
+__global__ void __launch_bounds__(256) k_init_m(LatView g, int q)
 {
     const int n = node_id();
-    if (n < g.N) mx::prep_node(g, n, q);
+    if (n < g.N) mx::init_node(g, n, q);
+}
+
+__global__ void __launch_bounds__(256) k_prep_m(LatView g, int src, int dst)
+{
+    const int n = node_id();
+    if (n < g.N) mx::prep_node(g, n, src, dst);
 }
 
 __global__ void __launch_bounds__(256) k_visc_m(LatView g, int q)
@@ -51,25 +58,43 @@ __global__ void __launch_bounds__(128) k_face_m(LatView g)
 __global__ void __launch_bounds__(256) k_update_m(LatView g, int jst)
 {
     const int n = node_id();
-    if (n < g.N) mx::update_node(g, n, jst, false);
+    if (n < g.N) mx::update_node(g, n, jst);
 }
 
-__global__ void __launch_bounds__(256) k_update_prep_m(LatView g, int jst)
+__global__ void k_flow_out_m(LatView g, int q)
 {
     const int n = node_id();
-    if (n < g.N) mx::update_node(g, n, jst, true);
+    if (n < g.N) mx::flow_out_node(g, n, q);
 }
 
-__global__ void k_recip(const double *__restrict__ a, double *__restrict__ b, long long n)
+__global__ void k_u_out_m(LatView g, int q, double *__restrict__ aos)
 {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n) b[t] = 1.0 / a[t];
+    const int n = node_id();
+    if (n >= g.N) return;
+    const float *W = lat_W(g, q);
+#pragma unroll
+    for (int c = 0; c < 5; ++c) aos[(size_t)(n + 1) * 5 + c] = (double)W[c * g.N + n] + (double)W[(5 + c) * g.N + n];
 }
 
 __global__ void k_to_float(const double *__restrict__ a, float *__restrict__ b, long long n)
 {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t < n) b[t] = (float)a[t];
+}
+
+// node32 = [9 node metrics, det] in FP32; idet32 = 1/det as hi, lo
+__global__ void k_node_geometry(const double *__restrict__ m9, const double *__restrict__ det, long long N,
+                                float *__restrict__ node32, float *__restrict__ idet32)
+{
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+#pragma unroll
+    for (int c = 0; c < 9; ++c) node32[c * N + n] = (float)m9[c * N + n];
+    node32[9 * N + n] = (float)det[n];
+    const double id = 1.0 / det[n];
+    const float h = (float)id;
+    idet32[n] = h;
+    idet32[N + n] = (float)(id - (double)h);
 }
 
 }  // namespace
@@ -79,11 +104,20 @@ void mixed_geometry(const StructuredLaunch &S)
     const long long N = (long long)S.ni * S.nj * S.nk;
     k_to_float<<<blocks_for(9 * N, 256), 256, 0, S.stream>>>(S.fm, S.fm32, 9 * N);
     k_to_float<<<blocks_for(3 * N, 256), 256, 0, S.stream>>>(S.fdet, S.fdet32, 3 * N);
-    k_to_float<<<blocks_for(9 * N, 256), 256, 0, S.stream>>>(S.m9, S.m932, 9 * N);
-    k_recip<<<blocks_for(N, 256), 256, 0, S.stream>>>(S.det, S.idet, N);
+    k_node_geometry<<<blocks_for(N, 256), 256, 0, S.stream>>>(S.m9, S.det, N, S.node32, S.idet32);
 }
 
-int mixed_stage(const StructuredLaunch &S, int jst, double dt, double *Lout, cudaEvent_t *ev, bool prep, bool fuse,
+void mixed_flow_out(const LatView &g, int q, cudaStream_t st)
+{
+    k_flow_out_m<<<blocks_for(g.N, 256), 256, 0, st>>>(g, q);
+}
+
+void mixed_u_out(const LatView &g, int q, double *aos, cudaStream_t st)
+{
+    k_u_out_m<<<blocks_for(g.N, 256), 256, 0, st>>>(g, q, aos);
+}
+
+int mixed_stage(const StructuredLaunch &S, int jst, double dt, double *Lout, cudaEvent_t *ev, int prep_from,
                 const char **names)
 {
     const LatView g = make_view(S, dt, Lout);
@@ -98,8 +132,12 @@ int mixed_stage(const StructuredLaunch &S, int jst, double dt, double *Lout, cud
         ++k;
     };
     mark();
-    if (prep) {
-        k_prep_m<<<nb256, 256, 0, st>>>(g, jst);
+    if (prep_from == kPrepFromFlow) {
+        k_init_m<<<nb256, 256, 0, st>>>(g, jst);
+        name("prep");
+        mark();
+    } else if (prep_from >= 0) {
+        k_prep_m<<<nb256, 256, 0, st>>>(g, prep_from, jst);
         name("prep");
         mark();
     }
@@ -120,13 +158,8 @@ int mixed_stage(const StructuredLaunch &S, int jst, double dt, double *Lout, cud
     k_face_m<2><<<nb128, 128, 0, st>>>(g);
     name("face_k");
     mark();
-    if (fuse) {
-        k_update_prep_m<<<nb256, 256, 0, st>>>(g, jst);
-        name("update+prep");
-    } else {
-        k_update_m<<<nb256, 256, 0, st>>>(g, jst);
-        name("update");
-    }
+    k_update_m<<<nb256, 256, 0, st>>>(g, jst);
+    name("update+prep");
     mark();
     return k;
 }

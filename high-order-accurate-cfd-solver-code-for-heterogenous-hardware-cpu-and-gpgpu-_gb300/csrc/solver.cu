@@ -40,7 +40,10 @@ struct cfd_solver {
     double *stage9 = nullptr;   // AoS staging, rows 0..N, 9 doubles
     double *stage5 = nullptr;   // AoS staging, rows 0..N, 5 doubles
     double *Lsoa = nullptr;
-    int prep_ready = -1;        // mixed form: stage whose U_Q outputs are current
+    // mixed form: the U slot holding the current state (-1: the uploaded FP64
+    // FLOW is current) and the stage whose U_Q outputs are ready (-1: none)
+    int cur_slot = -1;
+    int prep_ready = -1;
 };
 
 namespace {
@@ -117,7 +120,8 @@ cfd_status_t create_structured(cfd_solver *s, const cfd_geometry_t *g)
         if ((st = dalloc_t(s, 5 * N, &S.Q32)) || (st = dalloc_t(s, 5 * N, &S.R32)) || (st = dalloc_t(s, 15 * N, &S.FEG32))
             || (st = dalloc_t(s, 15 * N, &S.V32)) || (st = dalloc_t(s, 15 * N, &S.Fh32))
             || (st = dalloc_t(s, 9 * N, &S.fm32)) || (st = dalloc_t(s, 3 * N, &S.fdet32))
-            || (st = dalloc_t(s, 9 * N, &S.m932)) || (st = dalloc_t(s, N, &S.idet)))
+            || (st = dalloc_t(s, 10 * N, &S.node32)) || (st = dalloc_t(s, 2 * N, &S.idet32))
+            || (st = dalloc_t(s, 9 * N, &S.prim32)))
             return st;
         cudaMemsetAsync(S.V32, 0, 15 * N * sizeof(float), S.stream);
     } else {          // FP64 stage intermediates
@@ -148,15 +152,21 @@ cfd_status_t create_structured(cfd_solver *s, const cfd_geometry_t *g)
     return CFD_OK;
 }
 
+// where stage j's U_Q comes from (mixed form; the FP64 form always preps)
+int prep_source(const cfd_solver *s, int j)
+{
+    if (!s->mixed) return kPrepFromFlow;
+    if (s->prep_ready == j) return kPrepNone;
+    return s->cur_slot < 0 ? kPrepFromFlow : s->cur_slot;
+}
+
 cfd_status_t run_stage(cfd_solver *s, int j, double dt, bool want_L)
 {
     cfd_ctx *ctx = s->ctx;
     s->S.stream = ctx->stream;   // the context's stream may have been replaced
     if (s->path == CFD_PATH_STRUCTURED) {
-        const bool mixed = s->S.mixed != 0;
-        ctx->launches += structured_stage(s->S, j, dt, want_L ? s->Lsoa : nullptr, nullptr, nullptr,
-                                          !mixed || s->prep_ready != j, mixed);
-        if (mixed) s->prep_ready = j == 2 ? 0 : j + 1;
+        ctx->launches += structured_stage(s->S, j, dt, want_L ? s->Lsoa : nullptr, nullptr, nullptr, prep_source(s, j));
+        if (s->mixed) s->cur_slot = s->prep_ready = j == 2 ? 0 : j + 1;
     } else {
         double *Uj = s->U[j];
         launch_uq(ctx->stream, Uj, s->Q, s->grid, s->det, s->flow, s->roe, s->g_node + 1, s->n_rows, ctx->d_flags);
@@ -262,6 +272,7 @@ cfd_status_t cfd_solver_set_flow(cfd_solver_t *s, const cfd_flow_t *flow_host)
         const long long N = (long long)s->ni * s->nj * s->nk;
         s->S.stream = s->ctx->stream;
         s->prep_ready = -1;
+        s->cur_slot = -1;
         st = upload(s, s->stage9, flow_host, R * sizeof(cfd_flow_t));
         if (st == CFD_OK) aos_to_soa(s->ctx->stream, s->stage9, 9, 9, N, s->S.prim9);
     }
@@ -277,6 +288,11 @@ cfd_status_t cfd_solver_get_flow(cfd_solver_t *s, cfd_flow_t *flow_host)
     const size_t R = (size_t)s->n_rows;
     const double *src = s->flow;
     if (s->path == CFD_PATH_STRUCTURED) {
+        s->S.stream = s->ctx->stream;
+        if (s->mixed && s->cur_slot >= 0) {   // FP64 FLOW of the current hi/lo state
+            mixed_flow_out(make_view(s->S, 0.0, nullptr), s->cur_slot, s->S.stream);
+            s->ctx->launches += 1;
+        }
         soa_to_aos(s->ctx->stream, s->S.prim9, 9, 9, (long long)s->ni * s->nj * s->nk, s->stage9);
         src = s->stage9;
     }
@@ -293,7 +309,10 @@ cfd_status_t cfd_solver_get_u0(cfd_solver_t *s, cfd_column_t *u0_host)
     const size_t R = (size_t)s->n_rows;
     const double *src = s->U[0];
     if (s->path == CFD_PATH_STRUCTURED) {
-        soa_to_aos(s->ctx->stream, s->S.U[0], 5, 5, (long long)s->ni * s->nj * s->nk, s->stage5);
+        if (s->mixed)
+            mixed_u_out(make_view(s->S, 0.0, nullptr), 0, s->stage5, s->ctx->stream);
+        else
+            soa_to_aos(s->ctx->stream, s->S.U[0], 5, 5, (long long)s->ni * s->nj * s->nk, s->stage5);
         src = s->stage5;
     }
     cudaError_t e = cudaMemcpyAsync(u0_host, src, R * sizeof(cfd_column_t), cudaMemcpyDeviceToHost, s->ctx->stream);
@@ -345,9 +364,8 @@ cfd_status_t cfd_solver_profile_stage(cfd_solver_t *s, int32_t j, double del_t, 
     const char *snames[kMaxStageLaunches] = {};
     int nk = 3;
     if (s->path == CFD_PATH_STRUCTURED) {
-        const bool mixed = s->S.mixed != 0;
-        nk = structured_stage(s->S, j, del_t, nullptr, ev.data(), snames, !mixed || s->prep_ready != j, mixed);
-        if (mixed) s->prep_ready = j == 2 ? 0 : j + 1;
+        nk = structured_stage(s->S, j, del_t, nullptr, ev.data(), snames, prep_source(s, j));
+        if (s->mixed) s->cur_slot = s->prep_ready = j == 2 ? 0 : j + 1;
     } else {
         cudaEventRecord(ev[0], stream);
         double *Uj = s->U[j];

@@ -34,23 +34,31 @@ struct StructuredLaunch {
     float *Fh32 = nullptr;     // [3][5][N]
     float *fm32 = nullptr;     // [3][3][N]
     float *fdet32 = nullptr;   // [3][N]
-    float *m932 = nullptr;     // [9][N] node metrics
-    double *idet = nullptr;    // [N] 1/det
+    float *node32 = nullptr;   // [10][N] node metrics, det
+    float *idet32 = nullptr;   // [2][N] 1/det hi, lo
+    float *prim32 = nullptr;   // [9][N] FLOW in FP32
 };
 
-// The three face-flux launches of the mixed-precision form (mixed.cu).
-// Mixed-precision stage (mixed.cu).  With prep = false the stage's U_Q
-// outputs are taken as already produced (by the previous stage's fused
-// update); with fuse = true the update also produces the next stage's.
+// Where the mixed stage takes its U_Q (prep) from: nothing (the previous
+// stage's update already produced it), the FP64 FLOW (after an upload), or
+// the hi/lo state in U slot 0..2.
+constexpr int kPrepNone = -2;
+constexpr int kPrepFromFlow = -1;
+
+// Mixed-precision stage j (mixed.cu).  prep_from as above; the update always
+// produces the next stage's U_Q (its state lands in slot (j+1) mod 3).
 // Returns the number of launches; ev (optional) gets one event before and one
 // after each launch (launches + 1 events), names[i] the launch names.
-int mixed_stage(const StructuredLaunch &S, int j, double dt, double *Lout, cudaEvent_t *ev, bool prep, bool fuse,
+int mixed_stage(const StructuredLaunch &S, int j, double dt, double *Lout, cudaEvent_t *ev, int prep_from,
                 const char **names);
-// FP32 copies of the node metrics, face metrics and face dets, and 1/det
-// (once, after upload).
-// FP32 copies of the face and node metrics and 1/det (kernels launched: 4)
-constexpr int kMixedGeometryLaunches = 4;
+// FP32 copies of the face and node metrics and 1/det as hi/lo (once, after
+// upload; kernels launched: 3).
+constexpr int kMixedGeometryLaunches = 3;
 void mixed_geometry(const StructuredLaunch &S);
+// FP64 FLOW (g.prim9, SoA) from the hi/lo state in slot q; mu from prim32.
+void mixed_flow_out(const LatView &g, int q, cudaStream_t st);
+// FP64 U of slot q as AoS rows 1..N of 5 doubles.
+void mixed_u_out(const LatView &g, int q, double *aos, cudaStream_t st);
 
 // Device view of a StructuredLaunch for one stage.
 inline LatView make_view(const StructuredLaunch &S, double dt, double *Lout)
@@ -66,11 +74,14 @@ inline LatView make_view(const StructuredLaunch &S, double dt, double *Lout)
     g.det = S.det;
     g.fm = S.fm;
     g.fdet = S.fdet;
+    g.dt_hi = (float)dt;
+    g.dt_lo = (float)(dt - (double)g.dt_hi);
     g.fm32 = S.fm32;
     g.fdet32 = S.fdet32;
-    g.m9_32 = S.m932;
-    g.idet = S.idet;
+    g.node32 = S.node32;
+    g.idet32 = S.idet32;
     g.prim9 = S.prim9;
+    g.prim32 = S.prim32;
     g.U0 = S.U[0];
     g.U1 = S.U[1];
     g.U2 = S.U[2];
@@ -92,11 +103,11 @@ inline LatView make_view(const StructuredLaunch &S, double dt, double *Lout)
 // One RK stage j of the host loop; Lout (device [5][N]) may be null.
 // Returns the number of kernel launches; ev (optional, at least
 // kMaxStageLaunches+1 entries) receives events bracketing every launch and
-// names (optional) the launch names.  prep/fuse as for mixed_stage (the FP64
-// form always runs its own prep and no fused update).
+// names (optional) the launch names.  prep_from as for mixed_stage (the FP64
+// form always runs its own prep from FLOW).
 constexpr int kMaxStageLaunches = 6;
 int structured_stage(const StructuredLaunch &S, int j, double dt, double *Lout, cudaEvent_t *ev = nullptr,
-                     const char **names = nullptr, bool prep = true, bool fuse = false);
+                     const char **names = nullptr, int prep_from = kPrepFromFlow);
 
 void aos_to_soa(cudaStream_t st, const double *aos, int stride, int ncomp, long long N, double *soa);
 void soa_to_aos(cudaStream_t st, const double *soa, int stride, int ncomp, long long N, double *aos);
