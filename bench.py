@@ -46,7 +46,7 @@ UNIT = "cell-updates/s"
 # face dets 3), x3 stages.
 ALGO_BYTES_PER_CELL_UPDATE = 5 * 40 + 3 * 40 + 3 * 22 * 8          # 848
 # Per-launch compulsory bytes per node of each structured kernel (every
-# input and output element once): see the design doc, kernel table.
+# input and output element once).
 KERNEL_BYTES_PER_NODE = {
     "prep": (5 + 9 + 1 + 5 + 5 + 15 + 2) * 8,          # prims, metrics, det -> Q, U_j, F/E/G, sqrt(rho), H
     "viscous": (5 + 9 + 1 + 4 + 15 + 1) * 8,           # U_j, metrics, det, prims -> Fv/Ev/Gv, mu
@@ -56,10 +56,13 @@ KERNEL_BYTES_PER_NODE = {
     "face_k": (5 + 3 + 2 + 3 + 1 + 5 + 5) * 8,
     "update": (15 + 15 + 10 + 1 + 5 + 8) * 8,          # Fh, Fv/Ev/Gv, two U, det -> U, 8 FLOW fields
 }
-# FP64 operations per launch-unit of the structured FP64 kernels, counted by
-# ncu (sm__sass_thread_inst_executed_op_d{fma,mul,add}_pred_on.sum, FMA = 2)
-# on the 64^3 Taylor-Green case; profiles/structured_fp64_tgv.md.
-FP64_FLOP_PER_NODE = {}
+# FP64 operations per face of the FP64 face kernels, from ncu's FP64
+# instruction counters on the 64^3 Taylor-Green case (per face: 818 DFMA,
+# 784 DMUL, 575 DADD; FMA = 2), and the DRAM bytes the same capture measured
+# per face (dram__bytes_read.sum + dram__bytes_write.sum over 262,144 faces;
+# scaled by the face count of a launch for other sizes).
+FP64_FLOP_PER_NODE = {"face_i": 2995, "face_j": 2995, "face_k": 2995}
+DRAM_BYTES_PER_NODE = {"face_i": 153, "face_j": 155, "face_k": 155}
 
 
 def parse_args(argv=None):
@@ -325,7 +328,10 @@ def gpu_arm(args):
     fp64_roof = None
     if dom in FP64_FLOP_PER_NODE:
         f = FP64_FLOP_PER_NODE[dom] * N / (table[dom] * 1e-3)
-        fp64_roof = {"achieved": f / 1e12, "peak": fp64_peak / 1e12, "unit": "TFLOP/s", "frac": f / fp64_peak}
+        fp64_roof = {"kernel": dom, "achieved": f / 1e12, "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
+                     "frac": f / fp64_peak, "peak_source": "FP64 FMA probe of this run",
+                     "note": "DMUL/DADD count one FLOP but take a full FP64 issue slot"}
+    traffic = DRAM_BYTES_PER_NODE[dom] * N if dom in DRAM_BYTES_PER_NODE else None
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -339,7 +345,7 @@ def gpu_arm(args):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(host_in.nbytes),
                 "d2h_bytes_per_step": int(host_out.nbytes)},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_src,
+                     "frac": achieved / hbm_peak, "traffic": traffic, "peak_source": peak_src,
                      "note": "FP64-pipe bound; see roofline_fp64"},
         "roofline_fp64": fp64_roof,
         "step_algorithmic_gbs": ALGO_BYTES_PER_CELL_UPDATE * value / world / 1e9,

@@ -69,7 +69,7 @@ uint64_t instance_bytes(int precision, int64_t N)
 {
     const uint64_t doubles = (22 + 9 + 15) * (uint64_t)N + 14 * (uint64_t)(N + 1);
     // mixed: FP32 face/node geometry (12 + 10 + 2), prim32 (9), stage intermediates (55)
-    if (precision == CFD_PREC_MIXED) return doubles * 8 + (12 + 10 + 2 + 9 + 55) * (uint64_t)N * 4;
+    if (precision == CFD_PREC_MIXED) return doubles * 8 + (12 + 11 + 2 + 9 + 55) * (uint64_t)N * 4;
     return (doubles + 52 * (uint64_t)N) * 8;
 }
 
@@ -356,7 +356,7 @@ cfd_status_t cfd_batch_add(cfd_batch_t *b, const cfd_geometry_t *geom, const cfd
     if (b->precision == CFD_PREC_MIXED) {
         float *fm32, *fdet32, *node32, *idet32;
         if ((st = ialloc(b, I, 9 * Nz, &fm32)) || (st = ialloc(b, I, 3 * Nz, &fdet32))
-            || (st = ialloc(b, I, 10 * Nz, &node32)) || (st = ialloc(b, I, 2 * Nz, &idet32))
+            || (st = ialloc(b, I, 11 * Nz, &node32)) || (st = ialloc(b, I, 2 * Nz, &idet32))
             || (st = ialloc(b, I, 9 * Nz, &v.prim32)) || (st = ialloc(b, I, 5 * Nz, &v.Q32))
             || (st = ialloc(b, I, 5 * Nz, &v.R32)) || (st = ialloc(b, I, 15 * Nz, &v.FEG32))
             || (st = ialloc(b, I, 15 * Nz, &v.V32)) || (st = ialloc(b, I, 15 * Nz, &v.Fh32))) {

@@ -23,7 +23,7 @@ struct LatView {
     // geometry (FP64), and FP32 copies for the mixed form
     const double *m9, *det, *fm, *fdet;
     const float *fm32, *fdet32;
-    const float *node32;       // [10][N] 9 node metrics, then det (mixed form)
+    const float *node32;       // [11][N] 9 node metrics, det, det^(-1/3) (mixed form)
     const float *idet32;       // [2][N] 1/det as hi, lo (mixed form)
     // state
     double *prim9;             // FLOW fields u,v,w,p,t,rho,mu,a,e
@@ -39,9 +39,14 @@ struct LatView {
 
 enum { LF_U = 0, LF_V = 1, LF_W = 2, LF_P = 3, LF_T = 4, LF_RHO = 5, LF_MU = 6, LF_A = 7, LF_E = 8 };
 
-// periodic wrap for offsets of any size (|o| may exceed the extent)
+// periodic wrap of x = i + o, 0 <= i < n; one correction when |o| <= 3 <= n
+// (every stencil here), repeated for shorter extents
 __device__ __forceinline__ int lwrap(int x, int n)
 {
+    if (n >= 3) {
+        x += x < 0 ? n : 0;
+        return x >= n ? x - n : x;
+    }
     while (x < 0) x += n;
     while (x >= n) x -= n;
     return x;

@@ -17,6 +17,7 @@
 #pragma once
 
 #include "lattice.cuh"
+#include "physics_x2.cuh"
 
 namespace cfd {
 namespace mx {
@@ -222,7 +223,7 @@ __device__ __forceinline__ void visc_node(const LatView &g, int n, int q)
         const int c = d + 1;
         const float um = W[c * N + m1], up = W[c * N + p1];
         const float rm = W[m1], rp = W[p1];
-        const float dlt = (Ui[c] / Ui[0]) - ((0.25f * um + 0.5f * Ui[c] + 0.25f * up) / (0.25f * rm + 0.5f * Ui[0] + 0.25f * rp));
+        const float dlt = qdiv(Ui[c], Ui[0]) - qdiv(0.25f * um + 0.5f * Ui[c] + 0.25f * up, 0.25f * rm + 0.5f * Ui[0] + 0.25f * rp);
         KS[d] = dlt * dlt;
     }
     float m[9];
@@ -231,7 +232,7 @@ __device__ __forceinline__ void visc_node(const LatView &g, int n, int q)
     const float *F = g.prim32;
     const float prim[5] = {F[LF_RHO * N + n], F[LF_U * N + n], F[LF_V * N + n], F[LF_W * N + n], F[LF_P * N + n]};
     float Fv[5], Ev[5], Gv[5], mu;
-    viscous_node_flux<float>(dU, Ui, m, g.node32[9 * N + n], prim, KS, g.P, Fv, Ev, Gv, mu);
+    viscous_node_flux<float>(dU, Ui, m, g.node32[9 * N + n], g.node32[10 * N + n], prim, KS, g.P, Fv, Ev, Gv, mu);
 #pragma unroll
     for (int c = 0; c < 5; ++c) {
         g.V32[(0 * 5 + c) * N + n] = Fv[c];
@@ -245,16 +246,16 @@ __device__ __forceinline__ void mu_node(const LatView &g, int n, int q)
 {
     const int N = g.N;
     const float *W = lat_W(g, q);
-    const float U0 = W[n], iU0 = 1.0f / U0;
+    const float U0 = W[n], iU0 = qdiv(1.0f, U0);
     const float uu = W[N + n] * iU0, vv = W[2 * N + n] * iU0, ww = W[3 * N + n] * iU0;
     const float mach = (float)g.P.mach;
     const float d_temp = 1.4f * mach * mach * 0.4f * (W[4 * N + n] * iU0 - 0.5f * (uu * uu + vv * vv + ww * ww));
     const float sd = sqrtf(d_temp);
     const float S = 110.4f / (float)g.P.t_inf;
-    g.prim32[LF_MU * N + n] = (sd * sd * sd) * ((1.0f + S) / (d_temp + S));
+    g.prim32[LF_MU * N + n] = (sd * sd * sd) * qdiv(1.0f + S, d_temp + S);
 }
 
-// Face n+1/2 along D, all FP32.
+// Face n+1/2 along D, all FP32, on paired lanes (physics_x2.cuh).
 template <int D>
 __device__ __forceinline__ void face_node(const LatView &g, int n)
 {
@@ -264,11 +265,11 @@ __device__ __forceinline__ void face_node(const LatView &g, int n)
     int s[6];
 #pragma unroll
     for (int o = 0; o < 6; ++o) s[o] = lat_step(g, i, j, k, D, o - 2);
-    float pts[6][5];
+    float2 P[3][5];   // (point k, point 5-k)
 #pragma unroll
-    for (int o = 0; o < 6; ++o)
+    for (int o = 0; o < 3; ++o)
 #pragma unroll
-        for (int c = 0; c < 5; ++c) pts[o][c] = g.Q32[c * N + s[o]];
+        for (int c = 0; c < 5; ++c) P[o][c] = make_float2(g.Q32[c * N + s[o]], g.Q32[c * N + s[5 - o]]);
     float r[5];
     {
         const int l = s[2], rr = s[3];
@@ -277,15 +278,15 @@ __device__ __forceinline__ void face_node(const LatView &g, int n)
                            R[N + l], R[2 * N + l], R[4 * N + l], r);
     }
     float Fhat[5];
-    llf_face_flux<float>(pts, g.fm32[(D * 3 + 0) * N + n], g.fm32[(D * 3 + 1) * N + n], g.fm32[(D * 3 + 2) * N + n],
-                         g.fdet32[D * N + n], r, (float)g.P.eps, Fhat);
+    x2::llf_face_flux2(P, g.fm32[(D * 3 + 0) * N + n], g.fm32[(D * 3 + 1) * N + n], g.fm32[(D * 3 + 2) * N + n],
+                       g.fdet32[D * N + n], r, (float)g.P.eps, Fhat);
     const float *NF = g.FEG32 + (size_t)D * 5 * N;
 #pragma unroll
     for (int c = 0; c < 5; ++c) {
         float f[6];
 #pragma unroll
         for (int o = 0; o < 6; ++o) f[o] = NF[c * N + s[o]];
-        g.Fh32[(D * 5 + c) * N + n] = Fhat[c] + face_correction<float>(f);
+        g.Fh32[(D * 5 + c) * N + n] = Fhat[c] + x2::face_correction_sym(f);
     }
 }
 

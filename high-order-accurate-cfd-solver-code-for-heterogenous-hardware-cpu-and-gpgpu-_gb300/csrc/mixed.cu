@@ -48,8 +48,12 @@ __global__ void __launch_bounds__(256) k_mu_m(LatView g, int q)
     if (n < g.N) mx::mu_node(g, n, q);
 }
 
+#ifndef CFD_MFACE_MIN_BLOCKS
+#define CFD_MFACE_MIN_BLOCKS 8
+#endif
+
 template <int D>
-__global__ void __launch_bounds__(128) k_face_m(LatView g)
+__global__ void __launch_bounds__(128, CFD_MFACE_MIN_BLOCKS) k_face_m(LatView g)
 {
     const int n = node_id();
     if (n < g.N) mx::face_node<D>(g, n);
@@ -82,7 +86,7 @@ __global__ void k_to_float(const double *__restrict__ a, float *__restrict__ b, 
     if (t < n) b[t] = (float)a[t];
 }
 
-// node32 = [9 node metrics, det] in FP32; idet32 = 1/det as hi, lo
+// node32 = [9 node metrics, det, det^(-1/3)] in FP32; idet32 = 1/det as hi, lo
 __global__ void k_node_geometry(const double *__restrict__ m9, const double *__restrict__ det, long long N,
                                 float *__restrict__ node32, float *__restrict__ idet32)
 {
@@ -91,6 +95,7 @@ __global__ void k_node_geometry(const double *__restrict__ m9, const double *__r
 #pragma unroll
     for (int c = 0; c < 9; ++c) node32[c * N + n] = (float)m9[c * N + n];
     node32[9 * N + n] = (float)det[n];
+    node32[10 * N + n] = (float)(1.0 / cbrt(det[n]));
     const double id = 1.0 / det[n];
     const float h = (float)id;
     idet32[n] = h;

@@ -3,8 +3,9 @@
 //
 // Every function follows the reference kernels' formulas (cited per
 // function) with gamma = 1.4 written as the reference writes it (0.4, 1.4,
-// 0.2).  Functions are templated on the compute type T: double for the FP64
-// path, float for the parts the mixed-precision path runs in FP32.
+// 0.2).  Functions are templated on the compute type T; the mixed-precision
+// form instantiates them with float (the FP64 form uses the exact-order
+// restatement in physics_exact.cuh).  Repeated divisors are inverted once.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -14,12 +15,13 @@ namespace cfd {
 
 template <class T> __device__ __forceinline__ T sqr(T x) { return x * x; }
 
-// Total enthalpy per unit mass, U_Q.cl:64-65.
-template <class T>
-__device__ __forceinline__ T total_enthalpy(T rho, T u, T v, T w, T p)
-{
-    return ((p / T(0.4)) + T(0.5) * rho * (u * u + v * v + w * w) + p) / rho;
-}
+// Quotient and reciprocal square root.  The float forms use the hardware
+// approximations (__fdividef: about 2 ulp for |b| < 2^126; rsqrtf); other
+// types compute them exactly.
+template <class T> __device__ __forceinline__ T qdiv(T a, T b) { return a / b; }
+template <> __device__ __forceinline__ float qdiv<float>(float a, float b) { return __fdividef(a, b); }
+template <class T> __device__ __forceinline__ T qrsqrt(T x) { return T(1) / sqrt(x); }
+template <> __device__ __forceinline__ float qrsqrt<float>(float x) { return rsqrtf(x); }
 
 // Roe-averaged face state from the two adjacent nodes (U_Q.cl:60-109):
 // out = {u, v, w, h, rho}.  sb/hb belong to the neighbour, si/hi to the node.
@@ -27,12 +29,12 @@ template <class T>
 __device__ __forceinline__ void roe_average(T sb, T ub, T vb, T wb, T hb, T si, T ui, T vi, T wi, T hi,
                                             T out[5])
 {
-    const T den = sb + si;
+    const T iden = qdiv(T(1.0), sb + si);
     out[4] = sb * si;
-    out[0] = (sb * ub + si * ui) / den;
-    out[1] = (sb * vb + si * vi) / den;
-    out[2] = (sb * wb + si * wi) / den;
-    out[3] = (sb * hb + si * hi) / den;
+    out[0] = (sb * ub + si * ui) * iden;
+    out[1] = (sb * vb + si * vi) * iden;
+    out[2] = (sb * wb + si * wi) * iden;
+    out[3] = (sb * hb + si * hi) * iden;
 }
 
 // Roe eigen-system of one face (Weno.cl:337-413): k_bar = grad(zeta)/|grad(zeta)|
@@ -40,7 +42,7 @@ __device__ __forceinline__ void roe_average(T sb, T ub, T vb, T wb, T hb, T si, 
 // (R) eigenvector matrices of the Euler flux Jacobian along k_bar.
 template <class T>
 struct FaceEigen {
-    T kx, ky, kz, a, alpha, beta, theta, phi, ru, rv, rw, rr;
+    T kx, ky, kz, a, alpha, beta, theta, phi, ru, rv, rw, rr, irr, ia2;
 
     __device__ __forceinline__ void init(T mx, T my, T mz, const T roe[5])
     {
@@ -49,38 +51,41 @@ struct FaceEigen {
         rw = roe[2];
         const T rh = roe[3];
         rr = roe[4];
-        const T kk = sqrt(mx * mx + my * my + mz * mz);
+        const T ikk = qrsqrt(mx * mx + my * my + mz * mz);
         a = sqrt(T(0.4) * (rh - T(0.5) * (ru * ru + rv * rv + rw * rw)));
-        kx = mx / kk;
-        ky = my / kk;
-        kz = mz / kk;
+        kx = mx * ikk;
+        ky = my * ikk;
+        kz = mz * ikk;
         theta = kx * ru + ky * rv + kz * rw;
         phi = T(0.5) * T(0.4) * (ru * ru + rv * rv + rw * rw);
-        const T s2 = T(1.4142135623730951);  // sqrt(2.0)
-        alpha = rr / (s2 * a);
-        beta = T(1.0) / (s2 * rr * a);
+        const T is2 = T(0.70710678118654752);  // 1/sqrt(2.0)
+        const T ia = qdiv(T(1.0), a);
+        irr = qdiv(T(1.0), rr);
+        ia2 = ia * ia;
+        alpha = rr * ia * is2;
+        beta = irr * ia * is2;
     }
 
     // Left eigenvectors, rows of l_eigen_Q (Weno.cl:384-412).
     __device__ __forceinline__ void left(T Lm[5][5]) const
     {
-        const T a2 = a * a;
-        const T ph = phi / a2;
-        Lm[0][0] = kx * (T(1.0) - ph) - ((kz * rv - ky * rw) / rr);
-        Lm[0][1] = kx * T(0.4) * ru / a2;
-        Lm[0][2] = (kx * T(0.4) * rv / a2) + (kz / rr);
-        Lm[0][3] = (kx * T(0.4) * rw / a2) - (ky / rr);
-        Lm[0][4] = -kx * T(0.4) / a2;
-        Lm[1][0] = ky * (T(1.0) - ph) - ((kx * rw - kz * ru) / rr);
-        Lm[1][1] = (ky * T(0.4) * ru / a2) - kz / rr;
-        Lm[1][2] = ky * T(0.4) * rv / a2;
-        Lm[1][3] = (ky * T(0.4) * rw / a2) + (kx / rr);
-        Lm[1][4] = -ky * T(0.4) / a2;
-        Lm[2][0] = kz * (T(1.0) - ph) - ((ky * ru - kx * rv) / rr);
-        Lm[2][1] = kz * T(0.4) * ru / a2 + (ky / rr);
-        Lm[2][2] = kz * T(0.4) * rv / a2 - (kx / rr);
-        Lm[2][3] = kz * T(0.4) * rw / a2;
-        Lm[2][4] = -kz * T(0.4) / a2;
+        const T ph = phi * ia2;
+        const T g2 = T(0.4) * ia2;
+        Lm[0][0] = kx * (T(1.0) - ph) - ((kz * rv - ky * rw) * irr);
+        Lm[0][1] = kx * g2 * ru;
+        Lm[0][2] = (kx * g2 * rv) + (kz * irr);
+        Lm[0][3] = (kx * g2 * rw) - (ky * irr);
+        Lm[0][4] = -kx * g2;
+        Lm[1][0] = ky * (T(1.0) - ph) - ((kx * rw - kz * ru) * irr);
+        Lm[1][1] = (ky * g2 * ru) - kz * irr;
+        Lm[1][2] = ky * g2 * rv;
+        Lm[1][3] = (ky * g2 * rw) + (kx * irr);
+        Lm[1][4] = -ky * g2;
+        Lm[2][0] = kz * (T(1.0) - ph) - ((ky * ru - kx * rv) * irr);
+        Lm[2][1] = kz * g2 * ru + (ky * irr);
+        Lm[2][2] = kz * g2 * rv - (kx * irr);
+        Lm[2][3] = kz * g2 * rw;
+        Lm[2][4] = -kz * g2;
         Lm[3][0] = beta * (phi - theta * a);
         Lm[3][1] = -beta * (T(0.4) * ru - kx * a);
         Lm[3][2] = -beta * (T(0.4) * rv - ky * a);
@@ -93,130 +98,7 @@ struct FaceEigen {
         Lm[4][4] = beta * T(0.4);
     }
 
-    // Right eigenvectors times a characteristic vector c (Weno.cl:349-380 and
-    // the back-projection 2188-2289): q = R c.
-    __device__ __forceinline__ void right_times(const T c[5], T q[5]) const
-    {
-        const T e0 = ((phi + a * a) / T(0.4));
-        q[0] = kx * c[0] + ky * c[1] + kz * c[2] + alpha * c[3] + alpha * c[4];
-        q[1] = (kx * ru) * c[0] + (ky * ru - kz * rr) * c[1] + (kz * ru + ky * rr) * c[2]
-               + (alpha * (ru + kx * a)) * c[3] + (alpha * (ru - kx * a)) * c[4];
-        q[2] = (kx * rv + kz * rr) * c[0] + (ky * rv) * c[1] + (kz * rv - kx * rr) * c[2]
-               + (alpha * (rv + ky * a)) * c[3] + (alpha * (rv - ky * a)) * c[4];
-        q[3] = (kx * rw - ky * rr) * c[0] + (ky * rw + kx * rr) * c[1] + (kz * rw) * c[2]
-               + (alpha * (rw + kz * a)) * c[3] + (alpha * (rw - kz * a)) * c[4];
-        q[4] = (((kx * phi) / T(0.4)) + rr * (kz * rv - ky * rw)) * c[0]
-               + (((ky * phi) / T(0.4)) + rr * (kx * rw - kz * ru)) * c[1]
-               + (((kz * phi) / T(0.4)) + rr * (ky * ru - kx * rv)) * c[2]
-               + (alpha * (e0 + theta * a)) * c[3] + (alpha * (e0 - theta * a)) * c[4];
-    }
 };
-
-// WENO5 nonlinear interpolation of one characteristic variable to the face
-// between c[2] (left node) and c[3] (right node); c[0..5] are the six nodes
-// left-2 .. right+2.  Right-biased ("pos", linear weights 1/16, 5/8, 5/16)
-// and left-biased ("neg", 5/16, 5/8, 1/16) values, Jiang-Shu smoothness
-// indicators and weights d_k/(eps+IS_k)^2 (Weno.cl:1056-1280).
-template <class T>
-__device__ __forceinline__ void weno_pair(const T c[6], T eps, T &pos, T &neg)
-{
-    const T cm2 = c[0], cm1 = c[1], c0 = c[2], c1 = c[3], c2 = c[4], c3 = c[5];
-    const T p0 = (T(15.0) / T(8.0)) * c1 - (T(5.0) / T(4.0)) * c2 + (T(3.0) / T(8.0)) * c3;
-    const T p1 = (T(3.0) / T(8.0)) * c0 + (T(3.0) / T(4.0)) * c1 - (T(1.0) / T(8.0)) * c2;
-    const T p2 = (T(-1.0) / T(8.0)) * cm1 + (T(3.0) / T(4.0)) * c0 + (T(3.0) / T(8.0)) * c1;
-    const T m2 = (T(3.0) / T(8.0)) * cm2 - (T(5.0) / T(4.0)) * cm1 + (T(15.0) / T(8.0)) * c0;
-    // candidates m0 == p1 and m1 == p2 (same stencils, same arithmetic)
-    const T k13 = T(13.0) / T(12.0), k14 = T(1.0) / T(4.0);
-    const T ISm2 = k13 * sqr(cm2 - T(2.0) * cm1 + c0) + k14 * sqr(cm2 - T(4.0) * cm1 + T(3.0) * c0);
-    const T ISm1 = k13 * sqr(cm1 - T(2.0) * c0 + c1) + k14 * sqr(cm1 - c1);
-    const T ISm0 = k13 * sqr(c0 - T(2.0) * c1 + c2) + k14 * sqr(T(3.0) * c0 - T(4.0) * c1 + c2);
-    const T ISp2 = k13 * sqr(cm1 - T(2.0) * c0 + c1) + k14 * sqr(cm1 - T(4.0) * c0 + T(3.0) * c1);
-    const T ISp1 = k13 * sqr(c0 - T(2.0) * c1 + c2) + k14 * sqr(c0 - c2);
-    const T ISp0 = k13 * sqr(c1 - T(2.0) * c2 + c3) + k14 * sqr(T(3.0) * c1 - T(4.0) * c2 + c3);
-    const T d16 = T(1.0) / T(16.0), d58 = T(5.0) / T(8.0), d516 = T(5.0) / T(16.0);
-    // w_k = d_k / (eps + IS_k)^2, normalised once: sum(w_k x_k) / sum(w_k)
-    {
-        const T w0 = d16 / sqr(eps + ISp0), w1 = d58 / sqr(eps + ISp1), w2 = d516 / sqr(eps + ISp2);
-        pos = (w0 * p0 + w1 * p1 + w2 * p2) / (w0 + w1 + w2);
-    }
-    {
-        const T w0 = d516 / sqr(eps + ISm0), w1 = d58 / sqr(eps + ISm1), w2 = d16 / sqr(eps + ISm2);
-        neg = (w0 * p1 + w1 * p2 + w2 * m2) / (w0 + w1 + w2);
-    }
-}
-
-// Contravariant Euler flux of a face state q (conserved, per unit volume)
-// through the face metric (mx,my,mz): mx*F + my*E + mz*G with the Cartesian
-// fluxes of Weno.cl:2291-2507 (p = 0.4 (E - |m|^2/(2 rho)), E + p =
-// 1.4 E - 0.2 |m|^2/rho).  Also returns lambda_5 = U.m + c|m| of
-// Weno.cl:2511-2583 (element [4]).
-template <class T>
-__device__ __forceinline__ T contravariant_flux(const T q[5], T mx, T my, T mz, T f[5])
-{
-    const T ir = T(1.0) / q[0];
-    const T u = q[1] * ir, v = q[2] * ir, w = q[3] * ir;
-    const T ke2 = q[1] * u + q[2] * v + q[3] * w;        // |m|^2 / rho
-    const T pr = T(0.4) * (q[4] - T(0.5) * ke2);
-    const T hq = (T(1.4) * q[4] - T(0.2) * ke2);
-    const T un = mx * u + my * v + mz * w;
-    f[0] = q[0] * un;
-    f[1] = q[1] * un + mx * pr;
-    f[2] = q[2] * un + my * pr;
-    f[3] = q[3] * un + mz * pr;
-    f[4] = hq * un;
-    const T e = q[4] * ir - T(0.5) * (u * u + v * v + w * w);
-    const T c2k = T(1.4) * T(0.4) * e * (mx * mx + my * my + mz * mz);
-    return un + sqrt(c2k);
-}
-
-// Full LLF face flux of one face: Roe eigenvectors, characteristic
-// projection of the six stencil points, WENO5 both sides, back-projection,
-// contravariant fluxes x face det, lambda_5 based LLF (Weno.cl:2859-2947):
-// Fhat = 0.5 (Fp + Fn - alpha (det qp - det qn)),  alpha = max |lambda_5|.
-// pts[k][c]: conserved Q of nodes left-2 .. right+2.
-template <class T>
-__device__ __forceinline__ void llf_face_flux(const T pts[6][5], T mx, T my, T mz, T det_f, const T roe[5],
-                                              T eps, T Fhat[5])
-{
-    FaceEigen<T> eg;
-    eg.init(mx, my, mz, roe);
-    T cpos[5], cneg[5];
-    {
-        T Lm[5][5];
-        eg.left(Lm);
-#pragma unroll
-        for (int r = 0; r < 5; ++r) {
-            T cv[6];
-#pragma unroll
-            for (int k = 0; k < 6; ++k)
-                cv[k] = Lm[r][0] * pts[k][0] + Lm[r][1] * pts[k][1] + Lm[r][2] * pts[k][2] + Lm[r][3] * pts[k][3]
-                        + Lm[r][4] * pts[k][4];
-            weno_pair(cv, eps, cpos[r], cneg[r]);
-        }
-    }
-    T qp[5], qn[5];
-    eg.right_times(cpos, qp);
-    eg.right_times(cneg, qn);
-    T fp[5], fn[5];
-    const T lp = contravariant_flux(qp, mx, my, mz, fp);
-    const T ln = contravariant_flux(qn, mx, my, mz, fn);
-    const T alpha = fmax(fabs(lp), fabs(ln));
-#pragma unroll
-    for (int c = 0; c < 5; ++c)
-        Fhat[c] = T(0.5) * (det_f * fp[c] + det_f * fn[c] - alpha * (det_f * qp[c] - det_f * qn[c]));
-}
-
-// Sixth-order midpoint-and-node correction of a face flux (Weno.cl:2950-3058):
-// Fh = Fhat - d2/24 + 7 d4/5760 with d2 = (-5,39,-34,-34,39,-5)/48 and
-// d4 = (1,-3,2,2,-3,1)/2 of the node fluxes f[0..5] = left-2 .. right+2.
-template <class T>
-__device__ __forceinline__ T face_correction(const T f[6])
-{
-    const T d2 = (T(1.0) / T(48.0)) * (T(-5.0) * f[0] + T(39.0) * f[1] - T(34.0) * f[2] - T(34.0) * f[3]
-                                       + T(39.0) * f[4] - T(5.0) * f[5]);
-    const T d4 = (T(1.0) / T(2.0)) * (f[0] - T(3.0) * f[1] + T(2.0) * f[2] + T(2.0) * f[3] - T(3.0) * f[4] + f[5]);
-    return -(T(1.0) / T(24.0)) * d2 + (T(7.0) / T(5760.0)) * d4;
-}
 
 // Location-code-driven first derivative of the Viscous kernel
 // (Viscous.cl:285-332; the same branch set for eta and xi).  f[0..6] are the
@@ -261,16 +143,17 @@ struct Phys {
 // three directions (Viscous.cl:439-631), FMA-friendly rewrite for the
 // mixed-precision form (T = float there).  dU[d][c]: derivative of U_c along
 // direction d; Ui: U at the node; m: node metrics (9); det: node det;
-// prim: rho,u,v,w,p of FLOW at the node; KS: the three MTS test-filter
-// velocity-difference squares.  Writes contravariant Fv/Ev/Gv (x det) and mu.
+// DEL: the filter width det^(-1/3); prim: rho,u,v,w,p of FLOW at the node;
+// KS: the three MTS test-filter velocity-difference squares.  Writes
+// contravariant Fv/Ev/Gv (x det) and mu.
 template <class T>
-__device__ __forceinline__ void viscous_node_flux(const T dU[3][5], const T Ui[5], const T m[9], T det,
+__device__ __forceinline__ void viscous_node_flux(const T dU[3][5], const T Ui[5], const T m[9], T det, T DEL,
                                                   const T prim[5], const T KS[3], const Phys &P, T Fv[5], T Ev[5],
                                                   T Gv[5], T &mu_out)
 {
     const T Mach = (T)P.mach, Reyl = (T)P.reynolds, Pr = (T)P.prandtl, Free_t = (T)P.t_inf;
     const T U0 = Ui[0], U1 = Ui[1], U2 = Ui[2], U3 = Ui[3], U4 = Ui[4];
-    const T iU0 = T(1.0) / U0;
+    const T iU0 = qdiv(T(1.0), U0);
     const T iU00 = iU0 * iU0;
     T uc[3], vc[3], wc[3], tc[3];
 #pragma unroll
@@ -288,7 +171,7 @@ __device__ __forceinline__ void viscous_node_flux(const T dU[3][5], const T Ui[5
     const T d_temp = (T(1.4) * Mach * Mach * T(0.4) * ((U4 * iU0) - T(0.5) * (uu * uu + vv * vv + ww * ww)));
     const T sd = sqrt(d_temp);
     const T S = T(110.4) / Free_t;
-    const T mu = (sd * sd * sd) * ((T(1.0) + S) / (d_temp + S));
+    const T mu = (sd * sd * sd) * qdiv(T(1.0) + S, d_temp + S);
     mu_out = mu;
 
     const T zx = m[0], zy = m[1], zz = m[2], ex = m[3], ey = m[4], ez = m[5], xx = m[6], xy = m[7], xz = m[8];
@@ -301,9 +184,9 @@ __device__ __forceinline__ void viscous_node_flux(const T dU[3][5], const T Ui[5
     const T dtdx = tc[0] * zx + tc[1] * ex + tc[2] * xx, dtdy = tc[0] * zy + tc[1] * ey + tc[2] * xy,
             dtdz = tc[0] * zz + tc[1] * ez + tc[2] * xz;
 
-    const T kq = -(mu * T(1.4) / (Pr * Reyl));
+    const T kq = -(mu * T(1.4) * qdiv(T(1.0), Pr * Reyl));
     const T qx_ = kq * dtdx, qy_ = kq * dtdy, qz_ = kq * dtdz;   // Viscous.cl:461-463
-    const T mr = mu / Reyl;                                       // Viscous.cl:466-476
+    const T mr = mu * qdiv(T(1.0), Reyl);                                       // Viscous.cl:466-476
     const T txx = mr * (T(4.0 / 3.0) * dudx - T(2.0 / 3.0) * dvdy - T(2.0 / 3.0) * dwdz);
     const T tyy = mr * (T(4.0 / 3.0) * dvdy - T(2.0 / 3.0) * dudx - T(2.0 / 3.0) * dwdz);
     const T tzz = mr * (T(4.0 / 3.0) * dwdz - T(2.0 / 3.0) * dudx - T(2.0 / 3.0) * dvdy);
@@ -316,14 +199,13 @@ __device__ __forceinline__ void viscous_node_flux(const T dU[3][5], const T Ui[5
         const T s_xy = T(0.5) * sxy, s_yz = T(0.5) * syz, s_xz = T(0.5) * sxz;
         const T mod = sqrt(T(2.0) * ((s_xy * s_xy + s_yz * s_yz + s_xz * s_xz)
                                      + T(2.0 / 3.0) * (dudx * dudx + dvdy * dvdy + dwdz * dwdz)));
-        const T DEL = T(1.0) / cbrt(det);
         T ed[3];
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             const T sk = sqrt(KS[d]);
             if (mod != T(0.0)) {
-                const T R = (DEL * mod) / sk;
-                ed[d] = (C_MTS / (T(1.0) + R / C_T)) * DEL * sk;
+                const T R = qdiv(DEL * mod, sk);
+                ed[d] = qdiv(C_MTS, T(1.0) + R * (T(1.0) / C_T)) * DEL * sk;
             } else {
                 ed[d] = C_MTS * DEL * sk;
             }
@@ -335,7 +217,7 @@ __device__ __forceinline__ void viscous_node_flux(const T dU[3][5], const T Ui[5
         TXX = r2 * ed[0] * dudx;
         TYY = r2 * ed[1] * dvdy;
         TZZ = r2 * ed[2] * dwdz;
-        const T kQ = -(T(1.0) / (T(1.4) * T(0.4) * Mach * Mach));
+        const T kQ = -qdiv(T(1.0), T(1.4) * T(0.4) * Mach * Mach);
         const T Qx = kQ * ed[0] * dtdx, Qy = kQ * ed[1] * dtdy, Qz = kQ * ed[2] * dtdz;
         HX = Qx + (TXX + TXY + TXZ) * prim[1];
         HY = Qy + (TXY + TYY + TYZ) * prim[2];

@@ -120,7 +120,7 @@ cfd_status_t create_structured(cfd_solver *s, const cfd_geometry_t *g)
         if ((st = dalloc_t(s, 5 * N, &S.Q32)) || (st = dalloc_t(s, 5 * N, &S.R32)) || (st = dalloc_t(s, 15 * N, &S.FEG32))
             || (st = dalloc_t(s, 15 * N, &S.V32)) || (st = dalloc_t(s, 15 * N, &S.Fh32))
             || (st = dalloc_t(s, 9 * N, &S.fm32)) || (st = dalloc_t(s, 3 * N, &S.fdet32))
-            || (st = dalloc_t(s, 10 * N, &S.node32)) || (st = dalloc_t(s, 2 * N, &S.idet32))
+            || (st = dalloc_t(s, 11 * N, &S.node32)) || (st = dalloc_t(s, 2 * N, &S.idet32))
             || (st = dalloc_t(s, 9 * N, &S.prim32)))
             return st;
         cudaMemsetAsync(S.V32, 0, 15 * N * sizeof(float), S.stream);

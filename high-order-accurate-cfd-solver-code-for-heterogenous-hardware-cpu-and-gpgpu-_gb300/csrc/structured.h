@@ -34,7 +34,7 @@ struct StructuredLaunch {
     float *Fh32 = nullptr;     // [3][5][N]
     float *fm32 = nullptr;     // [3][3][N]
     float *fdet32 = nullptr;   // [3][N]
-    float *node32 = nullptr;   // [10][N] node metrics, det
+    float *node32 = nullptr;   // [11][N] node metrics, det, det^(-1/3)
     float *idet32 = nullptr;   // [2][N] 1/det hi, lo
     float *prim32 = nullptr;   // [9][N] FLOW in FP32
 };
