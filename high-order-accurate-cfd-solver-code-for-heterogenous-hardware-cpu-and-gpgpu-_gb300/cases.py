@@ -47,6 +47,21 @@ class Params:
 
 
 @dataclasses.dataclass
+class BoundaryLists:
+    """Node lists of the reference's boundary routine intialise()
+    (Flow_Initialisation.cpp:23-1394): row indices, visited in order,
+    outlet, then inlet, boundary (mirror copy) and wall (no-slip)."""
+    outlet: np.ndarray
+    inlet: np.ndarray
+    boundary: np.ndarray
+    wall: np.ndarray
+
+    def __post_init__(self):
+        for k in ("outlet", "inlet", "boundary", "wall"):
+            setattr(self, k, np.ascontiguousarray(getattr(self, k), dtype=np.int32))
+
+
+@dataclasses.dataclass
 class Case:
     name: str
     shape: tuple            # (ni, nj, nk) of owned nodes for structured cases
@@ -56,6 +71,7 @@ class Case:
     arrays: dict            # layout.empty_arrays(g_node + 1) filled
     params: Params
     dt: float
+    bc: BoundaryLists | None = None   # boundary routine lists (non-periodic cases)
 
     @property
     def n_rows(self) -> int:
@@ -335,7 +351,37 @@ def taylor_green(n=128, amp=0.05, mach=0.1, reynolds=1600.0, prandtl=0.72, t_inf
                 cfl_dt(a, rows, cfl))
 
 
-def ghost_box(shape=(10, 9, 8), seed=0, mach=1.5, amp=0.05) -> Case:
+# Boundary codes of owned nodes by the box faces they lie on, in the
+# reference's convention: a face code names the missing neighbour
+# (Flow_Initialisation.cpp:55-89: 1 no +j, 2 no +i, 3 no -j, 4 no -i,
+# 5 no -k, 6 no +k); edge and corner codes are those whose copy chains
+# (:139-340) step from the node into the interior.
+_EDGE_CODES = {("jmin", "kmax"): 15, ("imin", "jmin"): 16, ("jmin", "kmin"): 17, ("imax", "jmin"): 18,
+               ("jmax", "kmax"): 19, ("imin", "jmax"): 20, ("jmax", "kmin"): 21, ("imax", "jmax"): 22,
+               ("imin", "kmax"): 23, ("imin", "kmin"): 24, ("imax", "kmin"): 25, ("imax", "kmax"): 26}
+_CORNER_CODES = {("imin", "jmax", "kmax"): 7, ("imin", "jmax", "kmin"): 8, ("imax", "jmax", "kmin"): 9,
+                 ("imax", "jmax", "kmax"): 10, ("imin", "jmin", "kmax"): 11, ("imin", "jmin", "kmin"): 12,
+                 ("imax", "jmin", "kmin"): 13, ("imax", "jmin", "kmax"): 14}
+_FACE_CODES = {"jmax": 1, "imax": 2, "jmin": 3, "imin": 4, "kmin": 5, "kmax": 6}
+
+
+def reference_loc_codes(imin, imax, jmin, jmax, kmin, kmax) -> np.ndarray:
+    """loc of nodes from boolean masks of the six box faces (0 = interior)."""
+    flags = {"imin": imin, "imax": imax, "jmin": jmin, "jmax": jmax, "kmin": kmin, "kmax": kmax}
+    loc = np.zeros(np.shape(imin), dtype=np.int64)
+    count = sum(np.asarray(f, dtype=int) for f in flags.values())
+    for name, code in _FACE_CODES.items():
+        loc = np.where((count == 1) & flags[name], code, loc)
+    for names, code in _EDGE_CODES.items():
+        m = (count == 2) & np.logical_and.reduce([flags[n] for n in names])
+        loc = np.where(m, code, loc)
+    for names, code in _CORNER_CODES.items():
+        m = (count == 3) & np.logical_and.reduce([flags[n] for n in names])
+        loc = np.where(m, code, loc)
+    return loc
+
+
+def ghost_box(shape=(10, 9, 8), seed=0, mach=1.5, amp=0.05, bc: bool = False) -> Case:
     """Non-periodic box of owned nodes with three ghost layers on every side.
 
     Owned nodes carry ``loc`` = 0 in the interior and a code in 1..26 on the
@@ -388,12 +434,7 @@ def ghost_box(shape=(10, 9, 8), seed=0, mach=1.5, amp=0.05) -> Case:
     put("N4", nb(0, 0, 1))
     put("N5", nb(0, 0, -1))
     put("ID", order)
-    # boundary codes: count of box faces a node lies on -> distinct codes
-    on = [(ii == G) | (ii == G + ni - 1), (jj == G) | (jj == G + nj - 1), (kk == G) | (kk == G + nk - 1)]
-    face_code = (1 * (ii == G) + 2 * (ii == G + ni - 1) + 3 * (jj == G) + 4 * (jj == G + nj - 1)
-                 + 5 * (kk == G) + 6 * (kk == G + nk - 1))
-    nfaces = on[0].astype(int) + on[1].astype(int) + on[2].astype(int)
-    loc = np.where(nfaces == 0, 0, np.where(nfaces == 1, face_code, np.where(nfaces == 2, 6 + face_code, 14 + face_code)))
+    loc = reference_loc_codes(ii == G, ii == G + ni - 1, jj == G, jj == G + nj - 1, kk == G, kk == G + nk - 1)
     loc = np.where(owned, loc, 100)
     put("loc", loc)
 
@@ -428,4 +469,29 @@ def ghost_box(shape=(10, 9, 8), seed=0, mach=1.5, amp=0.05) -> Case:
     a["flow"][order.ravel()] = flow
     rows = np.arange(1, n_owned + 1)
     prm = Params(mach=mach)
-    return Case("ghost_box", (ni, nj, nk), False, n_owned, n_all, a, prm, cfl_dt(a, rows, 0.3))
+    c = Case("ghost_box", (ni, nj, nk), False, n_owned, n_all, a, prm, cfl_dt(a, rows, 0.3))
+    if bc:
+        # ID 10 marks the reference's singular wall nodes; the box has none
+        a["grid"]["ID"][:] = 0
+        c.bc = box_boundary_lists(a["grid"]["loc"], n_owned)
+    return c
+
+
+# Boundary type of each box face for ghost_box(bc=True): every type of the
+# boundary routine appears, edges and corners included.
+_BOX_FACE_TYPE = {4: "inlet", 2: "outlet", 3: "wall", 1: "boundary", 5: "wall", 6: "outlet"}
+_TYPES = ("outlet", "inlet", "boundary", "wall")
+
+
+def box_boundary_lists(loc: np.ndarray, sd_node: int) -> BoundaryLists:
+    """Lists of the owned boundary rows 1..sd_node by their loc code: face
+    codes by _BOX_FACE_TYPE, edge and corner codes 7..26 round-robin over
+    the four types."""
+    lists = {t: [] for t in _TYPES}
+    for r in range(1, sd_node + 1):
+        code = int(loc[r])
+        if 1 <= code <= 6:
+            lists[_BOX_FACE_TYPE[code]].append(r)
+        elif 7 <= code <= 26:
+            lists[_TYPES[code % 4]].append(r)
+    return BoundaryLists(**{t: np.array(v) for t, v in lists.items()})

@@ -43,6 +43,17 @@ class OrCase(C.Structure):
                            "F", "E", "G", "Fv", "Ev", "Gv", "roe")]
 
 
+class OrBcLists(C.Structure):
+    _fields_ = [("outlet", _vp), ("inlet", _vp), ("boundary", _vp), ("wall", _vp),
+                ("n_outlet", C.c_int), ("n_inlet", C.c_int), ("n_boundary", C.c_int), ("n_wall", C.c_int)]
+
+
+def make_bc(bc) -> OrBcLists:
+    """ctypes view of a cases.BoundaryLists (the arrays must stay alive)."""
+    return OrBcLists(_p(bc.outlet), _p(bc.inlet), _p(bc.boundary), _p(bc.wall),
+                     len(bc.outlet), len(bc.inlet), len(bc.boundary), len(bc.wall))
+
+
 def build(force: bool = False) -> None:
     """Compile the restatement (and the reference pin where possible)."""
     src = HERE / "cfd_oracle.c"
@@ -51,7 +62,9 @@ def build(force: bool = False) -> None:
         subprocess.run(["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
                         str(src), "-o", str(LIB), "-lm"], check=True)
     ref_dir = pathlib.Path(os.environ.get("CFD_REFERENCE_DIR", "/root/reference"))
-    if (ref_dir / "Weno.cl").exists() and (force or not REF_LIB.exists()):
+    ref_srcs = [HERE / n for n in ("build_ref.sh", "ref_kernels.cpp", "ref_bc.cpp", "ref_shim.h", "bc_ref_shim.h")]
+    stale = not REF_LIB.exists() or REF_LIB.stat().st_mtime < max(p.stat().st_mtime for p in ref_srcs)
+    if (ref_dir / "Weno.cl").exists() and (force or stale):
         subprocess.run(["bash", str(HERE / "build_ref.sh")], check=True)
 
 
@@ -71,6 +84,11 @@ def lib():
         _lib.oracle_viscous.argtypes = [C.c_int, C.POINTER(OrParams)] + [_vp] * 11
         _lib.oracle_weno.argtypes = ([C.c_int, C.c_int, C.c_double, C.c_double, C.POINTER(OrParams)]
                                      + [_vp] * 17)
+        _lib.oracle_boundary_fill.argtypes = [_vp, _vp, C.POINTER(OrBcLists), C.c_double, C.c_int, C.c_int]
+        _lib.oracle_boundary_fill.restype = C.c_int
+        _lib.oracle_rk3_steps_bc.argtypes = [C.POINTER(OrCase), C.POINTER(OrParams), C.c_double, C.c_int,
+                                             C.POINTER(OrBcLists)]
+        _lib.oracle_rk3_steps_bc.restype = C.c_int
         _lib.oracle_set_threads.argtypes = [C.c_int]
         _lib.oracle_set_poison.argtypes = [C.c_int]
         _lib.oracle_get_threads.restype = C.c_int
@@ -89,6 +107,8 @@ def ref():
         _ref.ref_viscous.argtypes = [C.c_int] + [_vp] * 11
         _ref.ref_viscous_param.argtypes = [C.c_int] + [C.c_double] * 4 + [_vp] * 11
         _ref.ref_weno.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double] + [_vp] * 16
+        _ref.ref_boundary_fill.argtypes = ([_vp, _vp, C.c_int] + [_vp, C.c_int] * 4
+                                           + [C.c_double, C.c_int, C.c_int])
     return _ref
 
 
@@ -135,6 +155,24 @@ def rk3_steps(arrays: dict, g_node: int, sd_node: int, params, dt: float, nsteps
     lib().oracle_rk3_steps(C.byref(c), C.byref(pr), float(dt), int(nsteps))
 
 
+def boundary_fill(arrays: dict, bc, mach: float, initial: int = 1, sd_node: int = 0) -> None:
+    """The boundary routine (intialise) on arrays["flow"] in place."""
+    lists = make_bc(bc)
+    rc = lib().oracle_boundary_fill(_p(arrays["grid"]), _p(arrays["flow"]), C.byref(lists), float(mach),
+                                    int(initial), int(sd_node))
+    if rc != 0:
+        raise ValueError("boundary lists need the reference's singular-node table")
+
+
+def rk3_steps_bc(arrays: dict, g_node: int, sd_node: int, params, dt: float, nsteps: int, bc) -> None:
+    """rk3_steps with the boundary routine after every stage."""
+    c = make_case(arrays, g_node, sd_node)
+    pr = make_params(params)
+    lists = make_bc(bc)
+    if lib().oracle_rk3_steps_bc(C.byref(c), C.byref(pr), float(dt), int(nsteps), C.byref(lists)) != 0:
+        raise ValueError("boundary lists need the reference's singular-node table")
+
+
 def uq(a: dict, n_items: int, U_out: np.ndarray) -> None:
     lib().oracle_uq(n_items, _p(U_out), _p(a["Q"]), _p(a["grid"]), _p(a["det"]), _p(a["flow"]), _p(a["roe"]))
 
@@ -179,6 +217,14 @@ def ref_weno(a: dict, n_items: int, mach: float, j: int, dt: float) -> None:
     ref().ref_weno(n_items, int(j), float(mach), float(dt), _p(a["deter"]), _p(a["det"]), _p(a["U0"]),
                    _p(a["U1"]), _p(a["U2"]), _p(a["grid"]), _p(a["Q"]), _p(a["metric"]), _p(a["roe"]),
                    _p(a["Fv"]), _p(a["Ev"]), _p(a["Gv"]), _p(a["F"]), _p(a["E"]), _p(a["G"]), _p(a["flow"]))
+
+
+def ref_boundary_fill(arrays: dict, bc, mach: float, initial: int = 1, sd_node: int = 0) -> None:
+    """The reference's own intialise() on arrays["flow"] in place."""
+    n = arrays["flow"].shape[0]
+    ref().ref_boundary_fill(_p(arrays["grid"]), _p(arrays["flow"]), n, _p(bc.outlet), len(bc.outlet),
+                            _p(bc.inlet), len(bc.inlet), _p(bc.boundary), len(bc.boundary), _p(bc.wall),
+                            len(bc.wall), float(mach), int(initial), int(sd_node))
 
 
 def ref_stage(a: dict, g_node: int, sd_node: int, params, j: int, dt: float) -> None:

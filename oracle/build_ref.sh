@@ -1,10 +1,12 @@
 #!/usr/bin/env bash
 # Builds the parity pin: the reference's own kernel sources (U_Q.cl,
 # Viscous.cl, Weno.cl), compiled where they lie as host C++ through
-# oracle/ref_shim.h, into oracle/_ref/libcfd_ref.so.  Outputs go only to
-# oracle/_ref/ (git-ignored).  The one generated file is a copy of Viscous.cl
-# whose four hard-coded constants (Mach, Reyl, Pr, Free_t) read globals, so
-# the pin also covers other flow parameters.  Needs the reference checkout;
+# oracle/ref_shim.h, and its boundary routine (Flow_Initialisation.cpp)
+# through oracle/bc_ref_shim.h, into oracle/_ref/libcfd_ref.so.  Outputs go only to
+# oracle/_ref/ (git-ignored).  Generated files: a copy of Viscous.cl whose
+# four hard-coded constants (Mach, Reyl, Pr, Free_t) read globals, so the pin
+# also covers other flow parameters, and a copy of Flow_Initialisation.cpp
+# with its include lines pointed at the shim.  Needs the reference checkout;
 # exits 0 without building when it is absent.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
@@ -23,7 +25,13 @@ sed -e 's/const double Mach = 1\.5;/const double Mach = ::ref_visc_mach;/' \
 for c in ref_visc_mach ref_visc_reyl ref_visc_pr ref_visc_tinf; do
     grep -q "= ::$c;" "$OUT/Viscous_param.cl" || { echo "build_ref: substitution of $c failed" >&2; exit 1; }
 done
+# The boundary routine: a copy whose two include lines name the shim instead
+# of functions.h (MPI + OpenCL) and the MPI header.
+sed -e 's|#include "functions.h"|#include "bc_ref_shim.h"|' \
+    -e 's|#include <openmpi-x86_64/mpi.h>||' \
+    "$REF_DIR/Flow_Initialisation.cpp" > "$OUT/Flow_Initialisation_ref.cpp"
+grep -q '#include "bc_ref_shim.h"' "$OUT/Flow_Initialisation_ref.cpp" || { echo "build_ref: include substitution failed" >&2; exit 1; }
 g++ -std=c++17 -O2 -ffp-contract=off -fopenmp -fPIC -shared -w \
     -I"$HERE" -I"$OUT" -I"$REF_DIR" \
-    "$HERE/ref_kernels.cpp" -o "$OUT/libcfd_ref.so"
+    "$HERE/ref_kernels.cpp" "$HERE/ref_bc.cpp" "$OUT/Flow_Initialisation_ref.cpp" -o "$OUT/libcfd_ref.so"
 echo "build_ref: built $OUT/libcfd_ref.so"

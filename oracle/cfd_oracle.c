@@ -554,3 +554,171 @@ void oracle_rk3_steps(or_case *c, const or_params *prm, double del_t, int nsteps
     for (int n = 0; n < nsteps; ++n)
         for (int j = 0; j < 3; ++j) oracle_stage(c, prm, j, del_t, NULL);
 }
+
+/* ------------------------------------------------- boundary routine ---- */
+
+/* Missing-neighbour slot l (towards the ghosts) and inward slot k of the
+ * face boundary codes 1..6 (Flow_Initialisation.cpp:55-89): 1 no element
+ * north (+j), 2 east (+i), 3 south (-j), 4 west (-i), 5 (-k), 6 (+k). */
+static const int bc_face_l[7] = {-1, 0, 1, 2, 3, 5, 4};
+static const int bc_face_k[7] = {-1, 2, 3, 0, 1, 4, 5};
+
+/* Neighbour-slot chains from an edge or corner node (codes 7..26) to the
+ * node it copies (Flow_Initialisation.cpp:139-340 and the same chains in the
+ * inlet, boundary and wall sections); -1 ends a chain. */
+static const int bc_edge_chain[20][3] = {
+    {1, 5, 2}, {1, 4, 2}, {3, 4, 2}, {3, 5, 2}, {1, 5, 0}, {1, 4, 0}, {3, 4, 0}, {3, 5, 0},
+    {5, 0, -1}, {1, 0, -1}, {4, 0, -1}, {3, 0, -1}, {5, 2, -1}, {1, 2, -1}, {4, 2, -1}, {3, 2, -1},
+    {1, 5, -1}, {1, 4, -1}, {3, 4, -1}, {3, 5, -1}};
+
+static inline int bc_nb(const or_grid *g, int r, int slot)
+{
+    const int32_t *N = &g[r].N0;
+    return N[slot];
+}
+
+static inline void bc_derive_rho_e(or_flow *f, double mach)
+{
+    f->rho = (1.4 * mach * mach) * (f->p / f->t);
+    f->e = f->p / (0.4 * f->rho);
+}
+
+/* the eight fields the routine copies between nodes (mu is never touched) */
+static inline void bc_copy8(or_flow *dst, const or_flow *src)
+{
+    dst->u = src->u;
+    dst->v = src->v;
+    dst->w = src->w;
+    dst->p = src->p;
+    dst->rho = src->rho;
+    dst->t = src->t;
+    dst->a = src->a;
+    dst->e = src->e;
+}
+
+enum { BC_OUTLET = 0, BC_INLET = 1, BC_BOUNDARY = 2, BC_WALL = 3 };
+
+static int bc_wall_singular(const or_grid *g, int r)
+{
+    const int loc = g[r].loc;
+    return loc == 29 || loc == 30 || (loc >= 33 && loc <= 56) || g[r].ID == 10;
+}
+
+/* One list of the routine, visited in order (Flow_Initialisation.cpp:50-342
+ * outlet, 343-624 inlet, 625-909 boundary, 910-1394 wall). */
+static void bc_list(int type, const or_grid *g, or_flow *F, const int32_t *rows, int n, double mach)
+{
+    for (int q = 0; q < n; ++q) {
+        const int b = rows[q];
+        const int loc = g[b].loc;
+        if (loc >= 1 && loc <= 6) {
+            const int l = bc_face_l[loc], k = bc_face_k[loc];
+            const int g1 = bc_nb(g, b, l), g2 = bc_nb(g, g1, l), g3 = bc_nb(g, g2, l);
+            const int s1 = bc_nb(g, b, k), s2 = bc_nb(g, s1, k), s3 = bc_nb(g, s2, k);
+            or_flow *fb = &F[b];
+            if (type == BC_OUTLET) {          /* :92-137 */
+                fb->u = F[s1].u;
+                fb->v = F[s1].v;
+                fb->w = F[s1].w;
+                fb->p = F[s1].p;
+                fb->t = F[s1].t;
+                bc_derive_rho_e(fb, mach);
+                fb->a = sqrt(1.4 * fb->p / fb->rho);
+                bc_copy8(&F[g1], fb);
+                bc_copy8(&F[g2], fb);
+                bc_copy8(&F[g3], fb);
+            } else if (type == BC_INLET) {    /* :385-419 */
+                fb->u = 1.0;
+                fb->v = 0.0;
+                fb->w = 0.0;
+                fb->p = 1.0 / (1.4 * mach * mach);
+                fb->t = 1.0;
+                bc_derive_rho_e(fb, mach);
+                fb->a = sqrt(1.4 * fb->p / fb->rho);
+                bc_copy8(&F[g1], fb);
+                bc_copy8(&F[g2], fb);
+                bc_copy8(&F[g3], fb);
+            } else if (type == BC_BOUNDARY) { /* :667-704 */
+                bc_copy8(fb, &F[s1]);
+                bc_copy8(&F[g1], &F[s1]);
+                bc_copy8(&F[g2], &F[s2]);
+                bc_copy8(&F[g3], &F[s3]);
+            } else {                          /* :953-990 */
+                fb->u = 0.0;
+                fb->v = 0.0;
+                fb->w = 0.0;
+                fb->p = F[s1].p;
+                fb->t = F[s1].t;
+                bc_derive_rho_e(fb, mach);
+                fb->a = sqrt(1.4 * fb->p / fb->rho);
+                const int gs[3] = {g1, g2, g3}, ss[3] = {s1, s2, s3};
+                for (int m = 0; m < 3; ++m) {
+                    or_flow *fg = &F[gs[m]];
+                    const or_flow *fs = &F[ss[m]];
+                    fg->u = (-1.0) * fs->u;
+                    fg->v = (-1.0) * fs->v;
+                    fg->w = (-1.0) * fs->w;
+                    fg->p = fs->p;
+                    fg->rho = fs->rho;
+                    fg->t = fs->t;
+                    fg->a = fs->a;
+                    fg->e = fs->e;
+                }
+            }
+        } else if (loc >= 7 && loc <= 26) {
+            const int *ch = bc_edge_chain[loc - 7];
+            int s = b;
+            for (int m = 0; m < 3 && ch[m] >= 0; ++m) s = bc_nb(g, s, ch[m]);
+            or_flow *fb = &F[b];
+            if (type == BC_WALL) {
+                fb->u = 0.0;
+                fb->v = 0.0;
+                fb->w = 0.0;
+            } else {
+                fb->u = F[s].u;
+                fb->v = F[s].v;
+                fb->w = F[s].w;
+            }
+            fb->p = F[s].p;
+            fb->t = F[s].t;
+            bc_derive_rho_e(fb, mach);
+        }
+        /* other codes: the routine has no branch for them */
+    }
+}
+
+int oracle_boundary_fill(const or_grid *grid, or_flow *flow, const or_bc_lists *bc, double mach, int initial,
+                         int sd_node)
+{
+    for (int q = 0; q < bc->n_wall; ++q)
+        if (bc_wall_singular(grid, bc->wall[q])) return -1;
+    if (initial == 0) {   /* Flow_Initialisation.cpp:35-48 */
+        for (int r = 1; r <= sd_node; ++r) {
+            or_flow *f = &flow[r];
+            f->u = 1.0;
+            f->v = 0.0;
+            f->w = 0.0;
+            f->p = 1.0 / (1.4 * mach * mach);
+            f->t = 1.0;
+            f->rho = (1.4 * mach * mach) * (f->p / f->t);
+            f->e = f->p / (0.4 * f->rho);
+            f->a = sqrt(1.4 * f->p / f->rho);
+        }
+    }
+    bc_list(BC_OUTLET, grid, flow, bc->outlet, bc->n_outlet, mach);
+    bc_list(BC_INLET, grid, flow, bc->inlet, bc->n_inlet, mach);
+    bc_list(BC_BOUNDARY, grid, flow, bc->boundary, bc->n_boundary, mach);
+    bc_list(BC_WALL, grid, flow, bc->wall, bc->n_wall, mach);
+    return 0;
+}
+
+/* Solver.cpp:364-658: the boundary routine after every stage. */
+int oracle_rk3_steps_bc(or_case *c, const or_params *prm, double del_t, int nsteps, const or_bc_lists *bc)
+{
+    for (int n = 0; n < nsteps; ++n)
+        for (int j = 0; j < 3; ++j) {
+            oracle_stage(c, prm, j, del_t, NULL);
+            if (bc && oracle_boundary_fill(c->grid, c->flow, bc, prm->mach, 1, c->sd_node) != 0) return -1;
+        }
+    return 0;
+}

@@ -11,6 +11,7 @@
  *   Viscous.cl   -> oracle_viscous   (node fluxes F,E,G and viscous/SGS fluxes)
  *   Weno.cl      -> oracle_weno      (characteristic WENO5 + LLF + RK stage)
  *   Solver.cpp:365-658 -> oracle_rk3_step (U_Q, Viscous, Weno per stage)
+ *   Flow_Initialisation.cpp:23-1394 -> oracle_boundary_fill (ghost fill)
  * The structs below are the reference's packed ABI (functions.h:49-113).
  *
  * Parity pin: the restatement is checked against the reference's own kernel
@@ -83,6 +84,27 @@ void oracle_stage(or_case *c, const or_params *prm, int j, double del_t, or_col5
 
 /* nsteps full SSP-RK3 steps (three stages each). */
 void oracle_rk3_steps(or_case *c, const or_params *prm, double del_t, int nsteps);
+
+/* Boundary node lists of the reference's boundary routine intialise()
+ * (Flow_Initialisation.cpp:23-1394): row indices in visiting order.  The
+ * routine's second half (:1395-2742) applies the same rules to the
+ * subdomain lists sd_*_node; pass those as a second set. */
+typedef struct {
+    const int32_t *outlet, *inlet, *boundary, *wall;
+    int n_outlet, n_inlet, n_boundary, n_wall;
+} or_bc_lists;
+
+/* intialise(RK) restated: with initial == 0 rows 1..sd_node first get the
+ * free stream; then outlet, inlet, boundary and wall nodes in that order --
+ * face codes 1..6 with their three ghost layers, edge and corner codes 7..26
+ * from a diagonal node.  Returns -1 (and changes nothing) when a wall node
+ * needs the reference's singular-node table (ID 10, codes 29/30, 33..56). */
+int oracle_boundary_fill(const or_grid *grid, or_flow *flow, const or_bc_lists *bc, double mach, int initial,
+                         int sd_node);
+
+/* oracle_rk3_steps with the boundary routine after every stage
+ * (Solver.cpp:364-658).  bc may be NULL.  Returns -1 as above. */
+int oracle_rk3_steps_bc(or_case *c, const or_params *prm, double del_t, int nsteps, const or_bc_lists *bc);
 
 /* Undefined-branch poisoning (NaN) for masking checks; off by default. */
 void oracle_set_poison(int on);

@@ -1,6 +1,7 @@
 """Generates the golden vectors under tests/golden/ from the reference's own
-kernel sources (U_Q.cl, Viscous.cl, Weno.cl compiled as host C++ by
-oracle/build_ref.sh).  Run in a checkout that has the reference sources:
+sources (U_Q.cl, Viscous.cl, Weno.cl and the boundary routine
+Flow_Initialisation.cpp, compiled as host C++ by oracle/build_ref.sh).  Run
+in a checkout that has the reference sources:
 
     python tests/golden/make_golden.py
 
@@ -75,10 +76,38 @@ def poison_mask(case, stages=3):
     return masks
 
 
-def main():
+BC_MACH = 0.8
+
+
+def make_bc_golden():
+    """bc_ghostbox.npz: the reference's boundary routine intialise()
+    (Flow_Initialisation.cpp:23-1394) on a ghost box whose boundary rows are
+    split over the outlet, inlet, boundary and wall lists (face, edge and
+    corner codes), from a seeded random FLOW, with initial = 1 and 0."""
+    box = cases.ghost_box(shape=(5, 4, 4), seed=3, bc=True)
+    rng = np.random.default_rng(20261203)
+    flow = box.arrays["flow"].copy()
+    flow[1:] = rng.uniform(0.5, 1.5, flow[1:].shape)
+    payload = {"in_grid": box.arrays["grid"], "in_flow": flow, "sd_node": np.array(box.sd_node),
+               "mach": np.array(BC_MACH)}
+    for t in ("outlet", "inlet", "boundary", "wall"):
+        payload[f"list_{t}"] = getattr(box.bc, t)
+    for initial in (1, 0):
+        a = {"grid": box.arrays["grid"].copy(), "flow": flow.copy()}
+        oracle.ref_boundary_fill(a, box.bc, BC_MACH, initial, box.sd_node)
+        payload[f"out_flow_initial{initial}"] = a["flow"]
+    np.savez_compressed(HERE / "bc_ghostbox.npz", **payload)
+    print("bc_ghostbox ->", (HERE / "bc_ghostbox.npz").stat().st_size, "bytes")
+
+
+def main(only=None):
     oracle.build()
     if not oracle.ref_available():
         raise SystemExit("reference build missing: run oracle/build_ref.sh in a checkout with the reference")
+    if only in (None, "bc"):
+        make_bc_golden()
+    if only == "bc":
+        return
     for name, case in golden_cases().items():
         stages = 1 if name == "ghostbox" else 3
         res = run(case, stages)
@@ -96,4 +125,5 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    # python tests/golden/make_golden.py [bc]   (bc: only the boundary-routine fixture)
+    main(sys.argv[1] if len(sys.argv) > 1 else None)
