@@ -86,6 +86,10 @@ PROTOTYPES = {
     "cfd_solver_stage": (C.c_int, [_vp, _i32, _d, _vp]),
     "cfd_solver_profile_stage": (C.c_int, [_vp, _i32, _d, _vp, _i32, C.POINTER(_i32)]),
     "cfd_probe_flops": (C.c_int, [_vp, _i32, C.POINTER(_d)]),
+    "cfd_bc_create": (C.c_int, [_vp, _vp, _i32] + [_vp, _i32] * 4 + [C.POINTER(_vp)]),
+    "cfd_bc_destroy": (C.c_int, [_vp]),
+    "cfd_boundary_fill": (C.c_int, [_vp, _vp, _vp, _d, _i32, _i32]),
+    "cfd_solver_set_boundary": (C.c_int, [_vp, _vp]),
     "cfd_batch_create": (C.c_int, [_vp, _i32, C.c_uint64, C.POINTER(_vp)]),
     "cfd_batch_destroy": (C.c_int, [_vp]),
     "cfd_batch_instance_bytes": (C.c_uint64, [_i32, C.c_int64]),

@@ -495,3 +495,156 @@ def box_boundary_lists(loc: np.ndarray, sd_node: int) -> BoundaryLists:
         elif 7 <= code <= 26:
             lists[_TYPES[code % 4]].append(r)
     return BoundaryLists(**{t: np.array(v) for t, v in lists.items()})
+
+
+# ------------------------------------------------- ghosted lattices ---
+
+GHOSTS = 3   # ghost layers beyond the owned nodes of a non-periodic direction
+
+
+def _index_derivative(X: np.ndarray, axis: int, periodic: bool, period: float = 0.0) -> np.ndarray:
+    """d X / d (index) along `axis`: 4th-order central (wrapped when
+    periodic, X(c + n) = X(c) + period); 2nd-order at the two outermost
+    layers of a non-periodic direction (ghost layers only)."""
+    if periodic:
+        n = X.shape[axis]
+        c = np.arange(n).reshape([-1 if a == axis else 1 for a in range(X.ndim)])
+
+        def r(s):   # X[c + s] continued across the wrap
+            return np.roll(X, -s, axis=axis) + period * np.floor_divide(c + s, n)
+        return (r(-2) - 8.0 * r(-1) + 8.0 * r(1) - r(2)) / 12.0
+    n = X.shape[axis]
+    Xt = np.moveaxis(X, axis, 0)
+    D = np.empty_like(Xt)
+    D[2:n - 2] = (Xt[0:n - 4] - 8.0 * Xt[1:n - 3] + 8.0 * Xt[3:n - 1] - Xt[4:n]) / 12.0
+    D[0] = (-3.0 * Xt[0] + 4.0 * Xt[1] - Xt[2]) / 2.0
+    D[1] = (Xt[2] - Xt[0]) / 2.0
+    D[n - 2] = (Xt[n - 1] - Xt[n - 3]) / 2.0
+    D[n - 1] = (3.0 * Xt[n - 1] - 4.0 * Xt[n - 2] + Xt[n - 3]) / 2.0
+    return np.moveaxis(D, 0, axis)
+
+
+def ghosted_lattice(name: str, X, Y, Z, periodic, prims, params: Params, mach: float, bc_type=None,
+                    cfl: float = 0.5, periods=None) -> Case:
+    """A case on an (i, j, k) lattice whose non-periodic directions carry
+    GHOSTS ghost layers on each side, in the reference layout.
+
+    X, Y, Z: node coordinates over the padded lattice [i, j, k]; periodic:
+    three flags; prims: (rho, u, v, w, p) arrays over the padded lattice;
+    bc_type(i, j, k, loc) -> "outlet" | "inlet" | "boundary" | "wall" | None
+    classifies each owned boundary node (padded indices) into the boundary
+    routine's lists.  Rows: owned nodes first (i fastest), then ghosts, as
+    the reference numbers them; the outermost ghosts of a non-periodic
+    direction point at themselves.  periods[d] = the (x, y, z) shift across
+    one period of direction d.  Node metrics come from 4th-order index
+    derivatives of the coordinates; half-point metrics by the six-point rule
+    on every row (the faces of the owned nodes are then single-valued)."""
+    pi_, pj, pk = X.shape
+    ext = (pi_, pj, pk)
+    G = GHOSTS
+    ii, jj, kk = np.meshgrid(np.arange(pi_), np.arange(pj), np.arange(pk), indexing="ij")
+    cc = (ii, jj, kk)
+    owned = np.ones(X.shape, dtype=bool)
+    for d in range(3):
+        if not periodic[d]:
+            owned &= (cc[d] >= G) & (cc[d] < ext[d] - G)
+    n_owned = int(owned.sum())
+    n_all = pi_ * pj * pk
+    order = np.zeros(X.shape, dtype=np.int64)
+    own_idx = np.argwhere(owned.transpose(2, 1, 0))[:, ::-1]
+    order[own_idx[:, 0], own_idx[:, 1], own_idx[:, 2]] = np.arange(1, n_owned + 1)
+    gh_idx = np.argwhere((~owned).transpose(2, 1, 0))[:, ::-1]
+    order[gh_idx[:, 0], gh_idx[:, 1], gh_idx[:, 2]] = np.arange(n_owned + 1, n_all + 1)
+
+    a = L.empty_arrays(n_all + 1)
+    _set_dummy_row(a)
+
+    def nb(d, o):
+        t = [ii, jj, kk]
+        c = cc[d] + o
+        t[d] = c % ext[d] if periodic[d] else np.clip(c, 0, ext[d] - 1)
+        return order[t[0], t[1], t[2]]
+
+    def put(field, vals):
+        a["grid"][field][order.ravel()] = np.asarray(vals).ravel()
+
+    put("x", X)
+    put("y", Y)
+    put("z", Z)
+    put("N1", nb(0, 1))
+    put("N3", nb(0, -1))
+    put("N0", nb(1, 1))
+    put("N2", nb(1, -1))
+    put("N4", nb(2, 1))
+    put("N5", nb(2, -1))
+    put("ID", np.zeros(X.shape, dtype=np.int64))
+    edge = [(cc[d] == G) & (not periodic[d]) for d in range(3)], [(cc[d] == ext[d] - G - 1) & (not periodic[d])
+                                                                     for d in range(3)]
+    loc = reference_loc_codes(edge[0][0], edge[1][0], edge[0][1], edge[1][1], edge[0][2], edge[1][2])
+    loc = np.where(owned, loc, 100)
+    put("loc", loc)
+
+    jac = np.empty(X.shape + (3, 3))
+    periods = periods or ((0.0, 0.0, 0.0),) * 3
+    for axis in range(3):
+        for comp, V in enumerate((X, Y, Z)):
+            jac[..., comp, axis] = _index_derivative(V, axis, periodic[axis], periods[axis][comp])
+    m9, det = _node_metrics(jac)
+    if not np.all(det > 0):
+        raise ValueError(f"{name}: the mapping folds (det <= 0 at {int((det <= 0).sum())} nodes)")
+    a["metric"][order.ravel(), 0:9] = m9.reshape(-1, 9)
+    a["det"][order.ravel()] = det.ravel()
+    half_point_metrics(a, n_all)
+
+    rho, u, v, w, p = (np.broadcast_to(q, X.shape) for q in prims)
+    flow = np.zeros((n_all, 9))
+    _flow_from_primitives(flow, rho.ravel(), u.ravel(), v.ravel(), w.ravel(), p.ravel(), mach)
+    a["flow"][order.ravel()] = flow
+    rows = np.arange(1, n_owned + 1)
+    shape = tuple(ext[d] if periodic[d] else ext[d] - 2 * G for d in range(3))
+    c = Case(name, shape, False, n_owned, n_all, a, params, cfl_dt(a, rows, cfl))
+    if bc_type is not None:
+        lists = {t: [] for t in _TYPES}
+        bidx = np.argwhere(owned & (loc > 0))
+        rws = order[bidx[:, 0], bidx[:, 1], bidx[:, 2]]
+        for (i, j, k), r in sorted(zip(map(tuple, bidx), rws), key=lambda t: t[1]):
+            t = bc_type(int(i), int(j), int(k), int(loc[i, j, k]))
+            if t is not None:
+                lists[t].append(int(r))
+        c.bc = BoundaryLists(**{t: np.array(v, dtype=np.int32) for t, v in lists.items()})
+    return c
+
+
+def channel(ni=16, nj=12, nk=8, mach=0.5, reynolds=500.0, amp=0.05, les=1, seed=0) -> Case:
+    """Wall-bounded channel on a perturbed grid: periodic in x (i) and z (k),
+    no-slip walls at y = 0 (j-min) and the upper boundary (j-max) split into
+    inlet (x < L/2) and outlet nodes, so the lattice path, the loc-code
+    branches and every face rule of the boundary routine run together.
+    Parabolic streamwise profile with a seeded perturbation."""
+    G = GHOSTS
+    Lx, H, Lz = 2.0, 1.0, 1.0
+    pj = nj + 2 * G
+    hx, hy, hz = Lx / ni, H / (nj - 1), Lz / nk
+    i, j, k = np.meshgrid(np.arange(ni), np.arange(pj) - G, np.arange(nk), indexing="ij")
+    xi, eta, zeta = i * hx, j * hy, k * hz
+    X = xi + amp * hx * np.sin(2 * np.pi * eta / H) * np.cos(2 * np.pi * zeta / Lz)
+    Y = eta + amp * hy * np.sin(2 * np.pi * xi / Lx) * np.cos(2 * np.pi * zeta / Lz)
+    Z = zeta + amp * hz * np.sin(2 * np.pi * xi / Lx) * np.sin(np.pi * eta / H)
+    rng = np.random.default_rng(seed)
+    yn = np.clip(Y / H, 0.0, 1.0)
+    u = 4.0 * yn * (1.0 - yn) + 0.02 * rng.standard_normal(X.shape)
+    v = 0.02 * rng.standard_normal(X.shape)
+    w = 0.02 * rng.standard_normal(X.shape)
+    p = 1.0 / (1.4 * mach * mach) * (1.0 + 0.01 * np.sin(2 * np.pi * X / Lx))
+    rho = np.ones(X.shape)
+    prm = Params(mach=mach, reynolds=reynolds, viscous=1, les=les)
+
+    def bc_type(ii, jj, kk, loc):
+        if loc == 3:
+            return "wall"
+        if loc == 1:
+            return "inlet" if ii < ni // 2 else "outlet"
+        return None
+
+    return ghosted_lattice("channel", X, Y, Z, (True, False, True), (rho, u, v, w, p), prm, mach, bc_type,
+                           periods=((Lx, 0.0, 0.0), (0.0, 0.0, 0.0), (0.0, 0.0, Lz)))

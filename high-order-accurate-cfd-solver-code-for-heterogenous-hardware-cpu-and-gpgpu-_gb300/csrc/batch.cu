@@ -299,9 +299,12 @@ cfd_status_t cfd_batch_add(cfd_batch_t *b, const cfd_geometry_t *geom, const cfd
             const int v = nb_of(geom->grid[r], slot);
             if (v < 0 || v > geom->g_node) return fail(ctx, CFD_EINVAL, "cfd_batch_add: neighbour index out of range");
         }
-    int ni = 0, nj = 0, nk = 0;
-    if (!detect_lattice(geom, ni, nj, nk) || !faces_single_valued(geom))
-        return fail(ctx, CFD_EUNSUPPORTED, "cfd_batch_add: batched instances must be periodic lattices");
+    LatticeMap map;
+    bool natural = map_lattice(geom, map) && !map.ghosted() && faces_single_valued(geom, map);
+    for (size_t n = 0; natural && n < map.row_of.size(); ++n) natural = map.row_of[n] == (int32_t)n + 1;
+    if (!natural)
+        return fail(ctx, CFD_EUNSUPPORTED, "cfd_batch_add: batched instances must be periodic lattices in row order");
+    const int ni = map.ni, nj = map.nj, nk = map.nk;
     const int N = ni * nj * nk;
     const uint64_t need = instance_bytes(b->precision, N);
     if (b->used + need > b->capacity) return fail(ctx, CFD_ENOMEM, "cfd_batch_add: device-memory budget exhausted");
@@ -340,6 +343,9 @@ cfd_status_t cfd_batch_add(cfd_batch_t *b, const cfd_geometry_t *geom, const cfd
     v.nk = nk;
     v.N = N;
     v.P = make_phys(&I.prm);
+    v.per = 7;            // periodic in every direction
+    v.loc8 = nullptr;
+    v.row_of = nullptr;
     v.dt = del_t;
     v.dt_hi = (float)del_t;
     v.dt_lo = (float)(del_t - (double)v.dt_hi);
@@ -376,7 +382,7 @@ cfd_status_t cfd_batch_add(cfd_batch_t *b, const cfd_geometry_t *geom, const cfd
     }
     cudaStream_t sm = ctx->stream;
     std::vector<double> h, hd, hf, hfd;
-    lattice_geometry_soa(geom, Nz, h, hd, hf, hfd);
+    lattice_geometry_soa(geom, map, h, hd, hf, hfd);
     cudaError_t e = cudaMemcpyAsync(m9, h.data(), 9 * Nz * 8, cudaMemcpyHostToDevice, sm);
     if (e == cudaSuccess) e = cudaMemcpyAsync(det, hd.data(), Nz * 8, cudaMemcpyHostToDevice, sm);
     if (e == cudaSuccess) e = cudaMemcpyAsync(fm, hf.data(), 9 * Nz * 8, cudaMemcpyHostToDevice, sm);

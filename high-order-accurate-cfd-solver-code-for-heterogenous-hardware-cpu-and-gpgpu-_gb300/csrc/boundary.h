@@ -1,0 +1,77 @@
+// boundary.h -- the reference's boundary routine intialise()
+// (Flow_Initialisation.cpp:23-1394) as device work: plan entries resolved
+// on the host, applied by one thread per entry (or in list order when the
+// entries of a list touch each other's rows).
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "cfd_rhs.h"
+#include "lattice.cuh"
+
+namespace cfd {
+
+// The four lists in the order the routine visits them.
+enum { BC_OUTLET = 0, BC_INLET = 1, BC_BOUNDARY = 2, BC_WALL = 3, BC_NTYPES = 4 };
+enum { BC_FACE = 0, BC_EDGE = 1 };
+
+// One list entry with its node chains resolved: the boundary node b; for a
+// face code (1..6) the three inward nodes s[0..2] along the interior slot
+// and the three ghosts g[0..2] along the missing slot; for an edge or corner
+// code (7..26) the diagonal source s[0].  Indices are reference rows, or
+// lattice nodes after remapping.
+struct BcEntry {
+    int32_t b, cls;
+    int32_t s[3];
+    int32_t g[3];
+};
+
+// Host plan of the four lists (reference rows).
+struct BcPlan {
+    std::vector<BcEntry> list[BC_NTYPES];
+    bool sequential[BC_NTYPES] = {false, false, false, false};
+};
+
+// Resolves the lists against the neighbour table.  Fails (with a message)
+// on an index outside [0, n_rows) and on wall nodes that need the
+// reference's singular-node table (ID 10, codes 29/30, 33..56); entries with
+// codes the routine has no branch for are dropped.
+bool bc_make_plan(const cfd_grid_t *grid, int32_t n_rows, const int32_t *const rows[BC_NTYPES],
+                  const int32_t n[BC_NTYPES], BcPlan &plan, std::string &err);
+
+// The same plan with every index mapped through n_of (reference row ->
+// lattice node); false if an index has no node.
+bool bc_remap(const BcPlan &in, const std::vector<int32_t> &n_of, BcPlan &out);
+
+// Device copy of a plan.
+struct BcDevice {
+    BcEntry *d[BC_NTYPES] = {nullptr, nullptr, nullptr, nullptr};
+    int n[BC_NTYPES] = {0, 0, 0, 0};
+    int seq[BC_NTYPES] = {0, 0, 0, 0};
+    int launches() const { return (n[0] > 0) + (n[1] > 0) + (n[2] > 0) + (n[3] > 0); }
+};
+cudaError_t bc_upload(const BcPlan &plan, BcDevice &dev, cudaStream_t st);
+void bc_free(BcDevice &dev);
+
+// The routine on FLOW in the reference layout (rows of 9 doubles) or on the
+// lattice's SoA FLOW fields [9][N] (boundary.cu, reference evaluation order).
+void bc_apply_aos(cudaStream_t st, const BcDevice &bc, double *flow_rows, double mach);
+void bc_apply_soa(cudaStream_t st, const BcDevice &bc, double *prim9, int N, double mach);
+// Free stream on rows 1..sd_node (the routine's initial == 0 branch).
+void bc_free_stream_aos(cudaStream_t st, double *flow_rows, int sd_node, double mach);
+// The mixed form: targets from the hi/lo state of U slot q (mixed.cu).
+void bc_apply_mixed(cudaStream_t st, const BcDevice &bc, const LatView &g, int q, double mach);
+
+}  // namespace cfd
+
+// Library object behind cfd_bc_t.
+struct cfd_bc {
+    cfd_ctx_t *ctx = nullptr;
+    int32_t n_rows = 0;
+    cfd::BcPlan plan;
+    cfd::BcDevice dev;
+};

@@ -35,7 +35,18 @@ struct LatView {
     float *Q32, *R32, *FEG32, *V32, *Fh32;
     unsigned *flags;           // error word of this lattice
     double *Lout;              // optional [5][N] right-hand side output
+    // Non-periodic directions: bit d of `per` set = direction d periodic.
+    // A non-periodic direction carries at least three ghost layers on each
+    // side; its stencils clamp at the box edge (the outermost ghosts'
+    // outward neighbour is the node itself) and loc8 holds the reference's
+    // loc codes (0 interior, 1..52 boundary, 100 ghost).  loc8 is null on a
+    // fully periodic lattice.
+    int per;
+    const unsigned char *loc8;
+    const int *row_of;         // node n -> reference row (null: row n + 1)
 };
+
+constexpr unsigned char kLocGhost = 100;
 
 enum { LF_U = 0, LF_V = 1, LF_W = 2, LF_P = 3, LF_T = 4, LF_RHO = 5, LF_MU = 6, LF_A = 7, LF_E = 8 };
 
@@ -61,14 +72,35 @@ __device__ __forceinline__ void lat_ijk(const LatView &g, int n, int &i, int &j,
     j = (int)(r - (unsigned)k * unj);
 }
 
+// clamp of x = i + o into [0, n) (non-periodic directions)
+__device__ __forceinline__ int lclamp(int x, int n) { return x < 0 ? 0 : (x >= n ? n - 1 : x); }
+
+__device__ __forceinline__ bool lat_periodic(const LatView &g, int d) { return (g.per >> d) & 1; }
+
 // node at offset o along direction d from (i,j,k)
 __device__ __forceinline__ int lat_step(const LatView &g, int i, int j, int k, int d, int o)
 {
-    if (d == 0) i = lwrap(i + o, g.ni);
-    else if (d == 1) j = lwrap(j + o, g.nj);
-    else k = lwrap(k + o, g.nk);
+    const bool p = lat_periodic(g, d);
+    if (d == 0) i = p ? lwrap(i + o, g.ni) : lclamp(i + o, g.ni);
+    else if (d == 1) j = p ? lwrap(j + o, g.nj) : lclamp(j + o, g.nj);
+    else k = p ? lwrap(k + o, g.nk) : lclamp(k + o, g.nk);
     return i + g.ni * (j + g.nj * k);
 }
+
+__device__ __forceinline__ int lat_coord(int i, int j, int k, int d) { return d == 0 ? i : (d == 1 ? j : k); }
+
+__device__ __forceinline__ int lat_extent(const LatView &g, int d) { return d == 0 ? g.ni : (d == 1 ? g.nj : g.nk); }
+
+// Face n+1/2 along a non-periodic d is needed (and its six-point stencil
+// lies in the box) for coordinates 2 .. n_d-4.
+__device__ __forceinline__ bool lat_face_needed(const LatView &g, int i, int j, int k, int d)
+{
+    if (lat_periodic(g, d)) return true;
+    const int c = lat_coord(i, j, k, d);
+    return c >= 2 && c <= lat_extent(g, d) - 4;
+}
+
+__device__ __forceinline__ bool lat_ghost(const LatView &g, int n) { return g.loc8 && g.loc8[n] == kLocGhost; }
 
 __device__ __forceinline__ double *lat_U(const LatView &g, int q) { return q == 0 ? g.U0 : (q == 1 ? g.U1 : g.U2); }
 

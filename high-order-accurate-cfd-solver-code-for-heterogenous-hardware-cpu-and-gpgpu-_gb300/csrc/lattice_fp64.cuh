@@ -56,8 +56,20 @@ __device__ __forceinline__ void prep_node(const LatView &g, int n, int q)
                 g.prim9[LF_W * N + n], g.prim9[LF_P * N + n]);
 }
 
-// Viscous.cl on a loc == 0 lattice: 4th-order central derivatives of U_q,
-// viscous + MTS SGS fluxes, mu.
+// The seven nodes at offsets -3..3 along d and their loc codes.
+__device__ __forceinline__ void loc_line(const LatView &g, int i, int j, int k, int d, int s[7], int L[7])
+{
+#pragma unroll
+    for (int o = 0; o < 7; ++o) {
+        s[o] = lat_step(g, i, j, k, d, o - 3);
+        L[o] = g.loc8[s[o]];
+    }
+}
+
+// Viscous.cl on a lattice: derivatives of U_q (4th-order central on a
+// periodic lattice, where every node has loc 0; the loc-code branches of
+// Viscous.cl:285-332 on a lattice with loc codes; zero at ghosts, which no
+// branch covers), viscous + MTS SGS fluxes, mu.
 __device__ __forceinline__ void visc_node(const LatView &g, int n, int q)
 {
     const int N = g.N;
@@ -65,15 +77,31 @@ __device__ __forceinline__ void visc_node(const LatView &g, int n, int q)
     int i, j, k;
     lat_ijk(g, n, i, j, k);
     double dU[3][5], KS[3], Ui[5];
+    const bool ghost = lat_ghost(g, n);
 #pragma unroll
     for (int c = 0; c < 5; ++c) Ui[c] = Uj[c * N + n];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const int m2 = lat_step(g, i, j, k, d, -2), m1 = lat_step(g, i, j, k, d, -1), p1 = lat_step(g, i, j, k, d, 1),
                   p2 = lat_step(g, i, j, k, d, 2);
+        if (ghost) {
 #pragma unroll
-        for (int c = 0; c < 5; ++c)
-            dU[d][c] = central4(Uj[c * N + m2], Uj[c * N + m1], Uj[c * N + p1], Uj[c * N + p2]);
+            for (int c = 0; c < 5; ++c) dU[d][c] = 0.0;
+        } else if (!g.loc8) {
+#pragma unroll
+            for (int c = 0; c < 5; ++c)
+                dU[d][c] = central4(Uj[c * N + m2], Uj[c * N + m1], Uj[c * N + p1], Uj[c * N + p2]);
+        } else {
+            int s[7], L[7];
+            loc_line(g, i, j, k, d, s, L);
+#pragma unroll
+            for (int c = 0; c < 5; ++c) {
+                double f[7];
+#pragma unroll
+                for (int o = 0; o < 7; ++o) f[o] = Uj[c * N + s[o]];
+                dU[d][c] = visc_deriv_ref(f, L);
+            }
+        }
         const int c = d + 1;
         KS[d] = ks(Ui[c], Ui[0], Uj[c * N + m1], Uj[m1], Uj[c * N + p1], Uj[p1]);
     }
@@ -111,6 +139,7 @@ __device__ __forceinline__ void face_node(const LatView &g, int n)
     const int N = g.N;
     int i, j, k;
     lat_ijk(g, n, i, j, k);
+    if (!lat_face_needed(g, i, j, k, D)) return;
     int s[6];
 #pragma unroll
     for (int o = 0; o < 6; ++o) s[o] = lat_step(g, i, j, k, D, o - 2);
@@ -138,12 +167,21 @@ __device__ __forceinline__ void face_node(const LatView &g, int n)
     }
 }
 
-// Weno.cl:3060-3135 at one node: L from the face fluxes and the viscous
-// divergence, SSP-RK3 stage jst, primitives.  With fuse_next the node then
-// runs the next stage's prep on the new primitives.
+// Weno.cl:3060-3135 at one owned node (ghosts are the boundary routine's):
+// L from the face fluxes and the viscous divergence (the loc-code branches
+// of Weno.cl:2732-2856 on a lattice with loc codes), SSP-RK3 stage jst,
+// primitives.  With fuse_next the node then runs the next stage's prep on
+// the new primitives.
 __device__ __forceinline__ void update_node(const LatView &g, int n, int jst, bool fuse_next)
 {
     const int N = g.N;
+    if (lat_ghost(g, n)) {
+        if (g.Lout) {
+#pragma unroll
+            for (int c = 0; c < 5; ++c) g.Lout[c * N + n] = 0.0;
+        }
+        return;
+    }
     int i, j, k;
     lat_ijk(g, n, i, j, k);
     double dflux[3][5], dvis[3][5];
@@ -152,7 +190,18 @@ __device__ __forceinline__ void update_node(const LatView &g, int n, int jst, bo
         const int m1 = lat_step(g, i, j, k, d, -1);
 #pragma unroll
         for (int c = 0; c < 5; ++c) dflux[d][c] = g.Fh[(d * 5 + c) * N + n] - g.Fh[(d * 5 + c) * N + m1];
-        if (g.P.viscous) {
+        if (g.P.viscous && g.loc8) {
+            int s[7], L[7];
+            loc_line(g, i, j, k, d, s, L);
+            const double *Vd = g.V + (size_t)d * 5 * N;
+#pragma unroll
+            for (int c = 0; c < 5; ++c) {
+                double f[7];
+#pragma unroll
+                for (int o = 0; o < 7; ++o) f[o] = Vd[c * N + s[o]];
+                dvis[d][c] = weno_visc_deriv_ref(f, L);
+            }
+        } else if (g.P.viscous) {
             const int m2 = lat_step(g, i, j, k, d, -2), p1 = lat_step(g, i, j, k, d, 1), p2 = lat_step(g, i, j, k, d, 2);
             const double *Vd = g.V + (size_t)d * 5 * N;
 #pragma unroll

@@ -16,6 +16,7 @@
 // explicit fmaf and plain additions, which contraction leaves exact.
 #pragma once
 
+#include "boundary.h"
 #include "lattice.cuh"
 #include "physics_x2.cuh"
 
@@ -197,9 +198,26 @@ __device__ __forceinline__ void prep_node(const LatView &g, int n, int src, int 
     derive(g, n, Un);
 }
 
+// Derivative of branch b (physics.cuh visc_branch) from the six neighbour
+// differences dl[m] = f[m+1] - f[m] of the values at offsets -3..3: every
+// formula rewritten as a sum of neighbour differences, which the hi/lo
+// state gives to FP32 accuracy.
+__device__ __forceinline__ float branch_deriv_diff(int b, const float dl[6])
+{
+    switch (b) {
+    case 1: return (1.0f / 6.0f) * (11.0f * dl[2] - 7.0f * dl[1] + 2.0f * dl[0]);
+    case 2: return (1.0f / 6.0f) * (11.0f * dl[3] - 7.0f * dl[4] + 2.0f * dl[5]);
+    case 3: return (1.0f / 6.0f) * (2.0f * dl[3] + 5.0f * dl[2] - dl[1]);
+    case 4: return (1.0f / 6.0f) * (2.0f * dl[2] + 5.0f * dl[3] - dl[4]);
+    case 5: return (1.0f / 12.0f) * (8.0f * (dl[2] + dl[3]) - (dl[1] + dl[2] + dl[3] + dl[4]));
+    default: return 0.0f;
+    }
+}
+
 // Viscous + MTS SGS fluxes from slot q.  Derivatives of U from hi/lo
-// differences (exact hi differences for neighbours within a factor of two);
-// everything else in FP32.
+// differences (exact hi differences for neighbours within a factor of two):
+// central on a periodic lattice, the reference's loc-code branches on a
+// lattice with loc codes, zero at ghosts; everything else in FP32.
 __device__ __forceinline__ void visc_node(const LatView &g, int n, int q)
 {
     const int N = g.N;
@@ -207,18 +225,40 @@ __device__ __forceinline__ void visc_node(const LatView &g, int n, int q)
     int i, j, k;
     lat_ijk(g, n, i, j, k);
     float dU[3][5], KS[3], Ui[5];
+    const bool ghost = lat_ghost(g, n);
 #pragma unroll
     for (int c = 0; c < 5; ++c) Ui[c] = W[c * N + n];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const int m2 = lat_step(g, i, j, k, d, -2), m1 = lat_step(g, i, j, k, d, -1), p1 = lat_step(g, i, j, k, d, 1),
                   p2 = lat_step(g, i, j, k, d, 2);
+        if (ghost) {
 #pragma unroll
-        for (int c = 0; c < 5; ++c) {
-            const float *H = W + c * N, *L = W + (5 + c) * N;
-            const float d1 = (H[p1] - H[m1]) + (L[p1] - L[m1]);
-            const float d2 = (H[p2] - H[m2]) + (L[p2] - L[m2]);
-            dU[d][c] = (1.0f / 12.0f) * (8.0f * d1 - d2);
+            for (int c = 0; c < 5; ++c) dU[d][c] = 0.0f;
+        } else if (!g.loc8) {
+#pragma unroll
+            for (int c = 0; c < 5; ++c) {
+                const float *H = W + c * N, *L = W + (5 + c) * N;
+                const float d1 = (H[p1] - H[m1]) + (L[p1] - L[m1]);
+                const float d2 = (H[p2] - H[m2]) + (L[p2] - L[m2]);
+                dU[d][c] = (1.0f / 12.0f) * (8.0f * d1 - d2);
+            }
+        } else {
+            int s[7], L7[7];
+#pragma unroll
+            for (int o = 0; o < 7; ++o) {
+                s[o] = lat_step(g, i, j, k, d, o - 3);
+                L7[o] = g.loc8[s[o]];
+            }
+            const int b = visc_branch(L7);
+#pragma unroll
+            for (int c = 0; c < 5; ++c) {
+                const float *H = W + c * N, *L = W + (5 + c) * N;
+                float dl[6];
+#pragma unroll
+                for (int m = 0; m < 6; ++m) dl[m] = (H[s[m + 1]] - H[s[m]]) + (L[s[m + 1]] - L[s[m]]);
+                dU[d][c] = branch_deriv_diff(b, dl);
+            }
         }
         const int c = d + 1;
         const float um = W[c * N + m1], up = W[c * N + p1];
@@ -262,6 +302,7 @@ __device__ __forceinline__ void face_node(const LatView &g, int n)
     const int N = g.N;
     int i, j, k;
     lat_ijk(g, n, i, j, k);
+    if (!lat_face_needed(g, i, j, k, D)) return;
     int s[6];
 #pragma unroll
     for (int o = 0; o < 6; ++o) s[o] = lat_step(g, i, j, k, D, o - 2);
@@ -301,6 +342,13 @@ __device__ __forceinline__ void face_node(const LatView &g, int n)
 __device__ __forceinline__ void update_node(const LatView &g, int n, int jst)
 {
     const int N = g.N;
+    if (lat_ghost(g, n)) {   // ghosts are the boundary routine's
+        if (g.Lout) {
+#pragma unroll
+            for (int c = 0; c < 5; ++c) g.Lout[c * N + n] = 0.0;
+        }
+        return;
+    }
     int i, j, k;
     lat_ijk(g, n, i, j, k);
     float Lf[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
@@ -309,7 +357,23 @@ __device__ __forceinline__ void update_node(const LatView &g, int n, int jst)
         const int m1 = lat_step(g, i, j, k, d, -1);
 #pragma unroll
         for (int c = 0; c < 5; ++c) Lf[c] += g.Fh32[(d * 5 + c) * N + n] - g.Fh32[(d * 5 + c) * N + m1];
-        if (g.P.viscous) {
+        if (g.P.viscous && g.loc8) {
+            int s[7], L7[7];
+#pragma unroll
+            for (int o = 0; o < 7; ++o) {
+                s[o] = lat_step(g, i, j, k, d, o - 3);
+                L7[o] = g.loc8[s[o]];
+            }
+            const int b = weno_visc_branch(L7);
+            const float *Vd = g.V32 + (size_t)d * 5 * N;
+#pragma unroll
+            for (int c = 0; c < 5; ++c) {
+                float f[7];
+#pragma unroll
+                for (int o = 0; o < 7; ++o) f[o] = Vd[c * N + s[o]];
+                Lf[c] += branch_deriv<float>(b, f);
+            }
+        } else if (g.P.viscous) {
             const int m2 = lat_step(g, i, j, k, d, -2), p1 = lat_step(g, i, j, k, d, 1), p2 = lat_step(g, i, j, k, d, 2);
             const float *Vd = g.V32 + (size_t)d * 5 * N;
 #pragma unroll
@@ -350,6 +414,83 @@ __device__ __forceinline__ void update_node(const LatView &g, int n, int jst)
     }
     store_state(g, jst == 2 ? 0 : jst + 1, n, Un);
     derive(g, n, Un);
+}
+
+// ------------------------------------------------ boundary routine ---
+
+// FP64 primitives of the hi/lo state of node n in slot q.
+__device__ __forceinline__ void state_prims(const LatView &g, int q, int n, double mach, double &rho, double &u,
+                                            double &v, double &w, double &p, double &t)
+{
+    const int N = g.N;
+    const float *W = lat_W(g, q);
+    double fu[5];
+    const double id = 1.0 / g.det[n];
+#pragma unroll
+    for (int c = 0; c < 5; ++c) fu[c] = id * ((double)W[c * N + n] + (double)W[(5 + c) * N + n]);
+    rho = fu[0];
+    u = fu[1] / fu[0];
+    v = fu[2] / fu[0];
+    w = fu[3] / fu[0];
+    const double e = fu[4] / fu[0] - 0.5 * (u * u + v * v + w * w);
+    p = e * rho * 0.4;
+    t = (1.4 * mach * mach) * (p / rho);
+}
+
+// Node n takes the state of primitives (rho, u, v, w, p) in slot q, and the
+// next stage's U_Q outputs.
+__device__ __forceinline__ void set_prims(const LatView &g, int q, int n, double rho, double u, double v, double w,
+                                          double p)
+{
+    const double D = g.det[n];
+    const double E = p / 0.4 + 0.5 * rho * (u * u + v * v + w * w);
+    const double U[5] = {D * rho, D * rho * u, D * rho * v, D * rho * w, D * E};
+    dfl Un[5];
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+        Un[c].h = (float)U[c];
+        Un[c].l = (float)(U[c] - (double)Un[c].h);
+    }
+    store_state(g, q, n, Un);
+    derive(g, n, Un);
+}
+
+// One entry of the reference's boundary routine (boundary.h) on the hi/lo
+// state in slot q: the same rules on (rho, u, v, w, p), the fields the next
+// stage reads (U_Q.cl takes rho, u, v, w, p of FLOW).
+__device__ __forceinline__ void bc_entry(const LatView &g, int type, const BcEntry &e, int q, double mach)
+{
+    const double gm2 = 1.4 * mach * mach;
+    double rho, u, v, w, p, t;
+    if (e.cls == BC_EDGE) {
+        state_prims(g, q, e.s[0], mach, rho, u, v, w, p, t);
+        if (type == BC_WALL) u = v = w = 0.0;
+        set_prims(g, q, e.b, gm2 * (p / t), u, v, w, p);
+        return;
+    }
+    if (type == BC_INLET || type == BC_OUTLET) {
+        if (type == BC_INLET) {
+            u = 1.0;
+            v = w = 0.0;
+            p = 1.0 / gm2;
+            t = 1.0;
+        } else {
+            state_prims(g, q, e.s[0], mach, rho, u, v, w, p, t);
+        }
+        rho = gm2 * (p / t);
+        set_prims(g, q, e.b, rho, u, v, w, p);
+        for (int m = 0; m < 3; ++m) set_prims(g, q, e.g[m], rho, u, v, w, p);
+        return;
+    }
+    // boundary (mirror copy) and wall (no slip): ghost m from inward node m
+    double sr[3], su[3], sv[3], sw[3], sp[3], st[3];
+    for (int m = 0; m < 3; ++m) state_prims(g, q, e.s[m], mach, sr[m], su[m], sv[m], sw[m], sp[m], st[m]);
+    if (type == BC_BOUNDARY)
+        set_prims(g, q, e.b, sr[0], su[0], sv[0], sw[0], sp[0]);
+    else
+        set_prims(g, q, e.b, gm2 * (sp[0] / st[0]), 0.0, 0.0, 0.0, sp[0]);
+    const double sg = type == BC_WALL ? -1.0 : 1.0;
+    for (int m = 0; m < 3; ++m) set_prims(g, q, e.g[m], sr[m], sg * su[m], sg * sv[m], sg * sw[m], sp[m]);
 }
 
 // FP64 FLOW of the state in slot q (boundary output): the FP64 form's

@@ -14,6 +14,7 @@
 // are in lattice_mixed.cuh.  This file is compiled with FMA contraction on
 // and approximate FP32 division/square root (the mixed form's error budget
 // is 1e-6 relative L2 against the FP64 form).
+#include "boundary.h"
 #include "internal.h"
 #include "lattice_mixed.cuh"
 #include "structured.h"
@@ -65,6 +66,17 @@ __global__ void __launch_bounds__(256) k_update_m(LatView g, int jst)
     if (n < g.N) mx::update_node(g, n, jst);
 }
 
+__global__ void k_bc_m(LatView g, const BcEntry *__restrict__ E, int n, int type, int q, double mach, int sequential)
+{
+    if (sequential) {
+        if (blockIdx.x == 0 && threadIdx.x == 0)
+            for (int e = 0; e < n; ++e) mx::bc_entry(g, type, E[e], q, mach);
+        return;
+    }
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < n) mx::bc_entry(g, type, E[e], q, mach);
+}
+
 __global__ void k_flow_out_m(LatView g, int q)
 {
     const int n = node_id();
@@ -76,8 +88,9 @@ __global__ void k_u_out_m(LatView g, int q, double *__restrict__ aos)
     const int n = node_id();
     if (n >= g.N) return;
     const float *W = lat_W(g, q);
+    const size_t r = g.row_of ? (size_t)g.row_of[n] : (size_t)n + 1;
 #pragma unroll
-    for (int c = 0; c < 5; ++c) aos[(size_t)(n + 1) * 5 + c] = (double)W[c * g.N + n] + (double)W[(5 + c) * g.N + n];
+    for (int c = 0; c < 5; ++c) aos[r * 5 + c] = (double)W[c * g.N + n] + (double)W[(5 + c) * g.N + n];
 }
 
 __global__ void k_to_float(const double *__restrict__ a, float *__restrict__ b, long long n)
@@ -110,6 +123,15 @@ void mixed_geometry(const StructuredLaunch &S)
     k_to_float<<<blocks_for(9 * N, 256), 256, 0, S.stream>>>(S.fm, S.fm32, 9 * N);
     k_to_float<<<blocks_for(3 * N, 256), 256, 0, S.stream>>>(S.fdet, S.fdet32, 3 * N);
     k_node_geometry<<<blocks_for(N, 256), 256, 0, S.stream>>>(S.m9, S.det, N, S.node32, S.idet32);
+}
+
+void bc_apply_mixed(cudaStream_t st, const BcDevice &bc, const LatView &g, int q, double mach)
+{
+    for (int t = 0; t < BC_NTYPES; ++t) {
+        if (bc.n[t] == 0) continue;
+        const unsigned blocks = bc.seq[t] ? 1u : blocks_for(bc.n[t], 128);
+        k_bc_m<<<blocks, bc.seq[t] ? 1 : 128, 0, st>>>(g, bc.d[t], bc.n[t], t, q, mach, bc.seq[t]);
+    }
 }
 
 void mixed_flow_out(const LatView &g, int q, cudaStream_t st)

@@ -100,37 +100,63 @@ struct FaceEigen {
 
 };
 
-// Location-code-driven first derivative of the Viscous kernel
-// (Viscous.cl:285-332; the same branch set for eta and xi).  f[0..6] are the
-// values at offsets -3..3, L[0..6] their loc codes.  Branches the reference
-// leaves undefined give 0.
-__device__ __forceinline__ double visc_deriv_ref(const double f[7], const int L[7])
+// Branch selection of the location-code-driven first derivative of the
+// Viscous kernel (Viscous.cl:285-332; the same set for eta and xi) from the
+// loc codes L[0..6] of offsets -3..3.  The reference tests its branches in
+// sequence and the last match wins: 1 one-sided backward, 2 one-sided
+// forward, 3/4 biased next to a boundary node, 5 central; 0 = no branch
+// (the derivative is 0).
+__device__ __forceinline__ int visc_branch(const int L[7])
 {
     const int L0 = L[3];
-    double D = 0.0;
-    if (L0 > 0 && L0 <= 52 && L[4] == 100) D = (1.0 / 6.0) * (11.0 * f[3] - 18.0 * f[2] + 9.0 * f[1] - 2.0 * f[0]);
-    if (L0 > 0 && L0 <= 52 && L[2] == 100) D = (1.0 / 6.0) * (-11.0 * f[3] + 18.0 * f[4] - 9.0 * f[5] + 2.0 * f[6]);
-    if (L0 == 0 && L[4] > 0 && L[4] <= 52 && L[5] == 100) D = (1.0 / 6.0) * (2.0 * f[4] + 3.0 * f[3] - 6.0 * f[2] + f[1]);
-    if (L0 == 0 && L[2] > 0 && L[1] == 100) D = (1.0 / 6.0) * ((-2.0) * f[2] - 3.0 * f[3] + 6.0 * f[4] - f[5]);
-    if (L0 == 0 && L[1] != 100 && L[2] != 100 && L[5] != 100 && L[4] != 100)
-        D = (1.0 / 12.0) * (8.0 * (f[4] - f[2]) - (f[5] - f[1]));
-    if (L0 > 0 && L[1] != 100 && L[2] != 100 && L[5] != 100 && L[4] != 100)
-        D = (1.0 / 12.0) * (8.0 * (f[4] - f[2]) - (f[5] - f[1]));
-    return D;
+    int b = 0;
+    if (L0 > 0 && L0 <= 52 && L[4] == 100) b = 1;
+    if (L0 > 0 && L0 <= 52 && L[2] == 100) b = 2;
+    if (L0 == 0 && L[4] > 0 && L[4] <= 52 && L[5] == 100) b = 3;
+    if (L0 == 0 && L[2] > 0 && L[1] == 100) b = 4;
+    if (L0 == 0 && L[1] != 100 && L[2] != 100 && L[5] != 100 && L[4] != 100) b = 5;
+    if (L0 > 0 && L[1] != 100 && L[2] != 100 && L[5] != 100 && L[4] != 100) b = 5;
+    return b;
 }
 
-// Viscous-flux derivative branches of the Weno kernel (Weno.cl:2732-2856).
-// The reference has no branch for a boundary node away from ghosts in this
-// direction (its value is uninitialised there); the central form is used.
-__device__ __forceinline__ double weno_visc_deriv_ref(const double f[7], const int L[7])
+// Viscous-flux derivative branches of the Weno kernel (Weno.cl:2732-2856):
+// central unless a one-sided or biased branch matches.  The reference has
+// no branch for a boundary node away from ghosts in a direction (its value
+// is uninitialised there); the central form is used.
+__device__ __forceinline__ int weno_visc_branch(const int L[7])
 {
     const int L0 = L[3];
-    double D = (1.0 / 12.0) * (8.0 * (f[4] - f[2]) - (f[5] - f[1]));
-    if (L0 > 0 && L0 <= 52 && L[4] == 100) D = (1.0 / 6.0) * (11.0 * f[3] - 18.0 * f[2] + 9.0 * f[1] - 2.0 * f[0]);
-    if (L0 > 0 && L0 <= 52 && L[2] == 100) D = (1.0 / 6.0) * (-11.0 * f[3] + 18.0 * f[4] - 9.0 * f[5] + 2.0 * f[6]);
-    if (L0 == 0 && L[4] > 0 && L[4] <= 52 && L[5] == 100) D = (1.0 / 6.0) * ((2.0) * f[4] + 3.0 * f[3] - 6.0 * f[2] + f[1]);
-    if (L0 == 0 && L[2] > 0 && L[2] <= 52 && L[1] == 100) D = (1.0 / 6.0) * ((-2.0) * f[2] - 3.0 * f[3] + 6.0 * f[4] - f[5]);
-    return D;
+    int b = 5;
+    if (L0 > 0 && L0 <= 52 && L[4] == 100) b = 1;
+    if (L0 > 0 && L0 <= 52 && L[2] == 100) b = 2;
+    if (L0 == 0 && L[4] > 0 && L[4] <= 52 && L[5] == 100) b = 3;
+    if (L0 == 0 && L[2] > 0 && L[2] <= 52 && L[1] == 100) b = 4;
+    return b;
+}
+
+// The derivative of branch b from the values f[0..6] at offsets -3..3, as
+// the reference writes each formula.
+template <class T>
+__device__ __forceinline__ T branch_deriv(int b, const T f[7])
+{
+    switch (b) {
+    case 1: return (T(1.0) / T(6.0)) * (T(11.0) * f[3] - T(18.0) * f[2] + T(9.0) * f[1] - T(2.0) * f[0]);
+    case 2: return (T(1.0) / T(6.0)) * (T(-11.0) * f[3] + T(18.0) * f[4] - T(9.0) * f[5] + T(2.0) * f[6]);
+    case 3: return (T(1.0) / T(6.0)) * (T(2.0) * f[4] + T(3.0) * f[3] - T(6.0) * f[2] + f[1]);
+    case 4: return (T(1.0) / T(6.0)) * ((T(-2.0)) * f[2] - T(3.0) * f[3] + T(6.0) * f[4] - f[5]);
+    case 5: return (T(1.0) / T(12.0)) * (T(8.0) * (f[4] - f[2]) - (f[5] - f[1]));
+    default: return T(0.0);
+    }
+}
+
+__device__ __forceinline__ double visc_deriv_ref(const double f[7], const int L[7])
+{
+    return branch_deriv<double>(visc_branch(L), f);
+}
+
+__device__ __forceinline__ double weno_visc_deriv_ref(const double f[7], const int L[7])
+{
+    return branch_deriv<double>(weno_visc_branch(L), f);
 }
 
 // Physical constants of one run.

@@ -3,18 +3,22 @@
 // with the state kept in device memory between stages and steps.
 //
 // Path selection at create time:
-//   CFD_PATH_STRUCTURED  the neighbour table is a periodic (i,j,k) lattice
-//                        with loc == 0 everywhere and single-valued face data
-//                        -> face-based SoA kernels (structured.cu)
+//   CFD_PATH_STRUCTURED  the neighbour table is an (i,j,k) lattice --
+//                        periodic, or with non-periodic directions padded by
+//                        ghost layers (lattice_host.h) -- with single-valued
+//                        face data -> face-based SoA kernels (structured.cu,
+//                        mixed.cu)
 //   CFD_PATH_GATHER      anything else -> the drop-in kernels on the
 //                        reference layout (dropin.cu), the same code the
 //                        cfd_uq/cfd_viscous/cfd_weno entry points run
-// Ghost rows are not refilled between stages (the reference's boundary
-// routine intialise(), Flow_Initialisation.cpp, is outside this library).
+// With cfd_solver_set_boundary the reference's boundary routine
+// (Flow_Initialisation.cpp, boundary.cu) runs after every stage, as the host
+// loop calls it (Solver.cpp:658).
 #include <cmath>
 #include <cstring>
 #include <vector>
 
+#include "boundary.h"
 #include "internal.h"
 #include "lattice_host.h"
 #include "structured.h"
@@ -44,6 +48,9 @@ struct cfd_solver {
     // FLOW is current) and the stage whose U_Q outputs are ready (-1: none)
     int cur_slot = -1;
     int prep_ready = -1;
+    cfd::LatticeMap map;        // lattice path: rows <-> nodes
+    cfd::BcDevice bc;           // boundary routine after every stage
+    bool has_bc = false;
 };
 
 namespace {
@@ -100,6 +107,7 @@ cfd_status_t create_structured(cfd_solver *s, const cfd_geometry_t *g)
 {
     const size_t N = (size_t)s->ni * s->nj * s->nk;
     StructuredLaunch &S = s->S;
+    S.per = s->map.per;
     S.ni = s->ni;
     S.nj = s->nj;
     S.nk = s->nk;
@@ -135,7 +143,7 @@ cfd_status_t create_structured(cfd_solver *s, const cfd_geometry_t *g)
     cudaMemsetAsync(s->stage9, 0, 9 * (N + 1) * sizeof(double), S.stream);
     // geometry AoS -> SoA on the host (one-off)
     std::vector<double> h, hd, hf, hfd;
-    lattice_geometry_soa(g, N, h, hd, hf, hfd);
+    lattice_geometry_soa(g, s->map, h, hd, hf, hfd);
     if ((st = upload(s, m9, h.data(), 9 * N * 8)) || (st = upload(s, det, hd.data(), N * 8))
         || (st = upload(s, fm, hf.data(), 9 * N * 8)) || (st = upload(s, fdet, hfd.data(), 3 * N * 8)))
         return st;
@@ -143,6 +151,19 @@ cfd_status_t create_structured(cfd_solver *s, const cfd_geometry_t *g)
     S.det = det;
     S.fm = fm;
     S.fdet = fdet;
+    bool identity = true;
+    for (size_t n = 0; n < N && identity; ++n) identity = s->map.row_of[n] == (int32_t)n + 1;
+    if (!identity) {
+        int *row_of;
+        if ((st = dalloc_t(s, N, &row_of)) || (st = upload(s, row_of, s->map.row_of.data(), N * sizeof(int))))
+            return st;
+        S.row_of = row_of;
+    }
+    if (s->map.ghosted()) {
+        unsigned char *loc8;
+        if ((st = dalloc_t(s, N, &loc8)) || (st = upload(s, loc8, s->map.loc.data(), N))) return st;
+        S.loc8 = loc8;
+    }
     if (s->mixed) {
         mixed_geometry(S);
         s->ctx->launches += kMixedGeometryLaunches;
@@ -167,6 +188,13 @@ cfd_status_t run_stage(cfd_solver *s, int j, double dt, bool want_L)
     if (s->path == CFD_PATH_STRUCTURED) {
         ctx->launches += structured_stage(s->S, j, dt, want_L ? s->Lsoa : nullptr, nullptr, nullptr, prep_source(s, j));
         if (s->mixed) s->cur_slot = s->prep_ready = j == 2 ? 0 : j + 1;
+        if (s->has_bc) {
+            if (s->mixed)
+                bc_apply_mixed(ctx->stream, s->bc, make_view(s->S, dt, nullptr), s->cur_slot, s->P.mach);
+            else
+                bc_apply_soa(ctx->stream, s->bc, s->S.prim9, (int)((long long)s->ni * s->nj * s->nk), s->P.mach);
+            ctx->launches += s->bc.launches();
+        }
     } else {
         double *Uj = s->U[j];
         launch_uq(ctx->stream, Uj, s->Q, s->grid, s->det, s->flow, s->roe, s->g_node + 1, s->n_rows, ctx->d_flags);
@@ -176,6 +204,10 @@ cfd_status_t run_stage(cfd_solver *s, int j, double dt, bool want_L)
                     s->metric, s->roe, s->Fv, s->Ev, s->Gv, s->F, s->E, s->G, s->flow, s->sd_node + 1, s->n_rows,
                     ctx->d_flags, want_L ? s->L : nullptr);
         ctx->launches += 3;
+        if (s->has_bc) {
+            bc_apply_aos(ctx->stream, s->bc, s->flow, s->P.mach);
+            ctx->launches += s->bc.launches();
+        }
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(ctx, e, "stage launch");
@@ -214,20 +246,19 @@ cfd_status_t cfd_solver_create(cfd_ctx_t *ctx, const cfd_geometry_t *geom, const
     s->g_node = geom->g_node;
     s->sd_node = geom->sd_node;
     s->n_rows = n_rows;
-    int ni = 0, nj = 0, nk = 0;
-    const bool lattice = force_path != CFD_PATH_GATHER && detect_lattice(geom, ni, nj, nk) && faces_single_valued(geom);
+    const bool lattice = force_path != CFD_PATH_GATHER && map_lattice(geom, s->map) && faces_single_valued(geom, s->map);
     if (force_path == CFD_PATH_STRUCTURED && !lattice) {
         delete s;
-        return fail(ctx, CFD_EINVAL, "cfd_solver_create: table is not a periodic lattice with single-valued faces");
+        return fail(ctx, CFD_EINVAL, "cfd_solver_create: table is not a lattice with single-valued faces");
     }
     s->path = lattice ? CFD_PATH_STRUCTURED : CFD_PATH_GATHER;
     if (s->mixed && s->path != CFD_PATH_STRUCTURED) {
         delete s;
         return fail(ctx, CFD_EUNSUPPORTED, "cfd_solver_create: mixed precision needs the structured path");
     }
-    s->ni = ni;
-    s->nj = nj;
-    s->nk = nk;
+    s->ni = lattice ? s->map.ni : 0;
+    s->nj = lattice ? s->map.nj : 0;
+    s->nk = lattice ? s->map.nk : 0;
     st = s->path == CFD_PATH_STRUCTURED ? create_structured(s, geom) : create_gather(s, geom);
     if (st != CFD_OK) {
         cfd_solver_destroy(s);
@@ -242,8 +273,35 @@ cfd_status_t cfd_solver_destroy(cfd_solver_t *s)
     if (!s) return CFD_EINVAL;
     use_device(s->ctx);
     cudaStreamSynchronize(s->ctx->stream);
+    bc_free(s->bc);
     for (void *p : s->allocs) cudaFree(p);
     delete s;
+    return CFD_OK;
+}
+
+cfd_status_t cfd_solver_set_boundary(cfd_solver_t *s, const cfd_bc_t *bc)
+{
+    if (!s) return CFD_EINVAL;
+    cfd_status_t st = use_device(s->ctx);
+    if (st != CFD_OK) return st;
+    cudaStreamSynchronize(s->ctx->stream);
+    bc_free(s->bc);
+    s->has_bc = false;
+    if (!bc) return CFD_OK;
+    if (bc->n_rows != s->n_rows) return fail(s->ctx, CFD_EINVAL, "cfd_solver_set_boundary: table size differs");
+    BcPlan plan;
+    if (s->path == CFD_PATH_STRUCTURED) {
+        if (!bc_remap(bc->plan, s->map.n_of_row, plan))
+            return fail(s->ctx, CFD_EUNSUPPORTED, "cfd_solver_set_boundary: a boundary row is not a lattice node");
+    } else {
+        plan = bc->plan;
+    }
+    cudaError_t e = bc_upload(plan, s->bc, s->ctx->stream);
+    if (e != cudaSuccess) {
+        bc_free(s->bc);
+        return cuda_fail(s->ctx, e, "cfd_solver_set_boundary upload");
+    }
+    s->has_bc = true;
     return CFD_OK;
 }
 
@@ -274,7 +332,7 @@ cfd_status_t cfd_solver_set_flow(cfd_solver_t *s, const cfd_flow_t *flow_host)
         s->prep_ready = -1;
         s->cur_slot = -1;
         st = upload(s, s->stage9, flow_host, R * sizeof(cfd_flow_t));
-        if (st == CFD_OK) aos_to_soa(s->ctx->stream, s->stage9, 9, 9, N, s->S.prim9);
+        if (st == CFD_OK) aos_to_soa(s->ctx->stream, s->stage9, 9, 9, N, s->S.prim9, s->S.row_of);
     }
     if (st != CFD_OK) return st;
     return drain(s->ctx);
@@ -293,7 +351,7 @@ cfd_status_t cfd_solver_get_flow(cfd_solver_t *s, cfd_flow_t *flow_host)
             mixed_flow_out(make_view(s->S, 0.0, nullptr), s->cur_slot, s->S.stream);
             s->ctx->launches += 1;
         }
-        soa_to_aos(s->ctx->stream, s->S.prim9, 9, 9, (long long)s->ni * s->nj * s->nk, s->stage9);
+        soa_to_aos(s->ctx->stream, s->S.prim9, 9, 9, (long long)s->ni * s->nj * s->nk, s->stage9, s->S.row_of);
         src = s->stage9;
     }
     cudaError_t e = cudaMemcpyAsync(flow_host, src, R * sizeof(cfd_flow_t), cudaMemcpyDeviceToHost, s->ctx->stream);
@@ -312,7 +370,7 @@ cfd_status_t cfd_solver_get_u0(cfd_solver_t *s, cfd_column_t *u0_host)
         if (s->mixed)
             mixed_u_out(make_view(s->S, 0.0, nullptr), 0, s->stage5, s->ctx->stream);
         else
-            soa_to_aos(s->ctx->stream, s->S.U[0], 5, 5, (long long)s->ni * s->nj * s->nk, s->stage5);
+            soa_to_aos(s->ctx->stream, s->S.U[0], 5, 5, (long long)s->ni * s->nj * s->nk, s->stage5, s->S.row_of);
         src = s->stage5;
     }
     cudaError_t e = cudaMemcpyAsync(u0_host, src, R * sizeof(cfd_column_t), cudaMemcpyDeviceToHost, s->ctx->stream);
@@ -342,7 +400,7 @@ cfd_status_t cfd_solver_stage(cfd_solver_t *s, int32_t j, double del_t, cfd_colu
         const size_t R = (size_t)s->n_rows;
         const double *src = s->L;
         if (s->path == CFD_PATH_STRUCTURED) {
-            soa_to_aos(s->ctx->stream, s->Lsoa, 5, 5, (long long)s->ni * s->nj * s->nk, s->stage5);
+            soa_to_aos(s->ctx->stream, s->Lsoa, 5, 5, (long long)s->ni * s->nj * s->nk, s->stage5, s->S.row_of);
             src = s->stage5;
         }
         cudaError_t e = cudaMemcpyAsync(L_host, src, R * sizeof(cfd_column_t), cudaMemcpyDeviceToHost, s->ctx->stream);
@@ -359,9 +417,9 @@ cfd_status_t cfd_solver_profile_stage(cfd_solver_t *s, int32_t j, double del_t, 
     if (st != CFD_OK) return st;
     cudaStream_t stream = s->ctx->stream;
     s->S.stream = stream;
-    std::vector<cudaEvent_t> ev(kMaxStageLaunches + 1);
+    std::vector<cudaEvent_t> ev(kMaxStageLaunches + 2);
     for (auto &e : ev) cudaEventCreate(&e);
-    const char *snames[kMaxStageLaunches] = {};
+    const char *snames[kMaxStageLaunches + 1] = {};
     int nk = 3;
     if (s->path == CFD_PATH_STRUCTURED) {
         nk = structured_stage(s->S, j, del_t, nullptr, ev.data(), snames, prep_source(s, j));
@@ -383,6 +441,18 @@ cfd_status_t cfd_solver_profile_stage(cfd_solver_t *s, int32_t j, double del_t, 
         snames[2] = "weno";
     }
     s->ctx->launches += nk;
+    if (s->has_bc) {   // the boundary routine as one timed entry
+        if (s->path != CFD_PATH_STRUCTURED)
+            bc_apply_aos(stream, s->bc, s->flow, s->P.mach);
+        else if (s->mixed)
+            bc_apply_mixed(stream, s->bc, make_view(s->S, del_t, nullptr), s->cur_slot, s->P.mach);
+        else
+            bc_apply_soa(stream, s->bc, s->S.prim9, (int)((long long)s->ni * s->nj * s->nk), s->P.mach);
+        s->ctx->launches += s->bc.launches();
+        cudaEventRecord(ev[nk + 1], stream);
+        snames[nk] = "boundary";
+        ++nk;
+    }
     cudaError_t e = cudaEventSynchronize(ev[nk]);
     if (e == cudaSuccess) {
         const int n = nk < max_out ? nk : max_out;

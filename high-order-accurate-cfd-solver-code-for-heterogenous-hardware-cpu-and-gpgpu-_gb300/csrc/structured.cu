@@ -70,23 +70,27 @@ __global__ void __launch_bounds__(128) k_update(LatView g, int jst)
     if (n < g.N) ex::update_node(g, n, jst, false);
 }
 
-// AoS rows 1..N (row stride `stride` doubles) <-> SoA [comp][N].
-__global__ void k_aos_to_soa(const double *__restrict__ aos, int stride, int ncomp, long long N, double *__restrict__ soa)
+// AoS reference rows (row stride `stride` doubles) <-> SoA [comp][N].
+__global__ void k_aos_to_soa(const double *__restrict__ aos, int stride, int ncomp, long long N,
+                             double *__restrict__ soa, const int *__restrict__ row_of)
 {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= N * ncomp) return;
     const long long n = t / ncomp;
     const int c = (int)(t % ncomp);
-    soa[c * N + n] = aos[(n + 1) * stride + c];
+    const long long r = row_of ? (long long)row_of[n] : n + 1;
+    soa[c * N + n] = aos[r * stride + c];
 }
 
-__global__ void k_soa_to_aos(const double *__restrict__ soa, int stride, int ncomp, long long N, double *__restrict__ aos)
+__global__ void k_soa_to_aos(const double *__restrict__ soa, int stride, int ncomp, long long N,
+                             double *__restrict__ aos, const int *__restrict__ row_of)
 {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= N * ncomp) return;
     const long long n = t / ncomp;
     const int c = (int)(t % ncomp);
-    aos[(n + 1) * stride + c] = soa[c * N + n];
+    const long long r = row_of ? (long long)row_of[n] : n + 1;
+    aos[r * stride + c] = soa[c * N + n];
 }
 
 }  // namespace
@@ -125,16 +129,16 @@ int structured_stage(const StructuredLaunch &S, int jst, double dt, double *Lout
     return 6;
 }
 
-void aos_to_soa(cudaStream_t st, const double *aos, int stride, int ncomp, long long N, double *soa)
+void aos_to_soa(cudaStream_t st, const double *aos, int stride, int ncomp, long long N, double *soa, const int *row_of)
 {
     const long long t = N * ncomp;
-    k_aos_to_soa<<<blocks_for(t, 256), 256, 0, st>>>(aos, stride, ncomp, N, soa);
+    k_aos_to_soa<<<blocks_for(t, 256), 256, 0, st>>>(aos, stride, ncomp, N, soa, row_of);
 }
 
-void soa_to_aos(cudaStream_t st, const double *soa, int stride, int ncomp, long long N, double *aos)
+void soa_to_aos(cudaStream_t st, const double *soa, int stride, int ncomp, long long N, double *aos, const int *row_of)
 {
     const long long t = N * ncomp;
-    k_soa_to_aos<<<blocks_for(t, 256), 256, 0, st>>>(soa, stride, ncomp, N, aos);
+    k_soa_to_aos<<<blocks_for(t, 256), 256, 0, st>>>(soa, stride, ncomp, N, aos, row_of);
 }
 
 }  // namespace cfd

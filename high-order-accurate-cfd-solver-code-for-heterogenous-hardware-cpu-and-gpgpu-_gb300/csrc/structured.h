@@ -37,6 +37,10 @@ struct StructuredLaunch {
     float *node32 = nullptr;   // [11][N] node metrics, det, det^(-1/3)
     float *idet32 = nullptr;   // [2][N] 1/det hi, lo
     float *prim32 = nullptr;   // [9][N] FLOW in FP32
+    // lattice shape beyond a plain periodic box (LatView::per, loc8, row_of)
+    int per = 7;
+    const unsigned char *loc8 = nullptr;
+    const int *row_of = nullptr;
 };
 
 // Where the mixed stage takes its U_Q (prep) from: nothing (the previous
@@ -97,6 +101,9 @@ inline LatView make_view(const StructuredLaunch &S, double dt, double *Lout)
     g.Fh32 = S.Fh32;
     g.flags = S.flags;
     g.Lout = Lout;
+    g.per = S.per;
+    g.loc8 = S.loc8;
+    g.row_of = S.row_of;
     return g;
 }
 
@@ -109,7 +116,11 @@ constexpr int kMaxStageLaunches = 6;
 int structured_stage(const StructuredLaunch &S, int j, double dt, double *Lout, cudaEvent_t *ev = nullptr,
                      const char **names = nullptr, int prep_from = kPrepFromFlow);
 
-void aos_to_soa(cudaStream_t st, const double *aos, int stride, int ncomp, long long N, double *soa);
-void soa_to_aos(cudaStream_t st, const double *soa, int stride, int ncomp, long long N, double *aos);
+// AoS reference rows <-> SoA [comp][N]; node n is row row_of[n] (row n + 1
+// when row_of is null).
+void aos_to_soa(cudaStream_t st, const double *aos, int stride, int ncomp, long long N, double *soa,
+                const int *row_of = nullptr);
+void soa_to_aos(cudaStream_t st, const double *soa, int stride, int ncomp, long long N, double *aos,
+                const int *row_of = nullptr);
 
 }  // namespace cfd

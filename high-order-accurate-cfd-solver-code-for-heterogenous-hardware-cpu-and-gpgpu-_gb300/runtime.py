@@ -14,6 +14,7 @@ from __future__ import annotations
 
 import ctypes as C
 import dataclasses
+import weakref
 
 import numpy as np
 
@@ -53,6 +54,9 @@ class Context:
             raise abi.CfdError(s, "cfd_ctx_create")
         self.h = h
         self._buffers = []
+        # solvers, batches and boundary plans of this context: closed before
+        # the context itself (they hold device memory and use its stream)
+        self._children = weakref.WeakSet()
 
     # -- errors --
     def check(self, status: int, where: str):
@@ -62,6 +66,8 @@ class Context:
 
     def close(self):
         if self.h:
+            for ch in list(self._children):
+                ch.close()
             for p in self._buffers:
                 self.lib.cfd_buffer_free(self.h, p)
             self._buffers = []
@@ -168,10 +174,47 @@ class SolverInfo:
     device_bytes: int
 
 
-class Solver:
-    """Resident RHS solver for one grid (cfd_solver_*)."""
+class Boundary:
+    """The reference's boundary routine for one table (cfd_bc_*): the plan of
+    a cases.BoundaryLists resolved against the neighbour table."""
 
-    def __init__(self, ctx: Context, case, params=None, force_path: int = -1, precision: int = 0):
+    def __init__(self, ctx: Context, grid: np.ndarray, bc):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        self._lists = tuple(np.ascontiguousarray(getattr(bc, t), dtype=np.int32)
+                            for t in ("outlet", "inlet", "boundary", "wall"))
+        args = []
+        for a in self._lists:
+            args += [_ptr(a) if a.size else None, int(a.size)]
+        h = C.c_void_p()
+        ctx.check(self.lib.cfd_bc_create(ctx.h, _ptr(grid), int(grid.shape[0]), *args, C.byref(h)), "cfd_bc_create")
+        self.h = h
+        ctx._children.add(self)
+
+    def fill(self, flow_dev: int, mach: float, initial: int = 1, sd_node: int = 0):
+        """intialise() on a device FLOW buffer (reference layout)."""
+        self.ctx.check(self.lib.cfd_boundary_fill(self.ctx.h, self.h, C.c_void_p(flow_dev), float(mach), int(initial),
+                                                  int(sd_node)), "cfd_boundary_fill")
+
+    def close(self):
+        if self.h and self.ctx.h:
+            self.lib.cfd_bc_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Solver:
+    """Resident RHS solver for one grid (cfd_solver_*).  A case with boundary
+    lists (case.bc) gets the reference's boundary routine after every stage
+    unless ``boundary=False``."""
+
+    def __init__(self, ctx: Context, case, params=None, force_path: int = -1, precision: int = 0,
+                 boundary: bool = True):
         self.ctx = ctx
         self.lib = ctx.lib
         a = case.arrays
@@ -185,11 +228,21 @@ class Solver:
         ctx.check(self.lib.cfd_solver_create(ctx.h, C.byref(geom), C.byref(pr), int(force_path), C.byref(h)),
                   "cfd_solver_create")
         self.h = h
+        ctx._children.add(self)
+        self.boundary = None
+        if boundary and getattr(case, "bc", None) is not None:
+            self.set_boundary(Boundary(ctx, a["grid"], case.bc))
+
+    def set_boundary(self, bnd: "Boundary | None"):
+        """Run the boundary routine after every stage (None: off)."""
+        self.ctx.check(self.lib.cfd_solver_set_boundary(self.h, bnd.h if bnd is not None else None),
+                       "cfd_solver_set_boundary")
+        self.boundary = bnd
 
     def close(self):
-        if self.h:
+        if self.h and self.ctx.h:
             self.lib.cfd_solver_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -258,15 +311,16 @@ class Batch:
         ctx.check(self.lib.cfd_batch_create(ctx.h, int(precision), int(capacity_bytes), C.byref(h)), "cfd_batch_create")
         self.h = h
         self.rows = {}
+        ctx._children.add(self)
 
     @staticmethod
     def instance_bytes(precision: int, nodes: int) -> int:
         return int(abi.load().cfd_batch_instance_bytes(int(precision), int(nodes)))
 
     def close(self):
-        if self.h:
+        if self.h and self.ctx.h:
             self.lib.cfd_batch_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:

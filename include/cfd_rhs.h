@@ -204,7 +204,12 @@ typedef struct {
 typedef struct cfd_solver cfd_solver_t;
 
 /* `force_path` = -1 chooses automatically; 0/1 forces a path (forcing the
- * structured path on a table that is not a periodic lattice -> CFD_EINVAL). */
+ * structured path on a table that is not a lattice -> CFD_EINVAL).  A
+ * lattice here is periodic in every direction, or has non-periodic
+ * directions whose outermost ghost rows point at themselves, at least three
+ * ghost layers beyond the owned rows (1..sd_node, loc != 100) and ghosts
+ * carrying loc 100 -- the face-based kernels then follow the reference's
+ * loc-code derivative branches. */
 cfd_status_t cfd_solver_create(cfd_ctx_t *ctx, const cfd_geometry_t *geom, const cfd_params_t *params,
                                int32_t force_path, cfd_solver_t **solver);
 cfd_status_t cfd_solver_destroy(cfd_solver_t *s);
@@ -219,6 +224,30 @@ cfd_status_t cfd_solver_step(cfd_solver_t *s, double del_t, int32_t nsteps);
 /* One stage j of the host loop; copies L (rows 0..g_node, owned rows set)
  * to L_host when non-NULL. */
 cfd_status_t cfd_solver_stage(cfd_solver_t *s, int32_t j, double del_t, cfd_column_t *L_host);
+
+/* ------------------------------------------------- boundary routine ---- */
+/* The reference's boundary routine intialise() (Flow_Initialisation.cpp:
+ * 23-1394, called after every RK stage at Solver.cpp:658) on the device.
+ * The four lists are the routine's wall_node, inlet_node, outlet_node and
+ * boundary_node arrays (row indices; the routine's second half,
+ * :1395-2742, applies the same rules to the subdomain lists sd_*_node --
+ * pass those to a second cfd_bc_t).  Face codes 1..6 fill the node and its
+ * three ghost layers, edge and corner codes 7..26 copy a diagonal node;
+ * wall nodes that need the reference's singular-node table (ID 10, loc
+ * 29/30/33..56) give CFD_EUNSUPPORTED.  `grid` is host memory, read once. */
+typedef struct cfd_bc cfd_bc_t;
+cfd_status_t cfd_bc_create(cfd_ctx_t *ctx, const cfd_grid_t *grid, int32_t n_rows, const int32_t *outlet,
+                           int32_t n_outlet, const int32_t *inlet, int32_t n_inlet, const int32_t *boundary,
+                           int32_t n_boundary, const int32_t *wall, int32_t n_wall, cfd_bc_t **bc);
+cfd_status_t cfd_bc_destroy(cfd_bc_t *bc);
+/* intialise() on a device FLOW buffer of the reference layout; with
+ * initial == 0 rows 1..sd_node first get the free stream
+ * (Flow_Initialisation.cpp:35-48). */
+cfd_status_t cfd_boundary_fill(cfd_ctx_t *ctx, const cfd_bc_t *bc, cfd_flow_t *FLOW, double Mach, int32_t initial,
+                               int32_t sd_node);
+/* The solver runs the routine after every stage (with its Mach number);
+ * NULL switches it off.  The solver keeps its own copy of the plan. */
+cfd_status_t cfd_solver_set_boundary(cfd_solver_t *s, const cfd_bc_t *bc);
 
 /* One stage j of the host loop with a CUDA event around every kernel
  * launch; out[i] receives each launch's name and device time.  The stage

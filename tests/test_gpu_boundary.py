@@ -1,0 +1,140 @@
+"""The boundary routine on the GPU and the lattice path with ghost layers.
+
+* cfd_boundary_fill against the golden vectors of the reference's own
+  routine (bit-exact: copies and the reference's formulas, compiled without
+  FMA contraction);
+* the wall-bounded channel (periodic x/z, walls and inlet/outlet in y) on the
+  face-based lattice path with the routine after every stage, against the
+  oracle (FP64: relative L2 <= 1e-12), against the drop-in gather path, and
+  in the mixed form (<= 1e-6 against FP64)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from helpers import rel_l2
+from test_oracle_boundary import golden_inputs
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+@pytest.mark.parametrize("initial", [1, 0])
+def test_boundary_fill_matches_reference_golden(ctx, initial):
+    from cfd_gb300 import runtime
+    z, a, bc = golden_inputs()
+    bnd = runtime.Boundary(ctx, a["grid"], bc)
+    dev = ctx.alloc(a["flow"].nbytes)
+    try:
+        ctx.write(dev, a["flow"])
+        bnd.fill(dev, float(z["mach"]), initial, int(z["sd_node"]))
+        out = np.empty_like(a["flow"])
+        ctx.read(out, dev)
+    finally:
+        ctx.free(dev)
+        bnd.close()
+    assert np.array_equal(out, z[f"out_flow_initial{initial}"])
+
+
+def test_singular_wall_node_is_unsupported(ctx):
+    from cfd_gb300 import abi, runtime
+    z, a, bc = golden_inputs()
+    a["grid"]["ID"][bc.wall[0]] = 10
+    with pytest.raises(abi.CfdError) as e:
+        runtime.Boundary(ctx, a["grid"], bc)
+    assert e.value.status == abi.EUNSUPPORTED
+
+
+def _assert_flow_close(got, want, tol=TOL):
+    """Rows 1.. (row 0 is the reference's dummy row, which the lattice path
+    does not process); names the worst rows and fields on failure."""
+    g, w = got[1:], want[1:]
+    err = rel_l2(g, w)
+    if not err <= tol:
+        d = np.abs(g - w)
+        rows = np.argsort(d.max(axis=1))[::-1][:5] + 1
+        fields = np.argsort(d.max(axis=0))[::-1][:3]
+        raise AssertionError(f"rel L2 {err:.3e}; worst rows {rows.tolist()}, fields {fields.tolist()}")
+
+
+def _channel():
+    from cfd_gb300 import cases
+    return cases.channel(ni=16, nj=12, nk=8)
+
+
+def test_channel_takes_the_lattice_path(ctx):
+    from cfd_gb300 import runtime
+    c = _channel()
+    s = runtime.Solver(ctx, c)
+    info = s.info()
+    s.close()
+    assert info.path == "structured" and tuple(info.shape) == (16, 18, 8)
+
+
+def test_channel_fp64_lattice_matches_oracle(ctx, oracle_mod):
+    """RHS of the first stage and three steps with the boundary routine."""
+    from cfd_gb300 import runtime
+    c = _channel()
+    own = slice(1, c.sd_node + 1)
+    s = runtime.Solver(ctx, c)
+    s.set_flow(c.arrays["flow"])
+    Lg = s.stage(0, c.dt)
+    a = c.copy().arrays
+    Lo = oracle_mod.stage(a, c.g_node, c.sd_node, c.params, 0, c.dt, want_L=True)
+    oracle_mod.boundary_fill(a, c.bc, c.params.mach, 1, c.sd_node)
+    flow = s.get_flow()
+    s.close()
+    assert rel_l2(Lg[own], Lo[own]) <= TOL
+    _assert_flow_close(flow, a["flow"])
+    s = runtime.Solver(ctx, c)
+    s.set_flow(c.arrays["flow"])
+    s.step(c.dt, 3)
+    flow = s.get_flow()
+    s.close()
+    a = c.copy().arrays
+    oracle_mod.rk3_steps_bc(a, c.g_node, c.sd_node, c.params, c.dt, 3, c.bc)
+    _assert_flow_close(flow, a["flow"])
+
+
+def test_channel_lattice_equals_gather_path(ctx):
+    from cfd_gb300 import runtime
+    c = _channel()
+    out = []
+    for force in (1, 0):
+        s = runtime.Solver(ctx, c, force_path=force)
+        s.set_flow(c.arrays["flow"])
+        s.step(c.dt, 4)
+        out.append(s.get_flow())
+        s.close()
+    _assert_flow_close(out[0], out[1])
+
+
+def test_channel_mixed_error_budget(ctx):
+    from cfd_gb300 import runtime
+    c = _channel()
+    res = []
+    for prec in (0, 1):
+        s = runtime.Solver(ctx, c, precision=prec)
+        s.set_flow(c.arrays["flow"])
+        s.step(c.dt, 10)
+        res.append(s.get_flow()[1:c.sd_node + 1])
+        s.close()
+    assert np.isfinite(res[1]).all()
+    assert rel_l2(res[1], res[0]) <= 1e-6
+
+
+def test_ghost_box_gather_path_with_boundary(ctx, oracle_mod):
+    """A table that is not a lattice with single-valued faces (ghosts carry
+    their own node metrics) runs the drop-in kernels; the boundary routine
+    follows every stage there too."""
+    from cfd_gb300 import cases, runtime
+    c = cases.ghost_box(shape=(7, 6, 5), seed=2, bc=True)
+    s = runtime.Solver(ctx, c)
+    assert s.info().path == "gather"
+    s.set_flow(c.arrays["flow"])
+    s.step(c.dt, 1)
+    flow = s.get_flow()
+    s.close()
+    a = c.copy().arrays
+    oracle_mod.rk3_steps_bc(a, c.g_node, c.sd_node, c.params, c.dt, 1, c.bc)
+    _assert_flow_close(flow, a["flow"])
