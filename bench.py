@@ -81,6 +81,9 @@ def parse_args(argv=None):
     p.add_argument("--serve-fp64", action="store_true", help="also serve the stream with the FP64 form")
     p.add_argument("--diag-steps", type=int, default=200,
                    help="steps of the kinetic-energy/enstrophy comparison on the main case (0 = skip)")
+    p.add_argument("--naca-steps", type=int, default=500,
+                   help="steps of the NACA0012 O-grid case, FP64 vs mixed with the boundary routine (0 = skip)")
+    p.add_argument("--naca-grid", default="512,128,32", help="NACA0012 O-grid nodes around,normal,span")
     return p.parse_args(argv)
 
 
@@ -361,6 +364,8 @@ def gpu_arm(args):
         line["batched"] = bench_batched(ctx, torch, stream, args)
     if args.serve_requests > 0:
         line["serving"] = bench_serving(ctx, args)
+    if args.naca_steps > 0:
+        line["naca0012"] = bench_naca(ctx, torch, stream, args)
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         rate, cores, secs = cpu_oracle_rate(case, args.cpu_steps)
@@ -476,6 +481,59 @@ def bench_diagnostics(ctx, case, args):
             "kinetic_energy_fp64": hist[0][:, 0].tolist(), "enstrophy_fp64": hist[0][:, 1].tolist(),
             "kinetic_energy_max_rel_err_mixed": float(err[:, 0].max()),
             "enstrophy_max_rel_err_mixed": float(err[:, 1].max())}
+
+
+def bench_naca(ctx, torch, stream, args):
+    """Shocked curvilinear case: NACA0012 O-grid (Mach 0.8, AoA 1.25 deg,
+    Re 5e5, MTS LES), no-slip wall and inlet/outlet far field filled by the
+    reference's boundary routine after every stage.  FP64 and mixed forms
+    from the same start (the free stream after one boundary fill); relative
+    L2 and Linf of density and pressure of the mixed form against FP64."""
+    import numpy as np
+    from cfd_gb300 import layout, runtime
+    from cfd_gb300 import cases
+    ni, nj, nk = (int(x) for x in args.naca_grid.split(","))
+    t0 = time.perf_counter()
+    case = cases.naca0012(ni=ni, nj=nj, nk=nk)
+    gen_s = time.perf_counter() - t0
+    # the reference fills the boundaries once before its time loop
+    bnd = runtime.Boundary(ctx, case.arrays["grid"], case.bc)
+    dev = ctx.alloc(case.arrays["flow"].nbytes)
+    ctx.write(dev, case.arrays["flow"])
+    bnd.fill(dev, case.params.mach, 1, case.sd_node)
+    flow0 = np.empty_like(case.arrays["flow"])
+    ctx.read(flow0, dev)
+    ctx.free(dev)
+    bnd.close()
+    N = case.sd_node
+    steps = args.naca_steps
+    out = {"workload": f"naca0012_ogrid_{ni}x{nj}x{nk}_m0.8_aoa1.25_re5e5_les", "grid": [ni, nj, nk],
+           "nodes_owned": N, "nodes_with_ghosts": case.g_node, "steps": steps, "dt": case.dt,
+           "case_generation_s": gen_s,
+           "boundary_lists": {t: int(len(getattr(case.bc, t))) for t in ("outlet", "inlet", "boundary", "wall")}}
+    res = {}
+    for prec in (0, 1):
+        s = runtime.Solver(ctx, case, precision=prec)
+        assert s.info().path == "structured"
+        s.set_flow(flow0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        s.step(case.dt, steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        secs = e0.elapsed_time(e1) / 1e3
+        res[prec] = s.get_flow()[1:N + 1]
+        s.close()
+        out["mixed" if prec else "fp64"] = {"value": N * steps / secs, "unit": UNIT, "ms_per_step": 1e3 * secs / steps}
+    f = layout.FLOW
+    for name in ("rho", "p"):
+        a, b = res[1][:, f[name]], res[0][:, f[name]]
+        out[f"{name}_rel_l2_mixed_vs_fp64"] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+        out[f"{name}_rel_linf_mixed_vs_fp64"] = float(np.abs(a - b).max() / np.abs(b).max())
+    out["finite"] = bool(np.isfinite(res[0]).all() and np.isfinite(res[1]).all())
+    out["mixed"]["speedup_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    return out
 
 
 def bench_serving(ctx, args):

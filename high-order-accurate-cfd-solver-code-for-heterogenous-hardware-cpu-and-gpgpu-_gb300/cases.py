@@ -503,45 +503,75 @@ GHOSTS = 3   # ghost layers beyond the owned nodes of a non-periodic direction
 
 
 def _index_derivative(X: np.ndarray, axis: int, periodic: bool, period: float = 0.0) -> np.ndarray:
-    """d X / d (index) along `axis`: 4th-order central (wrapped when
-    periodic, X(c + n) = X(c) + period); 2nd-order at the two outermost
-    layers of a non-periodic direction (ghost layers only)."""
+    """d X / d (index) along `axis`, 4th order: central (wrapped when
+    periodic, X(c + n) = X(c) + period), one-sided at the two outermost
+    layers of a non-periodic direction."""
+    n = X.shape[axis]
     if periodic:
-        n = X.shape[axis]
         c = np.arange(n).reshape([-1 if a == axis else 1 for a in range(X.ndim)])
 
         def r(s):   # X[c + s] continued across the wrap
             return np.roll(X, -s, axis=axis) + period * np.floor_divide(c + s, n)
         return (r(-2) - 8.0 * r(-1) + 8.0 * r(1) - r(2)) / 12.0
-    n = X.shape[axis]
     Xt = np.moveaxis(X, axis, 0)
     D = np.empty_like(Xt)
     D[2:n - 2] = (Xt[0:n - 4] - 8.0 * Xt[1:n - 3] + 8.0 * Xt[3:n - 1] - Xt[4:n]) / 12.0
-    D[0] = (-3.0 * Xt[0] + 4.0 * Xt[1] - Xt[2]) / 2.0
-    D[1] = (Xt[2] - Xt[0]) / 2.0
-    D[n - 2] = (Xt[n - 1] - Xt[n - 3]) / 2.0
-    D[n - 1] = (3.0 * Xt[n - 1] - 4.0 * Xt[n - 2] + Xt[n - 3]) / 2.0
+    D[0] = (-25.0 * Xt[0] + 48.0 * Xt[1] - 36.0 * Xt[2] + 16.0 * Xt[3] - 3.0 * Xt[4]) / 12.0
+    D[1] = (-3.0 * Xt[0] - 10.0 * Xt[1] + 18.0 * Xt[2] - 6.0 * Xt[3] + Xt[4]) / 12.0
+    D[n - 1] = -(-25.0 * Xt[n - 1] + 48.0 * Xt[n - 2] - 36.0 * Xt[n - 3] + 16.0 * Xt[n - 4] - 3.0 * Xt[n - 5]) / 12.0
+    D[n - 2] = -(-3.0 * Xt[n - 1] - 10.0 * Xt[n - 2] + 18.0 * Xt[n - 3] - 6.0 * Xt[n - 4] + Xt[n - 5]) / 12.0
     return np.moveaxis(D, 0, axis)
+
+
+def _mirror_pad(A: np.ndarray, axis: int, G: int, point: bool) -> np.ndarray:
+    """A padded by G layers on both ends of `axis`: the mirror image about
+    the end layer (point=True: point reflection 2 A[0] - A[m], for
+    coordinates; else the even copy A[m])."""
+    At = np.moveaxis(A, axis, 0)
+    lo = At[1:G + 1][::-1]
+    hi = At[-G - 1:-1][::-1]
+    if point:
+        lo = 2.0 * At[0] - lo
+        hi = 2.0 * At[-1] - hi
+    return np.moveaxis(np.concatenate([lo, At, hi], axis=0), 0, axis)
 
 
 def ghosted_lattice(name: str, X, Y, Z, periodic, prims, params: Params, mach: float, bc_type=None,
                     cfl: float = 0.5, periods=None) -> Case:
-    """A case on an (i, j, k) lattice whose non-periodic directions carry
-    GHOSTS ghost layers on each side, in the reference layout.
+    """A case on an (i, j, k) lattice of owned nodes whose non-periodic
+    directions get GHOSTS ghost layers on each side, in the reference layout.
 
-    X, Y, Z: node coordinates over the padded lattice [i, j, k]; periodic:
-    three flags; prims: (rho, u, v, w, p) arrays over the padded lattice;
-    bc_type(i, j, k, loc) -> "outlet" | "inlet" | "boundary" | "wall" | None
-    classifies each owned boundary node (padded indices) into the boundary
+    X, Y, Z: coordinates of the owned nodes [i, j, k]; periodic: three
+    flags; periods[d]: the (x, y, z) shift across one period of direction d;
+    prims: (rho, u, v, w, p) over the owned nodes; bc_type(i, j, k, loc) ->
+    "outlet" | "inlet" | "boundary" | "wall" | None classifies each owned
+    boundary node (indices of the padded lattice) into the boundary
     routine's lists.  Rows: owned nodes first (i fastest), then ghosts, as
     the reference numbers them; the outermost ghosts of a non-periodic
-    direction point at themselves.  periods[d] = the (x, y, z) shift across
-    one period of direction d.  Node metrics come from 4th-order index
-    derivatives of the coordinates; half-point metrics by the six-point rule
-    on every row (the faces of the owned nodes are then single-valued)."""
+    direction point at themselves.  Node metrics come from 4th-order index
+    derivatives over the owned nodes; ghosts carry the mirror image of the
+    owned metrics and state about the boundary node (their coordinates are
+    the point reflection); half-point metrics follow by the six-point rule
+    on every row, so the faces of the owned nodes are single-valued."""
+    G = GHOSTS
+    periods = periods or ((0.0, 0.0, 0.0),) * 3
+    jac = np.empty(X.shape + (3, 3))
+    for axis in range(3):
+        for comp, V in enumerate((X, Y, Z)):
+            jac[..., comp, axis] = _index_derivative(V, axis, periodic[axis], periods[axis][comp])
+    m9, det = _node_metrics(jac)
+    if not np.all(det > 0):
+        raise ValueError(f"{name}: the mapping folds (det <= 0 at {int((det <= 0).sum())} nodes)")
+    fields = [np.broadcast_to(q, X.shape).astype(np.float64) for q in prims]
+    for d in range(3):
+        if periodic[d]:
+            continue
+        X, Y, Z = (_mirror_pad(V, d, G, True) for V in (X, Y, Z))
+        m9 = _mirror_pad(m9, d, G, False)
+        det = _mirror_pad(det, d, G, False)
+        fields = [_mirror_pad(q, d, G, False) for q in fields]
     pi_, pj, pk = X.shape
     ext = (pi_, pj, pk)
-    G = GHOSTS
     ii, jj, kk = np.meshgrid(np.arange(pi_), np.arange(pj), np.arange(pk), indexing="ij")
     cc = (ii, jj, kk)
     owned = np.ones(X.shape, dtype=bool)
@@ -578,25 +608,16 @@ def ghosted_lattice(name: str, X, Y, Z, periodic, prims, params: Params, mach: f
     put("N4", nb(2, 1))
     put("N5", nb(2, -1))
     put("ID", np.zeros(X.shape, dtype=np.int64))
-    edge = [(cc[d] == G) & (not periodic[d]) for d in range(3)], [(cc[d] == ext[d] - G - 1) & (not periodic[d])
-                                                                     for d in range(3)]
-    loc = reference_loc_codes(edge[0][0], edge[1][0], edge[0][1], edge[1][1], edge[0][2], edge[1][2])
+    lo = [(cc[d] == G) & (not periodic[d]) for d in range(3)]
+    hi = [(cc[d] == ext[d] - G - 1) & (not periodic[d]) for d in range(3)]
+    loc = reference_loc_codes(lo[0], hi[0], lo[1], hi[1], lo[2], hi[2])
     loc = np.where(owned, loc, 100)
     put("loc", loc)
-
-    jac = np.empty(X.shape + (3, 3))
-    periods = periods or ((0.0, 0.0, 0.0),) * 3
-    for axis in range(3):
-        for comp, V in enumerate((X, Y, Z)):
-            jac[..., comp, axis] = _index_derivative(V, axis, periodic[axis], periods[axis][comp])
-    m9, det = _node_metrics(jac)
-    if not np.all(det > 0):
-        raise ValueError(f"{name}: the mapping folds (det <= 0 at {int((det <= 0).sum())} nodes)")
     a["metric"][order.ravel(), 0:9] = m9.reshape(-1, 9)
     a["det"][order.ravel()] = det.ravel()
     half_point_metrics(a, n_all)
 
-    rho, u, v, w, p = (np.broadcast_to(q, X.shape) for q in prims)
+    rho, u, v, w, p = fields
     flow = np.zeros((n_all, 9))
     _flow_from_primitives(flow, rho.ravel(), u.ravel(), v.ravel(), w.ravel(), p.ravel(), mach)
     a["flow"][order.ravel()] = flow
@@ -621,11 +642,9 @@ def channel(ni=16, nj=12, nk=8, mach=0.5, reynolds=500.0, amp=0.05, les=1, seed=
     inlet (x < L/2) and outlet nodes, so the lattice path, the loc-code
     branches and every face rule of the boundary routine run together.
     Parabolic streamwise profile with a seeded perturbation."""
-    G = GHOSTS
     Lx, H, Lz = 2.0, 1.0, 1.0
-    pj = nj + 2 * G
     hx, hy, hz = Lx / ni, H / (nj - 1), Lz / nk
-    i, j, k = np.meshgrid(np.arange(ni), np.arange(pj) - G, np.arange(nk), indexing="ij")
+    i, j, k = np.meshgrid(np.arange(ni), np.arange(nj), np.arange(nk), indexing="ij")
     xi, eta, zeta = i * hx, j * hy, k * hz
     X = xi + amp * hx * np.sin(2 * np.pi * eta / H) * np.cos(2 * np.pi * zeta / Lz)
     Y = eta + amp * hy * np.sin(2 * np.pi * xi / Lx) * np.cos(2 * np.pi * zeta / Lz)
@@ -648,3 +667,57 @@ def channel(ni=16, nj=12, nk=8, mach=0.5, reynolds=500.0, amp=0.05, les=1, seed=
 
     return ghosted_lattice("channel", X, Y, Z, (True, False, True), (rho, u, v, w, p), prm, mach, bc_type,
                            periods=((Lx, 0.0, 0.0), (0.0, 0.0, 0.0), (0.0, 0.0, Lz)))
+
+
+def naca0012_thickness(x: np.ndarray, t: float = 0.12) -> np.ndarray:
+    """Half thickness of the NACA 4-digit symmetric section, closed trailing
+    edge (last coefficient -0.1036), chord 1."""
+    return 5.0 * t * (0.2969 * np.sqrt(x) - 0.1260 * x - 0.3516 * x**2 + 0.2843 * x**3 - 0.1036 * x**4)
+
+
+def naca0012(ni=512, nj=128, nk=32, mach=0.8, aoa_deg=1.25, reynolds=5e5, span=0.2, radius=15.0, beta=6.0,
+             les=1, cfl=0.5) -> Case:
+    """Shocked transonic case: an algebraic O-grid around a NACA0012 section.
+
+    i (periodic) runs clockwise around the section from the trailing edge
+    over the lower surface, x = (1 + cos phi)/2 (cosine clustering at both
+    edges);
+    j runs from the wall to a circle of `radius` chords about mid-chord with
+    exponential clustering s = (e^(beta eta) - 1)/(e^beta - 1); k is the
+    periodic span; three ghost layers mirror the first and last owned
+    layers (ghosted_lattice).  The grid is rotated by -aoa about the
+    quarter chord, so the reference's free stream (u = 1, v = 0, its inlet
+    state) meets the section at the angle of attack.  Wall nodes are
+    no-slip walls; far-field nodes upstream of mid-chord are inlets, the
+    rest outlets.  Initial state: the free stream."""
+    i = np.arange(ni)
+    phi = -2.0 * np.pi * i / ni          # clockwise: (i, j, k) right-handed
+    xs = 0.5 * (1.0 + np.cos(phi))
+    ys = np.sign(np.sin(phi)) * naca0012_thickness(xs)
+    xo = 0.5 + radius * np.cos(phi)
+    yo = radius * np.sin(phi)
+    eta = np.arange(nj) / (nj - 1)
+    s = np.expm1(beta * eta) / np.expm1(beta)
+    X2 = xs[:, None] + s[None, :] * (xo - xs)[:, None]
+    Y2 = ys[:, None] + s[None, :] * (yo - ys)[:, None]
+    a = math.radians(aoa_deg)
+    Xr = 0.25 + (X2 - 0.25) * math.cos(a) + Y2 * math.sin(a)
+    Yr = -(X2 - 0.25) * math.sin(a) + Y2 * math.cos(a)
+    z = np.arange(nk) * span / nk
+    X = np.repeat(Xr[:, :, None], nk, axis=2)
+    Y = np.repeat(Yr[:, :, None], nk, axis=2)
+    Z = np.broadcast_to(z[None, None, :], X.shape).copy()
+    p_inf = 1.0 / (1.4 * mach * mach)
+    prims = (np.ones(X.shape), np.ones(X.shape), np.zeros(X.shape), np.zeros(X.shape), np.full(X.shape, p_inf))
+    prm = Params(mach=mach, reynolds=reynolds, viscous=1, les=les)
+    upstream = np.cos(phi) < 0.0
+
+    def bc_type(ii, jj, kk, loc):
+        if loc == 3:
+            return "wall"
+        if loc == 1:
+            return "inlet" if upstream[ii] else "outlet"
+        return None
+
+    return ghosted_lattice("naca0012", X, Y, Z, (True, False, True), prims, prm, mach, bc_type, cfl=cfl,
+                           periods=((0.0, 0.0, 0.0), (0.0, 0.0, 0.0), (0.0, 0.0, span)))

@@ -10,11 +10,11 @@ namespace {
 
 struct Ops {
     static __device__ __forceinline__ void prep(const LatView &g, int n, int q) { mx::init_node(g, n, q); }
-    static __device__ __forceinline__ void visc(const LatView &g, int n, int q) { mx::visc_node(g, n, q); }
+    static __device__ __forceinline__ void visc(const LatView &g, int n, int q) { mx::visc_node<false>(g, n, q); }
     static __device__ __forceinline__ void mu(const LatView &g, int n, int q) { mx::mu_node(g, n, q); }
     template <int D>
     static __device__ __forceinline__ void face(const LatView &g, int n) { mx::face_node<D>(g, n); }
-    static __device__ __forceinline__ void update(const LatView &g, int n, int j) { mx::update_node(g, n, j); }
+    static __device__ __forceinline__ void update(const LatView &g, int n, int j) { mx::update_node<false>(g, n, j); }
 };
 
 }  // namespace

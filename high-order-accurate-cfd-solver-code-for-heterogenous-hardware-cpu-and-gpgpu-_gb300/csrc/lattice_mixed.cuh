@@ -216,8 +216,10 @@ __device__ __forceinline__ float branch_deriv_diff(int b, const float dl[6])
 
 // Viscous + MTS SGS fluxes from slot q.  Derivatives of U from hi/lo
 // differences (exact hi differences for neighbours within a factor of two):
-// central on a periodic lattice, the reference's loc-code branches on a
-// lattice with loc codes, zero at ghosts; everything else in FP32.
+// central on a periodic lattice (LOC = false), the reference's loc-code
+// branches on a lattice with loc codes (LOC = true; zero at ghosts);
+// everything else in FP32.
+template <bool LOC>
 __device__ __forceinline__ void visc_node(const LatView &g, int n, int q)
 {
     const int N = g.N;
@@ -225,7 +227,7 @@ __device__ __forceinline__ void visc_node(const LatView &g, int n, int q)
     int i, j, k;
     lat_ijk(g, n, i, j, k);
     float dU[3][5], KS[3], Ui[5];
-    const bool ghost = lat_ghost(g, n);
+    const bool ghost = LOC && lat_ghost(g, n);
 #pragma unroll
     for (int c = 0; c < 5; ++c) Ui[c] = W[c * N + n];
 #pragma unroll
@@ -235,7 +237,7 @@ __device__ __forceinline__ void visc_node(const LatView &g, int n, int q)
         if (ghost) {
 #pragma unroll
             for (int c = 0; c < 5; ++c) dU[d][c] = 0.0f;
-        } else if (!g.loc8) {
+        } else if (!LOC) {
 #pragma unroll
             for (int c = 0; c < 5; ++c) {
                 const float *H = W + c * N, *L = W + (5 + c) * N;
@@ -338,11 +340,12 @@ __device__ __forceinline__ void face_node(const LatView &g, int n)
 //   jst 1: U2 = 3/4 U0 + 1/4 U1 + 1/4 dt L
 //   jst 2: U0 = 1/3 U0 + 2/3 U2 + 2/3 dt L
 // and the new state lands in slot (jst+1) mod 3, which is also the next
-// stage's U_Q slot.
+// stage's U_Q slot.  LOC as for visc_node.
+template <bool LOC>
 __device__ __forceinline__ void update_node(const LatView &g, int n, int jst)
 {
     const int N = g.N;
-    if (lat_ghost(g, n)) {   // ghosts are the boundary routine's
+    if (LOC && lat_ghost(g, n)) {   // ghosts are the boundary routine's
         if (g.Lout) {
 #pragma unroll
             for (int c = 0; c < 5; ++c) g.Lout[c * N + n] = 0.0;
@@ -357,7 +360,7 @@ __device__ __forceinline__ void update_node(const LatView &g, int n, int jst)
         const int m1 = lat_step(g, i, j, k, d, -1);
 #pragma unroll
         for (int c = 0; c < 5; ++c) Lf[c] += g.Fh32[(d * 5 + c) * N + n] - g.Fh32[(d * 5 + c) * N + m1];
-        if (g.P.viscous && g.loc8) {
+        if (LOC && g.P.viscous) {
             int s[7], L7[7];
 #pragma unroll
             for (int o = 0; o < 7; ++o) {

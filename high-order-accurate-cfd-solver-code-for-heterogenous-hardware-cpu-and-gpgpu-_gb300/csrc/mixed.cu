@@ -37,10 +37,11 @@ __global__ void __launch_bounds__(256) k_prep_m(LatView g, int src, int dst)
     if (n < g.N) mx::prep_node(g, n, src, dst);
 }
 
+template <bool LOC>
 __global__ void __launch_bounds__(256) k_visc_m(LatView g, int q)
 {
     const int n = node_id();
-    if (n < g.N) mx::visc_node(g, n, q);
+    if (n < g.N) mx::visc_node<LOC>(g, n, q);
 }
 
 __global__ void __launch_bounds__(256) k_mu_m(LatView g, int q)
@@ -60,10 +61,11 @@ __global__ void __launch_bounds__(128, CFD_MFACE_MIN_BLOCKS) k_face_m(LatView g)
     if (n < g.N) mx::face_node<D>(g, n);
 }
 
+template <bool LOC>
 __global__ void __launch_bounds__(256) k_update_m(LatView g, int jst)
 {
     const int n = node_id();
-    if (n < g.N) mx::update_node(g, n, jst);
+    if (n < g.N) mx::update_node<LOC>(g, n, jst);
 }
 
 __global__ void k_bc_m(LatView g, const BcEntry *__restrict__ E, int n, int type, int q, double mach, int sequential)
@@ -168,8 +170,12 @@ int mixed_stage(const StructuredLaunch &S, int jst, double dt, double *Lout, cud
         name("prep");
         mark();
     }
+    const bool loc = g.loc8 != nullptr;   // lattice with ghost layers and loc codes
     if (S.P.viscous) {
-        k_visc_m<<<nb256, 256, 0, st>>>(g, jst);
+        if (loc)
+            k_visc_m<true><<<nb256, 256, 0, st>>>(g, jst);
+        else
+            k_visc_m<false><<<nb256, 256, 0, st>>>(g, jst);
         name("viscous");
     } else {
         k_mu_m<<<nb256, 256, 0, st>>>(g, jst);
@@ -185,7 +191,10 @@ int mixed_stage(const StructuredLaunch &S, int jst, double dt, double *Lout, cud
     k_face_m<2><<<nb128, 128, 0, st>>>(g);
     name("face_k");
     mark();
-    k_update_m<<<nb256, 256, 0, st>>>(g, jst);
+    if (loc)
+        k_update_m<true><<<nb256, 256, 0, st>>>(g, jst);
+    else
+        k_update_m<false><<<nb256, 256, 0, st>>>(g, jst);
     name("update+prep");
     mark();
     return k;

@@ -101,3 +101,29 @@ def test_tgv_initial_kinetic_energy(pkg):
     ke, ens = diagnostics.kinetic_energy_enstrophy(c.arrays["flow"], c.arrays["metric"], c.arrays["det"], c.shape)
     assert abs(ke - 0.125) < 1e-12
     assert abs(ens - 0.375) < 2e-3            # 3/8 for the analytic field, 4th-order differences
+
+
+def test_naca0012_ogrid_geometry_and_lists(pkg):
+    """The O-grid: right-handed and unfolded, owned rows first, wall rows on
+    the section (loc 3), far-field rows (loc 1) split upstream/downstream,
+    three ghost layers (loc 100) on each side of the wall-normal direction."""
+    import numpy as np
+    from cfd_gb300 import cases
+    c = cases.naca0012(ni=48, nj=16, nk=4)
+    g = c.arrays["grid"]
+    assert c.shape == (48, 16, 4) and c.sd_node == 48 * 16 * 4 and c.g_node == 48 * 22 * 4
+    assert np.all(c.arrays["det"][1:] > 0)
+    loc = g["loc"]
+    assert np.all(loc[1:c.sd_node + 1] != 100) and np.all(loc[c.sd_node + 1:] == 100)
+    assert set(loc[c.bc.wall].tolist()) == {3} and len(c.bc.wall) == 48 * 4
+    far = np.concatenate([c.bc.inlet, c.bc.outlet])
+    assert set(loc[far].tolist()) == {1} and len(far) == 48 * 4
+    assert len(c.bc.inlet) == len(c.bc.outlet)               # upstream half / downstream half
+    a = np.radians(1.25)
+
+    def unrotated(rows):   # undo the angle-of-attack rotation about the quarter chord
+        x, y = g["x"][rows] - 0.25, g["y"][rows]
+        return 0.25 + x * np.cos(a) - y * np.sin(a), x * np.sin(a) + y * np.cos(a)
+    assert np.all(unrotated(c.bc.inlet)[0] < 0.5) and np.all(unrotated(c.bc.outlet)[0] >= 0.5)
+    x, y = unrotated(c.bc.wall)                               # wall rows lie on the section
+    assert np.allclose(np.abs(y), cases.naca0012_thickness(np.clip(x, 0, 1)), atol=1e-12)

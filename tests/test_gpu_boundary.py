@@ -138,3 +138,28 @@ def test_ghost_box_gather_path_with_boundary(ctx, oracle_mod):
     a = c.copy().arrays
     oracle_mod.rk3_steps_bc(a, c.g_node, c.sd_node, c.params, c.dt, 1, c.bc)
     _assert_flow_close(flow, a["flow"])
+
+
+def test_naca0012_ogrid_fp64_matches_oracle_and_mixed_budget(ctx, oracle_mod):
+    """Config 3's case at a reduced size: the O-grid on the lattice path with
+    the wall and inlet/outlet far field filled after every stage, FP64
+    against the oracle, and the mixed form's density and pressure."""
+    from cfd_gb300 import cases, layout, runtime
+    c = cases.naca0012(ni=64, nj=24, nk=4)
+    flow0 = c.copy().arrays
+    oracle_mod.boundary_fill(flow0, c.bc, c.params.mach, 1, c.sd_node)
+    res = {}
+    for prec in (0, 1):
+        s = runtime.Solver(ctx, c, precision=prec)
+        assert s.info().path == "structured"
+        s.set_flow(flow0["flow"])
+        s.step(c.dt, 3)
+        res[prec] = s.get_flow()
+        s.close()
+    a = {k: v.copy() for k, v in flow0.items()}
+    oracle_mod.rk3_steps_bc(a, c.g_node, c.sd_node, c.params, c.dt, 3, c.bc)
+    _assert_flow_close(res[0], a["flow"])
+    own = slice(1, c.sd_node + 1)
+    for name in ("rho", "p"):
+        k = layout.FLOW[name]
+        assert rel_l2(res[1][own, k], res[0][own, k]) <= 1e-6
