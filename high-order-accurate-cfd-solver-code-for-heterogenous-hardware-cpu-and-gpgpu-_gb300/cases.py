@@ -721,3 +721,25 @@ def naca0012(ni=512, nj=128, nk=32, mach=0.8, aoa_deg=1.25, reynolds=5e5, span=0
 
     return ghosted_lattice("naca0012", X, Y, Z, (True, False, True), prims, prm, mach, bc_type, cfl=cfl,
                            periods=((0.0, 0.0, 0.0), (0.0, 0.0, 0.0), (0.0, 0.0, span)))
+
+
+def duct(ni=12, nj=10, nk=9, mach=0.5, reynolds=500.0, amp=0.04, seed=1) -> Case:
+    """Square duct on a perturbed grid: periodic in x (i), no-slip walls on
+    all four sides in y (j) and z (k), so the lattice path carries edge
+    codes (15, 17, 19, 21) next to the face codes and the boundary
+    routine's wall list mixes face and edge entries."""
+    Lx, H, W = 2.0, 1.0, 1.0
+    hx, hy, hz = Lx / ni, H / (nj - 1), W / (nk - 1)
+    i, j, k = np.meshgrid(np.arange(ni), np.arange(nj), np.arange(nk), indexing="ij")
+    xi, eta, zeta = i * hx, j * hy, k * hz
+    X = xi + amp * hx * np.sin(np.pi * eta / H) * np.sin(np.pi * zeta / W)
+    Y = eta + amp * hy * np.sin(2 * np.pi * xi / Lx) * np.sin(np.pi * zeta / W)
+    Z = zeta + amp * hz * np.cos(2 * np.pi * xi / Lx) * np.sin(np.pi * eta / H)
+    rng = np.random.default_rng(seed)
+    u = 16.0 * (Y / H) * (1 - Y / H) * (Z / W) * (1 - Z / W) + 0.02 * rng.standard_normal(X.shape)
+    v = 0.02 * rng.standard_normal(X.shape)
+    w = 0.02 * rng.standard_normal(X.shape)
+    p = np.full(X.shape, 1.0 / (1.4 * mach * mach))
+    prm = Params(mach=mach, reynolds=reynolds, viscous=1, les=1)
+    return ghosted_lattice("duct", X, Y, Z, (True, False, False), (np.ones(X.shape), u, v, w, p), prm, mach,
+                           lambda ii, jj, kk, loc: "wall", periods=((Lx, 0.0, 0.0), (0.0, 0.0, 0.0), (0.0, 0.0, 0.0)))

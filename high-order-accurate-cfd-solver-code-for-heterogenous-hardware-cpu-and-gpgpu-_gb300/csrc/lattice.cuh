@@ -90,6 +90,7 @@ __device__ __forceinline__ int lat_step(const LatView &g, int i, int j, int k, i
 __device__ __forceinline__ int lat_coord(int i, int j, int k, int d) { return d == 0 ? i : (d == 1 ? j : k); }
 
 __device__ __forceinline__ int lat_extent(const LatView &g, int d) { return d == 0 ? g.ni : (d == 1 ? g.nj : g.nk); }
+inline int lat_extent_h(const LatView &g, int d) { return d == 0 ? g.ni : (d == 1 ? g.nj : g.nk); }
 
 // Face n+1/2 along a non-periodic d is needed (and its six-point stencil
 // lies in the box) for coordinates 2 .. n_d-4.

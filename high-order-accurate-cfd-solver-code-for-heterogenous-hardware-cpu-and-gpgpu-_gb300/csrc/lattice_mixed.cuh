@@ -345,11 +345,17 @@ template <bool LOC>
 __device__ __forceinline__ void update_node(const LatView &g, int n, int jst)
 {
     const int N = g.N;
-    if (LOC && lat_ghost(g, n)) {   // ghosts are the boundary routine's
+    if (LOC && lat_ghost(g, n)) {
+        // Ghosts are the boundary routine's, which fills those next to face
+        // nodes after this kernel; the others (behind edges and corners) keep
+        // their state, which moves on to the next stage's slot.
         if (g.Lout) {
 #pragma unroll
             for (int c = 0; c < 5; ++c) g.Lout[c * N + n] = 0.0;
         }
+        dfl Us[5];
+        load_state(g, jst, n, Us);
+        store_state(g, jst == 2 ? 0 : jst + 1, n, Us);
         return;
     }
     int i, j, k;

@@ -8,8 +8,9 @@
 // appears only where FLOW enters (after an upload) and where FLOW/U leave.
 // Stage intermediates are FP32 (half the bytes of the FP64 form).
 //
-// Kernels per stage: k_visc_m (radius-2 star), k_face_m<d> x3 (one thread
-// per face), k_update_m (RK stage + the next stage's U_Q); k_init_m /
+// Kernels per stage: k_visc_m (radius-2 star), k_face_tile_m<d> x3 (one
+// thread per face, stencil lines staged in shared memory), k_update_m (RK
+// stage + the next stage's U_Q); k_init_m /
 // k_prep_m supply U_Q when no update produced it.  The per-node operations
 // are in lattice_mixed.cuh.  This file is compiled with FMA contraction on
 // and approximate FP32 division/square root (the mixed form's error budget
@@ -54,11 +55,101 @@ __global__ void __launch_bounds__(256) k_mu_m(LatView g, int q)
 #define CFD_MFACE_MIN_BLOCKS 8
 #endif
 
+// Faces along D from a tile staged in shared memory: the block covers
+// kTile faces along D times kWide nodes across (axis A), one line of the
+// third axis (B).  It loads the stencil lines (kTile + 5 nodes along D) of
+// Q, the Roe inputs and the node fluxes along D once, coalesced along i,
+// and every face reads its six points from there.
 template <int D>
-__global__ void __launch_bounds__(128, CFD_MFACE_MIN_BLOCKS) k_face_m(LatView g)
+struct FaceTile {
+    static constexpr int kTile = D == 0 ? 32 : 8;       // faces along D
+    static constexpr int kWide = 128 / kTile;           // nodes across
+    static constexpr int A = D == 0 ? 1 : 0;            // axis across
+    static constexpr int B = D == 2 ? 1 : 2;            // axis of the block's line
+    static constexpr int kLine = kTile + 5;             // staged nodes along D
+    // smem index of (position b along D, a across); i is the fast index
+    static __device__ __forceinline__ int at(int b, int a) { return D == 0 ? a * kLine + b : b * kWide + a; }
+    // thread -> (t along D, a across), consecutive threads consecutive in i
+    static __device__ __forceinline__ void split(int x, int &t, int &a)
+    {
+        if (D == 0) { t = x % kTile; a = x / kTile; }
+        else { t = x / kWide; a = x % kWide; }
+    }
+};
+
+__device__ __forceinline__ int tile_coord(const LatView &g, int d, int c)
 {
-    const int n = node_id();
-    if (n < g.N) mx::face_node<D>(g, n);
+    const int n = lat_extent(g, d);
+    if (lat_periodic(g, d)) return ((c % n) + n) % n;
+    return c < 0 ? 0 : (c >= n ? n - 1 : c);
+}
+
+template <int D>
+__global__ void __launch_bounds__(128, CFD_MFACE_MIN_BLOCKS) k_face_tile_m(LatView g)
+{
+    using T = FaceTile<D>;
+    constexpr int S = T::kLine * T::kWide;
+    __shared__ float sQ[5][S], sR[5][S], sF[5][S];
+    const int N = g.N;
+    const int tD = blockIdx.x * T::kTile, tA = blockIdx.y * T::kWide, cB = blockIdx.z;
+    const int nA = lat_extent(g, T::A);
+    const float *NF = g.FEG32 + (size_t)D * 5 * N;
+    for (int m = threadIdx.x; m < S; m += blockDim.x) {
+        int b, a;
+        if (D == 0) { b = m % T::kLine; a = m / T::kLine; }
+        else { b = m / T::kWide; a = m % T::kWide; }
+        int c[3];
+        c[D] = tile_coord(g, D, tD + b - 2);
+        c[T::A] = tA + a < nA ? tA + a : nA - 1;
+        c[T::B] = cB;
+        const int node = c[0] + g.ni * (c[1] + g.nj * c[2]);
+        const int e = T::at(b, a);
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+            sQ[q][e] = g.Q32[q * N + node];
+            sR[q][e] = g.R32[q * N + node];
+            sF[q][e] = NF[q * N + node];
+        }
+    }
+    __syncthreads();
+    int t, a;
+    T::split(threadIdx.x, t, a);
+    int c[3];
+    c[D] = tD + t;
+    c[T::A] = tA + a;
+    c[T::B] = cB;
+    if (c[D] >= lat_extent(g, D) || c[T::A] >= nA || !lat_face_needed(g, c[0], c[1], c[2], D)) return;
+    const int n = c[0] + g.ni * (c[1] + g.nj * c[2]);
+    float2 P[3][5];
+#pragma unroll
+    for (int o = 0; o < 3; ++o)
+#pragma unroll
+        for (int q = 0; q < 5; ++q) P[o][q] = make_float2(sQ[q][T::at(t + o, a)], sQ[q][T::at(t + 5 - o, a)]);
+    float r[5];
+    {
+        const int er = T::at(t + 3, a), el = T::at(t + 2, a);
+        roe_average<float>(sR[3][er], sR[0][er], sR[1][er], sR[2][er], sR[4][er], sR[3][el], sR[0][el], sR[1][el],
+                           sR[2][el], sR[4][el], r);
+    }
+    float Fhat[5];
+    x2::llf_face_flux2(P, g.fm32[(D * 3 + 0) * N + n], g.fm32[(D * 3 + 1) * N + n], g.fm32[(D * 3 + 2) * N + n],
+                       g.fdet32[D * N + n], r, (float)g.P.eps, Fhat);
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+        float f[6];
+#pragma unroll
+        for (int o = 0; o < 6; ++o) f[o] = sF[q][T::at(t + o, a)];
+        g.Fh32[(D * 5 + q) * N + n] = Fhat[q] + x2::face_correction_sym(f);
+    }
+}
+
+template <int D>
+void launch_face_tile(const LatView &g, cudaStream_t st)
+{
+    using T = FaceTile<D>;
+    const dim3 grid((unsigned)((lat_extent_h(g, D) + T::kTile - 1) / T::kTile),
+                    (unsigned)((lat_extent_h(g, T::A) + T::kWide - 1) / T::kWide), (unsigned)lat_extent_h(g, T::B));
+    k_face_tile_m<D><<<grid, 128, 0, st>>>(g);
 }
 
 template <bool LOC>
@@ -150,7 +241,7 @@ int mixed_stage(const StructuredLaunch &S, int jst, double dt, double *Lout, cud
                 const char **names)
 {
     const LatView g = make_view(S, dt, Lout);
-    const unsigned nb256 = blocks_for(g.N, 256), nb128 = blocks_for(g.N, 128);
+    const unsigned nb256 = blocks_for(g.N, 256);
     cudaStream_t st = S.stream;
     int e = 0, k = 0;
     auto mark = [&]() {
@@ -182,13 +273,13 @@ int mixed_stage(const StructuredLaunch &S, int jst, double dt, double *Lout, cud
         name("mu_only");
     }
     mark();
-    k_face_m<0><<<nb128, 128, 0, st>>>(g);
+    launch_face_tile<0>(g, st);
     name("face_i");
     mark();
-    k_face_m<1><<<nb128, 128, 0, st>>>(g);
+    launch_face_tile<1>(g, st);
     name("face_j");
     mark();
-    k_face_m<2><<<nb128, 128, 0, st>>>(g);
+    launch_face_tile<2>(g, st);
     name("face_k");
     mark();
     if (loc)
