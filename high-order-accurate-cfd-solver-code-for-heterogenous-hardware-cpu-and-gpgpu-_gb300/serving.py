@@ -15,16 +15,24 @@ Requests that arrive while others run join at the next step boundary, so
 their work overlaps on the device with the solves already in flight.  The
 reference has no serving layer; this is the builder's request loop around the
 RHS path.  Latency = completion time - arrival time.
+
+Checkpoint/resume: with ``checkpoint_dir`` every solve keeps the reference's
+restart pair (files.py) under ``<dir>/req_<rid>/``, written every
+``checkpoint_every`` batch steps and at completion; a request admitted again
+(after the loop stopped, e.g. ``max_batch_steps``) starts from its newest
+complete restart with the remaining steps.  Restarting from FLOW at a step
+boundary is exact for the FP64 form (every stage's U_Q rebuilds U from FLOW).
 """
 from __future__ import annotations
 
 import dataclasses
 import math
+import pathlib
 import time
 
 import numpy as np
 
-from . import cases, runtime
+from . import cases, files, runtime
 
 
 @dataclasses.dataclass
@@ -90,13 +98,25 @@ class Server:
     def close(self):
         self.batch.close()
 
-    def run(self, requests: list, case_cache: dict | None = None, clock=time.perf_counter) -> dict:
+    def run(self, requests: list, case_cache: dict | None = None, clock=time.perf_counter,
+            checkpoint_dir=None, checkpoint_every: int = 0, max_batch_steps: int | None = None) -> dict:
         """Serves `requests` (sorted by arrival) in real time; returns the
-        completed solves and summary statistics."""
+        completed solves and summary statistics.  max_batch_steps stops the
+        loop early (the unfinished solves are reported as `pending`)."""
         case_cache = {} if case_cache is None else case_cache
         queue = list(sorted(requests, key=lambda r: r.arrival))
-        active = {}              # slot -> [request, remaining steps, admitted time]
+        active = {}              # slot -> [request, remaining steps, admitted time, case, next restart number]
         done = []
+
+        def ckpt_dir(req):
+            d = pathlib.Path(checkpoint_dir) / f"req_{req.rid}"
+            d.mkdir(parents=True, exist_ok=True)
+            return d
+
+        def checkpoint(slot):
+            req, left, _, case, num = active[slot]
+            files.write_restart(ckpt_dir(req), self.batch.get_flow(slot), case.sd_node, req.steps - left, num)
+            active[slot][4] = 3 - num
         budget = self.info0.capacity_bytes
         t0 = clock()
         steps_run = 0
@@ -113,13 +133,29 @@ class Server:
                         raise RuntimeError(f"request {req.rid} ({req.n}^3) exceeds the device budget")
                     break
                 c = case_cache.get(req.rid) or make_case(req)
-                slot = self.batch.add(c)
+                left, num, flow = req.steps, 1, None
+                if checkpoint_dir is not None:
+                    got = files.read_restart(ckpt_dir(req), c.sd_node)
+                    if got is not None:
+                        values, it, num = got
+                        flow = files.restart_flow(c.arrays["flow"], values, c.params.mach)
+                        left = req.steps - it
+                slot = self.batch.add(c, flow=flow)
                 used += need
-                active[slot] = [req, req.steps, clock() - t0]
+                active[slot] = [req, left, clock() - t0, c, num]
                 queue.pop(0)
+                if left <= 0:       # finished before the stop: report it again
+                    self.batch.remove(slot)
+                    active.pop(slot)
+                    done.append(Completed(req.rid, req.arrival, clock() - t0, clock() - t0, req.n ** 3, req.steps,
+                                          flow if self.keep_results else None))
             if not active:
+                if not queue:
+                    break
                 time.sleep(max(0.0, min(queue[0].arrival - (clock() - t0), 0.05)))
                 continue
+            if max_batch_steps is not None and steps_run >= max_batch_steps:
+                break
             if not tuned and len(active) > 1:
                 self.batch.tune(1)
                 tuned = True
@@ -128,11 +164,20 @@ class Server:
             finished = [s for s, a in active.items() if a[1] == 1]
             for s in list(active):
                 active[s][1] -= 1
+            if checkpoint_dir is not None:
+                for s in active:
+                    if s in finished or (checkpoint_every and steps_run % checkpoint_every == 0):
+                        checkpoint(s)
             for s in finished:
-                req, _, adm = active.pop(s)
+                req, _, adm, _, _ = active.pop(s)
                 flow = self.batch.get_flow(s) if self.keep_results else None
                 self.batch.remove(s)
                 done.append(Completed(req.rid, req.arrival, adm, clock() - t0, req.n ** 3, req.steps, flow))
+        pending = [a[0].rid for a in active.values()] + [r.rid for r in queue]
+        for s in list(active):          # a stop keeps the progress of the solves in flight
+            if checkpoint_dir is not None:
+                checkpoint(s)
+            self.batch.remove(s)
         makespan = clock() - t0
         lat = np.array([c.latency for c in done])
         work = float(sum(c.nodes * c.steps for c in done))
@@ -146,4 +191,5 @@ class Server:
             "latency_p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
             "latency_p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
             "latency_max_s": float(lat.max()) if len(lat) else None,
+            "pending": pending,
         }

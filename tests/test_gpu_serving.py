@@ -34,3 +34,33 @@ def test_served_results_equal_alone(ctx, precision):
         alone.step(req.steps)
         assert np.array_equal(alone.get_flow(s), c.flow), c.rid
         alone.close()
+
+
+def test_checkpoint_and_resume_equal_uninterrupted(ctx, tmp_path):
+    """FP64 serving stopped after a few batch steps (every solve in flight
+    checkpointed to its restart pair), then resumed by a new loop from the
+    restart files: every result equals the uninterrupted solve bit for bit
+    (restart values carry 17 digits, and the FP64 stage rebuilds U from
+    FLOW)."""
+    from cfd_gb300 import files, runtime, serving
+    reqs = serving.poisson_requests(5, rate=1000.0, n_range=(8, 12), steps_range=(6, 10), seed=11)
+    cache = {r.rid: serving.make_case(r) for r in reqs}
+    srv = serving.Server(ctx, precision=0, keep_results=True)
+    first = srv.run(reqs, case_cache=cache, checkpoint_dir=tmp_path, checkpoint_every=2, max_batch_steps=4)
+    srv.close()
+    assert first["pending"]                                    # stopped with work left
+    some = [r for r in reqs if (tmp_path / f"req_{r.rid}").exists()]
+    assert some and files.read_restart(tmp_path / f"req_{some[0].rid}", cache[some[0].rid].sd_node) is not None
+    left = [r for r in reqs if r.rid in first["pending"]]
+    srv = serving.Server(ctx, precision=0, keep_results=True)
+    second = srv.run(left, case_cache=cache, checkpoint_dir=tmp_path, checkpoint_every=2)
+    srv.close()
+    assert second["pending"] == [] and second["requests"] == len(left)
+    results = {c.rid: c.flow for c in first["completed"] + second["completed"]}
+    assert set(results) == {r.rid for r in reqs}
+    for r in reqs:
+        alone = runtime.Batch(ctx, 0)
+        s = alone.add(cache[r.rid])
+        alone.step(r.steps)
+        assert np.array_equal(alone.get_flow(s)[1:], results[r.rid][1:]), r.rid
+        alone.close()
