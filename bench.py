@@ -77,6 +77,8 @@ def parse_args(argv=None):
     p.add_argument("--no-mixed", action="store_true")
     p.add_argument("--batch-count", type=int, default=64, help="instances of the batched workload (0 = skip)")
     p.add_argument("--batch-steps", type=int, default=20)
+    p.add_argument("--batch-forms", default="fp64,mixed", help="forms of the batched leg (fp64, mixed or both)")
+    p.add_argument("--batch-tile", type=int, default=0, help="tile size of the batched leg (0 = tuned)")
     p.add_argument("--serve-requests", type=int, default=24, help="requests of the serving workload (0 = skip)")
     p.add_argument("--serve-fp64", action="store_true", help="also serve the stream with the FP64 form")
     p.add_argument("--diag-steps", type=int, default=200,
@@ -427,10 +429,15 @@ def bench_batched(ctx, torch, stream, args):
         return e0.elapsed_time(e1) / 1e3
 
     u_ref = None
-    for prec, steps in ((0, max(1, args.batch_steps // 5)), (1, args.batch_steps)):
+    forms = [f.strip() for f in args.batch_forms.split(",")]
+    runs = [(p, st) for p, st, f in ((0, max(1, args.batch_steps // 5), "fp64"), (1, args.batch_steps, "mixed"))
+            if f in forms]
+    for prec, steps in runs:
         b = runtime.Batch(ctx, prec)
         slots = [b.add(c) for c in cs]
-        if prec == 1:
+        if args.batch_tile:
+            b.set_tiling(args.batch_tile)
+        elif prec == 1:
             b.tune(1)
         b.step(1)
         secs = timed(b, steps)
@@ -443,6 +450,8 @@ def bench_batched(ctx, torch, stream, args):
             u_ref = [b.get_u0(s)[1:] for s in slots]
             ref_steps = 1 + steps
         b.close()
+    if u_ref is None or "mixed" not in out:
+        return out
     # mixed after the same number of steps as the FP64 reference
     b = runtime.Batch(ctx, 1)
     slots = [b.add(c) for c in cs]
@@ -524,8 +533,10 @@ def bench_naca(ctx, torch, stream, args):
         torch.cuda.synchronize()
         secs = e0.elapsed_time(e1) / 1e3
         res[prec] = s.get_flow()[1:N + 1]
+        prof = [s.profile_stage(j, case.dt) for j in range(3)]   # one more step, per-kernel times
         s.close()
-        out["mixed" if prec else "fp64"] = {"value": N * steps / secs, "unit": UNIT, "ms_per_step": 1e3 * secs / steps}
+        out["mixed" if prec else "fp64"] = {"value": N * steps / secs, "unit": UNIT, "ms_per_step": 1e3 * secs / steps,
+                                            "kernels_ms_per_stage": _kernel_table(prof)}
     f = layout.FLOW
     for name in ("rho", "p"):
         a, b = res[1][:, f[name]], res[0][:, f[name]]

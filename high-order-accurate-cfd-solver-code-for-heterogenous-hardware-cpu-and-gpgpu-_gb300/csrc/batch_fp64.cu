@@ -9,6 +9,7 @@ namespace cfd {
 namespace {
 
 struct Ops {
+    static constexpr int kMinBlocks = 1;
     static __device__ __forceinline__ void prep(const LatView &g, int n, int q) { ex::prep_node(g, n, q); }
     static __device__ __forceinline__ void visc(const LatView &g, int n, int q) { ex::visc_node(g, n, q); }
     static __device__ __forceinline__ void mu(const LatView &g, int n, int q) { ex::mu_node(g, n, q); }

@@ -71,9 +71,13 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned nblocks, un
     return s_ok != 0;
 }
 
+// Blocks of up to 256 threads (the tile sizes 64, 128, 256); Ops::kMinBlocks
+// bounds the registers so that many blocks stay resident (the mixed form is
+// latency bound; the FP64 form keeps its registers).
 template <class Ops>
-__global__ void k_batch_stage(const LatView *__restrict__ views, const BatchTile *__restrict__ tiles, int ntiles,
-                              int jst, unsigned *bar, unsigned *gflags, unsigned long long limit_ns)
+__global__ void __launch_bounds__(256, Ops::kMinBlocks)
+k_batch_stage(const LatView *__restrict__ views, const BatchTile *__restrict__ tiles, int ntiles, int jst,
+              unsigned *bar, unsigned *gflags, unsigned long long limit_ns)
 {
     const int items = 4 * ntiles;
     for (int w = blockIdx.x; w < items; w += gridDim.x) {

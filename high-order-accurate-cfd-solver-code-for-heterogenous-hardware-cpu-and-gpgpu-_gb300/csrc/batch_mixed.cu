@@ -8,7 +8,12 @@
 namespace cfd {
 namespace {
 
+#ifndef CFD_MBATCH_MIN_BLOCKS
+#define CFD_MBATCH_MIN_BLOCKS 3
+#endif
+
 struct Ops {
+    static constexpr int kMinBlocks = CFD_MBATCH_MIN_BLOCKS;
     static __device__ __forceinline__ void prep(const LatView &g, int n, int q) { mx::init_node(g, n, q); }
     static __device__ __forceinline__ void visc(const LatView &g, int n, int q) { mx::visc_node<false>(g, n, q); }
     static __device__ __forceinline__ void mu(const LatView &g, int n, int q) { mx::mu_node(g, n, q); }

@@ -38,8 +38,12 @@ __global__ void __launch_bounds__(256) k_prep_m(LatView g, int src, int dst)
     if (n < g.N) mx::prep_node(g, n, src, dst);
 }
 
+#ifndef CFD_MVISC_MIN_BLOCKS
+#define CFD_MVISC_MIN_BLOCKS 4
+#endif
+
 template <bool LOC>
-__global__ void __launch_bounds__(256) k_visc_m(LatView g, int q)
+__global__ void __launch_bounds__(256, CFD_MVISC_MIN_BLOCKS) k_visc_m(LatView g, int q)
 {
     const int n = node_id();
     if (n < g.N) mx::visc_node<LOC>(g, n, q);
