@@ -266,16 +266,26 @@ int mixed_stage(const StructuredLaunch &S, int jst, double dt, double *Lout, cud
         mark();
     }
     const bool loc = g.loc8 != nullptr;   // lattice with ghost layers and loc codes
+    // The viscous pass and the face passes are independent (the update reads
+    // both): without event timing the viscous pass runs on the side stream,
+    // concurrently with the faces.
+    const bool side = S.side && !ev;
+    cudaStream_t sv = side ? S.side : st;
+    if (side) {
+        cudaEventRecord(S.fork, st);
+        cudaStreamWaitEvent(sv, S.fork, 0);
+    }
     if (S.P.viscous) {
         if (loc)
-            k_visc_m<true><<<nb256, 256, 0, st>>>(g, jst);
+            k_visc_m<true><<<nb256, 256, 0, sv>>>(g, jst);
         else
-            k_visc_m<false><<<nb256, 256, 0, st>>>(g, jst);
+            k_visc_m<false><<<nb256, 256, 0, sv>>>(g, jst);
         name("viscous");
     } else {
-        k_mu_m<<<nb256, 256, 0, st>>>(g, jst);
+        k_mu_m<<<nb256, 256, 0, sv>>>(g, jst);
         name("mu_only");
     }
+    if (side) cudaEventRecord(S.join, sv);
     mark();
     launch_face_tile<0>(g, st);
     name("face_i");
@@ -286,6 +296,7 @@ int mixed_stage(const StructuredLaunch &S, int jst, double dt, double *Lout, cud
     launch_face_tile<2>(g, st);
     name("face_k");
     mark();
+    if (side) cudaStreamWaitEvent(st, S.join, 0);
     if (loc)
         k_update_m<true><<<nb256, 256, 0, st>>>(g, jst);
     else

@@ -167,6 +167,10 @@ cfd_status_t create_structured(cfd_solver *s, const cfd_geometry_t *g)
     if (s->mixed) {
         mixed_geometry(S);
         s->ctx->launches += kMixedGeometryLaunches;
+        if (cudaStreamCreateWithFlags(&S.side, cudaStreamNonBlocking) != cudaSuccess
+            || cudaEventCreateWithFlags(&S.fork, cudaEventDisableTiming) != cudaSuccess
+            || cudaEventCreateWithFlags(&S.join, cudaEventDisableTiming) != cudaSuccess)
+            return cuda_fail(s->ctx, cudaGetLastError(), "solver side stream");
     }
     cudaError_t e = cudaStreamSynchronize(S.stream);   // host vectors go out of scope
     if (e != cudaSuccess) return cuda_fail(s->ctx, e, "solver create sync");
@@ -273,6 +277,12 @@ cfd_status_t cfd_solver_destroy(cfd_solver_t *s)
     if (!s) return CFD_EINVAL;
     use_device(s->ctx);
     cudaStreamSynchronize(s->ctx->stream);
+    if (s->S.side) {
+        cudaStreamSynchronize(s->S.side);
+        cudaStreamDestroy(s->S.side);
+    }
+    if (s->S.fork) cudaEventDestroy(s->S.fork);
+    if (s->S.join) cudaEventDestroy(s->S.join);
     bc_free(s->bc);
     for (void *p : s->allocs) cudaFree(p);
     delete s;

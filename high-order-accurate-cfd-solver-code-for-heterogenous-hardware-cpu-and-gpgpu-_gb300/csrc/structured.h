@@ -37,6 +37,10 @@ struct StructuredLaunch {
     float *node32 = nullptr;   // [11][N] node metrics, det, det^(-1/3)
     float *idet32 = nullptr;   // [2][N] 1/det hi, lo
     float *prim32 = nullptr;   // [9][N] FLOW in FP32
+    // mixed form: side stream and fork/join events for the viscous pass
+    // (null: everything on `stream`)
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     // lattice shape beyond a plain periodic box (LatView::per, loc8, row_of)
     int per = 7;
     const unsigned char *loc8 = nullptr;
