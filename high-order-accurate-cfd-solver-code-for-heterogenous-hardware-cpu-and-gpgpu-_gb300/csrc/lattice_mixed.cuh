@@ -113,9 +113,10 @@ __device__ __forceinline__ void store_state(const LatView &g, int q, int n, cons
     }
 }
 
-// U_Q of the next stage from the state Un (= det * Q): the FP32 primitives
-// (prim32 rho,u,v,w,e,p,t,a), and the inputs of the face stage: Q, the Roe
-// inputs (u, v, w, sqrt(rho), H) and the contravariant node fluxes.
+// U_Q of the next stage from the state Un (= det * Q): the inputs of the
+// face stage -- Q, the Roe inputs (u, v, w, sqrt(rho), H), the contravariant
+// node fluxes -- and the pressure (prim32); the viscous pass takes rho from
+// Q and u, v, w from the Roe inputs, and FLOW leaves through flow_out_node.
 __device__ __forceinline__ void derive(const LatView &g, int n, const dfl Un[5])
 {
     const int N = g.N;
@@ -125,22 +126,12 @@ __device__ __forceinline__ void derive(const LatView &g, int n, const dfl Un[5])
     const float u = df_div_f(Un[1], Un[0], r0), v = df_div_f(Un[2], Un[0], r0), w = df_div_f(Un[3], Un[0], r0);
     const float ke = 0.5f * (u * u + v * v + w * w);
     const dfl q4 = df_div(Un[4], Un[0], r0);   // E / rho
-    const dfl e2 = df_add(q4, {-ke, 0.0f});
-    const float e = e2.h + e2.l;
+    const dfl e2 = df_add(q4, {-ke, 0.0f});      // internal energy e
     const dfl rho2 = df_mul(Un[0], idet);
     const float p = df_mul_f(df_mul(rho2, e2), {kGm1H, kGm1L});
     const float irho = 1.0f / rho;
     const float pr = p * irho;
-    const float mach = (float)g.P.mach;
-    float *F = g.prim32;
-    F[LF_RHO * N + n] = rho;
-    F[LF_U * N + n] = u;
-    F[LF_V * N + n] = v;
-    F[LF_W * N + n] = w;
-    F[LF_E * N + n] = e;
-    F[LF_P * N + n] = p;
-    F[LF_T * N + n] = (1.4f * mach * mach) * pr;
-    F[LF_A * N + n] = sqrtf(1.4f * pr);
+    g.prim32[LF_P * N + n] = p;
     if (!(isfinite(rho) && isfinite(u) && isfinite(v) && isfinite(w) && isfinite(p))) atomicOr(g.flags, 2u);
     const float E = df_mul_f(Un[4], idet);
     g.Q32[0 * N + n] = rho;
@@ -271,8 +262,7 @@ __device__ __forceinline__ void visc_node(const LatView &g, int n, int q)
     float m[9];
 #pragma unroll
     for (int c = 0; c < 9; ++c) m[c] = g.node32[c * N + n];
-    const float *F = g.prim32;
-    const float prim[5] = {F[LF_RHO * N + n], F[LF_U * N + n], F[LF_V * N + n], F[LF_W * N + n], F[LF_P * N + n]};
+    const float prim[5] = {g.Q32[n], g.R32[n], g.R32[N + n], g.R32[2 * N + n], g.prim32[LF_P * N + n]};
     float Fv[5], Ev[5], Gv[5], mu;
     viscous_node_flux<float>(dU, Ui, m, g.node32[9 * N + n], g.node32[10 * N + n], prim, KS, g.P, Fv, Ev, Gv, mu);
 #pragma unroll
