@@ -43,8 +43,14 @@ struct LatView {
     // fully periodic lattice.
     int per;
     const unsigned char *loc8;
+    // bit d: some owned node has a ghost within two nodes along d, so the
+    // loc-code branches matter there; along the other directions every
+    // branch of the reference is the central one
+    int locdirs;
     const int *row_of;         // node n -> reference row (null: row n + 1)
 };
+
+__device__ __forceinline__ bool lat_locdir(const LatView &g, int d) { return g.loc8 && ((g.locdirs >> d) & 1); }
 
 constexpr unsigned char kLocGhost = 100;
 

@@ -87,7 +87,7 @@ __device__ __forceinline__ void visc_node(const LatView &g, int n, int q)
         if (ghost) {
 #pragma unroll
             for (int c = 0; c < 5; ++c) dU[d][c] = 0.0;
-        } else if (!g.loc8) {
+        } else if (!lat_locdir(g, d)) {
 #pragma unroll
             for (int c = 0; c < 5; ++c)
                 dU[d][c] = central4(Uj[c * N + m2], Uj[c * N + m1], Uj[c * N + p1], Uj[c * N + p2]);
@@ -190,7 +190,7 @@ __device__ __forceinline__ void update_node(const LatView &g, int n, int jst, bo
         const int m1 = lat_step(g, i, j, k, d, -1);
 #pragma unroll
         for (int c = 0; c < 5; ++c) dflux[d][c] = g.Fh[(d * 5 + c) * N + n] - g.Fh[(d * 5 + c) * N + m1];
-        if (g.P.viscous && g.loc8) {
+        if (g.P.viscous && lat_locdir(g, d)) {
             int s[7], L[7];
             loc_line(g, i, j, k, d, s, L);
             const double *Vd = g.V + (size_t)d * 5 * N;

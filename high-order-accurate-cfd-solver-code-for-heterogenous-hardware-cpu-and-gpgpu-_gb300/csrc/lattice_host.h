@@ -32,6 +32,7 @@ inline int nb_of(const cfd_grid_t &g, int slot)
 struct LatticeMap {
     int ni = 0, nj = 0, nk = 0;
     int per = 7;                        // bit d: direction d periodic
+    int locdirs = 0;                    // bit d: an owned node has a ghost within 2 along d
     std::vector<int32_t> row_of;        // n -> reference row
     std::vector<int32_t> n_of_row;      // reference row -> n (-1: not a lattice node)
     std::vector<unsigned char> loc;     // loc code of node n (non-periodic lattices)
@@ -144,6 +145,20 @@ inline bool map_lattice(const cfd_geometry_t *g, LatticeMap &m)
                     for (int d = 0; d < 3; ++d)
                         if (!(per >> d & 1) && (c[d] < 3 || c[d] > m.extent(d) - 4)) return false;
             }
+    if (ghosted)
+        for (int k = 0; k < m.nk; ++k)
+            for (int j = 0; j < m.nj; ++j)
+                for (int i = 0; i < m.ni; ++i) {
+                    const int n = i + m.ni * (j + m.nj * k);
+                    if (m.loc[n] == 100) continue;
+                    const int c[3] = {i, j, k};
+                    for (int d = 0; d < 3; ++d)
+                        for (int o : {-2, -1, 1, 2}) {
+                            int cc[3] = {i, j, k};
+                            cc[d] = step(c[d], o, d);
+                            if (m.loc[cc[0] + m.ni * (cc[1] + m.nj * cc[2])] == 100) m.locdirs |= 1 << d;
+                        }
+                }
     return true;
 }
 

@@ -228,7 +228,7 @@ __device__ __forceinline__ void visc_node(const LatView &g, int n, int q)
         if (ghost) {
 #pragma unroll
             for (int c = 0; c < 5; ++c) dU[d][c] = 0.0f;
-        } else if (!LOC) {
+        } else if (!LOC || !lat_locdir(g, d)) {
 #pragma unroll
             for (int c = 0; c < 5; ++c) {
                 const float *H = W + c * N, *L = W + (5 + c) * N;
@@ -356,7 +356,7 @@ __device__ __forceinline__ void update_node(const LatView &g, int n, int jst)
         const int m1 = lat_step(g, i, j, k, d, -1);
 #pragma unroll
         for (int c = 0; c < 5; ++c) Lf[c] += g.Fh32[(d * 5 + c) * N + n] - g.Fh32[(d * 5 + c) * N + m1];
-        if (LOC && g.P.viscous) {
+        if (LOC && g.P.viscous && lat_locdir(g, d)) {
             int s[7], L7[7];
 #pragma unroll
             for (int o = 0; o < 7; ++o) {

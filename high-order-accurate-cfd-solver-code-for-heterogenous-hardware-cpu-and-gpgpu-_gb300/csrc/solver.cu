@@ -108,6 +108,7 @@ cfd_status_t create_structured(cfd_solver *s, const cfd_geometry_t *g)
     const size_t N = (size_t)s->ni * s->nj * s->nk;
     StructuredLaunch &S = s->S;
     S.per = s->map.per;
+    S.locdirs = s->map.locdirs;
     S.ni = s->ni;
     S.nj = s->nj;
     S.nk = s->nk;

@@ -44,6 +44,7 @@ struct StructuredLaunch {
     // lattice shape beyond a plain periodic box (LatView::per, loc8, row_of)
     int per = 7;
     const unsigned char *loc8 = nullptr;
+    int locdirs = 0;
     const int *row_of = nullptr;
 };
 
@@ -107,6 +108,7 @@ inline LatView make_view(const StructuredLaunch &S, double dt, double *Lout)
     g.Lout = Lout;
     g.per = S.per;
     g.loc8 = S.loc8;
+    g.locdirs = S.locdirs;
     g.row_of = S.row_of;
     return g;
 }
