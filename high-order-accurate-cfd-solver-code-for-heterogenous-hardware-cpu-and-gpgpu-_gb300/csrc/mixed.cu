@@ -163,15 +163,18 @@ __global__ void __launch_bounds__(256) k_update_m(LatView g, int jst)
     if (n < g.N) mx::update_node<LOC>(g, n, jst);
 }
 
+// one thread per (entry, target node); a list whose entries touch each
+// other's rows runs in list order on one thread
 __global__ void k_bc_m(LatView g, const BcEntry *__restrict__ E, int n, int type, int q, double mach, int sequential)
 {
     if (sequential) {
         if (blockIdx.x == 0 && threadIdx.x == 0)
-            for (int e = 0; e < n; ++e) mx::bc_entry(g, type, E[e], q, mach);
+            for (int e = 0; e < n; ++e)
+                for (int m = 0; m < 4; ++m) mx::bc_target(g, type, E[e], m, q, mach);
         return;
     }
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e < n) mx::bc_entry(g, type, E[e], q, mach);
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < 4 * n) mx::bc_target(g, type, E[t >> 2], t & 3, q, mach);
 }
 
 __global__ void k_flow_out_m(LatView g, int q)
@@ -226,7 +229,7 @@ void bc_apply_mixed(cudaStream_t st, const BcDevice &bc, const LatView &g, int q
 {
     for (int t = 0; t < BC_NTYPES; ++t) {
         if (bc.n[t] == 0) continue;
-        const unsigned blocks = bc.seq[t] ? 1u : blocks_for(bc.n[t], 128);
+        const unsigned blocks = bc.seq[t] ? 1u : blocks_for(4LL * bc.n[t], 128);
         k_bc_m<<<blocks, bc.seq[t] ? 1 : 128, 0, st>>>(g, bc.d[t], bc.n[t], t, q, mach, bc.seq[t]);
     }
 }
