@@ -9,7 +9,9 @@
 // arithmetic on the FP32 pipe.
 // FP32: characteristic projection, WENO5, LLF, face and node fluxes, the
 // viscous/SGS fluxes, the right-hand side sum, and the primitives derived
-// from the state each stage (rounded once from hi/lo quotients).
+// from the state each stage (rounded once from hi/lo quotients).  On a
+// lattice with ghost layers the same loc-code branches as the FP64 form,
+// and the boundary routine on the hi/lo state (bc_target).
 // FP64 only at the boundary: FLOW in (kPrepFromFlow) and FLOW/U out.
 // Include only from translation units compiled with FMA contraction and
 // approximate FP32 division/square root; the hi/lo routines below use

@@ -1,8 +1,8 @@
-// structured.cu -- face-based RHS kernels for a periodic (i,j,k) lattice,
-// FP64 form.
+// structured.cu -- face-based RHS kernels for an (i,j,k) lattice, FP64 form.
 //
-// When the reference's neighbour table is a periodic lattice (detected by the
-// solver at create time), the same arithmetic runs on a structure-of-arrays
+// When the reference's neighbour table is a lattice -- periodic, or padded by
+// ghost layers in non-periodic directions (detected by the solver at create
+// time, lattice_host.h) -- the same arithmetic runs on a structure-of-arrays
 // layout with index arithmetic instead of neighbour chains, and every face is
 // computed once.  The reference computes each face twice: as i+1/2 of node i
 // and as i-1/2 of node i+1, from identical inputs (the face metric and face

@@ -13,13 +13,13 @@ struct StructuredLaunch {
     int ni, nj, nk;
     cudaStream_t stream;
     Phys P;
-    int mixed;                 // 1: characteristic/WENO/LLF in FP32
+    int mixed;                 // 1: the mixed-precision form (mixed.cu)
     const double *m9;          // [9][N]   node metrics
     const double *det;         // [N]
     const double *fm;          // [3 dir][3 comp][N] metric of face n+1/2
     const double *fdet;        // [3][N]   det of face n+1/2
-    double *prim9;             // [9][N]   FLOW fields u,v,w,p,t,rho,mu,a,e
-    double *U[3];              // [5][N]   U0, U1, U2
+    double *prim9;             // [9][N]   FLOW fields u,v,w,p,t,rho,mu,a,e (mixed: in/out only)
+    double *U[3];              // [5][N]   U0, U1, U2 (mixed: hi/lo FP32 pairs in the same bytes)
     double *Q;                 // [5][N]
     double *FEG;               // [3][5][N] contravariant node fluxes
     double *V;                 // [3][5][N] viscous fluxes
@@ -36,12 +36,13 @@ struct StructuredLaunch {
     float *fdet32 = nullptr;   // [3][N]
     float *node32 = nullptr;   // [11][N] node metrics, det, det^(-1/3)
     float *idet32 = nullptr;   // [2][N] 1/det hi, lo
-    float *prim32 = nullptr;   // [9][N] FLOW in FP32
+    float *prim32 = nullptr;   // [9][N] FP32 pressure (LF_P) and mu (LF_MU) of the stage
     // mixed form: side stream and fork/join events for the viscous pass
     // (null: everything on `stream`)
     cudaStream_t side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
-    // lattice shape beyond a plain periodic box (LatView::per, loc8, row_of)
+    // lattice shape beyond a plain periodic box (LatView::per, loc8, locdirs,
+    // row_of)
     int per = 7;
     const unsigned char *loc8 = nullptr;
     int locdirs = 0;

@@ -194,3 +194,27 @@ def test_duct_edges_on_the_lattice_path(ctx, oracle_mod):
     a = layout.FLOW["a"]
     stale = np.abs(out["mixed"][own, a] - out["lattice"][own, a]) > 1e-6 * np.abs(out["lattice"][own, a])
     assert set(c.arrays["grid"]["loc"][1:c.sd_node + 1][stale].tolist()) <= set(range(7, 27))
+
+
+def test_channel_stages_out_of_order_and_profiled(ctx):
+    """Stages called out of the usual order (each stage's U_Q then comes from
+    the current state, copied into the stage's slot, ghosts included) and a
+    profiled stage (the boundary routine is one timed entry): the mixed form
+    tracks the FP64 form through the same calls."""
+    from cfd_gb300 import layout, runtime
+    c = _channel()
+    seq = (0, 0, 1, 2, 1, 2, 0)
+    out = {}
+    for prec in (0, 1):
+        s = runtime.Solver(ctx, c, precision=prec)
+        s.set_flow(c.arrays["flow"])
+        for j in seq:
+            s.stage(j, c.dt, want_L=False)
+        names = [n for n, _ in s.profile_stage(1, c.dt)]
+        assert names[-1] == "boundary"
+        out[prec] = s.get_flow()
+        s.close()
+    own = slice(1, c.sd_node + 1)
+    cols = [layout.FLOW[k] for k in ("rho", "u", "v", "w", "p")]
+    assert np.isfinite(out[1][own]).all()
+    assert rel_l2(out[1][own][:, cols], out[0][own][:, cols]) <= 1e-6
