@@ -75,6 +75,8 @@ def parse_args(argv=None):
     p.add_argument("--cpu-steps", type=int, default=1, help="full steps timed for the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-mixed", action="store_true")
+    p.add_argument("--dropin-steps", type=int, default=5,
+                   help="steps timed through the drop-in entry points (0 = skip)")
     p.add_argument("--batch-count", type=int, default=64, help="instances of the batched workload (0 = skip)")
     p.add_argument("--batch-steps", type=int, default=20)
     p.add_argument("--batch-forms", default="fp64,mixed", help="forms of the batched leg (fp64, mixed or both)")
@@ -360,6 +362,8 @@ def gpu_arm(args):
     }
     s64.close()
 
+    if args.dropin_steps > 0:
+        line["dropin"] = bench_dropin(ctx, torch, stream, case, args)
     if args.diag_steps > 0 and args.config.startswith("tgv"):
         line["tgv_diagnostics"] = bench_diagnostics(ctx, case, args)
     if args.batch_count > 0:
@@ -566,6 +570,55 @@ def bench_serving(ctx, args):
             "latency_p99_s": r["latency_p99_s"], "latency_max_s": r["latency_max_s"], "makespan_s": r["makespan_s"],
             "batch_steps": r["batch_steps"], "completed": r["requests"]}
     return out
+
+
+def bench_dropin(ctx, torch, stream, case, args):
+    """The FP64 step through the three drop-in entry points on the
+    reference's AoS buffers (what a reference host loop binds): U_Q ->
+    Viscous -> Weno per stage.  Device-resident rate, and end to end with
+    FLOW written from and read back to pinned host memory every step."""
+    import numpy as np
+    steps = max(1, min(args.steps, args.dropin_steps))
+    N = case.sd_node
+    dev = ctx.upload_case(case.arrays)
+    flow0 = case.arrays["flow"]
+
+    def run_step():
+        for j in range(3):
+            ctx.stage(dev, case.g_node, case.sd_node, case.params, j, case.dt)
+
+    for _ in range(2):
+        run_step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = ctx.launch_count
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+    for _ in range(steps):
+        run_step()
+    with torch.cuda.stream(stream):
+        e1.record(stream)
+    torch.cuda.synchronize()
+    secs = e0.elapsed_time(e1) / 1e3
+    launches = ctx.launch_count - launches0
+    host_in = torch.empty(flow0.shape, dtype=torch.float64, pin_memory=True).numpy()
+    host_out = torch.empty(flow0.shape, dtype=torch.float64, pin_memory=True).numpy()
+    host_in[...] = flow0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        ctx.write(dev["flow"], host_in)
+        run_step()
+        ctx.read(host_out, dev["flow"])
+        host_in, host_out = host_out, host_in
+    e2e_secs = time.perf_counter() - t0
+    for p in dev.values():
+        ctx.free(p)
+    return {"value": N * steps / secs, "unit": UNIT, "ms_per_step": 1e3 * secs / steps, "steps": steps,
+            "gpu_launches": launches,
+            "e2e": {"value": N * steps / e2e_secs, "unit": UNIT, "h2d_bytes_per_step": int(host_in.nbytes),
+                    "d2h_bytes_per_step": int(host_out.nbytes)},
+            "path": "cfd_uq / cfd_viscous / cfd_weno on the reference AoS buffers (neighbour-table gathers)"}
 
 
 def _kernel_table(prof) -> dict:

@@ -68,6 +68,7 @@ PROTOTYPES = {
     "cfd_ctx_set_async": (C.c_int, [_vp, C.c_int]),
     "cfd_ctx_synchronize": (C.c_int, [_vp]),
     "cfd_ctx_set_rows": (C.c_int, [_vp, _i32]),
+    "cfd_ctx_set_face_reuse": (C.c_int, [_vp, C.c_int]),
     "cfd_ctx_launch_count": (C.c_uint64, [_vp]),
     "cfd_buffer_alloc": (C.c_int, [_vp, C.c_size_t, C.POINTER(_vp)]),
     "cfd_buffer_free": (C.c_int, [_vp, _vp]),

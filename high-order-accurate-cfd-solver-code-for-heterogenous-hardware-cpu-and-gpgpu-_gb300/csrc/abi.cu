@@ -160,6 +160,7 @@ cfd_status_t cfd_ctx_destroy(cfd_ctx_t *ctx)
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     if (ctx->d_flags) cudaFree(ctx->d_flags);
     if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
+    if (ctx->d_face) cudaFree(ctx->d_face);
     delete ctx;
     return CFD_OK;
 }
@@ -195,6 +196,31 @@ cfd_status_t cfd_ctx_set_rows(cfd_ctx_t *ctx, int32_t n_rows)
 {
     if (!ctx || n_rows <= 0) return fail(ctx, CFD_EINVAL, "n_rows must be positive");
     ctx->n_rows = n_rows;
+    // cfd_weno's face scratch; without it (no memory) cfd_weno evaluates
+    // both faces per row, with the same results
+    if (ctx->face_rows < n_rows) {
+        cfd_status_t s = use_device(ctx);
+        if (s != CFD_OK) return s;
+        if (ctx->d_face) {
+            cudaStreamSynchronize(ctx->stream);
+            cudaFree(ctx->d_face);
+        }
+        ctx->d_face = nullptr;
+        ctx->face_rows = 0;
+        if (cudaMalloc(&ctx->d_face, (size_t)n_rows * 15 * sizeof(double)) == cudaSuccess)
+            ctx->face_rows = n_rows;
+        else {
+            cudaGetLastError();
+            ctx->d_face = nullptr;
+        }
+    }
+    return CFD_OK;
+}
+
+cfd_status_t cfd_ctx_set_face_reuse(cfd_ctx_t *ctx, int on)
+{
+    if (!ctx) return CFD_EINVAL;
+    ctx->face_reuse = on != 0;
     return CFD_OK;
 }
 
@@ -299,7 +325,8 @@ cfd_status_t cfd_weno(cfd_ctx_t *ctx, int32_t j, double Mach, double del_t, cons
                 (double *)U2, (const int *)Grid_P, (const double *)Q_C, (const double *)metric,
                 (const double *)ROE_AVER, (const double *)Fv, (const double *)Ev, (const double *)Gv,
                 (const double *)F, (const double *)E, (const double *)G, (double *)FLOW, n_items, ctx->n_rows,
-                ctx->d_flags, (double *)L_out);
+                ctx->d_flags, (double *)L_out, ctx->face_reuse ? ctx->d_face : nullptr, ctx->face_rows);
+    ctx->launches += weno_launches(ctx->face_reuse ? ctx->d_face : nullptr, ctx->face_rows, n_items) - 1;
     return after_launch(ctx, "cfd_weno launch");
 }
 

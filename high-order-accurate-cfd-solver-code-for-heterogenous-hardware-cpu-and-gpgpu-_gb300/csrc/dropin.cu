@@ -11,6 +11,15 @@
 // Arithmetic: the exact FP64 layer (physics_exact.cuh); this file is
 // compiled with --fmad=false so that results follow the reference's
 // evaluation order.
+//
+// Weno evaluates both faces of each direction at every row, so every
+// interior face is computed twice from identical inputs (as row n's +1/2
+// face and as row n+1's -1/2 face).  With a scratch buffer the launch is
+// split: k_weno_plus computes each row's +1/2 faces once, and k_weno<true>
+// takes a row's -1/2 face from its minus neighbour's +1/2 face wherever
+// every input of the two evaluations is bit-identical (stencil rows, face
+// metric, face det, Roe state); elsewhere it computes the face itself.
+// The results are the same bits either way.
 #include "internal.h"
 #include "physics_exact.cuh"
 
@@ -169,8 +178,106 @@ __global__ void __launch_bounds__(128) k_viscous(Phys P, const double *__restric
 }
 
 // ----------------------------------------------------------------- Weno --
+// Corrected face flux of row gid, direction d, side s (0: +1/2, 1: -1/2)
+// from the row's own face data (metric block 1+2d+s, DETERM 2d+s, ROE
+// block d+3s) over the stencil rows st[0..5] (offsets -2..3 for s = 0,
+// -3..2 for s = 1), Weno.cl:336-3058.
+__device__ __forceinline__ void face_side(const Phys &P, int gid, int d, int s, const int st[6],
+                                          const double *__restrict__ deter, const double *__restrict__ Q,
+                                          const double *__restrict__ metric, const double *__restrict__ roe,
+                                          const double *__restrict__ NF, double Fh[5])
+{
+    const double *fm = metric + 63 * (size_t)gid + 9 * (1 + 2 * d + s) + 3 * d;
+    const double det_f = deter[6 * (size_t)gid + 2 * d + s];
+    const double *ra = roe + 36 * (size_t)gid + 6 * (d + 3 * s);
+    const double rstate[5] = {ra[0], ra[1], ra[2], ra[4], ra[5]};
+    double pts[6][5], nfv[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+#pragma unroll
+        for (int c = 0; c < 5; ++c) pts[k][c] = Q[5 * (size_t)st[k] + c];
+    double Fhat[5];
+    ex::face_flux(pts, fm[0], fm[1], fm[2], det_f, rstate, P.eps, Fhat);
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) nfv[k] = NF[5 * (size_t)st[k] + c];
+        Fh[c] = ex::corrected(Fhat[c], nfv);
+    }
+}
+
+// Rows of offsets -2..3 of row n along d (chained neighbours); false if the
+// chain leaves [0, n_rows).
+__device__ __forceinline__ bool plus_line(const int *grid, int n, int n_rows, int d, int st[6])
+{
+    st[2] = n;
+    int m = n, p = n;
+#pragma unroll
+    for (int o = 1; o <= 3; ++o) {
+        p = grid_nb(grid, p, plus_slot(d));
+        if ((unsigned)p >= (unsigned)n_rows) return false;
+        st[2 + o] = p;
+        if (o <= 2) {
+            m = grid_nb(grid, m, minus_slot(d));
+            if ((unsigned)m >= (unsigned)n_rows) return false;
+            st[2 - o] = m;
+        }
+    }
+    return true;
+}
+
+// +1/2 face of every row gid < n_items along d = blockIdx.y whose stencil
+// stays in the table: Fp[(d*5 + c)*ld + gid].
+__global__ void __launch_bounds__(128, 2) k_weno_plus(Phys P, const double *__restrict__ deter,
+                                                       const int *__restrict__ grid, const double *__restrict__ Q,
+                                                       const double *__restrict__ metric,
+                                                       const double *__restrict__ roe, const double *__restrict__ F,
+                                                       const double *__restrict__ E, const double *__restrict__ G,
+                                                       int n_items, int n_rows, double *__restrict__ Fp, long long ld)
+{
+    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int d = blockIdx.y;
+    if (gid >= n_items) return;
+    int st[6];
+    if (!plus_line(grid, gid, n_rows, d, st)) return;
+    double Fh[5];
+    face_side(P, gid, d, 0, st, deter, Q, metric, roe, d == 0 ? F : (d == 1 ? E : G), Fh);
+#pragma unroll
+    for (int c = 0; c < 5; ++c) Fp[(d * 5 + c) * ld + gid] = Fh[c];
+}
+
+__device__ __forceinline__ bool same_bits(double a, double b) { return __double_as_longlong(a) == __double_as_longlong(b); }
+
+// Whether row gid's -1/2 face along d is the +1/2 face k_weno_plus computed
+// for n = its minus neighbour: n < n_items, n's stencil (offsets -2..3)
+// is gid's (offsets -3..2), and the face metric, face det and Roe state
+// are the same bits.
+__device__ __forceinline__ bool minus_face_is_plus_of(const int *grid, int gid, int d, const int idx[7], int n_items,
+                                                      int n_rows, const double *__restrict__ deter,
+                                                      const double *__restrict__ metric,
+                                                      const double *__restrict__ roe)
+{
+    const int n = idx[2];
+    if ((unsigned)n >= (unsigned)n_items) return false;
+    int st[6];
+    if (!plus_line(grid, n, n_rows, d, st)) return false;
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+        if (st[k] != idx[k]) return false;
+    const double *fg = metric + 63 * (size_t)gid + 9 * (2 + 2 * d) + 3 * d;
+    const double *fn = metric + 63 * (size_t)n + 9 * (1 + 2 * d) + 3 * d;
+    if (!same_bits(fg[0], fn[0]) || !same_bits(fg[1], fn[1]) || !same_bits(fg[2], fn[2])) return false;
+    if (!same_bits(deter[6 * (size_t)gid + 2 * d + 1], deter[6 * (size_t)n + 2 * d])) return false;
+    const double *rg = roe + 36 * (size_t)gid + 6 * (d + 3), *rn = roe + 36 * (size_t)n + 6 * d;
+    return same_bits(rg[0], rn[0]) && same_bits(rg[1], rn[1]) && same_bits(rg[2], rn[2]) && same_bits(rg[4], rn[4])
+           && same_bits(rg[5], rn[5]);
+}
+
 // Weno.cl:36-3137: per row, both faces of each direction from the row's own
 // face data (metric blocks, DETERM, ROE_AVERAGING), as the reference does.
+// REUSE: the +1/2 faces come from k_weno_plus (Fp) and the -1/2 faces from
+// the minus neighbour's entry where minus_face_is_plus_of holds.
+template <bool REUSE>
 __global__ void __launch_bounds__(128) k_weno(Phys P, int j, double mach, double dt, const double *__restrict__ deter,
                                               const double *__restrict__ det, double *__restrict__ U0,
                                               double *__restrict__ U1, double *__restrict__ U2,
@@ -180,7 +287,7 @@ __global__ void __launch_bounds__(128) k_weno(Phys P, int j, double mach, double
                                               const double *__restrict__ Gv, const double *__restrict__ F,
                                               const double *__restrict__ E, const double *__restrict__ G,
                                               double *__restrict__ flow, int n_items, int n_rows, unsigned *flags,
-                                              double *__restrict__ L_out)
+                                              double *__restrict__ L_out, const double *__restrict__ Fp, long long ld)
 {
     const int gid = blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= n_items) return;
@@ -195,27 +302,20 @@ __global__ void __launch_bounds__(128) k_weno(Phys P, int j, double mach, double
         const double *NF = d == 0 ? F : (d == 1 ? E : G);
         const double *VF = d == 0 ? Fv : (d == 1 ? Ev : Gv);
         double Fh[2][5];
-#pragma unroll 1
-        for (int s = 0; s < 2; ++s) {
-            // face metric block 1+2d+s, components of direction d
-            const double *fm = metric + 63 * (size_t)gid + 9 * (1 + 2 * d + s) + 3 * d;
-            const double det_f = deter[6 * (size_t)gid + 2 * d + s];
-            const double *ra = roe + 36 * (size_t)gid + 6 * (d + 3 * s);
-            const double rstate[5] = {ra[0], ra[1], ra[2], ra[4], ra[5]};
-            const int base = s == 0 ? 1 : 0;   // stencil rows: offsets -2..3 (plus) or -3..2 (minus)
-            double pts[6][5], nfv[6];
+        if (REUSE) {
 #pragma unroll
-            for (int k = 0; k < 6; ++k)
+            for (int c = 0; c < 5; ++c) Fh[0][c] = Fp[(d * 5 + c) * ld + gid];
+            if (minus_face_is_plus_of(grid, gid, d, idx[d], n_items, n_rows, deter, metric, roe)) {
+                const int n = idx[d][2];
 #pragma unroll
-                for (int c = 0; c < 5; ++c) pts[k][c] = Q[5 * (size_t)idx[d][base + k] + c];
-            double Fhat[5];
-            ex::face_flux(pts, fm[0], fm[1], fm[2], det_f, rstate, P.eps, Fhat);
-#pragma unroll
-            for (int c = 0; c < 5; ++c) {
-#pragma unroll
-                for (int k = 0; k < 6; ++k) nfv[k] = NF[5 * (size_t)idx[d][base + k] + c];
-                Fh[s][c] = ex::corrected(Fhat[c], nfv);
+                for (int c = 0; c < 5; ++c) Fh[1][c] = Fp[(d * 5 + c) * ld + n];
+            } else {
+                face_side(P, gid, d, 1, idx[d], deter, Q, metric, roe, NF, Fh[1]);
             }
+        } else {
+#pragma unroll 1
+            for (int s = 0; s < 2; ++s)   // stencil rows: offsets -2..3 (plus) or -3..2 (minus)
+                face_side(P, gid, d, s, idx[d] + (s == 0 ? 1 : 0), deter, Q, metric, roe, NF, Fh[s]);
         }
         int Lc[7];
 #pragma unroll
@@ -278,10 +378,18 @@ void launch_weno(cudaStream_t st, const Phys &P, int j, double mach, double dt, 
                  const double *det, double *U0, double *U1, double *U2, const int *grid, const double *Q,
                  const double *metric, const double *roe, const double *Fv, const double *Ev, const double *Gv,
                  const double *F, const double *E, const double *G, double *flow, int n_items, int n_rows,
-                 unsigned *flags, double *L_out)
+                 unsigned *flags, double *L_out, double *face_scratch, long long scratch_rows)
 {
-    k_weno<<<blocks_for(n_items, 128), 128, 0, st>>>(P, j, mach, dt, deter, det, U0, U1, U2, grid, Q, metric, roe, Fv,
-                                                     Ev, Gv, F, E, G, flow, n_items, n_rows, flags, L_out);
+    const unsigned nb = blocks_for(n_items, 128);
+    if (face_scratch && scratch_rows >= n_items) {
+        k_weno_plus<<<dim3(nb, 3), 128, 0, st>>>(P, deter, grid, Q, metric, roe, F, E, G, n_items, n_rows,
+                                                 face_scratch, scratch_rows);
+        k_weno<true><<<nb, 128, 0, st>>>(P, j, mach, dt, deter, det, U0, U1, U2, grid, Q, metric, roe, Fv, Ev, Gv, F, E,
+                                         G, flow, n_items, n_rows, flags, L_out, face_scratch, scratch_rows);
+    } else {
+        k_weno<false><<<nb, 128, 0, st>>>(P, j, mach, dt, deter, det, U0, U1, U2, grid, Q, metric, roe, Fv, Ev, Gv, F,
+                                          E, G, flow, n_items, n_rows, flags, L_out, nullptr, 0);
+    }
 }
 
 }  // namespace cfd

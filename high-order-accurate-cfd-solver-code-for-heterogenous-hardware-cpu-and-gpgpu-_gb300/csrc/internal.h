@@ -29,6 +29,11 @@ struct cfd_ctx {
     unsigned *h_flags = nullptr;   // pinned mirror
     uint64_t launches = 0;
     std::string last_error;
+    // cfd_weno's face scratch (15 doubles per row, allocated by
+    // cfd_ctx_set_rows; null: each row evaluates both faces itself)
+    double *d_face = nullptr;
+    long long face_rows = 0;
+    bool face_reuse = true;
 };
 
 namespace cfd {
@@ -59,6 +64,12 @@ void launch_weno(cudaStream_t st, const Phys &P, int j, double mach, double dt, 
                  const double *det, double *U0, double *U1, double *U2, const int *grid, const double *Q,
                  const double *metric, const double *roe, const double *Fv, const double *Ev, const double *Gv,
                  const double *F, const double *E, const double *G, double *flow, int n_items, int n_rows,
-                 unsigned *flags, double *L_out);
+                 unsigned *flags, double *L_out, double *face_scratch, long long scratch_rows);
+// Kernels one launch_weno issues: 2 with a face scratch of >= n_items rows
+// (15 doubles per row), else 1.
+inline int weno_launches(const double *face_scratch, long long scratch_rows, int n_items)
+{
+    return face_scratch && scratch_rows >= n_items ? 2 : 1;
+}
 
 }  // namespace cfd

@@ -92,6 +92,11 @@ class Context:
     def set_rows(self, n_rows: int):
         self.check(self.lib.cfd_ctx_set_rows(self.h, int(n_rows)), "cfd_ctx_set_rows")
 
+    def set_face_reuse(self, on: bool):
+        """cfd_weno: share each interior face between its two rows (default)
+        or evaluate both faces at every row as the reference does."""
+        self.check(self.lib.cfd_ctx_set_face_reuse(self.h, 1 if on else 0), "cfd_ctx_set_face_reuse")
+
     def set_async(self, on: bool):
         self.check(self.lib.cfd_ctx_set_async(self.h, 1 if on else 0), "cfd_ctx_set_async")
 

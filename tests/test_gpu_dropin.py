@@ -1,7 +1,8 @@
 """Drop-in entry points (cfd_uq, cfd_viscous, cfd_weno) on the GPU against
 the reference's golden vectors and the oracle.  Tolerance: relative L2
-<= 1e-12 (FP64; the GPU contracts a*b+c into FMA and its libm differs from
-the host's in the last ulp, so bitwise equality is not expected)."""
+<= 1e-12 (FP64 in the reference's evaluation order; the GPU's cbrt can
+differ from the host's in the last ulp, so bitwise equality with the host
+is not expected).  Face sharing inside cfd_weno is checked bit for bit."""
 from __future__ import annotations
 
 import numpy as np
@@ -135,3 +136,46 @@ def test_argument_validation(ctx):
     assert e.value.status == abi.EINVAL
     for p in dev.values():
         ctx.free(p)
+
+
+@pytest.mark.parametrize("maker", ["vortex", "tgv", "box", "channel"])
+def test_face_reuse_is_bit_identical(ctx, maker):
+    """cfd_weno with shared faces (the default) and with both faces evaluated
+    at every row (the reference's way) write the same bits to every buffer:
+    periodic tables (every face shared), the ghost box (loc codes, faces at
+    the box edge computed directly) and the walled channel with the boundary
+    routine after every stage."""
+    from cfd_gb300 import cases, runtime
+    if maker == "vortex":
+        c, stages = cases.isentropic_vortex(n=16, shape=(16, 12, 10)), 3
+    elif maker == "tgv":
+        c, stages = cases.taylor_green(n=14, shape=(14, 12, 10)), 3
+    elif maker == "box":
+        c, stages = cases.ghost_box(shape=(9, 8, 7), seed=5), 1
+    else:
+        c, stages = cases.channel(ni=12, nj=10, nk=6), 3
+    keys = ("U0", "U1", "U2", "Q", "roe", "F", "E", "G", "Fv", "Ev", "Gv", "flow", "L")
+    out = {}
+    for reuse in (True, False):
+        ctx.set_face_reuse(reuse)
+        bnd = runtime.Boundary(ctx, c.arrays["grid"], c.bc) if c.bc is not None else None
+        dev = ctx.upload_case(copy_arrays(c.arrays))
+        try:
+            for j in range(stages):
+                ctx.stage(dev, c.g_node, c.sd_node, c.params, j, c.dt, want_L=True)
+                if bnd is not None:
+                    bnd.fill(dev["flow"], c.params.mach, 1, c.sd_node)
+            res = {}
+            for k in keys:
+                like = c.arrays[k] if k in c.arrays else np.zeros((c.g_node + 1, 5))
+                res[k] = ctx.download(dev, k, like)
+            out[reuse] = res
+        finally:
+            ctx.set_face_reuse(True)
+            for p in dev.values():
+                ctx.free(p)
+            if bnd is not None:
+                bnd.close()
+    for k in keys:
+        a, b = out[True][k], out[False][k]
+        assert np.array_equal(a.view(np.uint64), b.view(np.uint64)), f"{maker}: {k} differs"
