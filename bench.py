@@ -9,10 +9,13 @@ Viscous -> Weno) over the whole grid.
 Arms:
   --impl gb300      (default) the CUDA library.  ``value``: FP64 form, state
                     resident in HBM, CUDA events on the launching stream;
-                    ``e2e``: the same through the public solver API with the
-                    FLOW buffer copied from / to pinned host memory every
-                    step; ``mixed``: the mixed-precision form, with its
-                    relative L2 error against the FP64 form on the same run.
+                    ``e2e``: the same metric through the drop-in entry points
+                    (cfd_uq / cfd_viscous / cfd_weno per stage, the calls a
+                    reference host binds) with FLOW copied from / to pinned
+                    host memory every step (``e2e_resident``: the same through
+                    the resident solver API); ``mixed``: the mixed-precision
+                    form, with its relative L2 error against the FP64 form on
+                    the same run.
   --impl reference  the reference algorithm on the host cores (the CPU
                     restatement in oracle/, all threads), same workload.
 
@@ -75,8 +78,8 @@ def parse_args(argv=None):
     p.add_argument("--cpu-steps", type=int, default=1, help="full steps timed for the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-mixed", action="store_true")
-    p.add_argument("--dropin-steps", type=int, default=5,
-                   help="steps timed through the drop-in entry points (0 = skip)")
+    p.add_argument("--dropin-steps", type=int, default=0,
+                   help="steps timed through the drop-in entry points (0 = --steps)")
     p.add_argument("--batch-count", type=int, default=64, help="instances of the batched workload (0 = skip)")
     p.add_argument("--batch-steps", type=int, default=20)
     p.add_argument("--batch-forms", default="fp64,mixed", help="forms of the batched leg (fp64, mixed or both)")
@@ -362,8 +365,12 @@ def gpu_arm(args):
     }
     s64.close()
 
-    if args.dropin_steps > 0:
-        line["dropin"] = bench_dropin(ctx, torch, stream, case, args)
+    # headline e2e: the reference-facing drop-in entry points with host FLOW
+    dropin = bench_dropin(ctx, torch, stream, case, args, world, device=f"cuda:{local}")
+    line["dropin"] = dropin
+    line["e2e_resident"] = dict(line["e2e"], api="cfd_solver_set_flow / cfd_solver_step / cfd_solver_get_flow")
+    line["e2e"] = dict(dropin["e2e"], api="cfd_uq / cfd_viscous / cfd_weno per stage, FLOW written and read "
+                                          "back every step (pinned host memory)")
     if args.diag_steps > 0 and args.config.startswith("tgv"):
         line["tgv_diagnostics"] = bench_diagnostics(ctx, case, args)
     if args.batch_count > 0:
@@ -572,13 +579,13 @@ def bench_serving(ctx, args):
     return out
 
 
-def bench_dropin(ctx, torch, stream, case, args):
+def bench_dropin(ctx, torch, stream, case, args, world: int = 1, device=None):
     """The FP64 step through the three drop-in entry points on the
     reference's AoS buffers (what a reference host loop binds): U_Q ->
     Viscous -> Weno per stage.  Device-resident rate, and end to end with
     FLOW written from and read back to pinned host memory every step."""
     import numpy as np
-    steps = max(1, min(args.steps, args.dropin_steps))
+    steps = args.dropin_steps if args.dropin_steps > 0 else args.steps
     N = case.sd_node
     dev = ctx.upload_case(case.arrays)
     flow0 = case.arrays["flow"]
@@ -589,6 +596,7 @@ def bench_dropin(ctx, torch, stream, case, args):
 
     for _ in range(2):
         run_step()
+    barrier(world)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     launches0 = ctx.launch_count
@@ -604,6 +612,7 @@ def bench_dropin(ctx, torch, stream, case, args):
     host_in = torch.empty(flow0.shape, dtype=torch.float64, pin_memory=True).numpy()
     host_out = torch.empty(flow0.shape, dtype=torch.float64, pin_memory=True).numpy()
     host_in[...] = flow0
+    barrier(world)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(steps):
@@ -612,11 +621,14 @@ def bench_dropin(ctx, torch, stream, case, args):
         ctx.read(host_out, dev["flow"])
         host_in, host_out = host_out, host_in
     e2e_secs = time.perf_counter() - t0
+    barrier(world)
     for p in dev.values():
         ctx.free(p)
-    return {"value": N * steps / secs, "unit": UNIT, "ms_per_step": 1e3 * secs / steps, "steps": steps,
+    value, tmax = aggregate(secs, N * steps, world, device=device)
+    e2e_value, _ = aggregate(e2e_secs, N * steps, world, device=device)
+    return {"value": value, "unit": UNIT, "ms_per_step": 1e3 * tmax / steps, "steps": steps,
             "gpu_launches": launches,
-            "e2e": {"value": N * steps / e2e_secs, "unit": UNIT, "h2d_bytes_per_step": int(host_in.nbytes),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(host_in.nbytes),
                     "d2h_bytes_per_step": int(host_out.nbytes)},
             "path": "cfd_uq / cfd_viscous / cfd_weno on the reference AoS buffers (neighbour-table gathers)"}
 
