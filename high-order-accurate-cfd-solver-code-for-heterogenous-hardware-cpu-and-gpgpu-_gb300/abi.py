@@ -90,6 +90,7 @@ PROTOTYPES = {
     "cfd_bc_create": (C.c_int, [_vp, _vp, _i32] + [_vp, _i32] * 4 + [C.POINTER(_vp)]),
     "cfd_bc_destroy": (C.c_int, [_vp]),
     "cfd_boundary_fill": (C.c_int, [_vp, _vp, _vp, _d, _i32, _i32]),
+    "cfd_rk3_step": (C.c_int, [_vp, _d, _d] + [_vp] * 16 + [_i32, _i32, C.POINTER(Params), _vp, _i32]),
     "cfd_solver_set_boundary": (C.c_int, [_vp, _vp]),
     "cfd_batch_create": (C.c_int, [_vp, _i32, C.c_uint64, C.POINTER(_vp)]),
     "cfd_batch_destroy": (C.c_int, [_vp]),

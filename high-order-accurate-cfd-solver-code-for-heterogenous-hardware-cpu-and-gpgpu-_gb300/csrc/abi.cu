@@ -1,6 +1,7 @@
 // abi.cu -- context, buffers and the three drop-in entry points of the C ABI.
 #include <cstring>
 
+#include "boundary.h"
 #include "internal.h"
 
 namespace cfd {
@@ -91,6 +92,76 @@ Phys make_phys(const cfd_params_t *p)
 
 using namespace cfd;
 
+namespace cfd {
+namespace {
+
+// One buffer argument of a kernel entry point.  Device pointers are used as
+// given.  A host pointer (the reference host's std::vector data) gets a
+// device mirror of n_rows rows owned by the context: the host rows are
+// copied in before the launch and, for buffers the call writes, back after
+// it -- the whole-array copies Solver.cpp:371-541 makes around every launch.
+struct BufArg {
+    void *user;
+    size_t row_bytes;
+    bool written;
+    void *dev = nullptr;
+    bool host = false;
+};
+
+template <size_t K>
+cfd_status_t stage_in(cfd_ctx *ctx, BufArg (&a)[K], const char *who)
+{
+    for (BufArg &b : a) {
+        if (!b.user) return fail(ctx, CFD_EINVAL, std::string(who) + ": null buffer");
+        if (is_device_pointer(b.user)) {
+            b.dev = b.user;
+            continue;
+        }
+        const size_t bytes = (size_t)ctx->n_rows * b.row_bytes;
+        auto it = ctx->mirrors.find(b.user);
+        if (it == ctx->mirrors.end() || it->second.second < bytes) {
+            if (it != ctx->mirrors.end()) {
+                cudaStreamSynchronize(ctx->stream);
+                cudaFree(it->second.first);
+                ctx->mirrors.erase(it);
+            }
+            void *d = nullptr;
+            cudaError_t e = cudaMalloc(&d, bytes);
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "device mirror of a host buffer");
+            it = ctx->mirrors.emplace(b.user, std::make_pair(d, bytes)).first;
+        }
+        b.dev = it->second.first;
+        b.host = true;
+        cudaError_t e = cudaMemcpyAsync(b.dev, b.user, bytes, cudaMemcpyHostToDevice, ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "host buffer copy in");
+    }
+    return CFD_OK;
+}
+
+// Copies written host buffers back (unless the launch itself failed) and
+// waits for them; returns the launch status or the copy's failure.
+template <size_t K>
+cfd_status_t stage_out(cfd_ctx *ctx, const BufArg (&a)[K], cfd_status_t launch_status)
+{
+    if (launch_status == CFD_ECUDA || launch_status == CFD_ENOMEM) return launch_status;
+    bool any = false;
+    for (const BufArg &b : a)
+        if (b.host && b.written) {
+            cudaError_t e = cudaMemcpyAsync(b.user, b.dev, (size_t)ctx->n_rows * b.row_bytes, cudaMemcpyDeviceToHost,
+                                            ctx->stream);
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "host buffer copy out");
+            any = true;
+        }
+    if (any) {
+        cudaError_t e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamSynchronize");
+    }
+    return launch_status;
+}
+
+}  // namespace
+}  // namespace cfd
+
 extern "C" {
 
 void cfd_params_default(cfd_params_t *p)
@@ -161,6 +232,7 @@ cfd_status_t cfd_ctx_destroy(cfd_ctx_t *ctx)
     if (ctx->d_flags) cudaFree(ctx->d_flags);
     if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
     if (ctx->d_face) cudaFree(ctx->d_face);
+    for (auto &m : ctx->mirrors) cudaFree(m.second.first);
     delete ctx;
     return CFD_OK;
 }
@@ -271,28 +343,27 @@ cfd_status_t cfd_buffer_read(cfd_ctx_t *ctx, void *dst, const void *src, size_t 
     return CFD_OK;
 }
 
-static cfd_status_t check_launch_args(cfd_ctx_t *ctx, int32_t n_items, std::initializer_list<const void *> ptrs,
-                                      const char *who)
+static cfd_status_t check_launch_args(cfd_ctx_t *ctx, int32_t n_items, const char *who)
 {
     if (!ctx) return CFD_EINVAL;
     if (ctx->n_rows <= 0) return fail(ctx, CFD_EINVAL, std::string(who) + ": call cfd_ctx_set_rows first");
     if (n_items <= 0 || n_items > ctx->n_rows)
         return fail(ctx, CFD_EINVAL, std::string(who) + ": n_items must be in [1, n_rows]");
-    cfd_status_t s = use_device(ctx);
-    if (s != CFD_OK) return s;
-    for (const void *p : ptrs)
-        if (!is_device_pointer(p)) return fail(ctx, CFD_EINVAL, std::string(who) + ": buffers must be device pointers");
-    return CFD_OK;
+    return use_device(ctx);
 }
+
 
 cfd_status_t cfd_uq(cfd_ctx_t *ctx, cfd_column_t *U_C, cfd_column_t *Q_C, const cfd_grid_t *Grid_P, const double *det,
                     cfd_flow_t *FLOW, cfd_roe_t *ROE_AVER, int32_t n_items)
 {
-    cfd_status_t s = check_launch_args(ctx, n_items, {U_C, Q_C, Grid_P, det, FLOW, ROE_AVER}, "cfd_uq");
+    cfd_status_t s = check_launch_args(ctx, n_items, "cfd_uq");
     if (s != CFD_OK) return s;
-    launch_uq(ctx->stream, (double *)U_C, (double *)Q_C, (const int *)Grid_P, det, (const double *)FLOW,
-              (double *)ROE_AVER, n_items, ctx->n_rows, ctx->d_flags);
-    return after_launch(ctx, "cfd_uq launch");
+    BufArg a[] = {{U_C, 40, true}, {Q_C, 40, true}, {(void *)Grid_P, 56, false}, {(void *)det, 8, false},
+                  {FLOW, 72, false}, {ROE_AVER, 288, true}};
+    if ((s = stage_in(ctx, a, "cfd_uq")) != CFD_OK) return s;
+    launch_uq(ctx->stream, (double *)a[0].dev, (double *)a[1].dev, (const int *)a[2].dev, (const double *)a[3].dev,
+              (const double *)a[4].dev, (double *)a[5].dev, n_items, ctx->n_rows, ctx->d_flags);
+    return stage_out(ctx, a, after_launch(ctx, "cfd_uq launch"));
 }
 
 cfd_status_t cfd_viscous(cfd_ctx_t *ctx, cfd_column_t *U_C, cfd_column_t *F_C, cfd_column_t *E_C, cfd_column_t *G_C,
@@ -300,13 +371,17 @@ cfd_status_t cfd_viscous(cfd_ctx_t *ctx, cfd_column_t *U_C, cfd_column_t *F_C, c
                          const cfd_metric_t *metric, const double *det, cfd_flow_t *FLOW, int32_t n_items,
                          const cfd_params_t *params)
 {
-    cfd_status_t s = check_launch_args(ctx, n_items, {U_C, F_C, E_C, G_C, Fv_C, Ev_C, Gv_C, Grid_P, metric, det, FLOW},
-                                       "cfd_viscous");
+    cfd_status_t s = check_launch_args(ctx, n_items, "cfd_viscous");
     if (s != CFD_OK) return s;
-    launch_viscous(ctx->stream, make_phys(params), (const double *)U_C, (double *)F_C, (double *)E_C, (double *)G_C,
-                   (double *)Fv_C, (double *)Ev_C, (double *)Gv_C, (const int *)Grid_P, (const double *)metric, det,
-                   (double *)FLOW, n_items, ctx->n_rows, ctx->d_flags);
-    return after_launch(ctx, "cfd_viscous launch");
+    BufArg a[] = {{U_C, 40, false},  {F_C, 40, true},    {E_C, 40, true},           {G_C, 40, true},
+                  {Fv_C, 40, true},  {Ev_C, 40, true},   {Gv_C, 40, true},          {(void *)Grid_P, 56, false},
+                  {(void *)metric, 504, false}, {(void *)det, 8, false}, {FLOW, 72, true}};
+    if ((s = stage_in(ctx, a, "cfd_viscous")) != CFD_OK) return s;
+    launch_viscous(ctx->stream, make_phys(params), (const double *)a[0].dev, (double *)a[1].dev, (double *)a[2].dev,
+                   (double *)a[3].dev, (double *)a[4].dev, (double *)a[5].dev, (double *)a[6].dev,
+                   (const int *)a[7].dev, (const double *)a[8].dev, (const double *)a[9].dev, (double *)a[10].dev,
+                   n_items, ctx->n_rows, ctx->d_flags);
+    return stage_out(ctx, a, after_launch(ctx, "cfd_viscous launch"));
 }
 
 cfd_status_t cfd_weno(cfd_ctx_t *ctx, int32_t j, double Mach, double del_t, const cfd_determ_t *deter,
@@ -316,18 +391,76 @@ cfd_status_t cfd_weno(cfd_ctx_t *ctx, int32_t j, double Mach, double del_t, cons
                       cfd_column_t *G, cfd_flow_t *FLOW, int32_t n_items, const cfd_params_t *params,
                       cfd_column_t *L_out)
 {
+    if (!ctx) return CFD_EINVAL;
     if (j < 0 || j > 2) return fail(ctx, CFD_EINVAL, "cfd_weno: stage j must be 0, 1 or 2");
-    cfd_status_t s = check_launch_args(
-        ctx, n_items, {deter, det, U0, U1, U2, Grid_P, Q_C, metric, ROE_AVER, Fv, Ev, Gv, F, E, G, FLOW}, "cfd_weno");
+    cfd_status_t s = check_launch_args(ctx, n_items, "cfd_weno");
     if (s != CFD_OK) return s;
-    if (L_out && !is_device_pointer(L_out)) return fail(ctx, CFD_EINVAL, "cfd_weno: L_out must be a device pointer");
-    launch_weno(ctx->stream, make_phys(params), j, Mach, del_t, (const double *)deter, det, (double *)U0, (double *)U1,
-                (double *)U2, (const int *)Grid_P, (const double *)Q_C, (const double *)metric,
-                (const double *)ROE_AVER, (const double *)Fv, (const double *)Ev, (const double *)Gv,
-                (const double *)F, (const double *)E, (const double *)G, (double *)FLOW, n_items, ctx->n_rows,
-                ctx->d_flags, (double *)L_out, ctx->face_reuse ? ctx->d_face : nullptr, ctx->face_rows);
-    ctx->launches += weno_launches(ctx->face_reuse ? ctx->d_face : nullptr, ctx->face_rows, n_items) - 1;
-    return after_launch(ctx, "cfd_weno launch");
+    BufArg a[] = {{(void *)deter, 48, false}, {(void *)det, 8, false},     {U0, 40, j == 2},
+                  {U1, 40, j == 0},           {U2, 40, j == 1},            {(void *)Grid_P, 56, false},
+                  {Q_C, 40, false},           {(void *)metric, 504, false}, {ROE_AVER, 288, false},
+                  {Fv, 40, false},            {Ev, 40, false},             {Gv, 40, false},
+                  {F, 40, false},             {E, 40, false},              {G, 40, false},
+                  {FLOW, 72, true}};
+    if ((s = stage_in(ctx, a, "cfd_weno")) != CFD_OK) return s;
+    BufArg l[] = {{L_out, 40, true}};
+    if (L_out && (s = stage_in(ctx, l, "cfd_weno")) != CFD_OK) return s;
+    double *const face = ctx->face_reuse ? ctx->d_face : nullptr;
+    launch_weno(ctx->stream, make_phys(params), j, Mach, del_t, (const double *)a[0].dev, (const double *)a[1].dev,
+                (double *)a[2].dev, (double *)a[3].dev, (double *)a[4].dev, (const int *)a[5].dev,
+                (const double *)a[6].dev, (const double *)a[7].dev, (const double *)a[8].dev,
+                (const double *)a[9].dev, (const double *)a[10].dev, (const double *)a[11].dev,
+                (const double *)a[12].dev, (const double *)a[13].dev, (const double *)a[14].dev, (double *)a[15].dev,
+                n_items, ctx->n_rows, ctx->d_flags, L_out ? (double *)l[0].dev : nullptr, face, ctx->face_rows);
+    ctx->launches += weno_launches(face, ctx->face_rows, n_items) - 1;
+    s = stage_out(ctx, a, after_launch(ctx, "cfd_weno launch"));
+    return L_out ? stage_out(ctx, l, s) : s;
+}
+
+cfd_status_t cfd_rk3_step(cfd_ctx_t *ctx, double Mach, double del_t, const cfd_determ_t *deter, const double *det,
+                          cfd_column_t *U0, cfd_column_t *U1, cfd_column_t *U2, const cfd_grid_t *Grid_P,
+                          cfd_column_t *Q_C, const cfd_metric_t *metric, cfd_roe_t *ROE_AVER, cfd_column_t *Fv,
+                          cfd_column_t *Ev, cfd_column_t *Gv, cfd_column_t *F, cfd_column_t *E, cfd_column_t *G,
+                          cfd_flow_t *FLOW, int32_t g_node, int32_t sd_node, const cfd_params_t *params,
+                          const cfd_bc_t *bc, int32_t nsteps)
+{
+    if (!ctx) return CFD_EINVAL;
+    if (nsteps < 1) return fail(ctx, CFD_EINVAL, "cfd_rk3_step: nsteps must be at least 1");
+    if (sd_node < 1 || sd_node > g_node) return fail(ctx, CFD_EINVAL, "cfd_rk3_step: need 1 <= sd_node <= g_node");
+    cfd_status_t s = check_launch_args(ctx, g_node + 1, "cfd_rk3_step");
+    if (s != CFD_OK) return s;
+    if (bc && bc->n_rows != ctx->n_rows)
+        return fail(ctx, CFD_EINVAL, "cfd_rk3_step: boundary lists were made for another table");
+    BufArg a[] = {{(void *)deter, 48, false}, {(void *)det, 8, false},     {U0, 40, true},
+                  {U1, 40, true},             {U2, 40, true},              {(void *)Grid_P, 56, false},
+                  {Q_C, 40, true},            {(void *)metric, 504, false}, {ROE_AVER, 288, true},
+                  {Fv, 40, true},             {Ev, 40, true},              {Gv, 40, true},
+                  {F, 40, true},              {E, 40, true},               {G, 40, true},
+                  {FLOW, 72, true}};
+    if ((s = stage_in(ctx, a, "cfd_rk3_step")) != CFD_OK) return s;
+    const Phys P = make_phys(params);
+    double *const face = ctx->face_reuse ? ctx->d_face : nullptr;
+    double *U[3] = {(double *)a[2].dev, (double *)a[3].dev, (double *)a[4].dev};
+    const int *grid = (const int *)a[5].dev;
+    const double *dt_ = (const double *)a[0].dev, *dd = (const double *)a[1].dev, *met = (const double *)a[7].dev;
+    double *Q = (double *)a[6].dev, *roe = (double *)a[8].dev, *flow = (double *)a[15].dev;
+    double *Fv_ = (double *)a[9].dev, *Ev_ = (double *)a[10].dev, *Gv_ = (double *)a[11].dev;
+    double *F_ = (double *)a[12].dev, *E_ = (double *)a[13].dev, *G_ = (double *)a[14].dev;
+    uint64_t n = 0;
+    for (int step = 0; step < nsteps; ++step)
+        for (int j = 0; j < 3; ++j) {   // Solver.cpp:365-658, j passed per stage
+            launch_uq(ctx->stream, U[j], Q, grid, dd, flow, roe, g_node + 1, ctx->n_rows, ctx->d_flags);
+            launch_viscous(ctx->stream, P, U[j], F_, E_, G_, Fv_, Ev_, Gv_, grid, met, dd, flow, g_node + 1,
+                           ctx->n_rows, ctx->d_flags);
+            launch_weno(ctx->stream, P, j, Mach, del_t, dt_, dd, U[0], U[1], U[2], grid, Q, met, roe, Fv_, Ev_, Gv_,
+                        F_, E_, G_, flow, sd_node + 1, ctx->n_rows, ctx->d_flags, nullptr, face, ctx->face_rows);
+            n += 2 + weno_launches(face, ctx->face_rows, sd_node + 1);
+            if (bc) {
+                bc_apply_aos(ctx->stream, bc->dev, flow, Mach);
+                n += bc->dev.launches();
+            }
+        }
+    ctx->launches += n - 1;
+    return stage_out(ctx, a, after_launch(ctx, "cfd_rk3_step launches"));
 }
 
 }  // extern "C"

@@ -6,6 +6,8 @@
 
 #include <cstdint>
 #include <string>
+#include <unordered_map>
+#include <utility>
 #include <vector>
 
 #include "cfd_rhs.h"
@@ -34,6 +36,9 @@ struct cfd_ctx {
     double *d_face = nullptr;
     long long face_rows = 0;
     bool face_reuse = true;
+    // device mirrors of host buffers handed to the kernel entry points:
+    // host pointer -> (device buffer, bytes)
+    std::unordered_map<const void *, std::pair<void *, size_t>> mirrors;
 };
 
 namespace cfd {

@@ -159,6 +159,23 @@ class Context:
                                      metric, ROE_AVER, Fv, Ev, Gv, F, E, G, FLOW, int(n_items), C.byref(pr), L_out),
                    "cfd_weno")
 
+    def rk3_step(self, bufs: dict, g_node: int, sd_node: int, params, dt: float, nsteps: int = 1, bc=None):
+        """cfd_rk3_step: nsteps SSP-RK3 steps on the reference buffers in one
+        call.  bufs maps buffer names to device pointers (ints) or host numpy
+        arrays of g_node + 1 rows (copied in and back by the library); bc is
+        an optional Boundary."""
+        def ptr(x):
+            if isinstance(x, np.ndarray):
+                assert x.flags["C_CONTIGUOUS"]
+                return C.c_void_p(x.ctypes.data)
+            return C.c_void_p(x)
+        b = {k: ptr(v) for k, v in bufs.items()}
+        pr = to_params(params)
+        self.check(self.lib.cfd_rk3_step(self.h, float(params.mach), float(dt), b["deter"], b["det"], b["U0"], b["U1"],
+                                         b["U2"], b["grid"], b["Q"], b["metric"], b["roe"], b["Fv"], b["Ev"], b["Gv"],
+                                         b["F"], b["E"], b["G"], b["flow"], int(g_node), int(sd_node), C.byref(pr),
+                                         bc.h if bc is not None else None, int(nsteps)), "cfd_rk3_step")
+
     def stage(self, dev: dict, g_node: int, sd_node: int, params, j: int, dt: float, want_L: bool = False):
         """One stage of the reference host loop (Solver.cpp:365-541) through
         the three drop-in entry points; U_Q writes U_j, Viscous reads U_j."""

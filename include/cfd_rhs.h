@@ -101,6 +101,20 @@ typedef struct {
 } cfd_roe_t;
 #pragma pack(pop)
 
+/* The packed sizes of functions.h:49-113, which the host's vectors have. */
+#ifdef __cplusplus
+#define CFD_SIZE_CHECK(T, n) static_assert(sizeof(T) == (n), #T " must match the reference layout")
+#else
+#define CFD_SIZE_CHECK(T, n) _Static_assert(sizeof(T) == (n), #T " must match the reference layout")
+#endif
+CFD_SIZE_CHECK(cfd_grid_t, 56);
+CFD_SIZE_CHECK(cfd_flow_t, 72);
+CFD_SIZE_CHECK(cfd_column_t, 40);
+CFD_SIZE_CHECK(cfd_metric_t, 504);
+CFD_SIZE_CHECK(cfd_determ_t, 48);
+CFD_SIZE_CHECK(cfd_roe_t, 288);
+#undef CFD_SIZE_CHECK
+
 /* -------------------------------------------------------- parameters ---- */
 typedef enum { CFD_PREC_FP64 = 0, CFD_PREC_MIXED = 1 } cfd_precision_t;
 
@@ -157,10 +171,15 @@ cfd_status_t cfd_buffer_write(cfd_ctx_t *ctx, void *device_dst, const void *host
 cfd_status_t cfd_buffer_read(cfd_ctx_t *ctx, void *host_dst, const void *device_src, size_t bytes);
 
 /* ------------------------------------------- drop-in kernel entry points -- */
-/* All buffer arguments are device pointers (cfd_buffer_alloc or any
- * cudaMalloc'd memory).  Argument order follows the reference kernels; the
- * trailing params pointer (NULL = reference constants) carries the constants
- * the reference hard-codes. */
+/* Buffer arguments are device pointers (cfd_buffer_alloc or any cudaMalloc'd
+ * memory; the resident mode: nothing is copied) or host pointers to arrays of
+ * n_rows rows (the reference host's std::vector data): a host buffer gets a
+ * device mirror owned by the context (one per host address, kept until
+ * cfd_ctx_destroy), its rows are copied in before the launch and, if the
+ * call writes it, back before the call returns -- the cl::copy of
+ * Solver.cpp:371-541 around each launch.  Argument order follows
+ * the reference kernels; the trailing params pointer (NULL = reference
+ * constants) carries the constants the reference hard-codes. */
 
 /* U_Q.cl:36-125: Roe averages of the six faces, U_C = det*Q, Q_C. */
 cfd_status_t cfd_uq(cfd_ctx_t *ctx, cfd_column_t *U_C, cfd_column_t *Q_C, const cfd_grid_t *Grid_P,
@@ -175,7 +194,7 @@ cfd_status_t cfd_viscous(cfd_ctx_t *ctx, cfd_column_t *U_C, cfd_column_t *F_C, c
 
 /* Weno.cl:36-3137: characteristic WENO5 + LLF + 6th-order flux correction +
  * viscous divergence, RHS L, SSP-RK3 stage j (0,1,2) and primitive update.
- * L_out (device, may be NULL) receives L per row. */
+ * L_out (may be NULL) receives L per row. */
 cfd_status_t cfd_weno(cfd_ctx_t *ctx, int32_t j, double Mach, double del_t, const cfd_determ_t *deter,
                       const double *det, cfd_column_t *U0, cfd_column_t *U1, cfd_column_t *U2,
                       const cfd_grid_t *Grid_P, cfd_column_t *Q_C, const cfd_metric_t *metric,
@@ -252,6 +271,19 @@ cfd_status_t cfd_bc_destroy(cfd_bc_t *bc);
  * (Flow_Initialisation.cpp:35-48). */
 cfd_status_t cfd_boundary_fill(cfd_ctx_t *ctx, const cfd_bc_t *bc, cfd_flow_t *FLOW, double Mach, int32_t initial,
                                int32_t sd_node);
+
+/* nsteps whole SSP-RK3 steps of the host loop (Solver.cpp:356-658) in one
+ * call on the reference buffers: per stage j, U_Q (rows 0..g_node, writes
+ * U_j), Viscous (rows 0..g_node), Weno stage j (rows 0..sd_node) and, if bc
+ * is not NULL, the boundary routine (initial = 1).  Buffers as for the
+ * kernel entry points (host buffers are copied in once and out once per
+ * call); argument order that of cfd_weno without j. */
+cfd_status_t cfd_rk3_step(cfd_ctx_t *ctx, double Mach, double del_t, const cfd_determ_t *deter, const double *det,
+                          cfd_column_t *U0, cfd_column_t *U1, cfd_column_t *U2, const cfd_grid_t *Grid_P,
+                          cfd_column_t *Q_C, const cfd_metric_t *metric, cfd_roe_t *ROE_AVER, cfd_column_t *Fv,
+                          cfd_column_t *Ev, cfd_column_t *Gv, cfd_column_t *F, cfd_column_t *E, cfd_column_t *G,
+                          cfd_flow_t *FLOW, int32_t g_node, int32_t sd_node, const cfd_params_t *params,
+                          const cfd_bc_t *bc, int32_t nsteps);
 /* The solver runs the routine after every stage (with its Mach number);
  * NULL switches it off.  The solver keeps its own copy of the plan. */
 cfd_status_t cfd_solver_set_boundary(cfd_solver_t *s, const cfd_bc_t *bc);

@@ -125,9 +125,11 @@ def test_argument_validation(ctx):
     with pytest.raises(abi.CfdError) as e:       # more items than rows
         ctx.uq(dev["U0"], dev["Q"], dev["grid"], dev["det"], dev["flow"], dev["roe"], c.g_node + 2)
     assert e.value.status == abi.EINVAL
-    host = np.zeros((c.g_node + 1, 5))
-    with pytest.raises(abi.CfdError) as e:       # host pointer where a device buffer is required
-        ctx.uq(host.ctypes.data, dev["Q"], dev["grid"], dev["det"], dev["flow"], dev["roe"], c.g_node + 1)
+    with pytest.raises(abi.CfdError) as e:       # a missing buffer
+        ctx.uq(None, dev["Q"], dev["grid"], dev["det"], dev["flow"], dev["roe"], c.g_node + 1)
+    assert e.value.status == abi.EINVAL
+    with pytest.raises(abi.CfdError) as e:       # sd_node beyond g_node
+        ctx.rk3_step(dev, c.g_node, c.g_node + 1, c.params, c.dt)
     assert e.value.status == abi.EINVAL
     with pytest.raises(abi.CfdError) as e:
         ctx.weno(3, 1.5, 0.01, dev["deter"], dev["det"], dev["U0"], dev["U1"], dev["U2"], dev["grid"], dev["Q"],
@@ -179,3 +181,79 @@ def test_face_reuse_is_bit_identical(ctx, maker):
     for k in keys:
         a, b = out[True][k], out[False][k]
         assert np.array_equal(a.view(np.uint64), b.view(np.uint64)), f"{maker}: {k} differs"
+
+
+def _host_stage(ctx, a, g_node, sd_node, params, j, dt, L=None):
+    """One stage through the entry points with host numpy arrays."""
+    p = {k: v.ctypes.data for k, v in a.items()}
+    Uj = p[("U0", "U1", "U2")[j]]
+    ctx.uq(Uj, p["Q"], p["grid"], p["det"], p["flow"], p["roe"], g_node + 1)
+    ctx.viscous(Uj, p["F"], p["E"], p["G"], p["Fv"], p["Ev"], p["Gv"], p["grid"], p["metric"], p["det"], p["flow"],
+                g_node + 1, params)
+    ctx.weno(j, params.mach, dt, p["deter"], p["det"], p["U0"], p["U1"], p["U2"], p["grid"], p["Q"], p["metric"],
+             p["roe"], p["Fv"], p["Ev"], p["Gv"], p["F"], p["E"], p["G"], p["flow"], sd_node + 1, params,
+             L.ctypes.data if L is not None else None)
+
+
+def _download_all(ctx, dev, like):
+    return {k: ctx.download(dev, k, like[k]) for k in like}
+
+
+def _assert_same(got, want, what):
+    for k in want:
+        assert np.array_equal(got[k].view(np.uint64), want[k].view(np.uint64)), f"{what}: {k} differs"
+
+
+@pytest.mark.parametrize("maker", ["vortex", "box"])
+def test_host_buffers_match_device_buffers(ctx, maker):
+    """The kernel entry points on host arrays (copied through the context's
+    device mirrors) write the same bits as on device buffers."""
+    from cfd_gb300 import cases
+    c, stages = ((cases.isentropic_vortex(n=12, shape=(12, 10, 8)), 3) if maker == "vortex"
+                 else (cases.ghost_box(shape=(9, 8, 7), seed=5), 1))
+    dev = ctx.upload_case(copy_arrays(c.arrays))
+    Ld = None
+    for j in range(stages):
+        ctx.stage(dev, c.g_node, c.sd_node, c.params, j, c.dt, want_L=True)
+        Ld = ctx.download(dev, "L", np.zeros((c.g_node + 1, 5)))
+    want = _download_all(ctx, dev, c.arrays)
+    for p in dev.values():
+        ctx.free(p)
+    a = copy_arrays(c.arrays)
+    L = np.zeros((c.g_node + 1, 5))
+    for j in range(stages):
+        _host_stage(ctx, a, c.g_node, c.sd_node, c.params, j, c.dt, L)
+    _assert_same(a, want, maker)
+    assert np.array_equal(L[: c.sd_node + 1], Ld[: c.sd_node + 1])
+
+
+@pytest.mark.parametrize("maker", ["tgv", "channel"])
+def test_rk3_step_matches_stage_calls(ctx, maker):
+    """cfd_rk3_step (two steps in one call; the channel with the boundary
+    routine after every stage) equals six stage calls, on device buffers and
+    on host arrays."""
+    from cfd_gb300 import cases, runtime
+    c = (cases.taylor_green(n=12, shape=(12, 10, 8)) if maker == "tgv" else cases.channel(ni=12, nj=10, nk=6))
+    bnd = runtime.Boundary(ctx, c.arrays["grid"], c.bc) if c.bc is not None else None
+    try:
+        dev = ctx.upload_case(copy_arrays(c.arrays))
+        for _ in range(2):
+            for j in range(3):
+                ctx.stage(dev, c.g_node, c.sd_node, c.params, j, c.dt)
+                if bnd is not None:
+                    bnd.fill(dev["flow"], c.params.mach, 1, c.sd_node)
+        want = _download_all(ctx, dev, c.arrays)
+        for p in dev.values():
+            ctx.free(p)
+        dev = ctx.upload_case(copy_arrays(c.arrays))
+        ctx.rk3_step(dev, c.g_node, c.sd_node, c.params, c.dt, nsteps=2, bc=bnd)
+        got = _download_all(ctx, dev, c.arrays)
+        for p in dev.values():
+            ctx.free(p)
+        _assert_same(got, want, maker + " device buffers")
+        a = copy_arrays(c.arrays)
+        ctx.rk3_step(a, c.g_node, c.sd_node, c.params, c.dt, nsteps=2, bc=bnd)
+        _assert_same(a, want, maker + " host arrays")
+    finally:
+        if bnd is not None:
+            bnd.close()
