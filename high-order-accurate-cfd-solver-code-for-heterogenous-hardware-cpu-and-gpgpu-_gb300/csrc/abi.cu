@@ -93,31 +93,17 @@ Phys make_phys(const cfd_params_t *p)
 using namespace cfd;
 
 namespace cfd {
-namespace {
 
-// One buffer argument of a kernel entry point.  Device pointers are used as
-// given.  A host pointer (the reference host's std::vector data) gets a
-// device mirror of n_rows rows owned by the context: the host rows are
-// copied in before the launch and, for buffers the call writes, back after
-// it -- the whole-array copies Solver.cpp:371-541 makes around every launch.
-struct BufArg {
-    void *user;
-    size_t row_bytes;
-    bool written;
-    void *dev = nullptr;
-    bool host = false;
-};
-
-template <size_t K>
-cfd_status_t stage_in(cfd_ctx *ctx, BufArg (&a)[K], const char *who)
+cfd_status_t stage_in(cfd_ctx *ctx, BufArg *a, int n, const char *who)
 {
-    for (BufArg &b : a) {
+    for (int i = 0; i < n; ++i) {
+        BufArg &b = a[i];
         if (!b.user) return fail(ctx, CFD_EINVAL, std::string(who) + ": null buffer");
         if (is_device_pointer(b.user)) {
             b.dev = b.user;
             continue;
         }
-        const size_t bytes = (size_t)ctx->n_rows * b.row_bytes;
+        const size_t bytes = (size_t)(b.rows > 0 ? b.rows : ctx->n_rows) * b.row_bytes;
         auto it = ctx->mirrors.find(b.user);
         if (it == ctx->mirrors.end() || it->second.second < bytes) {
             if (it != ctx->mirrors.end()) {
@@ -138,17 +124,14 @@ cfd_status_t stage_in(cfd_ctx *ctx, BufArg (&a)[K], const char *who)
     return CFD_OK;
 }
 
-// Copies written host buffers back (unless the launch itself failed) and
-// waits for them; returns the launch status or the copy's failure.
-template <size_t K>
-cfd_status_t stage_out(cfd_ctx *ctx, const BufArg (&a)[K], cfd_status_t launch_status)
+cfd_status_t stage_out(cfd_ctx *ctx, const BufArg *a, int n, cfd_status_t launch_status)
 {
     if (launch_status == CFD_ECUDA || launch_status == CFD_ENOMEM) return launch_status;
     bool any = false;
-    for (const BufArg &b : a)
-        if (b.host && b.written) {
-            cudaError_t e = cudaMemcpyAsync(b.user, b.dev, (size_t)ctx->n_rows * b.row_bytes, cudaMemcpyDeviceToHost,
-                                            ctx->stream);
+    for (int i = 0; i < n; ++i)
+        if (a[i].host && a[i].written) {
+            const size_t bytes = (size_t)(a[i].rows > 0 ? a[i].rows : ctx->n_rows) * a[i].row_bytes;
+            cudaError_t e = cudaMemcpyAsync(a[i].user, a[i].dev, bytes, cudaMemcpyDeviceToHost, ctx->stream);
             if (e != cudaSuccess) return cuda_fail(ctx, e, "host buffer copy out");
             any = true;
         }
@@ -159,7 +142,6 @@ cfd_status_t stage_out(cfd_ctx *ctx, const BufArg (&a)[K], cfd_status_t launch_s
     return launch_status;
 }
 
-}  // namespace
 }  // namespace cfd
 
 extern "C" {
@@ -360,10 +342,10 @@ cfd_status_t cfd_uq(cfd_ctx_t *ctx, cfd_column_t *U_C, cfd_column_t *Q_C, const 
     if (s != CFD_OK) return s;
     BufArg a[] = {{U_C, 40, true}, {Q_C, 40, true}, {(void *)Grid_P, 56, false}, {(void *)det, 8, false},
                   {FLOW, 72, false}, {ROE_AVER, 288, true}};
-    if ((s = stage_in(ctx, a, "cfd_uq")) != CFD_OK) return s;
+    if ((s = stage_in(ctx, a, 6, "cfd_uq")) != CFD_OK) return s;
     launch_uq(ctx->stream, (double *)a[0].dev, (double *)a[1].dev, (const int *)a[2].dev, (const double *)a[3].dev,
               (const double *)a[4].dev, (double *)a[5].dev, n_items, ctx->n_rows, ctx->d_flags);
-    return stage_out(ctx, a, after_launch(ctx, "cfd_uq launch"));
+    return stage_out(ctx, a, 6, after_launch(ctx, "cfd_uq launch"));
 }
 
 cfd_status_t cfd_viscous(cfd_ctx_t *ctx, cfd_column_t *U_C, cfd_column_t *F_C, cfd_column_t *E_C, cfd_column_t *G_C,
@@ -376,12 +358,12 @@ cfd_status_t cfd_viscous(cfd_ctx_t *ctx, cfd_column_t *U_C, cfd_column_t *F_C, c
     BufArg a[] = {{U_C, 40, false},  {F_C, 40, true},    {E_C, 40, true},           {G_C, 40, true},
                   {Fv_C, 40, true},  {Ev_C, 40, true},   {Gv_C, 40, true},          {(void *)Grid_P, 56, false},
                   {(void *)metric, 504, false}, {(void *)det, 8, false}, {FLOW, 72, true}};
-    if ((s = stage_in(ctx, a, "cfd_viscous")) != CFD_OK) return s;
+    if ((s = stage_in(ctx, a, 11, "cfd_viscous")) != CFD_OK) return s;
     launch_viscous(ctx->stream, make_phys(params), (const double *)a[0].dev, (double *)a[1].dev, (double *)a[2].dev,
                    (double *)a[3].dev, (double *)a[4].dev, (double *)a[5].dev, (double *)a[6].dev,
                    (const int *)a[7].dev, (const double *)a[8].dev, (const double *)a[9].dev, (double *)a[10].dev,
                    n_items, ctx->n_rows, ctx->d_flags);
-    return stage_out(ctx, a, after_launch(ctx, "cfd_viscous launch"));
+    return stage_out(ctx, a, 11, after_launch(ctx, "cfd_viscous launch"));
 }
 
 cfd_status_t cfd_weno(cfd_ctx_t *ctx, int32_t j, double Mach, double del_t, const cfd_determ_t *deter,
@@ -401,9 +383,9 @@ cfd_status_t cfd_weno(cfd_ctx_t *ctx, int32_t j, double Mach, double del_t, cons
                   {Fv, 40, false},            {Ev, 40, false},             {Gv, 40, false},
                   {F, 40, false},             {E, 40, false},              {G, 40, false},
                   {FLOW, 72, true}};
-    if ((s = stage_in(ctx, a, "cfd_weno")) != CFD_OK) return s;
+    if ((s = stage_in(ctx, a, 16, "cfd_weno")) != CFD_OK) return s;
     BufArg l[] = {{L_out, 40, true}};
-    if (L_out && (s = stage_in(ctx, l, "cfd_weno")) != CFD_OK) return s;
+    if (L_out && (s = stage_in(ctx, l, 1, "cfd_weno")) != CFD_OK) return s;
     double *const face = ctx->face_reuse ? ctx->d_face : nullptr;
     launch_weno(ctx->stream, make_phys(params), j, Mach, del_t, (const double *)a[0].dev, (const double *)a[1].dev,
                 (double *)a[2].dev, (double *)a[3].dev, (double *)a[4].dev, (const int *)a[5].dev,
@@ -412,8 +394,8 @@ cfd_status_t cfd_weno(cfd_ctx_t *ctx, int32_t j, double Mach, double del_t, cons
                 (const double *)a[12].dev, (const double *)a[13].dev, (const double *)a[14].dev, (double *)a[15].dev,
                 n_items, ctx->n_rows, ctx->d_flags, L_out ? (double *)l[0].dev : nullptr, face, ctx->face_rows);
     ctx->launches += weno_launches(face, ctx->face_rows, n_items) - 1;
-    s = stage_out(ctx, a, after_launch(ctx, "cfd_weno launch"));
-    return L_out ? stage_out(ctx, l, s) : s;
+    s = stage_out(ctx, a, 16, after_launch(ctx, "cfd_weno launch"));
+    return L_out ? stage_out(ctx, l, 1, s) : s;
 }
 
 cfd_status_t cfd_rk3_step(cfd_ctx_t *ctx, double Mach, double del_t, const cfd_determ_t *deter, const double *det,
@@ -436,7 +418,7 @@ cfd_status_t cfd_rk3_step(cfd_ctx_t *ctx, double Mach, double del_t, const cfd_d
                   {Fv, 40, true},             {Ev, 40, true},              {Gv, 40, true},
                   {F, 40, true},              {E, 40, true},               {G, 40, true},
                   {FLOW, 72, true}};
-    if ((s = stage_in(ctx, a, "cfd_rk3_step")) != CFD_OK) return s;
+    if ((s = stage_in(ctx, a, 16, "cfd_rk3_step")) != CFD_OK) return s;
     const Phys P = make_phys(params);
     double *const face = ctx->face_reuse ? ctx->d_face : nullptr;
     double *U[3] = {(double *)a[2].dev, (double *)a[3].dev, (double *)a[4].dev};
@@ -460,7 +442,7 @@ cfd_status_t cfd_rk3_step(cfd_ctx_t *ctx, double Mach, double del_t, const cfd_d
             }
         }
     ctx->launches += n - 1;
-    return stage_out(ctx, a, after_launch(ctx, "cfd_rk3_step launches"));
+    return stage_out(ctx, a, 16, after_launch(ctx, "cfd_rk3_step launches"));
 }
 
 }  // extern "C"

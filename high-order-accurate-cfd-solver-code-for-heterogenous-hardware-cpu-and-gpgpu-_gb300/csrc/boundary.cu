@@ -398,17 +398,18 @@ cfd_status_t cfd_boundary_fill(cfd_ctx_t *ctx, const cfd_bc_t *bc, cfd_flow_t *F
                                int32_t sd_node)
 {
     if (!ctx || !bc || !FLOW || !std::isfinite(Mach) || sd_node < 0 || sd_node >= bc->n_rows) return CFD_EINVAL;
-    if (!is_device_pointer(FLOW)) return fail(ctx, CFD_EINVAL, "cfd_boundary_fill: FLOW must be a device buffer");
     cfd_status_t st = use_device(ctx);
     if (st != CFD_OK) return st;
-    double *f = reinterpret_cast<double *>(FLOW);
+    BufArg a[] = {{FLOW, 72, true, bc->n_rows}};   // a device buffer, or the table's host FLOW rows
+    if ((st = stage_in(ctx, a, 1, "cfd_boundary_fill")) != CFD_OK) return st;
+    double *f = reinterpret_cast<double *>(a[0].dev);
     if (initial == 0) {
         bc_free_stream_aos(ctx->stream, f, sd_node, Mach);
         ctx->launches += sd_node > 0;
     }
     bc_apply_aos(ctx->stream, bc->dev, f, Mach);
     ctx->launches += bc->dev.launches();
-    return after_launch(ctx, "cfd_boundary_fill");
+    return stage_out(ctx, a, 1, after_launch(ctx, "cfd_boundary_fill"));
 }
 
 }  // extern "C"

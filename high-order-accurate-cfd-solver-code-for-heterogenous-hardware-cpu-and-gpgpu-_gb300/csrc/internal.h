@@ -59,6 +59,23 @@ Phys make_phys(const cfd_params_t *p);
 
 inline unsigned blocks_for(long long n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
+// One buffer argument of an entry point.  Device pointers are used as
+// given.  A host pointer (the reference host's std::vector data) gets a
+// device mirror of n_rows rows owned by the context: stage_in copies the
+// host rows in before the launch; stage_out copies buffers the call writes
+// back after it (unless the launch failed) and waits -- the whole-array
+// copies Solver.cpp:371-541 makes around every launch.
+struct BufArg {
+    void *user;
+    size_t row_bytes;
+    bool written;
+    long long rows = 0;   // rows of a host buffer (0: the context's n_rows)
+    void *dev = nullptr;
+    bool host = false;
+};
+cfd_status_t stage_in(cfd_ctx *ctx, BufArg *a, int n, const char *who);
+cfd_status_t stage_out(cfd_ctx *ctx, const BufArg *a, int n, cfd_status_t launch_status);
+
 // Drop-in kernel launchers (dropin.cu).  All pointers are device pointers.
 void launch_uq(cudaStream_t st, double *U, double *Q, const int *grid, const double *det, const double *flow,
                double *roe, int n_items, int n_rows, unsigned *flags);

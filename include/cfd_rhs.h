@@ -266,7 +266,9 @@ cfd_status_t cfd_bc_create(cfd_ctx_t *ctx, const cfd_grid_t *grid, int32_t n_row
                            int32_t n_outlet, const int32_t *inlet, int32_t n_inlet, const int32_t *boundary,
                            int32_t n_boundary, const int32_t *wall, int32_t n_wall, cfd_bc_t **bc);
 cfd_status_t cfd_bc_destroy(cfd_bc_t *bc);
-/* intialise() on a device FLOW buffer of the reference layout; with
+/* intialise() on a FLOW buffer of the reference layout (device, or the host
+ * rows of the table the lists were made for, copied as for the kernel entry
+ * points); with
  * initial == 0 rows 1..sd_node first get the free stream
  * (Flow_Initialisation.cpp:35-48). */
 cfd_status_t cfd_boundary_fill(cfd_ctx_t *ctx, const cfd_bc_t *bc, cfd_flow_t *FLOW, double Mach, int32_t initial,

@@ -1,8 +1,9 @@
 """A C++ host drives the drop-in entry points with no Python in the loop:
 tests/cpp/host_loop.cpp, built against include/cfd_rhs.h and
 libcfd_gb300.so, runs the reference host loop's stage sequence (cfd_uq ->
-cfd_viscous -> cfd_weno(j) -> cfd_boundary_fill) on a case written to disk;
-its FLOW must match the oracle (relative L2 <= 1e-12)."""
+cfd_viscous -> cfd_weno(j) -> cfd_boundary_fill) on a case written to disk
+-- on device buffers, on its host vectors directly, and as one cfd_rk3_step
+call; its FLOW must match the oracle (relative L2 <= 1e-12)."""
 from __future__ import annotations
 
 import pathlib
@@ -47,14 +48,15 @@ def _write_case(c, d):
         int(p.viscous), int(p.les), repr(c.dt), *n)) + "\n")
 
 
+@pytest.mark.parametrize("mode", ["device", "host", "rk3"])
 @pytest.mark.parametrize("name", ["channel", "vortex"])
-def test_cpp_host_loop_matches_oracle(name, oracle_mod, tmp_path):
+def test_cpp_host_loop_matches_oracle(name, mode, oracle_mod, tmp_path):
     from cfd_gb300 import cases
     c = cases.channel(ni=12, nj=10, nk=6) if name == "channel" else cases.isentropic_vortex(n=12)
     exe = _build(tmp_path)
     _write_case(c, tmp_path)
     steps = 2
-    r = subprocess.run([str(exe), str(tmp_path), str(steps)], capture_output=True, text=True)
+    r = subprocess.run([str(exe), str(tmp_path), str(steps), mode], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     got = np.fromfile(tmp_path / "flow_out.bin").reshape(-1, 9)
     a = c.copy().arrays
