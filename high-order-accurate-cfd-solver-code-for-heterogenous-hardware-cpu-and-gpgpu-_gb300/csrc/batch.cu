@@ -300,7 +300,8 @@ cfd_status_t cfd_batch_add(cfd_batch_t *b, const cfd_geometry_t *geom, const cfd
             if (v < 0 || v > geom->g_node) return fail(ctx, CFD_EINVAL, "cfd_batch_add: neighbour index out of range");
         }
     LatticeMap map;
-    bool natural = map_lattice(geom, map) && !map.ghosted() && faces_single_valued(geom, map);
+    bool natural = map_lattice(geom, map) && !map.ghosted() && faces_single_valued(geom, map)
+                   && (long long)map.ni * map.nj * map.nk <= kLatticeMaxNodes;
     for (size_t n = 0; natural && n < map.row_of.size(); ++n) natural = map.row_of[n] == (int32_t)n + 1;
     if (!natural)
         return fail(ctx, CFD_EUNSUPPORTED, "cfd_batch_add: batched instances must be periodic lattices in row order");

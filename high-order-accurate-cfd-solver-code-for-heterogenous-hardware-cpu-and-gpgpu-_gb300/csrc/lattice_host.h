@@ -22,6 +22,10 @@ inline int nb_of(const cfd_grid_t &g, int slot)
     }
 }
 
+// Largest lattice the face-based kernels address: they index component
+// arrays of up to 15 components as c * N + n in 32-bit arithmetic.
+constexpr long long kLatticeMaxNodes = 2147483647LL / 15;
+
 // A reference neighbour table seen as a lattice: node n = i + ni*(j + nj*k)
 // is reference row row_of[n].  Direction d (0 = i via N1/N3, 1 = j via
 // N0/N2, 2 = k via N4/N5) is either periodic (the +d chain closes) or

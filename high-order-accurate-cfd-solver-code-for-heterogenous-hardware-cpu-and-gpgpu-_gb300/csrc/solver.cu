@@ -252,10 +252,19 @@ cfd_status_t cfd_solver_create(cfd_ctx_t *ctx, const cfd_geometry_t *geom, const
     s->g_node = geom->g_node;
     s->sd_node = geom->sd_node;
     s->n_rows = n_rows;
-    const bool lattice = force_path != CFD_PATH_GATHER && map_lattice(geom, s->map) && faces_single_valued(geom, s->map);
+    bool lattice = force_path != CFD_PATH_GATHER && map_lattice(geom, s->map) && faces_single_valued(geom, s->map);
     if (force_path == CFD_PATH_STRUCTURED && !lattice) {
         delete s;
         return fail(ctx, CFD_EINVAL, "cfd_solver_create: table is not a lattice with single-valued faces");
+    }
+    if (lattice && (long long)s->map.ni * s->map.nj * s->map.nk > kLatticeMaxNodes) {
+        // beyond the face-based kernels' 32-bit addressing: the gather path
+        // (64-bit row offsets) takes the FP64 form
+        if (force_path == CFD_PATH_STRUCTURED || s->mixed) {
+            delete s;
+            return fail(ctx, CFD_EUNSUPPORTED, "cfd_solver_create: lattice larger than 143,165,576 nodes");
+        }
+        lattice = false;
     }
     s->path = lattice ? CFD_PATH_STRUCTURED : CFD_PATH_GATHER;
     if (s->mixed && s->path != CFD_PATH_STRUCTURED) {
