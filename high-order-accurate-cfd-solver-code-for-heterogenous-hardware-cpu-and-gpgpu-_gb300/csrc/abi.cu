@@ -343,8 +343,10 @@ cfd_status_t cfd_uq(cfd_ctx_t *ctx, cfd_column_t *U_C, cfd_column_t *Q_C, const 
     BufArg a[] = {{U_C, 40, true}, {Q_C, 40, true}, {(void *)Grid_P, 56, false}, {(void *)det, 8, false},
                   {FLOW, 72, false}, {ROE_AVER, 288, true}};
     if ((s = stage_in(ctx, a, 6, "cfd_uq")) != CFD_OK) return s;
-    launch_uq(ctx->stream, (double *)a[0].dev, (double *)a[1].dev, (const int *)a[2].dev, (const double *)a[3].dev,
-              (const double *)a[4].dev, (double *)a[5].dev, n_items, ctx->n_rows, ctx->d_flags);
+    ctx->launches += launch_uq(ctx->stream, (double *)a[0].dev, (double *)a[1].dev, (const int *)a[2].dev,
+                               (const double *)a[3].dev, (const double *)a[4].dev, (double *)a[5].dev, n_items,
+                               ctx->n_rows, ctx->d_flags, ctx->face_reuse ? ctx->d_face : nullptr,
+                               ctx->face_rows) - 1;
     return stage_out(ctx, a, 6, after_launch(ctx, "cfd_uq launch"));
 }
 
@@ -430,12 +432,13 @@ cfd_status_t cfd_rk3_step(cfd_ctx_t *ctx, double Mach, double del_t, const cfd_d
     uint64_t n = 0;
     for (int step = 0; step < nsteps; ++step)
         for (int j = 0; j < 3; ++j) {   // Solver.cpp:365-658, j passed per stage
-            launch_uq(ctx->stream, U[j], Q, grid, dd, flow, roe, g_node + 1, ctx->n_rows, ctx->d_flags);
+            n += launch_uq(ctx->stream, U[j], Q, grid, dd, flow, roe, g_node + 1, ctx->n_rows, ctx->d_flags, face,
+                           ctx->face_rows);
             launch_viscous(ctx->stream, P, U[j], F_, E_, G_, Fv_, Ev_, Gv_, grid, met, dd, flow, g_node + 1,
                            ctx->n_rows, ctx->d_flags);
             launch_weno(ctx->stream, P, j, Mach, del_t, dt_, dd, U[0], U[1], U[2], grid, Q, met, roe, Fv_, Ev_, Gv_,
                         F_, E_, G_, flow, sd_node + 1, ctx->n_rows, ctx->d_flags, nullptr, face, ctx->face_rows);
-            n += 2 + weno_launches(face, ctx->face_rows, sd_node + 1);
+            n += 1 + weno_launches(face, ctx->face_rows, sd_node + 1);
             if (bc) {
                 bc_apply_aos(ctx->stream, bc->dev, flow, Mach);
                 n += bc->dev.launches();

@@ -58,11 +58,25 @@ __device__ __forceinline__ bool gather_star(const int *grid, int gid, int n_rows
 enum { FU = 0, FV = 1, FW = 2, FP = 3, FT = 4, FRHO = 5, FMU = 6, FA = 7, FE = 8 };
 
 // ------------------------------------------------------------------ U_Q --
+// sqrt(rho) and total enthalpy of every row (U_Q.cl:60-65), once per row:
+// sh[2*row], sh[2*row + 1].  k_uq<true> reads them for the row and its six
+// neighbours instead of evaluating them seven times.
+__global__ void __launch_bounds__(128) k_uq_node(const double *__restrict__ flow, int n_rows, double *__restrict__ sh)
+{
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= n_rows) return;
+    const double *f = flow + 9 * (size_t)row;
+    const double rho = f[FRHO];
+    sh[2 * (size_t)row] = sqrt(rho);
+    sh[2 * (size_t)row + 1] = ex::enthalpy(rho, f[FU], f[FV], f[FW], f[FP]);
+}
+
 // U_Q.cl:36-125.
+template <bool SH>
 __global__ void __launch_bounds__(128) k_uq(double *__restrict__ U, double *__restrict__ Q,
                                             const int *__restrict__ grid, const double *__restrict__ det,
                                             const double *__restrict__ flow, double *__restrict__ roe, int n_items,
-                                            int n_rows, unsigned *flags)
+                                            int n_rows, unsigned *flags, const double *__restrict__ sh)
 {
     const int gid = blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= n_items) return;
@@ -77,18 +91,20 @@ __global__ void __launch_bounds__(128) k_uq(double *__restrict__ U, double *__re
     }
     const double *fi = flow + 9 * (size_t)gid;
     const double rho = fi[FRHO], u = fi[FU], v = fi[FV], w = fi[FW], p = fi[FP];
-    const double si = sqrt(rho);
-    const double hi = ex::enthalpy(rho, u, v, w, p);
+    const double si = SH ? sh[2 * (size_t)gid] : sqrt(rho);
+    const double hi = SH ? sh[2 * (size_t)gid + 1] : ex::enthalpy(rho, u, v, w, p);
     // ROE block order ip, jp, kp, im, jm, km; neighbour slots N1, N0, N4, N3, N2, N5
     const int slot_of_block[6] = {1, 0, 4, 3, 2, 5};
     double *r = roe + 36 * (size_t)gid;
 #pragma unroll
     for (int b = 0; b < 6; ++b) {
-        const double *fn = flow + 9 * (size_t)nb[slot_of_block[b]];
+        const int nr = nb[slot_of_block[b]];
+        const double *fn = flow + 9 * (size_t)nr;
         const double rb = fn[FRHO], ub = fn[FU], vb = fn[FV], wb = fn[FW], pb = fn[FP];
-        const double sb = sqrt(rb);
+        const double sb = SH ? sh[2 * (size_t)nr] : sqrt(rb);
+        const double hb = SH ? sh[2 * (size_t)nr + 1] : ex::enthalpy(rb, ub, vb, wb, pb);
         double ra[5];
-        ex::roe(sb, ub, vb, wb, ex::enthalpy(rb, ub, vb, wb, pb), si, u, v, w, hi, ra);
+        ex::roe(sb, ub, vb, wb, hb, si, u, v, w, hi, ra);
         r[6 * b + 0] = ra[0];
         r[6 * b + 1] = ra[1];
         r[6 * b + 2] = ra[2];
@@ -360,10 +376,17 @@ __global__ void __launch_bounds__(128) k_weno(Phys P, int j, double mach, double
         atomicOr(flags, CFD_FLAG_NONFINITE);
 }
 
-void launch_uq(cudaStream_t st, double *U, double *Q, const int *grid, const double *det, const double *flow,
-               double *roe, int n_items, int n_rows, unsigned *flags)
+int launch_uq(cudaStream_t st, double *U, double *Q, const int *grid, const double *det, const double *flow,
+              double *roe, int n_items, int n_rows, unsigned *flags, double *node_scratch, long long scratch_rows)
 {
-    k_uq<<<blocks_for(n_items, 128), 128, 0, st>>>(U, Q, grid, det, flow, roe, n_items, n_rows, flags);
+    if (node_scratch && scratch_rows >= n_rows) {   // 2 of the 15 doubles per row
+        k_uq_node<<<blocks_for(n_rows, 128), 128, 0, st>>>(flow, n_rows, node_scratch);
+        k_uq<true><<<blocks_for(n_items, 128), 128, 0, st>>>(U, Q, grid, det, flow, roe, n_items, n_rows, flags,
+                                                             node_scratch);
+        return 2;
+    }
+    k_uq<false><<<blocks_for(n_items, 128), 128, 0, st>>>(U, Q, grid, det, flow, roe, n_items, n_rows, flags, nullptr);
+    return 1;
 }
 
 void launch_viscous(cudaStream_t st, const Phys &P, const double *U, double *F, double *E, double *G, double *Fv,

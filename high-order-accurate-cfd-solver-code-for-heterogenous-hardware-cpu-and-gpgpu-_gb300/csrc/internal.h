@@ -77,8 +77,11 @@ cfd_status_t stage_in(cfd_ctx *ctx, BufArg *a, int n, const char *who);
 cfd_status_t stage_out(cfd_ctx *ctx, const BufArg *a, int n, cfd_status_t launch_status);
 
 // Drop-in kernel launchers (dropin.cu).  All pointers are device pointers.
-void launch_uq(cudaStream_t st, double *U, double *Q, const int *grid, const double *det, const double *flow,
-               double *roe, int n_items, int n_rows, unsigned *flags);
+// U_Q; with a scratch of >= n_rows rows (15 doubles each, cfd_weno's face
+// scratch) it first computes sqrt(rho) and H once per row.  Returns the
+// kernels launched (2 or 1).
+int launch_uq(cudaStream_t st, double *U, double *Q, const int *grid, const double *det, const double *flow,
+              double *roe, int n_items, int n_rows, unsigned *flags, double *node_scratch, long long scratch_rows);
 void launch_viscous(cudaStream_t st, const Phys &P, const double *U, double *F, double *E, double *G, double *Fv,
                     double *Ev, double *Gv, const int *grid, const double *metric, const double *det, double *flow,
                     int n_items, int n_rows, unsigned *flags);

@@ -203,13 +203,14 @@ cfd_status_t run_stage(cfd_solver *s, int j, double dt, bool want_L)
         }
     } else {
         double *Uj = s->U[j];
-        launch_uq(ctx->stream, Uj, s->Q, s->grid, s->det, s->flow, s->roe, s->g_node + 1, s->n_rows, ctx->d_flags);
+        const int nu = launch_uq(ctx->stream, Uj, s->Q, s->grid, s->det, s->flow, s->roe, s->g_node + 1, s->n_rows,
+                                 ctx->d_flags, s->face, s->n_rows);
         launch_viscous(ctx->stream, s->P, Uj, s->F, s->E, s->G, s->Fv, s->Ev, s->Gv, s->grid, s->metric, s->det,
                        s->flow, s->g_node + 1, s->n_rows, ctx->d_flags);
         launch_weno(ctx->stream, s->P, j, s->P.mach, dt, s->deter, s->det, s->U[0], s->U[1], s->U[2], s->grid, s->Q,
                     s->metric, s->roe, s->Fv, s->Ev, s->Gv, s->F, s->E, s->G, s->flow, s->sd_node + 1, s->n_rows,
                     ctx->d_flags, want_L ? s->L : nullptr, s->face, s->n_rows);
-        ctx->launches += 2 + weno_launches(s->face, s->n_rows, s->sd_node + 1);
+        ctx->launches += nu + 1 + weno_launches(s->face, s->n_rows, s->sd_node + 1);
         if (s->has_bc) {
             bc_apply_aos(ctx->stream, s->bc, s->flow, s->P.mach);
             ctx->launches += s->bc.launches();
@@ -448,7 +449,8 @@ cfd_status_t cfd_solver_profile_stage(cfd_solver_t *s, int32_t j, double del_t, 
     } else {
         cudaEventRecord(ev[0], stream);
         double *Uj = s->U[j];
-        launch_uq(stream, Uj, s->Q, s->grid, s->det, s->flow, s->roe, s->g_node + 1, s->n_rows, s->ctx->d_flags);
+        const int nu = launch_uq(stream, Uj, s->Q, s->grid, s->det, s->flow, s->roe, s->g_node + 1, s->n_rows,
+                                 s->ctx->d_flags, s->face, s->n_rows);
         cudaEventRecord(ev[1], stream);
         launch_viscous(stream, s->P, Uj, s->F, s->E, s->G, s->Fv, s->Ev, s->Gv, s->grid, s->metric, s->det, s->flow,
                        s->g_node + 1, s->n_rows, s->ctx->d_flags);
@@ -460,7 +462,8 @@ cfd_status_t cfd_solver_profile_stage(cfd_solver_t *s, int32_t j, double del_t, 
         snames[0] = "uq";
         snames[1] = "viscous";
         snames[2] = "weno";
-        s->ctx->launches += weno_launches(s->face, s->n_rows, s->sd_node + 1) - 1;   // weno: plus faces + update
+        // uq: per-row pass + Roe kernel; weno: plus faces + update
+        s->ctx->launches += (nu - 1) + weno_launches(s->face, s->n_rows, s->sd_node + 1) - 1;
     }
     s->ctx->launches += nk;
     if (s->has_bc) {   // the boundary routine as one timed entry

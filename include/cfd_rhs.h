@@ -152,12 +152,14 @@ cfd_status_t cfd_ctx_synchronize(cfd_ctx_t *ctx);
 /* Number of rows of every buffer (g_node + 1).  Neighbour indices outside
  * [0, n_rows) make a kernel skip the row and report CFD_EINVAL. */
 cfd_status_t cfd_ctx_set_rows(cfd_ctx_t *ctx, int32_t n_rows);
-/* cfd_weno computes each row's +1/2 faces once and takes a row's -1/2 face
- * from its minus neighbour's +1/2 face wherever the two evaluations have
- * bit-identical inputs (Weno.cl:336-3058 evaluates both at every row); the
- * results are the same bits.  on = 0 evaluates both faces at every row, as
- * the reference does.  Default 1 (needs 120 bytes per row, allocated by
- * cfd_ctx_set_rows). */
+/* Sharing of intermediates between rows (default on): cfd_weno computes each
+ * row's +1/2 faces once and takes a row's -1/2 face from its minus
+ * neighbour's +1/2 face wherever the two evaluations have bit-identical
+ * inputs (Weno.cl:336-3058 evaluates both at every row), and cfd_uq computes
+ * sqrt(rho) and H once per row instead of once per row and neighbour
+ * (U_Q.cl:60-109); the results are the same bits.  on = 0 evaluates
+ * everything per row, as the reference does.  Needs 120 bytes per row,
+ * allocated by cfd_ctx_set_rows. */
 cfd_status_t cfd_ctx_set_face_reuse(cfd_ctx_t *ctx, int on);
 /* Kernels this context launched since creation (for accounting). */
 uint64_t cfd_ctx_launch_count(const cfd_ctx_t *ctx);

@@ -142,8 +142,9 @@ def test_argument_validation(ctx):
 
 @pytest.mark.parametrize("maker", ["vortex", "tgv", "box", "channel"])
 def test_face_reuse_is_bit_identical(ctx, maker):
-    """cfd_weno with shared faces (the default) and with both faces evaluated
-    at every row (the reference's way) write the same bits to every buffer:
+    """cfd_uq / cfd_weno with shared intermediates (per-row sqrt(rho) and H,
+    shared faces: the default) and with everything evaluated per row (the
+    reference's way) write the same bits to every buffer:
     periodic tables (every face shared), the ghost box (loc codes, faces at
     the box edge computed directly) and the walled channel with the boundary
     routine after every stage."""
