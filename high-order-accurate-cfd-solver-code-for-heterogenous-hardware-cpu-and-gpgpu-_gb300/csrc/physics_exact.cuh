@@ -9,16 +9,28 @@
 // algebraic rewriting) and the translation units that include this header
 // are compiled with --fmad=false.  With IEEE-correct division and square
 // root on the GPU this reproduces the reference's results to the last bit
-// except where libm functions differ (cbrt).
+// except where libm functions differ (cbrt).  Divisions that share a divisor
+// use one IEEE reciprocal and an exactly checked correction (exact_div.cuh,
+// `Over`): the same bits as the division, for fewer FP64 instructions.
 #pragma once
 
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include "exact_div.cuh"
+
 namespace cfd {
 namespace ex {
 
 __device__ __forceinline__ double sq(double x) { return x * x; }
+
+// Division of several numerators by one divisor b: Over(b)(x) == x / b, bit
+// for bit (exact_div.cuh); the reciprocal is computed once.
+struct Over {
+    double b, y;
+    __device__ __forceinline__ explicit Over(double divisor) : b(divisor), y(1.0 / divisor) {}
+    __device__ __forceinline__ double operator()(double x) const { return xdiv::div(x, b, y); }
+};
 
 // U_Q.cl:64-65
 __device__ __forceinline__ double enthalpy(double rho, double u, double v, double w, double p)
@@ -31,10 +43,11 @@ __device__ __forceinline__ void roe(double sb, double ub, double vb, double wb, 
                                     double vi, double wi, double hi, double r[5])
 {
     r[4] = sb * si;
-    r[0] = (sb * ub + si * ui) / (sb + si);
-    r[1] = (sb * vb + si * vi) / (sb + si);
-    r[2] = (sb * wb + si * wi) / (sb + si);
-    r[3] = (sb * hb + si * hi) / (sb + si);
+    const Over d(sb + si);
+    r[0] = d(sb * ub + si * ui);
+    r[1] = d(sb * vb + si * vi);
+    r[2] = d(sb * wb + si * wi);
+    r[3] = d(sb * hb + si * hi);
 }
 
 // WENO5 pair, Weno.cl:1056-1280; c[0..5] = left-2 .. right+2.
@@ -59,40 +72,65 @@ __device__ __forceinline__ void weno_pair(const double cc[6], double eps, double
     const double wm0 = (5.0 / 16.0) / (sq(eps + (ISm0)));
     const double wm1 = (5.0 / 8.0) / (sq(eps + (ISm1)));
     const double wm2 = (1.0 / 16.0) / (sq(eps + (ISm2)));
-    const double Wp0 = wp0 / (wp0 + wp1 + wp2), Wp1 = wp1 / (wp0 + wp1 + wp2), Wp2 = wp2 / (wp0 + wp1 + wp2);
-    const double Wm0 = wm0 / (wm0 + wm1 + wm2), Wm1 = wm1 / (wm0 + wm1 + wm2), Wm2 = wm2 / (wm0 + wm1 + wm2);
+    const Over sp(wp0 + wp1 + wp2), sm(wm0 + wm1 + wm2);
+    const double Wp0 = sp(wp0), Wp1 = sp(wp1), Wp2 = sp(wp2);
+    const double Wm0 = sm(wm0), Wm1 = sm(wm1), Wm2 = sm(wm2);
     pos = Wp0 * p0 + Wp1 * p1 + Wp2 * p2;
     neg = Wm0 * m0 + Wm1 * m1 + Wm2 * m2;
 }
 
-// Cartesian Euler fluxes of a face state, Weno.cl:2291-2507.
-__device__ __forceinline__ void cart_flux(const double q[5], double F[5], double E[5], double G[5])
+// The quotients by rho of a face state q (conservative) that its Cartesian
+// fluxes and lambda_5 divide by q[0]: q1^2/q0, q2^2/q0, q3^2/q0,
+// q1 q2/q0, q1 q3/q0, q2 q3/q0, q1/q0, q2/q0, q3/q0, q4/q0.
+struct StateQuot {
+    double k1, k2, k3, e12, e13, e23, v1, v2, v3, v4;
+};
+
+__device__ __forceinline__ StateQuot state_quot(const double q[5])
 {
-    const double k1 = (q[1] * q[1] / q[0]), k2 = (q[2] * q[2] / q[0]), k3 = (q[3] * q[3] / q[0]);
+    const Over d(q[0]);
+    StateQuot t;
+    t.k1 = d(q[1] * q[1]);
+    t.k2 = d(q[2] * q[2]);
+    t.k3 = d(q[3] * q[3]);
+    t.e12 = d(q[1] * q[2]);
+    t.e13 = d(q[1] * q[3]);
+    t.e23 = d(q[2] * q[3]);
+    t.v1 = d(q[1]);
+    t.v2 = d(q[2]);
+    t.v3 = d(q[3]);
+    t.v4 = d(q[4]);
+    return t;
+}
+
+// Cartesian Euler fluxes of a face state, Weno.cl:2291-2507.
+__device__ __forceinline__ void cart_flux(const double q[5], const StateQuot &t, double F[5], double E[5], double G[5])
+{
+    const double k1 = t.k1, k2 = t.k2, k3 = t.k3;
     const double pr = 0.4 * (q[4] - 0.5 * (k1 + k2 + k3));
     const double hq = (1.4 * q[4] - 0.2 * (k1 + k2 + k3));
     F[0] = q[1];
     F[1] = k1 + pr;
-    F[2] = (q[1] * q[2]) / q[0];
-    F[3] = (q[1] * q[3]) / q[0];
-    F[4] = hq * (q[1] / q[0]);
+    F[2] = t.e12;
+    F[3] = t.e13;
+    F[4] = hq * t.v1;
     E[0] = q[2];
-    E[1] = (q[1] * q[2]) / q[0];
+    E[1] = t.e12;
     E[2] = k2 + pr;
-    E[3] = (q[2] * q[3]) / q[0];
-    E[4] = hq * (q[2] / q[0]);
+    E[3] = t.e23;
+    E[4] = hq * t.v2;
     G[0] = q[3];
-    G[1] = (q[1] * q[3]) / q[0];
-    G[2] = (q[2] * q[3]) / q[0];
+    G[1] = t.e13;
+    G[2] = t.e23;
     G[3] = k3 + pr;
-    G[4] = hq * (q[3] / q[0]);
+    G[4] = hq * t.v3;
 }
 
 // lambda_5 of a face state, Weno.cl:2511-2583 element [4].
-__device__ __forceinline__ double lambda5(const double q[5], double mx, double my, double mz)
+__device__ __forceinline__ double lambda5(const double q[5], const StateQuot &t, double mx, double my, double mz)
 {
-    return (mx * (q[1] / q[0]) + my * (q[2] / q[0]) + mz * (q[3] / q[0]))
-           + sqrt(1.4 * 0.4 * ((q[4] / q[0]) - ((q[1] * q[1] + q[2] * q[2] + q[3] * q[3]) / (2.0 * (q[0] * q[0]))))
+    return (mx * t.v1 + my * t.v2 + mz * t.v3)
+           + sqrt(1.4 * 0.4 * (t.v4 - ((q[1] * q[1] + q[2] * q[2] + q[3] * q[3]) / (2.0 * (q[0] * q[0]))))
                   * (mx * mx + my * my + mz * mz));
 }
 
@@ -106,20 +144,23 @@ __device__ __forceinline__ void face_flux(const double pts[6][5], double mx, dou
     const double ru = r[0], rv = r[1], rw = r[2], rh = r[3], rrho = r[4];
     const double kk = sqrt(mx * mx + my * my + mz * mz);
     const double a = sqrt(0.4 * (rh - 0.5 * (ru * ru + rv * rv + rw * rw)));
-    const double kx = mx / kk, ky = my / kk, kz = mz / kk;
+    const Over dk(kk);
+    const double kx = dk(mx), ky = dk(my), kz = dk(mz);
     const double theta = kx * ru + ky * rv + kz * rw;
     const double phi_sq = 0.5 * 0.4 * (ru * ru + rv * rv + rw * rw);
     const double alpha = rrho / (sqrt(2.0) * a);
     const double beta = 1.0 / (sqrt(2.0) * rrho * a);
     double cpos[5], cneg[5];
     {
+        const Over da(a * a), dr(rrho);
+        const double f = da(phi_sq);
         const double Lm[5][5] = {
-            {kx * (1.0 - (phi_sq / (a * a))) - ((kz * rv - ky * rw) / rrho), kx * 0.4 * ru / (a * a),
-             (kx * 0.4 * rv / (a * a)) + (kz / rrho), (kx * 0.4 * rw / (a * a)) - (ky / rrho), -kx * 0.4 / (a * a)},
-            {ky * (1.0 - (phi_sq / (a * a))) - ((kx * rw - kz * ru) / rrho), (ky * 0.4 * ru / (a * a)) - kz / rrho,
-             ky * 0.4 * rv / (a * a), (ky * 0.4 * rw / (a * a)) + (kx / rrho), -ky * 0.4 / (a * a)},
-            {kz * (1.0 - (phi_sq / (a * a))) - ((ky * ru - kx * rv) / rrho), kz * 0.4 * ru / (a * a) + (ky / rrho),
-             kz * 0.4 * rv / (a * a) - (kx / rrho), kz * 0.4 * rw / (a * a), -kz * 0.4 / (a * a)},
+            {kx * (1.0 - f) - dr(kz * rv - ky * rw), da(kx * 0.4 * ru), da(kx * 0.4 * rv) + dr(kz),
+             da(kx * 0.4 * rw) - dr(ky), da(-kx * 0.4)},
+            {ky * (1.0 - f) - dr(kx * rw - kz * ru), da(ky * 0.4 * ru) - dr(kz), da(ky * 0.4 * rv),
+             da(ky * 0.4 * rw) + dr(kx), da(-ky * 0.4)},
+            {kz * (1.0 - f) - dr(ky * ru - kx * rv), da(kz * 0.4 * ru) + dr(ky), da(kz * 0.4 * rv) - dr(kx),
+             da(kz * 0.4 * rw), da(-kz * 0.4)},
             {beta * (phi_sq - theta * a), -beta * (0.4 * ru - kx * a), -beta * (0.4 * rv - ky * a),
              -beta * (0.4 * rw - kz * a), beta * 0.4},
             {beta * (phi_sq + theta * a), -beta * (0.4 * ru + kx * a), -beta * (0.4 * rv + ky * a),
@@ -136,14 +177,15 @@ __device__ __forceinline__ void face_flux(const double pts[6][5], double mx, dou
     }
     double qp[5], qn[5];
     {
+        const Over d4(0.4);
         const double R[5][5] = {
             {kx, ky, kz, alpha, alpha},
             {kx * ru, ky * ru - kz * rrho, kz * ru + ky * rrho, alpha * (ru + kx * a), alpha * (ru - kx * a)},
             {kx * rv + kz * rrho, ky * rv, kz * rv - kx * rrho, alpha * (rv + ky * a), alpha * (rv - ky * a)},
             {kx * rw - ky * rrho, ky * rw + kx * rrho, kz * rw, alpha * (rw + kz * a), alpha * (rw - kz * a)},
-            {((kx * phi_sq) / 0.4) + rrho * (kz * rv - ky * rw), ((ky * phi_sq) / 0.4) + rrho * (kx * rw - kz * ru),
-             ((kz * phi_sq) / 0.4) + rrho * (ky * ru - kx * rv), alpha * (((phi_sq + a * a) / (0.4)) + theta * a),
-             alpha * (((phi_sq + a * a) / (0.4)) - theta * a)}};
+            {d4(kx * phi_sq) + rrho * (kz * rv - ky * rw), d4(ky * phi_sq) + rrho * (kx * rw - kz * ru),
+             d4(kz * phi_sq) + rrho * (ky * ru - kx * rv), alpha * (d4(phi_sq + a * a) + theta * a),
+             alpha * (d4(phi_sq + a * a) - theta * a)}};
 #pragma unroll
         for (int q = 0; q < 5; ++q) {
             qp[q] = R[q][0] * (cpos[0]) + R[q][1] * (cpos[1]) + R[q][2] * (cpos[2]) + R[q][3] * (cpos[3])
@@ -152,15 +194,16 @@ __device__ __forceinline__ void face_flux(const double pts[6][5], double mx, dou
                     + R[q][4] * (cneg[4]);
         }
     }
-    const double lp = lambda5(qp, mx, my, mz);
-    const double ln = lambda5(qn, mx, my, mz);
+    const StateQuot tp = state_quot(qp), tn = state_quot(qn);
+    const double lp = lambda5(qp, tp, mx, my, mz);
+    const double ln = lambda5(qn, tn, mx, my, mz);
     double al = __longlong_as_double(0x7ff8000000000000ULL);   // NaN when neither branch holds (NaN input)
     if (fabs(lp) >= fabs(ln)) al = fabs(lp);
     else if (fabs(ln) >= fabs(lp)) al = fabs(ln);
     double Fp[5], Ep[5], Gp[5];
-    cart_flux(qp, Fp, Ep, Gp);
+    cart_flux(qp, tp, Fp, Ep, Gp);
     double Fn[5], En[5], Gn[5];
-    cart_flux(qn, Fn, En, Gn);
+    cart_flux(qn, tn, Fn, En, Gn);
 #pragma unroll
     for (int c = 0; c < 5; ++c) {
         const double fcp = DET_F * (mx * Fp[c] + my * Ep[c] + mz * Gp[c]);
