@@ -75,6 +75,9 @@ def parse_args(argv=None):
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     p.add_argument("--config", choices=("tgv128", "tgv64", "vortex64"), default="tgv128")
+    p.add_argument("--les", choices=("mts", "smagorinsky"), default="mts",
+                   help="SGS model of the TGV workloads: the reference's mixed time scale (parity) or "
+                        "Smagorinsky C_s = 0.1 (the model config 2 names)")
     p.add_argument("--cpu-steps", type=int, default=1, help="full steps timed for the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-mixed", action="store_true")
@@ -94,12 +97,18 @@ def parse_args(argv=None):
     return p.parse_args(argv)
 
 
-def make_case(config: str):
+def make_case(config: str, les: str = "mts"):
+    import dataclasses
     from cfd_gb300 import cases
     if config in ("tgv128", "tgv64"):
         n = 128 if config == "tgv128" else 64
-        return cases.taylor_green(n=n), {"workload": f"taylor_green_{n}^3_curvilinear_les", "grid": [n, n, n],
-                                         "re": 1600, "mach": 0.1, "les": "mts"}
+        c = cases.taylor_green(n=n)
+        cfg = {"workload": f"taylor_green_{n}^3_curvilinear_les", "grid": [n, n, n], "re": 1600, "mach": 0.1,
+               "les": les}
+        if les == "smagorinsky":   # config 2's model (C_s = 0.1); the reference implements MTS only
+            c.params = dataclasses.replace(c.params, les=2, smagorinsky_cs=0.1)
+            cfg["smagorinsky_cs"] = 0.1
+        return c, cfg
     return cases.isentropic_vortex(n=64), {"workload": "isentropic_vortex_64^3_periodic_inviscid",
                                            "grid": [64, 64, 64]}
 
@@ -216,7 +225,7 @@ def reference_arm(args):
     world, rank, local = dist_env()
     if rank != 0:
         return 0
-    case, cfg = make_case(args.config)
+    case, cfg = make_case(args.config, args.les)
     import oracle
     oracle.build()
     cores = oracle.lib().oracle_get_threads()
@@ -256,7 +265,7 @@ def gpu_arm(args):
     __graft_entry__.load_package()
     from cfd_gb300 import abi, runtime
 
-    case, cfg = make_case(args.config)
+    case, cfg = make_case(args.config, args.les)
     N = case.sd_node
     ctx = runtime.Context(local)
     stream = torch.cuda.Stream(device=local)

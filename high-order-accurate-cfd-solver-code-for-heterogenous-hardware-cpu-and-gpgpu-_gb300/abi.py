@@ -30,7 +30,7 @@ class CfdError(RuntimeError):
 class Params(C.Structure):
     _fields_ = [("mach", C.c_double), ("reynolds", C.c_double), ("prandtl", C.c_double), ("t_inf", C.c_double),
                 ("weno_eps", C.c_double), ("viscous", C.c_int32), ("les", C.c_int32), ("precision", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("reserved", C.c_int32), ("smagorinsky_cs", C.c_double)]
 
 
 class Geometry(C.Structure):

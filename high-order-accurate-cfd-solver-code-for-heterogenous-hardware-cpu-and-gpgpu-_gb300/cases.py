@@ -35,7 +35,9 @@ class Params:
     The reference hard-codes mach/reynolds/prandtl/t_inf in Viscous.cl:30-33
     (1.5, 500, 0.72, 273) and weno_eps in Weno.cl:59 (10e-8); Weno takes Mach
     as an argument (Weno.cl:36).  ``viscous=0`` zeroes Fv/Ev/Gv (inviscid
-    runs); ``les=0`` drops the mixed-time-scale SGS terms.
+    runs); ``les`` selects the SGS model: 0 none, 1 the reference's mixed
+    time scale, 2 Smagorinsky with ``smagorinsky_cs`` (no counterpart in the
+    reference).
     """
     mach: float = 1.5
     reynolds: float = 500.0
@@ -44,6 +46,7 @@ class Params:
     weno_eps: float = 1e-7
     viscous: int = 1
     les: int = 1
+    smagorinsky_cs: float = 0.1
 
 
 @dataclasses.dataclass

@@ -85,6 +85,7 @@ Phys make_phys(const cfd_params_t *p)
     P.eps = p->weno_eps;
     P.viscous = p->viscous;
     P.les = p->les;
+    P.cs = p->smagorinsky_cs;
     return P;
 }
 
@@ -158,6 +159,7 @@ void cfd_params_default(cfd_params_t *p)
     p->viscous = 1;
     p->les = 1;
     p->precision = CFD_PREC_FP64;
+    p->smagorinsky_cs = 0.1;
 }
 
 const char *cfd_status_string(cfd_status_t s)

@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(128) k_viscous(Phys P, const double *__restric
             const double *um = U + 5 * (size_t)idx[d][2], *up = U + 5 * (size_t)idx[d][4];
             KS[d] = ex::ks(Ui[c], Ui[0], um[c], um[0], up[c], up[0]);
         }
-        const ex::Visc V{P.mach, P.reynolds, P.prandtl, P.t_inf, P.les};
+        const ex::Visc V{P.mach, P.reynolds, P.prandtl, P.t_inf, P.les, P.cs};
         ex::viscous_node(dU, Ui, m, D, prim, KS, V, Fvn, Evn, Gvn, mu);
     }
     double *o;

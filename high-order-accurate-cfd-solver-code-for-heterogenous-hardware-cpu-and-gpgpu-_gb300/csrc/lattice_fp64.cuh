@@ -111,7 +111,7 @@ __device__ __forceinline__ void visc_node(const LatView &g, int n, int q)
     const double prim[5] = {g.prim9[LF_RHO * N + n], g.prim9[LF_U * N + n], g.prim9[LF_V * N + n],
                             g.prim9[LF_W * N + n], g.prim9[LF_P * N + n]};
     double Fv[5], Ev[5], Gv[5], mu;
-    const Visc Vp{g.P.mach, g.P.reynolds, g.P.prandtl, g.P.t_inf, g.P.les};
+    const Visc Vp{g.P.mach, g.P.reynolds, g.P.prandtl, g.P.t_inf, g.P.les, g.P.cs};
     viscous_node(dU, Ui, m, g.det[n], prim, KS, Vp, Fv, Ev, Gv, mu);
 #pragma unroll
     for (int c = 0; c < 5; ++c) {

@@ -162,7 +162,8 @@ __device__ __forceinline__ double weno_visc_deriv_ref(const double f[7], const i
 // Physical constants of one run.
 struct Phys {
     double mach, reynolds, prandtl, t_inf, eps;
-    int viscous, les;
+    int viscous, les;   // les: 0 none, 1 mixed time scale, 2 Smagorinsky
+    double cs;          // Smagorinsky C_s
 };
 
 // Viscous and SGS fluxes at one node from the derivatives of U along the
@@ -220,20 +221,27 @@ __device__ __forceinline__ void viscous_node_flux(const T dU[3][5], const T Ui[5
     const T txy = mr * sxy, txz = mr * sxz, tyz = mr * syz;
 
     T TXY = 0, TYZ = 0, TXZ = 0, TXX = 0, TYY = 0, TZZ = 0, HX = 0, HY = 0, HZ = 0, DX = 0, DY = 0, DZ = 0;
-    if (P.les) {  // mixed-time-scale SGS model, Viscous.cl:490-558
+    if (P.les) {  // SGS model: mixed time scale (Viscous.cl:490-558) or Smagorinsky
         const T C_MTS = T(0.03), C_T = T(10.0);
         const T s_xy = T(0.5) * sxy, s_yz = T(0.5) * syz, s_xz = T(0.5) * sxz;
-        const T mod = sqrt(T(2.0) * ((s_xy * s_xy + s_yz * s_yz + s_xz * s_xz)
-                                     + T(2.0 / 3.0) * (dudx * dudx + dvdy * dvdy + dwdz * dwdz)));
         T ed[3];
+        if (P.les == 2) {   // (C_s Delta)^2 |S|, |S| = sqrt(2 S_ij S_ij), Delta = det^(1/3) = 1/DEL
+            const T S = sqrt(T(2.0) * (dudx * dudx + dvdy * dvdy + dwdz * dwdz)
+                             + T(4.0) * (s_xy * s_xy + s_yz * s_yz + s_xz * s_xz));
+            const T ls = qdiv(T(P.cs), DEL);
+            ed[0] = ed[1] = ed[2] = (ls * ls) * S;
+        } else {
+            const T mod = sqrt(T(2.0) * ((s_xy * s_xy + s_yz * s_yz + s_xz * s_xz)
+                                         + T(2.0 / 3.0) * (dudx * dudx + dvdy * dvdy + dwdz * dwdz)));
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            const T sk = sqrt(KS[d]);
-            if (mod != T(0.0)) {
-                const T R = qdiv(DEL * mod, sk);
-                ed[d] = qdiv(C_MTS, T(1.0) + R * (T(1.0) / C_T)) * DEL * sk;
-            } else {
-                ed[d] = C_MTS * DEL * sk;
+            for (int d = 0; d < 3; ++d) {
+                const T sk = sqrt(KS[d]);
+                if (mod != T(0.0)) {
+                    const T R = qdiv(DEL * mod, sk);
+                    ed[d] = qdiv(C_MTS, T(1.0) + R * (T(1.0) / C_T)) * DEL * sk;
+                } else {
+                    ed[d] = C_MTS * DEL * sk;
+                }
             }
         }
         const T r2 = T(-2.0) * U0;

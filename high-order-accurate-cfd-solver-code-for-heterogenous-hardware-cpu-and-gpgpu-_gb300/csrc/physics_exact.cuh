@@ -231,7 +231,8 @@ __device__ __forceinline__ double central4(double fm2, double fm1, double fp1, d
 
 struct Visc {
     double mach, reynolds, prandtl, t_inf;
-    int les;
+    int les;       // 0 none, 1 mixed time scale, 2 Smagorinsky
+    double cs;     // Smagorinsky C_s
 };
 
 // Viscous.cl:439-631 at one node, in the reference's order.  dU[d][c],
@@ -291,7 +292,15 @@ __device__ __forceinline__ void viscous_node(const double dU[3][5], const double
                                               + (2.0 / 3.0) * (stress_xx * stress_xx + stress_yy * stress_yy + stress_zz * stress_zz)));
         const double DEL = (1.0 / cbrt(DET_I));
         double EDDY_x, EDDY_y, EDDY_z;
-        if (mod_stress != 0.0) {
+        if (P.les == 2) {
+            // Smagorinsky (no counterpart in the reference): (C_s Delta)^2 |S|,
+            // |S| = sqrt(2 S_ij S_ij), Delta = det^(1/3) (the cell size; det is
+            // the cell volume), in the reference's SGS terms below
+            const double S = sqrt(2.0 * (stress_xx * stress_xx + stress_yy * stress_yy + stress_zz * stress_zz)
+                                  + 4.0 * (stress_xy * stress_xy + stress_yz * stress_yz + stress_xz * stress_xz));
+            const double ls = P.cs * cbrt(DET_I);
+            EDDY_x = EDDY_y = EDDY_z = (ls * ls) * S;
+        } else if (mod_stress != 0.0) {
             const double Rx = (DEL * (mod_stress)) / sqrt(KSv[0]);
             const double Ry = (DEL * (mod_stress)) / sqrt(KSv[1]);
             const double Rz = (DEL * (mod_stress)) / sqrt(KSv[2]);

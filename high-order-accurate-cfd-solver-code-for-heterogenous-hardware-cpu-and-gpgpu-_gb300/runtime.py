@@ -35,6 +35,7 @@ def to_params(p) -> abi.Params:
     out.weno_eps = p.weno_eps
     out.viscous, out.les = int(p.viscous), int(p.les)
     out.precision = int(getattr(p, "precision", 0))
+    out.smagorinsky_cs = float(getattr(p, "smagorinsky_cs", 0.1))
     return out
 
 

@@ -129,9 +129,14 @@ typedef struct {
     double t_inf;
     double weno_eps;
     int32_t viscous;     /* 0: Fv = Ev = Gv = 0 (inviscid)                    */
-    int32_t les;         /* 0: drop the mixed-time-scale SGS terms            */
+    int32_t les;         /* SGS model: 0 none, 1 mixed time scale (the
+                          * reference, Viscous.cl:490-558), 2 Smagorinsky   */
     int32_t precision;   /* cfd_precision_t (solver objects only)             */
     int32_t reserved;
+    double smagorinsky_cs; /* C_s of les = 2 (default 0.1): eddy viscosity
+                            * (C_s det^(1/3))^2 |S|, |S| = sqrt(2 S_ij S_ij),
+                            * in the reference's SGS stress and heat-flux
+                            * terms; no counterpart in the reference */
 } cfd_params_t;
 
 void cfd_params_default(cfd_params_t *p);

@@ -34,7 +34,7 @@ _vp = C.c_void_p
 class OrParams(C.Structure):
     _fields_ = [("mach", C.c_double), ("reynolds", C.c_double), ("prandtl", C.c_double),
                 ("t_inf", C.c_double), ("weno_eps", C.c_double), ("viscous", C.c_int),
-                ("les", C.c_int)]
+                ("les", C.c_int), ("smagorinsky_cs", C.c_double)]
 
 
 class OrCase(C.Structure):
@@ -118,7 +118,8 @@ def _p(a: np.ndarray):
 
 
 def make_params(p) -> OrParams:
-    return OrParams(p.mach, p.reynolds, p.prandtl, p.t_inf, p.weno_eps, int(p.viscous), int(p.les))
+    return OrParams(p.mach, p.reynolds, p.prandtl, p.t_inf, p.weno_eps, int(p.viscous), int(p.les),
+                    float(getattr(p, "smagorinsky_cs", 0.1)))
 
 
 def make_case(arrays: dict, g_node: int, sd_node: int) -> OrCase:

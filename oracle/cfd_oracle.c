@@ -222,7 +222,15 @@ void oracle_viscous(int n_items, const or_params *prm, const or_col5 *U_C,
             const double mod_stress = sqrt(2.0 * ((stress_xy * stress_xy + stress_yz * stress_yz + stress_xz * stress_xz) + (2.0 / 3.0) * (stress_xx * stress_xx + stress_yy * stress_yy + stress_zz * stress_zz)));
             const double DEL = (1.0 / cbrt(DET_I));
             double EDDY_x, EDDY_y, EDDY_z;
-            if (mod_stress != 0.0) {
+            if (prm->les == 2) {
+                /* Smagorinsky, a builder addition (the reference implements only
+                 * MTS): (C_s Delta)^2 |S|, |S| = sqrt(2 S_ij S_ij), isotropic,
+                 * Delta = det^(1/3) (det is the cell volume). */
+                const double S = sqrt(2.0 * (stress_xx * stress_xx + stress_yy * stress_yy + stress_zz * stress_zz)
+                                      + 4.0 * (stress_xy * stress_xy + stress_yz * stress_yz + stress_xz * stress_xz));
+                const double ls = prm->smagorinsky_cs * cbrt(DET_I);
+                EDDY_x = EDDY_y = EDDY_z = (ls * ls) * S;
+            } else if (mod_stress != 0.0) {
                 const double Rx = (DEL * (mod_stress)) / sqrt(KS_x);
                 const double Ry = (DEL * (mod_stress)) / sqrt(KS_y);
                 const double Rz = (DEL * (mod_stress)) / sqrt(KS_z);

@@ -46,7 +46,8 @@ typedef struct {
     double t_inf;
     double weno_eps;
     int viscous;   /* 0: zero Fv/Ev/Gv after the Viscous pass (inviscid runs) */
-    int les;       /* 0: drop the mixed-time-scale SGS terms                   */
+    int les;       /* SGS model: 0 none, 1 mixed time scale (the reference), 2 Smagorinsky */
+    double smagorinsky_cs; /* C_s of les = 2 (a builder addition: no reference to pin it) */
 } or_params;
 
 /* A whole case in the reference layout.  Index 0 is the reference's dummy row;
