@@ -13,8 +13,6 @@
 
 namespace cfd {
 
-template <class T> __device__ __forceinline__ T sqr(T x) { return x * x; }
-
 // Quotient and reciprocal square root.  The float forms use the hardware
 // approximations (__fdividef: about 2 ulp for |b| < 2^126; rsqrtf); other
 // types compute them exactly.
