@@ -347,6 +347,7 @@ cfd_status_t cfd_batch_add(cfd_batch_t *b, const cfd_geometry_t *geom, const cfd
     v.per = 7;            // periodic in every direction
     v.loc8 = nullptr;
     v.locdirs = 0;
+    v.locflag = nullptr;
     v.row_of = nullptr;
     v.dt = del_t;
     v.dt_hi = (float)del_t;

@@ -47,6 +47,10 @@ struct LatView {
     // loc-code branches matter there; along the other directions every
     // branch of the reference is the central one
     int locdirs;
+    // bit d of locflag[n]: node n takes a non-central loc-code branch along d
+    // (a node in the band next to the ghost layers); null: every node of a
+    // locdir direction evaluates its branches (mixed form only)
+    const unsigned char *locflag;
     const int *row_of;         // node n -> reference row (null: row n + 1)
 };
 

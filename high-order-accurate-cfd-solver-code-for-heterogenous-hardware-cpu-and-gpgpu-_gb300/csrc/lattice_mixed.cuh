@@ -221,6 +221,7 @@ __device__ __forceinline__ void visc_node(const LatView &g, int n, int q)
     lat_ijk(g, n, i, j, k);
     float dU[3][5], KS[3], Ui[5];
     const bool ghost = LOC && lat_ghost(g, n);
+    const unsigned lflag = (LOC && g.locflag) ? g.locflag[n] : 7u;
 #pragma unroll
     for (int c = 0; c < 5; ++c) Ui[c] = W[c * N + n];
 #pragma unroll
@@ -230,7 +231,7 @@ __device__ __forceinline__ void visc_node(const LatView &g, int n, int q)
         if (ghost) {
 #pragma unroll
             for (int c = 0; c < 5; ++c) dU[d][c] = 0.0f;
-        } else if (!LOC || !lat_locdir(g, d)) {
+        } else if (!LOC || !lat_locdir(g, d) || !((lflag >> d) & 1u)) {
 #pragma unroll
             for (int c = 0; c < 5; ++c) {
                 const float *H = W + c * N, *L = W + (5 + c) * N;
@@ -352,13 +353,14 @@ __device__ __forceinline__ void update_node(const LatView &g, int n, int jst)
     }
     int i, j, k;
     lat_ijk(g, n, i, j, k);
+    const unsigned lflag = (LOC && g.locflag) ? g.locflag[n] : 7u;
     float Lf[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const int m1 = lat_step(g, i, j, k, d, -1);
 #pragma unroll
         for (int c = 0; c < 5; ++c) Lf[c] += g.Fh32[(d * 5 + c) * N + n] - g.Fh32[(d * 5 + c) * N + m1];
-        if (LOC && g.P.viscous && lat_locdir(g, d)) {
+        if (LOC && g.P.viscous && lat_locdir(g, d) && ((lflag >> d) & 1u)) {
             int s[7], L7[7];
 #pragma unroll
             for (int o = 0; o < 7; ++o) {

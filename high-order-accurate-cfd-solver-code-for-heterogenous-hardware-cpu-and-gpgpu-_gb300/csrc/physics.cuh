@@ -104,7 +104,7 @@ struct FaceEigen {
 // sequence and the last match wins: 1 one-sided backward, 2 one-sided
 // forward, 3/4 biased next to a boundary node, 5 central; 0 = no branch
 // (the derivative is 0).
-__device__ __forceinline__ int visc_branch(const int L[7])
+__host__ __device__ __forceinline__ int visc_branch(const int L[7])
 {
     const int L0 = L[3];
     int b = 0;
@@ -121,7 +121,7 @@ __device__ __forceinline__ int visc_branch(const int L[7])
 // central unless a one-sided or biased branch matches.  The reference has
 // no branch for a boundary node away from ghosts in a direction (its value
 // is uninitialised there); the central form is used.
-__device__ __forceinline__ int weno_visc_branch(const int L[7])
+__host__ __device__ __forceinline__ int weno_visc_branch(const int L[7])
 {
     const int L0 = L[3];
     int b = 5;

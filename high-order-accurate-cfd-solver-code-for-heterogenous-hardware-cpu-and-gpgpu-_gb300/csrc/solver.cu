@@ -165,6 +165,34 @@ cfd_status_t create_structured(cfd_solver *s, const cfd_geometry_t *g)
         unsigned char *loc8;
         if ((st = dalloc_t(s, N, &loc8)) || (st = upload(s, loc8, s->map.loc.data(), N))) return st;
         S.loc8 = loc8;
+        if (s->mixed) {   // the nodes that take a non-central loc-code branch (LatView::locflag)
+            std::vector<unsigned char> flag(N, 0);
+            const LatticeMap &m = s->map;
+            for (int k = 0; k < m.nk; ++k)
+                for (int j = 0; j < m.nj; ++j)
+                    for (int i = 0; i < m.ni; ++i) {
+                        const int c[3] = {i, j, k};
+                        unsigned char f = 0;
+                        for (int d = 0; d < 3; ++d) {
+                            if (!((m.locdirs >> d) & 1)) continue;
+                            const int ext = m.extent(d);
+                            const bool per = (m.per >> d) & 1;
+                            int L7[7];
+                            for (int o = 0; o < 7; ++o) {
+                                int x = c[d] + o - 3;
+                                x = per ? (x + ext) % ext : (x < 0 ? 0 : (x >= ext ? ext - 1 : x));
+                                int cc[3] = {i, j, k};
+                                cc[d] = x;
+                                L7[o] = m.loc[(size_t)cc[0] + (size_t)m.ni * (cc[1] + (size_t)m.nj * cc[2])];
+                            }
+                            if (visc_branch(L7) != 5 || weno_visc_branch(L7) != 5) f |= (unsigned char)(1u << d);
+                        }
+                        flag[(size_t)i + (size_t)m.ni * (j + (size_t)m.nj * k)] = f;
+                    }
+            unsigned char *locflag;
+            if ((st = dalloc_t(s, N, &locflag)) || (st = upload(s, locflag, flag.data(), N))) return st;
+            S.locflag = locflag;
+        }
     }
     if (s->mixed) {
         mixed_geometry(S);

@@ -46,6 +46,7 @@ struct StructuredLaunch {
     int per = 7;
     const unsigned char *loc8 = nullptr;
     int locdirs = 0;
+    const unsigned char *locflag = nullptr;   // LatView::locflag
     const int *row_of = nullptr;
 };
 
@@ -110,6 +111,7 @@ inline LatView make_view(const StructuredLaunch &S, double dt, double *Lout)
     g.per = S.per;
     g.loc8 = S.loc8;
     g.locdirs = S.locdirs;
+    g.locflag = S.locflag;
     g.row_of = S.row_of;
     return g;
 }
