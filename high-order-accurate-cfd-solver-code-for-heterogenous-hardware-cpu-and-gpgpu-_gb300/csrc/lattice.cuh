@@ -49,7 +49,7 @@ struct LatView {
     int locdirs;
     // bit d of locflag[n]: node n takes a non-central loc-code branch along d
     // (a node in the band next to the ghost layers); null: every node of a
-    // locdir direction evaluates its branches (mixed form only)
+    // locdir direction evaluates its branches
     const unsigned char *locflag;
     const int *row_of;         // node n -> reference row (null: row n + 1)
 };

@@ -78,6 +78,9 @@ __device__ __forceinline__ void visc_node(const LatView &g, int n, int q)
     lat_ijk(g, n, i, j, k);
     double dU[3][5], KS[3], Ui[5];
     const bool ghost = lat_ghost(g, n);
+    // nodes outside the loc-code band take the central branch (the same
+    // expression as the reference's central branch: the same bits)
+    const unsigned lflag = g.locflag ? g.locflag[n] : 7u;
 #pragma unroll
     for (int c = 0; c < 5; ++c) Ui[c] = Uj[c * N + n];
 #pragma unroll
@@ -87,7 +90,7 @@ __device__ __forceinline__ void visc_node(const LatView &g, int n, int q)
         if (ghost) {
 #pragma unroll
             for (int c = 0; c < 5; ++c) dU[d][c] = 0.0;
-        } else if (!lat_locdir(g, d)) {
+        } else if (!lat_locdir(g, d) || !((lflag >> d) & 1u)) {
 #pragma unroll
             for (int c = 0; c < 5; ++c)
                 dU[d][c] = central4(Uj[c * N + m2], Uj[c * N + m1], Uj[c * N + p1], Uj[c * N + p2]);
@@ -185,12 +188,13 @@ __device__ __forceinline__ void update_node(const LatView &g, int n, int jst, bo
     int i, j, k;
     lat_ijk(g, n, i, j, k);
     double dflux[3][5], dvis[3][5];
+    const unsigned lflag = g.locflag ? g.locflag[n] : 7u;   // as in visc_node
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const int m1 = lat_step(g, i, j, k, d, -1);
 #pragma unroll
         for (int c = 0; c < 5; ++c) dflux[d][c] = g.Fh[(d * 5 + c) * N + n] - g.Fh[(d * 5 + c) * N + m1];
-        if (g.P.viscous && lat_locdir(g, d)) {
+        if (g.P.viscous && lat_locdir(g, d) && ((lflag >> d) & 1u)) {
             int s[7], L[7];
             loc_line(g, i, j, k, d, s, L);
             const double *Vd = g.V + (size_t)d * 5 * N;

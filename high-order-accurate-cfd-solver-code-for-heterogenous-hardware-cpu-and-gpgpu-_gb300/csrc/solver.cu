@@ -165,7 +165,7 @@ cfd_status_t create_structured(cfd_solver *s, const cfd_geometry_t *g)
         unsigned char *loc8;
         if ((st = dalloc_t(s, N, &loc8)) || (st = upload(s, loc8, s->map.loc.data(), N))) return st;
         S.loc8 = loc8;
-        if (s->mixed) {   // the nodes that take a non-central loc-code branch (LatView::locflag)
+        {   // the nodes that take a non-central loc-code branch (LatView::locflag)
             std::vector<unsigned char> flag(N, 0);
             const LatticeMap &m = s->map;
             for (int k = 0; k < m.nk; ++k)
