@@ -14,7 +14,9 @@ struct Ops {
     static __device__ __forceinline__ void visc(const LatView &g, int n, int q) { ex::visc_node(g, n, q); }
     static __device__ __forceinline__ void mu(const LatView &g, int n, int q) { ex::mu_node(g, n, q); }
     template <int D>
-    static __device__ __forceinline__ void face(const LatView &g, int n) { ex::face_node<D>(g, n); }
+    // plain divisions: in the persistent batched kernel the shared
+    // reciprocals measured 5 % slower (same bits either way)
+    static __device__ __forceinline__ void face(const LatView &g, int n) { ex::face_node<D, false>(g, n); }
     static __device__ __forceinline__ void update(const LatView &g, int n, int j) { ex::update_node(g, n, j, true); }
 };
 

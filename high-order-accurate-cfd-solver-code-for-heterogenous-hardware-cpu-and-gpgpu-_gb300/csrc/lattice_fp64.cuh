@@ -135,8 +135,9 @@ __device__ __forceinline__ void mu_node(const LatView &g, int n, int q)
 }
 
 // Face n+1/2 along D: Roe average of the two nodes, LLF face flux and the
-// 6th-order correction (Weno.cl:336-3058 for that face, once).
-template <int D>
+// 6th-order correction (Weno.cl:336-3058 for that face, once).  SD: shared
+// reciprocals for divisions by one divisor (physics_exact.cuh Over).
+template <int D, bool SD = true>
 __device__ __forceinline__ void face_node(const LatView &g, int n)
 {
     const int N = g.N;
@@ -154,11 +155,11 @@ __device__ __forceinline__ void face_node(const LatView &g, int n)
     double r[5];
     {
         const int l = s[2], rr = s[3];   // node (left) and its +D neighbour
-        roe(g.sh[rr], g.prim9[LF_U * N + rr], g.prim9[LF_V * N + rr], g.prim9[LF_W * N + rr], g.sh[N + rr], g.sh[l],
-            g.prim9[LF_U * N + l], g.prim9[LF_V * N + l], g.prim9[LF_W * N + l], g.sh[N + l], r);
+        roe<SD>(g.sh[rr], g.prim9[LF_U * N + rr], g.prim9[LF_V * N + rr], g.prim9[LF_W * N + rr], g.sh[N + rr],
+                g.sh[l], g.prim9[LF_U * N + l], g.prim9[LF_V * N + l], g.prim9[LF_W * N + l], g.sh[N + l], r);
     }
     double Fhat[5];
-    face_flux(pts, g.fm[(D * 3 + 0) * N + n], g.fm[(D * 3 + 1) * N + n], g.fm[(D * 3 + 2) * N + n], g.fdet[D * N + n],
+    face_flux<SD>(pts, g.fm[(D * 3 + 0) * N + n], g.fm[(D * 3 + 1) * N + n], g.fm[(D * 3 + 2) * N + n], g.fdet[D * N + n],
               r, g.P.eps, Fhat);
     const double *NF = g.FEG + (size_t)D * 5 * N;
 #pragma unroll

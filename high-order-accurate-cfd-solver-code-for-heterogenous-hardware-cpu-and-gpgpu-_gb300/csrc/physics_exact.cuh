@@ -24,12 +24,25 @@ namespace ex {
 
 __device__ __forceinline__ double sq(double x) { return x * x; }
 
-// Division of several numerators by one divisor b: Over(b)(x) == x / b, bit
-// for bit (exact_div.cuh); the reciprocal is computed once.
-struct Over {
+// Division of several numerators by one divisor b: Over<true>(b)(x) == x / b,
+// bit for bit, with the reciprocal computed once (exact_div.cuh);
+// Over<false> divides each numerator (the same bits; faster where the
+// kernel's occupancy hides the division latency, e.g. the batched form).
+template <bool SHARED>
+struct Over;
+
+template <>
+struct Over<true> {
     double b, y;
     __device__ __forceinline__ explicit Over(double divisor) : b(divisor), y(1.0 / divisor) {}
     __device__ __forceinline__ double operator()(double x) const { return xdiv::div(x, b, y); }
+};
+
+template <>
+struct Over<false> {
+    double b;
+    __device__ __forceinline__ explicit Over(double divisor) : b(divisor) {}
+    __device__ __forceinline__ double operator()(double x) const { return x / b; }
 };
 
 // U_Q.cl:64-65
@@ -39,11 +52,12 @@ __device__ __forceinline__ double enthalpy(double rho, double u, double v, doubl
 }
 
 // U_Q.cl:60-109 for one face: {u, v, w, h, rho}; (sb,...) the neighbour.
+template <bool SD = true>
 __device__ __forceinline__ void roe(double sb, double ub, double vb, double wb, double hb, double si, double ui,
                                     double vi, double wi, double hi, double r[5])
 {
     r[4] = sb * si;
-    const Over d(sb + si);
+    const Over<SD> d(sb + si);
     r[0] = d(sb * ub + si * ui);
     r[1] = d(sb * vb + si * vi);
     r[2] = d(sb * wb + si * wi);
@@ -51,6 +65,7 @@ __device__ __forceinline__ void roe(double sb, double ub, double vb, double wb, 
 }
 
 // WENO5 pair, Weno.cl:1056-1280; c[0..5] = left-2 .. right+2.
+template <bool SD = true>
 __device__ __forceinline__ void weno_pair(const double cc[6], double eps, double &pos, double &neg)
 {
     const double *c = cc + 2;   // c[0] = left node of the face
@@ -72,7 +87,7 @@ __device__ __forceinline__ void weno_pair(const double cc[6], double eps, double
     const double wm0 = (5.0 / 16.0) / (sq(eps + (ISm0)));
     const double wm1 = (5.0 / 8.0) / (sq(eps + (ISm1)));
     const double wm2 = (1.0 / 16.0) / (sq(eps + (ISm2)));
-    const Over sp(wp0 + wp1 + wp2), sm(wm0 + wm1 + wm2);
+    const Over<SD> sp(wp0 + wp1 + wp2), sm(wm0 + wm1 + wm2);
     const double Wp0 = sp(wp0), Wp1 = sp(wp1), Wp2 = sp(wp2);
     const double Wm0 = sm(wm0), Wm1 = sm(wm1), Wm2 = sm(wm2);
     pos = Wp0 * p0 + Wp1 * p1 + Wp2 * p2;
@@ -86,9 +101,10 @@ struct StateQuot {
     double k1, k2, k3, e12, e13, e23, v1, v2, v3, v4;
 };
 
+template <bool SD = true>
 __device__ __forceinline__ StateQuot state_quot(const double q[5])
 {
-    const Over d(q[0]);
+    const Over<SD> d(q[0]);
     StateQuot t;
     t.k1 = d(q[1] * q[1]);
     t.k2 = d(q[2] * q[2]);
@@ -138,13 +154,14 @@ __device__ __forceinline__ double lambda5(const double q[5], const StateQuot &t,
 // face metric and Roe state r = {u,v,w,h,rho}, projection of the six stencil
 // points pts (left-2 .. right+2), WENO5, back-projection, contravariant
 // fluxes x face det, lambda_5 LLF.
+template <bool SD = true>
 __device__ __forceinline__ void face_flux(const double pts[6][5], double mx, double my, double mz, double DET_F,
                                           const double r[5], double eps, double Fhat[5])
 {
     const double ru = r[0], rv = r[1], rw = r[2], rh = r[3], rrho = r[4];
     const double kk = sqrt(mx * mx + my * my + mz * mz);
     const double a = sqrt(0.4 * (rh - 0.5 * (ru * ru + rv * rv + rw * rw)));
-    const Over dk(kk);
+    const Over<SD> dk(kk);
     const double kx = dk(mx), ky = dk(my), kz = dk(mz);
     const double theta = kx * ru + ky * rv + kz * rw;
     const double phi_sq = 0.5 * 0.4 * (ru * ru + rv * rv + rw * rw);
@@ -152,7 +169,7 @@ __device__ __forceinline__ void face_flux(const double pts[6][5], double mx, dou
     const double beta = 1.0 / (sqrt(2.0) * rrho * a);
     double cpos[5], cneg[5];
     {
-        const Over da(a * a), dr(rrho);
+        const Over<SD> da(a * a), dr(rrho);
         const double f = da(phi_sq);
         const double Lm[5][5] = {
             {kx * (1.0 - f) - dr(kz * rv - ky * rw), da(kx * 0.4 * ru), da(kx * 0.4 * rv) + dr(kz),
@@ -172,12 +189,12 @@ __device__ __forceinline__ void face_flux(const double pts[6][5], double mx, dou
             for (int o = 0; o < 6; ++o)
                 cv[o] = Lm[q][0] * pts[o][0] + Lm[q][1] * pts[o][1] + Lm[q][2] * pts[o][2] + Lm[q][3] * pts[o][3]
                         + Lm[q][4] * pts[o][4];
-            weno_pair(cv, eps, cpos[q], cneg[q]);
+            weno_pair<SD>(cv, eps, cpos[q], cneg[q]);
         }
     }
     double qp[5], qn[5];
     {
-        const Over d4(0.4);
+        const Over<SD> d4(0.4);
         const double R[5][5] = {
             {kx, ky, kz, alpha, alpha},
             {kx * ru, ky * ru - kz * rrho, kz * ru + ky * rrho, alpha * (ru + kx * a), alpha * (ru - kx * a)},
@@ -194,7 +211,7 @@ __device__ __forceinline__ void face_flux(const double pts[6][5], double mx, dou
                     + R[q][4] * (cneg[4]);
         }
     }
-    const StateQuot tp = state_quot(qp), tn = state_quot(qn);
+    const StateQuot tp = state_quot<SD>(qp), tn = state_quot<SD>(qn);
     const double lp = lambda5(qp, tp, mx, my, mz);
     const double ln = lambda5(qn, tn, mx, my, mz);
     double al = __longlong_as_double(0x7ff8000000000000ULL);   // NaN when neither branch holds (NaN input)
