@@ -263,12 +263,17 @@ cfd_status_t cfd_ctx_set_rows(cfd_ctx_t *ctx, int32_t n_rows)
         }
         ctx->d_face = nullptr;
         ctx->face_rows = 0;
-        if (cudaMalloc(&ctx->d_face, (size_t)n_rows * 15 * sizeof(double)) == cudaSuccess)
-            ctx->face_rows = n_rows;
-        else {
-            cudaGetLastError();
-            ctx->d_face = nullptr;
+        void *buf = nullptr;
+        if (cudaMalloc(&buf, face_scratch_bytes(n_rows)) == cudaSuccess) {
+            double *f = static_cast<double *>(buf);
+            if (cudaMemset(face_stamps(f, n_rows), 0, (size_t)n_rows * 3 * sizeof(unsigned)) == cudaSuccess) {
+                ctx->d_face = f;
+                ctx->face_rows = n_rows;
+            } else {
+                cudaFree(buf);
+            }
         }
+        cudaGetLastError();   // a failed allocation only disables the sharing
     }
     return CFD_OK;
 }
@@ -396,7 +401,8 @@ cfd_status_t cfd_weno(cfd_ctx_t *ctx, int32_t j, double Mach, double del_t, cons
                 (const double *)a[6].dev, (const double *)a[7].dev, (const double *)a[8].dev,
                 (const double *)a[9].dev, (const double *)a[10].dev, (const double *)a[11].dev,
                 (const double *)a[12].dev, (const double *)a[13].dev, (const double *)a[14].dev, (double *)a[15].dev,
-                n_items, ctx->n_rows, ctx->d_flags, L_out ? (double *)l[0].dev : nullptr, face, ctx->face_rows);
+                n_items, ctx->n_rows, ctx->d_flags, L_out ? (double *)l[0].dev : nullptr, face, ctx->face_rows,
+                next_face_gen(ctx->face_gen));
     ctx->launches += weno_launches(face, ctx->face_rows, n_items) - 1;
     s = stage_out(ctx, a, 16, after_launch(ctx, "cfd_weno launch"));
     return L_out ? stage_out(ctx, l, 1, s) : s;
@@ -439,7 +445,8 @@ cfd_status_t cfd_rk3_step(cfd_ctx_t *ctx, double Mach, double del_t, const cfd_d
             launch_viscous(ctx->stream, P, U[j], F_, E_, G_, Fv_, Ev_, Gv_, grid, met, dd, flow, g_node + 1,
                            ctx->n_rows, ctx->d_flags);
             launch_weno(ctx->stream, P, j, Mach, del_t, dt_, dd, U[0], U[1], U[2], grid, Q, met, roe, Fv_, Ev_, Gv_,
-                        F_, E_, G_, flow, sd_node + 1, ctx->n_rows, ctx->d_flags, nullptr, face, ctx->face_rows);
+                        F_, E_, G_, flow, sd_node + 1, ctx->n_rows, ctx->d_flags, nullptr, face, ctx->face_rows,
+                        next_face_gen(ctx->face_gen));
             n += 1 + weno_launches(face, ctx->face_rows, sd_node + 1);
             if (bc) {
                 bc_apply_aos(ctx->stream, bc->dev, flow, Mach);

@@ -15,11 +15,13 @@
 // Weno evaluates both faces of each direction at every row, so every
 // interior face is computed twice from identical inputs (as row n's +1/2
 // face and as row n+1's -1/2 face).  With a scratch buffer the launch is
-// split: k_weno_plus computes each row's +1/2 faces once, and k_weno<true>
-// takes a row's -1/2 face from its minus neighbour's +1/2 face wherever
-// every input of the two evaluations is bit-identical (stencil rows, face
-// metric, face det, Roe state); elsewhere it computes the face itself.
-// The results are the same bits either way.
+// split: k_weno_plus computes each row's +1/2 face once and, where its plus
+// neighbour p has this row as its minus neighbour and every input of p's
+// -1/2 face is bit-identical (then so are the stencil rows; face metric,
+// face det and Roe state are compared), also stores it as p's -1/2 face,
+// stamped with the call's generation; k_weno<true> takes a row's -1/2 face
+// from there when stamped, else computes it itself.  The results are the
+// same bits either way.
 #include "internal.h"
 #include "physics_exact.cuh"
 
@@ -242,14 +244,20 @@ __device__ __forceinline__ bool plus_line(const int *grid, int n, int n_rows, in
     return true;
 }
 
+__device__ __forceinline__ bool same_bits(double a, double b) { return __double_as_longlong(a) == __double_as_longlong(b); }
+
 // +1/2 face of every row gid < n_items along d = blockIdx.y whose stencil
-// stays in the table: Fp[(d*5 + c)*ld + gid].
+// stays in the table: Fp[(d*5 + c)*ld + gid]; also p's -1/2 face
+// Fm[(d*5 + c)*ld + p] with stamp[d*ld + p] = gen for the plus neighbour p
+// whose minus neighbour is gid, when p's face data are gid's bit for bit.
 __global__ void __launch_bounds__(128, 2) k_weno_plus(Phys P, const double *__restrict__ deter,
                                                        const int *__restrict__ grid, const double *__restrict__ Q,
                                                        const double *__restrict__ metric,
                                                        const double *__restrict__ roe, const double *__restrict__ F,
                                                        const double *__restrict__ E, const double *__restrict__ G,
-                                                       int n_items, int n_rows, double *__restrict__ Fp, long long ld)
+                                                       int n_items, int n_rows, double *__restrict__ Fp,
+                                                       double *__restrict__ Fm, unsigned *__restrict__ stamp,
+                                                       unsigned gen, long long ld)
 {
     const int gid = blockIdx.x * blockDim.x + threadIdx.x;
     const int d = blockIdx.y;
@@ -260,39 +268,25 @@ __global__ void __launch_bounds__(128, 2) k_weno_plus(Phys P, const double *__re
     face_side(P, gid, d, 0, st, deter, Q, metric, roe, d == 0 ? F : (d == 1 ? E : G), Fh);
 #pragma unroll
     for (int c = 0; c < 5; ++c) Fp[(d * 5 + c) * ld + gid] = Fh[c];
-}
-
-__device__ __forceinline__ bool same_bits(double a, double b) { return __double_as_longlong(a) == __double_as_longlong(b); }
-
-// Whether row gid's -1/2 face along d is the +1/2 face k_weno_plus computed
-// for n = its minus neighbour: n < n_items, n's stencil (offsets -2..3)
-// is gid's (offsets -3..2), and the face metric, face det and Roe state
-// are the same bits.
-__device__ __forceinline__ bool minus_face_is_plus_of(const int *grid, int gid, int d, const int idx[7], int n_items,
-                                                      int n_rows, const double *__restrict__ deter,
-                                                      const double *__restrict__ metric,
-                                                      const double *__restrict__ roe)
-{
-    const int n = idx[2];
-    if ((unsigned)n >= (unsigned)n_items) return false;
-    int st[6];
-    if (!plus_line(grid, n, n_rows, d, st)) return false;
+    const int p = st[3];
+    if ((unsigned)p >= (unsigned)n_items || grid_nb(grid, p, minus_slot(d)) != gid) return;
+    // p's -1/2 face reads metric block 2+2d, DETERM 2d+1 and ROE block d+3 of p
+    const double *fg = metric + 63 * (size_t)gid + 9 * (1 + 2 * d) + 3 * d;
+    const double *fp = metric + 63 * (size_t)p + 9 * (2 + 2 * d) + 3 * d;
+    const double *rg = roe + 36 * (size_t)gid + 6 * d, *rp = roe + 36 * (size_t)p + 6 * (d + 3);
+    if (same_bits(fg[0], fp[0]) && same_bits(fg[1], fp[1]) && same_bits(fg[2], fp[2])
+        && same_bits(deter[6 * (size_t)gid + 2 * d], deter[6 * (size_t)p + 2 * d + 1]) && same_bits(rg[0], rp[0])
+        && same_bits(rg[1], rp[1]) && same_bits(rg[2], rp[2]) && same_bits(rg[4], rp[4]) && same_bits(rg[5], rp[5])) {
 #pragma unroll
-    for (int k = 0; k < 6; ++k)
-        if (st[k] != idx[k]) return false;
-    const double *fg = metric + 63 * (size_t)gid + 9 * (2 + 2 * d) + 3 * d;
-    const double *fn = metric + 63 * (size_t)n + 9 * (1 + 2 * d) + 3 * d;
-    if (!same_bits(fg[0], fn[0]) || !same_bits(fg[1], fn[1]) || !same_bits(fg[2], fn[2])) return false;
-    if (!same_bits(deter[6 * (size_t)gid + 2 * d + 1], deter[6 * (size_t)n + 2 * d])) return false;
-    const double *rg = roe + 36 * (size_t)gid + 6 * (d + 3), *rn = roe + 36 * (size_t)n + 6 * d;
-    return same_bits(rg[0], rn[0]) && same_bits(rg[1], rn[1]) && same_bits(rg[2], rn[2]) && same_bits(rg[4], rn[4])
-           && same_bits(rg[5], rn[5]);
+        for (int c = 0; c < 5; ++c) Fm[(d * 5 + c) * ld + p] = Fh[c];
+        stamp[d * ld + p] = gen;
+    }
 }
 
 // Weno.cl:36-3137: per row, both faces of each direction from the row's own
 // face data (metric blocks, DETERM, ROE_AVERAGING), as the reference does.
-// REUSE: the +1/2 faces come from k_weno_plus (Fp) and the -1/2 faces from
-// the minus neighbour's entry where minus_face_is_plus_of holds.
+// REUSE: the +1/2 faces come from k_weno_plus (Fp), the -1/2 faces from Fm
+// where stamped with this call's generation.
 template <bool REUSE>
 __global__ void __launch_bounds__(128) k_weno(Phys P, int j, double mach, double dt, const double *__restrict__ deter,
                                               const double *__restrict__ det, double *__restrict__ U0,
@@ -303,7 +297,9 @@ __global__ void __launch_bounds__(128) k_weno(Phys P, int j, double mach, double
                                               const double *__restrict__ Gv, const double *__restrict__ F,
                                               const double *__restrict__ E, const double *__restrict__ G,
                                               double *__restrict__ flow, int n_items, int n_rows, unsigned *flags,
-                                              double *__restrict__ L_out, const double *__restrict__ Fp, long long ld)
+                                              double *__restrict__ L_out, const double *__restrict__ Fp,
+                                              const double *__restrict__ Fm, const unsigned *__restrict__ stamp,
+                                              unsigned gen, long long ld)
 {
     const int gid = blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= n_items) return;
@@ -321,10 +317,9 @@ __global__ void __launch_bounds__(128) k_weno(Phys P, int j, double mach, double
         if (REUSE) {
 #pragma unroll
             for (int c = 0; c < 5; ++c) Fh[0][c] = Fp[(d * 5 + c) * ld + gid];
-            if (minus_face_is_plus_of(grid, gid, d, idx[d], n_items, n_rows, deter, metric, roe)) {
-                const int n = idx[d][2];
+            if (stamp[d * ld + gid] == gen) {
 #pragma unroll
-                for (int c = 0; c < 5; ++c) Fh[1][c] = Fp[(d * 5 + c) * ld + n];
+                for (int c = 0; c < 5; ++c) Fh[1][c] = Fm[(d * 5 + c) * ld + gid];
             } else {
                 face_side(P, gid, d, 1, idx[d], deter, Q, metric, roe, NF, Fh[1]);
             }
@@ -401,17 +396,20 @@ void launch_weno(cudaStream_t st, const Phys &P, int j, double mach, double dt, 
                  const double *det, double *U0, double *U1, double *U2, const int *grid, const double *Q,
                  const double *metric, const double *roe, const double *Fv, const double *Ev, const double *Gv,
                  const double *F, const double *E, const double *G, double *flow, int n_items, int n_rows,
-                 unsigned *flags, double *L_out, double *face_scratch, long long scratch_rows)
+                 unsigned *flags, double *L_out, double *face_scratch, long long scratch_rows, unsigned gen)
 {
     const unsigned nb = blocks_for(n_items, 128);
     if (face_scratch && scratch_rows >= n_items) {
-        k_weno_plus<<<dim3(nb, 3), 128, 0, st>>>(P, deter, grid, Q, metric, roe, F, E, G, n_items, n_rows,
-                                                 face_scratch, scratch_rows);
+        const long long ld = scratch_rows;
+        double *Fp = face_scratch, *Fm = face_scratch + 15 * ld;
+        unsigned *stamp = face_stamps(face_scratch, ld);
+        k_weno_plus<<<dim3(nb, 3), 128, 0, st>>>(P, deter, grid, Q, metric, roe, F, E, G, n_items, n_rows, Fp, Fm,
+                                                 stamp, gen, ld);
         k_weno<true><<<nb, 128, 0, st>>>(P, j, mach, dt, deter, det, U0, U1, U2, grid, Q, metric, roe, Fv, Ev, Gv, F, E,
-                                         G, flow, n_items, n_rows, flags, L_out, face_scratch, scratch_rows);
+                                         G, flow, n_items, n_rows, flags, L_out, Fp, Fm, stamp, gen, ld);
     } else {
         k_weno<false><<<nb, 128, 0, st>>>(P, j, mach, dt, deter, det, U0, U1, U2, grid, Q, metric, roe, Fv, Ev, Gv, F,
-                                          E, G, flow, n_items, n_rows, flags, L_out, nullptr, 0);
+                                          E, G, flow, n_items, n_rows, flags, L_out, nullptr, nullptr, nullptr, 0u, 0);
     }
 }
 

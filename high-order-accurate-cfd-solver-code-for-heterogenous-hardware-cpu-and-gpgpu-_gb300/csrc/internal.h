@@ -33,8 +33,9 @@ struct cfd_ctx {
     std::string last_error;
     // cfd_weno's face scratch (15 doubles per row, allocated by
     // cfd_ctx_set_rows; null: each row evaluates both faces itself)
-    double *d_face = nullptr;
+    double *d_face = nullptr;   // face_scratch_bytes(face_rows)
     long long face_rows = 0;
+    unsigned face_gen = 0;
     bool face_reuse = true;
     // device mirrors of host buffers handed to the kernel entry points:
     // host pointer -> (device buffer, bytes)
@@ -89,9 +90,20 @@ void launch_weno(cudaStream_t st, const Phys &P, int j, double mach, double dt, 
                  const double *det, double *U0, double *U1, double *U2, const int *grid, const double *Q,
                  const double *metric, const double *roe, const double *Fv, const double *Ev, const double *Gv,
                  const double *F, const double *E, const double *G, double *flow, int n_items, int n_rows,
-                 unsigned *flags, double *L_out, double *face_scratch, long long scratch_rows);
-// Kernels one launch_weno issues: 2 with a face scratch of >= n_items rows
-// (15 doubles per row), else 1.
+                 unsigned *flags, double *L_out, double *face_scratch, long long scratch_rows, unsigned gen);
+// Face scratch of launch_weno for `rows` rows: +1/2 faces [3][5][rows] and
+// -1/2 faces [3][5][rows] (doubles), then generation stamps [3][rows]
+// (unsigned, zero when allocated).  gen: a value new to the scratch on every
+// call (next_face_gen).
+inline size_t face_scratch_bytes(long long rows) { return (size_t)rows * (30 * sizeof(double) + 3 * sizeof(unsigned)); }
+inline unsigned *face_stamps(double *scratch, long long rows) { return reinterpret_cast<unsigned *>(scratch + 30 * rows); }
+inline unsigned next_face_gen(unsigned &g)
+{
+    g = g + 1 == 0 ? 1 : g + 1;
+    return g;
+}
+// Kernels one launch_weno issues: 2 with a face scratch of >= n_items rows,
+// else 1.
 inline int weno_launches(const double *face_scratch, long long scratch_rows, int n_items)
 {
     return face_scratch && scratch_rows >= n_items ? 2 : 1;

@@ -39,7 +39,8 @@ struct cfd_solver {
     double *U[3] = {nullptr, nullptr, nullptr};
     double *Q = nullptr, *F = nullptr, *E = nullptr, *G = nullptr, *Fv = nullptr, *Ev = nullptr, *Gv = nullptr;
     double *roe = nullptr, *L = nullptr;
-    double *face = nullptr;     // gather path: +1/2 face fluxes of the Weno pass [3][5][n_rows]
+    double *face = nullptr;     // gather path: the Weno pass's face scratch (face_scratch_bytes(n_rows))
+    unsigned face_gen = 0;
     // structured path
     cfd::StructuredLaunch S{};
     double *stage9 = nullptr;   // AoS staging, rows 0..N, 9 doubles
@@ -92,7 +93,9 @@ cfd_status_t create_gather(cfd_solver *s, const cfd_geometry_t *g)
     double **c5[] = {&s->Q, &s->F, &s->E, &s->G, &s->Fv, &s->Ev, &s->Gv, &s->L};
     for (double **p : c5)
         if ((st = dalloc_t(s, R * 5, p))) return st;
-    if ((st = dalloc_t(s, R * 36, &s->roe)) || (st = dalloc_t(s, R * 15, &s->face))) return st;
+    if ((st = dalloc_t(s, R * 36, &s->roe)) || (st = dalloc(s, face_scratch_bytes((long long)R), (void **)&s->face)))
+        return st;
+    cudaMemsetAsync(face_stamps(s->face, (long long)R), 0, R * 3 * sizeof(unsigned), s->ctx->stream);
     for (int q = 0; q < 3; ++q) cudaMemsetAsync(s->U[q], 0, R * 5 * sizeof(double), s->ctx->stream);
     for (double **p : c5) cudaMemsetAsync(*p, 0, R * 5 * sizeof(double), s->ctx->stream);
     cudaMemsetAsync(s->roe, 0, R * 36 * sizeof(double), s->ctx->stream);
@@ -237,7 +240,7 @@ cfd_status_t run_stage(cfd_solver *s, int j, double dt, bool want_L)
                        s->flow, s->g_node + 1, s->n_rows, ctx->d_flags);
         launch_weno(ctx->stream, s->P, j, s->P.mach, dt, s->deter, s->det, s->U[0], s->U[1], s->U[2], s->grid, s->Q,
                     s->metric, s->roe, s->Fv, s->Ev, s->Gv, s->F, s->E, s->G, s->flow, s->sd_node + 1, s->n_rows,
-                    ctx->d_flags, want_L ? s->L : nullptr, s->face, s->n_rows);
+                    ctx->d_flags, want_L ? s->L : nullptr, s->face, s->n_rows, next_face_gen(s->face_gen));
         ctx->launches += nu + 1 + weno_launches(s->face, s->n_rows, s->sd_node + 1);
         if (s->has_bc) {
             bc_apply_aos(ctx->stream, s->bc, s->flow, s->P.mach);
@@ -485,7 +488,7 @@ cfd_status_t cfd_solver_profile_stage(cfd_solver_t *s, int32_t j, double del_t, 
         cudaEventRecord(ev[2], stream);
         launch_weno(stream, s->P, j, s->P.mach, del_t, s->deter, s->det, s->U[0], s->U[1], s->U[2], s->grid, s->Q,
                     s->metric, s->roe, s->Fv, s->Ev, s->Gv, s->F, s->E, s->G, s->flow, s->sd_node + 1, s->n_rows,
-                    s->ctx->d_flags, nullptr, s->face, s->n_rows);
+                    s->ctx->d_flags, nullptr, s->face, s->n_rows, next_face_gen(s->face_gen));
         cudaEventRecord(ev[3], stream);
         snames[0] = "uq";
         snames[1] = "viscous";

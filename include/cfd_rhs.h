@@ -163,7 +163,7 @@ cfd_status_t cfd_ctx_set_rows(cfd_ctx_t *ctx, int32_t n_rows);
  * inputs (Weno.cl:336-3058 evaluates both at every row), and cfd_uq computes
  * sqrt(rho) and H once per row instead of once per row and neighbour
  * (U_Q.cl:60-109); the results are the same bits.  on = 0 evaluates
- * everything per row, as the reference does.  Needs 120 bytes per row,
+ * everything per row, as the reference does.  Needs 252 bytes per row,
  * allocated by cfd_ctx_set_rows. */
 cfd_status_t cfd_ctx_set_face_reuse(cfd_ctx_t *ctx, int on);
 /* Kernels this context launched since creation (for accounting). */
