@@ -95,12 +95,24 @@ __global__ void __launch_bounds__(128) k_uq(double *__restrict__ U, double *__re
     const double rho = fi[FRHO], u = fi[FU], v = fi[FV], w = fi[FW], p = fi[FP];
     const double si = SH ? sh[2 * (size_t)gid] : sqrt(rho);
     const double hi = SH ? sh[2 * (size_t)gid + 1] : ex::enthalpy(rho, u, v, w, p);
-    // ROE block order ip, jp, kp, im, jm, km; neighbour slots N1, N0, N4, N3, N2, N5
-    const int slot_of_block[6] = {1, 0, 4, 3, 2, 5};
+    // ROE block order ip, jp, kp, im, jm, km: block d is the +d face
+    // (neighbour slot plus_slot(d)), block d + 3 the -d face (minus_slot(d)).
+    //
+    // With SH the Roe state of a face is evaluated once.  roe() is symmetric
+    // in its two rows bit for bit (one product, and a sum of two products
+    // over a sum: IEEE addition and multiplication commute), so the +d
+    // block of row m equals the -d block of row q = plus(m) whenever
+    // minus(q) == m.  Row m then also stores it as q's -d block, provided q
+    // is a row of this launch, and row q skips that block: both rows test
+    // the same predicate (m, q < n_items, plus(m) == q, minus(q) == m), so
+    // every block has exactly one writer.
     double *r = roe + 36 * (size_t)gid;
 #pragma unroll
     for (int b = 0; b < 6; ++b) {
-        const int nr = nb[slot_of_block[b]];
+        const int d = b % 3;
+        const bool plus = b < 3;
+        const int nr = nb[plus ? plus_slot(d) : minus_slot(d)];
+        if (SH && !plus && nr < n_items && grid_nb(grid, nr, plus_slot(d)) == gid) continue;
         const double *fn = flow + 9 * (size_t)nr;
         const double rb = fn[FRHO], ub = fn[FU], vb = fn[FV], wb = fn[FW], pb = fn[FP];
         const double sb = SH ? sh[2 * (size_t)nr] : sqrt(rb);
@@ -112,6 +124,14 @@ __global__ void __launch_bounds__(128) k_uq(double *__restrict__ U, double *__re
         r[6 * b + 2] = ra[2];
         r[6 * b + 4] = ra[3];
         r[6 * b + 5] = ra[4];
+        if (SH && plus && nr < n_items && grid_nb(grid, nr, minus_slot(d)) == gid) {
+            double *rq = roe + 36 * (size_t)nr + 6 * (d + 3);
+            rq[0] = ra[0];
+            rq[1] = ra[1];
+            rq[2] = ra[2];
+            rq[4] = ra[3];
+            rq[5] = ra[4];
+        }
     }
     const double D = det[gid];
     const double ke = 0.5 * rho * (u * u + v * v + w * w);

@@ -184,6 +184,40 @@ def test_face_reuse_is_bit_identical(ctx, maker):
         assert np.array_equal(a.view(np.uint64), b.view(np.uint64)), f"{maker}: {k} differs"
 
 
+@pytest.mark.parametrize("maker", ["vortex", "box"])
+def test_uq_partial_range_shares_roe_exactly(ctx, maker):
+    """cfd_uq over the first n_items rows only: with shared Roe states (each
+    face evaluated once and stored for both of its rows) U, Q and ROE_AVER
+    are the same bits as with all six faces evaluated per row, and rows from
+    n_items on keep what they held (the launch writes no row outside its
+    range, also not as a neighbour's partner)."""
+    from cfd_gb300 import cases
+    c = (cases.isentropic_vortex(n=12, shape=(12, 10, 8)) if maker == "vortex"
+         else cases.ghost_box(shape=(9, 8, 7), seed=3))
+    rows = c.g_node + 1
+    for n_items in (1, 2, rows // 2 + 3, rows - 5, rows):
+        out = {}
+        for reuse in (True, False):
+            ctx.set_face_reuse(reuse)
+            a = copy_arrays(c.arrays)
+            for k in ("roe", "U0", "Q"):
+                a[k][...] = -7.25
+            dev = ctx.upload_case(a, names=["U0", "Q", "grid", "det", "flow", "roe"])
+            try:
+                ctx.uq(dev["U0"], dev["Q"], dev["grid"], dev["det"], dev["flow"], dev["roe"], n_items)
+                out[reuse] = {k: ctx.download(dev, k, a[k]) for k in ("roe", "U0", "Q")}
+            finally:
+                ctx.set_face_reuse(True)
+                for p in dev.values():
+                    ctx.free(p)
+        for k in ("roe", "U0", "Q"):
+            s, p = out[True][k], out[False][k]
+            assert np.array_equal(s.view(np.uint64), p.view(np.uint64)), f"{maker} n_items={n_items}: {k} differs"
+            assert np.all(s[n_items:] == -7.25), f"{maker} n_items={n_items}: {k} written outside the range"
+        written = [6 * b + o for b in range(6) for o in (0, 1, 2, 4, 5)]   # U_Q leaves slot 3 of each block
+        assert np.all(out[True]["roe"][:n_items, written] != -7.25), f"{maker} n_items={n_items}: a block unwritten"
+
+
 def _host_stage(ctx, a, g_node, sd_node, params, j, dt, L=None):
     """One stage through the entry points with host numpy arrays."""
     p = {k: v.ctypes.data for k, v in a.items()}
