@@ -89,6 +89,10 @@ def parse_args(argv=None):
     p.add_argument("--batch-tile", type=int, default=0, help="tile size of the batched leg (0 = tuned)")
     p.add_argument("--serve-requests", type=int, default=24, help="requests of the serving workload (0 = skip)")
     p.add_argument("--serve-fp64", action="store_true", help="also serve the stream with the FP64 form")
+    p.add_argument("--serve-fill", type=int, default=0,
+                   help="lattice nodes per batch step of the least_work policy (0 = the library default)")
+    p.add_argument("--serve-policies", default="least_work,all",
+                   help="scheduling policies of the serving leg, the first one reported as the result")
     p.add_argument("--diag-steps", type=int, default=200,
                    help="steps of the kinetic-energy/enstrophy comparison on the main case (0 = skip)")
     p.add_argument("--naca-steps", type=int, default=500,
@@ -570,22 +574,30 @@ def bench_naca(ctx, torch, stream, args):
 
 def bench_serving(ctx, args):
     """Continuous batching of a seeded Poisson request stream (mean 50/s;
-    vortex or Taylor-Green; edge log-uniform [32, 160]; steps U[50, 400])."""
+    vortex or Taylor-Green; edge log-uniform [32, 160]; steps U[50, 400]).
+    The first policy of --serve-policies gives the "mixed" (and "fp64")
+    entries; every further policy is reported beside it for comparison."""
     from cfd_gb300 import serving
     reqs = serving.poisson_requests(args.serve_requests)
     t0 = time.perf_counter()
     cache = {r.rid: serving.make_case(r) for r in reqs}
     gen_s = time.perf_counter() - t0
     out = {"requests": len(reqs), "arrival_rate_per_s": 50.0, "case_generation_s": gen_s,
-           "workload": "Poisson(50/s) vortex/TGV 50:50, edge log-uniform [32,160], steps U[50,400], seed 20261203"}
+           "workload": "Poisson(50/s) vortex/TGV 50:50, edge log-uniform [32,160], steps U[50,400], seed 20261203",
+           "fill_nodes": args.serve_fill or serving.FILL_NODES}
+    policies = [p for p in args.serve_policies.split(",") if p]
     for prec in ((1, 0) if args.serve_fp64 else (1,)):
-        srv = serving.Server(ctx, precision=prec, tune=True)
-        r = srv.run(reqs, case_cache=cache)
-        srv.close()
-        out["mixed" if prec else "fp64"] = {
-            "cell_updates_per_s": r["cell_updates_per_s"], "latency_p50_s": r["latency_p50_s"],
-            "latency_p99_s": r["latency_p99_s"], "latency_max_s": r["latency_max_s"], "makespan_s": r["makespan_s"],
-            "batch_steps": r["batch_steps"], "completed": r["requests"]}
+        for i, pol in enumerate(policies):
+            srv = serving.Server(ctx, precision=prec, tune=True, policy=pol,
+                                 fill_nodes=args.serve_fill or serving.FILL_NODES)
+            r = srv.run(reqs, case_cache=cache)
+            srv.close()
+            key = ("mixed" if prec else "fp64") + ("" if i == 0 else "_" + pol)
+            out[key] = {
+                "policy": pol, "cell_updates_per_s": r["cell_updates_per_s"], "latency_p50_s": r["latency_p50_s"],
+                "latency_p99_s": r["latency_p99_s"], "latency_mean_s": r["latency_mean_s"],
+                "latency_max_s": r["latency_max_s"], "makespan_s": r["makespan_s"],
+                "batch_steps": r["batch_steps"], "completed": r["requests"], "time_in_s": r["time_in_s"]}
     return out
 
 

@@ -49,7 +49,7 @@ class SolverInfo(C.Structure):
 
 class BatchInfo(C.Structure):
     _fields_ = [("n_active", C.c_int32), ("tile_nodes", C.c_int32), ("blocks", C.c_int32), ("graph", C.c_int32),
-                ("precision", C.c_int32), ("reserved", C.c_int32), ("nodes_total", C.c_uint64),
+                ("precision", C.c_int32), ("n_held", C.c_int32), ("nodes_total", C.c_uint64),
                 ("device_bytes", C.c_uint64), ("capacity_bytes", C.c_uint64)]
 
 
@@ -98,6 +98,7 @@ PROTOTYPES = {
     "cfd_batch_add": (C.c_int, [_vp, C.POINTER(Geometry), C.POINTER(Params), _vp, _d, C.POINTER(_i32)]),
     "cfd_batch_remove": (C.c_int, [_vp, _i32]),
     "cfd_batch_step": (C.c_int, [_vp, _i32]),
+    "cfd_batch_set_hold": (C.c_int, [_vp, _i32, _i32]),
     "cfd_batch_get_flow": (C.c_int, [_vp, _i32, _vp]),
     "cfd_batch_get_u0": (C.c_int, [_vp, _i32, _vp]),
     "cfd_batch_slot_status": (C.c_int, [_vp, _i32]),

@@ -79,7 +79,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
                 raise RuntimeError(f"nvcc failed on {src.name}")
             objs.append(str(obj))
     tmp = LIB.with_suffix(".so.tmp")
-    cmd = [cc, *ARCH, "-shared", "-o", str(tmp), *objs, "-lcudart"]
+    cmd = [cc, *ARCH, "-shared", "-o", str(tmp), *objs, "-lcudart", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         sys.stderr.write(r.stdout + r.stderr)

@@ -23,6 +23,7 @@ constexpr int kMaxSlots = 4096;
 
 struct BatchInst {
     bool active = false;
+    bool held = false;          // resident, but not advanced by cfd_batch_step
     int32_t g_node = 0;
     int ni = 0, nj = 0, nk = 0, N = 0;
     cfd_params_t prm{};
@@ -107,7 +108,7 @@ cfd_status_t rebuild(cfd_batch *b)
     uint64_t nodes = 0;
     for (size_t s = 0; s < b->slots.size(); ++s) {
         const BatchInst &I = b->slots[s];
-        if (!I.active) continue;
+        if (!I.active || I.held) continue;
         const int v = (int)views.size();
         views.push_back(I.view);
         for (int n0 = 0; n0 < I.N; n0 += T) tiles.push_back(BatchTile{v, n0, std::min(T, I.N - n0), 0});
@@ -294,11 +295,15 @@ cfd_status_t cfd_batch_add(cfd_batch_t *b, const cfd_geometry_t *geom, const cfd
     if (st != CFD_OK) return st;
     if (!geom->grid || !geom->det || !geom->deter || !geom->metric || geom->g_node < 1)
         return fail(ctx, CFD_EINVAL, "cfd_batch_add: bad geometry");
-    for (int32_t r = 0; r <= geom->g_node; ++r)
-        for (int slot = 0; slot < 6; ++slot) {
-            const int v = nb_of(geom->grid[r], slot);
-            if (v < 0 || v > geom->g_node) return fail(ctx, CFD_EINVAL, "cfd_batch_add: neighbour index out of range");
-        }
+    std::atomic<bool> out_of_range{false};
+    host_parallel_for((long long)geom->g_node + 1, [&](long long r0, long long r1) {
+        for (long long r = r0; r < r1; ++r)
+            for (int slot = 0; slot < 6; ++slot) {
+                const int v = nb_of(geom->grid[r], slot);
+                if (v < 0 || v > geom->g_node) out_of_range = true;
+            }
+    });
+    if (out_of_range) return fail(ctx, CFD_EINVAL, "cfd_batch_add: neighbour index out of range");
     LatticeMap map;
     bool natural = map_lattice(geom, map) && !map.ghosted() && faces_single_valued(geom, map)
                    && (long long)map.ni * map.nj * map.nk <= kLatticeMaxNodes;
@@ -384,12 +389,12 @@ cfd_status_t cfd_batch_add(cfd_batch_t *b, const cfd_geometry_t *geom, const cfd
         }
     }
     cudaStream_t sm = ctx->stream;
-    std::vector<double> h, hd, hf, hfd;
+    HostDoubles h, hd, hf, hfd;
     lattice_geometry_soa(geom, map, h, hd, hf, hfd);
-    cudaError_t e = cudaMemcpyAsync(m9, h.data(), 9 * Nz * 8, cudaMemcpyHostToDevice, sm);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(det, hd.data(), Nz * 8, cudaMemcpyHostToDevice, sm);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(fm, hf.data(), 9 * Nz * 8, cudaMemcpyHostToDevice, sm);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(fdet, hfd.data(), 3 * Nz * 8, cudaMemcpyHostToDevice, sm);
+    cudaError_t e = cudaMemcpyAsync(m9, host_ptr(h), 9 * Nz * 8, cudaMemcpyHostToDevice, sm);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(det, host_ptr(hd), Nz * 8, cudaMemcpyHostToDevice, sm);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(fm, host_ptr(hf), 9 * Nz * 8, cudaMemcpyHostToDevice, sm);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(fdet, host_ptr(hfd), 3 * Nz * 8, cudaMemcpyHostToDevice, sm);
     if (e == cudaSuccess) e = cudaMemcpyAsync(I.stage9, flow, 9 * (Nz + 1) * 8, cudaMemcpyHostToDevice, sm);
     if (e == cudaSuccess) e = cudaMemsetAsync(I.stage5, 0, 5 * (Nz + 1) * 8, sm);
     if (e == cudaSuccess) e = cudaMemsetAsync(v.flags, 0, sizeof(unsigned), sm);
@@ -444,6 +449,17 @@ cfd_status_t cfd_batch_remove(cfd_batch_t *b, int32_t slot)
     b->used -= b->slots[slot].bytes;
     free_instance(b->slots[slot]);
     b->dirty = true;
+    return CFD_OK;
+}
+
+cfd_status_t cfd_batch_set_hold(cfd_batch_t *b, int32_t slot, int32_t hold)
+{
+    if (!b || slot < 0 || slot >= (int)b->slots.size() || !b->slots[slot].active) return CFD_EINVAL;
+    BatchInst &I = b->slots[slot];
+    if (I.held != (hold != 0)) {
+        I.held = hold != 0;
+        b->dirty = true;    // the tile table of the next step leaves it out / takes it back
+    }
     return CFD_OK;
 }
 
@@ -583,9 +599,13 @@ cfd_status_t cfd_batch_info(const cfd_batch_t *b, cfd_batch_info_t *info)
 {
     if (!b || !info) return CFD_EINVAL;
     std::memset(info, 0, sizeof *info);
-    int n = 0;
-    for (auto &I : b->slots) n += I.active ? 1 : 0;
+    int n = 0, held = 0;
+    for (auto &I : b->slots) {
+        n += I.active ? 1 : 0;
+        held += I.active && I.held ? 1 : 0;
+    }
     info->n_active = n;
+    info->n_held = held;
     info->tile_nodes = b->threads;
     info->blocks = b->blocks;
     info->graph = b->graph_ok ? 1 : 0;

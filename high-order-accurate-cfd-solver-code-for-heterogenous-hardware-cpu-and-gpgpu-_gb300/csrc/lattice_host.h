@@ -1,14 +1,53 @@
 // lattice_host.h -- host-side checks that decide whether a reference
 // neighbour table can run on the face-based lattice kernels, and the
-// conversion of its geometry to the lattice layout.
+// conversion of its geometry to the lattice layout.  The per-node passes run
+// on up to 16 host threads: admitting a 160^3 lattice reads about 2 GB of
+// reference geometry.
 #pragma once
 
+#include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <memory>
+#include <thread>
 #include <vector>
 
 #include "cfd_rhs.h"
 
 namespace cfd {
+
+// fn(begin, end) over [0, n) in contiguous chunks of at least 64 Ki items,
+// on up to 16 threads; a thread that cannot be started runs its chunk on
+// the calling thread.
+template <class F>
+inline void host_parallel_for(long long n, F fn)
+{
+    const unsigned hw = std::max(1u, std::min(std::thread::hardware_concurrency(), 16u));
+    const long long T = std::max(1LL, std::min<long long>(hw, (n + 65535) / 65536));
+    const long long chunk = (n + T - 1) / T;
+    std::vector<std::thread> th;
+    for (long long t = 1; t < T; ++t) {
+        const long long b = t * chunk, e = std::min(n, b + chunk);
+        if (b >= e) break;
+        try {
+            th.emplace_back(fn, b, e);
+        } catch (...) {
+            fn(b, e);
+        }
+    }
+    fn(0LL, std::min(n, chunk));
+    for (auto &x : th) x.join();
+}
+
+// std::vector element type without value-initialisation: the conversion
+// writes every element, so the zero fill of a plain vector is wasted work.
+template <class T>
+struct NoInit {
+    T v;
+    NoInit() {}
+};
+using HostDoubles = std::vector<NoInit<double>>;
+inline double *host_ptr(HostDoubles &v) { return &v.data()->v; }
 
 inline int nb_of(const cfd_grid_t &g, int slot)
 {
@@ -100,22 +139,41 @@ inline bool map_lattice(const cfd_geometry_t *g, LatticeMap &m)
     m.per = per;
     m.row_of.assign(R, 0);
     m.n_of_row.assign(R + 1, -1);
-    // rows by walking +i, +j, +k from the origin
+    // rows by walking +i, +j, +k from the origin: the first row of every
+    // (j, k) line, then the lines in parallel, then a serial pass that
+    // rejects a row reached twice
+    const int lines = m.nj * m.nk;
+    std::vector<int32_t> first(lines);
     int rk = origin;
     for (int k = 0; k < m.nk; ++k) {
         int rj = rk;
         for (int j = 0; j < m.nj; ++j) {
-            int ri = rj;
-            for (int i = 0; i < m.ni; ++i) {
-                const int n = i + m.ni * (j + m.nj * k);
-                if (ri < 1 || ri > R || m.n_of_row[ri] >= 0) return false;
-                m.row_of[n] = ri;
-                m.n_of_row[ri] = n;
-                ri = nbr(ri, kSlotPlus[0]);
-            }
+            if (rj < 1 || rj > R) return false;
+            first[j + m.nj * k] = rj;
             rj = nbr(rj, kSlotPlus[1]);
         }
+        if (rk < 1 || rk > R) return false;
         rk = nbr(rk, kSlotPlus[2]);
+    }
+    std::atomic<bool> bad{false};
+    host_parallel_for(lines, [&](long long l0, long long l1) {
+        for (long long l = l0; l < l1 && !bad.load(std::memory_order_relaxed); ++l) {
+            int ri = first[l];
+            for (int i = 0; i < m.ni; ++i) {
+                if (ri < 1 || ri > R) {
+                    bad = true;
+                    break;
+                }
+                m.row_of[i + (size_t)m.ni * l] = ri;
+                ri = nbr(ri, kSlotPlus[0]);
+            }
+        }
+    });
+    if (bad) return false;
+    for (int n = 0; n < R; ++n) {
+        const int r = m.row_of[n];
+        if (m.n_of_row[r] >= 0) return false;
+        m.n_of_row[r] = n;
     }
     // every neighbour is the lattice neighbour (wrapped or clamped)
     auto step = [&](int c, int o, int d) {
@@ -125,44 +183,57 @@ inline bool map_lattice(const cfd_geometry_t *g, LatticeMap &m)
     };
     const bool ghosted = per != 7;
     if (ghosted) m.loc.assign(R, 0);
-    for (int k = 0; k < m.nk; ++k)
-        for (int j = 0; j < m.nj; ++j)
-            for (int i = 0; i < m.ni; ++i) {
-                const int n = i + m.ni * (j + m.nj * k);
-                const cfd_grid_t &row = g->grid[m.row_of[n]];
-                const int c[3] = {i, j, k};
-                for (int d = 0; d < 3; ++d)
-                    for (int o : {-1, 1}) {
-                        int cc[3] = {i, j, k};
-                        cc[d] = step(c[d], o, d);
-                        const int want = m.row_of[cc[0] + m.ni * (cc[1] + m.nj * cc[2])];
-                        if (nb_of(row, o > 0 ? kSlotPlus[d] : kSlotMinus[d]) != want) return false;
-                    }
-                const bool owned = m.row_of[n] <= g->sd_node;
-                if (!ghosted) {
-                    if (row.loc != 0 || g->g_node != g->sd_node) return false;
-                    continue;
+    // node n's coordinates
+    auto coords = [&](long long n, int c[3]) {
+        c[0] = (int)(n % m.ni);
+        c[1] = (int)((n / m.ni) % m.nj);
+        c[2] = (int)(n / ((long long)m.ni * m.nj));
+    };
+    host_parallel_for(R, [&](long long n0, long long n1) {
+        for (long long n = n0; n < n1 && !bad.load(std::memory_order_relaxed); ++n) {
+            int c[3];
+            coords(n, c);
+            const cfd_grid_t &row = g->grid[m.row_of[n]];
+            bool ok = true;
+            for (int d = 0; d < 3 && ok; ++d)
+                for (int o : {-1, 1}) {
+                    int cc[3] = {c[0], c[1], c[2]};
+                    cc[d] = step(c[d], o, d);
+                    const int want = m.row_of[cc[0] + m.ni * (cc[1] + (size_t)m.nj * cc[2])];
+                    if (nb_of(row, o > 0 ? kSlotPlus[d] : kSlotMinus[d]) != want) ok = false;
                 }
-                if (owned == (row.loc == 100) || row.loc < 0 || row.loc > 100) return false;
-                m.loc[n] = (unsigned char)row.loc;
-                if (owned)
+            const bool owned = m.row_of[n] <= g->sd_node;
+            if (ok && !ghosted) ok = row.loc == 0 && g->g_node == g->sd_node;
+            else if (ok) {
+                ok = owned != (row.loc == 100) && row.loc >= 0 && row.loc <= 100;
+                if (ok) m.loc[n] = (unsigned char)row.loc;
+                if (ok && owned)
                     for (int d = 0; d < 3; ++d)
-                        if (!(per >> d & 1) && (c[d] < 3 || c[d] > m.extent(d) - 4)) return false;
+                        if (!(per >> d & 1) && (c[d] < 3 || c[d] > m.extent(d) - 4)) ok = false;
             }
-    if (ghosted)
-        for (int k = 0; k < m.nk; ++k)
-            for (int j = 0; j < m.nj; ++j)
-                for (int i = 0; i < m.ni; ++i) {
-                    const int n = i + m.ni * (j + m.nj * k);
-                    if (m.loc[n] == 100) continue;
-                    const int c[3] = {i, j, k};
-                    for (int d = 0; d < 3; ++d)
-                        for (int o : {-2, -1, 1, 2}) {
-                            int cc[3] = {i, j, k};
-                            cc[d] = step(c[d], o, d);
-                            if (m.loc[cc[0] + m.ni * (cc[1] + m.nj * cc[2])] == 100) m.locdirs |= 1 << d;
-                        }
-                }
+            if (!ok) bad = true;
+        }
+    });
+    if (bad) return false;
+    if (ghosted) {
+        std::atomic<int> dirs{0};
+        host_parallel_for(R, [&](long long n0, long long n1) {
+            int mine = 0;
+            for (long long n = n0; n < n1; ++n) {
+                if (m.loc[n] == 100) continue;
+                int c[3];
+                coords(n, c);
+                for (int d = 0; d < 3; ++d)
+                    for (int o : {-2, -1, 1, 2}) {
+                        int cc[3] = {c[0], c[1], c[2]};
+                        cc[d] = step(c[d], o, d);
+                        if (m.loc[cc[0] + m.ni * (cc[1] + (size_t)m.nj * cc[2])] == 100) mine |= 1 << d;
+                    }
+            }
+            dirs.fetch_or(mine);
+        });
+        m.locdirs = dirs.load();
+    }
     return true;
 }
 
@@ -173,50 +244,57 @@ inline bool faces_single_valued(const cfd_geometry_t *g, const LatticeMap &m)
 {
     const double tol = 1e-13;
     auto close = [&](double a, double b, double scale) { return std::fabs(a - b) <= tol * scale; };
-    for (int k = 0; k < m.nk; ++k)
-        for (int j = 0; j < m.nj; ++j)
-            for (int i = 0; i < m.ni; ++i) {
-                const int n = i + m.ni * (j + m.nj * k);
-                const int r = m.row_of[n];
-                const double *mr = (const double *)&g->metric[r];
-                const double *dd = (const double *)&g->deter[r];
-                const int c[3] = {i, j, k};
-                for (int d = 0; d < 3; ++d) {
-                    if (!(m.per >> d & 1) && (c[d] < 2 || c[d] > m.extent(d) - 4)) continue;
-                    const int nbr = nb_of(g->grid[r], kSlotPlus[d]);
-                    const double *mn = (const double *)&g->metric[nbr];
-                    const double *dn = (const double *)&g->deter[nbr];
-                    double scale = 0;
-                    for (int q = 0; q < 3; ++q) scale = std::fmax(scale, std::fabs(mr[9 * (1 + 2 * d) + 3 * d + q]));
-                    for (int q = 0; q < 3; ++q)
-                        if (!close(mr[9 * (1 + 2 * d) + 3 * d + q], mn[9 * (2 + 2 * d) + 3 * d + q], scale)) return false;
-                    if (!close(dd[2 * d], dn[2 * d + 1], std::fabs(dd[2 * d]))) return false;
+    std::atomic<bool> bad{false};
+    host_parallel_for((long long)m.row_of.size(), [&](long long n0, long long n1) {
+        for (long long n = n0; n < n1 && !bad.load(std::memory_order_relaxed); ++n) {
+            const int c[3] = {(int)(n % m.ni), (int)((n / m.ni) % m.nj), (int)(n / ((long long)m.ni * m.nj))};
+            const int r = m.row_of[n];
+            const double *mr = (const double *)&g->metric[r];
+            const double *dd = (const double *)&g->deter[r];
+            for (int d = 0; d < 3; ++d) {
+                if (!(m.per >> d & 1) && (c[d] < 2 || c[d] > m.extent(d) - 4)) continue;
+                const int nbr = nb_of(g->grid[r], kSlotPlus[d]);
+                const double *mn = (const double *)&g->metric[nbr];
+                const double *dn = (const double *)&g->deter[nbr];
+                double scale = 0;
+                for (int q = 0; q < 3; ++q) scale = std::fmax(scale, std::fabs(mr[9 * (1 + 2 * d) + 3 * d + q]));
+                bool ok = close(dd[2 * d], dn[2 * d + 1], std::fabs(dd[2 * d]));
+                for (int q = 0; q < 3; ++q)
+                    ok = ok && close(mr[9 * (1 + 2 * d) + 3 * d + q], mn[9 * (2 + 2 * d) + 3 * d + q], scale);
+                if (!ok) {
+                    bad = true;
+                    break;
                 }
             }
-    return true;
+        }
+    });
+    return !bad;
 }
 
 // Geometry of a lattice as SoA host arrays: m9 [9][N], det [N], fm [3 dir][3
 // comp][N] (metric of face n+1/2), fdet [3][N] (det of face n+1/2).
-inline void lattice_geometry_soa(const cfd_geometry_t *g, const LatticeMap &map, std::vector<double> &m9,
-                                 std::vector<double> &det, std::vector<double> &fm, std::vector<double> &fdet)
+inline void lattice_geometry_soa(const cfd_geometry_t *g, const LatticeMap &map, HostDoubles &m9v,
+                                 HostDoubles &detv, HostDoubles &fmv, HostDoubles &fdetv)
 {
     const size_t N = map.row_of.size();
-    m9.assign(9 * N, 0.0);
-    det.assign(N, 0.0);
-    fm.assign(9 * N, 0.0);
-    fdet.assign(3 * N, 0.0);
-    for (size_t n = 0; n < N; ++n) {
-        const int r = map.row_of[n];
-        const double *m = (const double *)&g->metric[r];
-        const double *dd = (const double *)&g->deter[r];
-        for (int q = 0; q < 9; ++q) m9[q * N + n] = m[q];
-        det[n] = g->det[r];
-        for (int d = 0; d < 3; ++d) {
-            for (int c = 0; c < 3; ++c) fm[(d * 3 + c) * N + n] = m[9 * (1 + 2 * d) + 3 * d + c];
-            fdet[d * N + n] = dd[2 * d];
+    m9v.resize(9 * N);
+    detv.resize(N);
+    fmv.resize(9 * N);
+    fdetv.resize(3 * N);
+    double *m9 = host_ptr(m9v), *det = host_ptr(detv), *fm = host_ptr(fmv), *fdet = host_ptr(fdetv);
+    host_parallel_for((long long)N, [&](long long n0, long long n1) {
+        for (long long n = n0; n < n1; ++n) {
+            const int r = map.row_of[n];
+            const double *m = (const double *)&g->metric[r];
+            const double *dd = (const double *)&g->deter[r];
+            for (int q = 0; q < 9; ++q) m9[q * N + n] = m[q];
+            det[n] = g->det[r];
+            for (int d = 0; d < 3; ++d) {
+                for (int c = 0; c < 3; ++c) fm[(d * 3 + c) * N + n] = m[9 * (1 + 2 * d) + 3 * d + c];
+                fdet[d * N + n] = dd[2 * d];
+            }
         }
-    }
+    });
 }
 
 }  // namespace cfd

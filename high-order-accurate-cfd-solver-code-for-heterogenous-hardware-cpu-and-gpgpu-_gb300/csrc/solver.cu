@@ -147,10 +147,10 @@ cfd_status_t create_structured(cfd_solver *s, const cfd_geometry_t *g)
     cudaMemsetAsync(s->stage5, 0, 5 * (N + 1) * sizeof(double), S.stream);
     cudaMemsetAsync(s->stage9, 0, 9 * (N + 1) * sizeof(double), S.stream);
     // geometry AoS -> SoA on the host (one-off)
-    std::vector<double> h, hd, hf, hfd;
+    HostDoubles h, hd, hf, hfd;
     lattice_geometry_soa(g, s->map, h, hd, hf, hfd);
-    if ((st = upload(s, m9, h.data(), 9 * N * 8)) || (st = upload(s, det, hd.data(), N * 8))
-        || (st = upload(s, fm, hf.data(), 9 * N * 8)) || (st = upload(s, fdet, hfd.data(), 3 * N * 8)))
+    if ((st = upload(s, m9, host_ptr(h), 9 * N * 8)) || (st = upload(s, det, host_ptr(hd), N * 8))
+        || (st = upload(s, fm, host_ptr(hf), 9 * N * 8)) || (st = upload(s, fdet, host_ptr(hfd), 3 * N * 8)))
         return st;
     S.m9 = m9;
     S.det = det;

@@ -321,6 +321,7 @@ class BatchInfo:
     nodes_total: int
     device_bytes: int
     capacity_bytes: int
+    n_held: int = 0
 
 
 class Batch:
@@ -370,6 +371,10 @@ class Batch:
     def step(self, nsteps: int = 1):
         self.ctx.check(self.lib.cfd_batch_step(self.h, int(nsteps)), "cfd_batch_step")
 
+    def set_hold(self, slot: int, hold: bool):
+        """A held instance stays resident but is not advanced by step()."""
+        self.ctx.check(self.lib.cfd_batch_set_hold(self.h, int(slot), 1 if hold else 0), "cfd_batch_set_hold")
+
     def get_flow(self, slot: int) -> np.ndarray:
         out = np.empty((self.rows[slot], L.NFLOW))
         self.ctx.check(self.lib.cfd_batch_get_flow(self.h, int(slot), C.c_void_p(_ptr(out))), "cfd_batch_get_flow")
@@ -394,4 +399,4 @@ class Batch:
         i = abi.BatchInfo()
         self.ctx.check(self.lib.cfd_batch_info(self.h, C.byref(i)), "cfd_batch_info")
         return BatchInfo(i.n_active, i.tile_nodes, i.blocks, bool(i.graph), "mixed" if i.precision else "fp64",
-                         int(i.nodes_total), int(i.device_bytes), int(i.capacity_bytes))
+                         int(i.nodes_total), int(i.device_bytes), int(i.capacity_bytes), int(i.n_held))

@@ -7,7 +7,8 @@ stage over all instances) and, between steps:
 
 * admits queued requests in arrival order while their device-memory
   footprint fits the batch budget (``cfd_batch_instance_bytes``);
-* advances every admitted solve by one step;
+* picks the admitted solves that advance in this step (``policy``) and
+  advances them by one step in one batched launch sequence;
 * retires the solves that reached their step count (their FLOW is read back
   as the result) and frees their memory for the queue.
 
@@ -15,6 +16,20 @@ Requests that arrive while others run join at the next step boundary, so
 their work overlaps on the device with the solves already in flight.  The
 reference has no serving layer; this is the builder's request loop around the
 RHS path.  Latency = completion time - arrival time.
+
+Policies:
+
+* ``"all"``: every admitted solve advances every step.  Each solve then
+  finishes after its own step count of batch steps, but every batch step
+  costs the whole batch, so a small solve waits on the large ones.
+* ``"least_work"`` (default): the solves with the least remaining work
+  (nodes x remaining steps; arrival order breaks ties) advance, as many as
+  it takes to reach ``fill_nodes`` lattice nodes per step, enough to keep the
+  GPU busy; the others stay resident, held (``Batch.set_hold``).  This is
+  shortest-remaining-work-first with a minimum batch size: the device does
+  the same total work, and small solves finish first.  Under a sustained
+  overload of small requests a large one can wait indefinitely; ``"all"``
+  has no such case.
 
 Checkpoint/resume: with ``checkpoint_dir`` every solve keeps the reference's
 restart pair (files.py) under ``<dir>/req_<rid>/``, written every
@@ -77,6 +92,20 @@ def poisson_requests(count: int, rate: float = 50.0, n_range=(32, 160), steps_ra
     return out
 
 
+def least_work_first(entries, fill_nodes: int) -> set:
+    """Slots that advance under the "least_work" policy.  entries: iterable
+    of (slot, nodes, remaining steps, arrival).  Takes slots in order of
+    nodes x remaining steps (then arrival) until their nodes reach
+    fill_nodes; at least one slot when there is any."""
+    chosen, nodes = set(), 0
+    for slot, n, left, arrival in sorted(entries, key=lambda e: (e[1] * e[2], e[3], e[0])):
+        if chosen and nodes >= fill_nodes:
+            break
+        chosen.add(slot)
+        nodes += n
+    return chosen
+
+
 def make_case(req: Request):
     rng = np.random.default_rng(req.seed)
     if req.kind == "vortex":
@@ -84,13 +113,23 @@ def make_case(req: Request):
     return cases.taylor_green(n=req.n)
 
 
+# Lattice nodes per batch step under "least_work".  The batched mixed
+# stage kernel runs at 1.0e9 cell-updates/s from 2.6e5 nodes on and at
+# 1.06e9 from 1e6 (one GB300); a smaller step finishes small solves sooner.
+FILL_NODES = 1 << 20
+
+
 class Server:
     """Continuous-batching request loop over one ``runtime.Batch``."""
 
     def __init__(self, ctx, precision: int = 1, capacity_bytes: int = 0, keep_results: bool = False,
-                 tune: bool = False):
+                 tune: bool = False, policy: str = "least_work", fill_nodes: int = FILL_NODES):
+        if policy not in ("all", "least_work"):
+            raise ValueError(f"unknown policy {policy!r}")
         self.batch = runtime.Batch(ctx, precision, capacity_bytes)
         self.precision = precision
+        self.policy = policy
+        self.fill_nodes = int(fill_nodes)
         self.keep_results = keep_results
         self.tune = tune
         self.info0 = self.batch.info()
@@ -106,6 +145,7 @@ class Server:
         case_cache = {} if case_cache is None else case_cache
         queue = list(sorted(requests, key=lambda r: r.arrival))
         active = {}              # slot -> [request, remaining steps, admitted time, case, next restart number]
+        held = set()             # slots the batch currently leaves out of its steps
         done = []
 
         def ckpt_dir(req):
@@ -118,6 +158,7 @@ class Server:
             files.write_restart(ckpt_dir(req), self.batch.get_flow(slot), case.sd_node, req.steps - left, num)
             active[slot][4] = 3 - num
         budget = self.info0.capacity_bytes
+        spent = {"admit": 0.0, "step": 0.0, "retire": 0.0}   # wall time inside the batch calls
         t0 = clock()
         steps_run = 0
         tuned = not self.tune
@@ -140,7 +181,9 @@ class Server:
                         values, it, num = got
                         flow = files.restart_flow(c.arrays["flow"], values, c.params.mach)
                         left = req.steps - it
+                ta = clock()
                 slot = self.batch.add(c, flow=flow)
+                spent["admit"] += clock() - ta
                 used += need
                 active[slot] = [req, left, clock() - t0, c, num]
                 queue.pop(0)
@@ -156,13 +199,24 @@ class Server:
                 continue
             if max_batch_steps is not None and steps_run >= max_batch_steps:
                 break
-            if not tuned and len(active) > 1:
+            if self.policy == "all":
+                run = set(active)
+            else:
+                run = least_work_first(((s, a[0].n ** 3, a[1], a[0].arrival) for s, a in active.items()),
+                                       self.fill_nodes)
+            for s in active:
+                if (s in held) == (s in run):
+                    self.batch.set_hold(s, s not in run)
+                    held.symmetric_difference_update({s})
+            ts = clock()
+            if not tuned and len(run) > 1:
                 self.batch.tune(1)
                 tuned = True
             self.batch.step(1)
+            spent["step"] += clock() - ts
             steps_run += 1
-            finished = [s for s, a in active.items() if a[1] == 1]
-            for s in list(active):
+            finished = [s for s in run if active[s][1] == 1]
+            for s in run:
                 active[s][1] -= 1
             if checkpoint_dir is not None:
                 for s in active:
@@ -170,8 +224,11 @@ class Server:
                         checkpoint(s)
             for s in finished:
                 req, _, adm, _, _ = active.pop(s)
+                tr = clock()
                 flow = self.batch.get_flow(s) if self.keep_results else None
                 self.batch.remove(s)
+                spent["retire"] += clock() - tr
+                held.discard(s)
                 done.append(Completed(req.rid, req.arrival, adm, clock() - t0, req.n ** 3, req.steps, flow))
         pending = [a[0].rid for a in active.values()] + [r.rid for r in queue]
         for s in list(active):          # a stop keeps the progress of the solves in flight
@@ -191,5 +248,8 @@ class Server:
             "latency_p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
             "latency_p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
             "latency_max_s": float(lat.max()) if len(lat) else None,
+            "latency_mean_s": float(lat.mean()) if len(lat) else None,
+            "policy": self.policy,
+            "time_in_s": spent,
             "pending": pending,
         }

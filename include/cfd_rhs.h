@@ -322,7 +322,7 @@ typedef struct {
     int32_t blocks;            /* persistent grid size                        */
     int32_t graph;             /* 1 when steps replay a captured CUDA graph   */
     int32_t precision;         /* cfd_precision_t of the whole batch          */
-    int32_t reserved;
+    int32_t n_held;            /* instances held out of cfd_batch_step        */
     uint64_t nodes_total;
     uint64_t device_bytes;     /* admitted instance memory                    */
     uint64_t capacity_bytes;   /* admission budget                            */
@@ -338,9 +338,15 @@ uint64_t cfd_batch_instance_bytes(int32_t precision, int64_t nodes);
 cfd_status_t cfd_batch_add(cfd_batch_t *b, const cfd_geometry_t *geom, const cfd_params_t *params,
                            const cfd_flow_t *flow, double del_t, int32_t *slot);
 cfd_status_t cfd_batch_remove(cfd_batch_t *b, int32_t slot);
-/* nsteps SSP-RK3 steps of every instance.  CFD_ENONFINITE names the first
- * failing slot in cfd_last_error; the other instances advance normally. */
+/* nsteps SSP-RK3 steps of every instance that is not held.  CFD_ENONFINITE
+ * names the first failing slot in cfd_last_error; the other instances
+ * advance normally. */
 cfd_status_t cfd_batch_step(cfd_batch_t *b, int32_t nsteps);
+/* hold != 0: the instance stays resident (state, slot and memory) but
+ * cfd_batch_step leaves it out until it is released (hold = 0); a
+ * scheduler uses this to run a subset of the batch.  Takes effect at the
+ * next step (the tile table and graph are rebuilt once per change). */
+cfd_status_t cfd_batch_set_hold(cfd_batch_t *b, int32_t slot, int32_t hold);
 cfd_status_t cfd_batch_get_flow(cfd_batch_t *b, int32_t slot, cfd_flow_t *flow_host);
 /* U0 = det*Q of the current FLOW (the next stage's U_Q output). */
 cfd_status_t cfd_batch_get_u0(cfd_batch_t *b, int32_t slot, cfd_column_t *u0_host);

@@ -102,6 +102,41 @@ def test_add_remove_between_steps_and_slot_reuse(ctx):
         x.close()
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_held_instance_does_not_advance(ctx, precision):
+    """cfd_batch_set_hold: a held instance keeps its state through steps of
+    the others and, released, continues as if it had never paused."""
+    from cfd_gb300 import runtime
+    cs = mix_cases()
+    b = runtime.Batch(ctx, precision)
+    s = [b.add(c) for c in cs[:3]]
+    b.step(1)
+    before = b.get_flow(s[1])
+    b.set_hold(s[1], True)
+    b.set_hold(s[1], True)               # idempotent
+    assert b.info().n_held == 1
+    b.step(2)
+    assert np.array_equal(b.get_flow(s[1]), before)
+    b.set_hold(s[0], True)
+    b.set_hold(s[2], True)
+    b.step(1)                            # everything held: nothing moves
+    assert np.array_equal(b.get_flow(s[1]), before)
+    for x in s:
+        b.set_hold(x, False)
+    assert b.info().n_held == 0
+    b.step(1)
+    got = {x: b.get_flow(x) for x in s}
+    for x, c, n in zip(s, cs[:3], (4, 2, 4)):
+        alone = runtime.Batch(ctx, precision)
+        a = alone.add(c)
+        alone.step(n)
+        assert np.array_equal(alone.get_flow(a), got[x]), x
+        alone.close()
+    with pytest.raises(Exception):
+        b.set_hold(99, True)
+    b.close()
+
+
 def test_tuning_and_graph_do_not_change_results(ctx):
     from cfd_gb300 import runtime
     cs = mix_cases()
