@@ -1,5 +1,7 @@
-// exact_div.cuh -- x / b with a reciprocal shared between several numerators,
-// returning the same bits as IEEE division (round to nearest even).
+// exact_div.cuh -- IEEE-exact FP64 arithmetic with fewer FP64 instructions:
+// x / b with a reciprocal shared between several numerators (div), and
+// x * 2^K on the integer pipe (scale2).  Both return the same bits as the
+// IEEE operation (round to nearest even).
 //
 // Given y = 1/b (one IEEE division, reused for every numerator over b):
 //   q0 = RN(x*y),  r0 = RN(b*(-q0) + x),  q1 = RN(r0*y + q0)
@@ -52,6 +54,17 @@ CFD_XDIV_HD double fma_rn(double a, double b, double c)
 #endif
 }
 
+CFD_XDIV_HD double from_bits(uint64_t u)
+{
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double((long long)u);
+#else
+    double v;
+    __builtin_memcpy(&v, &u, 8);
+    return v;
+#endif
+}
+
 CFD_XDIV_HD double mul_rn(double a, double b)
 {
 #if defined(__CUDA_ARCH__)
@@ -93,6 +106,39 @@ CFD_XDIV_HD double div(double x, double b, double y)
     const double q = quotient(x, b, y, ok);
     if (__builtin_expect(ok, 1)) return q;
     return ieee_div(x, b);
+}
+
+// The IEEE product, out of line (scale2's rare case).
+#if defined(__CUDACC__)
+static __host__ __device__ __noinline__ double ieee_mul(double x, double c) { return x * c; }
+#else
+static double ieee_mul(double x, double c)
+{
+    volatile double r = x * c;
+    return r;
+}
+#endif
+
+// x * 2^K for a constant K, 1 <= |K| <= 8: the same bits as the IEEE product
+// x * 2^K.  When x and the product are normal numbers (biased exponents e and
+// e + K both in [1, 2046]) the product differs from x only in its exponent
+// field, so it is one integer add on the high word; +-0 stays +-0; every
+// other operand (subnormal, a product that would overflow or become
+// subnormal, Inf, NaN) takes the FP64 multiply out of line.  On a part whose
+// FP64 rate is a small fraction of its integer rate this takes a multiply
+// by 2, 4, 1/2, 1/4, ... off the FP64 pipe.
+template <int K>
+CFD_XDIV_HD double scale2(double x)
+{
+    static_assert(K != 0 && K >= -8 && K <= 8, "scale2: 1 <= |K| <= 8");
+    constexpr unsigned lo = K < 0 ? 1u + (unsigned)(-K) : 1u;       // smallest e with a normal product
+    constexpr unsigned hi = K > 0 ? 2046u - (unsigned)K : 2046u;     // largest
+    constexpr double c = K > 0 ? (double)(1u << (K > 0 ? K : 0)) : 1.0 / (double)(1u << (K < 0 ? -K : 0));
+    const uint64_t u = bits(x);
+    const unsigned e = (unsigned)(u >> 52) & 0x7ffu;
+    if (__builtin_expect(e - lo <= hi - lo, 1)) return from_bits(u + ((uint64_t)(int64_t)K << 52));
+    if ((u << 1) == 0) return x;
+    return ieee_mul(x, c);
 }
 
 }  // namespace xdiv

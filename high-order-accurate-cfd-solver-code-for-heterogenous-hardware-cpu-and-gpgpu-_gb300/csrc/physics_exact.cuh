@@ -69,18 +69,21 @@ template <bool SD = true>
 __device__ __forceinline__ void weno_pair(const double cc[6], double eps, double &pos, double &neg)
 {
     const double *c = cc + 2;   // c[0] = left node of the face
+    // products by 2, 4, 1/4 and 1/8 on the integer pipe (xdiv::scale2,
+    // the same bits as the multiplies)
+    using xdiv::scale2;
     const double p0 = (15.0 / 8.0) * c[1] - (5.0 / 4.0) * c[2] + (3.0 / 8.0) * c[3];
-    const double p1 = (3.0 / 8.0) * c[0] + (3.0 / 4.0) * c[1] - (1.0 / 8.0) * c[2];
-    const double p2 = (-1.0 / 8.0) * c[-1] + (3.0 / 4.0) * c[0] + (3.0 / 8.0) * c[1];
-    const double m0 = (3.0 / 8.0) * c[0] + (3.0 / 4.0) * c[1] - (1.0 / 8.0) * c[2];
-    const double m1 = (-1.0 / 8.0) * c[-1] + (3.0 / 4.0) * c[0] + (3.0 / 8.0) * c[1];
+    const double p1 = (3.0 / 8.0) * c[0] + (3.0 / 4.0) * c[1] - scale2<-3>(c[2]);
+    const double p2 = -scale2<-3>(c[-1]) + (3.0 / 4.0) * c[0] + (3.0 / 8.0) * c[1];
+    const double m0 = p1;
+    const double m1 = p2;
     const double m2 = (3.0 / 8.0) * c[-2] - (5.0 / 4.0) * c[-1] + (15.0 / 8.0) * c[0];
-    const double ISm2 = (13.0 / 12.0) * (sq(c[-2] - 2.0 * c[-1] + c[0])) + (1.0 / 4.0) * (sq(c[-2] - 4.0 * c[-1] + 3.0 * c[0]));
-    const double ISm1 = (13.0 / 12.0) * (sq(c[-1] - 2.0 * c[0] + c[1])) + (1.0 / 4.0) * (sq(c[-1] - c[1]));
-    const double ISm0 = (13.0 / 12.0) * (sq(c[0] - 2.0 * c[1] + c[2])) + (1.0 / 4.0) * (sq(3.0 * c[0] - 4.0 * c[1] + c[2]));
-    const double ISp2 = (13.0 / 12.0) * (sq(c[-1] - 2.0 * c[0] + c[1])) + (1.0 / 4.0) * (sq(c[-1] - 4.0 * c[0] + 3.0 * c[1]));
-    const double ISp1 = (13.0 / 12.0) * (sq(c[0] - 2.0 * c[1] + c[2])) + (1.0 / 4.0) * (sq(c[0] - c[2]));
-    const double ISp0 = (13.0 / 12.0) * (sq(c[1] - 2.0 * c[2] + c[3])) + (1.0 / 4.0) * (sq(3.0 * c[1] - 4.0 * c[2] + c[3]));
+    const double ISm2 = (13.0 / 12.0) * (sq(c[-2] - scale2<1>(c[-1]) + c[0])) + scale2<-2>(sq(c[-2] - scale2<2>(c[-1]) + 3.0 * c[0]));
+    const double ISm1 = (13.0 / 12.0) * (sq(c[-1] - scale2<1>(c[0]) + c[1])) + scale2<-2>(sq(c[-1] - c[1]));
+    const double ISm0 = (13.0 / 12.0) * (sq(c[0] - scale2<1>(c[1]) + c[2])) + scale2<-2>(sq(3.0 * c[0] - scale2<2>(c[1]) + c[2]));
+    const double ISp2 = (13.0 / 12.0) * (sq(c[-1] - scale2<1>(c[0]) + c[1])) + scale2<-2>(sq(c[-1] - scale2<2>(c[0]) + 3.0 * c[1]));
+    const double ISp1 = (13.0 / 12.0) * (sq(c[0] - scale2<1>(c[1]) + c[2])) + scale2<-2>(sq(c[0] - c[2]));
+    const double ISp0 = (13.0 / 12.0) * (sq(c[1] - scale2<1>(c[2]) + c[3])) + scale2<-2>(sq(3.0 * c[1] - scale2<2>(c[2]) + c[3]));
     const double wp0 = (1.0 / 16.0) / (sq(eps + (ISp0)));
     const double wp1 = (5.0 / 8.0) / (sq(eps + (ISp1)));
     const double wp2 = (5.0 / 16.0) / (sq(eps + (ISp2)));
@@ -123,7 +126,7 @@ __device__ __forceinline__ StateQuot state_quot(const double q[5])
 __device__ __forceinline__ void cart_flux(const double q[5], const StateQuot &t, double F[5], double E[5], double G[5])
 {
     const double k1 = t.k1, k2 = t.k2, k3 = t.k3;
-    const double pr = 0.4 * (q[4] - 0.5 * (k1 + k2 + k3));
+    const double pr = 0.4 * (q[4] - xdiv::scale2<-1>(k1 + k2 + k3));
     const double hq = (1.4 * q[4] - 0.2 * (k1 + k2 + k3));
     F[0] = q[1];
     F[1] = k1 + pr;
@@ -146,7 +149,7 @@ __device__ __forceinline__ void cart_flux(const double q[5], const StateQuot &t,
 __device__ __forceinline__ double lambda5(const double q[5], const StateQuot &t, double mx, double my, double mz)
 {
     return (mx * t.v1 + my * t.v2 + mz * t.v3)
-           + sqrt(1.4 * 0.4 * (t.v4 - ((q[1] * q[1] + q[2] * q[2] + q[3] * q[3]) / (2.0 * (q[0] * q[0]))))
+           + sqrt(1.4 * 0.4 * (t.v4 - ((q[1] * q[1] + q[2] * q[2] + q[3] * q[3]) / xdiv::scale2<1>(q[0] * q[0])))
                   * (mx * mx + my * my + mz * mz));
 }
 
@@ -160,7 +163,7 @@ __device__ __forceinline__ void face_flux(const double pts[6][5], double mx, dou
 {
     const double ru = r[0], rv = r[1], rw = r[2], rh = r[3], rrho = r[4];
     const double kk = sqrt(mx * mx + my * my + mz * mz);
-    const double a = sqrt(0.4 * (rh - 0.5 * (ru * ru + rv * rv + rw * rw)));
+    const double a = sqrt(0.4 * (rh - xdiv::scale2<-1>(ru * ru + rv * rv + rw * rw)));
     const Over<SD> dk(kk);
     const double kx = dk(mx), ky = dk(my), kz = dk(mz);
     const double theta = kx * ru + ky * rv + kz * rw;
@@ -226,7 +229,7 @@ __device__ __forceinline__ void face_flux(const double pts[6][5], double mx, dou
         const double fcp = DET_F * (mx * Fp[c] + my * Ep[c] + mz * Gp[c]);
         const double fcn = DET_F * (mx * Fn[c] + my * En[c] + mz * Gn[c]);
         const double qpd = DET_F * qp[c], qnd = DET_F * qn[c];
-        Fhat[c] = 0.5 * (fcp + fcn - al * (qpd - qnd));
+        Fhat[c] = xdiv::scale2<-1>(fcp + fcn - al * (qpd - qnd));
     }
 }
 
@@ -235,7 +238,7 @@ __device__ __forceinline__ void face_flux(const double pts[6][5], double mx, dou
 __device__ __forceinline__ double corrected(double Fhat, const double f[6])
 {
     const double d2 = (1.0 / 48.0) * (-5.0 * f[0] + 39.0 * f[1] - 34.0 * f[2] - 34.0 * f[3] + 39.0 * f[4] - 5.0 * f[5]);
-    const double d4 = (1.0 / 2.0) * (f[0] - 3.0 * f[1] + 2.0 * f[2] + 2.0 * f[3] - 3.0 * f[4] + f[5]);
+    const double d4 = xdiv::scale2<-1>(f[0] - 3.0 * f[1] + xdiv::scale2<1>(f[2]) + xdiv::scale2<1>(f[3]) - 3.0 * f[4] + f[5]);
     return Fhat - (1.0 / 24.0) * d2 + (7.0 / 5760.0) * d4;
 }
 
@@ -276,7 +279,7 @@ __device__ __forceinline__ void viscous_node(const double dU[3][5], const double
         tc[d] = (1.0 / U0_I) * (dU[d][4]) - (U4_I / ((U0_I * U0_I))) * (dU[d][0]) - (U1_I / U0_I) * uc[d]
                 - (U2_I / U0_I) * vc[d] - (U3_I / U0_I) * wc[d];
     const double d_temp = (1.4 * Mach * Mach * 0.4
-                           * ((U4_I / U0_I) - 0.5 * (((U1_I * U1_I) / (U0_I * U0_I)) + ((U2_I * U2_I) / (U0_I * U0_I))
+                           * ((U4_I / U0_I) - xdiv::scale2<-1>(((U1_I * U1_I) / (U0_I * U0_I)) + ((U2_I * U2_I) / (U0_I * U0_I))
                                                      + ((U3_I * U3_I) / (U0_I * U0_I)))));
     const double d_temp1 = sqrt(d_temp) * sqrt(d_temp) * sqrt(d_temp);
     const double mu = (d_temp1) * ((1.0 + (110.4 / Free_t)) / (d_temp + (110.4 / Free_t)));
@@ -301,11 +304,12 @@ __device__ __forceinline__ void viscous_node(const double dU[3][5], const double
     const double u = prim[1], v = prim[2], w = prim[3];
     if (P.les) {
         const double C_MTS = 0.03, C_T = 10.0;
-        const double stress_yz = (0.5 * (vc[0] * zeta_z + vc[1] * eta_z + vc[2] * xi_z + wc[0] * zeta_y + wc[1] * eta_y + wc[2] * xi_y));
-        const double stress_xz = (0.5 * (wc[0] * zeta_x + wc[1] * eta_x + wc[2] * xi_x + uc[0] * zeta_z + uc[1] * eta_z + uc[2] * xi_z));
-        const double stress_xy = (0.5 * s_xy);
+        using xdiv::scale2;   // products by powers of two on the integer pipe, same bits
+        const double stress_yz = (scale2<-1>(vc[0] * zeta_z + vc[1] * eta_z + vc[2] * xi_z + wc[0] * zeta_y + wc[1] * eta_y + wc[2] * xi_y));
+        const double stress_xz = (scale2<-1>(wc[0] * zeta_x + wc[1] * eta_x + wc[2] * xi_x + uc[0] * zeta_z + uc[1] * eta_z + uc[2] * xi_z));
+        const double stress_xy = (scale2<-1>(s_xy));
         const double stress_xx = GX(uc), stress_yy = GY(vc), stress_zz = GZ(wc);
-        const double mod_stress = sqrt(2.0 * ((stress_xy * stress_xy + stress_yz * stress_yz + stress_xz * stress_xz)
+        const double mod_stress = sqrt(scale2<1>((stress_xy * stress_xy + stress_yz * stress_yz + stress_xz * stress_xz)
                                               + (2.0 / 3.0) * (stress_xx * stress_xx + stress_yy * stress_yy + stress_zz * stress_zz)));
         const double DEL = (1.0 / cbrt(DET_I));
         double EDDY_x, EDDY_y, EDDY_z;
@@ -313,8 +317,8 @@ __device__ __forceinline__ void viscous_node(const double dU[3][5], const double
             // Smagorinsky (no counterpart in the reference): (C_s Delta)^2 |S|,
             // |S| = sqrt(2 S_ij S_ij), Delta = det^(1/3) (the cell size; det is
             // the cell volume), in the reference's SGS terms below
-            const double S = sqrt(2.0 * (stress_xx * stress_xx + stress_yy * stress_yy + stress_zz * stress_zz)
-                                  + 4.0 * (stress_xy * stress_xy + stress_yz * stress_yz + stress_xz * stress_xz));
+            const double S = sqrt(scale2<1>(stress_xx * stress_xx + stress_yy * stress_yy + stress_zz * stress_zz)
+                                  + scale2<2>(stress_xy * stress_xy + stress_yz * stress_yz + stress_xz * stress_xz));
             const double ls = P.cs * cbrt(DET_I);
             EDDY_x = EDDY_y = EDDY_z = (ls * ls) * S;
         } else if (mod_stress != 0.0) {
@@ -329,12 +333,13 @@ __device__ __forceinline__ void viscous_node(const double dU[3][5], const double
             EDDY_y = (C_MTS) * DEL * sqrt(KSv[1]);
             EDDY_z = (C_MTS) * DEL * sqrt(KSv[2]);
         }
-        TAU_XY = -2.0 * U0_I * EDDY_x * (0.5 * s_xy);
-        TAU_YZ = -2.0 * U0_I * EDDY_y * (stress_yz);
-        TAU_XZ = -2.0 * U0_I * EDDY_z * (stress_xz);
-        TAU_XX = -2.0 * U0_I * EDDY_x * stress_xx;
-        TAU_YY = -2.0 * U0_I * EDDY_y * stress_yy;
-        TAU_ZZ = -2.0 * U0_I * EDDY_z * stress_zz;
+        const double m2U0 = -scale2<1>(U0_I);   // -2.0 * U0_I
+        TAU_XY = m2U0 * EDDY_x * (stress_xy);
+        TAU_YZ = m2U0 * EDDY_y * (stress_yz);
+        TAU_XZ = m2U0 * EDDY_z * (stress_xz);
+        TAU_XX = m2U0 * EDDY_x * stress_xx;
+        TAU_YY = m2U0 * EDDY_y * stress_yy;
+        TAU_ZZ = m2U0 * EDDY_z * stress_zz;
         const double Q_x = (1.0 / (1.4 * 0.4 * Mach * Mach)) * (-1.0) * (EDDY_x) * GX(tc);
         const double Q_y = (1.0 / (1.4 * 0.4 * Mach * Mach)) * (-1.0) * (EDDY_y) * GY(tc);
         const double Q_z = (1.0 / (1.4 * 0.4 * Mach * Mach)) * (-1.0) * (EDDY_z) * GZ(tc);
@@ -384,7 +389,9 @@ __device__ __forceinline__ void node_flux(const double prim[5], const double m[9
 // velocity component c along its own direction.
 __device__ __forceinline__ double ks(double Uc_i, double U0_i, double Uc_m, double U0_m, double Uc_p, double U0_p)
 {
-    return sq(((Uc_i / U0_i) - ((0.25 * Uc_m + 0.5 * Uc_i + 0.25 * Uc_p) / (0.25 * U0_m + 0.5 * U0_i + 0.25 * U0_p))));
+    using xdiv::scale2;   // 0.25 * x and 0.5 * x on the integer pipe, same bits
+    return sq(((Uc_i / U0_i) - ((scale2<-2>(Uc_m) + scale2<-1>(Uc_i) + scale2<-2>(Uc_p))
+                                / (scale2<-2>(U0_m) + scale2<-1>(U0_i) + scale2<-2>(U0_p)))));
 }
 
 // Sutherland viscosity from U only (Viscous.cl:451-458).
@@ -392,7 +399,7 @@ __device__ __forceinline__ double mu_of(const double Ui[5], double Mach, double 
 {
     const double U0_I = Ui[0], U1_I = Ui[1], U2_I = Ui[2], U3_I = Ui[3], U4_I = Ui[4];
     const double d_temp = (1.4 * Mach * Mach * 0.4
-                           * ((U4_I / U0_I) - 0.5 * (((U1_I * U1_I) / (U0_I * U0_I)) + ((U2_I * U2_I) / (U0_I * U0_I))
+                           * ((U4_I / U0_I) - xdiv::scale2<-1>(((U1_I * U1_I) / (U0_I * U0_I)) + ((U2_I * U2_I) / (U0_I * U0_I))
                                                      + ((U3_I * U3_I) / (U0_I * U0_I)))));
     const double d_temp1 = sqrt(d_temp) * sqrt(d_temp) * sqrt(d_temp);
     return (d_temp1) * ((1.0 + (110.4 / Free_t)) / (d_temp + (110.4 / Free_t)));

@@ -1,6 +1,7 @@
 // exact_div_check.cpp -- cfd::xdiv::div(x, b, 1/b) against the host's IEEE
-// division x / b, bit for bit, on the pairs of div_cases.h.  Prints the
-// share of plain-case quotients (no fallback division).
+// division x / b, bit for bit, on the pairs of div_cases.h, and
+// cfd::xdiv::scale2<K>(x) against x * 2^K on every operand of those pairs.
+// Prints the share of plain-case quotients (no fallback division).
 //
 //   exact_div_check <rounds> <seed>
 #include <cstdio>
@@ -34,5 +35,28 @@ int main(int argc, char **argv)
     }
     std::printf("exact_div_check: %zu cases, %ld mismatches, plain case %.4f\n", X.size(), fails,
                 (double)plain / (double)X.size());
-    return fails == 0 ? 0 : 1;
+    long sfails = 0, scases = 0;
+    auto check = [&](double x, double got, double c) {
+        volatile double vx = x, vc = c;
+        const double want = vx * vc;
+        ++scases;
+        if (!(divcases::to_bits(got) == divcases::to_bits(want) || (std::isnan(got) && std::isnan(want)))) {
+            if (sfails < 10)
+                std::printf("SCALE2 MISMATCH x=%016llx c=%g want %016llx got %016llx\n",
+                            (unsigned long long)divcases::to_bits(x), c, (unsigned long long)divcases::to_bits(want),
+                            (unsigned long long)divcases::to_bits(got));
+            ++sfails;
+        }
+    };
+    for (const std::vector<double> *V : {&X, &B})
+        for (double x : *V) {
+            check(x, cfd::xdiv::scale2<1>(x), 2.0);
+            check(x, cfd::xdiv::scale2<2>(x), 4.0);
+            check(x, cfd::xdiv::scale2<3>(x), 8.0);
+            check(x, cfd::xdiv::scale2<-1>(x), 0.5);
+            check(x, cfd::xdiv::scale2<-2>(x), 0.25);
+            check(x, cfd::xdiv::scale2<-3>(x), 0.125);
+        }
+    std::printf("scale2: %ld cases, %ld scale2 mismatches\n", scases, sfails);
+    return fails == 0 && sfails == 0 ? 0 : 1;
 }

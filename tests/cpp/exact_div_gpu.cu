@@ -1,5 +1,6 @@
 // exact_div_gpu.cu -- cfd::xdiv::div(x, b, 1/b) on the GPU against the GPU's
-// own IEEE division x / b, bit for bit, on the pairs of div_cases.h.
+// own IEEE division x / b, bit for bit, on the pairs of div_cases.h, and
+// cfd::xdiv::scale2<K>(x) against the GPU's x * 2^K on every x.
 //
 //   exact_div_gpu <rounds> <seed>
 #include <cstdio>
@@ -15,6 +16,22 @@ __global__ void k_div(const double *x, const double *b, int n, double *want, dou
     const double y = 1.0 / b[i];
     want[i] = x[i] / b[i];
     got[i] = cfd::xdiv::div(x[i], b[i], y);
+}
+
+// out[6 * i + k]: scale2 of x[i] by 2, 4, 8, 1/2, 1/4, 1/8 (got) and the
+// FP64 products (want)
+__global__ void k_scale(const double *x, int n, const double *c, double *want, double *got)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double v = x[i];
+    got[6 * i + 0] = cfd::xdiv::scale2<1>(v);
+    got[6 * i + 1] = cfd::xdiv::scale2<2>(v);
+    got[6 * i + 2] = cfd::xdiv::scale2<3>(v);
+    got[6 * i + 3] = cfd::xdiv::scale2<-1>(v);
+    got[6 * i + 4] = cfd::xdiv::scale2<-2>(v);
+    got[6 * i + 5] = cfd::xdiv::scale2<-3>(v);
+    for (int k = 0; k < 6; ++k) want[6 * i + k] = v * c[k];
 }
 
 int main(int argc, char **argv)
@@ -47,9 +64,36 @@ int main(int argc, char **argv)
     }
     std::printf("exact_div_gpu: %d cases, %ld mismatches against the GPU division, %ld GPU/host division "
                 "differences (%s)\n", n, fails, host_diff, cudaGetErrorString(e));
+    // scale2 on every x and b (2n operands, 6 factors each)
+    const double cs[6] = {2.0, 4.0, 8.0, 0.5, 0.25, 0.125};
+    std::vector<double> V(X);
+    V.insert(V.end(), B.begin(), B.end());
+    const int m = (int)V.size();
+    double *dv, *dc, *sw, *sg;
+    long sfails = 0;
+    cudaError_t e2 = cudaSuccess;
+    if (cudaMalloc(&dv, m * sizeof(double)) || cudaMalloc(&dc, sizeof cs) || cudaMalloc(&sw, 6 * (size_t)m * 8)
+        || cudaMalloc(&sg, 6 * (size_t)m * 8)) {
+        std::printf("cudaMalloc failed\n");
+        return 2;
+    }
+    cudaMemcpy(dv, V.data(), m * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(dc, cs, sizeof cs, cudaMemcpyHostToDevice);
+    k_scale<<<(m + 255) / 256, 256>>>(dv, m, dc, sw, sg);
+    std::vector<double> SW(6 * (size_t)m), SG(6 * (size_t)m);
+    cudaMemcpy(SW.data(), sw, SW.size() * 8, cudaMemcpyDeviceToHost);
+    cudaMemcpy(SG.data(), sg, SG.size() * 8, cudaMemcpyDeviceToHost);
+    e2 = cudaDeviceSynchronize();
+    for (size_t i = 0; i < SW.size(); ++i)
+        sfails += !(divcases::to_bits(SG[i]) == divcases::to_bits(SW[i]) || (std::isnan(SG[i]) && std::isnan(SW[i])));
+    std::printf("scale2: %zu cases, %ld scale2 mismatches (%s)\n", SW.size(), sfails, cudaGetErrorString(e2));
+    cudaFree(dv);
+    cudaFree(dc);
+    cudaFree(sw);
+    cudaFree(sg);
     cudaFree(dx);
     cudaFree(db);
     cudaFree(dw);
     cudaFree(dg);
-    return (fails == 0 && e == cudaSuccess) ? 0 : 1;
+    return (fails == 0 && sfails == 0 && e == cudaSuccess && e2 == cudaSuccess) ? 0 : 1;
 }

@@ -1,8 +1,9 @@
-"""Shared-reciprocal division (csrc/exact_div.cuh) gives the bits of IEEE
-division x / b: on the host against the host's division (CPU), and on the GB300
-against the GPU's own division (GPU), on ~9 million operand pairs per run
-including quotients within ~2^-53 ulp of a rounding midpoint
-(tests/cpp/div_cases.h)."""
+"""Shared-reciprocal division and power-of-two scaling (csrc/exact_div.cuh)
+give the bits of IEEE division x / b and of the product x * 2^K: on the host
+against the host's arithmetic (CPU), and on the GB300 against the GPU's own
+(GPU), on ~9 million operand pairs per run including quotients within
+~2^-53 ulp of a rounding midpoint and operands of every class, subnormal,
+Inf and NaN included (tests/cpp/div_cases.h)."""
 from __future__ import annotations
 
 import pathlib
@@ -25,7 +26,7 @@ def test_exact_division_on_host(tmp_path):
                     str(CPP / "exact_div_check.cpp"), "-o", str(exe)], check=True)
     r = subprocess.run([str(exe), "1000000", "11"], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
-    assert " 0 mismatches" in r.stdout
+    assert " 0 mismatches" in r.stdout and " 0 scale2 mismatches" in r.stdout
 
 
 @pytest.mark.gpu
@@ -36,4 +37,4 @@ def test_exact_division_on_gpu(tmp_path):
                     "-I", str(CSRC), "-I", str(CPP), str(CPP / "exact_div_gpu.cu"), "-o", str(exe)], check=True)
     r = subprocess.run([str(exe), "1000000", "12"], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
-    assert " 0 mismatches" in r.stdout
+    assert " 0 mismatches" in r.stdout and " 0 scale2 mismatches" in r.stdout
