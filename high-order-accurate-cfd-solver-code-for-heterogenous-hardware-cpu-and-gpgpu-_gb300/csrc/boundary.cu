@@ -145,6 +145,14 @@ __global__ void k_bc(A F, const BcEntry *__restrict__ E, int n, int type, double
     if (q < n) apply_entry(F, type, E[q], mach);
 }
 
+// every entry of independent lists in one launch, one thread per entry
+template <class A>
+__global__ void k_bc_fused(A F, const BcEntry *__restrict__ E, BcOffsets off, double mach)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < off.o[BC_NTYPES]) apply_entry(F, bc_type_of(off, q), E[q], mach);
+}
+
 __global__ void k_free_stream(AosFlow F, int sd_node, double mach)
 {
     const int r = 1 + blockIdx.x * blockDim.x + threadIdx.x;
@@ -162,6 +170,10 @@ __global__ void k_free_stream(AosFlow F, int sd_node, double mach)
 template <class A>
 void launch_lists(cudaStream_t st, const BcDevice &bc, const A &F, double mach)
 {
+    if (bc.fused) {
+        if (bc.total() > 0) k_bc_fused<<<blocks_for(bc.total(), 128), 128, 0, st>>>(F, bc.all, bc.off, mach);
+        return;
+    }
     for (int t = 0; t < BC_NTYPES; ++t) {
         if (bc.n[t] == 0) continue;
         const unsigned blocks = bc.seq[t] ? 1u : blocks_for(bc.n[t], 128);
@@ -220,6 +232,31 @@ bool needs_order(int type, const std::vector<BcEntry> &list)
         }
     }
     return false;
+}
+
+// True when no row written by one list is read or written by another.
+bool lists_independent(const BcPlan &plan)
+{
+    std::unordered_map<int32_t, int> writer;   // row -> list
+    std::vector<int32_t> w, r;
+    for (int t = 0; t < BC_NTYPES; ++t)
+        for (const BcEntry &e : plan.list[t]) {
+            entry_rows(t, e, w, r);
+            for (int32_t x : w) {
+                auto it = writer.find(x);
+                if (it != writer.end() && it->second != t) return false;
+                writer[x] = t;
+            }
+        }
+    for (int t = 0; t < BC_NTYPES; ++t)
+        for (const BcEntry &e : plan.list[t]) {
+            entry_rows(t, e, w, r);
+            for (int32_t x : r) {
+                auto it = writer.find(x);
+                if (it != writer.end() && it->second != t) return false;
+            }
+        }
+    return true;
 }
 
 }  // namespace
@@ -284,6 +321,8 @@ bool bc_make_plan(const cfd_grid_t *grid, int32_t n_rows, const int32_t *const r
         }
         plan.sequential[t] = needs_order(t, plan.list[t]);
     }
+    plan.independent = !plan.sequential[0] && !plan.sequential[1] && !plan.sequential[2] && !plan.sequential[3]
+                       && lists_independent(plan);
     return true;
 }
 
@@ -294,6 +333,7 @@ bool bc_remap(const BcPlan &in, const std::vector<int32_t> &n_of, BcPlan &out)
         o = n_of[r];
         return true;
     };
+    out.independent = in.independent;   // the map is one to one
     for (int t = 0; t < BC_NTYPES; ++t) {
         out.list[t] = in.list[t];
         out.sequential[t] = in.sequential[t];
@@ -309,26 +349,28 @@ bool bc_remap(const BcPlan &in, const std::vector<int32_t> &n_of, BcPlan &out)
 cudaError_t bc_upload(const BcPlan &plan, BcDevice &dev, cudaStream_t st)
 {
     bc_free(dev);
+    std::vector<BcEntry> all;
     for (int t = 0; t < BC_NTYPES; ++t) {
         dev.n[t] = (int)plan.list[t].size();
         dev.seq[t] = plan.sequential[t] ? 1 : 0;
-        if (dev.n[t] == 0) continue;
-        cudaError_t e = cudaMalloc(&dev.d[t], plan.list[t].size() * sizeof(BcEntry));
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(dev.d[t], plan.list[t].data(), plan.list[t].size() * sizeof(BcEntry),
-                                cudaMemcpyHostToDevice, st);
-        if (e != cudaSuccess) return e;
+        dev.off.o[t] = (int)all.size();
+        all.insert(all.end(), plan.list[t].begin(), plan.list[t].end());
     }
+    dev.off.o[BC_NTYPES] = (int)all.size();
+    dev.fused = plan.independent;
+    if (all.empty()) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&dev.all, all.size() * sizeof(BcEntry));
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(dev.all, all.data(), all.size() * sizeof(BcEntry), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return e;
+    for (int t = 0; t < BC_NTYPES; ++t) dev.d[t] = dev.n[t] ? dev.all + dev.off.o[t] : nullptr;
     return cudaStreamSynchronize(st);
 }
 
 void bc_free(BcDevice &dev)
 {
-    for (int t = 0; t < BC_NTYPES; ++t) {
-        if (dev.d[t]) cudaFree(dev.d[t]);
-        dev.d[t] = nullptr;
-        dev.n[t] = 0;
-    }
+    if (dev.all) cudaFree(dev.all);
+    dev = BcDevice();
 }
 
 void bc_apply_aos(cudaStream_t st, const BcDevice &bc, double *flow_rows, double mach)
@@ -408,7 +450,7 @@ cfd_status_t cfd_boundary_fill(cfd_ctx_t *ctx, const cfd_bc_t *bc, cfd_flow_t *F
         ctx->launches += sd_node > 0;
     }
     bc_apply_aos(ctx->stream, bc->dev, f, Mach);
-    ctx->launches += bc->dev.launches();
+    ctx->launches += bc->dev.launches() - 1;   // after_launch counts one
     return stage_out(ctx, a, 1, after_launch(ctx, "cfd_boundary_fill"));
 }
 

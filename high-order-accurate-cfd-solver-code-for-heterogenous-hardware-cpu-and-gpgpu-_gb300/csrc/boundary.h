@@ -30,11 +30,26 @@ struct BcEntry {
     int32_t g[3];
 };
 
-// Host plan of the four lists (reference rows).
+// Host plan of the four lists (reference rows).  independent: no list
+// touches a row that another list writes, and no list needs its own order,
+// so all entries may run in one launch in any order.
 struct BcPlan {
     std::vector<BcEntry> list[BC_NTYPES];
     bool sequential[BC_NTYPES] = {false, false, false, false};
+    bool independent = false;
 };
+
+// Offsets of the lists in the concatenated entry array of one launch:
+// list t holds entries [o[t], o[t + 1]).
+struct BcOffsets {
+    int o[BC_NTYPES + 1];
+};
+
+// List of entry q of the concatenated array.
+__host__ __device__ __forceinline__ int bc_type_of(const BcOffsets &off, int q)
+{
+    return (q >= off.o[1]) + (q >= off.o[2]) + (q >= off.o[3]);
+}
 
 // Resolves the lists against the neighbour table.  Fails (with a message)
 // on an index outside [0, n_rows) and on wall nodes that need the
@@ -47,12 +62,21 @@ bool bc_make_plan(const cfd_grid_t *grid, int32_t n_rows, const int32_t *const r
 // lattice node); false if an index has no node.
 bool bc_remap(const BcPlan &in, const std::vector<int32_t> &n_of, BcPlan &out);
 
-// Device copy of a plan.
+// Device copy of a plan: the lists back to back in one array (list t at
+// d[t] = all + off.o[t]); a plan with independent lists runs as one launch.
 struct BcDevice {
+    BcEntry *all = nullptr;
     BcEntry *d[BC_NTYPES] = {nullptr, nullptr, nullptr, nullptr};
     int n[BC_NTYPES] = {0, 0, 0, 0};
     int seq[BC_NTYPES] = {0, 0, 0, 0};
-    int launches() const { return (n[0] > 0) + (n[1] > 0) + (n[2] > 0) + (n[3] > 0); }
+    BcOffsets off{};
+    bool fused = false;
+    int total() const { return off.o[BC_NTYPES]; }
+    int launches() const
+    {
+        if (fused) return total() > 0 ? 1 : 0;
+        return (n[0] > 0) + (n[1] > 0) + (n[2] > 0) + (n[3] > 0);
+    }
 };
 cudaError_t bc_upload(const BcPlan &plan, BcDevice &dev, cudaStream_t st);
 void bc_free(BcDevice &dev);

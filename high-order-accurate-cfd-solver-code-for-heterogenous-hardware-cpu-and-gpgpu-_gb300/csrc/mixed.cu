@@ -177,6 +177,13 @@ __global__ void k_bc_m(LatView g, const BcEntry *__restrict__ E, int n, int type
     if (t < 4 * n) mx::bc_target(g, type, E[t >> 2], t & 3, q, mach);
 }
 
+// every target of independent lists in one launch
+__global__ void k_bc_m_fused(LatView g, const BcEntry *__restrict__ E, BcOffsets off, int q, double mach)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < 4 * off.o[BC_NTYPES]) mx::bc_target(g, bc_type_of(off, t >> 2), E[t >> 2], t & 3, q, mach);
+}
+
 __global__ void k_flow_out_m(LatView g, int q)
 {
     const int n = node_id();
@@ -227,6 +234,10 @@ void mixed_geometry(const StructuredLaunch &S)
 
 void bc_apply_mixed(cudaStream_t st, const BcDevice &bc, const LatView &g, int q, double mach)
 {
+    if (bc.fused) {
+        if (bc.total() > 0) k_bc_m_fused<<<blocks_for(4LL * bc.total(), 128), 128, 0, st>>>(g, bc.all, bc.off, q, mach);
+        return;
+    }
     for (int t = 0; t < BC_NTYPES; ++t) {
         if (bc.n[t] == 0) continue;
         const unsigned blocks = bc.seq[t] ? 1u : blocks_for(4LL * bc.n[t], 128);

@@ -36,6 +36,42 @@ def test_boundary_fill_matches_reference_golden(ctx, initial):
     assert np.array_equal(out, z[f"out_flow_initial{initial}"])
 
 
+@pytest.mark.parametrize("variant,launches", [("channel", 1), ("channel_shared_row", 3), ("golden", 4)])
+def test_independent_lists_fill_in_one_launch(ctx, oracle_mod, variant, launches):
+    """Lists that touch no row another list writes (the channel's outlet,
+    inlet and walls) run as one launch over all entries.  A row in two lists
+    (written by both, so list order decides), or lists that read each
+    other's rows (the golden box), keep one launch per list in list order.
+    Every variant matches the oracle's routine bit for bit."""
+    from cfd_gb300 import cases, runtime
+    if variant == "golden":
+        z, a, bc = golden_inputs()
+        mach, sd_node = float(z["mach"]), int(z["sd_node"])
+    else:
+        c = cases.channel(ni=16, nj=12, nk=8)
+        a, bc = c.copy().arrays, c.bc
+        a["flow"][1:] = np.random.default_rng(3).uniform(0.5, 1.5, a["flow"][1:].shape)
+        mach, sd_node = c.params.mach, c.sd_node
+        if variant == "channel_shared_row":
+            bc = cases.BoundaryLists(outlet=bc.outlet, inlet=bc.inlet, boundary=bc.boundary,
+                                     wall=np.concatenate([bc.wall, bc.outlet[:1]]))
+    bnd = runtime.Boundary(ctx, a["grid"], bc)
+    dev = ctx.alloc(a["flow"].nbytes)
+    try:
+        ctx.write(dev, a["flow"])
+        n0 = ctx.launch_count
+        bnd.fill(dev, mach, 1, sd_node)
+        n = ctx.launch_count - n0
+        out = np.empty_like(a["flow"])
+        ctx.read(out, dev)
+    finally:
+        ctx.free(dev)
+        bnd.close()
+    oracle_mod.boundary_fill(a, bc, mach, 1, sd_node)
+    assert np.array_equal(out, a["flow"])
+    assert n == launches
+
+
 def test_singular_wall_node_is_unsupported(ctx):
     from cfd_gb300 import abi, runtime
     z, a, bc = golden_inputs()
@@ -166,8 +202,7 @@ def test_naca0012_ogrid_fp64_matches_oracle_and_mixed_budget(ctx, oracle_mod):
 
 
 def test_duct_edges_on_the_lattice_path(ctx, oracle_mod):
-    """Walls on four sides: face and edge codes in one wall list (run in list
-    order on the device, as its entries read each other's rows); FP64
+    """Walls on four sides: face and edge codes in one wall list; FP64
     lattice path against the oracle, the gather path, and the mixed form."""
     from cfd_gb300 import cases, runtime
     c = cases.duct()
