@@ -79,10 +79,17 @@ __global__ void __launch_bounds__(256, Ops::kMinBlocks)
 k_batch_stage(const LatView *__restrict__ views, const BatchTile *__restrict__ tiles, int ntiles, int jst,
               unsigned *bar, unsigned *gflags, unsigned long long limit_ns)
 {
+    // Item w is tile w >> 2; the four items of a tile go to four neighbouring
+    // blocks in the same round (they share the tile's data in L2).  The kind
+    // is rotated by the round, (w & 3) + round, which is still a permutation
+    // of the four kinds per tile: without it, a grid of a multiple of 4
+    // blocks gives each block one kind for the whole phase, and the blocks
+    // with the light viscous items idle at the barrier.
     const int items = 4 * ntiles;
+    const int per_round = max(1, (int)gridDim.x >> 2);
     for (int w = blockIdx.x; w < items; w += gridDim.x) {
         const BatchTile t = tiles[w >> 2];
-        const int kind = w & 3;
+        const int kind = ((w & 3) + (w >> 2) / per_round) & 3;
         if ((int)threadIdx.x < t.count) {
             const LatView &g = views[t.inst];
             const int n = t.n0 + threadIdx.x;
