@@ -8,15 +8,23 @@
 namespace cfd {
 namespace {
 
+// 1: shared reciprocals in the face flux (exact_div.cuh), as in the
+// single-lattice kernels.  Plain divisions measured faster here (64
+// vortices: 2.12e7 against 1.92e7 cell-updates/s; same bits either way).
+#ifndef CFD_FBATCH_SHARED_DIV
+#define CFD_FBATCH_SHARED_DIV 0
+#endif
+
 struct Ops {
     static constexpr int kMinBlocks = 1;
     static __device__ __forceinline__ void prep(const LatView &g, int n, int q) { ex::prep_node(g, n, q); }
     static __device__ __forceinline__ void visc(const LatView &g, int n, int q) { ex::visc_node(g, n, q); }
     static __device__ __forceinline__ void mu(const LatView &g, int n, int q) { ex::mu_node(g, n, q); }
     template <int D>
-    // plain divisions: in the persistent batched kernel the shared
-    // reciprocals measured 5 % slower (same bits either way)
-    static __device__ __forceinline__ void face(const LatView &g, int n) { ex::face_node<D, false>(g, n); }
+    static __device__ __forceinline__ void face(const LatView &g, int n)
+    {
+        ex::face_node<D, CFD_FBATCH_SHARED_DIV != 0>(g, n);
+    }
     static __device__ __forceinline__ void update(const LatView &g, int n, int j) { ex::update_node(g, n, j, true); }
 };
 
