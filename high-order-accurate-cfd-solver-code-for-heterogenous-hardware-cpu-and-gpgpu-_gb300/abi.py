@@ -97,7 +97,12 @@ PROTOTYPES = {
     "cfd_batch_instance_bytes": (C.c_uint64, [_i32, C.c_int64]),
     "cfd_batch_add": (C.c_int, [_vp, C.POINTER(Geometry), C.POINTER(Params), _vp, _d, C.POINTER(_i32)]),
     "cfd_batch_remove": (C.c_int, [_vp, _i32]),
+    "cfd_batch_stage": (C.c_int, [C.POINTER(Geometry), C.POINTER(Params), _vp, _d, C.POINTER(_vp)]),
+    "cfd_batch_add_staged": (C.c_int, [_vp, _vp, C.POINTER(_i32)]),
+    "cfd_batch_staged_free": (C.c_int, [_vp]),
     "cfd_batch_step": (C.c_int, [_vp, _i32]),
+    "cfd_batch_step_async": (C.c_int, [_vp, _i32]),
+    "cfd_batch_sync": (C.c_int, [_vp]),
     "cfd_batch_set_hold": (C.c_int, [_vp, _i32, _i32]),
     "cfd_batch_get_flow": (C.c_int, [_vp, _i32, _vp]),
     "cfd_batch_get_u0": (C.c_int, [_vp, _i32, _vp]),

@@ -7,6 +7,9 @@
 // the engine under the serving loop.
 #include <algorithm>
 #include <cstring>
+#include <memory>
+#include <new>
+#include <string>
 #include <vector>
 
 #include "batch_kernel.cuh"
@@ -58,6 +61,9 @@ struct cfd_batch {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
     uint64_t total_nodes = 0;
+    cudaEvent_t ev[2] = {nullptr, nullptr};   // ends of the last two cfd_batch_step_async calls
+    bool ev_live[2] = {false, false};
+    int ev_next = 0;
 };
 
 namespace {
@@ -277,6 +283,8 @@ cfd_status_t cfd_batch_destroy(cfd_batch_t *b)
     use_device(b->ctx);
     cudaStreamSynchronize(b->ctx->stream);
     drop_graph(b);
+    for (cudaEvent_t e : b->ev)
+        if (e) cudaEventDestroy(e);
     for (auto &I : b->slots) free_instance(I);
     if (b->d_views) cudaFree(b->d_views);
     if (b->d_tiles) cudaFree(b->d_tiles);
@@ -285,16 +293,38 @@ cfd_status_t cfd_batch_destroy(cfd_batch_t *b)
     return CFD_OK;
 }
 
-cfd_status_t cfd_batch_add(cfd_batch_t *b, const cfd_geometry_t *geom, const cfd_params_t *params,
-                           const cfd_flow_t *flow, double del_t, int32_t *slot_out)
+}  // extern "C"
+
+// An instance checked and converted on the host (cfd_batch_stage), waiting
+// for its device half (cfd_batch_add_staged).
+struct cfd_batch_staged {
+    cfd_status_t status = CFD_OK;
+    std::string error;
+    int32_t g_node = 0;
+    int ni = 0, nj = 0, nk = 0, N = 0;
+    cfd_params_t prm{};
+    double dt = 0.0;
+    HostDoubles m9, det, fm, fdet, flow;   // lattice geometry (SoA) and FLOW rows 0..N
+};
+
+extern "C" {
+
+cfd_status_t cfd_batch_stage(const cfd_geometry_t *geom, const cfd_params_t *params, const cfd_flow_t *flow,
+                             double del_t, cfd_batch_staged_t **out)
 {
-    if (!b || !geom || !flow || !slot_out || !std::isfinite(del_t)) return CFD_EINVAL;
-    *slot_out = -1;
-    cfd_ctx *ctx = b->ctx;
-    cfd_status_t st = use_device(ctx);
-    if (st != CFD_OK) return st;
+    if (!out) return CFD_EINVAL;
+    *out = nullptr;
+    cfd_batch_staged *S = new (std::nothrow) cfd_batch_staged;
+    if (!S) return CFD_ENOMEM;
+    *out = S;
+    auto bad = [&](cfd_status_t st, const char *msg) {
+        S->status = st;
+        S->error = msg;
+        return st;
+    };
+    if (!geom || !flow || !std::isfinite(del_t)) return bad(CFD_EINVAL, "cfd_batch_add: null argument or bad time step");
     if (!geom->grid || !geom->det || !geom->deter || !geom->metric || geom->g_node < 1)
-        return fail(ctx, CFD_EINVAL, "cfd_batch_add: bad geometry");
+        return bad(CFD_EINVAL, "cfd_batch_add: bad geometry");
     std::atomic<bool> out_of_range{false};
     host_parallel_for((long long)geom->g_node + 1, [&](long long r0, long long r1) {
         for (long long r = r0; r < r1; ++r)
@@ -303,15 +333,58 @@ cfd_status_t cfd_batch_add(cfd_batch_t *b, const cfd_geometry_t *geom, const cfd
                 if (v < 0 || v > geom->g_node) out_of_range = true;
             }
     });
-    if (out_of_range) return fail(ctx, CFD_EINVAL, "cfd_batch_add: neighbour index out of range");
+    if (out_of_range) return bad(CFD_EINVAL, "cfd_batch_add: neighbour index out of range");
     LatticeMap map;
     bool natural = map_lattice(geom, map) && !map.ghosted() && faces_single_valued(geom, map)
                    && (long long)map.ni * map.nj * map.nk <= kLatticeMaxNodes;
     for (size_t n = 0; natural && n < map.row_of.size(); ++n) natural = map.row_of[n] == (int32_t)n + 1;
     if (!natural)
-        return fail(ctx, CFD_EUNSUPPORTED, "cfd_batch_add: batched instances must be periodic lattices in row order");
-    const int ni = map.ni, nj = map.nj, nk = map.nk;
-    const int N = ni * nj * nk;
+        return bad(CFD_EUNSUPPORTED, "cfd_batch_add: batched instances must be periodic lattices in row order");
+    S->g_node = geom->g_node;
+    S->ni = map.ni;
+    S->nj = map.nj;
+    S->nk = map.nk;
+    S->N = map.ni * map.nj * map.nk;
+    cfd_params_default(&S->prm);
+    if (params) S->prm = *params;
+    S->dt = del_t;
+    lattice_geometry_soa(geom, map, S->m9, S->det, S->fm, S->fdet);
+    const size_t rows = 9 * ((size_t)S->N + 1);
+    S->flow.resize(rows);
+    const double *src = reinterpret_cast<const double *>(flow);
+    double *dst = host_ptr(S->flow);
+    host_parallel_for((long long)rows, [&](long long a, long long e) { std::copy(src + a, src + e, dst + a); });
+    return CFD_OK;
+}
+
+cfd_status_t cfd_batch_staged_free(cfd_batch_staged_t *staged)
+{
+    delete staged;
+    return CFD_OK;
+}
+
+cfd_status_t cfd_batch_add(cfd_batch_t *b, const cfd_geometry_t *geom, const cfd_params_t *params,
+                           const cfd_flow_t *flow, double del_t, int32_t *slot_out)
+{
+    if (!b || !slot_out) return CFD_EINVAL;
+    *slot_out = -1;
+    cfd_batch_staged *S = nullptr;
+    const cfd_status_t st = cfd_batch_stage(geom, params, flow, del_t, &S);
+    if (!S) return st;
+    return cfd_batch_add_staged(b, S, slot_out);
+}
+
+cfd_status_t cfd_batch_add_staged(cfd_batch_t *b, cfd_batch_staged_t *staged, int32_t *slot_out)
+{
+    std::unique_ptr<cfd_batch_staged> S(staged);
+    if (!b || !S || !slot_out) return CFD_EINVAL;
+    *slot_out = -1;
+    cfd_ctx *ctx = b->ctx;
+    if (S->status != CFD_OK) return fail(ctx, S->status, S->error);
+    cfd_status_t st = use_device(ctx);
+    if (st != CFD_OK) return st;
+    const int ni = S->ni, nj = S->nj, nk = S->nk;
+    const int N = S->N;
     const uint64_t need = instance_bytes(b->precision, N);
     if (b->used + need > b->capacity) return fail(ctx, CFD_ENOMEM, "cfd_batch_add: device-memory budget exhausted");
     int slot = -1;
@@ -326,14 +399,14 @@ cfd_status_t cfd_batch_add(cfd_batch_t *b, const cfd_geometry_t *geom, const cfd
         slot = (int)b->slots.size() - 1;
     }
     BatchInst &I = b->slots[slot];
-    I.g_node = geom->g_node;
+    I.g_node = S->g_node;
     I.ni = ni;
     I.nj = nj;
     I.nk = nk;
     I.N = N;
-    cfd_params_default(&I.prm);
-    if (params) I.prm = *params;
-    I.dt = del_t;
+    I.prm = S->prm;
+    I.dt = S->dt;
+    const double del_t = S->dt;
     const size_t Nz = (size_t)N;
     double *m9, *det, *fm, *fdet, *prim9, *U0, *U1, *U2;
     if ((st = ialloc(b, I, 9 * Nz, &m9)) || (st = ialloc(b, I, Nz, &det)) || (st = ialloc(b, I, 9 * Nz, &fm))
@@ -389,13 +462,12 @@ cfd_status_t cfd_batch_add(cfd_batch_t *b, const cfd_geometry_t *geom, const cfd
         }
     }
     cudaStream_t sm = ctx->stream;
-    HostDoubles h, hd, hf, hfd;
-    lattice_geometry_soa(geom, map, h, hd, hf, hfd);
-    cudaError_t e = cudaMemcpyAsync(m9, host_ptr(h), 9 * Nz * 8, cudaMemcpyHostToDevice, sm);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(det, host_ptr(hd), Nz * 8, cudaMemcpyHostToDevice, sm);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(fm, host_ptr(hf), 9 * Nz * 8, cudaMemcpyHostToDevice, sm);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(fdet, host_ptr(hfd), 3 * Nz * 8, cudaMemcpyHostToDevice, sm);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(I.stage9, flow, 9 * (Nz + 1) * 8, cudaMemcpyHostToDevice, sm);
+    cudaError_t e = cudaMemcpyAsync(m9, host_ptr(S->m9), 9 * Nz * 8, cudaMemcpyHostToDevice, sm);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(det, host_ptr(S->det), Nz * 8, cudaMemcpyHostToDevice, sm);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(fm, host_ptr(S->fm), 9 * Nz * 8, cudaMemcpyHostToDevice, sm);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(fdet, host_ptr(S->fdet), 3 * Nz * 8, cudaMemcpyHostToDevice, sm);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(I.stage9, host_ptr(S->flow), 9 * (Nz + 1) * 8, cudaMemcpyHostToDevice, sm);
     if (e == cudaSuccess) e = cudaMemsetAsync(I.stage5, 0, 5 * (Nz + 1) * 8, sm);
     if (e == cudaSuccess) e = cudaMemsetAsync(v.flags, 0, sizeof(unsigned), sm);
     for (double *u : {U0, U1, U2})
@@ -463,7 +535,10 @@ cfd_status_t cfd_batch_set_hold(cfd_batch_t *b, int32_t slot, int32_t hold)
     return CFD_OK;
 }
 
-cfd_status_t cfd_batch_step(cfd_batch_t *b, int32_t nsteps)
+namespace {
+
+// Queues nsteps steps of every instance that is not held.
+cfd_status_t enqueue_steps(cfd_batch_t *b, int32_t nsteps)
 {
     if (!b || nsteps < 0) return CFD_EINVAL;
     cfd_status_t st = use_device(b->ctx);
@@ -477,6 +552,46 @@ cfd_status_t cfd_batch_step(cfd_batch_t *b, int32_t nsteps)
         if (e != cudaSuccess) return cuda_fail(b->ctx, e, "batch step launch");
         b->ctx->launches += 3;
     }
+    return CFD_OK;
+}
+
+}  // namespace
+
+cfd_status_t cfd_batch_step(cfd_batch_t *b, int32_t nsteps)
+{
+    const cfd_status_t st = enqueue_steps(b, nsteps);
+    return st != CFD_OK ? st : finish(b);
+}
+
+cfd_status_t cfd_batch_step_async(cfd_batch_t *b, int32_t nsteps)
+{
+    cfd_status_t st = enqueue_steps(b, nsteps);
+    if (st != CFD_OK) return st;
+    const int k = b->ev_next;
+    if (!b->ev[k]) {
+        const cudaError_t e = cudaEventCreateWithFlags(&b->ev[k], cudaEventDisableTiming);
+        if (e != cudaSuccess) return cuda_fail(b->ctx, e, "cfd_batch_step_async event");
+    }
+    cudaError_t e = cudaEventRecord(b->ev[k], b->ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(b->ctx, e, "cfd_batch_step_async record");
+    b->ev_live[k] = true;
+    b->ev_next = k ^ 1;
+    // the previous call's steps: done before this call returns, so at most
+    // the steps of this call are still queued
+    if (b->ev_live[k ^ 1]) {
+        e = cudaEventSynchronize(b->ev[k ^ 1]);
+        b->ev_live[k ^ 1] = false;
+        if (e != cudaSuccess) return cuda_fail(b->ctx, e, "cfd_batch_step_async wait");
+    }
+    return CFD_OK;
+}
+
+cfd_status_t cfd_batch_sync(cfd_batch_t *b)
+{
+    if (!b) return CFD_EINVAL;
+    cfd_status_t st = use_device(b->ctx);
+    if (st != CFD_OK) return st;
+    b->ev_live[0] = b->ev_live[1] = false;
     return finish(b);
 }
 

@@ -324,6 +324,28 @@ class BatchInfo:
     n_held: int = 0
 
 
+class StagedInstance:
+    """A batch instance converted on the host (Batch.stage), not yet added;
+    freed if it is never added."""
+
+    def __init__(self, lib, h, rows: int):
+        self.lib, self.h, self.rows = lib, h, rows
+
+    def take(self):
+        h, self.h = self.h, None
+        if h is None:
+            raise ValueError("staged instance already added")
+        return h
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None) is not None:
+                self.lib.cfd_batch_staged_free(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+
 class Batch:
     """Many periodic-lattice instances advanced together (cfd_batch_*): one
     persistent launch per RK stage over all instances, CUDA-graph replay."""
@@ -364,12 +386,48 @@ class Batch:
         self.rows[slot.value] = case.g_node + 1
         return slot.value
 
+    @staticmethod
+    def stage(case, flow=None, dt=None, params=None) -> "StagedInstance":
+        """The host half of add() (cfd_batch_stage): checks the table and
+        converts geometry and FLOW into library-owned host memory.  Uses no
+        device, context or batch, and releases the GIL, so it can run on a
+        worker thread while the batch steps."""
+        lib = abi.load()
+        a = case.arrays
+        geom = abi.Geometry(case.g_node, case.sd_node, _ptr(a["grid"]), _ptr(a["det"]), _ptr(a["deter"]),
+                            _ptr(a["metric"]))
+        pr = to_params(params if params is not None else case.params)
+        f = np.ascontiguousarray(a["flow"] if flow is None else flow)
+        h = C.c_void_p()
+        st = lib.cfd_batch_stage(C.byref(geom), C.byref(pr), C.c_void_p(_ptr(f)),
+                                 float(case.dt if dt is None else dt), C.byref(h))
+        if not h.value:
+            raise abi.CfdError(st, "cfd_batch_stage: out of host memory")
+        return StagedInstance(lib, h, case.g_node + 1)
+
+    def add_staged(self, staged: "StagedInstance") -> int:
+        """The device half of add(): allocates, uploads and prepares a staged
+        instance (consumed, also on failure)."""
+        h = staged.take()
+        slot = C.c_int32()
+        self.ctx.check(self.lib.cfd_batch_add_staged(self.h, h, C.byref(slot)), "cfd_batch_add_staged")
+        self.rows[slot.value] = staged.rows
+        return slot.value
+
     def remove(self, slot: int):
         self.ctx.check(self.lib.cfd_batch_remove(self.h, int(slot)), "cfd_batch_remove")
         self.rows.pop(slot, None)
 
     def step(self, nsteps: int = 1):
         self.ctx.check(self.lib.cfd_batch_step(self.h, int(nsteps)), "cfd_batch_step")
+
+    def step_async(self, nsteps: int = 1):
+        """Queues the steps; returns once the previous call's steps are done."""
+        self.ctx.check(self.lib.cfd_batch_step_async(self.h, int(nsteps)), "cfd_batch_step_async")
+
+    def sync(self):
+        """Waits for every queued step; raises on their errors."""
+        self.ctx.check(self.lib.cfd_batch_sync(self.h), "cfd_batch_sync")
 
     def set_hold(self, slot: int, hold: bool):
         """A held instance stays resident but is not advanced by step()."""

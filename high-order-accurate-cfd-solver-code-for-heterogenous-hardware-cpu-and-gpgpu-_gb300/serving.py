@@ -8,7 +8,8 @@ stage over all instances) and, between steps:
 * admits queued requests in arrival order while their device-memory
   footprint fits the batch budget (``cfd_batch_instance_bytes``);
 * picks the admitted solves that advance in this step (``policy``) and
-  advances them by one step in one batched launch sequence;
+  queues one step of them (``Batch.step_async``: the host admits and
+  schedules the next step while the device runs this one);
 * retires the solves that reached their step count (their FLOW is read back
   as the result) and frees their memory for the queue.
 
@@ -40,6 +41,7 @@ boundary is exact for the FP64 form (every stage's U_Q rebuilds U from FLOW).
 """
 from __future__ import annotations
 
+import concurrent.futures as cf
 import dataclasses
 import math
 import pathlib
@@ -123,13 +125,15 @@ class Server:
     """Continuous-batching request loop over one ``runtime.Batch``."""
 
     def __init__(self, ctx, precision: int = 1, capacity_bytes: int = 0, keep_results: bool = False,
-                 tune: bool = False, policy: str = "least_work", fill_nodes: int = FILL_NODES):
+                 tune: bool = False, policy: str = "least_work", fill_nodes: int = FILL_NODES,
+                 stage_workers: int = 1):
         if policy not in ("all", "least_work"):
             raise ValueError(f"unknown policy {policy!r}")
         self.batch = runtime.Batch(ctx, precision, capacity_bytes)
         self.precision = precision
         self.policy = policy
         self.fill_nodes = int(fill_nodes)
+        self.stage_workers = int(stage_workers)
         self.keep_results = keep_results
         self.tune = tune
         self.info0 = self.batch.info()
@@ -158,14 +162,50 @@ class Server:
             files.write_restart(ckpt_dir(req), self.batch.get_flow(slot), case.sd_node, req.steps - left, num)
             active[slot][4] = 3 - num
         budget = self.info0.capacity_bytes
-        spent = {"admit": 0.0, "step": 0.0, "retire": 0.0}   # wall time inside the batch calls
+        spent = {"admit": 0.0, "step": 0.0, "sync": 0.0, "retire": 0.0}   # wall time inside the batch calls
+
+        def prepare(req):
+            """Host half of an admission: the case, its restart and the
+            staged instance (runs on the worker thread)."""
+            c = case_cache.get(req.rid) or make_case(req)
+            left, num, flow = req.steps, 1, None
+            if checkpoint_dir is not None:
+                got = files.read_restart(ckpt_dir(req), c.sd_node)
+                if got is not None:
+                    values, it, num = got
+                    flow = files.restart_flow(c.arrays["flow"], values, c.params.mach)
+                    left = req.steps - it
+            return c, left, num, flow, runtime.Batch.stage(c, flow=flow)
+
+        pool = cf.ThreadPoolExecutor(max_workers=self.stage_workers) if self.stage_workers > 0 else None
+        prepared = {}            # rid -> future of prepare(req)
+
+        def prepare_arrived(now, lookahead=2):
+            for req in queue[:lookahead]:
+                if req.arrival > now:
+                    break
+                if req.rid not in prepared:
+                    prepared[req.rid] = pool.submit(prepare, req)
+
+        try:
+            return self._loop(queue, active, held, done, prepare, prepare_arrived, prepared, pool, budget, spent,
+                              clock, checkpoint_dir, checkpoint_every, max_batch_steps, checkpoint)
+        finally:
+            if pool is not None:
+                pool.shutdown(wait=True, cancel_futures=True)
+
+    def _loop(self, queue, active, held, done, prepare, prepare_arrived, prepared, pool, budget, spent, clock,
+              checkpoint_dir, checkpoint_every, max_batch_steps, checkpoint):
         t0 = clock()
         steps_run = 0
         tuned = not self.tune
         while queue or active:
             now = clock() - t0
-            # admission: arrived requests in order while their footprint fits
+            # admission: arrived requests in order while their footprint fits;
+            # their host half runs on the worker while the device steps
             used = self.batch.info().device_bytes
+            if pool is not None:
+                prepare_arrived(now)
             while queue and queue[0].arrival <= now:
                 req = queue[0]
                 need = runtime.Batch.instance_bytes(self.precision, req.n ** 3)
@@ -173,16 +213,19 @@ class Server:
                     if not active:
                         raise RuntimeError(f"request {req.rid} ({req.n}^3) exceeds the device budget")
                     break
-                c = case_cache.get(req.rid) or make_case(req)
-                left, num, flow = req.steps, 1, None
-                if checkpoint_dir is not None:
-                    got = files.read_restart(ckpt_dir(req), c.sd_node)
-                    if got is not None:
-                        values, it, num = got
-                        flow = files.restart_flow(c.arrays["flow"], values, c.params.mach)
-                        left = req.steps - it
+                if pool is None:
+                    job = prepare(req)
+                else:
+                    if req.rid not in prepared:
+                        prepared[req.rid] = pool.submit(prepare, req)
+                    fut = prepared[req.rid]
+                    if not fut.done() and active:
+                        break                  # keep stepping; admit it when it is ready
+                    job = fut.result()
+                    del prepared[req.rid]
+                c, left, num, flow, staged = job
                 ta = clock()
-                slot = self.batch.add(c, flow=flow)
+                slot = self.batch.add_staged(staged)
                 spent["admit"] += clock() - ta
                 used += need
                 active[slot] = [req, left, clock() - t0, c, num]
@@ -212,12 +255,16 @@ class Server:
             if not tuned and len(run) > 1:
                 self.batch.tune(1)
                 tuned = True
-            self.batch.step(1)
+            self.batch.step_async(1)
             spent["step"] += clock() - ts
             steps_run += 1
             finished = [s for s in run if active[s][1] == 1]
             for s in run:
                 active[s][1] -= 1
+            if finished or checkpoint_dir is not None:
+                ts = clock()
+                self.batch.sync()          # results are read after the step has run
+                spent["sync"] += clock() - ts
             if checkpoint_dir is not None:
                 for s in active:
                     if s in finished or (checkpoint_every and steps_run % checkpoint_every == 0):
@@ -230,6 +277,7 @@ class Server:
                 spent["retire"] += clock() - tr
                 held.discard(s)
                 done.append(Completed(req.rid, req.arrival, adm, clock() - t0, req.n ** 3, req.steps, flow))
+        self.batch.sync()
         pending = [a[0].rid for a in active.values()] + [r.rid for r in queue]
         for s in list(active):          # a stop keeps the progress of the solves in flight
             if checkpoint_dir is not None:

@@ -337,11 +337,33 @@ uint64_t cfd_batch_instance_bytes(int32_t precision, int64_t nodes);
  * initial FLOW rows 0..g_node and time step; CFD_ENOMEM beyond the budget. */
 cfd_status_t cfd_batch_add(cfd_batch_t *b, const cfd_geometry_t *geom, const cfd_params_t *params,
                            const cfd_flow_t *flow, double del_t, int32_t *slot);
+/* cfd_batch_add in two halves.  cfd_batch_stage checks the table and
+ * converts the geometry and FLOW into host memory of its own; it touches no
+ * device, context or batch, so it may run on another host thread while the
+ * batch steps (the caller's arrays may be released once it returns).  It
+ * returns the check's status and, unless out of host memory, always sets
+ * *staged.  cfd_batch_add_staged allocates, uploads and prepares the staged
+ * instance (reporting a failed check with its message, as cfd_batch_add
+ * does) and frees *staged in every case; cfd_batch_staged_free discards one
+ * unused. */
+typedef struct cfd_batch_staged cfd_batch_staged_t;
+cfd_status_t cfd_batch_stage(const cfd_geometry_t *geom, const cfd_params_t *params, const cfd_flow_t *flow,
+                             double del_t, cfd_batch_staged_t **staged);
+cfd_status_t cfd_batch_add_staged(cfd_batch_t *b, cfd_batch_staged_t *staged, int32_t *slot);
+cfd_status_t cfd_batch_staged_free(cfd_batch_staged_t *staged);
 cfd_status_t cfd_batch_remove(cfd_batch_t *b, int32_t slot);
 /* nsteps SSP-RK3 steps of every instance that is not held.  CFD_ENONFINITE
  * names the first failing slot in cfd_last_error; the other instances
  * advance normally. */
 cfd_status_t cfd_batch_step(cfd_batch_t *b, int32_t nsteps);
+/* The same steps, queued: returns once the steps of the previous
+ * cfd_batch_step_async call have finished, with this call's steps still
+ * running, so the host can prepare the next step (admission, scheduling)
+ * while the device works.  Errors of queued steps (CFD_ENONFINITE,
+ * CFD_ETIMEOUT) are reported by the next cfd_batch_sync or cfd_batch_step. */
+cfd_status_t cfd_batch_step_async(cfd_batch_t *b, int32_t nsteps);
+/* Waits for every queued step and reports their status. */
+cfd_status_t cfd_batch_sync(cfd_batch_t *b);
 /* hold != 0: the instance stays resident (state, slot and memory) but
  * cfd_batch_step leaves it out until it is released (hold = 0); a
  * scheduler uses this to run a subset of the batch.  Takes effect at the

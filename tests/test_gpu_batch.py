@@ -137,6 +137,77 @@ def test_held_instance_does_not_advance(ctx, precision):
     b.close()
 
 
+def test_staged_add_equals_add(ctx):
+    """cfd_batch_stage on a worker thread + cfd_batch_add_staged give the
+    instance cfd_batch_add gives; a table the batch cannot take fails at
+    cfd_batch_add_staged with the same status; an unused staged instance is
+    freed."""
+    import concurrent.futures as cf
+    from cfd_gb300 import abi, cases, runtime
+    cs = mix_cases()
+    with cf.ThreadPoolExecutor(max_workers=2) as pool:
+        staged = list(pool.map(runtime.Batch.stage, cs[:2]))
+    a = runtime.Batch(ctx, 1)
+    s = [a.add_staged(st) for st in staged]
+    with pytest.raises(ValueError):
+        a.add_staged(staged[0])                      # consumed
+    a.step(2)
+    b = runtime.Batch(ctx, 1)
+    t = [b.add(c) for c in cs[:2]]
+    b.step(2)
+    for x, y in zip(s, t):
+        assert np.array_equal(a.get_flow(x), b.get_flow(y))
+    bad = runtime.Batch.stage(cases.ghost_box(shape=(6, 6, 6)))
+    with pytest.raises(abi.CfdError) as e:
+        a.add_staged(bad)
+    assert e.value.status == abi.EUNSUPPORTED
+    unused = runtime.Batch.stage(cs[3])
+    del unused
+    a.close()
+    b.close()
+
+
+def test_async_steps_equal_steps_and_report_at_sync(ctx):
+    """cfd_batch_step_async queues the same steps as cfd_batch_step (the
+    same bits), also across holds, removals and additions between calls;
+    a non-finite instance is reported by the next cfd_batch_sync."""
+    from cfd_gb300 import abi, runtime
+    cs = mix_cases()
+    a = runtime.Batch(ctx, 1)
+    s = [a.add(c) for c in cs[:3]]
+    for _ in range(3):
+        a.step_async(1)
+    a.set_hold(s[0], True)
+    a.step_async(2)
+    a.remove(s[2])
+    s3 = a.add(cs[3])
+    a.step_async(1)
+    a.sync()
+    b = runtime.Batch(ctx, 1)
+    t = [b.add(c) for c in cs[:3]]
+    b.step(3)
+    b.set_hold(t[0], True)
+    b.step(2)
+    b.remove(t[2])
+    t3 = b.add(cs[3])
+    b.step(1)
+    for x, y in ((s[0], t[0]), (s[1], t[1]), (s3, t3)):
+        assert np.array_equal(a.get_flow(x), b.get_flow(y))
+    a.close()
+    b.close()
+    bad = copy_arrays(cs[1].arrays)["flow"]
+    bad[7, 5] = np.nan
+    c = runtime.Batch(ctx, 0)
+    c.add(cs[0])
+    c.add(cs[1], flow=bad)
+    c.step_async(1)
+    c.step_async(1)
+    with pytest.raises(abi.CfdError) as e:
+        c.sync()
+    assert e.value.status == abi.ENONFINITE
+    c.close()
+
+
 def test_tuning_and_graph_do_not_change_results(ctx):
     from cfd_gb300 import runtime
     cs = mix_cases()

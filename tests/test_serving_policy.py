@@ -41,6 +41,13 @@ class FakeBatch:
         used = sum(100 * n for n, _ in self.slots.values())
         return types.SimpleNamespace(capacity_bytes=self.capacity, device_bytes=used)
 
+    @staticmethod
+    def stage(case, flow=None):
+        return case
+
+    def add_staged(self, staged):
+        return self.add(staged)
+
     def add(self, case, flow=None):
         s = min(set(range(len(self.slots) + 1)) - set(self.slots))
         self.slots[s] = (case.nodes, 0)
@@ -62,6 +69,12 @@ class FakeBatch:
                 nodes += nn
         FakeBatch.sim[0] += n * (nodes / self.rate + 1e-5)
 
+    def step_async(self, n=1):
+        self.step(n)
+
+    def sync(self):
+        pass
+
     def get_flow(self, slot):
         return np.array([float(self.slots[slot][1])])
 
@@ -73,21 +86,25 @@ class FakeBatch:
         pass
 
 
-def _serve(monkeypatch, reqs, policy, fill):
+def _serve(monkeypatch, reqs, policy, fill, workers=0):
     from cfd_gb300 import serving
     FakeBatch.sim = [0.0]
     monkeypatch.setattr(serving.runtime, "Batch", FakeBatch)
     monkeypatch.setattr(serving.time, "sleep", lambda s: FakeBatch.sim.__setitem__(0, FakeBatch.sim[0] + s))
     cache = {r.rid: types.SimpleNamespace(nodes=r.n ** 3) for r in reqs}
-    srv = serving.Server(None, precision=1, keep_results=True, policy=policy, fill_nodes=fill)
+    srv = serving.Server(None, precision=1, keep_results=True, policy=policy, fill_nodes=fill,
+                         stage_workers=workers)
     return srv.run(reqs, case_cache=cache, clock=lambda: FakeBatch.sim[0])
 
 
-@pytest.mark.parametrize("policy,fill", [("all", 0), ("least_work", 1), ("least_work", 300_000)])
-def test_every_solve_gets_its_steps(pkg, monkeypatch, policy, fill):
+@pytest.mark.parametrize("policy,fill,workers", [("all", 0, 0), ("least_work", 1, 0), ("least_work", 300_000, 0),
+                                                 ("least_work", 300_000, 1), ("all", 0, 2)])
+def test_every_solve_gets_its_steps(pkg, monkeypatch, policy, fill, workers):
+    """Also with the host half of admission on worker threads, where a
+    request joins once its staging is done."""
     from cfd_gb300 import serving
     reqs = serving.poisson_requests(30, rate=50.0, n_range=(16, 96), steps_range=(5, 60), seed=3)
-    out = _serve(monkeypatch, reqs, policy, fill)
+    out = _serve(monkeypatch, reqs, policy, fill, workers)
     assert out["requests"] == len(reqs) and out["pending"] == []
     assert out["policy"] == policy
     for c in out["completed"]:
