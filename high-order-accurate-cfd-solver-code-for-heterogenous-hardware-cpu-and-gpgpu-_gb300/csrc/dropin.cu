@@ -19,9 +19,11 @@
 // neighbour p has this row as its minus neighbour and every input of p's
 // -1/2 face is bit-identical (then so are the stencil rows; face metric,
 // face det and Roe state are compared), also stores it as p's -1/2 face,
-// stamped with the call's generation; k_weno<true> takes a row's -1/2 face
-// from there when stamped, else computes it itself.  The results are the
-// same bits either way.
+// stamped with the call's generation; k_weno_minus computes the -1/2 faces
+// left unstamped (box edges, loc codes, inconsistent tables), and
+// k_weno<true> reads both faces from the scratch, which keeps the FP64 face
+// code and its registers out of it.  The results are the same bits either
+// way.
 #include "internal.h"
 #include "physics_exact.cuh"
 
@@ -303,10 +305,54 @@ __global__ void __launch_bounds__(128, 2) k_weno_plus(Phys P, const double *__re
     }
 }
 
+// Rows of offsets -3..2 of row n along d; false if the chain leaves
+// [0, n_rows).
+__device__ __forceinline__ bool minus_line(const int *grid, int n, int n_rows, int d, int st[6])
+{
+    st[3] = n;
+    int m = n, p = n;
+#pragma unroll
+    for (int o = 1; o <= 3; ++o) {
+        m = grid_nb(grid, m, minus_slot(d));
+        if ((unsigned)m >= (unsigned)n_rows) return false;
+        st[3 - o] = m;
+        if (o <= 2) {
+            p = grid_nb(grid, p, plus_slot(d));
+            if ((unsigned)p >= (unsigned)n_rows) return false;
+            st[3 + o] = p;
+        }
+    }
+    return true;
+}
+
+// The -1/2 face of every row gid < n_items along d = blockIdx.y that
+// k_weno_plus did not stamp, from the row's own face data (metric block
+// 2+2d, DETERM 2d+1, ROE block d+3): Fm and stamp = gen.
+__global__ void __launch_bounds__(128, 2) k_weno_minus(Phys P, const double *__restrict__ deter,
+                                                        const int *__restrict__ grid, const double *__restrict__ Q,
+                                                        const double *__restrict__ metric,
+                                                        const double *__restrict__ roe, const double *__restrict__ F,
+                                                        const double *__restrict__ E, const double *__restrict__ G,
+                                                        int n_items, int n_rows, double *__restrict__ Fm,
+                                                        unsigned *__restrict__ stamp, unsigned gen, long long ld)
+{
+    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int d = blockIdx.y;
+    if (gid >= n_items || stamp[d * ld + gid] == gen) return;
+    int st[6];
+    if (!minus_line(grid, gid, n_rows, d, st)) return;   // k_weno reports the row
+    double Fh[5];
+    face_side(P, gid, d, 1, st, deter, Q, metric, roe, d == 0 ? F : (d == 1 ? E : G), Fh);
+#pragma unroll
+    for (int c = 0; c < 5; ++c) Fm[(d * 5 + c) * ld + gid] = Fh[c];
+    stamp[d * ld + gid] = gen;
+}
+
 // Weno.cl:36-3137: per row, both faces of each direction from the row's own
 // face data (metric blocks, DETERM, ROE_AVERAGING), as the reference does.
 // REUSE: the +1/2 faces come from k_weno_plus (Fp), the -1/2 faces from Fm
-// where stamped with this call's generation.
+// (k_weno_plus or k_weno_minus; every row whose stencil stays in the table
+// is stamped with this call's generation).
 template <bool REUSE>
 __global__ void __launch_bounds__(128) k_weno(Phys P, int j, double mach, double dt, const double *__restrict__ deter,
                                               const double *__restrict__ det, double *__restrict__ U0,
@@ -329,19 +375,22 @@ __global__ void __launch_bounds__(128) k_weno(Phys P, int j, double mach, double
         return;
     }
     double dflux[3][5], dvis[3][5];
-#pragma unroll 1
-    for (int d = 0; d < 3; ++d) {
+    bool bad = false;
+    // direction d's flux and viscous differences (unrolled over d with the
+    // faces from the scratch, a loop when the faces are evaluated here)
+    auto direction = [&](const int d) {
         const double *NF = d == 0 ? F : (d == 1 ? E : G);
         const double *VF = d == 0 ? Fv : (d == 1 ? Ev : Gv);
         double Fh[2][5];
         if (REUSE) {
+            if (stamp[d * ld + gid] != gen) {   // cannot happen when the star is in the table
+                bad = true;
+                return;
+            }
 #pragma unroll
-            for (int c = 0; c < 5; ++c) Fh[0][c] = Fp[(d * 5 + c) * ld + gid];
-            if (stamp[d * ld + gid] == gen) {
-#pragma unroll
-                for (int c = 0; c < 5; ++c) Fh[1][c] = Fm[(d * 5 + c) * ld + gid];
-            } else {
-                face_side(P, gid, d, 1, idx[d], deter, Q, metric, roe, NF, Fh[1]);
+            for (int c = 0; c < 5; ++c) {
+                Fh[0][c] = Fp[(d * 5 + c) * ld + gid];
+                Fh[1][c] = Fm[(d * 5 + c) * ld + gid];
             }
         } else {
 #pragma unroll 1
@@ -359,6 +408,18 @@ __global__ void __launch_bounds__(128) k_weno(Phys P, int j, double mach, double
             for (int o = 0; o < 7; ++o) f[o] = VF[5 * (size_t)idx[d][o] + c];
             dvis[d][c] = weno_visc_deriv_ref(f, Lc);
         }
+    };
+    if (REUSE) {
+        direction(0);
+        direction(1);
+        direction(2);
+    } else {
+#pragma unroll 1
+        for (int d = 0; d < 3; ++d) direction(d);
+    }
+    if (bad) {
+        atomicOr(flags, CFD_FLAG_BAD_INDEX);
+        return;
     }
     double L[5];
 #pragma unroll
@@ -425,6 +486,8 @@ void launch_weno(cudaStream_t st, const Phys &P, int j, double mach, double dt, 
         unsigned *stamp = face_stamps(face_scratch, ld);
         k_weno_plus<<<dim3(nb, 3), 128, 0, st>>>(P, deter, grid, Q, metric, roe, F, E, G, n_items, n_rows, Fp, Fm,
                                                  stamp, gen, ld);
+        k_weno_minus<<<dim3(nb, 3), 128, 0, st>>>(P, deter, grid, Q, metric, roe, F, E, G, n_items, n_rows, Fm, stamp,
+                                                  gen, ld);
         k_weno<true><<<nb, 128, 0, st>>>(P, j, mach, dt, deter, det, U0, U1, U2, grid, Q, metric, roe, Fv, Ev, Gv, F, E,
                                          G, flow, n_items, n_rows, flags, L_out, Fp, Fm, stamp, gen, ld);
     } else {

@@ -106,7 +106,7 @@ inline unsigned next_face_gen(unsigned &g)
 // else 1.
 inline int weno_launches(const double *face_scratch, long long scratch_rows, int n_items)
 {
-    return face_scratch && scratch_rows >= n_items ? 2 : 1;
+    return face_scratch && scratch_rows >= n_items ? 3 : 1;
 }
 
 }  // namespace cfd
