@@ -335,8 +335,13 @@ cfd_status_t cfd_batch_stage(const cfd_geometry_t *geom, const cfd_params_t *par
     });
     if (out_of_range) return bad(CFD_EINVAL, "cfd_batch_add: neighbour index out of range");
     LatticeMap map;
-    bool natural = map_lattice(geom, map) && !map.ghosted() && faces_single_valued(geom, map)
-                   && (long long)map.ni * map.nj * map.nk <= kLatticeMaxNodes;
+    bool natural = false;
+    try {
+        natural = map_lattice(geom, map) && !map.ghosted() && faces_single_valued(geom, map)
+                  && (long long)map.ni * map.nj * map.nk <= kLatticeMaxNodes;
+    } catch (const std::bad_alloc &) {
+        return bad(CFD_ENOMEM, "cfd_batch_add: out of host memory for the lattice map");
+    }
     for (size_t n = 0; natural && n < map.row_of.size(); ++n) natural = map.row_of[n] == (int32_t)n + 1;
     if (!natural)
         return bad(CFD_EUNSUPPORTED, "cfd_batch_add: batched instances must be periodic lattices in row order");
@@ -348,12 +353,17 @@ cfd_status_t cfd_batch_stage(const cfd_geometry_t *geom, const cfd_params_t *par
     cfd_params_default(&S->prm);
     if (params) S->prm = *params;
     S->dt = del_t;
-    lattice_geometry_soa(geom, map, S->m9, S->det, S->fm, S->fdet);
-    const size_t rows = 9 * ((size_t)S->N + 1);
-    S->flow.resize(rows);
-    const double *src = reinterpret_cast<const double *>(flow);
-    double *dst = host_ptr(S->flow);
-    host_parallel_for((long long)rows, [&](long long a, long long e) { std::copy(src + a, src + e, dst + a); });
+    try {
+        lattice_geometry_soa(geom, map, S->m9, S->det, S->fm, S->fdet);
+        const size_t rows = 9 * ((size_t)S->N + 1);
+        S->flow.resize(rows);
+        const double *src = reinterpret_cast<const double *>(flow);
+        double *dst = host_ptr(S->flow);
+        host_parallel_for((long long)rows, [&](long long a, long long e) { std::copy(src + a, src + e, dst + a); });
+    } catch (const std::bad_alloc &) {
+        S->m9 = S->det = S->fm = S->fdet = S->flow = HostDoubles();
+        return bad(CFD_ENOMEM, "cfd_batch_add: out of host memory for the staged geometry");
+    }
     return CFD_OK;
 }
 
