@@ -208,6 +208,26 @@ def test_async_steps_equal_steps_and_report_at_sync(ctx):
     c.close()
 
 
+def test_empty_batch_steps_and_info(ctx):
+    """Steps of a batch with no instance (or only held ones) do nothing and
+    succeed, in both forms and both step calls."""
+    from cfd_gb300 import runtime
+    for prec in (0, 1):
+        b = runtime.Batch(ctx, prec)
+        b.step(2)
+        b.step_async(1)
+        b.sync()
+        assert b.info().n_active == 0 and b.info().nodes_total == 0
+        s = b.add(mix_cases()[0])
+        flow = b.get_flow(s)
+        b.set_hold(s, True)
+        b.step(1)
+        assert np.array_equal(b.get_flow(s), flow)
+        b.remove(s)
+        b.step(1)
+        b.close()
+
+
 def test_tuning_and_graph_do_not_change_results(ctx):
     from cfd_gb300 import runtime
     cs = mix_cases()

@@ -125,6 +125,10 @@ def test_argument_validation(ctx):
     with pytest.raises(abi.CfdError) as e:       # more items than rows
         ctx.uq(dev["U0"], dev["Q"], dev["grid"], dev["det"], dev["flow"], dev["roe"], c.g_node + 2)
     assert e.value.status == abi.EINVAL
+    for n in (0, -1):                             # an empty or negative range
+        with pytest.raises(abi.CfdError) as e:
+            ctx.uq(dev["U0"], dev["Q"], dev["grid"], dev["det"], dev["flow"], dev["roe"], n)
+        assert e.value.status == abi.EINVAL
     with pytest.raises(abi.CfdError) as e:       # a missing buffer
         ctx.uq(None, dev["Q"], dev["grid"], dev["det"], dev["flow"], dev["roe"], c.g_node + 1)
     assert e.value.status == abi.EINVAL
