@@ -81,10 +81,17 @@ struct FaceTile {
     }
 };
 
+// coordinate c in [-2, n + kTile + 3) of a staged stencil line, wrapped
+// (periodic) or clamped; the wrap subtracts instead of dividing (c is at
+// most a few extents away from [0, n))
 __device__ __forceinline__ int tile_coord(const LatView &g, int d, int c)
 {
     const int n = lat_extent(g, d);
-    if (lat_periodic(g, d)) return ((c % n) + n) % n;
+    if (lat_periodic(g, d)) {
+        while (c < 0) c += n;
+        while (c >= n) c -= n;
+        return c;
+    }
     return c < 0 ? 0 : (c >= n ? n - 1 : c);
 }
 
