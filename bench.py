@@ -77,7 +77,7 @@ def parse_args(argv=None):
     p.add_argument("--config", choices=("tgv128", "tgv64", "vortex64"), default="tgv128")
     p.add_argument("--les", choices=("mts", "smagorinsky"), default="mts",
                    help="SGS model of the TGV workloads: the reference's mixed time scale (parity) or "
-                        "Smagorinsky C_s = 0.1 (the model config 2 names)")
+                        "Smagorinsky C_s = 0.1 (the model the Taylor-Green LES workload names)")
     p.add_argument("--cpu-steps", type=int, default=1, help="full steps timed for the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-mixed", action="store_true")
@@ -109,11 +109,11 @@ def make_case(config: str, les: str = "mts"):
         c = cases.taylor_green(n=n)
         cfg = {"workload": f"taylor_green_{n}^3_curvilinear_les", "grid": [n, n, n], "re": 1600, "mach": 0.1,
                "les": les}
-        if les == "smagorinsky":   # config 2's model (C_s = 0.1); the reference implements MTS only
+        if les == "smagorinsky":   # the Taylor-Green LES workload's model (C_s = 0.1); the reference implements MTS only
             c.params = dataclasses.replace(c.params, les=2, smagorinsky_cs=0.1)
             cfg["smagorinsky_cs"] = 0.1
         return c, cfg
-    # config 1 specifies WENO eps = 1e-6 (the reference's constant, 1e-7, is the parity tests' value)
+    # the 64^3 vortex workload specifies WENO eps = 1e-6 (the reference's constant, 1e-7, is the parity tests' value)
     return cases.isentropic_vortex(n=64, weno_eps=1e-6), {"workload": "isentropic_vortex_64^3_periodic_inviscid",
                                                           "grid": [64, 64, 64], "weno_eps": 1e-6}
 

@@ -1,6 +1,6 @@
 """Integral diagnostics of a lattice solution (host, numpy): volume-weighted
 kinetic energy and enstrophy, the quantities the Taylor-Green configuration
-is judged by.  Velocity gradients use the same fourth-order central
+reports.  Velocity gradients use the same fourth-order central
 differences in index space and node metrics as the viscous terms
 (Viscous.cl:285-453), so d u_a / d x_b = sum_d (d u_a / d zeta_d) zeta_d,b."""
 from __future__ import annotations

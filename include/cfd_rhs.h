@@ -49,7 +49,7 @@ typedef enum {
     CFD_ETIMEOUT = 3,      /* a bounded device wait gave up                       */
     CFD_ECUDA = 4,         /* a CUDA runtime call failed (see cfd_last_error)     */
     CFD_ENOMEM = 5,        /* device allocation failed                            */
-    CFD_EUNSUPPORTED = 6   /* request outside what this build supports            */
+    CFD_EUNSUPPORTED = 6   /* request outside what the library supports           */
 } cfd_status_t;
 
 /* ------------------------------------------------ reference data layout -- */

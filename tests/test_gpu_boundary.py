@@ -177,7 +177,7 @@ def test_ghost_box_gather_path_with_boundary(ctx, oracle_mod):
 
 
 def test_naca0012_ogrid_fp64_matches_oracle_and_mixed_budget(ctx, oracle_mod):
-    """Config 3's case at a reduced size: the O-grid on the lattice path with
+    """The NACA0012 O-grid case at a reduced size: the O-grid on the lattice path with
     the wall and inlet/outlet far field filled after every stage, FP64
     against the oracle, and the mixed form's density and pressure."""
     from cfd_gb300 import cases, layout, runtime

@@ -144,7 +144,7 @@ def test_mixed_precision_rejected_on_gather_path(ctx):
 
 
 def test_config1_vortex_64_rhs_and_100_steps(ctx, oracle_mod):
-    """Config 1 at its full size: the RHS of the 64^3 vortex against the
+    """The 64^3 isentropic vortex at its full size: the RHS of the 64^3 vortex against the
     oracle, then 100 SSP-RK3 steps of the face-based path against the drop-in
     (gather) path, an independent GPU implementation of the same kernels."""
     from cfd_gb300 import runtime
@@ -171,7 +171,7 @@ def test_config1_vortex_64_rhs_and_100_steps(ctx, oracle_mod):
 
 
 def test_tgv_kinetic_energy_and_enstrophy_mixed_vs_fp64(ctx):
-    """Config 2's diagnostics on a reduced grid: kinetic energy and enstrophy
+    """The Taylor-Green diagnostics on a reduced grid: kinetic energy and enstrophy
     of the mixed form track the FP64 form to within 1e-6 relative."""
     from cfd_gb300 import diagnostics, runtime
     c = make("tgv", n=24)

@@ -1,5 +1,5 @@
 """Smagorinsky SGS model (les = 2, C_s = params.smagorinsky_cs), the LES
-model config 2 names; the reference implements only the mixed-time-scale
+model the Taylor-Green LES workload names; the reference implements only the mixed-time-scale
 model (Viscous.cl:490-558), so parity for les = 2 is pinned to the oracle's
 restatement of this builder addition, not to the reference.
 
