@@ -234,9 +234,10 @@ __device__ __forceinline__ void visc_node(const LatView &g, int n, int q)
         } else if (!LOC || !lat_locdir(g, d) || !((lflag >> d) & 1u)) {
 #pragma unroll
             for (int c = 0; c < 5; ++c) {
+                // the state slot is read-only in this pass: non-coherent loads
                 const float *H = W + c * N, *L = W + (5 + c) * N;
-                const float d1 = (H[p1] - H[m1]) + (L[p1] - L[m1]);
-                const float d2 = (H[p2] - H[m2]) + (L[p2] - L[m2]);
+                const float d1 = (__ldg(H + p1) - __ldg(H + m1)) + (__ldg(L + p1) - __ldg(L + m1));
+                const float d2 = (__ldg(H + p2) - __ldg(H + m2)) + (__ldg(L + p2) - __ldg(L + m2));
                 dU[d][c] = (1.0f / 12.0f) * (8.0f * d1 - d2);
             }
         } else {
@@ -257,8 +258,8 @@ __device__ __forceinline__ void visc_node(const LatView &g, int n, int q)
             }
         }
         const int c = d + 1;
-        const float um = W[c * N + m1], up = W[c * N + p1];
-        const float rm = W[m1], rp = W[p1];
+        const float um = __ldg(W + c * N + m1), up = __ldg(W + c * N + p1);
+        const float rm = __ldg(W + m1), rp = __ldg(W + p1);
         const float dlt = qdiv(Ui[c], Ui[0]) - qdiv(0.25f * um + 0.5f * Ui[c] + 0.25f * up, 0.25f * rm + 0.5f * Ui[0] + 0.25f * rp);
         KS[d] = dlt * dlt;
     }
@@ -359,7 +360,8 @@ __device__ __forceinline__ void update_node(const LatView &g, int n, int jst)
     for (int d = 0; d < 3; ++d) {
         const int m1 = lat_step(g, i, j, k, d, -1);
 #pragma unroll
-        for (int c = 0; c < 5; ++c) Lf[c] += g.Fh32[(d * 5 + c) * N + n] - g.Fh32[(d * 5 + c) * N + m1];
+        for (int c = 0; c < 5; ++c)   // face and viscous fluxes are read-only here: non-coherent loads
+            Lf[c] += __ldg(g.Fh32 + (d * 5 + c) * N + n) - __ldg(g.Fh32 + (d * 5 + c) * N + m1);
         if (LOC && g.P.viscous && lat_locdir(g, d) && ((lflag >> d) & 1u)) {
             int s[7], L7[7];
 #pragma unroll
@@ -373,7 +375,7 @@ __device__ __forceinline__ void update_node(const LatView &g, int n, int jst)
             for (int c = 0; c < 5; ++c) {
                 float f[7];
 #pragma unroll
-                for (int o = 0; o < 7; ++o) f[o] = Vd[c * N + s[o]];
+                for (int o = 0; o < 7; ++o) f[o] = __ldg(Vd + c * N + s[o]);
                 Lf[c] += branch_deriv<float>(b, f);
             }
         } else if (g.P.viscous) {
@@ -381,7 +383,8 @@ __device__ __forceinline__ void update_node(const LatView &g, int n, int jst)
             const float *Vd = g.V32 + (size_t)d * 5 * N;
 #pragma unroll
             for (int c = 0; c < 5; ++c)
-                Lf[c] += (1.0f / 12.0f) * (8.0f * (Vd[c * N + p1] - Vd[c * N + m1]) - (Vd[c * N + p2] - Vd[c * N + m2]));
+                Lf[c] += (1.0f / 12.0f) * (8.0f * (__ldg(Vd + c * N + p1) - __ldg(Vd + c * N + m1))
+                                           - (__ldg(Vd + c * N + p2) - __ldg(Vd + c * N + m2)));
         }
     }
     if (g.Lout) {

@@ -116,10 +116,10 @@ __global__ void __launch_bounds__(128, CFD_MFACE_MIN_BLOCKS) k_face_tile_m(LatVi
         const int node = c[0] + g.ni * (c[1] + g.nj * c[2]);
         const int e = T::at(b, a);
 #pragma unroll
-        for (int q = 0; q < 5; ++q) {
-            sQ[q][e] = g.Q32[q * N + node];
-            sR[q][e] = g.R32[q * N + node];
-            sF[q][e] = NF[q * N + node];
+        for (int q = 0; q < 5; ++q) {   // read-only in this pass: non-coherent loads
+            sQ[q][e] = __ldg(g.Q32 + q * N + node);
+            sR[q][e] = __ldg(g.R32 + q * N + node);
+            sF[q][e] = __ldg(NF + q * N + node);
         }
     }
     __syncthreads();
