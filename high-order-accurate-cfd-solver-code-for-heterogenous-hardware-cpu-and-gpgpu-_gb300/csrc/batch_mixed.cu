@@ -19,7 +19,8 @@ struct Ops {
     static __device__ __forceinline__ void mu(const LatView &g, int n, int q) { mx::mu_node(g, n, q); }
     template <int D>
     static __device__ __forceinline__ void face(const LatView &g, int n) { mx::face_node<D>(g, n); }
-    static __device__ __forceinline__ void update(const LatView &g, int n, int j) { mx::update_node<false>(g, n, j); }
+    // fluxes written by phase A of the same launch: coherent loads
+    static __device__ __forceinline__ void update(const LatView &g, int n, int j) { mx::update_node<false, false>(g, n, j); }
 };
 
 }  // namespace

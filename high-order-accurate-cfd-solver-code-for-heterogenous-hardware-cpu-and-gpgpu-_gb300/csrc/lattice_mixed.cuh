@@ -334,10 +334,14 @@ __device__ __forceinline__ void face_node(const LatView &g, int n)
 //   jst 1: U2 = 3/4 U0 + 1/4 U1 + 1/4 dt L
 //   jst 2: U0 = 1/3 U0 + 2/3 U2 + 2/3 dt L
 // and the new state lands in slot (jst+1) mod 3, which is also the next
-// stage's U_Q slot.  LOC as for visc_node.
-template <bool LOC>
+// stage's U_Q slot.  LOC as for visc_node.  RO: the face and viscous
+// fluxes were written by an earlier launch, so they may be read through the
+// non-coherent path (not in the batched kernel, which writes them in the
+// same launch).
+template <bool LOC, bool RO = true>
 __device__ __forceinline__ void update_node(const LatView &g, int n, int jst)
 {
+    auto ld = [](const float *p) { return RO ? __ldg(p) : *p; };
     const int N = g.N;
     if (LOC && lat_ghost(g, n)) {
         // Ghosts are the boundary routine's, which fills those next to face
@@ -360,8 +364,7 @@ __device__ __forceinline__ void update_node(const LatView &g, int n, int jst)
     for (int d = 0; d < 3; ++d) {
         const int m1 = lat_step(g, i, j, k, d, -1);
 #pragma unroll
-        for (int c = 0; c < 5; ++c)   // face and viscous fluxes are read-only here: non-coherent loads
-            Lf[c] += __ldg(g.Fh32 + (d * 5 + c) * N + n) - __ldg(g.Fh32 + (d * 5 + c) * N + m1);
+        for (int c = 0; c < 5; ++c) Lf[c] += ld(g.Fh32 + (d * 5 + c) * N + n) - ld(g.Fh32 + (d * 5 + c) * N + m1);
         if (LOC && g.P.viscous && lat_locdir(g, d) && ((lflag >> d) & 1u)) {
             int s[7], L7[7];
 #pragma unroll
@@ -375,7 +378,7 @@ __device__ __forceinline__ void update_node(const LatView &g, int n, int jst)
             for (int c = 0; c < 5; ++c) {
                 float f[7];
 #pragma unroll
-                for (int o = 0; o < 7; ++o) f[o] = __ldg(Vd + c * N + s[o]);
+                for (int o = 0; o < 7; ++o) f[o] = ld(Vd + c * N + s[o]);
                 Lf[c] += branch_deriv<float>(b, f);
             }
         } else if (g.P.viscous) {
@@ -383,8 +386,8 @@ __device__ __forceinline__ void update_node(const LatView &g, int n, int jst)
             const float *Vd = g.V32 + (size_t)d * 5 * N;
 #pragma unroll
             for (int c = 0; c < 5; ++c)
-                Lf[c] += (1.0f / 12.0f) * (8.0f * (__ldg(Vd + c * N + p1) - __ldg(Vd + c * N + m1))
-                                           - (__ldg(Vd + c * N + p2) - __ldg(Vd + c * N + m2)));
+                Lf[c] += (1.0f / 12.0f) * (8.0f * (ld(Vd + c * N + p1) - ld(Vd + c * N + m1))
+                                           - (ld(Vd + c * N + p2) - ld(Vd + c * N + m2)));
         }
     }
     if (g.Lout) {
