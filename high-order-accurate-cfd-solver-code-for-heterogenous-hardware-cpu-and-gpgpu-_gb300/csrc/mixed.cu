@@ -38,12 +38,20 @@ __global__ void __launch_bounds__(256) k_prep_m(LatView g, int src, int dst)
     if (n < g.N) mx::prep_node(g, n, src, dst);
 }
 
+// Blocks of 256 per SM that the viscous pass's registers must allow: 6 on
+// periodic lattices (40 registers: latency bound, more warps help; 4, 5, 6,
+// 8 measured 0.122, 0.114, 0.112, 0.145 ms on TGV 128^3), 4 with loc codes
+// (64 registers; the branch code spills below that: 0.140 ms against 0.148
+// and 0.175 at 5 and 6 on the NACA0012 O-grid).
 #ifndef CFD_MVISC_MIN_BLOCKS
-#define CFD_MVISC_MIN_BLOCKS 4
+#define CFD_MVISC_MIN_BLOCKS 6
+#endif
+#ifndef CFD_MVISC_LOC_MIN_BLOCKS
+#define CFD_MVISC_LOC_MIN_BLOCKS 4
 #endif
 
 template <bool LOC>
-__global__ void __launch_bounds__(256, CFD_MVISC_MIN_BLOCKS) k_visc_m(LatView g, int q)
+__global__ void __launch_bounds__(256, LOC ? CFD_MVISC_LOC_MIN_BLOCKS : CFD_MVISC_MIN_BLOCKS) k_visc_m(LatView g, int q)
 {
     const int n = node_id();
     if (n < g.N) mx::visc_node<LOC>(g, n, q);
