@@ -24,6 +24,8 @@
 // k_weno<true> reads both faces from the scratch, which keeps the FP64 face
 // code and its registers out of it.  The results are the same bits either
 // way.
+#include <algorithm>
+
 #include "internal.h"
 #include "physics_exact.cuh"
 
@@ -325,9 +327,11 @@ __device__ __forceinline__ bool minus_line(const int *grid, int n, int n_rows, i
     return true;
 }
 
-// The -1/2 face of every row gid < n_items along d = blockIdx.y that
-// k_weno_plus did not stamp, from the row's own face data (metric block
-// 2+2d, DETERM 2d+1, ROE block d+3): Fm and stamp = gen.
+// The -1/2 face of every row gid < n_items along each d that k_weno_plus
+// did not stamp, from the row's own face data (metric block 2+2d, DETERM
+// 2d+1, ROE block d+3): Fm and stamp = gen.  A grid-stride scan of the
+// rows, direction by direction, with a resident-sized grid: on a periodic
+// lattice every face is stamped and the pass only reads the stamps.
 __global__ void __launch_bounds__(128, 2) k_weno_minus(Phys P, const double *__restrict__ deter,
                                                         const int *__restrict__ grid, const double *__restrict__ Q,
                                                         const double *__restrict__ metric,
@@ -336,16 +340,19 @@ __global__ void __launch_bounds__(128, 2) k_weno_minus(Phys P, const double *__r
                                                         int n_items, int n_rows, double *__restrict__ Fm,
                                                         unsigned *__restrict__ stamp, unsigned gen, long long ld)
 {
-    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
-    const int d = blockIdx.y;
-    if (gid >= n_items || stamp[d * ld + gid] == gen) return;
-    int st[6];
-    if (!minus_line(grid, gid, n_rows, d, st)) return;   // k_weno reports the row
-    double Fh[5];
-    face_side(P, gid, d, 1, st, deter, Q, metric, roe, d == 0 ? F : (d == 1 ? E : G), Fh);
+    const int stride = gridDim.x * blockDim.x;
+    for (int d = 0; d < 3; ++d) {
+        for (int gid = blockIdx.x * blockDim.x + threadIdx.x; gid < n_items; gid += stride) {
+            if (stamp[d * ld + gid] == gen) continue;
+            int st[6];
+            if (!minus_line(grid, gid, n_rows, d, st)) continue;   // k_weno reports the row
+            double Fh[5];
+            face_side(P, gid, d, 1, st, deter, Q, metric, roe, d == 0 ? F : (d == 1 ? E : G), Fh);
 #pragma unroll
-    for (int c = 0; c < 5; ++c) Fm[(d * 5 + c) * ld + gid] = Fh[c];
-    stamp[d * ld + gid] = gen;
+            for (int c = 0; c < 5; ++c) Fm[(d * 5 + c) * ld + gid] = Fh[c];
+            stamp[d * ld + gid] = gen;
+        }
+    }
 }
 
 // Weno.cl:36-3137: per row, both faces of each direction from the row's own
@@ -473,6 +480,20 @@ void launch_viscous(cudaStream_t st, const Phys &P, const double *U, double *F, 
                                                         n_rows, flags);
 }
 
+// Grid of k_weno_minus: two resident blocks of 128 per SM, at most one
+// thread per row.
+static unsigned minus_blocks(int n_items)
+{
+    const long long want = ((long long)n_items + 127) / 128;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess
+        || sms <= 0) {
+        cudaGetLastError();
+        return (unsigned)std::max(1LL, want);
+    }
+    return (unsigned)std::max(1LL, std::min<long long>(want, 2LL * sms));
+}
+
 void launch_weno(cudaStream_t st, const Phys &P, int j, double mach, double dt, const double *deter,
                  const double *det, double *U0, double *U1, double *U2, const int *grid, const double *Q,
                  const double *metric, const double *roe, const double *Fv, const double *Ev, const double *Gv,
@@ -486,8 +507,8 @@ void launch_weno(cudaStream_t st, const Phys &P, int j, double mach, double dt, 
         unsigned *stamp = face_stamps(face_scratch, ld);
         k_weno_plus<<<dim3(nb, 3), 128, 0, st>>>(P, deter, grid, Q, metric, roe, F, E, G, n_items, n_rows, Fp, Fm,
                                                  stamp, gen, ld);
-        k_weno_minus<<<dim3(nb, 3), 128, 0, st>>>(P, deter, grid, Q, metric, roe, F, E, G, n_items, n_rows, Fm, stamp,
-                                                  gen, ld);
+        k_weno_minus<<<minus_blocks(n_items), 128, 0, st>>>(P, deter, grid, Q, metric, roe, F, E, G, n_items, n_rows,
+                                                             Fm, stamp, gen, ld);
         k_weno<true><<<nb, 128, 0, st>>>(P, j, mach, dt, deter, det, U0, U1, U2, grid, Q, metric, roe, Fv, Ev, Gv, F, E,
                                          G, flow, n_items, n_rows, flags, L_out, Fp, Fm, stamp, gen, ld);
     } else {
