@@ -1,7 +1,7 @@
 // exact_div.cuh -- IEEE-exact FP64 arithmetic with fewer FP64 instructions:
-// x / b with a reciprocal shared between several numerators (div), and
-// x * 2^K on the integer pipe (scale2).  Both return the same bits as the
-// IEEE operation (round to nearest even).
+// x / b with a reciprocal shared between several numerators (div), x * 2^K
+// on the integer pipe (scale2), and 2^K / x from a reciprocal (pow2_over).
+// All return the same bits as the IEEE operation (round to nearest even).
 //
 // Given y = 1/b (one IEEE division, reused for every numerator over b):
 //   q0 = RN(x*y),  r0 = RN(b*(-q0) + x),  q1 = RN(r0*y + q0)
@@ -139,6 +139,26 @@ CFD_XDIV_HD double scale2(double x)
     if (__builtin_expect(e - lo <= hi - lo, 1)) return from_bits(u + ((uint64_t)(int64_t)K << 52));
     if ((u << 1) == 0) return x;
     return ieee_mul(x, c);
+}
+
+// 2^K / x for a constant K, 1 <= |K| <= 8: the same bits as the IEEE
+// division 2^K / x.  Rounding commutes with scaling by a power of two while
+// every value stays a normal number, so with r = 1 / x (IEEE reciprocal,
+// cheaper than a division) the quotient is r with its exponent moved by K;
+// r zero, subnormal or non-finite, or a result within one binade of the
+// normal range's ends, takes the division itself.
+template <int K>
+CFD_XDIV_HD double pow2_over(double x)
+{
+    static_assert(K != 0 && K >= -8 && K <= 8, "pow2_over: 1 <= |K| <= 8");
+    constexpr unsigned lo = K < 0 ? 2u + (unsigned)(-K) : 2u;
+    constexpr unsigned hi = K > 0 ? 2045u - (unsigned)K : 2045u;
+    constexpr double c = K > 0 ? (double)(1u << (K > 0 ? K : 0)) : 1.0 / (double)(1u << (K < 0 ? -K : 0));
+    const double r = 1.0 / x;
+    const uint64_t u = bits(r);
+    const unsigned e = (unsigned)(u >> 52) & 0x7ffu;
+    if (__builtin_expect(e - lo <= hi - lo, 1)) return from_bits(u + ((uint64_t)(int64_t)K << 52));
+    return ieee_div(c, x);
 }
 
 }  // namespace xdiv

@@ -84,12 +84,12 @@ __device__ __forceinline__ void weno_pair(const double cc[6], double eps, double
     const double ISp2 = (13.0 / 12.0) * (sq(c[-1] - scale2<1>(c[0]) + c[1])) + scale2<-2>(sq(c[-1] - scale2<2>(c[0]) + 3.0 * c[1]));
     const double ISp1 = (13.0 / 12.0) * (sq(c[0] - scale2<1>(c[1]) + c[2])) + scale2<-2>(sq(c[0] - c[2]));
     const double ISp0 = (13.0 / 12.0) * (sq(c[1] - scale2<1>(c[2]) + c[3])) + scale2<-2>(sq(3.0 * c[1] - scale2<2>(c[2]) + c[3]));
-    const double wp0 = (1.0 / 16.0) / (sq(eps + (ISp0)));
+    const double wp0 = xdiv::pow2_over<-4>(sq(eps + (ISp0)));   // (1/16) / ...
     const double wp1 = (5.0 / 8.0) / (sq(eps + (ISp1)));
     const double wp2 = (5.0 / 16.0) / (sq(eps + (ISp2)));
     const double wm0 = (5.0 / 16.0) / (sq(eps + (ISm0)));
     const double wm1 = (5.0 / 8.0) / (sq(eps + (ISm1)));
-    const double wm2 = (1.0 / 16.0) / (sq(eps + (ISm2)));
+    const double wm2 = xdiv::pow2_over<-4>(sq(eps + (ISm2)));   // (1/16) / ...
     const Over<SD> sp(wp0 + wp1 + wp2), sm(wm0 + wm1 + wm2);
     const double Wp0 = sp(wp0), Wp1 = sp(wp1), Wp2 = sp(wp2);
     const double Wm0 = sm(wm0), Wm1 = sm(wm1), Wm2 = sm(wm2);

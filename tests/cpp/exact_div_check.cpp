@@ -58,5 +58,25 @@ int main(int argc, char **argv)
             check(x, cfd::xdiv::scale2<-3>(x), 0.125);
         }
     std::printf("scale2: %ld cases, %ld scale2 mismatches\n", scases, sfails);
-    return fails == 0 && sfails == 0 ? 0 : 1;
+    long pfails = 0, pcases = 0;
+    auto pcheck = [&](double x, double got, double c) {
+        volatile double vx = x, vc = c;
+        const double want = vc / vx;
+        ++pcases;
+        if (!(divcases::to_bits(got) == divcases::to_bits(want) || (std::isnan(got) && std::isnan(want)))) {
+            if (pfails < 10)
+                std::printf("POW2_OVER MISMATCH x=%016llx c=%g want %016llx got %016llx\n",
+                            (unsigned long long)divcases::to_bits(x), c, (unsigned long long)divcases::to_bits(want),
+                            (unsigned long long)divcases::to_bits(got));
+            ++pfails;
+        }
+    };
+    for (const std::vector<double> *V : {&X, &B})
+        for (double x : *V) {
+            pcheck(x, cfd::xdiv::pow2_over<-4>(x), 0.0625);
+            pcheck(x, cfd::xdiv::pow2_over<-1>(x), 0.5);
+            pcheck(x, cfd::xdiv::pow2_over<3>(x), 8.0);
+        }
+    std::printf("pow2_over: %ld cases, %ld pow2_over mismatches\n", pcases, pfails);
+    return fails == 0 && sfails == 0 && pfails == 0 ? 0 : 1;
 }

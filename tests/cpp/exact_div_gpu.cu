@@ -34,6 +34,19 @@ __global__ void k_scale(const double *x, int n, const double *c, double *want, d
     for (int k = 0; k < 6; ++k) want[6 * i + k] = v * c[k];
 }
 
+// out[3 * i + k]: pow2_over of x[i] for 2^-4, 2^-1, 2^3 (got) and the FP64
+// divisions (want)
+__global__ void k_pow2_over(const double *x, int n, const double *c, double *want, double *got)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double v = x[i];
+    got[3 * i + 0] = cfd::xdiv::pow2_over<-4>(v);
+    got[3 * i + 1] = cfd::xdiv::pow2_over<-1>(v);
+    got[3 * i + 2] = cfd::xdiv::pow2_over<3>(v);
+    for (int k = 0; k < 3; ++k) want[3 * i + k] = c[k] / v;
+}
+
 int main(int argc, char **argv)
 {
     const long rounds = argc > 1 ? std::atol(argv[1]) : 100000;
@@ -87,6 +100,20 @@ int main(int argc, char **argv)
     for (size_t i = 0; i < SW.size(); ++i)
         sfails += !(divcases::to_bits(SG[i]) == divcases::to_bits(SW[i]) || (std::isnan(SG[i]) && std::isnan(SW[i])));
     std::printf("scale2: %zu cases, %ld scale2 mismatches (%s)\n", SW.size(), sfails, cudaGetErrorString(e2));
+    // pow2_over on every x and b (3 numerators each), reusing the buffers
+    const double pc[3] = {0.0625, 0.5, 8.0};
+    cudaMemcpy(dc, pc, sizeof pc, cudaMemcpyHostToDevice);
+    k_pow2_over<<<(m + 255) / 256, 256>>>(dv, m, dc, sw, sg);
+    std::vector<double> PW(3 * (size_t)m), PG(3 * (size_t)m);
+    cudaMemcpy(PW.data(), sw, PW.size() * 8, cudaMemcpyDeviceToHost);
+    cudaMemcpy(PG.data(), sg, PG.size() * 8, cudaMemcpyDeviceToHost);
+    const cudaError_t e3 = cudaDeviceSynchronize();
+    long pfails = 0;
+    for (size_t i = 0; i < PW.size(); ++i)
+        pfails += !(divcases::to_bits(PG[i]) == divcases::to_bits(PW[i]) || (std::isnan(PG[i]) && std::isnan(PW[i])));
+    std::printf("pow2_over: %zu cases, %ld pow2_over mismatches (%s)\n", PW.size(), pfails, cudaGetErrorString(e3));
+    sfails += pfails;
+    if (e3 != cudaSuccess) e2 = e3;
     cudaFree(dv);
     cudaFree(dc);
     cudaFree(sw);

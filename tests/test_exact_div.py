@@ -26,7 +26,7 @@ def test_exact_division_on_host(tmp_path):
                     str(CPP / "exact_div_check.cpp"), "-o", str(exe)], check=True)
     r = subprocess.run([str(exe), "1000000", "11"], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
-    assert " 0 mismatches" in r.stdout and " 0 scale2 mismatches" in r.stdout
+    assert " 0 mismatches" in r.stdout and " 0 scale2 mismatches" in r.stdout and " 0 pow2_over mismatches" in r.stdout
 
 
 @pytest.mark.gpu
@@ -37,4 +37,4 @@ def test_exact_division_on_gpu(tmp_path):
                     "-I", str(CSRC), "-I", str(CPP), str(CPP / "exact_div_gpu.cu"), "-o", str(exe)], check=True)
     r = subprocess.run([str(exe), "1000000", "12"], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
-    assert " 0 mismatches" in r.stdout and " 0 scale2 mismatches" in r.stdout
+    assert " 0 mismatches" in r.stdout and " 0 scale2 mismatches" in r.stdout and " 0 pow2_over mismatches" in r.stdout
