@@ -28,9 +28,10 @@ Policies:
   it takes to reach ``fill_nodes`` lattice nodes per step, enough to keep the
   GPU busy; the others stay resident, held (``Batch.set_hold``).  This is
   shortest-remaining-work-first with a minimum batch size: the device does
-  the same total work, and small solves finish first.  Under a sustained
-  overload of small requests a large one can wait indefinitely; ``"all"``
-  has no such case.
+  the same total work, and small solves finish first.  Solves that have
+  not advanced for ``max_hold_s`` seconds go first, the longest wait first
+  (aging), so a sustained stream of small requests cannot postpone a large
+  one indefinitely.
 
 Checkpoint/resume: with ``checkpoint_dir`` every solve keeps the reference's
 restart pair (files.py) under ``<dir>/req_<rid>/``, written every
@@ -94,13 +95,21 @@ def poisson_requests(count: int, rate: float = 50.0, n_range=(32, 160), steps_ra
     return out
 
 
-def least_work_first(entries, fill_nodes: int) -> set:
+def least_work_first(entries, fill_nodes: int, max_hold_s: float = math.inf) -> set:
     """Slots that advance under the "least_work" policy.  entries: iterable
-    of (slot, nodes, remaining steps, arrival).  Takes slots in order of
-    nodes x remaining steps (then arrival) until their nodes reach
-    fill_nodes; at least one slot when there is any."""
+    of (slot, nodes, remaining steps, arrival[, seconds since its last
+    step]).  Takes the slots that waited longer than max_hold_s first, the
+    longest wait first, then the others in order of nodes x remaining steps
+    (then arrival), until their nodes reach fill_nodes; at least one slot
+    when there is any."""
+    def key(e):
+        waited = e[4] if len(e) > 4 else 0.0
+        if waited > max_hold_s:
+            return (0, -waited, e[0])
+        return (1, e[1] * e[2], e[3], e[0])
+
     chosen, nodes = set(), 0
-    for slot, n, left, arrival in sorted(entries, key=lambda e: (e[1] * e[2], e[3], e[0])):
+    for slot, n, left, arrival, *_ in sorted(entries, key=key):
         if chosen and nodes >= fill_nodes:
             break
         chosen.add(slot)
@@ -126,7 +135,7 @@ class Server:
 
     def __init__(self, ctx, precision: int = 1, capacity_bytes: int = 0, keep_results: bool = False,
                  tune: bool = False, policy: str = "least_work", fill_nodes: int = FILL_NODES,
-                 stage_workers: int = 1):
+                 stage_workers: int = 1, max_hold_s: float = 5.0):
         if policy not in ("all", "least_work"):
             raise ValueError(f"unknown policy {policy!r}")
         self.batch = runtime.Batch(ctx, precision, capacity_bytes)
@@ -134,6 +143,7 @@ class Server:
         self.policy = policy
         self.fill_nodes = int(fill_nodes)
         self.stage_workers = int(stage_workers)
+        self.max_hold_s = float(max_hold_s)
         self.keep_results = keep_results
         self.tune = tune
         self.info0 = self.batch.info()
@@ -148,7 +158,8 @@ class Server:
         loop early (the unfinished solves are reported as `pending`)."""
         case_cache = {} if case_cache is None else case_cache
         queue = list(sorted(requests, key=lambda r: r.arrival))
-        active = {}              # slot -> [request, remaining steps, admitted time, case, next restart number]
+        active = {}              # slot -> [request, remaining steps, admitted time, case, next restart number,
+        #                                   time of its last step]
         held = set()             # slots the batch currently leaves out of its steps
         done = []
 
@@ -158,7 +169,7 @@ class Server:
             return d
 
         def checkpoint(slot):
-            req, left, _, case, num = active[slot]
+            req, left, _, case, num, _ = active[slot]
             files.write_restart(ckpt_dir(req), self.batch.get_flow(slot), case.sd_node, req.steps - left, num)
             active[slot][4] = 3 - num
         budget = self.info0.capacity_bytes
@@ -228,7 +239,7 @@ class Server:
                 slot = self.batch.add_staged(staged)
                 spent["admit"] += clock() - ta
                 used += need
-                active[slot] = [req, left, clock() - t0, c, num]
+                active[slot] = [req, left, clock() - t0, c, num, clock() - t0]
                 queue.pop(0)
                 if left <= 0:       # finished before the stop: report it again
                     self.batch.remove(slot)
@@ -245,8 +256,9 @@ class Server:
             if self.policy == "all":
                 run = set(active)
             else:
-                run = least_work_first(((s, a[0].n ** 3, a[1], a[0].arrival) for s, a in active.items()),
-                                       self.fill_nodes)
+                now = clock() - t0
+                run = least_work_first(((s, a[0].n ** 3, a[1], a[0].arrival, now - a[5]) for s, a in active.items()),
+                                       self.fill_nodes, self.max_hold_s)
             for s in active:
                 if (s in held) == (s in run):
                     self.batch.set_hold(s, s not in run)
@@ -259,8 +271,10 @@ class Server:
             spent["step"] += clock() - ts
             steps_run += 1
             finished = [s for s in run if active[s][1] == 1]
+            t_step = clock() - t0
             for s in run:
                 active[s][1] -= 1
+                active[s][5] = t_step
             if finished or checkpoint_dir is not None:
                 ts = clock()
                 self.batch.sync()          # results are read after the step has run
@@ -270,7 +284,7 @@ class Server:
                     if s in finished or (checkpoint_every and steps_run % checkpoint_every == 0):
                         checkpoint(s)
             for s in finished:
-                req, _, adm, _, _ = active.pop(s)
+                req, _, adm, _, _, _ = active.pop(s)
                 tr = clock()
                 flow = self.batch.get_flow(s) if self.keep_results else None
                 self.batch.remove(s)

@@ -125,6 +125,48 @@ def test_least_work_lowers_mean_latency(pkg, monkeypatch):
     assert srpt["makespan_s"] < 1.05 * lock["makespan_s"]
 
 
+def test_longest_waiting_slot_goes_first(pkg):
+    from cfd_gb300.serving import least_work_first
+    # (slot, nodes, remaining steps, arrival, seconds since its last step)
+    e = [(0, 1000, 10, 0.0, 9.0), (1, 10, 50, 0.1, 6.0), (2, 100, 3, 0.2, 0.0)]
+    assert least_work_first(e, 1) == {2}                   # no bound on the wait
+    assert least_work_first(e, 1, max_hold_s=5.0) == {0}   # waited longest, despite the most work
+    assert least_work_first(e, 1001, max_hold_s=5.0) == {0, 1}
+    assert least_work_first(e, 1011, max_hold_s=5.0) == {0, 1, 2}
+
+
+def test_aging_bounds_the_wait_of_a_large_solve(pkg, monkeypatch):
+    """A large solve among an overload of small ones: without aging it runs
+    after every small solve of the stream; with a short max_hold_s it takes
+    its turn among the longest-waiting solves and finishes well before the
+    stream is drained."""
+    from cfd_gb300 import serving
+
+    def stream():
+        reqs = [serving.Request(0, 0.0, "vortex", 96, 60, 1)]
+        # small solves (2.6 ms of simulated device time each) arriving every 1 ms: an overload
+        reqs += [serving.Request(r, 0.001 * r, "vortex", 40, 40, 1) for r in range(1, 600)]
+        return reqs
+
+    def finish_of_large(max_hold):
+        FakeBatch.sim = [0.0]
+        monkeypatch.setattr(serving.runtime, "Batch", FakeBatch)
+        monkeypatch.setattr(serving.time, "sleep", lambda s: FakeBatch.sim.__setitem__(0, FakeBatch.sim[0] + s))
+        reqs = stream()
+        cache = {r.rid: types.SimpleNamespace(nodes=r.n ** 3) for r in reqs}
+        srv = serving.Server(None, precision=1, keep_results=True, policy="least_work", fill_nodes=1,
+                             stage_workers=0, max_hold_s=max_hold)
+        out = srv.run(reqs, case_cache=cache, clock=lambda: FakeBatch.sim[0])
+        assert all(c.flow[0] == next(r for r in reqs if r.rid == c.rid).steps for c in out["completed"])
+        big = next(c for c in out["completed"] if c.rid == 0)
+        return big.finished, out["makespan_s"]
+
+    late, makespan = finish_of_large(1e9)
+    early, _ = finish_of_large(0.005)              # one step at least every ~5 ms
+    assert late > 0.9 * makespan                    # starved until the stream drained
+    assert early < 0.8 * late
+
+
 def test_unknown_policy_is_rejected(pkg):
     from cfd_gb300 import serving
     with pytest.raises(ValueError):
