@@ -135,7 +135,7 @@ class Server:
 
     def __init__(self, ctx, precision: int = 1, capacity_bytes: int = 0, keep_results: bool = False,
                  tune: bool = False, policy: str = "least_work", fill_nodes: int = FILL_NODES,
-                 stage_workers: int = 1, max_hold_s: float = 5.0):
+                 stage_workers: int = 1, max_hold_s: float = 5.0, steps_per_call: int = 8):
         if policy not in ("all", "least_work"):
             raise ValueError(f"unknown policy {policy!r}")
         self.batch = runtime.Batch(ctx, precision, capacity_bytes)
@@ -144,6 +144,7 @@ class Server:
         self.fill_nodes = int(fill_nodes)
         self.stage_workers = int(stage_workers)
         self.max_hold_s = float(max_hold_s)
+        self.steps_per_call = max(1, int(steps_per_call))
         self.keep_results = keep_results
         self.tune = tune
         self.info0 = self.batch.info()
@@ -267,13 +268,19 @@ class Server:
             if not tuned and len(run) > 1:
                 self.batch.tune(1)
                 tuned = True
-            self.batch.step_async(1)
+            # several steps per call while nothing can change the schedule: no
+            # request left to arrive, no solve of the step finishing before
+            # its last step, no checkpoint or stop in between
+            k = 1
+            if not queue and checkpoint_dir is None and max_batch_steps is None:
+                k = max(1, min(self.steps_per_call, min(active[s][1] for s in run)))
+            self.batch.step_async(k)
             spent["step"] += clock() - ts
-            steps_run += 1
-            finished = [s for s in run if active[s][1] == 1]
+            steps_run += k
+            finished = [s for s in run if active[s][1] == k]
             t_step = clock() - t0
             for s in run:
-                active[s][1] -= 1
+                active[s][1] -= k
                 active[s][5] = t_step
             if finished or checkpoint_dir is not None:
                 ts = clock()
