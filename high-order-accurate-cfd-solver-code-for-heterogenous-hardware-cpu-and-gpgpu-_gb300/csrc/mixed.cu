@@ -316,15 +316,29 @@ int mixed_stage(const StructuredLaunch &S, int jst, double dt, double *Lout, cud
     }
     if (side) cudaEventRecord(S.join, sv);
     mark();
+    // the three face passes write separate fluxes: the j and k passes run on
+    // their own streams, so that no pass waits for the last wave of another
+    const bool fside = side && S.face_side[0] && S.face_side[1];
+    cudaStream_t sj = fside ? S.face_side[0] : st, sk = fside ? S.face_side[1] : st;
+    if (fside) {
+        cudaStreamWaitEvent(sj, S.fork, 0);
+        cudaStreamWaitEvent(sk, S.fork, 0);
+    }
     launch_face_tile<0>(g, st);
     name("face_i");
     mark();
-    launch_face_tile<1>(g, st);
+    launch_face_tile<1>(g, sj);
     name("face_j");
     mark();
-    launch_face_tile<2>(g, st);
+    launch_face_tile<2>(g, sk);
     name("face_k");
     mark();
+    if (fside) {
+        cudaEventRecord(S.face_join[0], sj);
+        cudaEventRecord(S.face_join[1], sk);
+        cudaStreamWaitEvent(st, S.face_join[0], 0);
+        cudaStreamWaitEvent(st, S.face_join[1], 0);
+    }
     if (side) cudaStreamWaitEvent(st, S.join, 0);
     if (loc)
         k_update_m<true><<<nb256, 256, 0, st>>>(g, jst);

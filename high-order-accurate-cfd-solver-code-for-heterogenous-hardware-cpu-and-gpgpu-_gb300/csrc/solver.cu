@@ -204,6 +204,10 @@ cfd_status_t create_structured(cfd_solver *s, const cfd_geometry_t *g)
             || cudaEventCreateWithFlags(&S.fork, cudaEventDisableTiming) != cudaSuccess
             || cudaEventCreateWithFlags(&S.join, cudaEventDisableTiming) != cudaSuccess)
             return cuda_fail(s->ctx, cudaGetLastError(), "solver side stream");
+        for (int f = 0; f < 2; ++f)
+            if (cudaStreamCreateWithFlags(&S.face_side[f], cudaStreamNonBlocking) != cudaSuccess
+                || cudaEventCreateWithFlags(&S.face_join[f], cudaEventDisableTiming) != cudaSuccess)
+                return cuda_fail(s->ctx, cudaGetLastError(), "solver face streams");
     }
     cudaError_t e = cudaStreamSynchronize(S.stream);   // host vectors go out of scope
     if (e != cudaSuccess) return cuda_fail(s->ctx, e, "solver create sync");
@@ -326,6 +330,13 @@ cfd_status_t cfd_solver_destroy(cfd_solver_t *s)
     }
     if (s->S.fork) cudaEventDestroy(s->S.fork);
     if (s->S.join) cudaEventDestroy(s->S.join);
+    for (int f = 0; f < 2; ++f) {
+        if (s->S.face_side[f]) {
+            cudaStreamSynchronize(s->S.face_side[f]);
+            cudaStreamDestroy(s->S.face_side[f]);
+        }
+        if (s->S.face_join[f]) cudaEventDestroy(s->S.face_join[f]);
+    }
     bc_free(s->bc);
     for (void *p : s->allocs) cudaFree(p);
     delete s;

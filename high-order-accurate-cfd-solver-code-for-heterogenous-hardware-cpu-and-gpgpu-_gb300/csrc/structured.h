@@ -37,10 +37,12 @@ struct StructuredLaunch {
     float *node32 = nullptr;   // [11][N] node metrics, det, det^(-1/3)
     float *idet32 = nullptr;   // [2][N] 1/det hi, lo
     float *prim32 = nullptr;   // [9][N] FP32 pressure (LF_P) and mu (LF_MU) of the stage
-    // mixed form: side stream and fork/join events for the viscous pass
-    // (null: everything on `stream`)
+    // mixed form: side stream and fork/join events for the viscous pass,
+    // and two more for the j and k face passes (null: everything on `stream`)
     cudaStream_t side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
+    cudaStream_t face_side[2] = {nullptr, nullptr};
+    cudaEvent_t face_join[2] = {nullptr, nullptr};
     // lattice shape beyond a plain periodic box (LatView::per, loc8, locdirs,
     // row_of)
     int per = 7;
