@@ -72,9 +72,21 @@ __global__ void __launch_bounds__(256) k_mu_m(LatView g, int q)
 // third axis (B).  It loads the stencil lines (kTile + 5 nodes along D) of
 // Q, the Roe inputs and the node fluxes along D once, coalesced along i,
 // and every face reads its six points from there.
+// Faces per tile along D (a block of 128 threads covers kTile x 128/kTile
+// faces).  TGV 128^3: i tiles of 16 / 32 / 64 / 128 took 0.097 / 0.093 /
+// 0.091 / 0.090 ms, j/k tiles of 4 / 8 / 16 / 32 took 0.098 / 0.094 /
+// 0.092 / 0.102-0.146 ms; 64 keeps small lattices' i lines from idling
+// most of a block.
+#ifndef CFD_MFACE_TILE_I
+#define CFD_MFACE_TILE_I 64
+#endif
+#ifndef CFD_MFACE_TILE_JK
+#define CFD_MFACE_TILE_JK 16
+#endif
+
 template <int D>
 struct FaceTile {
-    static constexpr int kTile = D == 0 ? 32 : 8;       // faces along D
+    static constexpr int kTile = D == 0 ? CFD_MFACE_TILE_I : CFD_MFACE_TILE_JK;   // faces along D
     static constexpr int kWide = 128 / kTile;           // nodes across
     static constexpr int A = D == 0 ? 1 : 0;            // axis across
     static constexpr int B = D == 2 ? 1 : 2;            // axis of the block's line
