@@ -20,10 +20,13 @@
  * sizes.  Row 0 is the reference's dummy row; the NDRange of U_Q and Viscous
  * is g_node+1 rows, that of Weno sd_node+1 rows (Solver.cpp:31-38).
  *
- * Beyond the drop-in, the library offers a resident solver object that runs
- * whole SSP-RK3 steps on the device (cfd_solver_*), selecting a face-based
- * structured-grid path when the neighbour table is a periodic lattice, and a
- * batched solver for many grids in one launch per stage (cfd_batch_*).
+ * Beyond the drop-in, the library offers whole SSP-RK3 steps on the same
+ * buffers (cfd_rk3_step), the reference's boundary routine on the device
+ * (cfd_bc_*, cfd_boundary_fill), a resident solver object (cfd_solver_*)
+ * that selects a face-based lattice path when the neighbour table is a
+ * lattice (periodic, or with ghost layers in non-periodic directions) and
+ * runs FP64 or mixed precision, and a batched solver for many grids in one
+ * launch per stage with scheduling hooks for a request loop (cfd_batch_*).
  *
  * Error handling: every entry point returns a cfd_status_t; none exits the
  * process (the reference prints and calls exit(1), Solver.cpp:378-381).
