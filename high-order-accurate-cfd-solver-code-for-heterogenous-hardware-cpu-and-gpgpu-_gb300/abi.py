@@ -107,6 +107,8 @@ PROTOTYPES = {
     "cfd_batch_get_flow": (C.c_int, [_vp, _i32, _vp]),
     "cfd_batch_get_u0": (C.c_int, [_vp, _i32, _vp]),
     "cfd_batch_slot_status": (C.c_int, [_vp, _i32]),
+    "cfd_batch_set_flow": (C.c_int, [_vp, _i32, _vp]),
+    "cfd_batch_set_wait_limit": (C.c_int, [_vp, C.c_int64]),
     "cfd_batch_set_tiling": (C.c_int, [_vp, _i32, _i32, _i32]),
     "cfd_batch_tune": (C.c_int, [_vp, _i32]),
     "cfd_batch_info": (C.c_int, [_vp, C.POINTER(BatchInfo)]),

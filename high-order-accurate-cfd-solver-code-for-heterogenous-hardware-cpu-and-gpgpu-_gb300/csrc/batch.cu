@@ -27,6 +27,9 @@ constexpr int kMaxSlots = 4096;
 struct BatchInst {
     bool active = false;
     bool held = false;          // resident, but not advanced by cfd_batch_step
+    bool in_table = false;      // in the tile table of the last rebuild
+    bool stepped = false;       // advanced by a step queued since the last finish()
+    bool interrupted = false;   // a barrier timeout cut one of its steps short
     int32_t g_node = 0;
     int ni = 0, nj = 0, nk = 0, N = 0;
     cfd_params_t prm{};
@@ -54,6 +57,7 @@ struct cfd_batch {
     unsigned *d_words = nullptr;          // [0..1] barrier, [2] batch flags, [4..] per-slot flags
     int threads = 128;
     int blocks_override = 0;
+    long long wait_limit_ns = -1;         // barrier deadline (< 0: 5 s + 50 ns per node)
     int blocks = 0;
     bool dirty = true;
     bool use_graph = true;
@@ -113,8 +117,9 @@ cfd_status_t rebuild(cfd_batch *b)
     const int T = b->threads;
     uint64_t nodes = 0;
     for (size_t s = 0; s < b->slots.size(); ++s) {
-        const BatchInst &I = b->slots[s];
-        if (!I.active || I.held) continue;
+        BatchInst &I = b->slots[s];
+        I.in_table = I.active && !I.held;
+        if (!I.in_table) continue;
         const int v = (int)views.size();
         views.push_back(I.view);
         for (int n0 = 0; n0 < I.N; n0 += T) tiles.push_back(BatchTile{v, n0, std::min(T, I.N - n0), 0});
@@ -167,7 +172,8 @@ BatchLaunch launch_of(cfd_batch *b)
     L.bar = bar_words(b);
     L.gflags = batch_flags(b);
     // generous deadline for the barrier: 5 s + 50 ns per node of the batch
-    L.limit_ns = 5000000000ULL + 50ULL * b->total_nodes;
+    L.limit_ns = b->wait_limit_ns >= 0 ? (unsigned long long)b->wait_limit_ns
+                                       : 5000000000ULL + 50ULL * b->total_nodes;
     L.stream = b->ctx->stream;
     return L;
 }
@@ -213,6 +219,15 @@ void try_capture(cfd_batch *b)
 
 // Waits for the stream; batch-level flags become the status, per-slot flags
 // stay readable through cfd_batch_slot_status.
+//
+// A barrier timeout: the blocks that gave up skipped phase B of that stage,
+// so the state of every instance in the launched tile table is part old,
+// part new.  Those instances are marked interrupted (cfd_batch_step refuses
+// to advance them until cfd_batch_set_flow restores them or they are
+// removed), and the batch words are cleared so that the timeout is reported
+// once.  The barrier itself needs no repair: every block counts its arrival
+// before it waits, and the last one resets the count and advances the
+// generation, so the words are consistent after every launch.
 cfd_status_t finish(cfd_batch *b)
 {
     std::vector<unsigned> w(4 + b->slots.size());
@@ -220,7 +235,24 @@ cfd_status_t finish(cfd_batch *b)
                                     b->ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->ctx->stream);
     if (e != cudaSuccess) return cuda_fail(b->ctx, e, "batch finish");
-    if (w[2] & CFD_FLAG_TIMEOUT) return fail(b->ctx, CFD_ETIMEOUT, "batch: grid barrier deadline expired");
+    const bool timeout = (w[2] & CFD_FLAG_TIMEOUT) != 0;
+    std::string which;
+    for (size_t s = 0; s < b->slots.size(); ++s) {
+        BatchInst &I = b->slots[s];
+        if (timeout && I.active && I.stepped) {
+            I.interrupted = true;
+            which += (which.empty() ? "" : ",") + std::to_string(s);
+        }
+        I.stepped = false;
+    }
+    if (timeout) {
+        e = cudaMemsetAsync(b->d_words, 0, 4 * sizeof(unsigned), b->ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(b->ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(b->ctx, e, "batch finish (clear timeout)");
+        return fail(b->ctx, CFD_ETIMEOUT,
+                    "batch: grid barrier deadline expired; slots " + which
+                        + " interrupted (restore with cfd_batch_set_flow or remove)");
+    }
     for (size_t s = 0; s < b->slots.size(); ++s)
         if (b->slots[s].active && (w[4 + s] & CFD_FLAG_NONFINITE))
             return fail(b->ctx, CFD_ENONFINITE, "batch: non-finite state in slot " + std::to_string(s));
@@ -553,8 +585,16 @@ cfd_status_t enqueue_steps(cfd_batch_t *b, int32_t nsteps)
     if (!b || nsteps < 0) return CFD_EINVAL;
     cfd_status_t st = use_device(b->ctx);
     if (st != CFD_OK) return st;
+    for (size_t s = 0; s < b->slots.size(); ++s) {
+        const BatchInst &I = b->slots[s];
+        if (I.active && !I.held && I.interrupted)
+            return fail(b->ctx, CFD_ETIMEOUT,
+                        "cfd_batch_step: slot " + std::to_string(s)
+                            + " was interrupted by a barrier timeout; restore it with cfd_batch_set_flow or remove it");
+    }
     if (b->dirty && (st = rebuild(b)) != CFD_OK) return st;
     if (b->ntiles == 0 || nsteps == 0) return CFD_OK;
+    for (auto &I : b->slots) I.stepped = I.stepped || (I.active && I.in_table);
     if (b->use_graph && !b->graph_ok) try_capture(b);
     cudaStream_t sm = b->ctx->stream;
     for (int s = 0; s < nsteps; ++s) {
@@ -637,11 +677,49 @@ cfd_status_t cfd_batch_get_u0(cfd_batch_t *b, int32_t slot, cfd_column_t *host)
 cfd_status_t cfd_batch_slot_status(cfd_batch_t *b, int32_t slot)
 {
     if (!b || slot < 0 || slot >= (int)b->slots.size() || !b->slots[slot].active) return CFD_EINVAL;
+    if (b->slots[slot].interrupted) return CFD_ETIMEOUT;
     unsigned w = 0;
     cudaError_t e = cudaMemcpyAsync(&w, slot_flags(b, slot), sizeof w, cudaMemcpyDeviceToHost, b->ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->ctx->stream);
     if (e != cudaSuccess) return cuda_fail(b->ctx, e, "cfd_batch_slot_status");
     return (w & CFD_FLAG_NONFINITE) ? CFD_ENONFINITE : CFD_OK;
+}
+
+cfd_status_t cfd_batch_set_flow(cfd_batch_t *b, int32_t slot, const cfd_flow_t *flow_host)
+{
+    if (!b || !flow_host || slot < 0 || slot >= (int)b->slots.size() || !b->slots[slot].active) return CFD_EINVAL;
+    cfd_status_t st = use_device(b->ctx);
+    if (st != CFD_OK) return st;
+    BatchInst &I = b->slots[slot];
+    cudaStream_t sm = b->ctx->stream;
+    // queued steps finish first (they may still read this instance)
+    cudaError_t e = cudaStreamSynchronize(sm);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(I.stage9, flow_host, 9 * ((size_t)I.N + 1) * 8, cudaMemcpyHostToDevice, sm);
+    if (e == cudaSuccess) e = cudaMemsetAsync(slot_flags(b, slot), 0, sizeof(unsigned), sm);
+    if (e != cudaSuccess) return cuda_fail(b->ctx, e, "cfd_batch_set_flow upload");
+    aos_to_soa(sm, I.stage9, 9, 9, I.N, I.view.prim9);
+    if (b->precision == CFD_PREC_MIXED)
+        batch_prep_mixed(I.view, sm);
+    else
+        batch_prep_fp64(I.view, sm);
+    b->ctx->launches += 2;
+    e = cudaStreamSynchronize(sm);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(b->ctx, e, "cfd_batch_set_flow prep");
+    I.interrupted = false;
+    return CFD_OK;
+}
+
+cfd_status_t cfd_batch_set_wait_limit(cfd_batch_t *b, int64_t limit_ns)
+{
+    if (!b) return CFD_EINVAL;
+    const long long v = limit_ns < 0 ? -1 : (long long)limit_ns;
+    if (v != b->wait_limit_ns) {
+        b->wait_limit_ns = v;
+        b->dirty = true;   // the captured graph holds the old deadline
+    }
+    return CFD_OK;
 }
 
 cfd_status_t cfd_batch_set_tiling(cfd_batch_t *b, int32_t tile_nodes, int32_t max_blocks, int32_t use_graph)

@@ -446,6 +446,17 @@ class Batch:
     def slot_status(self, slot: int) -> int:
         return int(self.lib.cfd_batch_slot_status(self.h, int(slot)))
 
+    def set_flow(self, slot: int, flow: np.ndarray):
+        """Replace an instance's state (FLOW rows 0..g_node) and prepare its
+        next step; the recovery path after a barrier timeout."""
+        f = np.ascontiguousarray(flow, dtype=np.float64)
+        assert f.shape == (self.rows[slot], L.NFLOW)
+        self.ctx.check(self.lib.cfd_batch_set_flow(self.h, int(slot), C.c_void_p(_ptr(f))), "cfd_batch_set_flow")
+
+    def set_wait_limit(self, limit_ns: int = -1):
+        """Grid-barrier deadline in ns (< 0: the library default)."""
+        self.ctx.check(self.lib.cfd_batch_set_wait_limit(self.h, int(limit_ns)), "cfd_batch_set_wait_limit")
+
     def set_tiling(self, tile_nodes: int = 0, max_blocks: int = 0, use_graph: bool = True):
         self.ctx.check(self.lib.cfd_batch_set_tiling(self.h, int(tile_nodes), int(max_blocks), 1 if use_graph else 0),
                        "cfd_batch_set_tiling")

@@ -375,7 +375,23 @@ cfd_status_t cfd_batch_set_hold(cfd_batch_t *b, int32_t slot, int32_t hold);
 cfd_status_t cfd_batch_get_flow(cfd_batch_t *b, int32_t slot, cfd_flow_t *flow_host);
 /* U0 = det*Q of the current FLOW (the next stage's U_Q output). */
 cfd_status_t cfd_batch_get_u0(cfd_batch_t *b, int32_t slot, cfd_column_t *u0_host);
+/* CFD_ENONFINITE after a non-finite state; CFD_ETIMEOUT while the slot is
+ * interrupted (below). */
 cfd_status_t cfd_batch_slot_status(cfd_batch_t *b, int32_t slot);
+/* Replaces the state of an instance with FLOW rows 0..g_node (host memory)
+ * and prepares its next step, as cfd_batch_add does; clears the slot's
+ * error flags.  Waits for queued steps first.  This is the recovery path
+ * after a barrier timeout and the restore path of a checkpoint. */
+cfd_status_t cfd_batch_set_flow(cfd_batch_t *b, int32_t slot, const cfd_flow_t *flow_host);
+/* Deadline of the persistent kernel's grid barrier in nanoseconds (< 0: the
+ * default, 5 s + 50 ns per batched node).  A block that waits longer gives up
+ * and skips the rest of that stage; the step reports CFD_ETIMEOUT once (the
+ * reference exits the process on any kernel failure, Solver.cpp:378-381)
+ * and every instance it was advancing is marked interrupted: its state is
+ * part old, part new, so cfd_batch_step refuses to advance it
+ * (CFD_ETIMEOUT) until cfd_batch_set_flow restores it or it is removed.
+ * Instances that were held are not affected. */
+cfd_status_t cfd_batch_set_wait_limit(cfd_batch_t *b, int64_t limit_ns);
 /* tile_nodes in {64, 128, 256} (0 = keep), max_blocks (0 = occupancy limit),
  * use_graph 0/1. */
 cfd_status_t cfd_batch_set_tiling(cfd_batch_t *b, int32_t tile_nodes, int32_t max_blocks, int32_t use_graph);
