@@ -18,7 +18,8 @@ OK, EINVAL, ENONFINITE, ETIMEOUT, ECUDA, ENOMEM, EUNSUPPORTED = range(7)
 STATUS_NAMES = {0: "CFD_OK", 1: "CFD_EINVAL", 2: "CFD_ENONFINITE", 3: "CFD_ETIMEOUT", 4: "CFD_ECUDA",
                 5: "CFD_ENOMEM", 6: "CFD_EUNSUPPORTED"}
 PATH_GATHER, PATH_STRUCTURED = 0, 1
-PREC_FP64, PREC_MIXED = 0, 1
+PREC_FP64, PREC_MIXED, PREC_SPLIT = 0, 1, 2
+PREC_NAMES = {PREC_FP64: "fp64", PREC_MIXED: "mixed", PREC_SPLIT: "split"}
 
 
 class CfdError(RuntimeError):

@@ -34,9 +34,10 @@ def nvcc() -> str:
 # Translation units whose FP64 arithmetic must follow the reference's
 # evaluation order: no contraction of a*b+c into FMA.
 EXACT_FP64 = {"dropin.cu", "structured.cu", "batch_fp64.cu", "boundary.cu"}
-# Translation units of the mixed-precision form: approximate FP32 division and
-# square root (single-precision only; FP64 arithmetic is unaffected).
-FAST_FP32 = {"mixed.cu", "batch_mixed.cu"}
+# Translation units of the mixed and split precision forms: approximate FP32
+# division and square root (single-precision only; FP64 arithmetic is
+# unaffected) and FMA contraction.
+FAST_FP32 = {"mixed.cu", "batch_mixed.cu", "split.cu", "batch_split.cu"}
 
 
 def sources() -> list[pathlib.Path]:

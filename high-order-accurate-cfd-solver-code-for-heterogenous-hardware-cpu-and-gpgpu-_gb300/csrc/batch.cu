@@ -81,6 +81,9 @@ uint64_t instance_bytes(int precision, int64_t N)
     const uint64_t doubles = (22 + 9 + 15) * (uint64_t)N + 14 * (uint64_t)(N + 1);
     // mixed: FP32 face/node geometry (12 + 10 + 2), prim32 (9), stage intermediates (55)
     if (precision == CFD_PREC_MIXED) return doubles * 8 + (12 + 11 + 2 + 9 + 55) * (uint64_t)N * 4;
+    // split: FP32 face metrics (9), node geometry (11), prim32 (9), Q32/R32/FEG32/V32 (40) and the hi/lo
+    // state copy (10); FP64 1/det and Fh (16)
+    if (precision == CFD_PREC_SPLIT) return (doubles + 16 * (uint64_t)N) * 8 + (9 + 11 + 9 + 40 + 10) * (uint64_t)N * 4;
     return (doubles + 52 * (uint64_t)N) * 8;
 }
 
@@ -150,7 +153,9 @@ cfd_status_t rebuild(cfd_batch *b)
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int occ = b->precision == CFD_PREC_MIXED ? batch_occupancy_mixed(T) : batch_occupancy_fp64(T);
+    const int occ = b->precision == CFD_PREC_MIXED   ? batch_occupancy_mixed(T)
+                    : b->precision == CFD_PREC_SPLIT ? batch_occupancy_split(T)
+                                                     : batch_occupancy_fp64(T);
     if (occ <= 0) return fail(b->ctx, CFD_EUNSUPPORTED, "batch: stage kernel does not fit at this tile size");
     int blocks = occ * sms;
     if (b->blocks_override > 0) blocks = std::min(blocks, b->blocks_override);
@@ -182,7 +187,9 @@ cudaError_t launch_step(cfd_batch *b)
 {
     const BatchLaunch L = launch_of(b);
     for (int j = 0; j < 3; ++j) {
-        cudaError_t e = b->precision == CFD_PREC_MIXED ? batch_stage_mixed(L, j) : batch_stage_fp64(L, j);
+        cudaError_t e = b->precision == CFD_PREC_MIXED   ? batch_stage_mixed(L, j)
+                        : b->precision == CFD_PREC_SPLIT ? batch_stage_split(L, j)
+                                                         : batch_stage_fp64(L, j);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
@@ -265,7 +272,8 @@ std::vector<std::pair<void *, size_t>> mutable_arrays(const BatchInst &I, int pr
     const size_t N = (size_t)I.N;
     std::vector<std::pair<void *, size_t>> v = {{I.view.prim9, 9 * N * 8}, {I.view.U0, 5 * N * 8},
                                                 {I.view.U1, 5 * N * 8}, {I.view.U2, 5 * N * 8}};
-    if (precision == CFD_PREC_MIXED) {
+    if (precision == CFD_PREC_SPLIT) v.push_back({I.view.Whl, 10 * N * 4});
+    if (precision == CFD_PREC_MIXED || precision == CFD_PREC_SPLIT) {
         v.push_back({I.view.prim32, 9 * N * 4});
         v.push_back({I.view.Q32, 5 * N * 4});
         v.push_back({I.view.R32, 5 * N * 4});
@@ -286,7 +294,7 @@ uint64_t cfd_batch_instance_bytes(int32_t precision, int64_t nodes) { return ins
 
 cfd_status_t cfd_batch_create(cfd_ctx_t *ctx, int32_t precision, uint64_t capacity_bytes, cfd_batch_t **out)
 {
-    if (!ctx || !out || (precision != CFD_PREC_FP64 && precision != CFD_PREC_MIXED)) return CFD_EINVAL;
+    if (!ctx || !out || precision < CFD_PREC_FP64 || precision > CFD_PREC_SPLIT) return CFD_EINVAL;
     *out = nullptr;
     cfd_status_t s = use_device(ctx);
     if (s != CFD_OK) return s;
@@ -496,6 +504,20 @@ cfd_status_t cfd_batch_add_staged(cfd_batch_t *b, cfd_batch_staged_t *staged, in
         v.fdet32 = fdet32;
         v.node32 = node32;
         v.idet32 = idet32;
+    } else if (b->precision == CFD_PREC_SPLIT) {
+        float *fm32, *node32;
+        double *idet64;
+        if ((st = ialloc(b, I, 9 * Nz, &fm32)) || (st = ialloc(b, I, 11 * Nz, &node32)) || (st = ialloc(b, I, Nz, &idet64))
+            || (st = ialloc(b, I, 9 * Nz, &v.prim32)) || (st = ialloc(b, I, 5 * Nz, &v.Q32))
+            || (st = ialloc(b, I, 5 * Nz, &v.R32)) || (st = ialloc(b, I, 15 * Nz, &v.FEG32))
+            || (st = ialloc(b, I, 15 * Nz, &v.V32)) || (st = ialloc(b, I, 15 * Nz, &v.Fh))
+            || (st = ialloc(b, I, 10 * Nz, &v.Whl))) {
+            free_instance(I);
+            return st;
+        }
+        v.fm32 = fm32;
+        v.node32 = node32;
+        v.idet64 = idet64;
     } else {
         if ((st = ialloc(b, I, 5 * Nz, &v.Q)) || (st = ialloc(b, I, 15 * Nz, &v.FEG)) || (st = ialloc(b, I, 15 * Nz, &v.V))
             || (st = ialloc(b, I, 2 * Nz, &v.sh)) || (st = ialloc(b, I, 15 * Nz, &v.Fh))) {
@@ -514,8 +536,8 @@ cfd_status_t cfd_batch_add_staged(cfd_batch_t *b, cfd_batch_staged_t *staged, in
     if (e == cudaSuccess) e = cudaMemsetAsync(v.flags, 0, sizeof(unsigned), sm);
     for (double *u : {U0, U1, U2})
         if (e == cudaSuccess) e = cudaMemsetAsync(u, 0, 5 * Nz * 8, sm);
-    if (e == cudaSuccess) e = b->precision == CFD_PREC_MIXED ? cudaMemsetAsync(v.V32, 0, 15 * Nz * 4, sm)
-                                                              : cudaMemsetAsync(v.V, 0, 15 * Nz * 8, sm);
+    if (e == cudaSuccess) e = b->precision != CFD_PREC_FP64 ? cudaMemsetAsync(v.V32, 0, 15 * Nz * 4, sm)
+                                                             : cudaMemsetAsync(v.V, 0, 15 * Nz * 8, sm);
     if (e != cudaSuccess) {
         cudaStreamSynchronize(sm);
         free_instance(I);
@@ -538,10 +560,26 @@ cfd_status_t cfd_batch_add_staged(cfd_batch_t *b, cfd_batch_staged_t *staged, in
         S.idet32 = const_cast<float *>(v.idet32);
         mixed_geometry(S);
         batch_prep_mixed(v, sm);
+    } else if (b->precision == CFD_PREC_SPLIT) {
+        StructuredLaunch S{};
+        S.ni = ni;
+        S.nj = nj;
+        S.nk = nk;
+        S.stream = sm;
+        S.fm = fm;
+        S.m9 = m9;
+        S.det = det;
+        S.fm32 = const_cast<float *>(v.fm32);
+        S.node32 = const_cast<float *>(v.node32);
+        S.idet64 = const_cast<double *>(v.idet64);
+        split_geometry(S);
+        batch_prep_split(v, sm);
     } else {
         batch_prep_fp64(v, sm);
     }
-    ctx->launches += b->precision == CFD_PREC_MIXED ? 2 + kMixedGeometryLaunches : 2;
+    ctx->launches += b->precision == CFD_PREC_MIXED   ? 2 + kMixedGeometryLaunches
+                     : b->precision == CFD_PREC_SPLIT ? 2 + kSplitGeometryLaunches
+                                                      : 2;
     e = cudaStreamSynchronize(sm);   // host geometry vectors go out of scope
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -652,6 +690,7 @@ cfd_status_t cfd_batch_get_flow(cfd_batch_t *b, int32_t slot, cfd_flow_t *host)
     BatchInst &I = b->slots[slot];
     // mixed: FP64 FLOW of the hi/lo state (after whole steps it is in slot 0)
     if (b->precision == CFD_PREC_MIXED) mixed_flow_out(I.view, 0, b->ctx->stream);
+    if (b->precision == CFD_PREC_SPLIT) split_flow_out(I.view, 0, b->ctx->stream);
     soa_to_aos(b->ctx->stream, I.view.prim9, 9, 9, I.N, I.stage9);
     cudaError_t e = cudaMemcpyAsync(host, I.stage9, 9 * ((size_t)I.N + 1) * 8, cudaMemcpyDeviceToHost, b->ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->ctx->stream);
@@ -701,6 +740,8 @@ cfd_status_t cfd_batch_set_flow(cfd_batch_t *b, int32_t slot, const cfd_flow_t *
     aos_to_soa(sm, I.stage9, 9, 9, I.N, I.view.prim9);
     if (b->precision == CFD_PREC_MIXED)
         batch_prep_mixed(I.view, sm);
+    else if (b->precision == CFD_PREC_SPLIT)
+        batch_prep_split(I.view, sm);
     else
         batch_prep_fp64(I.view, sm);
     b->ctx->launches += 2;

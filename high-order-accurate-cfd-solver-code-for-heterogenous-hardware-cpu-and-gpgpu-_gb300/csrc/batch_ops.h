@@ -25,11 +25,14 @@ struct BatchLaunch {
 // One RK stage j (cooperative launch).  Returns the launch error.
 cudaError_t batch_stage_fp64(const BatchLaunch &b, int j);
 cudaError_t batch_stage_mixed(const BatchLaunch &b, int j);
+cudaError_t batch_stage_split(const BatchLaunch &b, int j);
 // Stage-0 prep of one lattice.
 void batch_prep_fp64(const LatView &g, cudaStream_t st);
 void batch_prep_mixed(const LatView &g, cudaStream_t st);
+void batch_prep_split(const LatView &g, cudaStream_t st);
 // Co-resident blocks per SM of the stage kernel at `threads` per block.
 int batch_occupancy_fp64(int threads);
 int batch_occupancy_mixed(int threads);
+int batch_occupancy_split(int threads);
 
 }  // namespace cfd

@@ -89,6 +89,59 @@ void bc_apply_soa(cudaStream_t st, const BcDevice &bc, double *prim9, int N, dou
 void bc_free_stream_aos(cudaStream_t st, double *flow_rows, int sd_node, double mach);
 // The mixed form: targets from the hi/lo state of U slot q (mixed.cu).
 void bc_apply_mixed(cudaStream_t st, const BcDevice &bc, const LatView &g, int q, double mach);
+// The split form: targets from the FP64 state of U slot q (split.cu).
+void bc_apply_split(cudaStream_t st, const BcDevice &bc, const LatView &g, int q, double mach);
+
+// Target m of one entry of the routine on a lattice state held in a
+// precision form's own representation: m = 0 the boundary node, m = 1..3
+// its ghosts (face codes; edge and corner codes have only m = 0).  The same
+// rules on (rho, u, v, w, p), the fields the next stage reads (U_Q.cl takes
+// rho, u, v, w, p of FLOW): outlet copies the first inward node into the
+// node and its ghosts, inlet writes the free stream (Flow_Initialisation.cpp
+// :35-48), boundary mirrors inward node m into ghost m, wall sets zero
+// velocity at the node and mirrors with the velocity negated; edge and
+// corner codes copy the diagonal source.  Each target depends only on inward
+// nodes, which the entry does not write.  St provides
+// prims(n, rho, u, v, w, p, t) and set(n, rho, u, v, w, p).
+template <class St>
+__device__ __forceinline__ void bc_target_rules(const St &S, int type, const BcEntry &e, int m, double mach)
+{
+    const double gm2 = 1.4 * mach * mach;
+    double rho, u, v, w, p, t;
+    if (e.cls == BC_EDGE) {
+        if (m != 0) return;
+        S.prims(e.s[0], rho, u, v, w, p, t);
+        if (type == BC_WALL) u = v = w = 0.0;
+        S.set(e.b, gm2 * (p / t), u, v, w, p);
+        return;
+    }
+    const int node = m == 0 ? e.b : e.g[m - 1];
+    // the routine writes the targets in order: when a collapsed chain names a
+    // node twice, the later target's write stands
+    for (int k = m; k < 3; ++k)
+        if (e.g[k] == node) return;
+    if (type == BC_INLET || type == BC_OUTLET) {   // node and ghosts alike
+        if (type == BC_INLET) {
+            u = 1.0;
+            v = w = 0.0;
+            p = 1.0 / gm2;
+            t = 1.0;
+        } else {
+            S.prims(e.s[0], rho, u, v, w, p, t);
+        }
+        S.set(node, gm2 * (p / t), u, v, w, p);
+        return;
+    }
+    // boundary (mirror copy) and wall (no slip): ghost m from inward node m,
+    // the node itself from the first inward node
+    S.prims(e.s[m == 0 ? 0 : m - 1], rho, u, v, w, p, t);
+    if (m == 0 && type == BC_WALL)
+        S.set(node, gm2 * (p / t), 0.0, 0.0, 0.0, p);
+    else if (type == BC_WALL)
+        S.set(node, rho, -u, -v, -w, p);
+    else
+        S.set(node, rho, u, v, w, p);
+}
 
 }  // namespace cfd
 

@@ -14,7 +14,9 @@ namespace cfd {
 //
 // Mixed form: U0/U1/U2 hold each conserved value as an unevaluated sum of
 // two FP32 numbers (hi + lo, about 48 significant bits) in the same bytes as
-// the FP64 form's [5][N] doubles: hi at [c][N], lo at [5 + c][N].
+// the FP64 form's [5][N] doubles: hi at [c][N], lo at [5 + c][N].  Split
+// form: U0/U1/U2 are the FP64 form's doubles, the stage intermediates FP32
+// (Q32, R32, FEG32, V32) except the face fluxes Fh (FP64).
 struct LatView {
     int ni, nj, nk, N;
     Phys P;
@@ -25,6 +27,8 @@ struct LatView {
     const float *fm32, *fdet32;
     const float *node32;       // [11][N] 9 node metrics, det, det^(-1/3) (mixed form)
     const float *idet32;       // [2][N] 1/det as hi, lo (mixed form)
+    const double *idet64;      // [N] 1/det (split form)
+    float *Whl;                // [10][N] hi/lo copy of the current stage's state (split form)
     // state
     double *prim9;             // FLOW fields u,v,w,p,t,rho,mu,a,e
     float *prim32;             // the same fields in FP32 (mixed form)

@@ -464,49 +464,26 @@ __device__ __forceinline__ void set_prims(const LatView &g, int q, int n, double
     derive(g, n, Un);
 }
 
-// Target m of one entry of the reference's boundary routine (boundary.h) on
-// the hi/lo state in slot q: m = 0 the boundary node, m = 1..3 its ghosts
-// (face codes; edge and corner codes have only m = 0).  The same rules on
-// (rho, u, v, w, p), the fields the next stage reads (U_Q.cl takes rho, u,
-// v, w, p of FLOW); each target depends only on inward nodes, which the
-// entry does not write.
+// Target m of one entry of the reference's boundary routine
+// (bc_target_rules) on the hi/lo state in slot q.
+struct HiLoState {
+    const LatView &g;
+    int q;
+    double mach;
+    __device__ __forceinline__ void prims(int n, double &rho, double &u, double &v, double &w, double &p,
+                                          double &t) const
+    {
+        state_prims(g, q, n, mach, rho, u, v, w, p, t);
+    }
+    __device__ __forceinline__ void set(int n, double rho, double u, double v, double w, double p) const
+    {
+        set_prims(g, q, n, rho, u, v, w, p);
+    }
+};
+
 __device__ __forceinline__ void bc_target(const LatView &g, int type, const BcEntry &e, int m, int q, double mach)
 {
-    const double gm2 = 1.4 * mach * mach;
-    double rho, u, v, w, p, t;
-    if (e.cls == BC_EDGE) {
-        if (m != 0) return;
-        state_prims(g, q, e.s[0], mach, rho, u, v, w, p, t);
-        if (type == BC_WALL) u = v = w = 0.0;
-        set_prims(g, q, e.b, gm2 * (p / t), u, v, w, p);
-        return;
-    }
-    const int node = m == 0 ? e.b : e.g[m - 1];
-    // the routine writes the targets in order: when a collapsed chain names a
-    // node twice, the later target's write stands
-    for (int k = m; k < 3; ++k)
-        if (e.g[k] == node) return;
-    if (type == BC_INLET || type == BC_OUTLET) {   // node and ghosts alike
-        if (type == BC_INLET) {
-            u = 1.0;
-            v = w = 0.0;
-            p = 1.0 / gm2;
-            t = 1.0;
-        } else {
-            state_prims(g, q, e.s[0], mach, rho, u, v, w, p, t);
-        }
-        set_prims(g, q, node, gm2 * (p / t), u, v, w, p);
-        return;
-    }
-    // boundary (mirror copy) and wall (no slip): ghost m from inward node m,
-    // the node itself from the first inward node
-    state_prims(g, q, e.s[m == 0 ? 0 : m - 1], mach, rho, u, v, w, p, t);
-    if (m == 0 && type == BC_WALL)
-        set_prims(g, q, node, gm2 * (p / t), 0.0, 0.0, 0.0, p);
-    else if (type == BC_WALL)
-        set_prims(g, q, node, rho, -u, -v, -w, p);
-    else
-        set_prims(g, q, node, rho, u, v, w, p);
+    bc_target_rules(HiLoState{g, q, mach}, type, e, m, mach);
 }
 
 // FP64 FLOW of the state in slot q (boundary output): the FP64 form's

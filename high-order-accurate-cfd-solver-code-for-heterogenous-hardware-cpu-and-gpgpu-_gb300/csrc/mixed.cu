@@ -16,6 +16,7 @@
 // and approximate FP32 division/square root (the mixed form's error budget
 // is 1e-6 relative L2 against the FP64 form).
 #include "boundary.h"
+#include "face_tile.cuh"
 #include "internal.h"
 #include "lattice_mixed.cuh"
 #include "structured.h"
@@ -67,16 +68,11 @@ __global__ void __launch_bounds__(256) k_mu_m(LatView g, int q)
 #define CFD_MFACE_MIN_BLOCKS 8
 #endif
 
-// Faces along D from a tile staged in shared memory: the block covers
-// kTile faces along D times kWide nodes across (axis A), one line of the
-// third axis (B).  It loads the stencil lines (kTile + 5 nodes along D) of
-// Q, the Roe inputs and the node fluxes along D once, coalesced along i,
-// and every face reads its six points from there.
 // Faces per tile along D (a block of 128 threads covers kTile x 128/kTile
-// faces).  TGV 128^3: i tiles of 16 / 32 / 64 / 128 took 0.097 / 0.093 /
-// 0.091 / 0.090 ms, j/k tiles of 4 / 8 / 16 / 32 took 0.098 / 0.094 /
-// 0.092 / 0.102-0.146 ms; 64 keeps small lattices' i lines from idling
-// most of a block.
+// faces; face_tile.cuh).  TGV 128^3: i tiles of 16 / 32 / 64 / 128 took
+// 0.097 / 0.093 / 0.091 / 0.090 ms, j/k tiles of 4 / 8 / 16 / 32 took 0.098
+// / 0.094 / 0.092 / 0.102-0.146 ms; 64 keeps small lattices' i lines from
+// idling most of a block.
 #ifndef CFD_MFACE_TILE_I
 #define CFD_MFACE_TILE_I 64
 #endif
@@ -85,82 +81,28 @@ __global__ void __launch_bounds__(256) k_mu_m(LatView g, int q)
 #endif
 
 template <int D>
-struct FaceTile {
-    static constexpr int kTile = D == 0 ? CFD_MFACE_TILE_I : CFD_MFACE_TILE_JK;   // faces along D
-    static constexpr int kWide = 128 / kTile;           // nodes across
-    static constexpr int A = D == 0 ? 1 : 0;            // axis across
-    static constexpr int B = D == 2 ? 1 : 2;            // axis of the block's line
-    static constexpr int kLine = kTile + 5;             // staged nodes along D
-    // smem index of (position b along D, a across); i is the fast index
-    static __device__ __forceinline__ int at(int b, int a) { return D == 0 ? a * kLine + b : b * kWide + a; }
-    // thread -> (t along D, a across), consecutive threads consecutive in i
-    static __device__ __forceinline__ void split(int x, int &t, int &a)
-    {
-        if (D == 0) { t = x % kTile; a = x / kTile; }
-        else { t = x / kWide; a = x % kWide; }
-    }
-};
-
-// coordinate c in [-2, n + kTile + 3) of a staged stencil line, wrapped
-// (periodic) or clamped; the wrap subtracts instead of dividing (c is at
-// most a few extents away from [0, n))
-__device__ __forceinline__ int tile_coord(const LatView &g, int d, int c)
-{
-    const int n = lat_extent(g, d);
-    if (lat_periodic(g, d)) {
-        while (c < 0) c += n;
-        while (c >= n) c -= n;
-        return c;
-    }
-    return c < 0 ? 0 : (c >= n ? n - 1 : c);
-}
+using MTile = FaceTile<D, D == 0 ? CFD_MFACE_TILE_I : CFD_MFACE_TILE_JK>;
 
 template <int D>
-__global__ void __launch_bounds__(128, CFD_MFACE_MIN_BLOCKS) k_face_tile_m(LatView g)
+__global__ void __launch_bounds__(kFaceThreads, CFD_MFACE_MIN_BLOCKS) k_face_tile_m(LatView g)
 {
-    using T = FaceTile<D>;
-    constexpr int S = T::kLine * T::kWide;
-    __shared__ float sQ[5][S], sR[5][S], sF[5][S];
+    using T = MTile<D>;
+    constexpr int S = T::kStaged;
+    __shared__ float sQ[5 * S], sR[5 * S], sF[5 * S];
+    stage_face_lines<T, D>(g, sQ, sR, sF);
+    int n, t, a;
+    if (!tile_face<T, D>(g, n, t, a)) return;
     const int N = g.N;
-    const int tD = blockIdx.x * T::kTile, tA = blockIdx.y * T::kWide, cB = blockIdx.z;
-    const int nA = lat_extent(g, T::A);
-    const float *NF = g.FEG32 + (size_t)D * 5 * N;
-    for (int m = threadIdx.x; m < S; m += blockDim.x) {
-        int b, a;
-        if (D == 0) { b = m % T::kLine; a = m / T::kLine; }
-        else { b = m / T::kWide; a = m % T::kWide; }
-        int c[3];
-        c[D] = tile_coord(g, D, tD + b - 2);
-        c[T::A] = tA + a < nA ? tA + a : nA - 1;
-        c[T::B] = cB;
-        const int node = c[0] + g.ni * (c[1] + g.nj * c[2]);
-        const int e = T::at(b, a);
-#pragma unroll
-        for (int q = 0; q < 5; ++q) {   // read-only in this pass: non-coherent loads
-            sQ[q][e] = __ldg(g.Q32 + q * N + node);
-            sR[q][e] = __ldg(g.R32 + q * N + node);
-            sF[q][e] = __ldg(NF + q * N + node);
-        }
-    }
-    __syncthreads();
-    int t, a;
-    T::split(threadIdx.x, t, a);
-    int c[3];
-    c[D] = tD + t;
-    c[T::A] = tA + a;
-    c[T::B] = cB;
-    if (c[D] >= lat_extent(g, D) || c[T::A] >= nA || !lat_face_needed(g, c[0], c[1], c[2], D)) return;
-    const int n = c[0] + g.ni * (c[1] + g.nj * c[2]);
     float2 P[3][5];
 #pragma unroll
     for (int o = 0; o < 3; ++o)
 #pragma unroll
-        for (int q = 0; q < 5; ++q) P[o][q] = make_float2(sQ[q][T::at(t + o, a)], sQ[q][T::at(t + 5 - o, a)]);
+        for (int q = 0; q < 5; ++q) P[o][q] = make_float2(sQ[q * S + T::at(t + o, a)], sQ[q * S + T::at(t + 5 - o, a)]);
     float r[5];
     {
         const int er = T::at(t + 3, a), el = T::at(t + 2, a);
-        roe_average<float>(sR[3][er], sR[0][er], sR[1][er], sR[2][er], sR[4][er], sR[3][el], sR[0][el], sR[1][el],
-                           sR[2][el], sR[4][el], r);
+        roe_average<float>(sR[3 * S + er], sR[er], sR[S + er], sR[2 * S + er], sR[4 * S + er], sR[3 * S + el], sR[el],
+                           sR[S + el], sR[2 * S + el], sR[4 * S + el], r);
     }
     float Fhat[5];
     x2::llf_face_flux2(P, g.fm32[(D * 3 + 0) * N + n], g.fm32[(D * 3 + 1) * N + n], g.fm32[(D * 3 + 2) * N + n],
@@ -169,7 +111,7 @@ __global__ void __launch_bounds__(128, CFD_MFACE_MIN_BLOCKS) k_face_tile_m(LatVi
     for (int q = 0; q < 5; ++q) {
         float f[6];
 #pragma unroll
-        for (int o = 0; o < 6; ++o) f[o] = sF[q][T::at(t + o, a)];
+        for (int o = 0; o < 6; ++o) f[o] = sF[q * S + T::at(t + o, a)];
         g.Fh32[(D * 5 + q) * N + n] = Fhat[q] + x2::face_correction_sym(f);
     }
 }
@@ -177,10 +119,7 @@ __global__ void __launch_bounds__(128, CFD_MFACE_MIN_BLOCKS) k_face_tile_m(LatVi
 template <int D>
 void launch_face_tile(const LatView &g, cudaStream_t st)
 {
-    using T = FaceTile<D>;
-    const dim3 grid((unsigned)((lat_extent_h(g, D) + T::kTile - 1) / T::kTile),
-                    (unsigned)((lat_extent_h(g, T::A) + T::kWide - 1) / T::kWide), (unsigned)lat_extent_h(g, T::B));
-    k_face_tile_m<D><<<grid, 128, 0, st>>>(g);
+    k_face_tile_m<D><<<MTile<D>::grid(g), kFaceThreads, 0, st>>>(g);
 }
 
 template <bool LOC>

@@ -95,11 +95,20 @@ __device__ __forceinline__ float2 contravariant_flux2(const float2 q[5], float m
     return add2(un, make_float2(sqrtf(c2k.x), sqrtf(c2k.y)));
 }
 
-// LLF face flux (Weno.cl:2859-2947): Fhat = 0.5 det (Fp + Fn - alpha (qp - qn)),
-// alpha = max |lambda_5|.  P[k][c] = (Q_c of stencil point k, Q_c of point
-// 5-k), k = 0..2, points left-2 .. right+2; roe = Roe state of the face.
-__device__ __forceinline__ void llf_face_flux2(const float2 P[3][5], float mx, float my, float mz, float det_f,
-                                               const float roe[5], float eps, float Fhat[5])
+// Reconstructed face states of one face on the two lanes, (pos, neg):
+// the Roe eigen-system of the face, the characteristic projection of the
+// stencil, WENO5 on both sides and the back-projection (Weno.cl:337-413,
+// 1056-2289).  P[k][c] = (Q_c of stencil point k, Q_c of point 5-k), k =
+// 0..2, points left-2 .. right+2; roe = Roe state of the face.
+// DEV: the stencil enters as its deviation from ref (the face's left node)
+// and ref is added back to the face states.  The projection is linear and
+// WENO5 is unchanged by a constant shift (candidate weights sum to one, the
+// smoothness indicators see differences only), so this is the same
+// reconstruction; in FP32 its rounding scales with the variation across the
+// stencil instead of with Q, and a uniform stencil returns ref exactly.
+template <bool DEV = false>
+__device__ __forceinline__ void reconstruct_face2(const float2 P[3][5], float mx, float my, float mz,
+                                                  const float roe[5], float eps, const float *ref, float2 q[5])
 {
     FaceEigen<float> eg;
     eg.init(mx, my, mz, roe);
@@ -107,19 +116,36 @@ __device__ __forceinline__ void llf_face_flux2(const float2 P[3][5], float mx, f
     {
         float Lm[5][5];
         eg.left(Lm);
+        float2 Pd[3][5];
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+            for (int c = 0; c < 5; ++c) Pd[k][c] = DEV ? sub2(P[k][c], b2(ref[c])) : P[k][c];
 #pragma unroll
         for (int r = 0; r < 5; ++r) {
             float2 cv[3];
 #pragma unroll
             for (int k = 0; k < 3; ++k)
-                cv[k] = fma2(b2(Lm[r][0]), P[k][0], fma2(b2(Lm[r][1]), P[k][1], fma2(b2(Lm[r][2]), P[k][2],
-                             fma2(b2(Lm[r][3]), P[k][3], mul2(b2(Lm[r][4]), P[k][4])))));
+                cv[k] = fma2(b2(Lm[r][0]), Pd[k][0], fma2(b2(Lm[r][1]), Pd[k][1], fma2(b2(Lm[r][2]), Pd[k][2],
+                             fma2(b2(Lm[r][3]), Pd[k][3], mul2(b2(Lm[r][4]), Pd[k][4])))));
             const float2 st[6] = {cv[0], cv[1], cv[2], swap2(cv[2]), swap2(cv[1]), swap2(cv[0])};
             C[r] = weno5_pos2(st, eps);
         }
     }
-    float2 q[5], f[5];
     right_times2(eg, C, q);
+    if (DEV) {
+#pragma unroll
+        for (int c = 0; c < 5; ++c) q[c] = add2(q[c], b2(ref[c]));
+    }
+}
+
+// LLF face flux (Weno.cl:2859-2947): Fhat = 0.5 det (Fp + Fn - alpha (qp - qn)),
+// alpha = max |lambda_5|, all FP32.
+__device__ __forceinline__ void llf_face_flux2(const float2 P[3][5], float mx, float my, float mz, float det_f,
+                                               const float roe[5], float eps, float Fhat[5])
+{
+    float2 q[5], f[5];
+    reconstruct_face2<false>(P, mx, my, mz, roe, eps, nullptr, q);
     const float2 lam = contravariant_flux2(q, mx, my, mz, f);
     const float alpha = fmaxf(fabsf(lam.x), fabsf(lam.y));
     const float2 sa = make_float2(-alpha, alpha);
@@ -128,6 +154,52 @@ __device__ __forceinline__ void llf_face_flux2(const float2 P[3][5], float mx, f
         const float2 t = fma2(sa, q[c], f[c]);
         Fhat[c] = (0.5f * det_f) * (t.x + t.y);
     }
+}
+
+// The same LLF face flux with the metric and Jacobian products in FP64 (the
+// split form): the face states (q+, q-) reconstructed as deviations from
+// the face's left node (reconstruct_face2<true>), their velocities and
+// pressures, lambda_5 and the dissipation alpha (q+ - q-) in FP32; the
+// contravariant velocity U_n = m . u with the FP64 face metric (dm), the
+// central sum of the contravariant fluxes q U_n + m p and (E + p) U_n of
+// both states, and its product by det_f / 2 in FP64 (Weno.cl:2585-2728,
+// 2913-2947).  m (FP32) is the same face metric rounded, for the
+// eigenvectors and lambda_5.  extra[c] (FP32) is added to component c
+// together with the FP32 dissipation term, in one FP64 operation.
+__device__ __forceinline__ void llf_face_flux2_split(const float2 P[3][5], float mx, float my, float mz,
+                                                     const double dm[3], double det_f, const float roe[5], float eps,
+                                                     const float extra[5], double Fhat[5])
+{
+    float2 q[5];
+    const float ref[5] = {P[2][0].x, P[2][1].x, P[2][2].x, P[2][3].x, P[2][4].x};   // the left node
+    reconstruct_face2<true>(P, mx, my, mz, roe, eps, ref, q);
+    const float2 ir = rcp2(q[0]);
+    const float2 u = mul2(q[1], ir), v = mul2(q[2], ir), w = mul2(q[3], ir);
+    const float2 ke2 = fma2(q[1], u, fma2(q[2], v, mul2(q[3], w)));        // |m|^2 / rho
+    const float2 pr = mul2(b2(0.4f), fma2(b2(-0.5f), ke2, q[4]));
+    // lambda_5 = U.m + c |m| in FP32 (the LLF speed)
+    const float2 un32 = fma2(b2(mx), u, fma2(b2(my), v, mul2(b2(mz), w)));
+    const float2 e = fma2(q[4], ir, mul2(b2(-0.5f), fma2(u, u, fma2(v, v, mul2(w, w)))));
+    const float2 c2k = mul2(b2(1.4f * 0.4f * (mx * mx + my * my + mz * mz)), e);
+    const float2 lam = add2(un32, make_float2(sqrtf(c2k.x), sqrtf(c2k.y)));
+    const float alpha = fmaxf(fabsf(lam.x), fabsf(lam.y));
+    // FP32 terms of each component: the extra term less the dissipation
+    const double hd = 0.5 * det_f;
+    const float hd32 = (float)hd;
+    float x[5];
+#pragma unroll
+    for (int c = 0; c < 5; ++c) x[c] = fmaf(-hd32 * alpha, q[c].x - q[c].y, extra[c]);
+    // FP64 central sum of the contravariant fluxes of both states
+    const double unp = fma(dm[0], (double)u.x, fma(dm[1], (double)v.x, dm[2] * (double)w.x));
+    const double unn = fma(dm[0], (double)u.y, fma(dm[1], (double)v.y, dm[2] * (double)w.y));
+    const double ps = (double)(pr.x + pr.y);
+    double t[5];
+    t[0] = fma((double)q[0].x, unp, (double)q[0].y * unn);
+#pragma unroll
+    for (int c = 1; c < 4; ++c) t[c] = fma(dm[c - 1], ps, fma((double)q[c].x, unp, (double)q[c].y * unn));
+    t[4] = fma((double)(q[4].x + pr.x), unp, (double)(q[4].y + pr.y) * unn);
+#pragma unroll
+    for (int c = 0; c < 5; ++c) Fhat[c] = fma(hd, t[c], (double)x[c]);
 }
 
 // Sixth-order correction of a face flux from the node fluxes f[0..5]

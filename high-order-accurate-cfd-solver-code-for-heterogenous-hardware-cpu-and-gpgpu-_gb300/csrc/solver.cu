@@ -30,7 +30,8 @@ struct cfd_solver {
     int path = CFD_PATH_GATHER;
     int32_t g_node = 0, sd_node = 0, n_rows = 0;
     int ni = 0, nj = 0, nk = 0;
-    bool mixed = false;
+    bool mixed = false;         // a reduced-precision form (mixed or split): U slots tracked below
+    int form = CFD_PREC_FP64;   // cfd_precision_t
     std::vector<void *> allocs;
     uint64_t bytes = 0;
     // gather path (reference layout, device)
@@ -118,7 +119,7 @@ cfd_status_t create_structured(cfd_solver *s, const cfd_geometry_t *g)
     S.nk = s->nk;
     S.stream = s->ctx->stream;
     S.P = s->P;
-    S.mixed = s->mixed ? 1 : 0;
+    S.mixed = s->form;
     S.flags = s->ctx->d_flags;
     double *m9, *det, *fm, *fdet;
     cfd_status_t st;
@@ -129,7 +130,15 @@ cfd_status_t create_structured(cfd_solver *s, const cfd_geometry_t *g)
         return st;
     for (int q = 0; q < 3; ++q)
         if ((st = dalloc_t(s, 5 * N, &S.U[q]))) return st;
-    if (s->mixed) {   // FP32 stage intermediates
+    if (s->form == CFD_PREC_SPLIT) {   // FP32 stage intermediates, FP64 face fluxes
+        if ((st = dalloc_t(s, 5 * N, &S.Q32)) || (st = dalloc_t(s, 5 * N, &S.R32)) || (st = dalloc_t(s, 15 * N, &S.FEG32))
+            || (st = dalloc_t(s, 15 * N, &S.V32)) || (st = dalloc_t(s, 15 * N, &S.Fh))
+            || (st = dalloc_t(s, 9 * N, &S.fm32)) || (st = dalloc_t(s, 11 * N, &S.node32))
+            || (st = dalloc_t(s, N, &S.idet64)) || (st = dalloc_t(s, 9 * N, &S.prim32))
+            || (st = dalloc_t(s, 10 * N, &S.Whl)))
+            return st;
+        cudaMemsetAsync(S.V32, 0, 15 * N * sizeof(float), S.stream);
+    } else if (s->mixed) {   // FP32 stage intermediates
         if ((st = dalloc_t(s, 5 * N, &S.Q32)) || (st = dalloc_t(s, 5 * N, &S.R32)) || (st = dalloc_t(s, 15 * N, &S.FEG32))
             || (st = dalloc_t(s, 15 * N, &S.V32)) || (st = dalloc_t(s, 15 * N, &S.Fh32))
             || (st = dalloc_t(s, 9 * N, &S.fm32)) || (st = dalloc_t(s, 3 * N, &S.fdet32))
@@ -198,8 +207,13 @@ cfd_status_t create_structured(cfd_solver *s, const cfd_geometry_t *g)
         }
     }
     if (s->mixed) {
-        mixed_geometry(S);
-        s->ctx->launches += kMixedGeometryLaunches;
+        if (s->form == CFD_PREC_SPLIT) {
+            split_geometry(S);
+            s->ctx->launches += kSplitGeometryLaunches;
+        } else {
+            mixed_geometry(S);
+            s->ctx->launches += kMixedGeometryLaunches;
+        }
         if (cudaStreamCreateWithFlags(&S.side, cudaStreamNonBlocking) != cudaSuccess
             || cudaEventCreateWithFlags(&S.fork, cudaEventDisableTiming) != cudaSuccess
             || cudaEventCreateWithFlags(&S.join, cudaEventDisableTiming) != cudaSuccess)
@@ -230,7 +244,9 @@ cfd_status_t run_stage(cfd_solver *s, int j, double dt, bool want_L)
         ctx->launches += structured_stage(s->S, j, dt, want_L ? s->Lsoa : nullptr, nullptr, nullptr, prep_source(s, j));
         if (s->mixed) s->cur_slot = s->prep_ready = j == 2 ? 0 : j + 1;
         if (s->has_bc) {
-            if (s->mixed)
+            if (s->form == CFD_PREC_SPLIT)
+                bc_apply_split(ctx->stream, s->bc, make_view(s->S, dt, nullptr), s->cur_slot, s->P.mach);
+            else if (s->mixed)
                 bc_apply_mixed(ctx->stream, s->bc, make_view(s->S, dt, nullptr), s->cur_slot, s->P.mach);
             else
                 bc_apply_soa(ctx->stream, s->bc, s->S.prim9, (int)((long long)s->ni * s->nj * s->nk), s->P.mach);
@@ -284,7 +300,12 @@ cfd_status_t cfd_solver_create(cfd_ctx_t *ctx, const cfd_geometry_t *geom, const
     cfd_params_default(&s->prm);
     if (params) s->prm = *params;
     s->P = make_phys(&s->prm);
-    s->mixed = s->prm.precision == CFD_PREC_MIXED;
+    if (s->prm.precision < CFD_PREC_FP64 || s->prm.precision > CFD_PREC_SPLIT) {
+        delete s;
+        return fail(ctx, CFD_EINVAL, "cfd_solver_create: unknown precision");
+    }
+    s->form = s->prm.precision;
+    s->mixed = s->form != CFD_PREC_FP64;
     s->g_node = geom->g_node;
     s->sd_node = geom->sd_node;
     s->n_rows = n_rows;
@@ -305,7 +326,7 @@ cfd_status_t cfd_solver_create(cfd_ctx_t *ctx, const cfd_geometry_t *geom, const
     s->path = lattice ? CFD_PATH_STRUCTURED : CFD_PATH_GATHER;
     if (s->mixed && s->path != CFD_PATH_STRUCTURED) {
         delete s;
-        return fail(ctx, CFD_EUNSUPPORTED, "cfd_solver_create: mixed precision needs the structured path");
+        return fail(ctx, CFD_EUNSUPPORTED, "cfd_solver_create: the mixed and split forms need the structured path");
     }
     s->ni = lattice ? s->map.ni : 0;
     s->nj = lattice ? s->map.nj : 0;
@@ -377,7 +398,7 @@ cfd_status_t cfd_solver_info(const cfd_solver_t *s, cfd_solver_info_t *info)
     info->ni = s->ni;
     info->nj = s->nj;
     info->nk = s->nk;
-    info->precision = s->mixed ? CFD_PREC_MIXED : CFD_PREC_FP64;
+    info->precision = s->form;
     info->device_bytes = s->bytes;
     return CFD_OK;
 }
@@ -411,8 +432,11 @@ cfd_status_t cfd_solver_get_flow(cfd_solver_t *s, cfd_flow_t *flow_host)
     const double *src = s->flow;
     if (s->path == CFD_PATH_STRUCTURED) {
         s->S.stream = s->ctx->stream;
-        if (s->mixed && s->cur_slot >= 0) {   // FP64 FLOW of the current hi/lo state
-            mixed_flow_out(make_view(s->S, 0.0, nullptr), s->cur_slot, s->S.stream);
+        if (s->mixed && s->cur_slot >= 0) {   // FP64 FLOW of the current state
+            if (s->form == CFD_PREC_SPLIT)
+                split_flow_out(make_view(s->S, 0.0, nullptr), s->cur_slot, s->S.stream);
+            else
+                mixed_flow_out(make_view(s->S, 0.0, nullptr), s->cur_slot, s->S.stream);
             s->ctx->launches += 1;
         }
         soa_to_aos(s->ctx->stream, s->S.prim9, 9, 9, (long long)s->ni * s->nj * s->nk, s->stage9, s->S.row_of);
@@ -431,7 +455,7 @@ cfd_status_t cfd_solver_get_u0(cfd_solver_t *s, cfd_column_t *u0_host)
     const size_t R = (size_t)s->n_rows;
     const double *src = s->U[0];
     if (s->path == CFD_PATH_STRUCTURED) {
-        if (s->mixed)
+        if (s->form == CFD_PREC_MIXED)
             mixed_u_out(make_view(s->S, 0.0, nullptr), 0, s->stage5, s->ctx->stream);
         else
             soa_to_aos(s->ctx->stream, s->S.U[0], 5, 5, (long long)s->ni * s->nj * s->nk, s->stage5, s->S.row_of);
@@ -511,6 +535,8 @@ cfd_status_t cfd_solver_profile_stage(cfd_solver_t *s, int32_t j, double del_t, 
     if (s->has_bc) {   // the boundary routine as one timed entry
         if (s->path != CFD_PATH_STRUCTURED)
             bc_apply_aos(stream, s->bc, s->flow, s->P.mach);
+        else if (s->form == CFD_PREC_SPLIT)
+            bc_apply_split(stream, s->bc, make_view(s->S, del_t, nullptr), s->cur_slot, s->P.mach);
         else if (s->mixed)
             bc_apply_mixed(stream, s->bc, make_view(s->S, del_t, nullptr), s->cur_slot, s->P.mach);
         else

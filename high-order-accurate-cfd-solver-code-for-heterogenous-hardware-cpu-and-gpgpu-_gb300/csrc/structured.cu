@@ -98,6 +98,7 @@ __global__ void k_soa_to_aos(const double *__restrict__ soa, int stride, int nco
 int structured_stage(const StructuredLaunch &S, int jst, double dt, double *Lout, cudaEvent_t *ev,
                      const char **names, int prep_from)
 {
+    if (S.mixed == 2) return split_stage(S, jst, dt, Lout, ev, prep_from, names);
     if (S.mixed) return mixed_stage(S, jst, dt, Lout, ev, prep_from, names);
     const LatView g = make_view(S, dt, Lout);
     const unsigned nb = blocks_for(g.N, 128);

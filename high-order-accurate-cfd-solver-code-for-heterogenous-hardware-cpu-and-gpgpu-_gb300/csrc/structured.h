@@ -13,7 +13,7 @@ struct StructuredLaunch {
     int ni, nj, nk;
     cudaStream_t stream;
     Phys P;
-    int mixed;                 // 1: the mixed-precision form (mixed.cu)
+    int mixed;                 // 1: the mixed-precision form (mixed.cu); 2: the split form (split.cu)
     const double *m9;          // [9][N]   node metrics
     const double *det;         // [N]
     const double *fm;          // [3 dir][3 comp][N] metric of face n+1/2
@@ -36,6 +36,8 @@ struct StructuredLaunch {
     float *fdet32 = nullptr;   // [3][N]
     float *node32 = nullptr;   // [11][N] node metrics, det, det^(-1/3)
     float *idet32 = nullptr;   // [2][N] 1/det hi, lo
+    double *idet64 = nullptr;  // [N] 1/det (split form)
+    float *Whl = nullptr;      // [10][N] hi/lo read copy of the stage's state (split form)
     float *prim32 = nullptr;   // [9][N] FP32 pressure (LF_P) and mu (LF_MU) of the stage
     // mixed form: side stream and fork/join events for the viscous pass,
     // and two more for the j and k face passes (null: everything on `stream`)
@@ -73,6 +75,20 @@ void mixed_flow_out(const LatView &g, int q, cudaStream_t st);
 // FP64 U of slot q as AoS rows 1..N of 5 doubles.
 void mixed_u_out(const LatView &g, int q, double *aos, cudaStream_t st);
 
+// Split-precision stage j (split.cu): the same sequencing and prep sources
+// as mixed_stage, the state in FP64 slots.
+int split_stage(const StructuredLaunch &S, int j, double dt, double *Lout, cudaEvent_t *ev, int prep_from,
+                const char **names);
+// FP32 copies of the face and node metrics and the FP64 1/det (once, after
+// upload; kernels launched: 2).
+constexpr int kSplitGeometryLaunches = 2;
+void split_geometry(const StructuredLaunch &S);
+// FP64 FLOW (g.prim9, SoA) from the FP64 state in slot q; mu from prim32.
+void split_flow_out(const LatView &g, int q, cudaStream_t st);
+// U_Q of slot dst from FLOW (src = kPrepFromFlow) or from the state in slot
+// src (one launch).
+void split_prep(const LatView &g, int src, int dst, cudaStream_t st);
+
 // Device view of a StructuredLaunch for one stage.
 inline LatView make_view(const StructuredLaunch &S, double dt, double *Lout)
 {
@@ -93,6 +109,8 @@ inline LatView make_view(const StructuredLaunch &S, double dt, double *Lout)
     g.fdet32 = S.fdet32;
     g.node32 = S.node32;
     g.idet32 = S.idet32;
+    g.idet64 = S.idet64;
+    g.Whl = S.Whl;
     g.prim9 = S.prim9;
     g.prim32 = S.prim32;
     g.U0 = S.U[0];

@@ -277,7 +277,7 @@ class Solver:
         i = abi.SolverInfo()
         self.ctx.check(self.lib.cfd_solver_info(self.h, C.byref(i)), "cfd_solver_info")
         return SolverInfo("structured" if i.path == abi.PATH_STRUCTURED else "gather", (i.ni, i.nj, i.nk),
-                          "mixed" if i.precision == abi.PREC_MIXED else "fp64", int(i.device_bytes))
+                          abi.PREC_NAMES[i.precision], int(i.device_bytes))
 
     def set_flow(self, flow: np.ndarray):
         assert flow.shape == (self.g_node + 1, L.NFLOW) and flow.dtype == np.float64
@@ -467,5 +467,5 @@ class Batch:
     def info(self) -> BatchInfo:
         i = abi.BatchInfo()
         self.ctx.check(self.lib.cfd_batch_info(self.h, C.byref(i)), "cfd_batch_info")
-        return BatchInfo(i.n_active, i.tile_nodes, i.blocks, bool(i.graph), "mixed" if i.precision else "fp64",
+        return BatchInfo(i.n_active, i.tile_nodes, i.blocks, bool(i.graph), abi.PREC_NAMES[i.precision],
                          int(i.nodes_total), int(i.device_bytes), int(i.capacity_bytes), int(i.n_held))

@@ -119,7 +119,23 @@ CFD_SIZE_CHECK(cfd_roe_t, 288);
 #undef CFD_SIZE_CHECK
 
 /* -------------------------------------------------------- parameters ---- */
-typedef enum { CFD_PREC_FP64 = 0, CFD_PREC_MIXED = 1 } cfd_precision_t;
+/* Arithmetic of a solver or batch (no counterpart in the reference, whose
+ * kernels are FP64 throughout):
+ *   CFD_PREC_FP64   the reference's FP64 arithmetic in its evaluation order
+ *                   (relative L2 <= 1e-12 against it);
+ *   CFD_PREC_MIXED  everything in FP32 on the FP32 pipe: the conserved state
+ *                   and the RK3 accumulation as hi + lo pairs of FP32 numbers
+ *                   (double-float, about 48 bits), the geometry as FP32
+ *                   copies -- no FP64 instruction in a stage;
+ *   CFD_PREC_SPLIT  FP64 for the conserved state, the RK3 accumulation,
+ *                   Q = U/det, the metric/Jacobian products of the face flux
+ *                   (DET_f (m_f . F), Weno.cl:2585-2728) with its LLF
+ *                   average and the flux difference L; FP32 for the
+ *                   characteristic projection, WENO5, the LLF speed and
+ *                   dissipation, the viscous and SGS fluxes and the node
+ *                   fluxes of the sixth-order correction.
+ * The mixed and split forms run on lattices only (structured path). */
+typedef enum { CFD_PREC_FP64 = 0, CFD_PREC_MIXED = 1, CFD_PREC_SPLIT = 2 } cfd_precision_t;
 
 /* The constants the reference hard-codes (Viscous.cl:30-33 Mach 1.5,
  * Reyl 500, Pr 0.72, Free_t 273; Weno.cl:59 Epsilon 10e-8).  A NULL params
