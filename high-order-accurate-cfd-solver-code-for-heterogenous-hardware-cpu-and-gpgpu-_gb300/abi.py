@@ -115,7 +115,19 @@ PROTOTYPES = {
     "cfd_batch_info": (C.c_int, [_vp, C.POINTER(BatchInfo)]),
     "cfd_lattice_stage_static": (C.c_int, [_vp, _i32, _i32, _i32, _i32, _d, C.POINTER(Params)] + [_vp] * 8),
 }
-STATIC_MAX_NODES = 32768
+
+
+def _header_define(name: str) -> int:
+    """An integer #define of include/cfd_rhs.h (the one source of the value)."""
+    import re
+    text = (pathlib.Path(__file__).resolve().parent.parent / "include" / "cfd_rhs.h").read_text()
+    m = re.search(r"^#define\s+" + name + r"\s+(\d+)", text, flags=re.M)
+    if not m:
+        raise RuntimeError(f"{name} not defined in include/cfd_rhs.h")
+    return int(m.group(1))
+
+
+STATIC_MAX_NODES = _header_define("CFD_STATIC_MAX_NODES")
 
 _lib = None
 

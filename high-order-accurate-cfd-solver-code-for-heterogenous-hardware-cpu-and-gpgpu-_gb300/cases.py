@@ -8,6 +8,9 @@ benchmark configurations describe are generated here, deterministically:
 * ``taylor_green``      -- periodic [0, 2 pi)^3 with sinusoidally perturbed
   node positions x_i = xi_i + A sin(xi_j) sin(xi_k) (cyclic), analytic
   metrics, Taylor-Green vortex initial condition.
+* ``shock_slab``        -- the perturbed periodic lattice of the Taylor-Green
+  case with a high-pressure, high-density slab drifting along x: shocks
+  from its edges (the shocked curvilinear workload's discontinuity).
 * ``ghost_box``         -- a non-periodic box surrounded by three layers of
   ghost nodes (loc = 100) with boundary codes on the faces, edges and corners,
   used to exercise the one-sided stencil branches keyed on ``loc``.
@@ -301,16 +304,14 @@ def isentropic_vortex(n=64, length=10.0, beta=5.0, u_inf=0.5, center=(5.0, 5.0),
                 cfl_dt(a, rows, cfl))
 
 
-def taylor_green(n=128, amp=0.05, mach=0.1, reynolds=1600.0, prandtl=0.72, t_inf=273.0,
-                 weno_eps=1e-7, cfl=0.5, les=1, shape=None) -> Case:
-    """Taylor-Green vortex on a periodic [0, 2 pi)^3 grid with perturbed nodes
+def _perturbed_periodic_box(ni, nj, nk, amp):
+    """Reference arrays of a periodic [0, 2 pi)^3 lattice with perturbed nodes
     x = xi1 + A sin xi2 sin xi3, y = xi2 + A sin xi3 sin xi1,
-    z = xi3 + A sin xi1 sin xi2.  Node metrics and det come from the analytic
-    Jacobian (index coordinates, spacing h = 2 pi / n); face metrics and face
-    determinants by the reference's six-point midpoint rule.  Initial state
-    u = sin x cos y cos z, v = -cos x sin y cos z, w = 0, rho = 1,
-    p = 1/(gamma M^2) + (cos 2x + cos 2y)(cos 2z + 2)/16."""
-    ni, nj, nk = shape if shape is not None else (n, n, n)
+    z = xi3 + A sin xi1 sin xi2: the neighbour table, node metrics and det
+    from the analytic Jacobian (index coordinates, spacing h = 2 pi / n per
+    direction), face metrics and face determinants by the reference's
+    six-point midpoint rule.  Returns the arrays and the node coordinates
+    (flattened in row order)."""
     hs = (2 * math.pi / ni, 2 * math.pi / nj, 2 * math.pi / nk)
     # arrays in row order [k, j, i] (i fastest)
     x3, x2, x1 = np.meshgrid(np.arange(nk) * hs[2], np.arange(nj) * hs[1], np.arange(ni) * hs[0], indexing="ij")
@@ -338,9 +339,18 @@ def taylor_green(n=128, amp=0.05, mach=0.1, reynolds=1600.0, prandtl=0.72, t_inf
     a["metric"][1:, 0:9] = m9.reshape(-1, 9)
     a["det"][1:] = det.ravel()
     _lattice_half_points(a, m9, det)
+    return a, X.ravel(), Y.ravel(), Z.ravel()
 
+
+def taylor_green(n=128, amp=0.05, mach=0.1, reynolds=1600.0, prandtl=0.72, t_inf=273.0,
+                 weno_eps=1e-7, cfl=0.5, les=1, shape=None) -> Case:
+    """Taylor-Green vortex on the perturbed periodic [0, 2 pi)^3 lattice
+    (_perturbed_periodic_box).  Initial state u = sin x cos y cos z,
+    v = -cos x sin y cos z, w = 0, rho = 1,
+    p = 1/(gamma M^2) + (cos 2x + cos 2y)(cos 2z + 2)/16."""
+    ni, nj, nk = shape if shape is not None else (n, n, n)
+    a, xx, yy, zz = _perturbed_periodic_box(ni, nj, nk, amp)
     gam = 1.4
-    xx, yy, zz = X.ravel(), Y.ravel(), Z.ravel()
     u = np.sin(xx) * np.cos(yy) * np.cos(zz)
     v = -np.cos(xx) * np.sin(yy) * np.cos(zz)
     w = np.zeros_like(u)
@@ -352,6 +362,35 @@ def taylor_green(n=128, amp=0.05, mach=0.1, reynolds=1600.0, prandtl=0.72, t_inf
                  viscous=1, les=les)
     return Case("taylor_green", (ni, nj, nk), True, ni * nj * nk, ni * nj * nk, a, prm,
                 cfl_dt(a, rows, cfl))
+
+
+def shock_slab(shape=(256, 64, 64), amp=0.05, mach=0.8, reynolds=5e5, prandtl=0.72, t_inf=273.0,
+               p_ratio=10.0, rho_ratio=4.0, drift=1.5, weno_eps=1e-7, cfl=0.5, les=1) -> Case:
+    """A shocked flow on the perturbed periodic lattice (_perturbed_periodic_box,
+    the same curvilinear geometry as the Taylor-Green case): the slab
+    pi/2 <= x < 3 pi/2 starts at p_ratio times the free-stream pressure
+    1/(gamma M^2) and rho_ratio times its density (rho = 1 outside), with
+    discontinuous edges; every node moves with u = drift x the free-stream
+    sound speed 1/M along x.  Each slab edge is a Riemann problem: shocks and
+    contacts run out from both edges from the first step.  The drift keeps
+    u > 0 throughout, so the contravariant velocity along i is positive and
+    the reference's LLF speed (lambda_5 = U.grad(zeta) + c|grad(zeta)| only,
+    Weno.cl:2859-2911) bounds the wave speeds there.  Viscous with the MTS
+    LES model at the NACA0012 workload's Mach and Reynolds numbers."""
+    ni, nj, nk = shape
+    a, xx, yy, zz = _perturbed_periodic_box(ni, nj, nk, amp)
+    gam = 1.4
+    p_inf = 1.0 / (gam * mach * mach)
+    inside = (xx >= 0.5 * math.pi) & (xx < 1.5 * math.pi)
+    rho = np.where(inside, rho_ratio, 1.0)
+    p = np.where(inside, p_ratio * p_inf, p_inf)
+    u = np.full_like(rho, drift / mach)
+    z0 = np.zeros_like(rho)
+    _flow_from_primitives(a["flow"][1:], rho, u, z0, z0, p, mach)
+    rows = np.arange(1, ni * nj * nk + 1)
+    prm = Params(mach=mach, reynolds=reynolds, prandtl=prandtl, t_inf=t_inf, weno_eps=weno_eps,
+                 viscous=1, les=les)
+    return Case("shock_slab", (ni, nj, nk), True, ni * nj * nk, ni * nj * nk, a, prm, cfl_dt(a, rows, cfl))
 
 
 # Boundary codes of owned nodes by the box faces they lie on, in the

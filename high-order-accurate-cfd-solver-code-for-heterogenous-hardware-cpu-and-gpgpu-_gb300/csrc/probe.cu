@@ -1,8 +1,8 @@
-// probe.cu -- measured arithmetic peaks for the rooflines the benchmark
-// reports.  The measured peaks cover HBM bandwidth and bf16 tensor
-// throughput only; the FP64 path is bounded by the FP64 pipe and the mixed
-// path partly by FP32, so their denominators are measured here: independent
-// FMA chains (8 per thread, no memory traffic), timed with CUDA events.
+// probe.cu -- measured arithmetic peaks (cfd_probe_flops), a public
+// diagnostic: the FP64 path is bounded by the FP64 pipe and the reduced
+// forms partly by FP32, so their roofline denominators are measured here:
+// independent FMA chains (8 per thread, no memory traffic), timed with CUDA
+// events.  HBM bandwidth and tensor throughput are measured elsewhere.
 #include "internal.h"
 
 namespace cfd {

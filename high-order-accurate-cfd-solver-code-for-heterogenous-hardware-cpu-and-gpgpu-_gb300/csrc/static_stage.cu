@@ -18,7 +18,9 @@
 // them.  Host code cannot use the array's name as a device address, so the
 // first call on each device looks the address up with cudaGetSymbolAddress
 // (with that device current) and caches it; make that first call before any
-// stream capture begins.
+// stream capture begins.  The cached address belongs to the device's
+// current context: after cudaDeviceReset the process must not call the
+// entry point again.
 #include <mutex>
 
 #include "internal.h"
@@ -106,7 +108,8 @@ extern "C" cfd_status_t cfd_lattice_stage_static(void *cuda_stream, int32_t ni, 
     const long long N = (long long)ni * nj * nk;
     if (N > CFD_STATIC_MAX_NODES) return CFD_EINVAL;   // beyond the static scratch array
     if (!det || !deter || !metric || !U0 || !U1 || !U2 || !FLOW) return CFD_EINVAL;
-    if (params && params->precision == CFD_PREC_MIXED) return CFD_EUNSUPPORTED;   // FP64 form only
+    if (params && params->precision != CFD_PREC_FP64) return CFD_EUNSUPPORTED;   // FP64 form only
+    if (cudaPeekAtLastError() != cudaSuccess) return CFD_ECUDA;   // an earlier error, left for the caller
     double *base = nullptr;
     cfd_status_t s = scratch_address(&base);
     if (s != CFD_OK) return s;
@@ -171,7 +174,8 @@ extern "C" cfd_status_t cfd_lattice_stage_static(void *cuda_stream, int32_t ni, 
     from_soa(st, S.U[advanced], 5, 0, 5, N, (double *)Ucaller[advanced]);
     if (L_out) from_soa(st, Lsoa, 5, 0, 5, N, (double *)L_out);
 
-    e = cudaGetLastError();
+    // peek, not get: a failed launch stays readable by the caller's own checks
+    e = cudaPeekAtLastError();
     if (e != cudaSuccess) return CFD_ECUDA;
     unsigned flags = 0;
     e = cudaMemcpyAsync(&flags, S.flags, sizeof(unsigned), cudaMemcpyDeviceToHost, st);

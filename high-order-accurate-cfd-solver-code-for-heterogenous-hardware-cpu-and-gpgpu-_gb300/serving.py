@@ -95,6 +95,32 @@ def poisson_requests(count: int, rate: float = 50.0, n_range=(32, 160), steps_ra
     return out
 
 
+def mean_request_work(n_range=(32, 160), steps_range=(50, 400), samples: int = 400000, seed: int = 1) -> float:
+    """Mean cell-updates (nodes x steps) of one request of the stream that
+    poisson_requests draws with these ranges: the mean of n^3 over the
+    rounded log-uniform edge (sampled) times the mean step count."""
+    rng = np.random.default_rng(seed)
+    n = np.round(np.exp(rng.uniform(math.log(n_range[0]), math.log(n_range[1]), samples)))
+    return float(np.mean(n ** 3)) * 0.5 * (steps_range[0] + steps_range[1])
+
+
+def make_cases(requests, workers: int = 0) -> dict:
+    """rid -> case of every request, generated on a pool of host threads
+    (the generators spend their time in numpy, which releases the GIL).
+    Taylor-Green cases of one edge are identical, so each edge is made once."""
+    import os
+    workers = workers or min(16, os.cpu_count() or 1)
+    tgv_edges = sorted({r.n for r in requests if r.kind == "tgv"})
+    with cf.ThreadPoolExecutor(max_workers=workers) as ex:
+        tgv = dict(zip(tgv_edges, ex.map(lambda n: cases.taylor_green(n=n), tgv_edges)))
+        vort = [r for r in requests if r.kind != "tgv"]
+        made = dict(zip((r.rid for r in vort), ex.map(make_case, vort)))
+    for r in requests:
+        if r.kind == "tgv":
+            made[r.rid] = tgv[r.n]
+    return made
+
+
 def least_work_first(entries, fill_nodes: int, max_hold_s: float = math.inf) -> set:
     """Slots that advance under the "least_work" policy.  entries: iterable
     of (slot, nodes, remaining steps, arrival[, seconds since its last

@@ -417,8 +417,12 @@ cfd_status_t cfd_batch_tune(cfd_batch_t *b, int32_t steps_per_trial);
 cfd_status_t cfd_batch_info(const cfd_batch_t *b, cfd_batch_info_t *info);
 
 /* ------------------------------------------------------------ probes ---- */
-/* Measured FMA throughput of this device (FLOP/s, FMA = 2 FLOP): fp64 != 0
- * for double, 0 for float.  Denominator of the FP64/FP32 rooflines. */
+/* A public diagnostic with no counterpart in the reference: the measured
+ * FMA throughput of this device (FLOP/s, FMA = 2 FLOP; fp64 != 0 for
+ * double, 0 for float), from eight independent FMA chains per thread on
+ * every SM.  A
+ * caller divides its own FLOP rate by it to express a kernel as a fraction
+ * of the device's FP64 or FP32 peak (the FP64 roofline of the RHS path). */
 cfd_status_t cfd_probe_flops(cfd_ctx_t *ctx, int32_t fp64, double *flops_per_s);
 
 /* ------------------------------------------- allocation-free RK3 stage -- */
@@ -433,10 +437,12 @@ cfd_status_t cfd_probe_flops(cfd_ctx_t *ctx, int32_t fp64, double *flops_per_s);
  * held until the process exits).  The caller passes the reference-layout
  * device buffers, rows 1..ni*nj*nk in lattice order (i fastest); det, deter
  * and metric are read; FLOW, U_j, the U the stage advances and L_out (may be
- * NULL) are written; FP64 form only (CFD_PREC_MIXED -> CFD_EUNSUPPORTED).
+ * NULL) are written; FP64 form only (another precision -> CFD_EUNSUPPORTED).
  * Larger lattices are rejected with CFD_EINVAL.  The
  * first call on each device looks up the array's device address; make it
- * before any stream capture.  All calls share the array: calls that overlap
+ * before any stream capture.  The address is kept for the process: do not
+ * call the entry point after cudaDeviceReset.  A CUDA error already pending
+ * on the calling thread is left in place and reported as CFD_ECUDA.  All calls share the array: calls that overlap
  * on the GPU race and must be serialised by the caller.  The call waits for
  * the stage to finish on `cuda_stream` and returns its status. */
 #define CFD_STATIC_MAX_NODES 32768

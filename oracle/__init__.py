@@ -5,7 +5,12 @@ bench.py may import this package; the product never does.  It wraps two
 shared libraries through ctypes:
 
 * ``liboracle.so`` -- the C restatement in cfd_oracle.c (always built;
-  plain C + OpenMP, portable to the Arm GPU host);
+  plain C + OpenMP, portable to the Arm GPU host), compiled -O2 without
+  FMA contraction: the parity build, bit-exact against the reference's own
+  kernels on x86;
+* ``liboracle_timed.so`` -- the same source compiled for speed (-O3, FMA
+  contraction allowed, the host core named when it is a Neoverse V2): the
+  CPU baseline that bench.py times, never a parity checker;
 * ``_ref/libcfd_ref.so`` -- the reference's own kernel sources compiled as
   host C++ (build_ref.sh; only where the reference checkout exists).  It pins
   the restatement; golden vectors committed under tests/golden/ were made
@@ -25,7 +30,11 @@ import numpy as np
 
 HERE = pathlib.Path(__file__).resolve().parent
 LIB = HERE / "liboracle.so"
+TIMED_LIB = HERE / "liboracle_timed.so"
 REF_LIB = HERE / "_ref" / "libcfd_ref.so"
+# The reference checkout: CFD_REFERENCE_DIR, else a directory named
+# "reference" beside this repository.
+REFERENCE_DIR = pathlib.Path(os.environ.get("CFD_REFERENCE_DIR", HERE.parent.parent / "reference"))
 
 _dp = C.POINTER(C.c_double)
 _vp = C.c_void_p
@@ -54,14 +63,38 @@ def make_bc(bc) -> OrBcLists:
                      len(bc.outlet), len(bc.inlet), len(bc.boundary), len(bc.wall))
 
 
+def _host_core_flags() -> list[str]:
+    """-mcpu for the timed build: Grace's Neoverse V2 named explicitly when
+    /proc/cpuinfo reports that core (CPU part 0xd4f); nothing elsewhere."""
+    import platform
+    if platform.machine() not in ("aarch64", "arm64"):
+        return []
+    try:
+        info = pathlib.Path("/proc/cpuinfo").read_text()
+    except OSError:
+        return []
+    return ["-mcpu=neoverse-v2"] if "0xd4f" in info else []
+
+
+TIMED_FLAGS = ["-std=gnu11", "-O3", "-ffp-contract=fast", "-fopenmp"]
+
+
+def timed_build_flags() -> str:
+    return " ".join(TIMED_FLAGS + _host_core_flags())
+
+
 def build(force: bool = False) -> None:
-    """Compile the restatement (and the reference pin where possible)."""
+    """Compile the restatement (parity and timed builds) and the reference
+    pin where the reference checkout exists."""
     src = HERE / "cfd_oracle.c"
-    if force or not LIB.exists() or LIB.stat().st_mtime < max(src.stat().st_mtime,
-                                                               (HERE / "cfd_oracle.h").stat().st_mtime):
+    newest = max(src.stat().st_mtime, (HERE / "cfd_oracle.h").stat().st_mtime)
+    if force or not LIB.exists() or LIB.stat().st_mtime < newest:
         subprocess.run(["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
                         str(src), "-o", str(LIB), "-lm"], check=True)
-    ref_dir = pathlib.Path(os.environ.get("CFD_REFERENCE_DIR", "/root/reference"))
+    if force or not TIMED_LIB.exists() or TIMED_LIB.stat().st_mtime < newest:
+        subprocess.run(["gcc", *TIMED_FLAGS, *_host_core_flags(), "-fPIC", "-shared", str(src), "-o",
+                        str(TIMED_LIB), "-lm"], check=True)
+    ref_dir = REFERENCE_DIR
     ref_srcs = [HERE / n for n in ("build_ref.sh", "ref_kernels.cpp", "ref_bc.cpp", "ref_shim.h", "bc_ref_shim.h")]
     stale = not REF_LIB.exists() or REF_LIB.stat().st_mtime < max(p.stat().st_mtime for p in ref_srcs)
     if (ref_dir / "Weno.cl").exists() and (force or stale):
@@ -69,30 +102,47 @@ def build(force: bool = False) -> None:
 
 
 _lib = None
+_timed = None
 _ref = None
 
 
 def lib():
+    """The parity build."""
     global _lib
     if _lib is None:
         if not LIB.exists():
             build()
-        _lib = C.CDLL(str(LIB))
-        _lib.oracle_stage.argtypes = [C.POINTER(OrCase), C.POINTER(OrParams), C.c_int, C.c_double, _vp]
-        _lib.oracle_rk3_steps.argtypes = [C.POINTER(OrCase), C.POINTER(OrParams), C.c_double, C.c_int]
-        _lib.oracle_uq.argtypes = [C.c_int] + [_vp] * 6
-        _lib.oracle_viscous.argtypes = [C.c_int, C.POINTER(OrParams)] + [_vp] * 11
-        _lib.oracle_weno.argtypes = ([C.c_int, C.c_int, C.c_double, C.c_double, C.POINTER(OrParams)]
-                                     + [_vp] * 17)
-        _lib.oracle_boundary_fill.argtypes = [_vp, _vp, C.POINTER(OrBcLists), C.c_double, C.c_int, C.c_int]
-        _lib.oracle_boundary_fill.restype = C.c_int
-        _lib.oracle_rk3_steps_bc.argtypes = [C.POINTER(OrCase), C.POINTER(OrParams), C.c_double, C.c_int,
-                                             C.POINTER(OrBcLists)]
-        _lib.oracle_rk3_steps_bc.restype = C.c_int
-        _lib.oracle_set_threads.argtypes = [C.c_int]
-        _lib.oracle_set_poison.argtypes = [C.c_int]
-        _lib.oracle_get_threads.restype = C.c_int
+        _lib = _declare(C.CDLL(str(LIB)))
     return _lib
+
+
+def timed_lib():
+    """The build that bench.py times as the CPU baseline."""
+    global _timed
+    if _timed is None:
+        if not TIMED_LIB.exists():
+            build()
+        _timed = _declare(C.CDLL(str(TIMED_LIB)))
+    return _timed
+
+
+def _declare(L):
+    """Argument and result types of the restatement's entry points."""
+    L.oracle_stage.argtypes = [C.POINTER(OrCase), C.POINTER(OrParams), C.c_int, C.c_double, _vp]
+    L.oracle_rk3_steps.argtypes = [C.POINTER(OrCase), C.POINTER(OrParams), C.c_double, C.c_int]
+    L.oracle_uq.argtypes = [C.c_int] + [_vp] * 6
+    L.oracle_viscous.argtypes = [C.c_int, C.POINTER(OrParams)] + [_vp] * 11
+    L.oracle_weno.argtypes = ([C.c_int, C.c_int, C.c_double, C.c_double, C.POINTER(OrParams)]
+                                 + [_vp] * 17)
+    L.oracle_boundary_fill.argtypes = [_vp, _vp, C.POINTER(OrBcLists), C.c_double, C.c_int, C.c_int]
+    L.oracle_boundary_fill.restype = C.c_int
+    L.oracle_rk3_steps_bc.argtypes = [C.POINTER(OrCase), C.POINTER(OrParams), C.c_double, C.c_int,
+                                         C.POINTER(OrBcLists)]
+    L.oracle_rk3_steps_bc.restype = C.c_int
+    L.oracle_set_threads.argtypes = [C.c_int]
+    L.oracle_set_poison.argtypes = [C.c_int]
+    L.oracle_get_threads.restype = C.c_int
+    return L
 
 
 def ref_available() -> bool:
@@ -150,10 +200,11 @@ def stage(arrays: dict, g_node: int, sd_node: int, params, j: int, dt: float, wa
     return Lout
 
 
-def rk3_steps(arrays: dict, g_node: int, sd_node: int, params, dt: float, nsteps: int) -> None:
+def rk3_steps(arrays: dict, g_node: int, sd_node: int, params, dt: float, nsteps: int, timed: bool = False) -> None:
+    """nsteps whole SSP-RK3 steps in place (timed: through the timed build)."""
     c = make_case(arrays, g_node, sd_node)
     pr = make_params(params)
-    lib().oracle_rk3_steps(C.byref(c), C.byref(pr), float(dt), int(nsteps))
+    (timed_lib() if timed else lib()).oracle_rk3_steps(C.byref(c), C.byref(pr), float(dt), int(nsteps))
 
 
 def boundary_fill(arrays: dict, bc, mach: float, initial: int = 1, sd_node: int = 0) -> None:

@@ -10,7 +10,8 @@
 # exits 0 without building when it is absent.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF_DIR="${CFD_REFERENCE_DIR:-/root/reference}"
+# the reference checkout: CFD_REFERENCE_DIR, else "reference" beside this repository
+REF_DIR="${CFD_REFERENCE_DIR:-$HERE/../../reference}"
 OUT="$HERE/_ref"
 if [ ! -f "$REF_DIR/Weno.cl" ]; then
     echo "build_ref: reference sources not found at $REF_DIR; skipping" >&2

@@ -75,3 +75,10 @@ def test_header_compiles_standalone(tmp_path, lang, compiler):
     r = subprocess.run([compiler, "-fsyntax-only", "-Wall", "-Werror", f"-I{ROOT / 'include'}", str(src)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_static_node_limit_comes_from_the_header(pkg):
+    from cfd_gb300 import abi
+    text = (ROOT / "include" / "cfd_rhs.h").read_text()
+    m = re.search(r"^#define\s+CFD_STATIC_MAX_NODES\s+(\d+)", text, flags=re.M)
+    assert m and int(m.group(1)) == abi.STATIC_MAX_NODES

@@ -3,8 +3,9 @@
 It exists for callers that cannot allocate device memory while they step a
 solution, so it keeps its intermediates in a library-owned static device
 array instead.  Its results must equal those of the resident solver's
-structured path (cfd_solver_stage) on two stages in a row, within the FP64
-tolerance of the other tests.  This file is collected last so that a run
+structured path (cfd_solver_stage) on the three stages of a step called in
+a row, and its state slots those of the oracle, within the FP64 tolerance
+of the other tests.  This file is collected last so that a run
 that stops at the first failure has run every other test already."""
 from __future__ import annotations
 
@@ -27,7 +28,10 @@ def _static_stage(ctx, dev, shape, j, dt, params):
                                             dev["metric"], dev["U0"], dev["U1"], dev["U2"], dev["flow"], dev["L"])
 
 
-def test_static_stage_matches_solver_stage(ctx):
+def test_static_stage_matches_solver_stage(ctx, oracle_mod):
+    """Three calls in a row (stages 0, 1 and 2, the last advancing U0): L and
+    FLOW after each against the resident solver, and the three state slots
+    after the step against the oracle."""
     from cfd_gb300 import abi, cases, runtime
     c = cases.taylor_green(n=20, shape=(20, 18, 16))
     assert c.sd_node <= abi.STATIC_MAX_NODES
@@ -39,7 +43,7 @@ def test_static_stage_matches_solver_stage(ctx):
     # not by the entry point)
     dev = ctx.upload_case(c.arrays, names=["det", "deter", "metric", "flow", "U0", "U1", "U2", "L"])
     own = slice(1, c.sd_node + 1)
-    for j in (0, 1):                      # two calls in a row
+    for j in (0, 1, 2):                   # calls in a row
         L_ref = s.stage(j, c.dt)
         flow_ref = s.get_flow()
         st = _static_stage(ctx, dev, c.shape, j, c.dt, c.params)
@@ -49,6 +53,12 @@ def test_static_stage_matches_solver_stage(ctx):
         assert rel_l2(L_new[own], L_ref[own]) <= TOL, f"stage {j} L"
         assert rel_l2(flow_new[own], flow_ref[own]) <= TOL, f"stage {j} FLOW"
     s.close()
+    a = {k: v.copy() for k, v in c.arrays.items()}
+    for j in range(3):
+        oracle_mod.stage(a, c.g_node, c.sd_node, c.params, j, c.dt)
+    for k in ("U0", "U1", "U2"):
+        got = ctx.download(dev, k, c.arrays[k])
+        assert rel_l2(got[own], a[k][own]) <= TOL, k
     for p in dev.values():
         ctx.free(p)
 
