@@ -51,7 +51,8 @@ class SolverInfo(C.Structure):
 class BatchInfo(C.Structure):
     _fields_ = [("n_active", C.c_int32), ("tile_nodes", C.c_int32), ("blocks", C.c_int32), ("graph", C.c_int32),
                 ("precision", C.c_int32), ("n_held", C.c_int32), ("nodes_total", C.c_uint64),
-                ("device_bytes", C.c_uint64), ("capacity_bytes", C.c_uint64)]
+                ("device_bytes", C.c_uint64), ("capacity_bytes", C.c_uint64), ("face_tiles", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 _vp = C.c_void_p
@@ -128,6 +129,7 @@ def _header_define(name: str) -> int:
 
 
 STATIC_MAX_NODES = _header_define("CFD_STATIC_MAX_NODES")
+BATCH_FACE_TILES = _header_define("CFD_BATCH_FACE_TILES")
 
 _lib = None
 

@@ -53,6 +53,12 @@ struct cfd_batch {
     BatchTile *d_tiles = nullptr;
     size_t tiles_cap = 0;
     int ntiles = 0;
+    // tiled form (reduced-precision batches): phase A items (viscous ranges
+    // and shared-memory face tiles); d_tiles then holds phase B's 1-D tiles
+    bool face_tiles = false;
+    BatchItem *d_items = nullptr;
+    size_t items_cap = 0;
+    int nitems = 0;
     int n_views = 0;
     unsigned *d_words = nullptr;          // [0..1] barrier, [2] batch flags, [4..] per-slot flags
     int threads = 128;
@@ -113,11 +119,48 @@ cfd_status_t ialloc(cfd_batch *b, BatchInst &I, size_t count, T **p)
     return CFD_OK;
 }
 
+// The face tiles of direction D of lattice view v (FaceTile<D, tile>::grid).
+template <int D>
+void face_tile_items(const LatView &g, int v, std::vector<BatchItem> &out)
+{
+    using T = FaceTile<D, D == 0 ? kBatchTileI : kBatchTileJK>;
+    const dim3 gr = T::grid(g);
+    for (unsigned z = 0; z < gr.z; ++z)
+        for (unsigned y = 0; y < gr.y; ++y)
+            for (unsigned x = 0; x < gr.x; ++x)
+                out.push_back(BatchItem{v, 1 + D, (int)x * T::kTile, (int)y * T::kWide, (int)z, 0});
+}
+
+// Phase A items of the tiled form in launch order: position w is taken by
+// block w % G in round w / G; its kind is (block + round) mod 4 while that
+// kind has items left (else the next kind that has), so that every block
+// cycles through the kinds and neighbouring blocks work on the same region.
+std::vector<BatchItem> order_items(std::vector<BatchItem> q[4], int G)
+{
+    size_t total = 0, head[4] = {0, 0, 0, 0};
+    for (int k = 0; k < 4; ++k) total += q[k].size();
+    std::vector<BatchItem> out;
+    out.reserve(total);
+    for (size_t w = 0; w < total; ++w) {
+        const int k0 = (int)(((w % G) + (w / G)) & 3);
+        for (int t = 0; t < 4; ++t) {
+            const int k = (k0 + t) & 3;
+            if (head[k] < q[k].size()) {
+                out.push_back(q[k][head[k]++]);
+                break;
+            }
+        }
+    }
+    return out;
+}
+
 cfd_status_t rebuild(cfd_batch *b)
 {
     std::vector<LatView> views;
     std::vector<BatchTile> tiles;
-    const int T = b->threads;
+    std::vector<BatchItem> kinds[4];
+    const bool tiled = b->face_tiles && b->precision != CFD_PREC_FP64;
+    const int T = tiled ? kFaceThreads : b->threads;
     uint64_t nodes = 0;
     for (size_t s = 0; s < b->slots.size(); ++s) {
         BatchInst &I = b->slots[s];
@@ -126,6 +169,12 @@ cfd_status_t rebuild(cfd_batch *b)
         const int v = (int)views.size();
         views.push_back(I.view);
         for (int n0 = 0; n0 < I.N; n0 += T) tiles.push_back(BatchTile{v, n0, std::min(T, I.N - n0), 0});
+        if (tiled) {
+            for (int n0 = 0; n0 < I.N; n0 += T) kinds[0].push_back(BatchItem{v, 0, n0, std::min(T, I.N - n0), 0, 0});
+            face_tile_items<0>(I.view, v, kinds[1]);
+            face_tile_items<1>(I.view, v, kinds[2]);
+            face_tile_items<2>(I.view, v, kinds[3]);
+        }
         nodes += (uint64_t)I.N;
     }
     cudaStream_t st = b->ctx->stream;
@@ -153,14 +202,31 @@ cfd_status_t rebuild(cfd_batch *b)
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int occ = b->precision == CFD_PREC_MIXED   ? batch_occupancy_mixed(T)
-                    : b->precision == CFD_PREC_SPLIT ? batch_occupancy_split(T)
+    const int occ = b->precision == CFD_PREC_MIXED   ? batch_occupancy_mixed(T, tiled)
+                    : b->precision == CFD_PREC_SPLIT ? batch_occupancy_split(T, tiled)
                                                      : batch_occupancy_fp64(T);
     if (occ <= 0) return fail(b->ctx, CFD_EUNSUPPORTED, "batch: stage kernel does not fit at this tile size");
     int blocks = occ * sms;
     if (b->blocks_override > 0) blocks = std::min(blocks, b->blocks_override);
-    blocks = std::max(1, std::min(blocks, 4 * std::max(b->ntiles, 1)));
+    size_t n_a = 4 * (size_t)std::max(b->ntiles, 1);   // phase A items
+    if (tiled) n_a = std::max<size_t>(1, kinds[0].size() + kinds[1].size() + kinds[2].size() + kinds[3].size());
+    blocks = std::max(1, (int)std::min<size_t>((size_t)blocks, n_a));
     b->blocks = blocks;
+    b->nitems = 0;
+    if (tiled) {
+        const std::vector<BatchItem> items = order_items(kinds, blocks);
+        if (items.size() > b->items_cap) {
+            if (b->d_items) cudaFree(b->d_items);
+            b->items_cap = std::max<size_t>(items.size(), 2 * b->items_cap);
+            e = cudaMalloc(&b->d_items, b->items_cap * sizeof(BatchItem));
+            if (e != cudaSuccess) return cuda_fail(b->ctx, e, "batch item table");
+        }
+        if (!items.empty())
+            e = cudaMemcpyAsync(b->d_items, items.data(), items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return cuda_fail(b->ctx, e, "batch item table upload");
+        b->nitems = (int)items.size();
+    }
     drop_graph(b);
     b->dirty = false;
     return CFD_OK;
@@ -174,6 +240,9 @@ BatchLaunch launch_of(cfd_batch *b)
     L.ntiles = b->ntiles;
     L.threads = b->threads;
     L.blocks = b->blocks;
+    L.tiled = b->nitems > 0 ? 1 : 0;
+    L.items = b->d_items;
+    L.nitems = b->nitems;
     L.bar = bar_words(b);
     L.gflags = batch_flags(b);
     // generous deadline for the barrier: 5 s + 50 ns per node of the batch
@@ -328,6 +397,7 @@ cfd_status_t cfd_batch_destroy(cfd_batch_t *b)
     for (auto &I : b->slots) free_instance(I);
     if (b->d_views) cudaFree(b->d_views);
     if (b->d_tiles) cudaFree(b->d_tiles);
+    if (b->d_items) cudaFree(b->d_items);
     if (b->d_words) cudaFree(b->d_words);
     delete b;
     return CFD_OK;
@@ -765,9 +835,17 @@ cfd_status_t cfd_batch_set_wait_limit(cfd_batch_t *b, int64_t limit_ns)
 
 cfd_status_t cfd_batch_set_tiling(cfd_batch_t *b, int32_t tile_nodes, int32_t max_blocks, int32_t use_graph)
 {
-    if (!b || (tile_nodes != 0 && tile_nodes != 64 && tile_nodes != 128 && tile_nodes != 256) || max_blocks < 0)
+    if (!b || max_blocks < 0) return CFD_EINVAL;
+    if (tile_nodes != 0 && tile_nodes != 64 && tile_nodes != 128 && tile_nodes != 256
+        && tile_nodes != CFD_BATCH_FACE_TILES)
         return CFD_EINVAL;
-    if (tile_nodes) b->threads = tile_nodes;
+    if (tile_nodes == CFD_BATCH_FACE_TILES && b->precision == CFD_PREC_FP64) return CFD_EINVAL;
+    if (tile_nodes == CFD_BATCH_FACE_TILES) {
+        b->face_tiles = true;
+    } else if (tile_nodes) {
+        b->face_tiles = false;
+        b->threads = tile_nodes;
+    }
     b->blocks_override = max_blocks;
     b->use_graph = use_graph != 0;
     b->dirty = true;
@@ -801,14 +879,20 @@ cfd_status_t cfd_batch_tune(cfd_batch_t *b, int32_t steps_per_trial)
         }
     };
     copy_all(true);
-    const int candidates[3] = {64, 128, 256};
-    int best = b->threads;
+    // 1-D tiles of 64, 128, 256 nodes, and for the reduced forms the
+    // shared-memory face tiles
+    std::vector<int> candidates = {64, 128, 256};
+    if (b->precision != CFD_PREC_FP64) candidates.push_back(CFD_BATCH_FACE_TILES);
+    const int threads0 = b->threads;
+    const bool faces0 = b->face_tiles;
+    int best = faces0 ? CFD_BATCH_FACE_TILES : threads0;
     float best_ms = 1e30f;
     cudaEvent_t t0, t1;
     cudaEventCreate(&t0);
     cudaEventCreate(&t1);
     for (int T : candidates) {
-        b->threads = T;
+        b->face_tiles = T == CFD_BATCH_FACE_TILES;
+        if (!b->face_tiles) b->threads = T;
         b->dirty = true;
         if ((st = rebuild(b)) != CFD_OK) continue;
         if (b->use_graph) try_capture(b);
@@ -834,7 +918,8 @@ cfd_status_t cfd_batch_tune(cfd_batch_t *b, int32_t steps_per_trial)
     e = cudaStreamSynchronize(sm);
     cudaFree(backup);
     if (e != cudaSuccess) return cuda_fail(b->ctx, e, "cfd_batch_tune restore");
-    b->threads = best;
+    b->face_tiles = best == CFD_BATCH_FACE_TILES;
+    b->threads = b->face_tiles ? threads0 : best;
     b->dirty = true;
     return rebuild(b);
 }
@@ -850,7 +935,8 @@ cfd_status_t cfd_batch_info(const cfd_batch_t *b, cfd_batch_info_t *info)
     }
     info->n_active = n;
     info->n_held = held;
-    info->tile_nodes = b->threads;
+    info->tile_nodes = b->face_tiles && b->precision != CFD_PREC_FP64 ? kFaceThreads : b->threads;
+    info->face_tiles = b->face_tiles && b->precision != CFD_PREC_FP64 ? 1 : 0;
     info->blocks = b->blocks;
     info->graph = b->graph_ok ? 1 : 0;
     info->precision = b->precision;

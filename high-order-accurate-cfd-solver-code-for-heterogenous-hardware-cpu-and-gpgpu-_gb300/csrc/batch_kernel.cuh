@@ -17,6 +17,7 @@
 // translation unit compiled with that form's flags.
 #pragma once
 
+#include "face_tile.cuh"
 #include "lattice.cuh"
 
 namespace cfd {
@@ -108,6 +109,51 @@ k_batch_stage(const LatView *__restrict__ views, const BatchTile *__restrict__ t
     if (!grid_barrier(bar, gridDim.x, limit_ns, gflags)) return;
     for (int w = blockIdx.x; w < ntiles; w += gridDim.x) {
         const BatchTile t = tiles[w];
+        if ((int)threadIdx.x < t.count) Ops::update(views[t.inst], t.n0 + threadIdx.x, jst);
+    }
+}
+
+// One work item of phase A of the tiled form (the reduced-precision
+// forms): kind 0 a viscous range of one lattice (a = first node, b = nodes),
+// kind 1 + D a face tile along D (a = first face along D, b = first node
+// across, c = line of the third axis; face_tile.cuh).
+struct BatchItem {
+    int inst, kind, a, b, c, pad;
+};
+
+// The persistent stage over items: phase A's face items stage their stencil
+// lines in shared memory as the single-lattice face passes do (Ops::face_tile)
+// instead of gathering each face's points through L1; phase B updates 1-D
+// tiles (upd) of kFaceThreads nodes.  The item order (built on the host)
+// rotates the kinds across rounds of the grid, as k_batch_stage does.
+template <class Ops>
+__global__ void __launch_bounds__(kFaceThreads, Ops::kMinBlocksTiled)
+k_batch_stage_tiled(const LatView *__restrict__ views, const BatchItem *__restrict__ items, int nitems,
+                    const BatchTile *__restrict__ upd, int nupd, int jst, unsigned *bar, unsigned *gflags,
+                    unsigned long long limit_ns)
+{
+    __shared__ float smem[Ops::kTileSmemFloats];
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const BatchItem it = items[w];
+        const LatView &g = views[it.inst];
+        const TileAt at{it.a, it.b, it.c};
+        if (it.kind == 0) {
+            if ((int)threadIdx.x < it.b) {
+                if (g.P.viscous) Ops::visc(g, it.a + threadIdx.x, jst);
+                else Ops::mu(g, it.a + threadIdx.x, jst);
+            }
+        } else if (it.kind == 1) {
+            Ops::template face_tile<0>(g, at, smem);
+        } else if (it.kind == 2) {
+            Ops::template face_tile<1>(g, at, smem);
+        } else {
+            Ops::template face_tile<2>(g, at, smem);
+        }
+        __syncthreads();   // the next item restages smem
+    }
+    if (!grid_barrier(bar, gridDim.x, limit_ns, gflags)) return;
+    for (int w = blockIdx.x; w < nupd; w += gridDim.x) {
+        const BatchTile t = upd[w];
         if ((int)threadIdx.x < t.count) Ops::update(views[t.inst], t.n0 + threadIdx.x, jst);
     }
 }

@@ -19,6 +19,7 @@
 #pragma once
 
 #include "boundary.h"
+#include "face_tile.cuh"
 #include "lattice.cuh"
 #include "physics_x2.cuh"
 
@@ -324,6 +325,34 @@ __device__ __forceinline__ void face_node(const LatView &g, int n)
 #pragma unroll
         for (int o = 0; o < 6; ++o) f[o] = NF[c * N + s[o]];
         g.Fh32[(D * 5 + c) * N + n] = Fhat[c] + x2::face_correction_sym(f);
+    }
+}
+
+// Faces along D of one staged tile (face_tile.cuh): the block of
+// kFaceThreads threads stages the tile's stencil lines into smem
+// (tile_smem_floats<T>() floats) and each thread evaluates its face.  Every
+// thread of the block must call it (it synchronises the block).  RO as in
+// stage_face_lines.
+template <class T, int D, bool RO = true>
+__device__ __forceinline__ void face_tile(const LatView &g, TileAt at, float *smem)
+{
+    constexpr int S = T::kStaged;
+    float *sQ = smem, *sR = smem + 5 * S, *sF = smem + 10 * S;
+    stage_face_lines<T, D, RO>(g, at, sQ, sR, sF);
+    int n, t, a;
+    if (!tile_face<T, D>(g, at, n, t, a)) return;
+    const int N = g.N;
+    float2 P[3][5];
+    float r[5];
+    tile_stencil<T>(sQ, sR, t, a, P, r);
+    float Fhat[5];
+    x2::llf_face_flux2(P, g.fm32[(D * 3 + 0) * N + n], g.fm32[(D * 3 + 1) * N + n], g.fm32[(D * 3 + 2) * N + n],
+                       g.fdet32[D * N + n], r, (float)g.P.eps, Fhat);
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+        float f[6];
+        tile_node_fluxes<T>(sF, q, t, a, f);
+        g.Fh32[(D * 5 + q) * N + n] = Fhat[q] + x2::face_correction_sym(f);
     }
 }
 

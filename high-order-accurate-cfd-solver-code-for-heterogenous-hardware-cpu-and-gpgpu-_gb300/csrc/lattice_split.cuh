@@ -130,17 +130,14 @@ __host__ __device__ __forceinline__ LatView hilo_view(const LatView &g)
 }
 
 // The FP64 face flux of face n+1/2 along D from its stencil (P, pairs of
-// points k and 5-k), Roe state r and node fluxes f along D, plus the FP32
-// sixth-order correction of each component.
+// points k and 5-k) and Roe state r, plus corr, the FP32 sixth-order
+// correction of each component.
 template <int D>
 __device__ __forceinline__ void face_flux(const LatView &g, int n, const float2 P[3][5], const float r[5],
-                                          const float f[5][6], double out[5])
+                                          const float corr[5], double out[5])
 {
     const int N = g.N;
     const double dm[3] = {g.fm[(D * 3 + 0) * N + n], g.fm[(D * 3 + 1) * N + n], g.fm[(D * 3 + 2) * N + n]};
-    float corr[5];
-#pragma unroll
-    for (int c = 0; c < 5; ++c) corr[c] = x2::face_correction_sym(f[c]);
     x2::llf_face_flux2_split(P, g.fm32[(D * 3 + 0) * N + n], g.fm32[(D * 3 + 1) * N + n],
                              g.fm32[(D * 3 + 2) * N + n], dm, g.fdet[D * N + n], r, (float)g.P.eps, corr, out);
 }
@@ -170,15 +167,45 @@ __device__ __forceinline__ void face_node(const LatView &g, int n)
                            R[N + l], R[2 * N + l], R[4 * N + l], r);
     }
     const float *NF = g.FEG32 + (size_t)D * 5 * N;
-    float f[5][6];
+    float corr[5];
 #pragma unroll
-    for (int c = 0; c < 5; ++c)
+    for (int c = 0; c < 5; ++c) {
+        float f[6];
 #pragma unroll
-        for (int o = 0; o < 6; ++o) f[c][o] = NF[c * N + s[o]];
+        for (int o = 0; o < 6; ++o) f[o] = NF[c * N + s[o]];
+        corr[c] = x2::face_correction_sym(f);
+    }
     double Fh[5];
-    face_flux<D>(g, n, P, r, f, Fh);
+    face_flux<D>(g, n, P, r, corr, Fh);
 #pragma unroll
     for (int c = 0; c < 5; ++c) g.Fh[(D * 5 + c) * N + n] = Fh[c];
+}
+
+// Faces along D of one staged tile (mx::face_tile with the FP64 face
+// flux of face_flux written to Fh).
+template <class T, int D, bool RO = true>
+__device__ __forceinline__ void face_tile(const LatView &g, TileAt at, float *smem)
+{
+    constexpr int S = T::kStaged;
+    float *sQ = smem, *sR = smem + 5 * S, *sF = smem + 10 * S;
+    stage_face_lines<T, D, RO>(g, at, sQ, sR, sF);
+    int n, t, a;
+    if (!tile_face<T, D>(g, at, n, t, a)) return;
+    const int N = g.N;
+    float2 P[3][5];
+    float r[5];
+    tile_stencil<T>(sQ, sR, t, a, P, r);
+    float corr[5];
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+        float f[6];
+        tile_node_fluxes<T>(sF, q, t, a, f);
+        corr[q] = x2::face_correction_sym(f);
+    }
+    double Fh[5];
+    face_flux<D>(g, n, P, r, corr, Fh);
+#pragma unroll
+    for (int q = 0; q < 5; ++q) g.Fh[(D * 5 + q) * N + n] = Fh[q];
 }
 
 // RHS and SSP-RK3 stage jst: the face-flux difference in FP64, the viscous

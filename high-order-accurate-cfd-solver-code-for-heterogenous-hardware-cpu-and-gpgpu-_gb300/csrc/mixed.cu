@@ -87,33 +87,8 @@ template <int D>
 __global__ void __launch_bounds__(kFaceThreads, CFD_MFACE_MIN_BLOCKS) k_face_tile_m(LatView g)
 {
     using T = MTile<D>;
-    constexpr int S = T::kStaged;
-    __shared__ float sQ[5 * S], sR[5 * S], sF[5 * S];
-    stage_face_lines<T, D>(g, sQ, sR, sF);
-    int n, t, a;
-    if (!tile_face<T, D>(g, n, t, a)) return;
-    const int N = g.N;
-    float2 P[3][5];
-#pragma unroll
-    for (int o = 0; o < 3; ++o)
-#pragma unroll
-        for (int q = 0; q < 5; ++q) P[o][q] = make_float2(sQ[q * S + T::at(t + o, a)], sQ[q * S + T::at(t + 5 - o, a)]);
-    float r[5];
-    {
-        const int er = T::at(t + 3, a), el = T::at(t + 2, a);
-        roe_average<float>(sR[3 * S + er], sR[er], sR[S + er], sR[2 * S + er], sR[4 * S + er], sR[3 * S + el], sR[el],
-                           sR[S + el], sR[2 * S + el], sR[4 * S + el], r);
-    }
-    float Fhat[5];
-    x2::llf_face_flux2(P, g.fm32[(D * 3 + 0) * N + n], g.fm32[(D * 3 + 1) * N + n], g.fm32[(D * 3 + 2) * N + n],
-                       g.fdet32[D * N + n], r, (float)g.P.eps, Fhat);
-#pragma unroll
-    for (int q = 0; q < 5; ++q) {
-        float f[6];
-#pragma unroll
-        for (int o = 0; o < 6; ++o) f[o] = sF[q * S + T::at(t + o, a)];
-        g.Fh32[(D * 5 + q) * N + n] = Fhat[q] + x2::face_correction_sym(f);
-    }
+    __shared__ float smem[tile_smem_floats<T>()];
+    mx::face_tile<T, D>(g, tile_of_block<T>(), smem);
 }
 
 template <int D>

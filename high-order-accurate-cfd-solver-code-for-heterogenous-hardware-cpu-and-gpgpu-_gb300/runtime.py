@@ -322,6 +322,7 @@ class BatchInfo:
     device_bytes: int
     capacity_bytes: int
     n_held: int = 0
+    face_tiles: bool = False
 
 
 class StagedInstance:
@@ -458,6 +459,8 @@ class Batch:
         self.ctx.check(self.lib.cfd_batch_set_wait_limit(self.h, int(limit_ns)), "cfd_batch_set_wait_limit")
 
     def set_tiling(self, tile_nodes: int = 0, max_blocks: int = 0, use_graph: bool = True):
+        """tile_nodes: 64/128/256 (1-D tiles), abi.BATCH_FACE_TILES (shared-memory
+        face tiles, mixed and split batches), 0 keeps the current choice."""
         self.ctx.check(self.lib.cfd_batch_set_tiling(self.h, int(tile_nodes), int(max_blocks), 1 if use_graph else 0),
                        "cfd_batch_set_tiling")
 
@@ -468,4 +471,5 @@ class Batch:
         i = abi.BatchInfo()
         self.ctx.check(self.lib.cfd_batch_info(self.h, C.byref(i)), "cfd_batch_info")
         return BatchInfo(i.n_active, i.tile_nodes, i.blocks, bool(i.graph), abi.PREC_NAMES[i.precision],
-                         int(i.nodes_total), int(i.device_bytes), int(i.capacity_bytes), int(i.n_held))
+                         int(i.nodes_total), int(i.device_bytes), int(i.capacity_bytes), int(i.n_held),
+                         bool(i.face_tiles))

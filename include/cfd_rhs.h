@@ -345,6 +345,8 @@ typedef struct {
     uint64_t nodes_total;
     uint64_t device_bytes;     /* admitted instance memory                    */
     uint64_t capacity_bytes;   /* admission budget                            */
+    int32_t face_tiles;        /* 1: phase A in shared-memory face tiles      */
+    int32_t reserved;
 } cfd_batch_info_t;
 
 /* capacity_bytes = 0: 85 % of the device memory free at creation. */
@@ -408,11 +410,18 @@ cfd_status_t cfd_batch_set_flow(cfd_batch_t *b, int32_t slot, const cfd_flow_t *
  * (CFD_ETIMEOUT) until cfd_batch_set_flow restores it or it is removed.
  * Instances that were held are not affected. */
 cfd_status_t cfd_batch_set_wait_limit(cfd_batch_t *b, int64_t limit_ns);
-/* tile_nodes in {64, 128, 256} (0 = keep), max_blocks (0 = occupancy limit),
+/* tile_nodes in {64, 128, 256}: phase A of a stage works on 1-D tiles of
+ * that many nodes, each face evaluated from its own stencil gathers;
+ * CFD_BATCH_FACE_TILES (mixed and split batches): phase A works on the
+ * viscous ranges and on 2-D face tiles whose stencil lines a block of 128
+ * threads stages in shared memory (32 faces along i x 4, or 16 along j or k
+ * x 8); 0 keeps the current choice.  max_blocks (0 = occupancy limit),
  * use_graph 0/1. */
+#define CFD_BATCH_FACE_TILES 1
 cfd_status_t cfd_batch_set_tiling(cfd_batch_t *b, int32_t tile_nodes, int32_t max_blocks, int32_t use_graph);
-/* Times each tile size on the live batch (state saved and restored) and
- * keeps the fastest. */
+/* Times each tiling (1-D tiles of 64, 128, 256 nodes and, for the mixed and
+ * split batches, the face tiles) on the live batch (state saved and
+ * restored) and keeps the fastest. */
 cfd_status_t cfd_batch_tune(cfd_batch_t *b, int32_t steps_per_trial);
 cfd_status_t cfd_batch_info(const cfd_batch_t *b, cfd_batch_info_t *info);
 

@@ -282,3 +282,31 @@ def test_nonfinite_instance_is_isolated(ctx):
     assert np.array_equal(alone.get_flow(a), b.get_flow(s_good))
     b.close()
     alone.close()
+
+
+@pytest.mark.parametrize("precision", [1, 2])
+def test_face_tiles_equal_node_tiles_bitwise(ctx, precision):
+    """Phase A on shared-memory face tiles (CFD_BATCH_FACE_TILES) evaluates
+    the same arithmetic as the 1-D tiles: the same bits."""
+    from cfd_gb300 import abi, runtime
+    cs = mix_cases()
+    out = []
+    for tiling in (128, abi.BATCH_FACE_TILES):
+        b = runtime.Batch(ctx, precision)
+        slots = [b.add(c) for c in cs]
+        b.set_tiling(tiling)
+        assert b.info().face_tiles == (tiling == abi.BATCH_FACE_TILES)
+        b.step(3)
+        out.append([b.get_u0(s) for s in slots])
+        b.close()
+    for a, t in zip(*out):
+        assert np.array_equal(a, t)
+
+
+def test_face_tiles_refused_for_fp64(ctx):
+    from cfd_gb300 import abi, runtime
+    b = runtime.Batch(ctx, 0)
+    with pytest.raises(abi.CfdError) as e:
+        b.set_tiling(abi.BATCH_FACE_TILES)
+    assert e.value.status == abi.EINVAL
+    b.close()
