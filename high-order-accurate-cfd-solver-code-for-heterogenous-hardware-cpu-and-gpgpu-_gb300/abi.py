@@ -114,6 +114,8 @@ PROTOTYPES = {
     "cfd_batch_set_tiling": (C.c_int, [_vp, _i32, _i32, _i32]),
     "cfd_batch_tune": (C.c_int, [_vp, _i32]),
     "cfd_batch_info": (C.c_int, [_vp, C.POINTER(BatchInfo)]),
+    "cfd_compact_metrics": (C.c_int, [_vp, _i32, _d, _vp, _vp]),
+    "cfd_half_point_metrics": (C.c_int, [_vp, _i32, _i32, _vp, _vp, _vp]),
     "cfd_lattice_stage_static": (C.c_int, [_vp, _i32, _i32, _i32, _i32, _d, C.POINTER(Params)] + [_vp] * 8),
 }
 

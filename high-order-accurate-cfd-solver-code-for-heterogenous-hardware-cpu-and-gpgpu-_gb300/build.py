@@ -40,6 +40,11 @@ EXACT_FP64 = {"dropin.cu", "structured.cu", "batch_fp64.cu", "boundary.cu"}
 FAST_FP32 = {"mixed.cu", "batch_mixed.cu", "split.cu", "batch_split.cu"}
 
 
+# Translation units whose host code follows the reference's evaluation order
+# (the geometry producer): no FMA contraction of host arithmetic either.
+EXACT_HOST = {"geometry.cu"}
+
+
 def sources() -> list[pathlib.Path]:
     return sorted(CSRC.glob("*.cu"))
 
@@ -66,6 +71,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
         fmad = ["--fmad=false"] if src.name in EXACT_FP64 else []
         if src.name in FAST_FP32:
             fmad += ["--prec-div=false", "--prec-sqrt=false"]
+        if src.name in EXACT_HOST:
+            fmad += ["-Xcompiler", "-ffp-contract=off"]
         user = os.environ.get("CFD_NVCC_EXTRA", "").split()
         cmd = [cc, *ARCH, *NVCC_FLAGS, *fmad, *extra, *user, "-c", str(src), "-o", str(obj)]
         r = subprocess.run(cmd, capture_output=True, text=True)

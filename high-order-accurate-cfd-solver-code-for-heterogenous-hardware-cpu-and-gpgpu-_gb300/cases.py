@@ -423,6 +423,54 @@ def reference_loc_codes(imin, imax, jmin, jmax, kmin, kmax) -> np.ndarray:
     return loc
 
 
+def box_mesh(shape=(12, 10, 8), amp=0.04, lengths=(1.0, 0.8, 0.6)):
+    """A curvilinear box as the reference's mesh tools hand it to its
+    geometry routines: rows 1..N in lattice order (i fastest), neighbour 0
+    where the box ends, the reference's loc codes on its faces, edges and
+    corners, ID 0.  Nodes x = L1 (s1 + A sin(pi s2) sin(pi s3)), y and z
+    alike (cyclic), s_d = index / (n_d - 1).  Returns the GRID array and the
+    analytic node metrics [N, 9] and det [N] (index coordinates)."""
+    ni, nj, nk = shape
+    k, j, i = np.meshgrid(np.arange(nk), np.arange(nj), np.arange(ni), indexing="ij")
+    s1, s2, s3 = i / (ni - 1), j / (nj - 1), k / (nk - 1)
+    A, pi = amp, math.pi
+    L1, L2, L3 = lengths
+    X = L1 * (s1 + A * np.sin(pi * s2) * np.sin(pi * s3))
+    Y = L2 * (s2 + A * np.sin(pi * s3) * np.sin(pi * s1))
+    Z = L3 * (s3 + A * np.sin(pi * s1) * np.sin(pi * s2))
+    N = ni * nj * nk
+    g = np.zeros(N + 1, L.GRID_DTYPE)
+    g["x"][1:], g["y"][1:], g["z"][1:] = X.ravel(), Y.ravel(), Z.ravel()
+    row = (i + ni * (j + nj * k)) + 1
+
+    def nb(di, dj, dk):
+        ii, jj, kk = i + di, j + dj, k + dk
+        inside = (ii >= 0) & (ii < ni) & (jj >= 0) & (jj < nj) & (kk >= 0) & (kk < nk)
+        return np.where(inside, (ii + ni * (jj + nj * kk)) + 1, 0).ravel()
+
+    g["N0"][1:], g["N1"][1:], g["N2"][1:] = nb(0, 1, 0), nb(1, 0, 0), nb(0, -1, 0)
+    g["N3"][1:], g["N4"][1:], g["N5"][1:] = nb(-1, 0, 0), nb(0, 0, 1), nb(0, 0, -1)
+    g["ID"][1:] = 0
+    g["loc"][1:] = reference_loc_codes(i == 0, i == ni - 1, j == 0, j == nj - 1, k == 0, k == nk - 1).ravel()
+    assert (row.ravel() == np.arange(1, N + 1)).all()
+    # analytic Jacobian d(x, y, z)/d(i, j, k)
+    c1, c2, c3 = np.cos(pi * s1), np.cos(pi * s2), np.cos(pi * s3)
+    n1, n2, n3 = np.sin(pi * s1), np.sin(pi * s2), np.sin(pi * s3)
+    h = (1.0 / (ni - 1), 1.0 / (nj - 1), 1.0 / (nk - 1))
+    jac = np.empty(X.shape + (3, 3))
+    jac[..., 0, 0] = L1 * h[0]
+    jac[..., 0, 1] = L1 * A * pi * c2 * n3 * h[1]
+    jac[..., 0, 2] = L1 * A * pi * n2 * c3 * h[2]
+    jac[..., 1, 0] = L2 * A * pi * n3 * c1 * h[0]
+    jac[..., 1, 1] = L2 * h[1]
+    jac[..., 1, 2] = L2 * A * pi * c3 * n1 * h[2]
+    jac[..., 2, 0] = L3 * A * pi * c1 * n2 * h[0]
+    jac[..., 2, 1] = L3 * A * pi * n1 * c2 * h[1]
+    jac[..., 2, 2] = L3 * h[2]
+    m9, det = _node_metrics(jac)
+    return g, m9.reshape(-1, 9), det.ravel()
+
+
 def ghost_box(shape=(10, 9, 8), seed=0, mach=1.5, amp=0.05, bc: bool = False) -> Case:
     """Non-periodic box of owned nodes with three ghost layers on every side.
 

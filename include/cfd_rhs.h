@@ -425,6 +425,31 @@ cfd_status_t cfd_batch_set_tiling(cfd_batch_t *b, int32_t tile_nodes, int32_t ma
 cfd_status_t cfd_batch_tune(cfd_batch_t *b, int32_t steps_per_trial);
 cfd_status_t cfd_batch_info(const cfd_batch_t *b, cfd_batch_info_t *info);
 
+/* ------------------------------------------------- geometry producer ---- */
+/* The inputs the kernels read, computed from a node table as the reference
+ * computes them once before its time loop.  Host functions (all pointers
+ * host memory, rows 0..n_rows-1, row 0 the dummy row); the results equal
+ * the reference's bit for bit.
+ *
+ * cfd_compact_metrics (Grid_Transformation.cpp:22-1045, metric_term()):
+ * x, y, z differentiated along every grid line by the sixth-order compact
+ * scheme (alpha = 1/3, coefficients 7/9 and 1/36; one-sided 197/60 closures
+ * and 2/11 rows next to the ends) with computational spacing del_zeta; det
+ * of the Jacobian and the node metrics (cofactors / det) into det[] and the
+ * node block of metric[] (zeta_x .. xi_z).  A line starts at a row with no
+ * neighbour (index 0) in the + direction (zeta: N1, eta: N0, xi: N4 with
+ * loc <= 28, 30 or 31) and follows the - neighbours to a row that has none.
+ * Rows with ID 10 (the reference's C-grid wake-cut branches) ->
+ * CFD_EUNSUPPORTED; a line of fewer than three rows -> CFD_EINVAL. */
+cfd_status_t cfd_compact_metrics(const cfd_grid_t *grid, int32_t n_rows, double del_zeta, double *det,
+                                 cfd_metric_t *metric);
+/* cfd_half_point_metrics (Main.cpp:2369-2440): the six face blocks of
+ * metric[] and deter[] for rows 1..n_owned by the six-point midpoint rule
+ * (3, -25, 150, 150, -25, 3)/256 of the node blocks and det along each
+ * direction. */
+cfd_status_t cfd_half_point_metrics(const cfd_grid_t *grid, int32_t n_rows, int32_t n_owned, const double *det,
+                                    cfd_metric_t *metric, cfd_determ_t *deter);
+
 /* ------------------------------------------------------------ probes ---- */
 /* A public diagnostic with no counterpart in the reference: the measured
  * FMA throughput of this device (FLOP/s, FMA = 2 FLOP; fp64 != 0 for

@@ -32,6 +32,7 @@ HERE = pathlib.Path(__file__).resolve().parent
 LIB = HERE / "liboracle.so"
 TIMED_LIB = HERE / "liboracle_timed.so"
 REF_LIB = HERE / "_ref" / "libcfd_ref.so"
+REF_GEOM_LIB = HERE / "_ref" / "libcfd_ref_geom.so"
 # The reference checkout: CFD_REFERENCE_DIR, else a directory named
 # "reference" beside this repository.
 REFERENCE_DIR = pathlib.Path(os.environ.get("CFD_REFERENCE_DIR", HERE.parent.parent / "reference"))
@@ -95,8 +96,9 @@ def build(force: bool = False) -> None:
         subprocess.run(["gcc", *TIMED_FLAGS, *_host_core_flags(), "-fPIC", "-shared", str(src), "-o",
                         str(TIMED_LIB), "-lm"], check=True)
     ref_dir = REFERENCE_DIR
-    ref_srcs = [HERE / n for n in ("build_ref.sh", "ref_kernels.cpp", "ref_bc.cpp", "ref_shim.h", "bc_ref_shim.h")]
-    stale = not REF_LIB.exists() or REF_LIB.stat().st_mtime < max(p.stat().st_mtime for p in ref_srcs)
+    ref_srcs = [HERE / n for n in ("build_ref.sh", "ref_kernels.cpp", "ref_bc.cpp", "ref_shim.h", "bc_ref_shim.h",
+                                   "ref_metrics.cpp", "metric_ref_shim.h")]
+    stale = not REF_GEOM_LIB.exists() or REF_LIB.stat().st_mtime < max(p.stat().st_mtime for p in ref_srcs)
     if (ref_dir / "Weno.cl").exists() and (force or stale):
         subprocess.run(["bash", str(HERE / "build_ref.sh")], check=True)
 
@@ -104,6 +106,7 @@ def build(force: bool = False) -> None:
 _lib = None
 _timed = None
 _ref = None
+_ref_geom = None
 
 
 def lib():
@@ -142,6 +145,9 @@ def _declare(L):
     L.oracle_set_threads.argtypes = [C.c_int]
     L.oracle_set_poison.argtypes = [C.c_int]
     L.oracle_get_threads.restype = C.c_int
+    L.oracle_compact_metrics.argtypes = [_vp, C.c_int, C.c_double, _vp, _vp]
+    L.oracle_compact_metrics.restype = C.c_int
+    L.oracle_half_point_metrics.argtypes = [_vp, C.c_int, _vp, _vp, _vp]
     return L
 
 
@@ -286,3 +292,40 @@ def ref_stage(a: dict, g_node: int, sd_node: int, params, j: int, dt: float) -> 
     ref_uq(a, g_node + 1, Uj)
     ref_viscous(a, g_node + 1, params, Uj)
     ref_weno(a, sd_node + 1, params.mach, j, dt)
+
+
+# ------------------------------------------------------- geometry producer --
+
+def compact_metrics(grid: np.ndarray, det: np.ndarray, metric: np.ndarray, del_zeta: float = 1.0) -> None:
+    """Node metrics (metric[:, 0:9]) and det by the compact scheme, in place."""
+    if lib().oracle_compact_metrics(_p(grid), int(grid.shape[0]), float(del_zeta), _p(det), _p(metric)) != 0:
+        raise ValueError("table has ID 10 rows or a line shorter than three rows")
+
+
+def half_point_metrics(grid: np.ndarray, n_owned: int, det: np.ndarray, metric: np.ndarray, deter: np.ndarray) -> None:
+    """Face metrics and face dets of rows 1..n_owned, in place."""
+    lib().oracle_half_point_metrics(_p(grid), int(n_owned), _p(det), _p(metric), _p(deter))
+
+
+def ref_geom_available() -> bool:
+    return REF_GEOM_LIB.exists()
+
+
+def ref_geom():
+    global _ref_geom
+    if _ref_geom is None:
+        _ref_geom = C.CDLL(str(REF_GEOM_LIB))
+        _ref_geom.ref_compact_metrics.argtypes = [_vp, C.c_int, _vp, _vp]
+        _ref_geom.ref_half_point_metrics.argtypes = [_vp, C.c_int, C.c_int, _vp, _vp, _vp]
+    return _ref_geom
+
+
+def ref_compact_metrics(grid: np.ndarray, det: np.ndarray, metric: np.ndarray) -> None:
+    """The reference's own metric_term() (node block of metric, det), in place."""
+    ref_geom().ref_compact_metrics(_p(grid), int(grid.shape[0]), _p(det), _p(metric))
+
+
+def ref_half_point_metrics(grid: np.ndarray, n_owned: int, det: np.ndarray, metric: np.ndarray,
+                           deter: np.ndarray) -> None:
+    """The reference's own half-point block of Main.cpp, in place."""
+    ref_geom().ref_half_point_metrics(_p(grid), int(grid.shape[0]), int(n_owned), _p(det), _p(metric), _p(deter))

@@ -19,6 +19,7 @@
 
 #include <math.h>
 #include <stddef.h>
+#include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
 #include <omp.h>
@@ -729,4 +730,187 @@ int oracle_rk3_steps_bc(or_case *c, const or_params *prm, double del_t, int nste
             if (bc && oracle_boundary_fill(c->grid, c->flow, bc, prm->mach, 1, c->sd_node) != 0) return -1;
         }
     return 0;
+}
+
+/* ------------------------------------------------------ geometry producer */
+
+/* neighbour slot s of row r (0 = none) */
+static int nb(const or_grid *g, int r, int s)
+{
+    switch (s) {
+    case 0: return g[r].N0;
+    case 1: return g[r].N1;
+    case 2: return g[r].N2;
+    case 3: return g[r].N3;
+    case 4: return g[r].N4;
+    default: return g[r].N5;
+    }
+}
+
+/* coordinate c (0 x, 1 y, 2 z) of row r */
+static double crd(const or_grid *g, int r, int c) { return c == 0 ? g[r].x : (c == 1 ? g[r].y : g[r].z); }
+
+/* One line of Grid_Transformation.cpp:29-204 (zeta; the eta and xi blocks
+ * are the same with other slots): tridiagonal rows a/d/b and right-hand
+ * sides c[3] along the line from `start` (no + neighbour, slot P) through the
+ * - neighbours (slot Mn), then the reference's elimination from the far end
+ * and substitution from `start`.  J[row*3 + c] receives d x_c / d dir. */
+static int compact_line(const or_grid *g, int start, int P, int Mn, double dz, int n_rows, double *J,
+                        double *a, double *b, double *dd, double *cc, double *dp, double *cp)
+{
+    int i = start, step = 0;
+    while (i != 0) {
+        if (step >= n_rows) return -1;   /* a closed chain: not a line */
+        const int p1 = nb(g, i, P), p2 = nb(g, p1, P), p3 = nb(g, p2, P), p4 = nb(g, p3, P), p5 = nb(g, p4, P);
+        const int m1 = nb(g, i, Mn), m2 = nb(g, m1, Mn), m3 = nb(g, m2, Mn), m4 = nb(g, m3, Mn), m5 = nb(g, m4, Mn);
+        for (int c = 0; c < 3; ++c) {
+            double *rhs = cc + 3 * step + c;
+            if (step > 1) {   /* interior: alpha = 1/3, 7/9 and 1/36 (:46-52) */
+                b[step] = 1.0 / 3.0;
+                dd[step] = 1.0;
+                a[step] = 1.0 / 3.0;
+                *rhs = (1.0 / dz) * ((-1.0 / 36.0) * crd(g, m2, c) - (7.0 / 9.0) * crd(g, m1, c)
+                                     + (7.0 / 9.0) * crd(g, p1, c) + (1.0 / 36.0) * crd(g, p2, c));
+            }
+            if (step == 0 && p1 == 0) {   /* the + end (:55-62) */
+                b[step] = 5.0;
+                dd[step] = 1.0;
+                a[step] = 0.0;
+                *rhs = (1.0 / dz) * ((197.0 / 60.0) * crd(g, i, c) + (5.0 / 12.0) * crd(g, m1, c) - (5.0) * crd(g, m2, c)
+                                     + (5.0 / 3.0) * crd(g, m3, c) - (5.0 / 12.0) * crd(g, m4, c)
+                                     + (1.0 / 20.0) * crd(g, m5, c));
+            }
+            if (step == 1) {   /* next to the + end (:63-70) */
+                b[step] = 2.0 / 11.0;
+                dd[step] = 1.0;
+                a[step] = 2.0 / 11.0;
+                *rhs = (1.0 / dz) * ((20.0 / 33.0) * crd(g, p1, c) + (35.0 / 132.0) * crd(g, i, c)
+                                     - (34.0 / 33.0) * crd(g, m1, c) + (7.0 / 33.0) * crd(g, m2, c)
+                                     - (2.0 / 33.0) * crd(g, m3, c) + (1.0 / 132.0) * crd(g, m4, c));
+            }
+            if (step > 1 && m2 == 0 && m1 != 0) {   /* next to the - end (:72-79) */
+                b[step] = 2.0 / 11.0;
+                dd[step] = 1.0;
+                a[step] = 2.0 / 11.0;
+                *rhs = (1.0 / dz) * (-1.0) * ((20.0 / 33.0) * crd(g, m1, c) + (35.0 / 132.0) * crd(g, i, c)
+                                              - (34.0 / 33.0) * crd(g, p1, c) + (7.0 / 33.0) * crd(g, p2, c)
+                                              - (2.0 / 33.0) * crd(g, p3, c) + (1.0 / 132.0) * crd(g, p4, c));
+            }
+            if (step != 0 && m1 == 0) {   /* the - end (:80-87) */
+                b[step] = 0.0;
+                dd[step] = 1.0;
+                a[step] = 5.0;
+                *rhs = (1.0 / dz) * (-1.0) * ((197.0 / 60.0) * crd(g, i, c) + (5.0 / 12.0) * crd(g, p1, c)
+                                              - (5.0) * crd(g, p2, c) + (5.0 / 3.0) * crd(g, p3, c)
+                                              - (5.0 / 12.0) * crd(g, p4, c) + (1.0 / 20.0) * crd(g, p5, c));
+            }
+        }
+        i = m1;
+        ++step;
+    }
+    const int M = step - 1;
+    if (M < 2) return -1;
+    /* elimination from the far end (:133-152) */
+    dp[M - 1] = dd[M - 1] - ((b[M - 1] * a[M]) / dd[M]);
+    for (int c = 0; c < 3; ++c) cp[3 * (M - 1) + c] = cc[3 * (M - 1) + c] - ((cc[3 * M + c] * b[M - 1]) / dd[M]);
+    for (int s = M - 2; s >= 0; --s) {
+        dp[s] = dd[s] - ((b[s] * a[s + 1]) / dp[s + 1]);
+        for (int c = 0; c < 3; ++c) cp[3 * s + c] = cc[3 * s + c] - ((cp[3 * (s + 1) + c] * b[s]) / dp[s + 1]);
+    }
+    /* substitution from the + end (:154-204) */
+    i = start;
+    step = 0;
+    while (i != 0) {
+        const int prev = nb(g, i, P);
+        for (int c = 0; c < 3; ++c) {
+            double *Jc = J + 3 * (size_t)i + c;
+            if (step > 0 && step < M) *Jc = (cp[3 * step + c] - a[step] * J[3 * (size_t)prev + c]) / dp[step];
+            if (step == 0) *Jc = cp[c] / dp[0];
+            if (step == M) *Jc = (cc[3 * step + c] - a[M] * J[3 * (size_t)prev + c]) / dd[M];
+        }
+        i = nb(g, i, Mn);
+        ++step;
+    }
+    return 0;
+}
+
+int oracle_compact_metrics(const or_grid *g, int n_rows, double dz, double *det, or_metric *metric)
+{
+    for (int r = 1; r < n_rows; ++r)
+        if (g[r].ID == 10) return -1;
+    /* J[d][row][c] = d x_c / d dir_d, zero where no line passes */
+    double *J = (double *)calloc((size_t)3 * 3 * n_rows, sizeof(double));
+    double *w = (double *)malloc((size_t)14 * n_rows * sizeof(double));
+    if (!J || !w) {
+        free(J);
+        free(w);
+        return -1;
+    }
+    double *a = w, *b = w + n_rows, *dd = w + 2 * n_rows, *dp = w + 3 * n_rows, *cc = w + 4 * n_rows,
+           *cp = w + 7 * n_rows;
+    /* zeta: + is N1, - is N3 (:29-36); eta: N0 / N2 (:213-218); xi: N4 / N5
+     * with the reference's loc condition (:328-334) */
+    static const int P[3] = {1, 0, 4}, Mn[3] = {3, 2, 5};
+    int rc = 0;
+    for (int r = 1; r < n_rows && rc == 0; ++r)
+        for (int d = 0; d < 3 && rc == 0; ++d) {
+            if (nb(g, r, P[d]) != 0) continue;
+            const int loc = g[r].loc;
+            if (d == 2 && !(loc == 30 || loc == 31 || loc <= 27 || loc == 28)) continue;
+            rc = compact_line(g, r, P[d], Mn[d], dz, n_rows, J + (size_t)3 * n_rows * d, a, b, dd, cc, dp, cp);
+        }
+    if (rc == 0) {
+        const double *Jz = J, *Je = J + 3 * (size_t)n_rows, *Jx = J + 6 * (size_t)n_rows;
+        for (int r = 1; r < n_rows; ++r) {
+            const double x_zeta = Jz[3 * r], y_zeta = Jz[3 * r + 1], z_zeta = Jz[3 * r + 2];
+            const double x_eta = Je[3 * r], y_eta = Je[3 * r + 1], z_eta = Je[3 * r + 2];
+            const double x_xi = Jx[3 * r], y_xi = Jx[3 * r + 1], z_xi = Jx[3 * r + 2];
+            /* :447 and :1029-1037 */
+            const double D = (((x_zeta) * ((y_eta * z_xi) - (y_xi * z_eta))) + ((x_eta) * ((y_xi * z_zeta) - (y_zeta * z_xi)))
+                              + ((x_xi) * ((y_zeta * z_eta) - (y_eta * z_zeta))));
+            double *m = metric[r].m;
+            det[r] = D;
+            m[0] = (1.0 / D) * (y_eta * z_xi - y_xi * z_eta);
+            m[1] = (1.0 / D) * (z_eta * x_xi - z_xi * x_eta);
+            m[2] = (1.0 / D) * (x_eta * y_xi - x_xi * y_eta);
+            m[3] = (1.0 / D) * (y_xi * z_zeta - y_zeta * z_xi);
+            m[4] = (1.0 / D) * (z_xi * x_zeta - z_zeta * x_xi);
+            m[5] = (1.0 / D) * (x_xi * y_zeta - x_zeta * y_xi);
+            m[6] = (1.0 / D) * (y_zeta * z_eta - y_eta * z_zeta);
+            m[7] = (1.0 / D) * (z_zeta * x_eta - z_eta * x_zeta);
+            m[8] = (1.0 / D) * (x_zeta * y_eta - x_eta * y_zeta);
+        }
+    }
+    free(J);
+    free(w);
+    return rc;
+}
+
+/* (3 f0 - 25 f1 + 150 f2 + 150 f3 - 25 f4 + 3 f5) / 256 in the reference's order */
+static double six_point(double f0, double f1, double f2, double f3, double f4, double f5)
+{
+    return (1.0 / 256.0) * (3.0 * (f0) - 25.0 * (f1) + 150.0 * (f2) + 150.0 * (f3) - 25.0 * (f4) + 3.0 * (f5));
+}
+
+void oracle_half_point_metrics(const or_grid *g, int n_owned, const double *det, or_metric *metric,
+                               or_determ *deter)
+{
+    /* direction d: + slot, - slot; the + face block 1 + 2d, the - face 2 + 2d */
+    static const int P[3] = {1, 0, 4}, Mn[3] = {3, 2, 5};
+    for (int r = 1; r <= n_owned; ++r) {
+        double *fd = &deter[r].ip;
+        for (int d = 0; d < 3; ++d) {
+            const int m1 = nb(g, r, Mn[d]), m2 = nb(g, m1, Mn[d]), m3 = nb(g, m2, Mn[d]);
+            const int p1 = nb(g, r, P[d]), p2 = nb(g, p1, P[d]), p3 = nb(g, p2, P[d]);
+            double *plus = metric[r].m + 9 * (1 + 2 * d), *minus = metric[r].m + 9 * (2 + 2 * d);
+            for (int c = 0; c < 9; ++c) {
+                plus[c] = six_point(metric[m2].m[c], metric[m1].m[c], metric[r].m[c], metric[p1].m[c],
+                                    metric[p2].m[c], metric[p3].m[c]);
+                minus[c] = six_point(metric[m3].m[c], metric[m2].m[c], metric[m1].m[c], metric[r].m[c],
+                                     metric[p1].m[c], metric[p2].m[c]);
+            }
+            fd[2 * d] = six_point(det[m2], det[m1], det[r], det[p1], det[p2], det[p3]);
+            fd[2 * d + 1] = six_point(det[m3], det[m2], det[m1], det[r], det[p1], det[p2]);
+        }
+    }
 }

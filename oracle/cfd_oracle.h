@@ -12,6 +12,8 @@
  *   Weno.cl      -> oracle_weno      (characteristic WENO5 + LLF + RK stage)
  *   Solver.cpp:365-658 -> oracle_rk3_step (U_Q, Viscous, Weno per stage)
  *   Flow_Initialisation.cpp:23-1394 -> oracle_boundary_fill (ghost fill)
+ *   Grid_Transformation.cpp:22-1045 -> oracle_compact_metrics (node metrics)
+ *   Main.cpp:2369-2440 -> oracle_half_point_metrics (face metrics, face dets)
  * The structs below are the reference's packed ABI (functions.h:49-113).
  *
  * Parity pin: the restatement is checked against the reference's own kernel
@@ -106,6 +108,22 @@ int oracle_boundary_fill(const or_grid *grid, or_flow *flow, const or_bc_lists *
 /* oracle_rk3_steps with the boundary routine after every stage
  * (Solver.cpp:364-658).  bc may be NULL.  Returns -1 as above. */
 int oracle_rk3_steps_bc(or_case *c, const or_params *prm, double del_t, int nsteps, const or_bc_lists *bc);
+
+/* Node Jacobians by the sixth-order compact scheme along every line of
+ * the node table, det and the node metrics as cofactors / det
+ * (Grid_Transformation.cpp:22-1045, metric_term()).  A line starts at a row
+ * with no neighbour in the + direction (zeta: N1, eta: N0, xi: N4, subject
+ * to the reference's start conditions) and walks the - neighbours to the
+ * row that has none; rows 1..n_rows-1.  Writes det[] and the node block
+ * (columns 0..8) of metric[].  Returns -1 (writing nothing) when a row has
+ * ID 10 (the reference's C-grid wake-cut branches) or a line is shorter
+ * than three rows. */
+int oracle_compact_metrics(const or_grid *grid, int n_rows, double del_zeta, double *det, or_metric *metric);
+
+/* Face metrics and face dets of rows 1..n_owned by the six-point midpoint
+ * rule (3, -25, 150, 150, -25, 3)/256 of node values (Main.cpp:2369-2440). */
+void oracle_half_point_metrics(const or_grid *grid, int n_owned, const double *det, or_metric *metric,
+                               or_determ *deter);
 
 /* Undefined-branch poisoning (NaN) for masking checks; off by default. */
 void oracle_set_poison(int on);
