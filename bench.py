@@ -360,6 +360,7 @@ def gpu_arm(args):
                 "rel_l2_vs_fp64": rel_l2(um[1:], u64[1:]), "steps_compared": args.warmup + args.steps + 1,
                 "dtype": FORM_DTYPES[prec], "gpu_launches": launchesm, "clocks": clocks_m,
                 "step_algorithmic_hbm_frac": ALGO_BYTES_PER_CELL_UPDATE * vm / world / 1e9 / hbm_peak,
+                "face_tiles_tuned": list(sm.info().face_tiles),
                 "kernels_ms_per_stage": _kernel_table(prof_m)}
             sm.close()
 
@@ -524,8 +525,8 @@ def bench_batched(ctx, torch, stream, args):
         secs = timed(b, steps)
         info = b.info()
         out[key] = {"value": nodes * steps / secs, "unit": UNIT, "ms_per_step": 1e3 * secs / steps, "steps": steps,
-                    "dtype": FORM_DTYPES[prec], "tile_nodes": info.tile_nodes, "blocks": info.blocks,
-                    "cuda_graph": info.graph, "device_gb": info.device_bytes / 1e9}
+                    "dtype": FORM_DTYPES[prec], "tile_nodes": info.tile_nodes, "face_tiles": info.face_tiles,
+                    "blocks": info.blocks, "cuda_graph": info.graph, "device_gb": info.device_bytes / 1e9}
         if prec == FP64:
             u_ref = [b.get_u0(s)[1:] for s in slots]
         b.close()

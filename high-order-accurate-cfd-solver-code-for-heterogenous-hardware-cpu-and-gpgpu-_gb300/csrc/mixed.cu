@@ -69,32 +69,42 @@ __global__ void __launch_bounds__(256) k_mu_m(LatView g, int q)
 #endif
 
 // Faces per tile along D (a block of 128 threads covers kTile x 128/kTile
-// faces; face_tile.cuh).  TGV 128^3: i tiles of 16 / 32 / 64 / 128 took
-// 0.097 / 0.093 / 0.091 / 0.090 ms, j/k tiles of 4 / 8 / 16 / 32 took 0.098
-// / 0.094 / 0.092 / 0.102-0.146 ms; 64 keeps small lattices' i lines from
-// idling most of a block.
-#ifndef CFD_MFACE_TILE_I
-#define CFD_MFACE_TILE_I 64
-#endif
-#ifndef CFD_MFACE_TILE_JK
-#define CFD_MFACE_TILE_JK 16
-#endif
+// faces; face_tile.cuh), StructuredLaunch::tile_i / tile_jk.  TGV 128^3: i
+// tiles of 16 / 32 / 64 / 128 took 0.097 / 0.093 / 0.091 / 0.090 ms, j/k
+// tiles of 4 / 8 / 16 / 32 took 0.098 / 0.094 / 0.092 / 0.102-0.146 ms; the
+// defaults 64 and 16 keep small lattices' i lines from idling most of a
+// block, and the solver's tuner picks per lattice.
 
-template <int D>
-using MTile = FaceTile<D, D == 0 ? CFD_MFACE_TILE_I : CFD_MFACE_TILE_JK>;
-
-template <int D>
+// One instance per candidate tile width (face_tile.cuh): faces along i of
+// 32, 64 or 128, along j or k of 8, 16 or 32; the solver times them when it
+// is created and keeps the fastest per direction (the same arithmetic,
+// only the staging differs).
+template <int D, int TILE>
 __global__ void __launch_bounds__(kFaceThreads, CFD_MFACE_MIN_BLOCKS) k_face_tile_m(LatView g)
 {
-    using T = MTile<D>;
+    using T = FaceTile<D, TILE>;
     __shared__ float smem[tile_smem_floats<T>()];
     mx::face_tile<T, D>(g, tile_of_block<T>(), smem);
 }
 
-template <int D>
-void launch_face_tile(const LatView &g, cudaStream_t st)
+template <int D, int TILE>
+void launch_tile_m(const LatView &g, cudaStream_t st)
 {
-    k_face_tile_m<D><<<MTile<D>::grid(g), kFaceThreads, 0, st>>>(g);
+    k_face_tile_m<D, TILE><<<FaceTile<D, TILE>::grid(g), kFaceThreads, 0, st>>>(g);
+}
+
+template <int D>
+void launch_face_tile(const LatView &g, cudaStream_t st, int tile)
+{
+    if constexpr (D == 0) {
+        if (tile == 32) launch_tile_m<0, 32>(g, st);
+        else if (tile == 128) launch_tile_m<0, 128>(g, st);
+        else launch_tile_m<0, 64>(g, st);
+    } else {
+        if (tile == 8) launch_tile_m<D, 8>(g, st);
+        else if (tile == 32) launch_tile_m<D, 32>(g, st);
+        else launch_tile_m<D, 16>(g, st);
+    }
 }
 
 template <bool LOC>
@@ -250,13 +260,13 @@ int mixed_stage(const StructuredLaunch &S, int jst, double dt, double *Lout, cud
         cudaStreamWaitEvent(sj, S.fork, 0);
         cudaStreamWaitEvent(sk, S.fork, 0);
     }
-    launch_face_tile<0>(g, st);
+    launch_face_tile<0>(g, st, S.tile_i);
     name("face_i");
     mark();
-    launch_face_tile<1>(g, sj);
+    launch_face_tile<1>(g, sj, S.tile_jk);
     name("face_j");
     mark();
-    launch_face_tile<2>(g, sk);
+    launch_face_tile<2>(g, sk, S.tile_jk);
     name("face_k");
     mark();
     if (fside) {
@@ -273,6 +283,39 @@ int mixed_stage(const StructuredLaunch &S, int jst, double dt, double *Lout, cud
     name("update+prep");
     mark();
     return k;
+}
+
+void mixed_face_pass(const StructuredLaunch &S, int d, int tile, cudaStream_t st)
+{
+    const LatView g = make_view(S, 0.0, nullptr);
+    if (d == 0) launch_face_tile<0>(g, st, tile);
+    else if (d == 1) launch_face_tile<1>(g, st, tile);
+    else launch_face_tile<2>(g, st, tile);
+}
+
+namespace {
+
+// rho = 1, zero velocity, p = 1: the FP32 face inputs of a uniform state
+__global__ void k_uniform_inputs(float *Q32, float *R32, float *FEG32, long long N)
+{
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    const float q[5] = {1.0f, 0.0f, 0.0f, 0.0f, 2.5f}, r[5] = {0.0f, 0.0f, 0.0f, 1.0f, 3.5f};
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+        Q32[c * N + n] = q[c];
+        R32[c * N + n] = r[c];
+    }
+#pragma unroll
+    for (int c = 0; c < 15; ++c) FEG32[c * N + n] = 0.0f;
+}
+
+}  // namespace
+
+void reduced_uniform_inputs(const StructuredLaunch &S, cudaStream_t st)
+{
+    const long long N = (long long)S.ni * S.nj * S.nk;
+    k_uniform_inputs<<<blocks_for(N, 256), 256, 0, st>>>(S.Q32, S.R32, S.FEG32, N);
 }
 
 }  // namespace cfd

@@ -14,8 +14,11 @@
 // With cfd_solver_set_boundary the reference's boundary routine
 // (Flow_Initialisation.cpp, boundary.cu) runs after every stage, as the host
 // loop calls it (Solver.cpp:658).
+#include <array>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <vector>
 
 #include "boundary.h"
@@ -107,6 +110,8 @@ cfd_status_t create_gather(cfd_solver *s, const cfd_geometry_t *g)
     if (e != cudaSuccess) return cuda_fail(s->ctx, e, "solver create sync");
     return CFD_OK;
 }
+
+cfd_status_t tune_face_tiles(cfd_solver *s);
 
 cfd_status_t create_structured(cfd_solver *s, const cfd_geometry_t *g)
 {
@@ -225,6 +230,70 @@ cfd_status_t create_structured(cfd_solver *s, const cfd_geometry_t *g)
     }
     cudaError_t e = cudaStreamSynchronize(S.stream);   // host vectors go out of scope
     if (e != cudaSuccess) return cuda_fail(s->ctx, e, "solver create sync");
+    if (s->mixed) return tune_face_tiles(s);
+    return CFD_OK;
+}
+
+// Face-tile widths of the mixed and split face passes, timed once per form
+// and lattice shape in this process (candidates: 32, 64, 128 faces along i;
+// 8, 16, 32 along j and k, which share one width).  The passes run on a
+// uniform state in the FP32 face inputs, which the first stage overwrites;
+// every width evaluates the same arithmetic, so the choice changes no
+// result.
+std::mutex g_tile_mutex;
+std::map<std::array<int, 7>, std::pair<int, int>> g_tile_cache;
+
+cfd_status_t tune_face_tiles(cfd_solver *s)
+{
+    StructuredLaunch &S = s->S;
+    const std::array<int, 7> key = {s->form, S.ni, S.nj, S.nk, S.per, S.loc8 ? 1 : 0, s->ctx->device};
+    {
+        std::lock_guard<std::mutex> lock(g_tile_mutex);
+        auto it = g_tile_cache.find(key);
+        if (it != g_tile_cache.end()) {
+            S.tile_i = it->second.first;
+            S.tile_jk = it->second.second;
+            return CFD_OK;
+        }
+    }
+    cudaStream_t st = s->ctx->stream;
+    auto pass = [&](int d, int tile) {
+        if (s->form == CFD_PREC_SPLIT) split_face_pass(S, d, tile, st);
+        else mixed_face_pass(S, d, tile, st);
+    };
+    reduced_uniform_inputs(S, st);
+    cudaEvent_t t0, t1;
+    if (cudaEventCreate(&t0) != cudaSuccess || cudaEventCreate(&t1) != cudaSuccess)
+        return cuda_fail(s->ctx, cudaGetLastError(), "face-tile tuner events");
+    auto time_ms = [&](std::initializer_list<int> dirs, int tile) {
+        for (int d : dirs) pass(d, tile);   // warm-up
+        cudaEventRecord(t0, st);
+        for (int r = 0; r < 3; ++r)
+            for (int d : dirs) pass(d, tile);
+        cudaEventRecord(t1, st);
+        float ms = 1e30f;
+        if (cudaEventSynchronize(t1) == cudaSuccess) cudaEventElapsedTime(&ms, t0, t1);
+        s->ctx->launches += 4 * dirs.size();
+        return ms;
+    };
+    float best_i = 1e30f, best_jk = 1e30f;
+    int ti = S.tile_i, tjk = S.tile_jk;
+    for (int c : {32, 64, 128}) {
+        const float ms = time_ms({0}, c);
+        if (ms < best_i) best_i = ms, ti = c;
+    }
+    for (int c : {8, 16, 32}) {
+        const float ms = time_ms({1, 2}, c);
+        if (ms < best_jk) best_jk = ms, tjk = c;
+    }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(s->ctx, e, "face-tile tuner");
+    S.tile_i = ti;
+    S.tile_jk = tjk;
+    std::lock_guard<std::mutex> lock(g_tile_mutex);
+    g_tile_cache[key] = {ti, tjk};
     return CFD_OK;
 }
 
@@ -400,6 +469,23 @@ cfd_status_t cfd_solver_info(const cfd_solver_t *s, cfd_solver_info_t *info)
     info->nk = s->nk;
     info->precision = s->form;
     info->device_bytes = s->bytes;
+    info->face_tile_i = s->mixed && s->path == CFD_PATH_STRUCTURED ? s->S.tile_i : 0;
+    info->face_tile_jk = s->mixed && s->path == CFD_PATH_STRUCTURED ? s->S.tile_jk : 0;
+    return CFD_OK;
+}
+
+cfd_status_t cfd_solver_set_face_tiles(cfd_solver_t *s, int32_t tile_i, int32_t tile_jk)
+{
+    if (!s) return CFD_EINVAL;
+    if (!(s->mixed && s->path == CFD_PATH_STRUCTURED)) return fail(s->ctx, CFD_EUNSUPPORTED, "face tiles: mixed or split lattice only");
+    if ((tile_i != 0 && tile_i != 32 && tile_i != 64 && tile_i != 128)
+        || (tile_jk != 0 && tile_jk != 8 && tile_jk != 16 && tile_jk != 32))
+        return fail(s->ctx, CFD_EINVAL, "face tiles: tile_i in {32, 64, 128}, tile_jk in {8, 16, 32}");
+    cfd_status_t st = use_device(s->ctx);
+    if (st != CFD_OK) return st;
+    cudaStreamSynchronize(s->ctx->stream);
+    if (tile_i) s->S.tile_i = tile_i;
+    if (tile_jk) s->S.tile_jk = tile_jk;
     return CFD_OK;
 }
 

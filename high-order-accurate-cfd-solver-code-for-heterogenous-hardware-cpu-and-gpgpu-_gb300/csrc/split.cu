@@ -60,28 +60,36 @@ __global__ void __launch_bounds__(256) k_mu_s(LatView g)
 #ifndef CFD_SFACE_MIN_BLOCKS
 #define CFD_SFACE_MIN_BLOCKS 6
 #endif
-#ifndef CFD_SFACE_TILE_I
-#define CFD_SFACE_TILE_I 64
-#endif
-#ifndef CFD_SFACE_TILE_JK
-#define CFD_SFACE_TILE_JK 16
-#endif
-
-template <int D>
-using STile = FaceTile<D, D == 0 ? CFD_SFACE_TILE_I : CFD_SFACE_TILE_JK>;
-
-template <int D>
+// One instance per candidate tile width (face_tile.cuh): faces along i of
+// 32, 64 or 128, along j or k of 8, 16 or 32; the solver times them when it
+// is created and keeps the fastest per direction (the same arithmetic,
+// only the staging differs).
+template <int D, int TILE>
 __global__ void __launch_bounds__(kFaceThreads, CFD_SFACE_MIN_BLOCKS) k_face_tile_s(LatView g)
 {
-    using T = STile<D>;
+    using T = FaceTile<D, TILE>;
     __shared__ float smem[tile_smem_floats<T>()];
     sp::face_tile<T, D>(g, tile_of_block<T>(), smem);
 }
 
-template <int D>
-void launch_face_tile_s(const LatView &g, cudaStream_t st)
+template <int D, int TILE>
+void launch_tile_s(const LatView &g, cudaStream_t st)
 {
-    k_face_tile_s<D><<<STile<D>::grid(g), kFaceThreads, 0, st>>>(g);
+    k_face_tile_s<D, TILE><<<FaceTile<D, TILE>::grid(g), kFaceThreads, 0, st>>>(g);
+}
+
+template <int D>
+void launch_face_tile_s(const LatView &g, cudaStream_t st, int tile)
+{
+    if constexpr (D == 0) {
+        if (tile == 32) launch_tile_s<0, 32>(g, st);
+        else if (tile == 128) launch_tile_s<0, 128>(g, st);
+        else launch_tile_s<0, 64>(g, st);
+    } else {
+        if (tile == 8) launch_tile_s<D, 8>(g, st);
+        else if (tile == 32) launch_tile_s<D, 32>(g, st);
+        else launch_tile_s<D, 16>(g, st);
+    }
 }
 
 template <bool LOC>
@@ -215,13 +223,13 @@ int split_stage(const StructuredLaunch &S, int jst, double dt, double *Lout, cud
         cudaStreamWaitEvent(sj, S.fork, 0);
         cudaStreamWaitEvent(sk, S.fork, 0);
     }
-    launch_face_tile_s<0>(g, st);
+    launch_face_tile_s<0>(g, st, S.tile_i);
     name("face_i");
     mark();
-    launch_face_tile_s<1>(g, sj);
+    launch_face_tile_s<1>(g, sj, S.tile_jk);
     name("face_j");
     mark();
-    launch_face_tile_s<2>(g, sk);
+    launch_face_tile_s<2>(g, sk, S.tile_jk);
     name("face_k");
     mark();
     if (fside) {
@@ -238,6 +246,14 @@ int split_stage(const StructuredLaunch &S, int jst, double dt, double *Lout, cud
     name("update+prep");
     mark();
     return k;
+}
+
+void split_face_pass(const StructuredLaunch &S, int d, int tile, cudaStream_t st)
+{
+    const LatView g = make_view(S, 0.0, nullptr);
+    if (d == 0) launch_face_tile_s<0>(g, st, tile);
+    else if (d == 1) launch_face_tile_s<1>(g, st, tile);
+    else launch_face_tile_s<2>(g, st, tile);
 }
 
 }  // namespace cfd

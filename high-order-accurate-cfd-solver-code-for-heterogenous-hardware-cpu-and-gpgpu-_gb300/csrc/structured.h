@@ -47,6 +47,9 @@ struct StructuredLaunch {
     cudaEvent_t face_join[2] = {nullptr, nullptr};
     // lattice shape beyond a plain periodic box (LatView::per, loc8, locdirs,
     // row_of)
+    // face-tile widths of the mixed and split face passes: faces along i
+    // (32, 64 or 128) and along j and k (8, 16 or 32) per block of 128
+    int tile_i = 64, tile_jk = 16;
     int per = 7;
     const unsigned char *loc8 = nullptr;
     int locdirs = 0;
@@ -144,6 +147,13 @@ inline LatView make_view(const StructuredLaunch &S, double dt, double *Lout)
 constexpr int kMaxStageLaunches = 6;
 int structured_stage(const StructuredLaunch &S, int j, double dt, double *Lout, cudaEvent_t *ev = nullptr,
                      const char **names = nullptr, int prep_from = kPrepFromFlow);
+
+// One face pass along d with face tiles of width `tile` (the tuner's
+// candidates, mixed.cu / split.cu), and a uniform state in the FP32 face
+// inputs (Q32, R32, FEG32) for timing them before any state exists.
+void mixed_face_pass(const StructuredLaunch &S, int d, int tile, cudaStream_t st);
+void split_face_pass(const StructuredLaunch &S, int d, int tile, cudaStream_t st);
+void reduced_uniform_inputs(const StructuredLaunch &S, cudaStream_t st);
 
 // AoS reference rows <-> SoA [comp][N]; node n is row row_of[n] (row n + 1
 // when row_of is null).

@@ -195,6 +195,7 @@ class SolverInfo:
     shape: tuple
     precision: str
     device_bytes: int
+    face_tiles: tuple = (0, 0)     # (along i, along j and k); mixed/split lattices
 
 
 class Boundary:
@@ -277,7 +278,12 @@ class Solver:
         i = abi.SolverInfo()
         self.ctx.check(self.lib.cfd_solver_info(self.h, C.byref(i)), "cfd_solver_info")
         return SolverInfo("structured" if i.path == abi.PATH_STRUCTURED else "gather", (i.ni, i.nj, i.nk),
-                          abi.PREC_NAMES[i.precision], int(i.device_bytes))
+                          abi.PREC_NAMES[i.precision], int(i.device_bytes), (int(i.face_tile_i), int(i.face_tile_jk)))
+
+    def set_face_tiles(self, tile_i: int = 0, tile_jk: int = 0):
+        """Fix the face-tile widths of a mixed or split lattice solver."""
+        self.ctx.check(self.lib.cfd_solver_set_face_tiles(self.h, int(tile_i), int(tile_jk)),
+                       "cfd_solver_set_face_tiles")
 
     def set_flow(self, flow: np.ndarray):
         assert flow.shape == (self.g_node + 1, L.NFLOW) and flow.dtype == np.float64

@@ -251,6 +251,8 @@ typedef struct {
     int32_t precision;         /* cfd_precision_t                            */
     int32_t reserved;
     uint64_t device_bytes;     /* device memory held by the solver           */
+    int32_t face_tile_i;       /* mixed/split lattice: faces per tile along i */
+    int32_t face_tile_jk;      /*   and along j and k (0 otherwise)          */
 } cfd_solver_info_t;
 
 typedef struct cfd_solver cfd_solver_t;
@@ -266,6 +268,13 @@ cfd_status_t cfd_solver_create(cfd_ctx_t *ctx, const cfd_geometry_t *geom, const
                                int32_t force_path, cfd_solver_t **solver);
 cfd_status_t cfd_solver_destroy(cfd_solver_t *s);
 cfd_status_t cfd_solver_info(const cfd_solver_t *s, cfd_solver_info_t *info);
+/* Face-tile widths of the mixed and split face passes (blocks of 128
+ * threads staging their stencil lines in shared memory): tile_i faces along
+ * i (32, 64 or 128) and tile_jk along j and k (8, 16 or 32); 0 keeps a
+ * width.  cfd_solver_create times every width once per form and lattice
+ * shape in the process and keeps the fastest; the widths change no result
+ * bit.  CFD_EUNSUPPORTED for FP64 or gather-path solvers. */
+cfd_status_t cfd_solver_set_face_tiles(cfd_solver_t *s, int32_t tile_i, int32_t tile_jk);
 /* State in/out as FLOW rows 0..g_node (host pointers). */
 cfd_status_t cfd_solver_set_flow(cfd_solver_t *s, const cfd_flow_t *flow_host);
 cfd_status_t cfd_solver_get_flow(cfd_solver_t *s, cfd_flow_t *flow_host);
