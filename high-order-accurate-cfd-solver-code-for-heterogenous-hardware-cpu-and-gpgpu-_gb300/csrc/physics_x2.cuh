@@ -160,12 +160,16 @@ __device__ __forceinline__ void llf_face_flux2(const float2 P[3][5], float mx, f
 // split form): the face states (q+, q-) reconstructed as deviations from
 // the face's left node (reconstruct_face2<true>), their velocities and
 // pressures, lambda_5 and the dissipation alpha (q+ - q-) in FP32; the
-// contravariant velocity U_n = m . u with the FP64 face metric (dm), the
-// central sum of the contravariant fluxes q U_n + m p and (E + p) U_n of
-// both states, and its product by det_f / 2 in FP64 (Weno.cl:2585-2728,
-// 2913-2947).  m (FP32) is the same face metric rounded, for the
-// eigenvectors and lambda_5.  extra[c] (FP32) is added to component c
-// together with the FP32 dissipation term, in one FP64 operation.
+// contravariant fluxes' metric products and their product by det_f / 2 in
+// FP64 (Weno.cl:2585-2728, 2913-2947).  The central sum of the two states'
+// fluxes q U_n + m p (and (E + p) U_n) is taken as
+//   q+ U+ + q- U- = (q+ + q-) (U+ + U-) / 2 + (q+ - q-) (U+ - U-) / 2:
+// the first term, which carries the metric, in FP64 with U+ + U- = m.(u+ +
+// u-) from the FP64 face metric dm; the second, a product of two
+// differences across the face, in FP32 with the dissipation.  A uniform
+// stencil (q+ = q-) gives exactly the FP64 flux of that state.  m (FP32) is
+// the face metric rounded, for the eigenvectors and lambda_5.  extra[c]
+// (FP32) is added to component c with the other FP32 terms.
 __device__ __forceinline__ void llf_face_flux2_split(const float2 P[3][5], float mx, float my, float mz,
                                                      const double dm[3], double det_f, const float roe[5], float eps,
                                                      const float extra[5], double Fhat[5])
@@ -183,23 +187,26 @@ __device__ __forceinline__ void llf_face_flux2_split(const float2 P[3][5], float
     const float2 c2k = mul2(b2(1.4f * 0.4f * (mx * mx + my * my + mz * mz)), e);
     const float2 lam = add2(un32, make_float2(sqrtf(c2k.x), sqrtf(c2k.y)));
     const float alpha = fmaxf(fabsf(lam.x), fabsf(lam.y));
-    // FP32 terms of each component: the extra term less the dissipation
     const double hd = 0.5 * det_f;
     const float hd32 = (float)hd;
-    float x[5];
+    // FP32 terms: extra, less the dissipation, plus the difference term
+    // (q+ - q-) (U+ - U-) / 2, all times det_f / 2 where they belong
+    const float dun = un32.x - un32.y;
+    float qs[5], x[5];
 #pragma unroll
-    for (int c = 0; c < 5; ++c) x[c] = fmaf(-hd32 * alpha, q[c].x - q[c].y, extra[c]);
-    // FP64 central sum of the contravariant fluxes of both states
-    const double unp = fma(dm[0], (double)u.x, fma(dm[1], (double)v.x, dm[2] * (double)w.x));
-    const double unn = fma(dm[0], (double)u.y, fma(dm[1], (double)v.y, dm[2] * (double)w.y));
-    const double ps = (double)(pr.x + pr.y);
-    double t[5];
-    t[0] = fma((double)q[0].x, unp, (double)q[0].y * unn);
+    for (int c = 0; c < 5; ++c) {
+        const float qp = c == 4 ? q[4].x + pr.x : q[c].x, qn = c == 4 ? q[4].y + pr.y : q[c].y;
+        qs[c] = qp + qn;
+        x[c] = fmaf(hd32, fmaf(0.5f * (qp - qn), dun, -alpha * (q[c].x - q[c].y)), extra[c]);
+    }
+    // FP64: the metric products of the sum term and of the pressure
+    const double hsun = hd * (0.5 * fma(dm[0], (double)(u.x + u.y), fma(dm[1], (double)(v.x + v.y),
+                                                                         dm[2] * (double)(w.x + w.y))));
+    const double hps = hd * (double)(pr.x + pr.y);
+    Fhat[0] = fma((double)qs[0], hsun, (double)x[0]);
 #pragma unroll
-    for (int c = 1; c < 4; ++c) t[c] = fma(dm[c - 1], ps, fma((double)q[c].x, unp, (double)q[c].y * unn));
-    t[4] = fma((double)(q[4].x + pr.x), unp, (double)(q[4].y + pr.y) * unn);
-#pragma unroll
-    for (int c = 0; c < 5; ++c) Fhat[c] = fma(hd, t[c], (double)x[c]);
+    for (int c = 1; c < 4; ++c) Fhat[c] = fma(dm[c - 1], hps, fma((double)qs[c], hsun, (double)x[c]));
+    Fhat[4] = fma((double)qs[4], hsun, (double)x[4]);
 }
 
 // Sixth-order correction of a face flux from the node fluxes f[0..5]
