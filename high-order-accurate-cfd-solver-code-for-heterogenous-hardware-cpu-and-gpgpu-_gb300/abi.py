@@ -92,6 +92,7 @@ PROTOTYPES = {
     "cfd_solver_profile_stage": (C.c_int, [_vp, _i32, _d, _vp, _i32, C.POINTER(_i32)]),
     "cfd_probe_flops": (C.c_int, [_vp, _i32, C.POINTER(_d)]),
     "cfd_bc_create": (C.c_int, [_vp, _vp, _i32] + [_vp, _i32] * 4 + [C.POINTER(_vp)]),
+    "cfd_bc_create_singular": (C.c_int, [_vp, _vp, _i32] + [_vp, _i32] * 4 + [_vp, _vp, _i32, C.POINTER(_vp)]),
     "cfd_bc_destroy": (C.c_int, [_vp]),
     "cfd_boundary_fill": (C.c_int, [_vp, _vp, _vp, _d, _i32, _i32]),
     "cfd_rk3_step": (C.c_int, [_vp, _d, _d] + [_vp] * 16 + [_i32, _i32, C.POINTER(Params), _vp, _i32]),

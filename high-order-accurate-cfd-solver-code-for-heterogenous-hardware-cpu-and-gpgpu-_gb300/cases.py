@@ -56,15 +56,27 @@ class Params:
 class BoundaryLists:
     """Node lists of the reference's boundary routine intialise()
     (Flow_Initialisation.cpp:23-1394): row indices, visited in order,
-    outlet, then inlet, boundary (mirror copy) and wall (no-slip)."""
+    outlet, then inlet, boundary (mirror copy) and wall (no-slip).
+
+    ``singular`` (rows x 6, int32) is the reference's singular-node table of
+    a wake cut (functions.h ``singul``, filled in Main.cpp:1612-1700): the
+    neighbours across the cut that the wall rules of ID 10 and codes 29/30,
+    33..52 read.  ``tips`` are the trailing-edge rows the solver fixes after
+    the routine (Solver.cpp:660-683)."""
     outlet: np.ndarray
     inlet: np.ndarray
     boundary: np.ndarray
     wall: np.ndarray
+    singular: np.ndarray | None = None
+    tips: np.ndarray | None = None
 
     def __post_init__(self):
         for k in ("outlet", "inlet", "boundary", "wall"):
             setattr(self, k, np.ascontiguousarray(getattr(self, k), dtype=np.int32))
+        if self.singular is not None:
+            self.singular = np.ascontiguousarray(self.singular, dtype=np.int32).reshape(-1, 6)
+        if self.tips is not None:
+            self.tips = np.ascontiguousarray(self.tips, dtype=np.int32)
 
 
 @dataclasses.dataclass
@@ -564,6 +576,60 @@ def ghost_box(shape=(10, 9, 8), seed=0, mach=1.5, amp=0.05, bc: bool = False) ->
         # ID 10 marks the reference's singular wall nodes; the box has none
         a["grid"]["ID"][:] = 0
         c.bc = box_boundary_lists(a["grid"]["loc"], n_owned)
+    return c
+
+
+# Codes of the reference's singular wall branches: 29/30 (a node beyond
+# the cut), 33..52 (the multi-pass corner codes; Flow_Initialisation.cpp
+# :1276-1392).  53..56 are left out: the routine never sets their slots.
+SINGULAR_CODES = (29, 30) + tuple(range(33, 53))
+
+
+def with_singular_nodes(c: Case, seed: int = 0, n_tips: int = 4, face_code: int | None = None) -> Case:
+    """Relabels wall nodes of ``c`` (a case with boundary lists) as the
+    reference's singular wall nodes, in place: rows of one wall face code
+    (the most common one unless given) take every singular code of the
+    routine, some with ID 10 (over the face code and over codes 33..52),
+    plus a wall edge or corner with ID 10 where the case has one; a
+    singular-node table whose slots name seeded owned rows (in a C-grid they
+    are the nodes across the wake cut; here any owned row exercises the same
+    index chains); and ``n_tips`` tip rows.  Every loc code stays in 1..52,
+    so the kernels' boundary branches treat the relabelled nodes as the face
+    nodes they were."""
+    g = c.arrays["grid"]
+    rng = np.random.default_rng(seed + 17)
+    wall = np.asarray(c.bc.wall)
+    codes = g["loc"][wall]
+    if face_code is None:
+        faces = codes[(codes >= 1) & (codes <= 6)]
+        face_code = int(np.bincount(faces).argmax())
+    rows = wall[codes == face_code]
+    edges = wall[(codes >= 7) & (codes <= 26)]
+    need = len(SINGULAR_CODES) + 6
+    if rows.size < need:
+        raise ValueError(f"{rows.size} wall rows with code {face_code}; the relabelling needs {need}")
+    chosen = rows[rng.choice(rows.size, size=need, replace=False)]
+    g["ID"][wall] = 0
+    for r, code in zip(chosen, SINGULAR_CODES):
+        g["loc"][r] = code
+    marked = list(chosen[2:8]) + list(chosen[len(SINGULAR_CODES):])   # over 33..52 and over the face code
+    if edges.size:
+        marked.append(edges[0])
+    g["ID"][marked] = 10
+    owned = np.arange(1, c.sd_node + 1)
+    sing = np.zeros((c.g_node + 1, 6), dtype=np.int32)
+    for r in list(chosen) + marked:
+        sing[r] = rng.choice(owned, size=6)
+    tips = rng.choice(owned, size=n_tips, replace=False).astype(np.int32)
+    c.bc = BoundaryLists(c.bc.outlet, c.bc.inlet, c.bc.boundary, c.bc.wall, singular=sing, tips=tips)
+    return c
+
+
+def singular_box(shape=(10, 9, 8), seed=0, mach=1.5, n_tips: int = 4) -> Case:
+    """ghost_box(bc=True) with singular wall nodes on its south (-j) wall
+    (with_singular_nodes)."""
+    c = with_singular_nodes(ghost_box(shape=shape, seed=seed, mach=mach, bc=True), seed, n_tips, face_code=3)
+    c.name = "singular_box"
     return c
 
 

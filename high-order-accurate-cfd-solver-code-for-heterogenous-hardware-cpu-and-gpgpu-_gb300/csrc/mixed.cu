@@ -114,8 +114,9 @@ __global__ void __launch_bounds__(256) k_update_m(LatView g, int jst)
     if (n < g.N) mx::update_node<LOC>(g, n, jst);
 }
 
-// one thread per (entry, target node); a list whose entries touch each
-// other's rows runs in list order on one thread
+// one thread per (entry, target node), a group of entries (one singular
+// wall node) on one thread in order; a list whose groups touch each other's
+// rows runs in list order on one thread
 __global__ void k_bc_m(LatView g, const BcEntry *__restrict__ E, int n, int type, int q, double mach, int sequential)
 {
     if (sequential) {
@@ -125,14 +126,19 @@ __global__ void k_bc_m(LatView g, const BcEntry *__restrict__ E, int n, int type
         return;
     }
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < 4 * n) mx::bc_target(g, type, E[t >> 2], t & 3, q, mach);
+    if (t < 4 * n)
+        bc_for_group<4>(E, t >> 2, n, t & 3,
+                        [&](const BcEntry &e, int m) { mx::bc_target(g, type, e, m, q, mach); });
 }
 
 // every target of independent lists in one launch
 __global__ void k_bc_m_fused(LatView g, const BcEntry *__restrict__ E, BcOffsets off, int q, double mach)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < 4 * off.o[BC_NTYPES]) mx::bc_target(g, bc_type_of(off, t >> 2), E[t >> 2], t & 3, q, mach);
+    if (t >= 4 * off.o[BC_NTYPES]) return;
+    const int type = bc_type_of(off, t >> 2);
+    bc_for_group<4>(E, t >> 2, off.o[BC_NTYPES], t & 3,
+                    [&](const BcEntry &e, int m) { mx::bc_target(g, type, e, m, q, mach); });
 }
 
 __global__ void k_flow_out_m(LatView g, int q)

@@ -108,13 +108,18 @@ __global__ void k_bc_s(LatView g, const BcEntry *__restrict__ E, int n, int type
         return;
     }
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < 4 * n) sp::bc_target(g, type, E[t >> 2], t & 3, q, mach);
+    if (t < 4 * n)
+        bc_for_group<4>(E, t >> 2, n, t & 3,
+                        [&](const BcEntry &e, int m) { sp::bc_target(g, type, e, m, q, mach); });
 }
 
 __global__ void k_bc_s_fused(LatView g, const BcEntry *__restrict__ E, BcOffsets off, int q, double mach)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < 4 * off.o[BC_NTYPES]) sp::bc_target(g, bc_type_of(off, t >> 2), E[t >> 2], t & 3, q, mach);
+    if (t >= 4 * off.o[BC_NTYPES]) return;
+    const int type = bc_type_of(off, t >> 2);
+    bc_for_group<4>(E, t >> 2, off.o[BC_NTYPES], t & 3,
+                    [&](const BcEntry &e, int m) { sp::bc_target(g, type, e, m, q, mach); });
 }
 
 __global__ void k_flow_out_s(LatView g, int q)

@@ -200,7 +200,9 @@ class SolverInfo:
 
 class Boundary:
     """The reference's boundary routine for one table (cfd_bc_*): the plan of
-    a cases.BoundaryLists resolved against the neighbour table."""
+    a cases.BoundaryLists resolved against the neighbour table.  A
+    BoundaryLists with a singular-node table or tip rows goes through
+    cfd_bc_create_singular."""
 
     def __init__(self, ctx: Context, grid: np.ndarray, bc):
         self.ctx = ctx
@@ -211,7 +213,20 @@ class Boundary:
         for a in self._lists:
             args += [_ptr(a) if a.size else None, int(a.size)]
         h = C.c_void_p()
-        ctx.check(self.lib.cfd_bc_create(ctx.h, _ptr(grid), int(grid.shape[0]), *args, C.byref(h)), "cfd_bc_create")
+        sing = getattr(bc, "singular", None)
+        tips = getattr(bc, "tips", None)
+        if sing is None and tips is None:
+            ctx.check(self.lib.cfd_bc_create(ctx.h, _ptr(grid), int(grid.shape[0]), *args, C.byref(h)),
+                      "cfd_bc_create")
+        else:
+            self._sing = None if sing is None else np.ascontiguousarray(sing, dtype=np.int32).reshape(-1, 6)
+            if self._sing is not None and self._sing.shape[0] != grid.shape[0]:
+                raise ValueError("singular table needs one row of six slots per grid row")
+            self._tips = np.ascontiguousarray(tips if tips is not None else [], dtype=np.int32)
+            ctx.check(self.lib.cfd_bc_create_singular(
+                ctx.h, _ptr(grid), int(grid.shape[0]), *args, _ptr(self._sing) if self._sing is not None else None,
+                _ptr(self._tips) if self._tips.size else None, int(self._tips.size), C.byref(h)),
+                "cfd_bc_create_singular")
         self.h = h
         ctx._children.add(self)
 

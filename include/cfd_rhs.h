@@ -295,11 +295,32 @@ cfd_status_t cfd_solver_stage(cfd_solver_t *s, int32_t j, double del_t, cfd_colu
  * pass those to a second cfd_bc_t).  Face codes 1..6 fill the node and its
  * three ghost layers, edge and corner codes 7..26 copy a diagonal node;
  * wall nodes that need the reference's singular-node table (ID 10, loc
- * 29/30/33..56) give CFD_EUNSUPPORTED.  `grid` is host memory, read once. */
+ * 29/30/33..56) give CFD_EUNSUPPORTED here (see cfd_bc_create_singular).
+ * `grid` is host memory, read once. */
 typedef struct cfd_bc cfd_bc_t;
 cfd_status_t cfd_bc_create(cfd_ctx_t *ctx, const cfd_grid_t *grid, int32_t n_rows, const int32_t *outlet,
                            int32_t n_outlet, const int32_t *inlet, int32_t n_inlet, const int32_t *boundary,
                            int32_t n_boundary, const int32_t *wall, int32_t n_wall, cfd_bc_t **bc);
+/* cfd_bc_create for grids with a wake cut (C-grids): `singular` (host, may
+ * be NULL) is the reference's singular-node table -- six neighbour slots per
+ * row, row-major [n_rows][6], the `singular[].n_n[0..5]` array that
+ * Main.cpp:1612-1700 fills with the neighbours across the cut.  Wall nodes
+ * with ID 10 or loc 29/30/33..52 then get the routine's singular branches
+ * (Flow_Initialisation.cpp:1194-1392) after the rule of their code: codes
+ * 29/30 the node rule from the node beyond singular[b][3]; ID 10 the node
+ * rule from singular[b][3] and three mirror passes of three ghosts each;
+ * codes 33..52 the node rule from singular[b][0] and two or three (node
+ * rule, mirror pass) pairs.  Wall codes 53..56 give CFD_EUNSUPPORTED (the
+ * routine runs their mirror pass with slots it never sets).  `tips`
+ * (n_tips rows) are the trailing-edge rows the solver loop fixes after the
+ * routine (Solver.cpp:660-683: zero velocity, p and t of the slot-3
+ * neighbour, rho and e derived); they run after every list of this object,
+ * so with a second cfd_bc_t for the subdomain lists pass them to the one
+ * applied last. */
+cfd_status_t cfd_bc_create_singular(cfd_ctx_t *ctx, const cfd_grid_t *grid, int32_t n_rows, const int32_t *outlet,
+                                    int32_t n_outlet, const int32_t *inlet, int32_t n_inlet, const int32_t *boundary,
+                                    int32_t n_boundary, const int32_t *wall, int32_t n_wall, const int32_t *singular,
+                                    const int32_t *tips, int32_t n_tips, cfd_bc_t **bc);
 cfd_status_t cfd_bc_destroy(cfd_bc_t *bc);
 /* intialise() on a FLOW buffer of the reference layout (device, or the host
  * rows of the table the lists were made for, copied as for the kernel entry

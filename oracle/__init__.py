@@ -55,13 +55,18 @@ class OrCase(C.Structure):
 
 class OrBcLists(C.Structure):
     _fields_ = [("outlet", _vp), ("inlet", _vp), ("boundary", _vp), ("wall", _vp),
-                ("n_outlet", C.c_int), ("n_inlet", C.c_int), ("n_boundary", C.c_int), ("n_wall", C.c_int)]
+                ("n_outlet", C.c_int), ("n_inlet", C.c_int), ("n_boundary", C.c_int), ("n_wall", C.c_int),
+                ("singular", _vp), ("tips", _vp), ("n_tips", C.c_int)]
 
 
 def make_bc(bc) -> OrBcLists:
     """ctypes view of a cases.BoundaryLists (the arrays must stay alive)."""
+    sing = getattr(bc, "singular", None)
+    tips = getattr(bc, "tips", None)
     return OrBcLists(_p(bc.outlet), _p(bc.inlet), _p(bc.boundary), _p(bc.wall),
-                     len(bc.outlet), len(bc.inlet), len(bc.boundary), len(bc.wall))
+                     len(bc.outlet), len(bc.inlet), len(bc.boundary), len(bc.wall),
+                     _p(sing) if sing is not None else None, _p(tips) if tips is not None and len(tips) else None,
+                     0 if tips is None else len(tips))
 
 
 def _host_core_flags() -> list[str]:
@@ -164,7 +169,7 @@ def ref():
         _ref.ref_viscous_param.argtypes = [C.c_int] + [C.c_double] * 4 + [_vp] * 11
         _ref.ref_weno.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double] + [_vp] * 16
         _ref.ref_boundary_fill.argtypes = ([_vp, _vp, C.c_int] + [_vp, C.c_int] * 4
-                                           + [C.c_double, C.c_int, C.c_int])
+                                           + [C.c_double, C.c_int, C.c_int, _vp])
     return _ref
 
 
@@ -219,7 +224,7 @@ def boundary_fill(arrays: dict, bc, mach: float, initial: int = 1, sd_node: int 
     rc = lib().oracle_boundary_fill(_p(arrays["grid"]), _p(arrays["flow"]), C.byref(lists), float(mach),
                                     int(initial), int(sd_node))
     if rc != 0:
-        raise ValueError("boundary lists need the reference's singular-node table")
+        raise ValueError("a wall node needs the singular-node table (none given) or has code 53..56")
 
 
 def rk3_steps_bc(arrays: dict, g_node: int, sd_node: int, params, dt: float, nsteps: int, bc) -> None:
@@ -228,7 +233,7 @@ def rk3_steps_bc(arrays: dict, g_node: int, sd_node: int, params, dt: float, nst
     pr = make_params(params)
     lists = make_bc(bc)
     if lib().oracle_rk3_steps_bc(C.byref(c), C.byref(pr), float(dt), int(nsteps), C.byref(lists)) != 0:
-        raise ValueError("boundary lists need the reference's singular-node table")
+        raise ValueError("a wall node needs the singular-node table (none given) or has code 53..56")
 
 
 def uq(a: dict, n_items: int, U_out: np.ndarray) -> None:
@@ -278,11 +283,15 @@ def ref_weno(a: dict, n_items: int, mach: float, j: int, dt: float) -> None:
 
 
 def ref_boundary_fill(arrays: dict, bc, mach: float, initial: int = 1, sd_node: int = 0) -> None:
-    """The reference's own intialise() on arrays["flow"] in place."""
+    """The reference's own intialise() on arrays["flow"] in place, with the
+    singular-node table of ``bc`` when it has one (the tip fix-ups belong to
+    the solver loop, not to intialise, and are not applied here)."""
     n = arrays["flow"].shape[0]
+    sing = getattr(bc, "singular", None)
     ref().ref_boundary_fill(_p(arrays["grid"]), _p(arrays["flow"]), n, _p(bc.outlet), len(bc.outlet),
                             _p(bc.inlet), len(bc.inlet), _p(bc.boundary), len(bc.boundary), _p(bc.wall),
-                            len(bc.wall), float(mach), int(initial), int(sd_node))
+                            len(bc.wall), float(mach), int(initial), int(sd_node),
+                            _p(sing) if sing is not None else None)
 
 
 def ref_stage(a: dict, g_node: int, sd_node: int, params, j: int, dt: float) -> None:

@@ -613,9 +613,103 @@ static int bc_wall_singular(const or_grid *g, int r)
     return loc == 29 || loc == 30 || (loc >= 33 && loc <= 56) || g[r].ID == 10;
 }
 
+/* neighbour slot s of row r in the singular table */
+static inline int bc_sing(const int32_t *sing, int r, int s) { return sing[(size_t)r * 6 + s]; }
+
+/* The wall rule of one node from source row s: zero velocity, p and t of s,
+ * rho and e derived; a untouched (Flow_Initialisation.cpp:1194-1222). */
+static void bc_wall_from(or_flow *F, int b, int s, double mach)
+{
+    or_flow *fb = &F[b];
+    fb->u = 0.0;
+    fb->v = 0.0;
+    fb->w = 0.0;
+    fb->p = F[s].p;
+    fb->t = F[s].t;
+    bc_derive_rho_e(fb, mach);
+}
+
+/* One mirror pass of the singular branches (:1242-1270, :1354-1382): the
+ * three ghosts along slot l of wall node b take the three nodes along slot
+ * k from the singular neighbour singular[b][k], velocity negated, and the
+ * wall node's a. */
+static void bc_singular_mirror(const or_grid *g, or_flow *F, const int32_t *sing, int b, int l, int k)
+{
+    int gr = b, sr = -1;
+    for (int m = 0; m < 3; ++m) {
+        gr = bc_nb(g, gr, l);
+        sr = m == 0 ? bc_sing(sing, b, k) : bc_nb(g, sr, k);
+        or_flow *fg = &F[gr];
+        const or_flow *fs = &F[sr];
+        fg->u = (-1.0) * fs->u;
+        fg->v = (-1.0) * fs->v;
+        fg->w = (-1.0) * fs->w;
+        fg->p = fs->p;
+        fg->rho = fs->rho;
+        fg->t = fs->t;
+        fg->a = F[b].a;
+        fg->e = fs->e;
+    }
+}
+
+/* The passes (l = ghost slot, k = singular slot) of the codes 33..52
+ * (:1285-1342): 33..36 and 41..44 and 49..52 take two, 37..40 and 45..48
+ * three.  Returns the number of passes written to lk. */
+static int bc_multi_pass(int loc, int lk[3][2])
+{
+    int n = 0;
+    if ((loc >= 33 && loc <= 40)) { lk[n][0] = 2; lk[n][1] = 0; ++n; }
+    else if (loc >= 41 && loc <= 48) { lk[n][0] = 0; lk[n][1] = 2; ++n; }
+    else if (loc == 49 || loc == 52) { lk[n][0] = 5; lk[n][1] = 4; ++n; }
+    else { lk[n][0] = 4; lk[n][1] = 5; ++n; }   /* 50, 51 */
+    if (loc == 33 || loc == 43 || loc == 51 || loc == 52 || loc == 39 || loc == 40 || loc == 47 || loc == 48) {
+        lk[n][0] = 3; lk[n][1] = 1;
+    } else if (loc == 35 || loc == 41 || loc == 49 || loc == 50 || loc == 37 || loc == 38 || loc == 45 || loc == 46) {
+        lk[n][0] = 1; lk[n][1] = 3;
+    } else if (loc == 34 || loc == 44) {
+        lk[n][0] = 5; lk[n][1] = 4;
+    } else {   /* 36, 42 */
+        lk[n][0] = 4; lk[n][1] = 5;
+    }
+    ++n;
+    if ((loc >= 37 && loc <= 40) || (loc >= 45 && loc <= 48)) {
+        if (loc == 37 || loc == 40 || loc == 48 || loc == 45) { lk[n][0] = 5; lk[n][1] = 4; }
+        else { lk[n][0] = 4; lk[n][1] = 5; }
+        ++n;
+    }
+    return n;
+}
+
+/* The singular-node branches of one wall node, after its face or edge rule
+ * (Flow_Initialisation.cpp:1194-1392): codes 29 and 30 (in the routine's
+ * chain of codes) from the node beyond singular[b][3]; ID 10 (other codes)
+ * the node from singular[b][3] and three mirror passes; codes 33..52 the
+ * node from singular[b][0], then per pass the node from singular[b][k] and
+ * a mirror pass. */
+static void bc_wall_singular_branches(const or_grid *g, or_flow *F, const int32_t *sing, int b, double mach)
+{
+    const int loc = g[b].loc;
+    if (loc == 29 || loc == 30) bc_wall_from(F, b, bc_nb(g, bc_sing(sing, b, 3), loc == 29 ? 4 : 5), mach);
+    if (g[b].ID == 10 && loc != 29 && loc != 30) {
+        static const int lk10[3][2] = {{2, 0}, {0, 2}, {1, 3}};
+        bc_wall_from(F, b, bc_sing(sing, b, 3), mach);
+        for (int h = 0; h < 3; ++h) bc_singular_mirror(g, F, sing, b, lk10[h][0], lk10[h][1]);
+    }
+    if (loc >= 33 && loc <= 52) {
+        int lk[3][2];
+        const int n = bc_multi_pass(loc, lk);
+        bc_wall_from(F, b, bc_sing(sing, b, 0), mach);
+        for (int h = 0; h < n; ++h) {
+            bc_wall_from(F, b, bc_sing(sing, b, lk[h][1]), mach);
+            bc_singular_mirror(g, F, sing, b, lk[h][0], lk[h][1]);
+        }
+    }
+}
+
 /* One list of the routine, visited in order (Flow_Initialisation.cpp:50-342
  * outlet, 343-624 inlet, 625-909 boundary, 910-1394 wall). */
-static void bc_list(int type, const or_grid *g, or_flow *F, const int32_t *rows, int n, double mach)
+static void bc_list(int type, const or_grid *g, or_flow *F, const int32_t *rows, int n, double mach,
+                    const int32_t *sing)
 {
     for (int q = 0; q < n; ++q) {
         const int b = rows[q];
@@ -693,14 +787,17 @@ static void bc_list(int type, const or_grid *g, or_flow *F, const int32_t *rows,
             bc_derive_rho_e(fb, mach);
         }
         /* other codes: the routine has no branch for them */
+        if (type == BC_WALL && sing && bc_wall_singular(g, b)) bc_wall_singular_branches(g, F, sing, b, mach);
     }
 }
 
 int oracle_boundary_fill(const or_grid *grid, or_flow *flow, const or_bc_lists *bc, double mach, int initial,
                          int sd_node)
 {
-    for (int q = 0; q < bc->n_wall; ++q)
-        if (bc_wall_singular(grid, bc->wall[q])) return -1;
+    for (int q = 0; q < bc->n_wall; ++q) {
+        const int r = bc->wall[q], loc = grid[r].loc;
+        if (bc_wall_singular(grid, r) && (!bc->singular || (loc >= 53 && loc <= 56))) return -1;
+    }
     if (initial == 0) {   /* Flow_Initialisation.cpp:35-48 */
         for (int r = 1; r <= sd_node; ++r) {
             or_flow *f = &flow[r];
@@ -714,10 +811,12 @@ int oracle_boundary_fill(const or_grid *grid, or_flow *flow, const or_bc_lists *
             f->a = sqrt(1.4 * f->p / f->rho);
         }
     }
-    bc_list(BC_OUTLET, grid, flow, bc->outlet, bc->n_outlet, mach);
-    bc_list(BC_INLET, grid, flow, bc->inlet, bc->n_inlet, mach);
-    bc_list(BC_BOUNDARY, grid, flow, bc->boundary, bc->n_boundary, mach);
-    bc_list(BC_WALL, grid, flow, bc->wall, bc->n_wall, mach);
+    bc_list(BC_OUTLET, grid, flow, bc->outlet, bc->n_outlet, mach, NULL);
+    bc_list(BC_INLET, grid, flow, bc->inlet, bc->n_inlet, mach, NULL);
+    bc_list(BC_BOUNDARY, grid, flow, bc->boundary, bc->n_boundary, mach, NULL);
+    bc_list(BC_WALL, grid, flow, bc->wall, bc->n_wall, mach, bc->singular);
+    /* Solver.cpp:660-683: the tips after the routine, from their slot-3 node */
+    for (int q = 0; q < bc->n_tips; ++q) bc_wall_from(flow, bc->tips[q], bc_nb(grid, bc->tips[q], 3), mach);
     return 0;
 }
 

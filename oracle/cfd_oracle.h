@@ -95,13 +95,23 @@ void oracle_rk3_steps(or_case *c, const or_params *prm, double del_t, int nsteps
 typedef struct {
     const int32_t *outlet, *inlet, *boundary, *wall;
     int n_outlet, n_inlet, n_boundary, n_wall;
+    /* singular-node table of the wake cut (functions.h singul; the
+     * reference fills it in Main.cpp:1640-1700): six neighbour slots per
+     * row, row-major [rows][6]; NULL when no wall node needs it. */
+    const int32_t *singular;
+    /* trailing-edge tip rows fixed after the routine (Solver.cpp:660-683) */
+    const int32_t *tips;
+    int n_tips;
 } or_bc_lists;
 
 /* intialise(RK) restated: with initial == 0 rows 1..sd_node first get the
  * free stream; then outlet, inlet, boundary and wall nodes in that order --
  * face codes 1..6 with their three ghost layers, edge and corner codes 7..26
- * from a diagonal node.  Returns -1 (and changes nothing) when a wall node
- * needs the reference's singular-node table (ID 10, codes 29/30, 33..56). */
+ * from a diagonal node, and on walls the singular-node branches (codes
+ * 29/30, ID 10, codes 33..52) from the singular table; then the tip rows.
+ * Returns -1 (and changes nothing) when a wall node needs the singular
+ * table and none is given, or has a code 53..56 (the routine leaves the
+ * mirror slots of those codes unset). */
 int oracle_boundary_fill(const or_grid *grid, or_flow *flow, const or_bc_lists *bc, double mach, int initial,
                          int sd_node);
 

@@ -1,7 +1,8 @@
 // ref_bc.cpp -- TEST INFRASTRUCTURE ONLY.  Drives the reference's own
 // boundary routine intialise() (Flow_Initialisation.cpp, built from the copy
 // under oracle/_ref/) on arrays in the reference layout, to pin the oracle's
-// restatement (oracle_boundary_fill).
+// restatement (oracle_boundary_fill).  sing (may be null) is the
+// singular-node table, six slots per row.
 #include <cstdint>
 
 #include "bc_ref_shim.h"
@@ -22,10 +23,13 @@ struct ref_grid_row { double x, y, z; int32_t N[6]; int32_t ID, loc; };
 extern "C" void ref_boundary_fill(const ref_grid_row *grid, FLOW_VARIABLES *flow, int n_rows,
                                   const int32_t *outlet, int n_outlet, const int32_t *inlet, int n_inlet,
                                   const int32_t *boundary, int n_boundary, const int32_t *wall, int n_wall,
-                                  double mach, int initial_flag, int n_owned)
+                                  double mach, int initial_flag, int n_owned, const int32_t *sing)
 {
     node.assign(n_rows, MNODE{});
     singular.assign(n_rows, singul{});
+    if (sing)
+        for (int r = 0; r < n_rows; ++r)
+            for (int s = 0; s < 6; ++s) singular[r].n_n[s] = sing[(size_t)r * 6 + s];
     FLOW.assign(flow, flow + n_rows);
     for (int r = 0; r < n_rows; ++r) {
         for (int s = 0; s < 6; ++s) node[r].n_n[s] = grid[r].N[s];

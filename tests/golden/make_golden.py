@@ -100,13 +100,41 @@ def make_bc_golden():
     print("bc_ghostbox ->", (HERE / "bc_ghostbox.npz").stat().st_size, "bytes")
 
 
+def make_bc_singular_golden():
+    """bc_singular.npz: the reference's intialise() with its singular-node
+    wall branches (Flow_Initialisation.cpp:1194-1392: codes 29/30, ID 10,
+    codes 33..52) on cases.singular_box, from a seeded random FLOW, with
+    initial = 1 and 0.  The table and the relabelled grid are stored with
+    the lists; the tip rows are not part of intialise and are left out."""
+    box = cases.singular_box(shape=(8, 6, 8), seed=5)
+    rng = np.random.default_rng(20261204)
+    flow = box.arrays["flow"].copy()
+    flow[1:] = rng.integers(50, 151, flow[1:].shape) / 100.0   # few distinct inputs: a small fixture
+    grid = box.arrays["grid"].copy()
+    for k in ("x", "y", "z"):
+        grid[k] = 0.0   # the routine reads only the neighbour slots, ID and loc
+    payload = {"in_grid": grid, "in_flow": flow, "sd_node": np.array(box.sd_node),
+               "mach": np.array(BC_MACH), "singular": box.bc.singular}
+    for t in ("outlet", "inlet", "boundary", "wall"):
+        payload[f"list_{t}"] = getattr(box.bc, t)
+    bc = cases.BoundaryLists(box.bc.outlet, box.bc.inlet, box.bc.boundary, box.bc.wall, singular=box.bc.singular)
+    for initial in (1, 0):
+        a = {"grid": grid.copy(), "flow": flow.copy()}
+        oracle.ref_boundary_fill(a, bc, BC_MACH, initial, box.sd_node)
+        payload[f"out_flow_initial{initial}"] = a["flow"]
+    np.savez_compressed(HERE / "bc_singular.npz", **payload)
+    print("bc_singular ->", (HERE / "bc_singular.npz").stat().st_size, "bytes")
+
+
 def main(only=None):
     oracle.build()
     if not oracle.ref_available():
         raise SystemExit("reference build missing: run oracle/build_ref.sh in a checkout with the reference")
     if only in (None, "bc"):
         make_bc_golden()
-    if only == "bc":
+    if only in (None, "bc", "bc_singular"):
+        make_bc_singular_golden()
+    if only in ("bc", "bc_singular"):
         return
     for name, case in golden_cases().items():
         stages = 1 if name == "ghostbox" else 3
@@ -125,5 +153,5 @@ def main(only=None):
 
 
 if __name__ == "__main__":
-    # python tests/golden/make_golden.py [bc]   (bc: only the boundary-routine fixture)
+    # python tests/golden/make_golden.py [bc|bc_singular]   (only the boundary-routine fixtures / the singular one)
     main(sys.argv[1] if len(sys.argv) > 1 else None)

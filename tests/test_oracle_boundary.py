@@ -96,3 +96,105 @@ def test_channel_steps_with_boundary_match_reference(oracle_mod):
     assert np.array_equal(a["U0"][defined], b["U0"][defined])
     undefined_locs = set(c.arrays["grid"]["loc"][~defined].tolist())
     assert undefined_locs <= {1, 3}
+
+
+# ---------------------------------------------------------------- singular --
+# The wall rules of the singular-node table (Flow_Initialisation.cpp
+# :1194-1392: codes 29/30 from the node beyond singular[b][3]; ID 10 the node
+# from singular[b][3] and three mirror passes; codes 33..52 the node from
+# singular[b][0], then per pass the node from singular[b][k] and a mirror
+# pass) and the tip rows (Solver.cpp:660-683).
+
+SINGULAR_GOLDEN = pathlib.Path(__file__).resolve().parent / "golden" / "bc_singular.npz"
+
+
+def singular_golden_inputs():
+    from cfd_gb300 import cases, layout
+    z = np.load(SINGULAR_GOLDEN)
+    n = z["in_grid"].shape[0]
+    a = layout.empty_arrays(n)
+    a["grid"][...] = z["in_grid"]
+    a["flow"][...] = z["in_flow"]
+    bc = cases.BoundaryLists(*(z[f"list_{t}"] for t in ("outlet", "inlet", "boundary", "wall")),
+                             singular=z["singular"])
+    return z, a, bc
+
+
+@pytest.mark.parametrize("initial", [1, 0])
+def test_singular_wall_matches_golden(oracle_mod, initial):
+    z, a, bc = singular_golden_inputs()
+    oracle_mod.boundary_fill(a, bc, float(z["mach"]), initial, int(z["sd_node"]))
+    assert np.array_equal(a["flow"], z[f"out_flow_initial{initial}"])
+
+
+def test_singular_golden_covers_every_branch(oracle_mod):
+    """Every singular code, ID 10 over a face code, over an edge code and
+    over codes 33..52; and the table changes the result."""
+    from cfd_gb300 import cases
+    z, a, bc = singular_golden_inputs()
+    g = a["grid"]
+    wall = bc.wall
+    assert set(cases.SINGULAR_CODES) <= set(g["loc"][wall].tolist())
+    id10 = wall[g["ID"][wall] == 10]
+    codes10 = set(g["loc"][id10].tolist())
+    assert 3 in codes10 and codes10 & set(range(7, 27)) and codes10 & set(range(33, 53))
+    other = bc.singular.copy()
+    other[other != 0] = np.roll(other[other != 0], 1)
+    b = {k: v.copy() for k, v in a.items()}
+    oracle_mod.boundary_fill(b, cases.BoundaryLists(bc.outlet, bc.inlet, bc.boundary, bc.wall, singular=other),
+                             float(z["mach"]), 1, int(z["sd_node"]))
+    assert not np.array_equal(b["flow"], z["out_flow_initial1"])
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_singular_wall_matches_reference_build(oracle_mod, seed):
+    if not oracle_mod.ref_available():
+        pytest.skip("reference build absent")
+    from cfd_gb300 import cases
+    c = cases.singular_box(shape=(10, 9, 8), seed=seed)
+    bc = cases.BoundaryLists(c.bc.outlet, c.bc.inlet, c.bc.boundary, c.bc.wall, singular=c.bc.singular)
+    rng = np.random.default_rng(seed + 3)
+    a = c.copy().arrays
+    a["flow"][1:] = rng.uniform(0.5, 1.5, a["flow"][1:].shape)
+    b = {k: v.copy() for k, v in a.items()}
+    oracle_mod.boundary_fill(a, bc, 0.7, 1, c.sd_node)
+    oracle_mod.ref_boundary_fill(b, bc, 0.7, 1, c.sd_node)
+    assert np.array_equal(a["flow"], b["flow"])
+
+
+def test_tips_after_the_routine(oracle_mod):
+    """Each tip row: zero velocity, p and t of its slot-3 neighbour, rho and e
+    derived, a untouched -- applied after every list."""
+    from cfd_gb300 import cases, layout
+    c = cases.singular_box(seed=2)
+    F = layout.FLOW
+    rng = np.random.default_rng(9)
+    a = c.copy().arrays
+    a["flow"][1:] = rng.uniform(0.5, 1.5, a["flow"][1:].shape)
+    notips = cases.BoundaryLists(c.bc.outlet, c.bc.inlet, c.bc.boundary, c.bc.wall, singular=c.bc.singular)
+    b = {k: v.copy() for k, v in a.items()}
+    oracle_mod.boundary_fill(a, c.bc, 0.7, 1, c.sd_node)
+    oracle_mod.boundary_fill(b, notips, 0.7, 1, c.sd_node)
+    m = 0.7
+    for t in c.bc.tips:
+        s = int(b["grid"]["N3"][t])
+        exp = b["flow"][t].copy()
+        exp[[F["u"], F["v"], F["w"]]] = 0.0
+        exp[F["p"]], exp[F["t"]] = b["flow"][s, F["p"]], b["flow"][s, F["t"]]
+        exp[F["rho"]] = (1.4 * m * m) * (exp[F["p"]] / exp[F["t"]])
+        exp[F["e"]] = exp[F["p"]] / (0.4 * exp[F["rho"]])
+        b["flow"][t] = exp
+    assert np.array_equal(a["flow"], b["flow"])
+
+
+def test_unset_singular_codes_are_rejected(oracle_mod):
+    """Codes 53..56 run the routine's mirror passes with slots it never set."""
+    from cfd_gb300 import cases
+    c = cases.singular_box(seed=0)
+    a = c.copy().arrays
+    r = int(c.bc.wall[np.flatnonzero(a["grid"]["loc"][c.bc.wall] == 3)[0]])
+    a["grid"]["loc"][r] = 54
+    before = a["flow"].copy()
+    with pytest.raises(ValueError):
+        oracle_mod.boundary_fill(a, c.bc, 0.8, 1, c.sd_node)
+    assert np.array_equal(a["flow"], before)
