@@ -91,6 +91,7 @@ PROTOTYPES = {
     "cfd_solver_stage": (C.c_int, [_vp, _i32, _d, _vp]),
     "cfd_solver_profile_stage": (C.c_int, [_vp, _i32, _d, _vp, _i32, C.POINTER(_i32)]),
     "cfd_probe_flops": (C.c_int, [_vp, _i32, C.POINTER(_d)]),
+    "cfd_probe_emu64": (C.c_int, [_vp, C.c_int64, C.c_uint64, C.POINTER(C.c_int64)]),
     "cfd_bc_create": (C.c_int, [_vp, _vp, _i32] + [_vp, _i32] * 4 + [C.POINTER(_vp)]),
     "cfd_bc_create_singular": (C.c_int, [_vp, _vp, _i32] + [_vp, _i32] * 4 + [_vp, _vp, _i32, C.POINTER(_vp)]),
     "cfd_bc_destroy": (C.c_int, [_vp]),

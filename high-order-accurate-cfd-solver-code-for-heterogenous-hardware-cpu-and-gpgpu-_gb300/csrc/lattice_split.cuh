@@ -53,16 +53,18 @@ __device__ __forceinline__ void store_state(const LatView &g, int q, int n, cons
 __device__ __forceinline__ void derive(const LatView &g, int n, const double Un[5])
 {
     const int N = g.N;
+    using emu::d2f;   // FP32 <-> FP64 conversions on the integer pipe (same bits)
+    using emu::f2d;
 #pragma unroll
     for (int c = 0; c < 5; ++c) {
-        const float h = (float)Un[c];
+        const float h = d2f(Un[c]);
         g.Whl[c * N + n] = h;
-        g.Whl[(5 + c) * N + n] = (float)(Un[c] - (double)h);
+        g.Whl[(5 + c) * N + n] = d2f(Un[c] - f2d(h));
     }
     const double id = g.idet64[n];
     float q[5];
 #pragma unroll
-    for (int c = 0; c < 5; ++c) q[c] = (float)(Un[c] * id);
+    for (int c = 0; c < 5; ++c) q[c] = d2f(Un[c] * id);
     const float rho = q[0];
     const float ir = 1.0f / rho;
     const float u = q[1] * ir, v = q[2] * ir, w = q[3] * ir;
@@ -139,7 +141,7 @@ __device__ __forceinline__ void face_flux(const LatView &g, int n, const float2 
     const int N = g.N;
     const double dm[3] = {g.fm[(D * 3 + 0) * N + n], g.fm[(D * 3 + 1) * N + n], g.fm[(D * 3 + 2) * N + n]};
     x2::llf_face_flux2_split(P, g.fm32[(D * 3 + 0) * N + n], g.fm32[(D * 3 + 1) * N + n],
-                             g.fm32[(D * 3 + 2) * N + n], dm, g.fdet[D * N + n], r, (float)g.P.eps, corr, out);
+                             g.fm32[(D * 3 + 2) * N + n], dm, g.fdet[D * N + n], r, emu::d2f(g.P.eps), corr, out);
 }
 
 // Face n+1/2 along D with its stencil read from the lattice (the batched
@@ -267,7 +269,7 @@ __device__ __forceinline__ void update_node(const LatView &g, int n, int jst)
         }
     }
 #pragma unroll
-    for (int c = 0; c < 5; ++c) Ld[c] += (double)Lv[c];
+    for (int c = 0; c < 5; ++c) Ld[c] += emu::f2d(Lv[c]);
     if (g.Lout) {
 #pragma unroll
         for (int c = 0; c < 5; ++c) g.Lout[c * N + n] = -Ld[c];

@@ -14,6 +14,7 @@
 // LLF and the sixth-order correction); only the lane packing is new.
 #pragma once
 
+#include "emu64.cuh"
 #include "physics.cuh"
 
 namespace cfd {
@@ -188,7 +189,7 @@ __device__ __forceinline__ void llf_face_flux2_split(const float2 P[3][5], float
     const float2 lam = add2(un32, make_float2(sqrtf(c2k.x), sqrtf(c2k.y)));
     const float alpha = fmaxf(fabsf(lam.x), fabsf(lam.y));
     const double hd = 0.5 * det_f;
-    const float hd32 = (float)hd;
+    const float hd32 = emu::d2f(hd);
     // FP32 terms: extra, less the dissipation, plus the difference term
     // (q+ - q-) (U+ - U-) / 2, all times det_f / 2 where they belong
     const float dun = un32.x - un32.y;
@@ -199,14 +200,15 @@ __device__ __forceinline__ void llf_face_flux2_split(const float2 P[3][5], float
         qs[c] = qp + qn;
         x[c] = fmaf(hd32, fmaf(0.5f * (qp - qn), dun, -alpha * (q[c].x - q[c].y)), extra[c]);
     }
-    // FP64: the metric products of the sum term and of the pressure
-    const double hsun = hd * (0.5 * fma(dm[0], (double)(u.x + u.y), fma(dm[1], (double)(v.x + v.y),
-                                                                         dm[2] * (double)(w.x + w.y))));
-    const double hps = hd * (double)(pr.x + pr.y);
-    Fhat[0] = fma((double)qs[0], hsun, (double)x[0]);
+    // FP64: the metric products of the sum term and of the pressure (the
+    // FP32 -> FP64 conversions on the integer pipe, emu::f2d: exact)
+    using emu::f2d;
+    const double hsun = hd * (0.5 * fma(dm[0], f2d(u.x + u.y), fma(dm[1], f2d(v.x + v.y), dm[2] * f2d(w.x + w.y))));
+    const double hps = hd * f2d(pr.x + pr.y);
+    Fhat[0] = fma(f2d(qs[0]), hsun, f2d(x[0]));
 #pragma unroll
-    for (int c = 1; c < 4; ++c) Fhat[c] = fma(dm[c - 1], hps, fma((double)qs[c], hsun, (double)x[c]));
-    Fhat[4] = fma((double)qs[4], hsun, (double)x[4]);
+    for (int c = 1; c < 4; ++c) Fhat[c] = fma(dm[c - 1], hps, fma(f2d(qs[c]), hsun, f2d(x[c])));
+    Fhat[4] = fma(f2d(qs[4]), hsun, f2d(x[4]));
 }
 
 // Sixth-order correction of a face flux from the node fluxes f[0..5]

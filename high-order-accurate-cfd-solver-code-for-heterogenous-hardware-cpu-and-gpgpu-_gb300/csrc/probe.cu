@@ -1,12 +1,91 @@
-// probe.cu -- measured arithmetic peaks (cfd_probe_flops), a public
-// diagnostic: the FP64 path is bounded by the FP64 pipe and the reduced
-// forms partly by FP32, so their roofline denominators are measured here:
+// probe.cu -- public diagnostics.  cfd_probe_flops: measured arithmetic
+// peaks; the FP64 path is bounded by the FP64 pipe and the reduced forms
+// partly by FP32, so their roofline denominators are measured here:
 // independent FMA chains (8 per thread, no memory traffic), timed with CUDA
 // events.  HBM bandwidth and tensor throughput are measured elsewhere.
+// cfd_probe_emu64: the integer-pipe binary64 routines (emu64.cuh) against
+// the hardware instructions on seeded operands.
+#include "emu64.cuh"
 #include "internal.h"
 
 namespace cfd {
 namespace {
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z)
+{
+    z += 0x9e3779b97f4a7c15ULL;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    return z ^ (z >> 31);
+}
+
+// A seeded binary64 operand of class cls: 0 everyday magnitudes, 1 the full
+// exponent range, 2 sparse significands (rounding ties), 3 zeros,
+// subnormals, infinities, NaN and the ends of the range, 4 around the
+// binary32 range (for the conversions); 5 (second operand only) close to
+// minus the first (cancellation).
+__device__ double operand(uint64_t &st, int cls, double first, bool second)
+{
+    const uint64_t r = mix64(st++), r2 = mix64(st++);
+    const uint64_t sign = (r2 & 1u) << 63;
+    uint64_t man = r & emu::kFrac, ex;
+    switch (cls) {
+    case 0: ex = 1000 + (r2 >> 8) % 47; break;
+    case 1: ex = 1 + (r2 >> 8) % 2046; break;
+    case 2:
+        man &= mix64(st++) & mix64(st++);
+        ex = 980 + (r2 >> 8) % 87;
+        break;
+    case 3: {
+        const int k = (int)((r2 >> 8) % 8);
+        if (k == 0) return 0.0;
+        if (k == 1) return -0.0;
+        if (k == 2) return emu::f64(sign | man);
+        if (k == 3) return emu::f64(sign | (0x7ffULL << 52));
+        if (k == 4) return emu::f64(0x7ff8000000000000ULL | man);
+        ex = k == 5 ? 1 + (r2 >> 12) % 60 : (k == 6 ? 2046 - (r2 >> 12) % 60 : 1000 + (r2 >> 8) % 47);
+        break;
+    }
+    case 4: ex = 860 + (r2 >> 8) % 330; break;
+    default: {
+        if (!second) {
+            ex = 1000 + (r2 >> 8) % 47;
+            break;
+        }
+        const uint64_t uo = emu::u64(first);
+        const uint64_t eo = ((uo >> 52) & 0x7ff) + (uint64_t)((r2 >> 8) % 3) - 1;
+        const uint64_t pert = (r >> 3) & ((1ull << ((r2 >> 16) % 53)) - 1);
+        return emu::f64(((~uo) & emu::kSign) | (eo << 52) | (((uo & emu::kFrac) ^ pert) & emu::kFrac));
+    }
+    }
+    return emu::f64(sign | (ex << 52) | man);
+}
+
+__device__ __forceinline__ bool same64(double x, double y) { return (x != x && y != y) || emu::u64(x) == emu::u64(y); }
+__device__ __forceinline__ bool same32(float x, float y)
+{
+    return (x != x && y != y) || __float_as_uint(x) == __float_as_uint(y);
+}
+
+// per thread `per` operand pairs of class cls; bad[0..3] count the
+// mismatches of f2d, d2f, add/sub and mul
+__global__ void k_emu_check(int cls, uint64_t seed, int per, unsigned long long *bad)
+{
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint64_t st = mix64(seed ^ (t * 0x632be59bd9b4e019ULL) ^ ((uint64_t)cls << 56));
+    unsigned long long nb[4] = {0, 0, 0, 0};
+    for (int i = 0; i < per; ++i) {
+        const double a = operand(st, cls, 0.0, false);
+        const double b = operand(st, cls, a, true);
+        const float fa = __uint_as_float((uint32_t)mix64(st++));   // every binary32 bit pattern
+        nb[0] += !same64(emu::f2d(fa), (double)fa) + !same64(emu::f2d(__double2float_rn(a)), (double)__double2float_rn(a));
+        nb[1] += !same32(emu::d2f(a), __double2float_rn(a)) + !same32(emu::d2f(b), __double2float_rn(b));
+        nb[2] += !same64(emu::add(a, b), __dadd_rn(a, b)) + !same64(emu::sub(a, b), __dsub_rn(a, b));
+        nb[3] += !same64(emu::mul(a, b), __dmul_rn(a, b));
+    }
+    for (int k = 0; k < 4; ++k)
+        if (nb[k]) atomicAdd(bad + k, nb[k]);
+}
 
 template <class T>
 __global__ void __launch_bounds__(256) k_fma_chain(int iters, T b, T c, T *out)
@@ -63,4 +142,28 @@ extern "C" cfd_status_t cfd_probe_flops(cfd_ctx_t *ctx, int32_t fp64, double *fl
     cfd_status_t s = cfd::use_device(ctx);
     if (s != CFD_OK) return s;
     return fp64 ? cfd::run_probe<double>(ctx, 2048, flops_per_s) : cfd::run_probe<float>(ctx, 65536, flops_per_s);
+}
+
+extern "C" cfd_status_t cfd_probe_emu64(cfd_ctx_t *ctx, int64_t n_per_class, uint64_t seed, int64_t mismatches[4])
+{
+    if (!ctx || !mismatches || n_per_class < 1) return CFD_EINVAL;
+    cfd_status_t s = cfd::use_device(ctx);
+    if (s != CFD_OK) return s;
+    const int threads = 256;
+    const int per = 64;
+    const long long blocks = (n_per_class + (long long)threads * per - 1) / ((long long)threads * per);
+    if (blocks > (1LL << 30)) return CFD_EINVAL;
+    unsigned long long *bad = nullptr;
+    cudaError_t e = cudaMalloc(&bad, 4 * sizeof(unsigned long long));
+    if (e != cudaSuccess) return cfd::cuda_fail(ctx, e, "cfd_probe_emu64 alloc");
+    cudaMemsetAsync(bad, 0, 4 * sizeof(unsigned long long), ctx->stream);
+    for (int cls = 0; cls < 6; ++cls) cfd::k_emu_check<<<(unsigned)blocks, threads, 0, ctx->stream>>>(cls, seed, per, bad);
+    ctx->launches += 6;
+    unsigned long long h[4] = {0, 0, 0, 0};
+    e = cudaMemcpyAsync(h, bad, sizeof h, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(bad);
+    if (e != cudaSuccess) return cfd::cuda_fail(ctx, e, "cfd_probe_emu64");
+    for (int k = 0; k < 4; ++k) mismatches[k] = (int64_t)h[k];
+    return CFD_OK;
 }

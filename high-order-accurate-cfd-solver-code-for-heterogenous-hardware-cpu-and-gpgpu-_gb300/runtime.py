@@ -90,6 +90,14 @@ class Context:
         self.check(self.lib.cfd_probe_flops(self.h, 1 if fp64 else 0, C.byref(out)), "cfd_probe_flops")
         return out.value
 
+    def probe_emu64(self, n_per_class: int = 1 << 22, seed: int = 1) -> tuple:
+        """Mismatch counts (f2d, d2f, add/sub, mul) of the integer-pipe
+        binary64 routines against the device's instructions
+        (cfd_probe_emu64); all zero on a correct build."""
+        out = (C.c_int64 * 4)()
+        self.check(self.lib.cfd_probe_emu64(self.h, int(n_per_class), int(seed), out), "cfd_probe_emu64")
+        return tuple(int(v) for v in out)
+
     def set_rows(self, n_rows: int):
         self.check(self.lib.cfd_ctx_set_rows(self.h, int(n_rows)), "cfd_ctx_set_rows")
 
