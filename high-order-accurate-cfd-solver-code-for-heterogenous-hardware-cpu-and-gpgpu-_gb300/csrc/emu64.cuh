@@ -81,6 +81,34 @@ __device__ __forceinline__ float d2f(double x)
     return __uint_as_float((hi & 0x80000000u) | (((e - 896u) << 23) + m23 + up));
 }
 
+// The double-float pair of x: hi = (float)x (round to nearest even) and
+// lo = (float)(x - hi) -- the same bits as those two conversions with the
+// FP64 subtraction between them, which is exact.  For a biased exponent e in
+// [950, 1099] the 29 significand bits below hi's 23 give the difference
+// directly: D = those bits, less 2^29 when hi rounded up, is an integer of
+// at most 29 bits with x - hi = sign(x) D 2^(e - 1075); its float (one
+// rounding, the only one) scaled by that power of two is lo.  Other
+// exponents take the conversions.
+__device__ __forceinline__ void hi_lo(double x, float &hi, float &lo)
+{
+    const uint64_t u = u64(x);
+    const uint32_t hw = (uint32_t)(u >> 32), lw = (uint32_t)u;
+    const uint32_t e = (hw >> 20) & 0x7ffu;
+    if (__builtin_expect(e - 950u >= 150u, 0)) {
+        hi = d2f(x);
+        lo = d2f(x - f2d(hi));
+        return;
+    }
+    const uint32_t m23 = ((hw & 0xfffffu) << 3) | (lw >> 29);
+    const uint32_t r = lw & 0x1fffffffu;
+    const uint32_t up = (uint32_t)(r > 0x10000000u) | ((uint32_t)(r == 0x10000000u) & m23 & 1u);
+    hi = __uint_as_float((hw & 0x80000000u) | (((e - 896u) << 23) + m23 + up));
+    const int D = (int)r - (int)(up << 29);
+    const float f = __int2float_rn(D);   // |D| <= 2^28: a normal float, rounded once
+    lo = D == 0 ? 0.0f
+                : __uint_as_float((__float_as_uint(f) + ((e - 1075u) << 23)) ^ (hw & 0x80000000u));
+}
+
 // a + b.  With |X| >= |Y| (exponents ex >= ey, d = ex - ey) the
 // significands, shifted left by 10 (leading bit at 62, ten guard bits), are
 // aligned by d with the bits shifted out of Y collected in bit 0 (sticky).

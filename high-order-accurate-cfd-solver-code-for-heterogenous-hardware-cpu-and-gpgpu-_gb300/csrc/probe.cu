@@ -68,7 +68,7 @@ __device__ __forceinline__ bool same32(float x, float y)
 }
 
 // per thread `per` operand pairs of class cls; bad[0..3] count the
-// mismatches of f2d, d2f, add/sub and mul
+// mismatches of f2d, d2f (and the hi/lo split), add/sub and mul
 __global__ void k_emu_check(int cls, uint64_t seed, int per, unsigned long long *bad)
 {
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -80,6 +80,13 @@ __global__ void k_emu_check(int cls, uint64_t seed, int per, unsigned long long 
         const float fa = __uint_as_float((uint32_t)mix64(st++));   // every binary32 bit pattern
         nb[0] += !same64(emu::f2d(fa), (double)fa) + !same64(emu::f2d(__double2float_rn(a)), (double)__double2float_rn(a));
         nb[1] += !same32(emu::d2f(a), __double2float_rn(a)) + !same32(emu::d2f(b), __double2float_rn(b));
+        {
+            float h, l;
+            emu::hi_lo(a, h, l);
+            const float hn = __double2float_rn(a);
+            const float ln = __double2float_rn(__dsub_rn(a, (double)hn));
+            nb[1] += !same32(h, hn) + !same32(l, ln);
+        }
         nb[2] += !same64(emu::add(a, b), __dadd_rn(a, b)) + !same64(emu::sub(a, b), __dsub_rn(a, b));
         nb[3] += !same64(emu::mul(a, b), __dmul_rn(a, b));
     }
