@@ -19,7 +19,10 @@
 // exponents near the range ends, or a failed test -- takes the IEEE division
 // x / b itself.  The results are therefore identical to x / b for all
 // inputs; the gain is 4 FP64 instructions per shared division instead of a
-// full division sequence.
+// full division sequence.  quotient_int goes further on a part whose FP64
+// rate is a small fraction of its integer rate: only q0 on the FP64 pipe,
+// its rounding decided from the exact integer remainder of the significands
+// (the default of div()).
 #pragma once
 
 #include <cstdint>
@@ -99,11 +102,49 @@ static __host__ __device__ __noinline__ double ieee_div(double x, double b) { re
 static double ieee_div(double x, double b) { return x / b; }
 #endif
 
+// x / b given y = 1 / b (IEEE), with the rounding decided on the integer
+// pipe.  q0 = RN(x*y) lies within two ulps of x/b.  With significands X, B,
+// Q (53-bit integers, hidden bit set) and s = ex - eb - eq + 1075 (52 or 53
+// in the plain case), X*2^s and Q*B are the dividend and q0 times the
+// divisor on a common scale, so R = X*2^s - Q*B is the exact remainder
+// (|R| < 2^56: the low 64 bits of both products give it).  x/b is
+// (Q + R/B) ulps, never exactly halfway between two doubles, so the
+// correctly rounded quotient is q0 moved by the nearest integer to R/B,
+// found by comparing 2R with +-B and +-3B.  The plain case: x, q0 and
+// 1/b normal (b below 2^1022), the significand of q0 in
+// [2^52 + 3, 2^53 - 2] (a step of up to two ulps then rounds within the
+// binade, or lands exactly on its upper end) and |R/B| < 5/2 (it is at most
+// 3/2 when y = RN(1/b)); everything else takes the division.  One FP64
+// multiply instead of the four FP64 operations of quotient().
+CFD_XDIV_HD double quotient_int(double x, double b, double y, bool &ok)
+{
+    const double q0 = mul_rn(x, y);
+    const uint64_t ux = bits(x), ub = bits(b), uq = bits(q0);
+    const int ex = (int)((ux >> 52) & 0x7ff), eb = (int)((ub >> 52) & 0x7ff), eq = (int)((uq >> 52) & 0x7ff);
+    const uint64_t X = (ux & 0x000fffffffffffffULL) | 0x0010000000000000ULL;
+    const uint64_t B = (ub & 0x000fffffffffffffULL) | 0x0010000000000000ULL;
+    const uint64_t F = uq & 0x000fffffffffffffULL;
+    const int s = ex - eb - eq + 1075;
+    const int64_t R = (int64_t)((X << (s & 63)) - (F | 0x0010000000000000ULL) * B);
+    const int64_t R2 = R * 2, Bs = (int64_t)B, B3 = 3 * (int64_t)B;
+    const int d = (int)(R2 > Bs) + (int)(R2 > B3) - (int)(R2 < -Bs) - (int)(R2 < -B3);
+    ok = (unsigned)(ex - 1) < 2046u && (unsigned)(eb - 1) < 2044u && (unsigned)(eq - 1) < 2045u
+         && (unsigned)(s - 52) < 2u && F - 3u < 0x000ffffffffffffcULL && R2 < 5 * Bs && R2 > -5 * Bs;
+    return from_bits(uq + (uint64_t)(int64_t)d);
+}
+
+// Which plain-case quotient div() uses: the integer-pipe rounding
+// (quotient_int, 1 FP64 operation; GB300 TGV 128^3: face pass 7.72 ->
+// 6.80 ms) or the FP64 Markstein step (quotient, 4).
+#ifndef CFD_XDIV_INT
+#define CFD_XDIV_INT 1
+#endif
+
 // x / b given y = 1 / b (IEEE): the same bits as x / b.
 CFD_XDIV_HD double div(double x, double b, double y)
 {
     bool ok;
-    const double q = quotient(x, b, y, ok);
+    const double q = CFD_XDIV_INT ? quotient_int(x, b, y, ok) : quotient(x, b, y, ok);
     if (__builtin_expect(ok, 1)) return q;
     return ieee_div(x, b);
 }

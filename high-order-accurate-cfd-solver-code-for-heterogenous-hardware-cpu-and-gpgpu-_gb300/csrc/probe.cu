@@ -6,6 +6,7 @@
 // cfd_probe_emu64: the integer-pipe binary64 routines (emu64.cuh) against
 // the hardware instructions on seeded operands.
 #include "emu64.cuh"
+#include "exact_div.cuh"
 #include "internal.h"
 
 namespace cfd {
@@ -67,13 +68,15 @@ __device__ __forceinline__ bool same32(float x, float y)
     return (x != x && y != y) || __float_as_uint(x) == __float_as_uint(y);
 }
 
-// per thread `per` operand pairs of class cls; bad[0..3] count the
-// mismatches of f2d, d2f (and the hi/lo split), add/sub and mul
+// per thread `per` operand pairs of class cls; bad[0..4] count the
+// mismatches of f2d, d2f (and the hi/lo split), add/sub, mul and the
+// division from a shared reciprocal (xdiv::quotient_int where it accepts the
+// operands, and xdiv::div)
 __global__ void k_emu_check(int cls, uint64_t seed, int per, unsigned long long *bad)
 {
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint64_t st = mix64(seed ^ (t * 0x632be59bd9b4e019ULL) ^ ((uint64_t)cls << 56));
-    unsigned long long nb[4] = {0, 0, 0, 0};
+    unsigned long long nb[5] = {0, 0, 0, 0, 0};
     for (int i = 0; i < per; ++i) {
         const double a = operand(st, cls, 0.0, false);
         const double b = operand(st, cls, a, true);
@@ -89,8 +92,15 @@ __global__ void k_emu_check(int cls, uint64_t seed, int per, unsigned long long 
         }
         nb[2] += !same64(emu::add(a, b), __dadd_rn(a, b)) + !same64(emu::sub(a, b), __dsub_rn(a, b));
         nb[3] += !same64(emu::mul(a, b), __dmul_rn(a, b));
+        {
+            const double y = 1.0 / b;
+            bool ok;
+            const double q = xdiv::quotient_int(a, b, y, ok);
+            nb[4] += ok && !same64(q, a / b);
+            nb[4] += !same64(xdiv::div(a, b, y), a / b);
+        }
     }
-    for (int k = 0; k < 4; ++k)
+    for (int k = 0; k < 5; ++k)
         if (nb[k]) atomicAdd(bad + k, nb[k]);
 }
 
@@ -151,7 +161,7 @@ extern "C" cfd_status_t cfd_probe_flops(cfd_ctx_t *ctx, int32_t fp64, double *fl
     return fp64 ? cfd::run_probe<double>(ctx, 2048, flops_per_s) : cfd::run_probe<float>(ctx, 65536, flops_per_s);
 }
 
-extern "C" cfd_status_t cfd_probe_emu64(cfd_ctx_t *ctx, int64_t n_per_class, uint64_t seed, int64_t mismatches[4])
+extern "C" cfd_status_t cfd_probe_emu64(cfd_ctx_t *ctx, int64_t n_per_class, uint64_t seed, int64_t mismatches[5])
 {
     if (!ctx || !mismatches || n_per_class < 1) return CFD_EINVAL;
     cfd_status_t s = cfd::use_device(ctx);
@@ -161,16 +171,16 @@ extern "C" cfd_status_t cfd_probe_emu64(cfd_ctx_t *ctx, int64_t n_per_class, uin
     const long long blocks = (n_per_class + (long long)threads * per - 1) / ((long long)threads * per);
     if (blocks > (1LL << 30)) return CFD_EINVAL;
     unsigned long long *bad = nullptr;
-    cudaError_t e = cudaMalloc(&bad, 4 * sizeof(unsigned long long));
+    cudaError_t e = cudaMalloc(&bad, 5 * sizeof(unsigned long long));
     if (e != cudaSuccess) return cfd::cuda_fail(ctx, e, "cfd_probe_emu64 alloc");
-    cudaMemsetAsync(bad, 0, 4 * sizeof(unsigned long long), ctx->stream);
+    cudaMemsetAsync(bad, 0, 5 * sizeof(unsigned long long), ctx->stream);
     for (int cls = 0; cls < 6; ++cls) cfd::k_emu_check<<<(unsigned)blocks, threads, 0, ctx->stream>>>(cls, seed, per, bad);
     ctx->launches += 6;
-    unsigned long long h[4] = {0, 0, 0, 0};
+    unsigned long long h[5] = {0, 0, 0, 0, 0};
     e = cudaMemcpyAsync(h, bad, sizeof h, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     cudaFree(bad);
     if (e != cudaSuccess) return cfd::cuda_fail(ctx, e, "cfd_probe_emu64");
-    for (int k = 0; k < 4; ++k) mismatches[k] = (int64_t)h[k];
+    for (int k = 0; k < 5; ++k) mismatches[k] = (int64_t)h[k];
     return CFD_OK;
 }

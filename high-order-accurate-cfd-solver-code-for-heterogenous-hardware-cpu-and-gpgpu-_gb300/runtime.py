@@ -91,10 +91,10 @@ class Context:
         return out.value
 
     def probe_emu64(self, n_per_class: int = 1 << 22, seed: int = 1) -> tuple:
-        """Mismatch counts (f2d, d2f, add/sub, mul) of the integer-pipe
-        binary64 routines against the device's instructions
-        (cfd_probe_emu64); all zero on a correct build."""
-        out = (C.c_int64 * 4)()
+        """Mismatch counts (f2d, d2f, add/sub, mul, shared-reciprocal
+        division) of the integer-pipe binary64 routines against the device's
+        instructions (cfd_probe_emu64); all zero on a correct build."""
+        out = (C.c_int64 * 5)()
         self.check(self.lib.cfd_probe_emu64(self.h, int(n_per_class), int(seed), out), "cfd_probe_emu64")
         return tuple(int(v) for v in out)
 

@@ -489,19 +489,20 @@ cfd_status_t cfd_half_point_metrics(const cfd_grid_t *grid, int32_t n_rows, int3
  * of the device's FP64 or FP32 peak (the FP64 roofline of the RHS path). */
 cfd_status_t cfd_probe_flops(cfd_ctx_t *ctx, int32_t fp64, double *flops_per_s);
 /* A public diagnostic with no counterpart in the reference: the library's
- * integer-pipe binary64 routines (the exact FP32 -> FP64 conversion, the
+ * integer-pipe binary64 routines -- the exact FP32 -> FP64 conversion, the
  * round-to-nearest FP64 -> FP32 conversion and the double-float split
- * hi = (float)x, lo = (float)(x - hi), FP64 add, subtract and
- * multiply, which the split precision form uses to keep its conversions off
- * the FP64 pipe) against the device's own instructions on about
- * n_per_class seeded operand pairs in each of six classes (everyday
+ * hi = (float)x, lo = (float)(x - hi), FP64 add, subtract and multiply
+ * (the split precision form keeps its conversions off the FP64 pipe with
+ * them), and the division x / b from a reciprocal shared between
+ * numerators (the FP64 form) -- against the device's own instructions on
+ * about n_per_class seeded operand pairs in each of six classes (everyday
  * magnitudes, the full exponent range, sparse significands that produce
  * rounding ties, zeros / subnormals / infinities / NaN / range ends, values
- * around the binary32 range, near cancellation).  mismatches[0..3] receive
+ * around the binary32 range, near cancellation).  mismatches[0..4] receive
  * the counts of results whose bits differ, for f2d, d2f (with the split),
- * add/sub and mul
- * (NaN matches NaN); all four are 0 on a correct build. */
-cfd_status_t cfd_probe_emu64(cfd_ctx_t *ctx, int64_t n_per_class, uint64_t seed, int64_t mismatches[4]);
+ * add/sub, mul and the shared-reciprocal division (NaN matches NaN); all
+ * five are 0 on a correct build. */
+cfd_status_t cfd_probe_emu64(cfd_ctx_t *ctx, int64_t n_per_class, uint64_t seed, int64_t mismatches[5]);
 
 /* ------------------------------------------- allocation-free RK3 stage -- */
 /* No counterpart in the reference.  For callers that must not allocate
