@@ -9,10 +9,11 @@ namespace cfd {
 namespace {
 
 // 1: shared reciprocals in the face flux (exact_div.cuh), as in the
-// single-lattice kernels.  Plain divisions measured faster here (64
-// vortices: 2.12e7 against 1.92e7 cell-updates/s; same bits either way).
+// single-lattice kernels; 0: a division per quotient.  Same bits either
+// way; with the quotients' rounding on the integer pipe the shared form is
+// the faster here too (64 vortices: 2.30e7 against 2.15e7 cell-updates/s).
 #ifndef CFD_FBATCH_SHARED_DIV
-#define CFD_FBATCH_SHARED_DIV 0
+#define CFD_FBATCH_SHARED_DIV 1
 #endif
 
 struct Ops {

@@ -133,6 +133,64 @@ CFD_XDIV_HD double quotient_int(double x, double b, double y, bool &ok)
     return from_bits(uq + (uint64_t)(int64_t)d);
 }
 
+#if defined(__CUDACC__)
+// 1 / b rounded to nearest even, for b whose reciprocal is a normal number
+// (biased exponent eb in [1, 2044]) and whose significand B is not a power
+// of two (that reciprocal is exact and returned directly): a float
+// reciprocal of B's top 24 bits seeds one Newton step on the FP64 pipe,
+//   e = RN(1 - |b| y0),  y1 = RN(y0 e + y0)   (relative error ~2^-47),
+// and the rounding is then decided on the integer pipe: with Y the
+// significand of y1, R = 2^105 - Y*B is the exact remainder (|R| < 2^61:
+// the seed is within 1.5 2^-23 and the step squares that, so the low 64
+// bits of the product give it), R/B is estimated from the top
+// bits of R and Y (Y ~ 2^105 / B), the estimate's remainder R1 is exact, and
+// Y moves by the nearest integer to R/B (2^105 / B is never halfway between
+// two integers).  ok = false (and the caller divides) outside that case.
+__device__ __forceinline__ double rcp_int(double b, bool &ok)
+{
+    const uint64_t ub = bits(b);
+    const int eb = (int)((ub >> 52) & 0x7ff);
+    const uint64_t F = ub & 0x000fffffffffffffULL, B = F | 0x0010000000000000ULL;
+    const uint64_t sign = ub & 0x8000000000000000ULL;
+    const float rf = __frcp_rn(__uint_as_float(0x3f800000u | (uint32_t)(F >> 29)));   // ~ 2^52 / B, in (0.5, 1]
+    const uint32_t rb = __float_as_uint(rf);
+    const int ey0 = (int)(rb >> 23) - 127 + 2046 - eb;   // biased exponent of rf * 2^(1023 - eb)
+    const double y0 = from_bits(((uint64_t)(unsigned)ey0 << 52) | ((uint64_t)(rb & 0x7fffffu) << 29));
+    const double e = fma_rn(-from_bits(ub & 0x7fffffffffffffffULL), y0, 1.0);
+    const double y1 = fma_rn(y0, e, y0);
+    const uint64_t u1 = bits(y1);
+    const uint64_t Y = (u1 & 0x000fffffffffffffULL) | 0x0010000000000000ULL;
+    const int64_t R = (int64_t)(0ULL - Y * B);
+    const int64_t d0 = ((R >> 29) * (int64_t)(Y >> 23)) >> 53;   // < 2^62 before the shift
+    const int64_t R1 = R - d0 * (int64_t)B;
+    const int64_t R2 = 2 * R1, Bs = (int64_t)B;
+    const int64_t d = d0 + (int64_t)(R2 > Bs) + (int64_t)(R2 > 3 * Bs) - (int64_t)(R2 < -Bs);
+    const uint64_t Yn = Y + (uint64_t)d;
+    ok = (unsigned)(eb - 1) < 2044u && F != 0 && (int)((u1 >> 52) & 0x7ff) == 2045 - eb && R2 < 5 * Bs
+         && R2 > -5 * Bs && (Yn >> 52) == 1u;
+    return from_bits(sign | ((uint64_t)(2045 - eb) << 52) | (Yn & 0x000fffffffffffffULL));
+}
+#endif
+
+// 1 / b, the same bits as the IEEE division (rcp_int's plain case on the
+// device when CFD_XDIV_RCP is set -- the default; GB300 TGV 128^3: FP64
+// face pass 6.62 -> 6.42 ms -- else the division).
+#ifndef CFD_XDIV_RCP
+#define CFD_XDIV_RCP 1
+#endif
+CFD_XDIV_HD double rcp(double b)
+{
+#if defined(__CUDA_ARCH__)
+    if (CFD_XDIV_RCP) {
+        bool ok;
+        const double y = rcp_int(b, ok);
+        if (__builtin_expect(ok, 1)) return y;
+        return ieee_div(1.0, b);
+    }
+#endif
+    return 1.0 / b;
+}
+
 // Which plain-case quotient div() uses: the integer-pipe rounding
 // (quotient_int, 1 FP64 operation; GB300 TGV 128^3: face pass 7.72 ->
 // 6.80 ms) or the FP64 Markstein step (quotient, 4).
@@ -148,6 +206,10 @@ CFD_XDIV_HD double div(double x, double b, double y)
     if (__builtin_expect(ok, 1)) return q;
     return ieee_div(x, b);
 }
+
+// x / b for a divisor used once: its reciprocal (rcp) and the quotient's
+// rounding (div); the same bits as x / b.
+CFD_XDIV_HD double divide(double x, double b) { return div(x, b, rcp(b)); }
 
 // The IEEE product, out of line (scale2's rare case).
 #if defined(__CUDACC__)
@@ -195,7 +257,7 @@ CFD_XDIV_HD double pow2_over(double x)
     constexpr unsigned lo = K < 0 ? 2u + (unsigned)(-K) : 2u;
     constexpr unsigned hi = K > 0 ? 2045u - (unsigned)K : 2045u;
     constexpr double c = K > 0 ? (double)(1u << (K > 0 ? K : 0)) : 1.0 / (double)(1u << (K < 0 ? -K : 0));
-    const double r = 1.0 / x;
+    const double r = rcp(x);
     const uint64_t u = bits(r);
     const unsigned e = (unsigned)(u >> 52) & 0x7ffu;
     if (__builtin_expect(e - lo <= hi - lo, 1)) return from_bits(u + ((uint64_t)(int64_t)K << 52));

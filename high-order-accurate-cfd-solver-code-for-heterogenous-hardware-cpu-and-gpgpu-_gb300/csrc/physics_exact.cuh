@@ -10,8 +10,11 @@
 // are compiled with --fmad=false.  With IEEE-correct division and square
 // root on the GPU this reproduces the reference's results to the last bit
 // except where libm functions differ (cbrt).  Divisions that share a divisor
-// use one IEEE reciprocal and an exactly checked correction (exact_div.cuh,
-// `Over`): the same bits as the division, for fewer FP64 instructions.
+// use one reciprocal and an exactly checked correction (exact_div.cuh,
+// `Over`), and the reciprocals, the corrections and the single divisions
+// decide their rounding from exact integer remainders: the same bits as the
+// division, with most of the work moved from the FP64 pipe (two operations
+// per clock per SM on GB300) to the integer pipes.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -34,7 +37,7 @@ struct Over;
 template <>
 struct Over<true> {
     double b, y;
-    __device__ __forceinline__ explicit Over(double divisor) : b(divisor), y(1.0 / divisor) {}
+    __device__ __forceinline__ explicit Over(double divisor) : b(divisor), y(xdiv::rcp(divisor)) {}
     __device__ __forceinline__ double operator()(double x) const { return xdiv::div(x, b, y); }
 };
 
@@ -44,6 +47,14 @@ struct Over<false> {
     __device__ __forceinline__ explicit Over(double divisor) : b(divisor) {}
     __device__ __forceinline__ double operator()(double x) const { return x / b; }
 };
+
+// a / b with the same bits: xdiv::divide (reciprocal and quotient rounding
+// on the integer pipe) when CFD_EXACT_DIVIDE is set (the default), else the
+// division.
+#ifndef CFD_EXACT_DIVIDE
+#define CFD_EXACT_DIVIDE 1
+#endif
+__device__ __forceinline__ double dv(double a, double b) { return CFD_EXACT_DIVIDE ? xdiv::divide(a, b) : a / b; }
 
 // U_Q.cl:64-65
 __device__ __forceinline__ double enthalpy(double rho, double u, double v, double w, double p)
@@ -85,10 +96,10 @@ __device__ __forceinline__ void weno_pair(const double cc[6], double eps, double
     const double ISp1 = (13.0 / 12.0) * (sq(c[0] - scale2<1>(c[1]) + c[2])) + scale2<-2>(sq(c[0] - c[2]));
     const double ISp0 = (13.0 / 12.0) * (sq(c[1] - scale2<1>(c[2]) + c[3])) + scale2<-2>(sq(3.0 * c[1] - scale2<2>(c[2]) + c[3]));
     const double wp0 = xdiv::pow2_over<-4>(sq(eps + (ISp0)));   // (1/16) / ...
-    const double wp1 = (5.0 / 8.0) / (sq(eps + (ISp1)));
-    const double wp2 = (5.0 / 16.0) / (sq(eps + (ISp2)));
-    const double wm0 = (5.0 / 16.0) / (sq(eps + (ISm0)));
-    const double wm1 = (5.0 / 8.0) / (sq(eps + (ISm1)));
+    const double wp1 = dv(5.0 / 8.0, sq(eps + (ISp1)));
+    const double wp2 = dv(5.0 / 16.0, sq(eps + (ISp2)));
+    const double wm0 = dv(5.0 / 16.0, sq(eps + (ISm0)));
+    const double wm1 = dv(5.0 / 8.0, sq(eps + (ISm1)));
     const double wm2 = xdiv::pow2_over<-4>(sq(eps + (ISm2)));   // (1/16) / ...
     const Over<SD> sp(wp0 + wp1 + wp2), sm(wm0 + wm1 + wm2);
     const double Wp0 = sp(wp0), Wp1 = sp(wp1), Wp2 = sp(wp2);
@@ -149,7 +160,7 @@ __device__ __forceinline__ void cart_flux(const double q[5], const StateQuot &t,
 __device__ __forceinline__ double lambda5(const double q[5], const StateQuot &t, double mx, double my, double mz)
 {
     return (mx * t.v1 + my * t.v2 + mz * t.v3)
-           + sqrt(1.4 * 0.4 * (t.v4 - ((q[1] * q[1] + q[2] * q[2] + q[3] * q[3]) / xdiv::scale2<1>(q[0] * q[0])))
+           + sqrt(1.4 * 0.4 * (t.v4 - dv(q[1] * q[1] + q[2] * q[2] + q[3] * q[3], xdiv::scale2<1>(q[0] * q[0])))
                   * (mx * mx + my * my + mz * mz));
 }
 
@@ -168,8 +179,8 @@ __device__ __forceinline__ void face_flux(const double pts[6][5], double mx, dou
     const double kx = dk(mx), ky = dk(my), kz = dk(mz);
     const double theta = kx * ru + ky * rv + kz * rw;
     const double phi_sq = 0.5 * 0.4 * (ru * ru + rv * rv + rw * rw);
-    const double alpha = rrho / (sqrt(2.0) * a);
-    const double beta = 1.0 / (sqrt(2.0) * rrho * a);
+    const double alpha = dv(rrho, sqrt(2.0) * a);
+    const double beta = dv(1.0, sqrt(2.0) * rrho * a);
     double cpos[5], cneg[5];
     {
         const Over<SD> da(a * a), dr(rrho);

@@ -98,6 +98,9 @@ __global__ void k_emu_check(int cls, uint64_t seed, int per, unsigned long long 
             const double q = xdiv::quotient_int(a, b, y, ok);
             nb[4] += ok && !same64(q, a / b);
             nb[4] += !same64(xdiv::div(a, b, y), a / b);
+            const double yi = xdiv::rcp_int(b, ok);
+            nb[4] += ok && !same64(yi, y);
+            nb[4] += !same64(xdiv::rcp(b), y) + !same64(xdiv::divide(a, b), a / b);
         }
     }
     for (int k = 0; k < 5; ++k)

@@ -27,12 +27,16 @@
 #include "lattice_fp64.cuh"
 #include "structured.h"
 
-// Minimum resident blocks per SM requested for the FP64 face kernel (its
-// register budget): 3 (168 registers at 128 threads per block, 88 B of
-// spill) runs the pass 3 % faster than 2 (230 registers, none) on GB300
-// once the quotients' rounding is on the integer pipe.
+// Minimum resident blocks per SM requested for the FP64 face kernels (their
+// register budget) along i and j, and along k: with the divisions' rounding
+// on the integer pipe, 3 (168 registers at 128 threads per block) runs the
+// i and j passes fastest on GB300 (TGV 128^3: 6.24 ms against 6.71 at 2),
+// 2 the k pass (6.34 against 6.75 ms; its stencil strides a whole plane).
 #ifndef CFD_FACE_MIN_BLOCKS
 #define CFD_FACE_MIN_BLOCKS 3
+#endif
+#ifndef CFD_FACE_K_MIN_BLOCKS
+#define CFD_FACE_K_MIN_BLOCKS 2
 #endif
 
 namespace cfd {
@@ -60,7 +64,7 @@ __global__ void __launch_bounds__(128) k_mu_only(LatView g, int q)
 }
 
 template <int D>
-__global__ void __launch_bounds__(128, CFD_FACE_MIN_BLOCKS) k_face(LatView g)
+__global__ void __launch_bounds__(128, D == 2 ? CFD_FACE_K_MIN_BLOCKS : CFD_FACE_MIN_BLOCKS) k_face(LatView g)
 {
     const int n = node_id();
     if (n < g.N) ex::face_node<D>(g, n);

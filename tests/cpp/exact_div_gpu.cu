@@ -1,6 +1,7 @@
 // exact_div_gpu.cu -- cfd::xdiv::div(x, b, 1/b) on the GPU against the GPU's
-// own IEEE division x / b, bit for bit, on the pairs of div_cases.h, and
-// cfd::xdiv::scale2<K>(x) against the GPU's x * 2^K on every x.
+// own IEEE division x / b, bit for bit, on the pairs of div_cases.h,
+// cfd::xdiv::scale2<K>(x) against the GPU's x * 2^K on every x, pow2_over,
+// and the integer-pipe reciprocal (rcp_int) and single division (divide).
 //
 //   exact_div_gpu <rounds> <seed>
 #include <cstdio>
@@ -16,6 +17,21 @@ __global__ void k_div(const double *x, const double *b, int n, double *want, dou
     const double y = 1.0 / b[i];
     want[i] = x[i] / b[i];
     got[i] = cfd::xdiv::div(x[i], b[i], y);
+}
+
+// the reciprocal of b[i] with its rounding on the integer pipe
+// (xdiv::rcp_int where it accepts b, else the division) and x / b through
+// xdiv::divide, against the GPU's 1.0 / b and x / b: out[2 * i + k]
+__global__ void k_rcp(const double *x, const double *b, int n, double *want, double *got)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    bool ok;
+    const double y = cfd::xdiv::rcp_int(b[i], ok);
+    got[2 * i + 0] = ok ? y : 1.0 / b[i];
+    want[2 * i + 0] = 1.0 / b[i];
+    got[2 * i + 1] = cfd::xdiv::divide(x[i], b[i]);
+    want[2 * i + 1] = x[i] / b[i];
 }
 
 // out[6 * i + k]: scale2 of x[i] by 2, 4, 8, 1/2, 1/4, 1/8 (got) and the
@@ -114,6 +130,18 @@ int main(int argc, char **argv)
     std::printf("pow2_over: %zu cases, %ld pow2_over mismatches (%s)\n", PW.size(), pfails, cudaGetErrorString(e3));
     sfails += pfails;
     if (e3 != cudaSuccess) e2 = e3;
+    // reciprocals and single divisions on the pairs (x, b), reusing the buffers (2n <= 6m entries)
+    k_rcp<<<(n + 255) / 256, 256>>>(dx, db, n, sw, sg);
+    std::vector<double> RW(2 * (size_t)n), RG(2 * (size_t)n);
+    cudaMemcpy(RW.data(), sw, RW.size() * 8, cudaMemcpyDeviceToHost);
+    cudaMemcpy(RG.data(), sg, RG.size() * 8, cudaMemcpyDeviceToHost);
+    const cudaError_t e4 = cudaDeviceSynchronize();
+    long rfails = 0;
+    for (size_t i = 0; i < RW.size(); ++i)
+        rfails += !(divcases::to_bits(RG[i]) == divcases::to_bits(RW[i]) || (std::isnan(RG[i]) && std::isnan(RW[i])));
+    std::printf("rcp/divide: %zu cases, %ld rcp mismatches (%s)\n", RW.size(), rfails, cudaGetErrorString(e4));
+    sfails += rfails;
+    if (e4 != cudaSuccess) e2 = e4;
     cudaFree(dv);
     cudaFree(dc);
     cudaFree(sw);
