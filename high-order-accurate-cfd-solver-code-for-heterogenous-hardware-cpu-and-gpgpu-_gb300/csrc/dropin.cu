@@ -144,12 +144,13 @@ __global__ void __launch_bounds__(128) k_uq(double *__restrict__ U, double *__re
     Ur[1] = D * rho * u;
     Ur[2] = D * rho * v;
     Ur[3] = D * rho * w;
-    Ur[4] = D * ((p / 0.4) + ke);
+    const double E = ex::dv(p, 0.4) + ke;
+    Ur[4] = D * E;
     Qr[0] = rho;
     Qr[1] = rho * u;
     Qr[2] = rho * v;
     Qr[3] = rho * w;
-    Qr[4] = ((p / 0.4) + ke);
+    Qr[4] = E;
 }
 
 // -------------------------------------------------------------- Viscous --

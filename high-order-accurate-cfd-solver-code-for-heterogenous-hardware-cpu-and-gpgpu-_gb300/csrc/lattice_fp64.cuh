@@ -21,7 +21,7 @@ __device__ __forceinline__ void prep_values(const LatView &g, int n, int q, doub
     const int N = g.N;
     const double D = g.det[n];
     const double ke = 0.5 * rho * (u * u + v * v + w * w);
-    const double E = (p / 0.4) + ke;
+    const double E = dv(p, 0.4) + ke;
     double *Uq = lat_U(g, q);
     g.Q[0 * N + n] = rho;
     g.Q[1 * N + n] = rho * u;

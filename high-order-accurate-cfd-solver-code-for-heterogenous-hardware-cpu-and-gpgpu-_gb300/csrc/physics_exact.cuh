@@ -59,7 +59,7 @@ __device__ __forceinline__ double dv(double a, double b) { return CFD_EXACT_DIVI
 // U_Q.cl:64-65
 __device__ __forceinline__ double enthalpy(double rho, double u, double v, double w, double p)
 {
-    return ((p / 0.4) + 0.5 * rho * (u * u + v * v + w * w) + p) / rho;
+    return dv((dv(p, 0.4) + 0.5 * rho * (u * u + v * v + w * w) + p), rho);
 }
 
 // U_Q.cl:60-109 for one face: {u, v, w, h, rho}; (sb,...) the neighbour.
@@ -278,38 +278,43 @@ __device__ __forceinline__ void viscous_node(const double dU[3][5], const double
     const double zeta_x = m[0], zeta_y = m[1], zeta_z = m[2], eta_x = m[3], eta_y = m[4], eta_z = m[5];
     const double xi_x = m[6], xi_y = m[7], xi_z = m[8];
     const double U0_I = Ui[0], U1_I = Ui[1], U2_I = Ui[2], U3_I = Ui[3], U4_I = Ui[4];
+    // the divisions by U0 and by U0^2 share their reciprocals (Over: the
+    // same bits as each division)
+    const Over<true> o1(U0_I), o2(U0_I * U0_I);
+    const double r0 = o1(1.0), a1 = o2(U1_I), a2 = o2(U2_I), a3 = o2(U3_I), a4 = o2(U4_I);
     double uc[3], vc[3], wc[3], tc[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        uc[d] = (1.0 / U0_I) * (dU[d][1]) - (U1_I / ((U0_I * U0_I))) * (dU[d][0]);
-        vc[d] = (1.0 / U0_I) * (dU[d][2]) - (U2_I / ((U0_I * U0_I))) * (dU[d][0]);
-        wc[d] = (1.0 / U0_I) * (dU[d][3]) - (U3_I / ((U0_I * U0_I))) * (dU[d][0]);
+        uc[d] = r0 * (dU[d][1]) - a1 * (dU[d][0]);
+        vc[d] = r0 * (dU[d][2]) - a2 * (dU[d][0]);
+        wc[d] = r0 * (dU[d][3]) - a3 * (dU[d][0]);
     }
+    const double v1 = o1(U1_I), v2 = o1(U2_I), v3 = o1(U3_I);
 #pragma unroll
     for (int d = 0; d < 3; ++d)
-        tc[d] = (1.0 / U0_I) * (dU[d][4]) - (U4_I / ((U0_I * U0_I))) * (dU[d][0]) - (U1_I / U0_I) * uc[d]
-                - (U2_I / U0_I) * vc[d] - (U3_I / U0_I) * wc[d];
+        tc[d] = r0 * (dU[d][4]) - a4 * (dU[d][0]) - v1 * uc[d] - v2 * vc[d] - v3 * wc[d];
     const double d_temp = (1.4 * Mach * Mach * 0.4
-                           * ((U4_I / U0_I) - xdiv::scale2<-1>(((U1_I * U1_I) / (U0_I * U0_I)) + ((U2_I * U2_I) / (U0_I * U0_I))
-                                                     + ((U3_I * U3_I) / (U0_I * U0_I)))));
+                           * (o1(U4_I) - xdiv::scale2<-1>(o2(U1_I * U1_I) + o2(U2_I * U2_I) + o2(U3_I * U3_I))));
     const double d_temp1 = sqrt(d_temp) * sqrt(d_temp) * sqrt(d_temp);
-    const double mu = (d_temp1) * ((1.0 + (110.4 / Free_t)) / (d_temp + (110.4 / Free_t)));
+    const double st = dv(110.4, Free_t);
+    const double mu = (d_temp1) * dv(1.0 + st, d_temp + st);
     mu_out = mu;
 #define GX(a) ((a)[0] * zeta_x + (a)[1] * eta_x + (a)[2] * xi_x)
 #define GY(a) ((a)[0] * zeta_y + (a)[1] * eta_y + (a)[2] * xi_y)
 #define GZ(a) ((a)[0] * zeta_z + (a)[1] * eta_z + (a)[2] * xi_z)
-    const double qz = (-1.0) * (mu * 1.4 / (Pr * Reyl)) * GX(tc);
-    const double qe = (-1.0) * (mu * 1.4 / (Pr * Reyl)) * GY(tc);
-    const double qx = (-1.0) * (mu * 1.4 / (Pr * Reyl)) * GZ(tc);
-    const double tauzz = (mu / Reyl) * ((4.0 / 3.0) * GX(uc) - (2.0 / 3.0) * GY(vc) - (2.0 / 3.0) * GZ(wc));
-    const double tauee = (mu / Reyl) * ((4.0 / 3.0) * GY(vc) - (2.0 / 3.0) * GX(uc) - (2.0 / 3.0) * GZ(wc));
-    const double tauxx = (mu / Reyl) * ((4.0 / 3.0) * GZ(wc) - (2.0 / 3.0) * GX(uc) - (2.0 / 3.0) * GY(vc));
+    const double kq = dv(mu * 1.4, Pr * Reyl), mr = dv(mu, Reyl);
+    const double qz = (-1.0) * kq * GX(tc);
+    const double qe = (-1.0) * kq * GY(tc);
+    const double qx = (-1.0) * kq * GZ(tc);
+    const double tauzz = mr * ((4.0 / 3.0) * GX(uc) - (2.0 / 3.0) * GY(vc) - (2.0 / 3.0) * GZ(wc));
+    const double tauee = mr * ((4.0 / 3.0) * GY(vc) - (2.0 / 3.0) * GX(uc) - (2.0 / 3.0) * GZ(wc));
+    const double tauxx = mr * ((4.0 / 3.0) * GZ(wc) - (2.0 / 3.0) * GX(uc) - (2.0 / 3.0) * GY(vc));
     const double s_xy = uc[0] * zeta_y + uc[1] * eta_y + uc[2] * xi_y + vc[0] * zeta_x + vc[1] * eta_x + vc[2] * xi_x;
     const double s_xz = uc[0] * zeta_z + uc[1] * eta_z + uc[2] * xi_z + wc[0] * zeta_x + wc[1] * eta_x + wc[2] * xi_x;
     const double s_yz = vc[0] * zeta_z + vc[1] * eta_z + vc[2] * xi_z + wc[0] * zeta_y + wc[1] * eta_y + wc[2] * xi_y;
-    const double tauze = (mu / Reyl) * s_xy;
-    const double tauzx = (mu / Reyl) * s_xz;
-    const double tauex = (mu / Reyl) * s_yz;
+    const double tauze = mr * s_xy;
+    const double tauzx = mr * s_xz;
+    const double tauex = mr * s_yz;
     double TAU_XY = 0, TAU_YZ = 0, TAU_XZ = 0, TAU_XX = 0, TAU_YY = 0, TAU_ZZ = 0;
     double H_X = 0, H_Y = 0, H_Z = 0, D_X = 0, D_Y = 0, D_Z = 0;
     const double u = prim[1], v = prim[2], w = prim[3];
@@ -322,7 +327,7 @@ __device__ __forceinline__ void viscous_node(const double dU[3][5], const double
         const double stress_xx = GX(uc), stress_yy = GY(vc), stress_zz = GZ(wc);
         const double mod_stress = sqrt(scale2<1>((stress_xy * stress_xy + stress_yz * stress_yz + stress_xz * stress_xz)
                                               + (2.0 / 3.0) * (stress_xx * stress_xx + stress_yy * stress_yy + stress_zz * stress_zz)));
-        const double DEL = (1.0 / cbrt(DET_I));
+        const double DEL = dv(1.0, cbrt(DET_I));
         double EDDY_x, EDDY_y, EDDY_z;
         if (P.les == 2) {
             // Smagorinsky (no counterpart in the reference): (C_s Delta)^2 |S|,
@@ -333,12 +338,13 @@ __device__ __forceinline__ void viscous_node(const double dU[3][5], const double
             const double ls = P.cs * cbrt(DET_I);
             EDDY_x = EDDY_y = EDDY_z = (ls * ls) * S;
         } else if (mod_stress != 0.0) {
-            const double Rx = (DEL * (mod_stress)) / sqrt(KSv[0]);
-            const double Ry = (DEL * (mod_stress)) / sqrt(KSv[1]);
-            const double Rz = (DEL * (mod_stress)) / sqrt(KSv[2]);
-            EDDY_x = (C_MTS / (1.0 + (1.0 * Rx / (C_T)))) * DEL * sqrt(KSv[0]);
-            EDDY_y = (C_MTS / (1.0 + (1.0 * Ry / (C_T)))) * DEL * sqrt(KSv[1]);
-            EDDY_z = (C_MTS / (1.0 + (1.0 * Rz / (C_T)))) * DEL * sqrt(KSv[2]);
+            const double Rx = dv(DEL * (mod_stress), sqrt(KSv[0]));
+            const double Ry = dv(DEL * (mod_stress), sqrt(KSv[1]));
+            const double Rz = dv(DEL * (mod_stress), sqrt(KSv[2]));
+            const Over<true> oct(C_T);
+            EDDY_x = dv(C_MTS, 1.0 + oct(1.0 * Rx)) * DEL * sqrt(KSv[0]);
+            EDDY_y = dv(C_MTS, 1.0 + oct(1.0 * Ry)) * DEL * sqrt(KSv[1]);
+            EDDY_z = dv(C_MTS, 1.0 + oct(1.0 * Rz)) * DEL * sqrt(KSv[2]);
         } else {
             EDDY_x = (C_MTS) * DEL * sqrt(KSv[0]);
             EDDY_y = (C_MTS) * DEL * sqrt(KSv[1]);
@@ -351,9 +357,10 @@ __device__ __forceinline__ void viscous_node(const double dU[3][5], const double
         TAU_XX = m2U0 * EDDY_x * stress_xx;
         TAU_YY = m2U0 * EDDY_y * stress_yy;
         TAU_ZZ = m2U0 * EDDY_z * stress_zz;
-        const double Q_x = (1.0 / (1.4 * 0.4 * Mach * Mach)) * (-1.0) * (EDDY_x) * GX(tc);
-        const double Q_y = (1.0 / (1.4 * 0.4 * Mach * Mach)) * (-1.0) * (EDDY_y) * GY(tc);
-        const double Q_z = (1.0 / (1.4 * 0.4 * Mach * Mach)) * (-1.0) * (EDDY_z) * GZ(tc);
+        const double ck = dv(1.0, 1.4 * 0.4 * Mach * Mach);
+        const double Q_x = ck * (-1.0) * (EDDY_x) * GX(tc);
+        const double Q_y = ck * (-1.0) * (EDDY_y) * GY(tc);
+        const double Q_z = ck * (-1.0) * (EDDY_z) * GZ(tc);
         H_X = Q_x + (TAU_XX * u + TAU_XY * u + TAU_XZ * u);
         H_Y = Q_y + (TAU_XY * v + TAU_YY * v + TAU_YZ * v);
         H_Z = Q_z + (TAU_XZ * w + TAU_YZ * w + TAU_ZZ * w);
@@ -384,7 +391,7 @@ __device__ __forceinline__ void node_flux(const double prim[5], const double m[9
                                           double E[5], double G[5])
 {
     const double rho = prim[0], u = prim[1], v = prim[2], w = prim[3], p = prim[4];
-    const double Et = (((p / 0.4) + 0.5 * rho * (u * u + v * v + w * w)) + p);
+    const double Et = ((dv(p, 0.4) + 0.5 * rho * (u * u + v * v + w * w)) + p);
     const double tF[5] = {rho * u, rho * u * u + p, rho * v * u, rho * u * w, Et * u};
     const double tE[5] = {rho * v, rho * v * u, rho * v * v + p, rho * v * w, Et * v};
     const double tG[5] = {rho * w, rho * u * w, rho * v * w, rho * w * w + p, Et * w};
@@ -401,19 +408,20 @@ __device__ __forceinline__ void node_flux(const double prim[5], const double m[9
 __device__ __forceinline__ double ks(double Uc_i, double U0_i, double Uc_m, double U0_m, double Uc_p, double U0_p)
 {
     using xdiv::scale2;   // 0.25 * x and 0.5 * x on the integer pipe, same bits
-    return sq(((Uc_i / U0_i) - ((scale2<-2>(Uc_m) + scale2<-1>(Uc_i) + scale2<-2>(Uc_p))
-                                / (scale2<-2>(U0_m) + scale2<-1>(U0_i) + scale2<-2>(U0_p)))));
+    return sq((dv(Uc_i, U0_i) - dv(scale2<-2>(Uc_m) + scale2<-1>(Uc_i) + scale2<-2>(Uc_p),
+                                   scale2<-2>(U0_m) + scale2<-1>(U0_i) + scale2<-2>(U0_p))));
 }
 
 // Sutherland viscosity from U only (Viscous.cl:451-458).
 __device__ __forceinline__ double mu_of(const double Ui[5], double Mach, double Free_t)
 {
     const double U0_I = Ui[0], U1_I = Ui[1], U2_I = Ui[2], U3_I = Ui[3], U4_I = Ui[4];
+    const Over<true> o2(U0_I * U0_I);
     const double d_temp = (1.4 * Mach * Mach * 0.4
-                           * ((U4_I / U0_I) - xdiv::scale2<-1>(((U1_I * U1_I) / (U0_I * U0_I)) + ((U2_I * U2_I) / (U0_I * U0_I))
-                                                     + ((U3_I * U3_I) / (U0_I * U0_I)))));
+                           * (dv(U4_I, U0_I) - xdiv::scale2<-1>(o2(U1_I * U1_I) + o2(U2_I * U2_I) + o2(U3_I * U3_I))));
     const double d_temp1 = sqrt(d_temp) * sqrt(d_temp) * sqrt(d_temp);
-    return (d_temp1) * ((1.0 + (110.4 / Free_t)) / (d_temp + (110.4 / Free_t)));
+    const double st = dv(110.4, Free_t);
+    return (d_temp1) * dv(1.0 + st, d_temp + st);
 }
 
 // SSP-RK3 stage j and primitive recovery (Weno.cl:3084-3135).  Returns the
@@ -431,20 +439,24 @@ __device__ __forceinline__ void rk_and_primitives(int j, double del_t, double ma
 #pragma unroll
         for (int c = 0; c < 5; ++c) Un[c] = (3.0 / 4.0) * U0[c] + (1.0 / 4.0) * U1[c] + 0.25 * del_t * L[c];
     } else {
+        const Over<true> d3(3.0);
 #pragma unroll
-        for (int c = 0; c < 5; ++c) Un[c] = (U0[c] / 3.0) + ((2.0 / 3.0) * U2[c]) + (2.0 / 3.0) * (del_t * L[c]);
+        for (int c = 0; c < 5; ++c) Un[c] = d3(U0[c]) + ((2.0 / 3.0) * U2[c]) + (2.0 / 3.0) * (del_t * L[c]);
     }
     double fu[5];
+    const double idet = dv(1.0, det);
 #pragma unroll
-    for (int c = 0; c < 5; ++c) fu[c] = (1.0 / det) * Un[c];
+    for (int c = 0; c < 5; ++c) fu[c] = idet * Un[c];
     rho = fu[0];
-    u = fu[1] / fu[0];
-    v = fu[2] / fu[0];
-    w = fu[3] / fu[0];
-    e = (fu[4] / fu[0]) - 0.5 * (u * u + v * v + w * w);
+    const Over<true> d0(fu[0]);   // u, v, w, e share the divisor rho
+    u = d0(fu[1]);
+    v = d0(fu[2]);
+    w = d0(fu[3]);
+    e = d0(fu[4]) - 0.5 * (u * u + v * v + w * w);
     p = e * rho * 0.4;
-    t = (1.4 * mach * mach) * (p / rho);
-    a_ = sqrt(1.4 * p / rho);
+    const Over<true> dr(rho);
+    t = (1.4 * mach * mach) * dr(p);
+    a_ = sqrt(dr(1.4 * p));
 }
 
 }  // namespace ex
