@@ -275,7 +275,12 @@ __device__ __forceinline__ bool same_bits(double a, double b) { return __double_
 // stays in the table: Fp[(d*5 + c)*ld + gid]; also p's -1/2 face
 // Fm[(d*5 + c)*ld + p] with stamp[d*ld + p] = gen for the plus neighbour p
 // whose minus neighbour is gid, when p's face data are gid's bit for bit.
-__global__ void __launch_bounds__(128, 2) k_weno_plus(Phys P, const double *__restrict__ deter,
+// blocks per SM the +1/2-face kernel's register budget allows: 2 (GB300,
+// TGV 128^3: drop-in 2.89e7 cell-updates/s against 2.85e7 at 3)
+#ifndef CFD_WENO_PLUS_MIN_BLOCKS
+#define CFD_WENO_PLUS_MIN_BLOCKS 2
+#endif
+__global__ void __launch_bounds__(128, CFD_WENO_PLUS_MIN_BLOCKS) k_weno_plus(Phys P, const double *__restrict__ deter,
                                                        const int *__restrict__ grid, const double *__restrict__ Q,
                                                        const double *__restrict__ metric,
                                                        const double *__restrict__ roe, const double *__restrict__ F,
