@@ -29,11 +29,12 @@
 
 // Minimum resident blocks per SM requested for the FP64 face kernels (their
 // register budget) along i and j, and along k: with the divisions' rounding
-// on the integer pipe, 3 (168 registers at 128 threads per block) runs the
-// i and j passes fastest on GB300 (TGV 128^3: 6.24 ms against 6.71 at 2),
-// 2 the k pass (6.34 against 6.75 ms; its stencil strides a whole plane).
+// on the integer pipe, 4 (128 registers at 128 threads per block, some
+// spill) runs the i and j passes fastest on GB300 (TGV 128^3: 6.13 ms,
+// against 6.24 at 3 and 6.71 at 2), 2 the k pass (6.33 against 6.70 at 3;
+// its stencil strides a whole plane).
 #ifndef CFD_FACE_MIN_BLOCKS
-#define CFD_FACE_MIN_BLOCKS 3
+#define CFD_FACE_MIN_BLOCKS 4
 #endif
 #ifndef CFD_FACE_K_MIN_BLOCKS
 #define CFD_FACE_K_MIN_BLOCKS 2
