@@ -60,7 +60,7 @@ struct cfd_batch {
     size_t items_cap = 0;
     int nitems = 0;
     int n_views = 0;
-    unsigned *d_words = nullptr;          // [0..1] barrier, [2] batch flags, [4..] per-slot flags
+    unsigned *d_words = nullptr;          // [0..1] barrier, [2] batch flags, [3] phase-A work counter, [4..] per-slot flags
     int threads = 128;
     int blocks_override = 0;
     long long wait_limit_ns = -1;         // barrier deadline (< 0: 5 s + 50 ns per node)
@@ -131,10 +131,10 @@ void face_tile_items(const LatView &g, int v, std::vector<BatchItem> &out)
                 out.push_back(BatchItem{v, 1 + D, (int)x * T::kTile, (int)y * T::kWide, (int)z, 0});
 }
 
-// Phase A items of the tiled form in launch order: position w is taken by
-// block w % G in round w / G; its kind is (block + round) mod 4 while that
-// kind has items left (else the next kind that has), so that every block
-// cycles through the kinds and neighbouring blocks work on the same region.
+// Phase A items of the tiled form in the order the blocks take them (from
+// the shared counter): position w has kind (w % G + w / G) mod 4 while that
+// kind has items left (else the next kind that has), so that the blocks
+// running at one time work on every kind of the same region.
 std::vector<BatchItem> order_items(std::vector<BatchItem> q[4], int G)
 {
     size_t total = 0, head[4] = {0, 0, 0, 0};
@@ -836,7 +836,7 @@ cfd_status_t cfd_batch_set_wait_limit(cfd_batch_t *b, int64_t limit_ns)
 cfd_status_t cfd_batch_set_tiling(cfd_batch_t *b, int32_t tile_nodes, int32_t max_blocks, int32_t use_graph)
 {
     if (!b || max_blocks < 0) return CFD_EINVAL;
-    if (tile_nodes != 0 && tile_nodes != 64 && tile_nodes != 128 && tile_nodes != 256
+    if (tile_nodes != 0 && tile_nodes != 32 && tile_nodes != 64 && tile_nodes != 128 && tile_nodes != 256
         && tile_nodes != CFD_BATCH_FACE_TILES)
         return CFD_EINVAL;
     if (tile_nodes == CFD_BATCH_FACE_TILES && b->precision == CFD_PREC_FP64) return CFD_EINVAL;
@@ -879,9 +879,9 @@ cfd_status_t cfd_batch_tune(cfd_batch_t *b, int32_t steps_per_trial)
         }
     };
     copy_all(true);
-    // 1-D tiles of 64, 128, 256 nodes, and for the reduced forms the
+    // 1-D tiles of 32, 64, 128, 256 nodes, and for the reduced forms the
     // shared-memory face tiles
-    std::vector<int> candidates = {64, 128, 256};
+    std::vector<int> candidates = {32, 64, 128, 256};
     if (b->precision != CFD_PREC_FP64) candidates.push_back(CFD_BATCH_FACE_TILES);
     const int threads0 = b->threads;
     const bool faces0 = b->face_tiles;

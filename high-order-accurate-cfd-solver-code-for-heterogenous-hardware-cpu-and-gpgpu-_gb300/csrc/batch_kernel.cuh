@@ -4,7 +4,8 @@
 // count), tile size = block size, so one thread owns one node of a tile.
 // A stage has two phases separated by a grid-wide barrier:
 //   A  for every tile: viscous fluxes and the three face fluxes (4 work items
-//      per tile, interleaved so that neighbouring blocks share a tile's data)
+//      per tile, taken in order from a shared counter, so that blocks that
+//      run at the same time share a tile's data and none waits long)
 //   B  for every tile: RHS, RK stage, primitives, and the next stage's prep
 //      (U_Q) on the new primitives
 // The kernel is launched cooperatively (all blocks co-resident) with at most
@@ -39,6 +40,9 @@ __device__ __forceinline__ unsigned long long global_ns()
 // Sense-reversing grid barrier over `nblocks` co-resident blocks.
 // bar[0] = arrival count, bar[1] = generation.  Returns false (and sets the
 // timeout bit) if the generation does not advance before the deadline.
+// The last block to arrive also clears bar[3], the phase-A work counter
+// (every block has stopped taking phase-A items when it arrives), so the
+// next launch starts from item 0.
 __device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned nblocks, unsigned long long limit_ns,
                                              unsigned *gflags)
 {
@@ -51,6 +55,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned nblocks, un
         __threadfence();
         const unsigned arrived = atomicAdd(bar, 1u);
         if (arrived == nblocks - 1) {
+            atomicExch(bar + 3, 0u);
             atomicExch(bar, 0u);
             __threadfence();
             atomicAdd(bar + 1, 1u);
@@ -72,7 +77,30 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned nblocks, un
     return s_ok != 0;
 }
 
-// Blocks of up to 256 threads (the tile sizes 64, 128, 256); Ops::kMinBlocks
+// Next phase-A item of this block: blocks take items in order from a
+// shared counter (bar[3]), so a block that finishes early takes more and
+// no block idles long at the barrier (with a fixed item-to-block map some
+// blocks ran phase A ~10 % longer than the rest and everyone waited).
+__device__ __forceinline__ int next_item(unsigned *bar)
+{
+    __shared__ int s_w;
+    __syncthreads();   // every thread is done with the previous item
+    if (threadIdx.x == 0) s_w = (int)atomicAdd(bar + 3, 1u);
+    __syncthreads();
+    return s_w;
+}
+
+// Phase A's item order: kind-major (1: every tile's i faces, then every
+// tile's j faces, then k, then the viscous items -- the blocks running at
+// one time work on one direction, as the single-lattice passes do) or
+// tile-major (0: the four kinds of a tile one after the other).  64
+// vortices, tuned tiles: mixed 1.33e9 against 1.29e9 cell-updates/s, split
+// 1.02e9 against 9.6e8.
+#ifndef CFD_BATCH_KIND_MAJOR
+#define CFD_BATCH_KIND_MAJOR 1
+#endif
+
+// Blocks of up to 256 threads (the tile sizes 32, 64, 128, 256); Ops::kMinBlocks
 // bounds the registers so that many blocks stay resident (the mixed form is
 // latency bound; the FP64 form keeps its registers).
 template <class Ops>
@@ -80,17 +108,19 @@ __global__ void __launch_bounds__(256, Ops::kMinBlocks)
 k_batch_stage(const LatView *__restrict__ views, const BatchTile *__restrict__ tiles, int ntiles, int jst,
               unsigned *bar, unsigned *gflags, unsigned long long limit_ns)
 {
-    // Item w is tile w >> 2; the four items of a tile go to four neighbouring
-    // blocks in the same round (they share the tile's data in L2).  The kind
-    // is rotated by the round, (w & 3) + round, which is still a permutation
-    // of the four kinds per tile: without it, a grid of a multiple of 4
-    // blocks gives each block one kind for the whole phase, and the blocks
-    // with the light viscous items idle at the barrier.
+    // Item w: tile w % ntiles of kind w / ntiles (kind-major), or tile w >> 2
+    // of kind w & 3 (the four items of a tile taken one after the other, by
+    // different blocks at about the same time: they share the tile's data in
+    // L2).
     const int items = 4 * ntiles;
-    const int per_round = max(1, (int)gridDim.x >> 2);
-    for (int w = blockIdx.x; w < items; w += gridDim.x) {
+    for (int w = next_item(bar); w < items; w = next_item(bar)) {
+#if CFD_BATCH_KIND_MAJOR
+        const BatchTile t = tiles[w % ntiles];
+        const int kind = (w / ntiles + 1) & 3;   // i faces, j faces, k faces, then the viscous items
+#else
         const BatchTile t = tiles[w >> 2];
-        const int kind = ((w & 3) + (w >> 2) / per_round) & 3;
+        const int kind = w & 3;
+#endif
         if ((int)threadIdx.x < t.count) {
             const LatView &g = views[t.inst];
             const int n = t.n0 + threadIdx.x;
@@ -133,7 +163,7 @@ k_batch_stage_tiled(const LatView *__restrict__ views, const BatchItem *__restri
                     unsigned long long limit_ns)
 {
     __shared__ float smem[Ops::kTileSmemFloats];
-    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+    for (int w = next_item(bar); w < nitems; w = next_item(bar)) {
         const BatchItem it = items[w];
         const LatView &g = views[it.inst];
         const TileAt at{it.a, it.b, it.c};
@@ -149,8 +179,7 @@ k_batch_stage_tiled(const LatView *__restrict__ views, const BatchItem *__restri
         } else {
             Ops::template face_tile<2>(g, at, smem);
         }
-        __syncthreads();   // the next item restages smem
-    }
+    }   // next_item synchronises the block before the next item restages smem
     if (!grid_barrier(bar, gridDim.x, limit_ns, gflags)) return;
     for (int w = blockIdx.x; w < nupd; w += gridDim.x) {
         const BatchTile t = upd[w];

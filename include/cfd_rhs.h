@@ -440,7 +440,7 @@ cfd_status_t cfd_batch_set_flow(cfd_batch_t *b, int32_t slot, const cfd_flow_t *
  * (CFD_ETIMEOUT) until cfd_batch_set_flow restores it or it is removed.
  * Instances that were held are not affected. */
 cfd_status_t cfd_batch_set_wait_limit(cfd_batch_t *b, int64_t limit_ns);
-/* tile_nodes in {64, 128, 256}: phase A of a stage works on 1-D tiles of
+/* tile_nodes in {32, 64, 128, 256}: phase A of a stage works on 1-D tiles of
  * that many nodes, each face evaluated from its own stencil gathers;
  * CFD_BATCH_FACE_TILES (mixed and split batches): phase A works on the
  * viscous ranges and on 2-D face tiles whose stencil lines a block of 128
@@ -449,7 +449,7 @@ cfd_status_t cfd_batch_set_wait_limit(cfd_batch_t *b, int64_t limit_ns);
  * use_graph 0/1. */
 #define CFD_BATCH_FACE_TILES 1
 cfd_status_t cfd_batch_set_tiling(cfd_batch_t *b, int32_t tile_nodes, int32_t max_blocks, int32_t use_graph);
-/* Times each tiling (1-D tiles of 64, 128, 256 nodes and, for the mixed and
+/* Times each tiling (1-D tiles of 32, 64, 128, 256 nodes and, for the mixed and
  * split batches, the face tiles) on the live batch (state saved and
  * restored) and keeps the fastest. */
 cfd_status_t cfd_batch_tune(cfd_batch_t *b, int32_t steps_per_trial);

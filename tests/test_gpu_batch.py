@@ -228,6 +228,25 @@ def test_empty_batch_steps_and_info(ctx):
         b.close()
 
 
+@pytest.mark.parametrize("tile", [32, 64, 256])
+def test_every_tile_size_gives_the_same_bits(ctx, tile):
+    """The batched kernel takes phase-A items from a shared counter, in an
+    order that depends on timing; every item writes only its own faces, so
+    the results do not depend on the tile size or on which block took what."""
+    from cfd_gb300 import runtime
+    cs = mix_cases()
+    out = []
+    for t in (128, tile):
+        b = runtime.Batch(ctx, 1)
+        b.set_tiling(t, 0, use_graph=False)
+        ss = [b.add(c) for c in cs]
+        b.step(3)
+        out.append([b.get_flow(s_) for s_ in ss])
+        b.close()
+    for a, c in zip(*out):
+        assert np.array_equal(a, c)
+
+
 def test_tuning_and_graph_do_not_change_results(ctx):
     from cfd_gb300 import runtime
     cs = mix_cases()
@@ -239,7 +258,7 @@ def test_tuning_and_graph_do_not_change_results(ctx):
     ts = [tuned.add(c) for c in cs]
     tuned.tune(1)                        # trials run on the live batch, state restored
     tuned.step(2)
-    assert tuned.info().tile_nodes in (64, 128, 256)
+    assert tuned.info().tile_nodes in (32, 64, 128, 256)
     for r, t in zip(rs, ts):
         assert np.array_equal(ref.get_flow(r), tuned.get_flow(t))
     ref.close()
