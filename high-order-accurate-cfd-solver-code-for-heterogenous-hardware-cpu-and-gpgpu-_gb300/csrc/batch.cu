@@ -132,15 +132,20 @@ void face_tile_items(const LatView &g, int v, std::vector<BatchItem> &out)
 }
 
 // Phase A items of the tiled form in the order the blocks take them (from
-// the shared counter): position w has kind (w % G + w / G) mod 4 while that
-// kind has items left (else the next kind that has), so that the blocks
-// running at one time work on every kind of the same region.
+// the shared counter): kind-major as the 1-D form (CFD_BATCH_KIND_MAJOR),
+// else position w has kind (w % G + w / G) mod 4 while that kind has items
+// left (else the next kind that has), so that the blocks running at one
+// time work on every kind of the same region.
 std::vector<BatchItem> order_items(std::vector<BatchItem> q[4], int G)
 {
     size_t total = 0, head[4] = {0, 0, 0, 0};
     for (int k = 0; k < 4; ++k) total += q[k].size();
     std::vector<BatchItem> out;
     out.reserve(total);
+    if (CFD_BATCH_KIND_MAJOR) {   // as the 1-D form: i, j, k faces, then the viscous ranges
+        for (int k : {1, 2, 3, 0}) out.insert(out.end(), q[k].begin(), q[k].end());
+        return out;
+    }
     for (size_t w = 0; w < total; ++w) {
         const int k0 = (int)(((w % G) + (w / G)) & 3);
         for (int t = 0; t < 4; ++t) {
