@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(128) k_uq(double *__restrict__ U, double *__re
         }
     }
     const double D = det[gid];
-    const double ke = 0.5 * rho * (u * u + v * v + w * w);
+    const double ke = xdiv::scale2<-1>(rho) * (u * u + v * v + w * w);   // 0.5 rho, same bits
     double *Ur = U + 5 * (size_t)gid, *Qr = Q + 5 * (size_t)gid;
     Ur[0] = D * rho;
     Ur[1] = D * rho * u;

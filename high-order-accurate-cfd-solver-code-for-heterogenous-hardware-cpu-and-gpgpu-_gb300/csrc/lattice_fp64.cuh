@@ -20,7 +20,7 @@ __device__ __forceinline__ void prep_values(const LatView &g, int n, int q, doub
 {
     const int N = g.N;
     const double D = g.det[n];
-    const double ke = 0.5 * rho * (u * u + v * v + w * w);
+    const double ke = xdiv::scale2<-1>(rho) * (u * u + v * v + w * w);   // 0.5 rho on the integer pipe, same bits
     const double E = dv(p, 0.4) + ke;
     double *Uq = lat_U(g, q);
     g.Q[0 * N + n] = rho;

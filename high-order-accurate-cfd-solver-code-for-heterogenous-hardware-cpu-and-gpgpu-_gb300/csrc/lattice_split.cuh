@@ -237,7 +237,7 @@ __device__ __forceinline__ void update_node(const LatView &g, int n, int jst)
     int i, j, k;
     lat_ijk(g, n, i, j, k);
     const unsigned lflag = (LOC && g.locflag) ? g.locflag[n] : 7u;
-    double Ld[5] = {0.0, 0.0, 0.0, 0.0, 0.0};   // sum of flux differences (= -L)
+    double Ld[5];   // sum of flux differences (= -L), started by the i direction's
     float Lv[5] = {0.f, 0.f, 0.f, 0.f, 0.f};     // viscous divergence
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
@@ -245,7 +245,10 @@ __device__ __forceinline__ void update_node(const LatView &g, int n, int jst)
         // FP64 pipe: the integer-pipe add (emu::add) costs more issue than it
         // frees here (TGV 128^3: update 0.23 -> 0.31 ms with one direction)
 #pragma unroll
-        for (int c = 0; c < 5; ++c) Ld[c] += ldd(g.Fh + (d * 5 + c) * N + n) - ldd(g.Fh + (d * 5 + c) * N + m1);
+        for (int c = 0; c < 5; ++c) {
+            const double df = ldd(g.Fh + (d * 5 + c) * N + n) - ldd(g.Fh + (d * 5 + c) * N + m1);
+            Ld[c] = d == 0 ? df : Ld[c] + df;
+        }
         if (LOC && g.P.viscous && lat_locdir(g, d) && ((lflag >> d) & 1u)) {
             int s[7], L7[7];
 #pragma unroll

@@ -59,7 +59,7 @@ __device__ __forceinline__ double dv(double a, double b) { return CFD_EXACT_DIVI
 // U_Q.cl:64-65
 __device__ __forceinline__ double enthalpy(double rho, double u, double v, double w, double p)
 {
-    return dv((dv(p, 0.4) + 0.5 * rho * (u * u + v * v + w * w) + p), rho);
+    return dv((dv(p, 0.4) + xdiv::scale2<-1>(rho) * (u * u + v * v + w * w) + p), rho);
 }
 
 // U_Q.cl:60-109 for one face: {u, v, w, h, rho}; (sb,...) the neighbour.
@@ -257,7 +257,7 @@ __device__ __forceinline__ double corrected(double Fhat, const double f[6])
 // branch of Weno.cl:2771-2778); f[0..4] = offsets -2..2.
 __device__ __forceinline__ double central4(double fm2, double fm1, double fp1, double fp2)
 {
-    return (1.0 / 12.0) * (8.0 * (fp1 - fm1) - (fp2 - fm2));
+    return (1.0 / 12.0) * (xdiv::scale2<3>(fp1 - fm1) - (fp2 - fm2));   // 8 (...) on the integer pipe, same bits
 }
 
 struct Visc {
@@ -391,7 +391,7 @@ __device__ __forceinline__ void node_flux(const double prim[5], const double m[9
                                           double E[5], double G[5])
 {
     const double rho = prim[0], u = prim[1], v = prim[2], w = prim[3], p = prim[4];
-    const double Et = ((dv(p, 0.4) + 0.5 * rho * (u * u + v * v + w * w)) + p);
+    const double Et = ((dv(p, 0.4) + xdiv::scale2<-1>(rho) * (u * u + v * v + w * w)) + p);
     const double tF[5] = {rho * u, rho * u * u + p, rho * v * u, rho * u * w, Et * u};
     const double tE[5] = {rho * v, rho * v * u, rho * v * v + p, rho * v * w, Et * v};
     const double tG[5] = {rho * w, rho * u * w, rho * v * w, rho * w * w + p, Et * w};
@@ -452,7 +452,7 @@ __device__ __forceinline__ void rk_and_primitives(int j, double del_t, double ma
     u = d0(fu[1]);
     v = d0(fu[2]);
     w = d0(fu[3]);
-    e = d0(fu[4]) - 0.5 * (u * u + v * v + w * w);
+    e = d0(fu[4]) - xdiv::scale2<-1>(u * u + v * v + w * w);
     p = e * rho * 0.4;
     const Over<true> dr(rho);
     t = (1.4 * mach * mach) * dr(p);
