@@ -28,13 +28,15 @@
 #include "structured.h"
 
 // Minimum resident blocks per SM requested for the FP64 face kernels (their
-// register budget) along i and j, and along k: with the divisions' rounding
-// on the integer pipe, 4 (128 registers at 128 threads per block, some
-// spill) runs the i and j passes fastest on GB300 (TGV 128^3: 6.13 ms,
-// against 6.24 at 3 and 6.71 at 2), 2 the k pass (6.33 against 6.70 at 3;
-// its stencil strides a whole plane).
+// register budget) along i and j, and along k.  With the divisions' rounding
+// on the integer pipe, 3 (168 registers at 128 threads per block) runs the
+// i and j passes best across the benchmark's lattices on GB300: 4 (128
+// registers, some spill) is 0.9 % faster on TGV 128^3 but 5-6 % slower on
+// the NACA0012 O-grid and the shocked slab, 2 is 7 % slower on TGV.  2 runs
+// the k pass fastest (6.33 against 6.70 ms at 3 on TGV; its stencil strides
+// a whole plane).
 #ifndef CFD_FACE_MIN_BLOCKS
-#define CFD_FACE_MIN_BLOCKS 4
+#define CFD_FACE_MIN_BLOCKS 3
 #endif
 #ifndef CFD_FACE_K_MIN_BLOCKS
 #define CFD_FACE_K_MIN_BLOCKS 2
