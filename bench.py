@@ -408,7 +408,8 @@ def gpu_arm(args):
         "config": cfg,
         "run": {"parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                 "l2": "inputs larger than L2 (resident working set %.2f GB)" % (s64.info().device_bytes / 1e9),
-                "path": "structured face-based, exact FP64 evaluation order"},
+                "path": "structured face-based, exact FP64 evaluation order",
+                "fp64_face_blocks_tuned": list(s64.info().face_blocks)},
         "gpu_launches": launches64,
         "clocks": clocks,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(host_in.nbytes),
@@ -610,6 +611,8 @@ def bench_naca(ctx, torch, stream, args):
         s = runtime.Solver(ctx, case, precision=prec)
         assert s.info().path == "structured"
         s.set_flow(flow0)
+        s.step(case.dt, 1)        # untimed: the first stage runs the FP64 face tuner
+        s.set_flow(flow0)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         e0.record(stream)
@@ -619,9 +622,12 @@ def bench_naca(ctx, torch, stream, args):
         secs = e0.elapsed_time(e1) / 1e3
         res[prec] = s.get_flow()[1:N + 1]
         prof = [s.profile_stage(j, case.dt) for j in range(3)]   # one more step, per-kernel times
+        mb = list(s.info().face_blocks)
         s.close()
         out[FORM_NAMES[prec]] = {"value": N * steps / secs, "unit": UNIT, "ms_per_step": 1e3 * secs / steps,
                                  "dtype": FORM_DTYPES[prec], "kernels_ms_per_stage": _kernel_table(prof)}
+        if prec == FP64:
+            out["fp64"]["face_blocks_tuned"] = mb
     f = layout.FLOW
     for prec in (SPLIT, MIXED):
         key = FORM_NAMES[prec]
@@ -773,6 +779,8 @@ def bench_shock(ctx, torch, stream, args):
     for prec in (FP64, SPLIT, MIXED):
         s = runtime.Solver(ctx, case, precision=prec)
         s.set_flow(case.arrays["flow"])
+        s.step(case.dt, 1)        # untimed: the first stage runs the FP64 face tuner
+        s.set_flow(case.arrays["flow"])
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         e0.record(stream)
@@ -781,9 +789,12 @@ def bench_shock(ctx, torch, stream, args):
         torch.cuda.synchronize()
         secs = e0.elapsed_time(e1) / 1e3
         res[prec] = s.get_flow()
+        mb = list(s.info().face_blocks)
         s.close()
         out[FORM_NAMES[prec]] = {"value": N * steps / secs, "unit": UNIT, "ms_per_step": 1e3 * secs / steps,
                                  "dtype": FORM_DTYPES[prec], "shock": front(res[prec])}
+        if prec == FP64:
+            out["fp64"]["face_blocks_tuned"] = mb
     f = layout.FLOW
     for prec in (SPLIT, MIXED):
         key = FORM_NAMES[prec]

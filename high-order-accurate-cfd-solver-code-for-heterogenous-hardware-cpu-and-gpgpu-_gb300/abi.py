@@ -46,7 +46,8 @@ class KernelTime(C.Structure):
 class SolverInfo(C.Structure):
     _fields_ = [("path", C.c_int32), ("ni", C.c_int32), ("nj", C.c_int32), ("nk", C.c_int32),
                 ("precision", C.c_int32), ("reserved", C.c_int32), ("device_bytes", C.c_uint64),
-                ("face_tile_i", C.c_int32), ("face_tile_jk", C.c_int32)]
+                ("face_tile_i", C.c_int32), ("face_tile_jk", C.c_int32), ("face_blocks", C.c_int32 * 3),
+                ("reserved2", C.c_int32)]
 
 
 class BatchInfo(C.Structure):
@@ -85,6 +86,7 @@ PROTOTYPES = {
     "cfd_solver_info": (C.c_int, [_vp, C.POINTER(SolverInfo)]),
     "cfd_solver_set_flow": (C.c_int, [_vp, _vp]),
     "cfd_solver_set_face_tiles": (C.c_int, [_vp, _i32, _i32]),
+    "cfd_solver_set_face_blocks": (C.c_int, [_vp, _i32, _i32, _i32]),
     "cfd_solver_get_flow": (C.c_int, [_vp, _vp]),
     "cfd_solver_get_u0": (C.c_int, [_vp, _vp]),
     "cfd_solver_step": (C.c_int, [_vp, _d, _i32]),

@@ -33,7 +33,8 @@ def nvcc() -> str:
 
 # Translation units whose FP64 arithmetic must follow the reference's
 # evaluation order: no contraction of a*b+c into FMA.
-EXACT_FP64 = {"dropin.cu", "structured.cu", "batch_fp64.cu", "boundary.cu"}
+EXACT_FP64 = {"dropin.cu", "structured.cu", "batch_fp64.cu", "boundary.cu", "face_fp64_mb2.cu", "face_fp64_mb3.cu",
+              "face_fp64_mb4.cu"}
 # Translation units of the mixed and split precision forms: approximate FP32
 # division and square root (single-precision only; FP64 arithmetic is
 # unaffected) and FMA contraction.

@@ -57,6 +57,7 @@ struct cfd_solver {
     cfd::LatticeMap map;        // lattice path: rows <-> nodes
     cfd::BcDevice bc;           // boundary routine after every stage
     bool has_bc = false;
+    bool fp64_tune = false;     // FP64 lattice: time the face passes' budgets at the first stage
 };
 
 namespace {
@@ -112,6 +113,7 @@ cfd_status_t create_gather(cfd_solver *s, const cfd_geometry_t *g)
 }
 
 cfd_status_t tune_face_tiles(cfd_solver *s);
+cfd_status_t tune_fp64_faces(cfd_solver *s, int j);
 
 cfd_status_t create_structured(cfd_solver *s, const cfd_geometry_t *g)
 {
@@ -231,6 +233,7 @@ cfd_status_t create_structured(cfd_solver *s, const cfd_geometry_t *g)
     cudaError_t e = cudaStreamSynchronize(S.stream);   // host vectors go out of scope
     if (e != cudaSuccess) return cuda_fail(s->ctx, e, "solver create sync");
     if (s->mixed) return tune_face_tiles(s);
+    s->fp64_tune = true;   // on the first stage's real inputs (tune_fp64_faces)
     return CFD_OK;
 }
 
@@ -297,6 +300,67 @@ cfd_status_t tune_face_tiles(cfd_solver *s)
     return CFD_OK;
 }
 
+// Register budgets of the FP64 face passes (2, 3 or 4 blocks of 128 per
+// SM, per direction), timed once per lattice shape in this process, at the
+// solver's first stage: that stage's prep runs first (it runs again in the
+// stage itself, writing the same values), then each budget's face pass on
+// the real inputs (their output, the face fluxes, is rewritten by the
+// stage).  A uniform state does not do: the exact divisions take data-
+// dependent paths, and budgets timed on one mispredicted the NACA0012 and
+// shocked-slab lattices by 10 %.  The best budget depends on the shape;
+// every budget gives the same bits.
+std::mutex g_fp64_face_mutex;
+std::map<std::array<int, 6>, std::array<int, 3>> g_fp64_face_cache;
+
+std::array<int, 6> fp64_face_key(const cfd_solver *s)
+{
+    const StructuredLaunch &S = s->S;
+    return {S.ni, S.nj, S.nk, S.per, S.loc8 ? 1 : 0, s->ctx->device};
+}
+
+cfd_status_t tune_fp64_faces(cfd_solver *s, int j)
+{
+    s->fp64_tune = false;
+    StructuredLaunch &S = s->S;
+    const std::array<int, 6> key = fp64_face_key(s);
+    {
+        std::lock_guard<std::mutex> lock(g_fp64_face_mutex);
+        auto it = g_fp64_face_cache.find(key);
+        if (it != g_fp64_face_cache.end()) {
+            for (int d = 0; d < 3; ++d) S.face_mb[d] = it->second[d];
+            return CFD_OK;
+        }
+    }
+    cudaStream_t st = s->ctx->stream;
+    fp64_prep_pass(S, j);
+    s->ctx->launches += 1;
+    cudaEvent_t t0, t1;
+    if (cudaEventCreate(&t0) != cudaSuccess || cudaEventCreate(&t1) != cudaSuccess)
+        return cuda_fail(s->ctx, cudaGetLastError(), "FP64 face tuner events");
+    std::array<int, 3> pick = {S.face_mb[0], S.face_mb[1], S.face_mb[2]};
+    for (int d = 0; d < 3; ++d) {
+        float best = 1e30f;
+        for (int mb : {2, 3, 4}) {
+            fp64_face_pass(S, d, mb, st);   // warm-up
+            cudaEventRecord(t0, st);
+            for (int r = 0; r < 2; ++r) fp64_face_pass(S, d, mb, st);
+            cudaEventRecord(t1, st);
+            float ms = 1e30f;
+            if (cudaEventSynchronize(t1) == cudaSuccess) cudaEventElapsedTime(&ms, t0, t1);
+            s->ctx->launches += 3;
+            if (ms < best) best = ms, pick[d] = mb;
+        }
+    }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(s->ctx, e, "FP64 face tuner");
+    for (int d = 0; d < 3; ++d) S.face_mb[d] = pick[d];
+    std::lock_guard<std::mutex> lock(g_fp64_face_mutex);
+    g_fp64_face_cache[key] = pick;
+    return CFD_OK;
+}
+
 // where stage j's U_Q comes from (mixed form; the FP64 form always preps)
 int prep_source(const cfd_solver *s, int j)
 {
@@ -310,6 +374,10 @@ cfd_status_t run_stage(cfd_solver *s, int j, double dt, bool want_L)
     cfd_ctx *ctx = s->ctx;
     s->S.stream = ctx->stream;   // the context's stream may have been replaced
     if (s->path == CFD_PATH_STRUCTURED) {
+        if (s->fp64_tune) {
+            const cfd_status_t st = tune_fp64_faces(s, j);
+            if (st != CFD_OK) return st;
+        }
         ctx->launches += structured_stage(s->S, j, dt, want_L ? s->Lsoa : nullptr, nullptr, nullptr, prep_source(s, j));
         if (s->mixed) s->cur_slot = s->prep_ready = j == 2 ? 0 : j + 1;
         if (s->has_bc) {
@@ -471,6 +539,8 @@ cfd_status_t cfd_solver_info(const cfd_solver_t *s, cfd_solver_info_t *info)
     info->device_bytes = s->bytes;
     info->face_tile_i = s->mixed && s->path == CFD_PATH_STRUCTURED ? s->S.tile_i : 0;
     info->face_tile_jk = s->mixed && s->path == CFD_PATH_STRUCTURED ? s->S.tile_jk : 0;
+    if (!s->mixed && s->path == CFD_PATH_STRUCTURED)
+        for (int d = 0; d < 3; ++d) info->face_blocks[d] = s->S.face_mb[d];
     return CFD_OK;
 }
 
@@ -486,6 +556,23 @@ cfd_status_t cfd_solver_set_face_tiles(cfd_solver_t *s, int32_t tile_i, int32_t 
     cudaStreamSynchronize(s->ctx->stream);
     if (tile_i) s->S.tile_i = tile_i;
     if (tile_jk) s->S.tile_jk = tile_jk;
+    return CFD_OK;
+}
+
+cfd_status_t cfd_solver_set_face_blocks(cfd_solver_t *s, int32_t blocks_i, int32_t blocks_j, int32_t blocks_k)
+{
+    if (!s) return CFD_EINVAL;
+    if (s->mixed || s->path != CFD_PATH_STRUCTURED)
+        return fail(s->ctx, CFD_EUNSUPPORTED, "face blocks: FP64 lattice only");
+    const int32_t b[3] = {blocks_i, blocks_j, blocks_k};
+    for (int d = 0; d < 3; ++d)
+        if (b[d] != 0 && (b[d] < 2 || b[d] > 4)) return fail(s->ctx, CFD_EINVAL, "face blocks: 2, 3 or 4 (0 keeps)");
+    cfd_status_t st = use_device(s->ctx);
+    if (st != CFD_OK) return st;
+    cudaStreamSynchronize(s->ctx->stream);
+    for (int d = 0; d < 3; ++d)
+        if (b[d]) s->S.face_mb[d] = b[d];
+    s->fp64_tune = false;   // the caller's choice stands
     return CFD_OK;
 }
 
@@ -595,6 +682,10 @@ cfd_status_t cfd_solver_profile_stage(cfd_solver_t *s, int32_t j, double del_t, 
     for (auto &e : ev) cudaEventCreate(&e);
     const char *snames[kMaxStageLaunches + 1] = {};
     int nk = 3;
+    if (s->path == CFD_PATH_STRUCTURED && s->fp64_tune && (st = tune_fp64_faces(s, j)) != CFD_OK) {
+        for (auto &e : ev) cudaEventDestroy(e);
+        return st;
+    }
     if (s->path == CFD_PATH_STRUCTURED) {
         nk = structured_stage(s->S, j, del_t, nullptr, ev.data(), snames, prep_source(s, j));
         if (s->mixed) s->cur_slot = s->prep_ready = j == 2 ? 0 : j + 1;

@@ -13,7 +13,8 @@
 //   k_prep    pointwise: Q, U_j = det*Q (U_Q.cl), contravariant node fluxes
 //             F,E,G (Viscous.cl:560-631), sqrt(rho) and H for the Roe average
 //   k_visc    radius-2 star: viscous + MTS SGS fluxes Fv,Ev,Gv and mu
-//   k_face<d> one thread per face i+1/2 along d: Roe eigenvectors, WENO5,
+//   k_face<d, mb> one thread per face i+1/2 along d (face_fp64.cuh, at the
+//     register budget the solver's tuner picked): Roe eigenvectors, WENO5,
 //             LLF, 6th-order correction -> corrected face flux
 //   k_update  pointwise + radius-2: L = -(flux differences + viscous
 //             divergence), SSP-RK3 stage j, primitive recovery
@@ -26,21 +27,6 @@
 #include "internal.h"
 #include "lattice_fp64.cuh"
 #include "structured.h"
-
-// Minimum resident blocks per SM requested for the FP64 face kernels (their
-// register budget) along i and j, and along k.  With the divisions' rounding
-// on the integer pipe, 3 (168 registers at 128 threads per block) runs the
-// i and j passes best across the benchmark's lattices on GB300: 4 (128
-// registers, some spill) is 0.9 % faster on TGV 128^3 but 5-6 % slower on
-// the NACA0012 O-grid and the shocked slab, 2 is 7 % slower on TGV.  2 runs
-// the k pass fastest (6.33 against 6.70 ms at 3 on TGV; its stencil strides
-// a whole plane).
-#ifndef CFD_FACE_MIN_BLOCKS
-#define CFD_FACE_MIN_BLOCKS 3
-#endif
-#ifndef CFD_FACE_K_MIN_BLOCKS
-#define CFD_FACE_K_MIN_BLOCKS 2
-#endif
 
 namespace cfd {
 
@@ -66,12 +52,6 @@ __global__ void __launch_bounds__(128) k_mu_only(LatView g, int q)
     if (n < g.N) ex::mu_node(g, n, q);
 }
 
-template <int D>
-__global__ void __launch_bounds__(128, D == 2 ? CFD_FACE_K_MIN_BLOCKS : CFD_FACE_MIN_BLOCKS) k_face(LatView g)
-{
-    const int n = node_id();
-    if (n < g.N) ex::face_node<D>(g, n);
-}
 
 __global__ void __launch_bounds__(128) k_update(LatView g, int jst)
 {
@@ -128,15 +108,36 @@ int structured_stage(const StructuredLaunch &S, int jst, double dt, double *Lout
     else
         k_mu_only<<<nb, 128, 0, st>>>(g, jst);
     mark();
-    k_face<0><<<nb, 128, 0, st>>>(g);
+    fp64_face_pass(g, 0, S.face_mb[0], st);
     mark();
-    k_face<1><<<nb, 128, 0, st>>>(g);
+    fp64_face_pass(g, 1, S.face_mb[1], st);
     mark();
-    k_face<2><<<nb, 128, 0, st>>>(g);
+    fp64_face_pass(g, 2, S.face_mb[2], st);
     mark();
     k_update<<<nb, 128, 0, st>>>(g, jst);
     mark();
     return 6;
+}
+
+void fp64_face_pass(const LatView &g, int d, int mb, cudaStream_t st)
+{
+    if (mb == 2)
+        fp64_face_pass_mb2(g, d, st);
+    else if (mb == 4)
+        fp64_face_pass_mb4(g, d, st);
+    else
+        fp64_face_pass_mb3(g, d, st);
+}
+
+void fp64_face_pass(const StructuredLaunch &S, int d, int mb, cudaStream_t st)
+{
+    fp64_face_pass(make_view(S, 0.0, nullptr), d, mb, st);
+}
+
+void fp64_prep_pass(const StructuredLaunch &S, int jst)
+{
+    const LatView g = make_view(S, 0.0, nullptr);
+    k_prep<<<blocks_for(g.N, 128), 128, 0, S.stream>>>(g, jst);
 }
 
 void aos_to_soa(cudaStream_t st, const double *aos, int stride, int ncomp, long long N, double *soa, const int *row_of)

@@ -50,6 +50,9 @@ struct StructuredLaunch {
     // face-tile widths of the mixed and split face passes: faces along i
     // (32, 64 or 128) and along j and k (8, 16 or 32) per block of 128
     int tile_i = 64, tile_jk = 16;
+    // FP64 form: blocks of 128 per SM the face passes along i, j, k request
+    // (2, 3 or 4: their register budget; the solver's tuner picks)
+    int face_mb[3] = {3, 3, 2};
     int per = 7;
     const unsigned char *loc8 = nullptr;
     int locdirs = 0;
@@ -151,6 +154,14 @@ int structured_stage(const StructuredLaunch &S, int j, double dt, double *Lout, 
 // One face pass along d with face tiles of width `tile` (the tuner's
 // candidates, mixed.cu / split.cu), and a uniform state in the FP32 face
 // inputs (Q32, R32, FEG32) for timing them before any state exists.
+// The FP64 face pass along d at `mb` blocks per SM (face_fp64_mb*.cu), and
+// stage jst's prep alone (the face passes' inputs, for the tuner).
+void fp64_face_pass_mb2(const LatView &g, int d, cudaStream_t st);
+void fp64_face_pass_mb3(const LatView &g, int d, cudaStream_t st);
+void fp64_face_pass_mb4(const LatView &g, int d, cudaStream_t st);
+void fp64_face_pass(const LatView &g, int d, int mb, cudaStream_t st);
+void fp64_face_pass(const StructuredLaunch &S, int d, int mb, cudaStream_t st);
+void fp64_prep_pass(const StructuredLaunch &S, int jst);
 void mixed_face_pass(const StructuredLaunch &S, int d, int tile, cudaStream_t st);
 void split_face_pass(const StructuredLaunch &S, int d, int tile, cudaStream_t st);
 void reduced_uniform_inputs(const StructuredLaunch &S, cudaStream_t st);

@@ -204,6 +204,7 @@ class SolverInfo:
     precision: str
     device_bytes: int
     face_tiles: tuple = (0, 0)     # (along i, along j and k); mixed/split lattices
+    face_blocks: tuple = (0, 0, 0)  # blocks per SM of the i, j, k face passes; FP64 lattices
 
 
 class Boundary:
@@ -301,12 +302,19 @@ class Solver:
         i = abi.SolverInfo()
         self.ctx.check(self.lib.cfd_solver_info(self.h, C.byref(i)), "cfd_solver_info")
         return SolverInfo("structured" if i.path == abi.PATH_STRUCTURED else "gather", (i.ni, i.nj, i.nk),
-                          abi.PREC_NAMES[i.precision], int(i.device_bytes), (int(i.face_tile_i), int(i.face_tile_jk)))
+                          abi.PREC_NAMES[i.precision], int(i.device_bytes), (int(i.face_tile_i), int(i.face_tile_jk)),
+                          tuple(int(b) for b in i.face_blocks))
 
     def set_face_tiles(self, tile_i: int = 0, tile_jk: int = 0):
         """Fix the face-tile widths of a mixed or split lattice solver."""
         self.ctx.check(self.lib.cfd_solver_set_face_tiles(self.h, int(tile_i), int(tile_jk)),
                        "cfd_solver_set_face_tiles")
+
+    def set_face_blocks(self, blocks_i: int = 0, blocks_j: int = 0, blocks_k: int = 0):
+        """Fix the register budgets (blocks per SM) of an FP64 lattice solver's
+        face passes."""
+        self.ctx.check(self.lib.cfd_solver_set_face_blocks(self.h, int(blocks_i), int(blocks_j), int(blocks_k)),
+                       "cfd_solver_set_face_blocks")
 
     def set_flow(self, flow: np.ndarray):
         assert flow.shape == (self.g_node + 1, L.NFLOW) and flow.dtype == np.float64

@@ -253,6 +253,9 @@ typedef struct {
     uint64_t device_bytes;     /* device memory held by the solver           */
     int32_t face_tile_i;       /* mixed/split lattice: faces per tile along i */
     int32_t face_tile_jk;      /*   and along j and k (0 otherwise)          */
+    int32_t face_blocks[3];    /* FP64 lattice: blocks of 128 per SM the i, j,
+                                  k face passes request (0 otherwise)        */
+    int32_t reserved2;
 } cfd_solver_info_t;
 
 typedef struct cfd_solver cfd_solver_t;
@@ -275,6 +278,14 @@ cfd_status_t cfd_solver_info(const cfd_solver_t *s, cfd_solver_info_t *info);
  * shape in the process and keeps the fastest; the widths change no result
  * bit.  CFD_EUNSUPPORTED for FP64 or gather-path solvers. */
 cfd_status_t cfd_solver_set_face_tiles(cfd_solver_t *s, int32_t tile_i, int32_t tile_jk);
+/* Register budgets of the FP64 face passes along i, j and k: the blocks of
+ * 128 threads per SM their launch bounds request (2, 3 or 4; 0 keeps one).
+ * The solver's first stage times the three per direction on its real
+ * inputs, once per lattice shape in the process, and keeps the fastest
+ * (cfd_solver_info reports 3, 3, 2 before that); every budget gives the same
+ * bits.
+ * CFD_EUNSUPPORTED for the reduced forms and gather-path solvers. */
+cfd_status_t cfd_solver_set_face_blocks(cfd_solver_t *s, int32_t blocks_i, int32_t blocks_j, int32_t blocks_k);
 /* State in/out as FLOW rows 0..g_node (host pointers). */
 cfd_status_t cfd_solver_set_flow(cfd_solver_t *s, const cfd_flow_t *flow_host);
 cfd_status_t cfd_solver_get_flow(cfd_solver_t *s, cfd_flow_t *flow_host);
