@@ -114,7 +114,7 @@ static double ieee_div(double x, double b) { return x / b; }
 // 1/b normal (b below 2^1022), the significand of q0 in
 // [2^52 + 3, 2^53 - 2] (a step of up to two ulps then rounds within the
 // binade, or lands exactly on its upper end) and |R/B| < 5/2 (it is at most
-// 3/2 when y = RN(1/b)); everything else takes the division.  One FP64
+// 3/2 when y = RN(1/b)); everything else takes div_rare.  One FP64
 // multiply instead of the four FP64 operations of quotient().
 CFD_XDIV_HD double quotient_int(double x, double b, double y, bool &ok)
 {
@@ -133,10 +133,28 @@ CFD_XDIV_HD double quotient_int(double x, double b, double y, bool &ok)
     return from_bits(uq + (uint64_t)(int64_t)d);
 }
 
+// x / b outside the plain cases.  A zero x over a normal b is the zero whose
+// sign is the exclusive or of the operands' signs (IEEE 754 6.3), set on the
+// integer pipe: flows that stay two-dimensional in a three-dimensional
+// lattice divide exact zeros (a velocity component, a metric term, a
+// derivative across the extrusion) at every node and face.  Everything else
+// is the IEEE division.  Out of line, as the division was: the plain case
+// carries none of it and the kernels' code stays the size it was.
+#if defined(__CUDACC__)
+static __host__ __device__ __noinline__ double div_rare(double x, double b)
+#else
+static double div_rare(double x, double b)
+#endif
+{
+    const uint64_t ux = bits(x), ub = bits(b);
+    if ((ux << 1) == 0 && (unsigned)((ub >> 52) & 0x7ff) - 1u < 2046u) return from_bits((ux ^ ub) & 0x8000000000000000ULL);
+    return ieee_div(x, b);
+}
+
 #if defined(__CUDACC__)
 // 1 / b rounded to nearest even, for b whose reciprocal is a normal number
 // (biased exponent eb in [1, 2044]) and whose significand B is not a power
-// of two (that reciprocal is exact and returned directly): a float
+// of two (rcp returns that exact reciprocal in its rare branch): a float
 // reciprocal of B's top 24 bits seeds one Newton step on the FP64 pipe,
 //   e = RN(1 - |b| y0),  y1 = RN(y0 e + y0)   (relative error ~2^-47),
 // and the rounding is then decided on the integer pipe: with Y the
@@ -170,6 +188,19 @@ __device__ __forceinline__ double rcp_int(double b, bool &ok)
          && R2 > -5 * Bs && (Yn >> 52) == 1u;
     return from_bits(sign | ((uint64_t)(2045 - eb) << 52) | (Yn & 0x000fffffffffffffULL));
 }
+
+// 1 / b outside rcp_int's plain case: a power of two b = 2^(eb - 1023) has
+// the exact reciprocal 2^(1023 - eb), biased exponent 2046 - eb, normal for
+// eb in [1, 2045] (a density or a metric of exactly 1 is common); anything
+// else is the IEEE division.  Out of line.
+static __device__ __noinline__ double rcp_rare(double b)
+{
+    const uint64_t ub = bits(b);
+    const unsigned eb = (unsigned)(ub >> 52) & 0x7ffu;
+    if ((ub & 0x000fffffffffffffULL) == 0 && eb - 1u < 2045u)
+        return from_bits((ub & 0x8000000000000000ULL) | ((uint64_t)(2046u - eb) << 52));
+    return 1.0 / b;
+}
 #endif
 
 // 1 / b, the same bits as the IEEE division (rcp_int's plain case on the
@@ -185,7 +216,7 @@ CFD_XDIV_HD double rcp(double b)
         bool ok;
         const double y = rcp_int(b, ok);
         if (__builtin_expect(ok, 1)) return y;
-        return ieee_div(1.0, b);
+        return rcp_rare(b);
     }
 #endif
     return 1.0 / b;
@@ -204,7 +235,7 @@ CFD_XDIV_HD double div(double x, double b, double y)
     bool ok;
     const double q = CFD_XDIV_INT ? quotient_int(x, b, y, ok) : quotient(x, b, y, ok);
     if (__builtin_expect(ok, 1)) return q;
-    return ieee_div(x, b);
+    return div_rare(x, b);
 }
 
 // x / b for a divisor used once: its reciprocal (rcp) and the quotient's

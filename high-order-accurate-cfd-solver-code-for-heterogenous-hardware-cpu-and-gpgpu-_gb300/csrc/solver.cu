@@ -57,7 +57,7 @@ struct cfd_solver {
     cfd::LatticeMap map;        // lattice path: rows <-> nodes
     cfd::BcDevice bc;           // boundary routine after every stage
     bool has_bc = false;
-    bool fp64_tune = false;     // FP64 lattice: time the face passes' budgets at the first stage
+    int fp64_tune = -1;         // FP64 lattice: stages before the face passes' budgets are timed (-1: none)
 };
 
 namespace {
@@ -233,7 +233,7 @@ cfd_status_t create_structured(cfd_solver *s, const cfd_geometry_t *g)
     cudaError_t e = cudaStreamSynchronize(S.stream);   // host vectors go out of scope
     if (e != cudaSuccess) return cuda_fail(s->ctx, e, "solver create sync");
     if (s->mixed) return tune_face_tiles(s);
-    s->fp64_tune = true;   // on the first stage's real inputs (tune_fp64_faces)
+    s->fp64_tune = 1;   // on the second stage's real inputs (tune_fp64_faces)
     return CFD_OK;
 }
 
@@ -302,13 +302,15 @@ cfd_status_t tune_face_tiles(cfd_solver *s)
 
 // Register budgets of the FP64 face passes (2, 3 or 4 blocks of 128 per
 // SM, per direction), timed once per lattice shape in this process, at the
-// solver's first stage: that stage's prep runs first (it runs again in the
+// solver's second stage: that stage's prep runs first (it runs again in the
 // stage itself, writing the same values), then each budget's face pass on
 // the real inputs (their output, the face fluxes, is rewritten by the
 // stage).  A uniform state does not do: the exact divisions take data-
 // dependent paths, and budgets timed on one mispredicted the NACA0012 and
-// shocked-slab lattices by 10 %.  The best budget depends on the shape;
-// every budget gives the same bits.
+// shocked-slab lattices by 10 %.  Nor does the first stage of an impulsive
+// start, whose state is still exactly uniform (zeros and ones everywhere)
+// where every later stage carries rounding-level differences.  The best
+// budget depends on the shape; every budget gives the same bits.
 std::mutex g_fp64_face_mutex;
 std::map<std::array<int, 6>, std::array<int, 3>> g_fp64_face_cache;
 
@@ -320,7 +322,7 @@ std::array<int, 6> fp64_face_key(const cfd_solver *s)
 
 cfd_status_t tune_fp64_faces(cfd_solver *s, int j)
 {
-    s->fp64_tune = false;
+    s->fp64_tune = -1;
     StructuredLaunch &S = s->S;
     const std::array<int, 6> key = fp64_face_key(s);
     {
@@ -374,9 +376,11 @@ cfd_status_t run_stage(cfd_solver *s, int j, double dt, bool want_L)
     cfd_ctx *ctx = s->ctx;
     s->S.stream = ctx->stream;   // the context's stream may have been replaced
     if (s->path == CFD_PATH_STRUCTURED) {
-        if (s->fp64_tune) {
+        if (s->fp64_tune == 0) {
             const cfd_status_t st = tune_fp64_faces(s, j);
             if (st != CFD_OK) return st;
+        } else if (s->fp64_tune > 0) {
+            --s->fp64_tune;
         }
         ctx->launches += structured_stage(s->S, j, dt, want_L ? s->Lsoa : nullptr, nullptr, nullptr, prep_source(s, j));
         if (s->mixed) s->cur_slot = s->prep_ready = j == 2 ? 0 : j + 1;
@@ -572,7 +576,7 @@ cfd_status_t cfd_solver_set_face_blocks(cfd_solver_t *s, int32_t blocks_i, int32
     cudaStreamSynchronize(s->ctx->stream);
     for (int d = 0; d < 3; ++d)
         if (b[d]) s->S.face_mb[d] = b[d];
-    s->fp64_tune = false;   // the caller's choice stands
+    s->fp64_tune = -1;   // the caller's choice stands
     return CFD_OK;
 }
 
@@ -682,7 +686,7 @@ cfd_status_t cfd_solver_profile_stage(cfd_solver_t *s, int32_t j, double del_t, 
     for (auto &e : ev) cudaEventCreate(&e);
     const char *snames[kMaxStageLaunches + 1] = {};
     int nk = 3;
-    if (s->path == CFD_PATH_STRUCTURED && s->fp64_tune && (st = tune_fp64_faces(s, j)) != CFD_OK) {
+    if (s->path == CFD_PATH_STRUCTURED && s->fp64_tune >= 0 && (st = tune_fp64_faces(s, j)) != CFD_OK) {
         for (auto &e : ev) cudaEventDestroy(e);
         return st;
     }

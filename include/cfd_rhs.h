@@ -280,7 +280,7 @@ cfd_status_t cfd_solver_info(const cfd_solver_t *s, cfd_solver_info_t *info);
 cfd_status_t cfd_solver_set_face_tiles(cfd_solver_t *s, int32_t tile_i, int32_t tile_jk);
 /* Register budgets of the FP64 face passes along i, j and k: the blocks of
  * 128 threads per SM their launch bounds request (2, 3 or 4; 0 keeps one).
- * The solver's first stage times the three per direction on its real
+ * The solver's second stage times the three per direction on its real
  * inputs, once per lattice shape in the process, and keeps the fastest
  * (cfd_solver_info reports 3, 3, 2 before that); every budget gives the same
  * bits.

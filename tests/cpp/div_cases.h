@@ -2,8 +2,8 @@
 // patterns of every class, magnitudes of a flow solution, quotients within
 // ~2^-53 ulp of a rounding midpoint (for odd 54-bit M and small c,
 // B = c/M mod 2^54 gives B*M = K*2^54 + c, and K/B lies c/(2B) ulp from
-// the midpoint M*2^-54), exact quotients, extreme exponents, and the
-// special values.
+// the midpoint M*2^-54), exact quotients, zero numerators, power-of-two
+// divisors, extreme exponents, and the special values.
 #pragma once
 
 #include <cmath>
@@ -88,6 +88,9 @@ inline void make(long n, uint64_t seed, std::vector<double> &X, std::vector<doub
             const double b = std::ldexp((double)(r.next() >> 35), -(int)(r.next() % 30)) + 1.0;
             add(q * b, b);
         }
+        add((r.next() & 1) ? 0.0 : -0.0, ordinary(r));   // zero numerators
+        // power-of-two divisors, subnormal to the largest
+        add(ordinary(r), std::ldexp((r.next() & 1) ? 1.0 : -1.0, (int)(r.next() % 2098) - 1074));
         {
             const int e1 = (int)(r.next() % 2046) + 1, e2 = (int)(r.next() % 2046) + 1;
             add(from_bits(((uint64_t)e1 << 52) | (r.next() & 0x000fffffffffffffULL)),
