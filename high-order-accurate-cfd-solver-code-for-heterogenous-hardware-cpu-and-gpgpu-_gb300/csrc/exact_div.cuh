@@ -133,21 +133,31 @@ CFD_XDIV_HD double quotient_int(double x, double b, double y, bool &ok)
     return from_bits(uq + (uint64_t)(int64_t)d);
 }
 
-// x / b outside the plain cases.  A zero x over a normal b is the zero whose
-// sign is the exclusive or of the operands' signs (IEEE 754 6.3), set on the
-// integer pipe: flows that stay two-dimensional in a three-dimensional
-// lattice divide exact zeros (a velocity component, a metric term, a
-// derivative across the extrusion) at every node and face.  Everything else
-// is the IEEE division.  Out of line, as the division was: the plain case
-// carries none of it and the kernels' code stays the size it was.
+// x / b outside the plain cases.  Zero and infinite operands have exact
+// results (IEEE 754 6.1, 6.3, 7.3): 0 / nonzero and finite / Inf are zeros,
+// nonzero / 0 and Inf / finite are infinities, each with the exclusive or of
+// the operands' signs; they are set on the integer pipe.  Flows that stay
+// two-dimensional in a three-dimensional lattice divide exact zeros (a
+// velocity component, a metric term, a derivative across the extrusion) at
+// every node and face, and the MTS model divides by a test-filter value of
+// exactly 0 across the extrusion and then by the infinite quotient.
+// Everything else (0 / 0, Inf / Inf, NaN, subnormal operands, quotients near
+// the ends of the range) is the IEEE division.  Out of line, as the division
+// was: the plain case carries none of it and the kernels' code stays the
+// size it was.
 #if defined(__CUDACC__)
 static __host__ __device__ __noinline__ double div_rare(double x, double b)
 #else
 static double div_rare(double x, double b)
 #endif
 {
+    constexpr uint64_t kSign = 0x8000000000000000ULL, kInf = 0x7ff0000000000000ULL;
     const uint64_t ux = bits(x), ub = bits(b);
-    if ((ux << 1) == 0 && (unsigned)((ub >> 52) & 0x7ff) - 1u < 2046u) return from_bits((ux ^ ub) & 0x8000000000000000ULL);
+    const uint64_t ax = ux & ~kSign, ab = ub & ~kSign, sign = (ux ^ ub) & kSign;
+    if (ax <= kInf && ab <= kInf && !(ax == ab && (ax == 0 || ax == kInf))) {
+        if (ax == 0 || ab == kInf) return from_bits(sign);
+        if (ab == 0 || ax == kInf) return from_bits(sign | kInf);
+    }
     return ieee_div(x, b);
 }
 
@@ -189,16 +199,20 @@ __device__ __forceinline__ double rcp_int(double b, bool &ok)
     return from_bits(sign | ((uint64_t)(2045 - eb) << 52) | (Yn & 0x000fffffffffffffULL));
 }
 
-// 1 / b outside rcp_int's plain case: a power of two b = 2^(eb - 1023) has
-// the exact reciprocal 2^(1023 - eb), biased exponent 2046 - eb, normal for
-// eb in [1, 2045] (a density or a metric of exactly 1 is common); anything
-// else is the IEEE division.  Out of line.
+// 1 / b outside rcp_int's plain case: 1 / +-0 = +-Inf and 1 / +-Inf = +-0
+// (IEEE 754 7.3, 6.1); a power of two b = 2^(eb - 1023) has the exact
+// reciprocal 2^(1023 - eb), biased exponent 2046 - eb, normal for eb in
+// [1, 2045] (a density or a metric of exactly 1 is common); anything else
+// is the IEEE division.  Out of line.
 static __device__ __noinline__ double rcp_rare(double b)
 {
-    const uint64_t ub = bits(b);
+    constexpr uint64_t kSign = 0x8000000000000000ULL, kInf = 0x7ff0000000000000ULL;
+    const uint64_t ub = bits(b), ab = ub & ~kSign;
+    if (ab == 0) return from_bits((ub & kSign) | kInf);
+    if (ab == kInf) return from_bits(ub & kSign);
     const unsigned eb = (unsigned)(ub >> 52) & 0x7ffu;
     if ((ub & 0x000fffffffffffffULL) == 0 && eb - 1u < 2045u)
-        return from_bits((ub & 0x8000000000000000ULL) | ((uint64_t)(2046u - eb) << 52));
+        return from_bits((ub & kSign) | ((uint64_t)(2046u - eb) << 52));
     return 1.0 / b;
 }
 #endif
