@@ -16,9 +16,10 @@
 // integers); the right side is |b| with its exponent moved, exact.
 // Anything outside the plain case -- a zero, subnormal or non-finite value
 // anywhere, q1 a power of two (whose lower neighbour is half an ulp away),
-// exponents near the range ends, or a failed test -- takes the IEEE division
-// x / b itself.  The results are therefore identical to x / b for all
-// inputs; the gain is 4 FP64 instructions per shared division instead of a
+// exponents near the range ends, or a failed test -- takes div_rare: IEEE
+// 754's exact results for zero and infinite operands, else the IEEE
+// division x / b itself.  The results are therefore identical to x / b for
+// all inputs; the gain is 4 FP64 instructions per shared division instead of a
 // full division sequence.  quotient_int goes further on a part whose FP64
 // rate is a small fraction of its integer rate: only q0 on the FP64 pipe,
 // its rounding decided from the exact integer remainder of the significands
