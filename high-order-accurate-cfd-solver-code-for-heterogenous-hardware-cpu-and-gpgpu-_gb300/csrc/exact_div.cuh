@@ -134,26 +134,50 @@ CFD_XDIV_HD double quotient_int(double x, double b, double y, bool &ok)
     return from_bits(uq + (uint64_t)(int64_t)d);
 }
 
-// x / b outside the plain cases.  Zero and infinite operands have exact
-// results (IEEE 754 6.1, 6.3, 7.3): 0 / nonzero and finite / Inf are zeros,
-// nonzero / 0 and Inf / finite are infinities, each with the exclusive or of
-// the operands' signs; they are set on the integer pipe.  Flows that stay
-// two-dimensional in a three-dimensional lattice divide exact zeros (a
-// velocity component, a metric term, a derivative across the extrusion) at
-// every node and face, and the MTS model divides by a test-filter value of
-// exactly 0 across the extrusion and then by the infinite quotient.
-// Everything else (0 / 0, Inf / Inf, NaN, subnormal operands, quotients near
-// the ends of the range) is the IEEE division.  Out of line, as the division
-// was: the plain case carries none of it and the kernels' code stays the
-// size it was.
+// x / b given y = 1 / b, outside quotient_int's plain case.
+//  * q0 = RN(x*y) within three ulps of either end of its binade (the plain
+//    case's margin): x / b is (Q + R/B) ulps as there, and when that lies in
+//    q0's binade -- F*B + R >= 0 at the lower end (x / b at least 2^e), R <
+//    (2^52 - F)*B at the upper end (below 2^(e+1)) -- rounding at q0's ulp
+//    is correct, and a step onto 2^(e+1) carries into the exponent field.
+//    Exact powers of two and their neighbours are common quotients: a WENO
+//    weight over three equal smoothness indicators (a uniform region), a
+//    unit normal's component on an extruded lattice.
+//  * Zero and infinite operands have exact results (IEEE 754 6.1, 6.3, 7.3):
+//    0 / nonzero and finite / Inf are zeros, nonzero / 0 and Inf / finite
+//    are infinities, each with the exclusive or of the operands' signs.
+//    Flows that stay two-dimensional in a three-dimensional lattice divide
+//    exact zeros (a velocity component, a metric term, a derivative across
+//    the extrusion) at every node and face, and the MTS model divides by a
+//    test-filter value of exactly 0 across the extrusion and then by the
+//    infinite quotient.
+// All on the integer pipe; everything else (0 / 0, Inf / Inf, NaN,
+// subnormal operands, quotients near the ends of the range or leaving q0's
+// binade) is the IEEE division.  Out of line, as the division was: the
+// plain case carries none of it and the kernels' code stays the size it was.
 #if defined(__CUDACC__)
-static __host__ __device__ __noinline__ double div_rare(double x, double b)
+static __host__ __device__ __noinline__ double div_rare(double x, double b, double y)
 #else
-static double div_rare(double x, double b)
+static double div_rare(double x, double b, double y)
 #endif
 {
     constexpr uint64_t kSign = 0x8000000000000000ULL, kInf = 0x7ff0000000000000ULL;
+    constexpr uint64_t kFrac = 0x000fffffffffffffULL, kHidden = 0x0010000000000000ULL;
     const uint64_t ux = bits(x), ub = bits(b);
+    {
+        const double q0 = mul_rn(x, y);
+        const uint64_t uq = bits(q0);
+        const int ex = (int)((ux >> 52) & 0x7ff), eb = (int)((ub >> 52) & 0x7ff), eq = (int)((uq >> 52) & 0x7ff);
+        const uint64_t X = (ux & kFrac) | kHidden, B = (ub & kFrac) | kHidden, F = uq & kFrac;
+        const int s = ex - eb - eq + 1075;
+        const int64_t R = (int64_t)((X << (s & 63)) - (F | kHidden) * B);
+        const int64_t R2 = R * 2, Bs = (int64_t)B, B3 = 3 * (int64_t)B;
+        const int d = (int)(R2 > Bs) + (int)(R2 > B3) - (int)(R2 < -Bs) - (int)(R2 < -B3);
+        if ((unsigned)(ex - 1) < 2046u && (unsigned)(eb - 1) < 2044u && (unsigned)(eq - 1) < 2045u
+            && (unsigned)(s - 52) < 2u && R2 < 5 * Bs && R2 > -5 * Bs
+            && ((F < 3u && R + (int64_t)F * Bs >= 0) || (F > kFrac - 3u && R < (int64_t)(kHidden - F) * Bs)))
+            return from_bits(uq + (uint64_t)(int64_t)d);
+    }
     const uint64_t ax = ux & ~kSign, ab = ub & ~kSign, sign = (ux ^ ub) & kSign;
     if (ax <= kInf && ab <= kInf && !(ax == ab && (ax == 0 || ax == kInf))) {
         if (ax == 0 || ab == kInf) return from_bits(sign);
@@ -250,7 +274,7 @@ CFD_XDIV_HD double div(double x, double b, double y)
     bool ok;
     const double q = CFD_XDIV_INT ? quotient_int(x, b, y, ok) : quotient(x, b, y, ok);
     if (__builtin_expect(ok, 1)) return q;
-    return div_rare(x, b);
+    return div_rare(x, b, y);
 }
 
 // x / b for a divisor used once: its reciprocal (rcp) and the quotient's

@@ -2,8 +2,9 @@
 // patterns of every class, magnitudes of a flow solution, quotients within
 // ~2^-53 ulp of a rounding midpoint (for odd 54-bit M and small c,
 // B = c/M mod 2^54 gives B*M = K*2^54 + c, and K/B lies c/(2B) ulp from
-// the midpoint M*2^-54), exact quotients, zero numerators, power-of-two
-// divisors, extreme exponents, and the special values.
+// the midpoint M*2^-54), exact quotients, quotients at and next to a power
+// of two, zero numerators, power-of-two divisors, extreme exponents, and the
+// special values.
 #pragma once
 
 #include <cmath>
@@ -89,6 +90,14 @@ inline void make(long n, uint64_t seed, std::vector<double> &X, std::vector<doub
             add(q * b, b);
         }
         add((r.next() & 1) ? 0.0 : -0.0, ordinary(r));   // zero numerators
+        {   // quotients at the ends of a binade: exact powers of two and their neighbours
+            const double b = ordinary(r);
+            const int k = (int)(r.next() % 40) - 20, m = (int)(r.next() % 7) - 3;
+            add(std::ldexp(b, k), b);
+            add(std::ldexp(std::nextafter(b, m < 0 ? 0.0 : 2.0 * b), k), b);
+            add(std::ldexp(b, k) * (1.0 + m * 0x1p-52), b);
+            add(std::ldexp(b, k), b * (1.0 + m * 0x1p-52));
+        }
         // power-of-two divisors, subnormal to the largest
         add(ordinary(r), std::ldexp((r.next() & 1) ? 1.0 : -1.0, (int)(r.next() % 2098) - 1074));
         {
