@@ -265,9 +265,12 @@ cfd_status_t tune_face_tiles(cfd_solver *s)
         else mixed_face_pass(S, d, tile, st);
     };
     reduced_uniform_inputs(S, st);
-    cudaEvent_t t0, t1;
-    if (cudaEventCreate(&t0) != cudaSuccess || cudaEventCreate(&t1) != cudaSuccess)
-        return cuda_fail(s->ctx, cudaGetLastError(), "face-tile tuner events");
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    if (cudaEventCreate(&t0) != cudaSuccess || cudaEventCreate(&t1) != cudaSuccess) {
+        const cudaError_t ce = cudaGetLastError();
+        if (t0) cudaEventDestroy(t0);
+        return cuda_fail(s->ctx, ce, "face-tile tuner events");
+    }
     auto time_ms = [&](std::initializer_list<int> dirs, int tile) {
         for (int d : dirs) pass(d, tile);   // warm-up
         cudaEventRecord(t0, st);
@@ -336,9 +339,12 @@ cfd_status_t tune_fp64_faces(cfd_solver *s, int j)
     cudaStream_t st = s->ctx->stream;
     fp64_prep_pass(S, j);
     s->ctx->launches += 1;
-    cudaEvent_t t0, t1;
-    if (cudaEventCreate(&t0) != cudaSuccess || cudaEventCreate(&t1) != cudaSuccess)
-        return cuda_fail(s->ctx, cudaGetLastError(), "FP64 face tuner events");
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    if (cudaEventCreate(&t0) != cudaSuccess || cudaEventCreate(&t1) != cudaSuccess) {
+        const cudaError_t ce = cudaGetLastError();
+        if (t0) cudaEventDestroy(t0);
+        return cuda_fail(s->ctx, ce, "FP64 face tuner events");
+    }
     std::array<int, 3> pick = {S.face_mb[0], S.face_mb[1], S.face_mb[2]};
     for (int d = 0; d < 3; ++d) {
         float best = 1e30f;
