@@ -1,5 +1,9 @@
 // batch_fp64.cu -- the batched persistent stage kernel instantiated with the
 // per-node operations of the exact FP64 evaluation order (compiled with --fmad=false) form.
+// The batched stage runs 8 warps per SM: too few to hide the integer
+// product's latency, so the divisions' first quotient comes from the FP64
+// multiply (exact_div.cuh, CFD_XDIV_QPROD; the same bits either way).
+#define CFD_XDIV_QPROD 0
 #include "batch_kernel.cuh"
 #include "batch_ops.h"
 #include "internal.h"

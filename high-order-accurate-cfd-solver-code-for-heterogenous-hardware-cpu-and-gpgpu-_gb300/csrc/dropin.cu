@@ -24,6 +24,11 @@
 // k_weno<true> reads both faces from the scratch, which keeps the FP64 face
 // code and its registers out of it.  The results are the same bits either
 // way.
+// The drop-in's face kernel runs at 2 blocks of 128 per SM: too few warps
+// to hide the integer product's latency, so the divisions' first quotient
+// comes from the FP64 multiply (exact_div.cuh, CFD_XDIV_QPROD; the same bits
+// either way).
+#define CFD_XDIV_QPROD 0
 #include <algorithm>
 
 #include "internal.h"

@@ -35,8 +35,27 @@
 #define CFD_XDIV_HD inline
 #endif
 
+// Where quotient_int's first quotient q0 comes from: 1 (the default) the
+// top 53 bits of the integer product of the significands of x and y (no
+// FP64 instruction; the faster choice in kernels with warps to hide its
+// integer latency, 3 or more blocks of 128 per SM), 0 the FP64 product
+// RN(x*y) (kernels at 2 blocks per SM: the drop-in's face kernel, the
+// batched stage, the FP64 face passes at that budget).  A translation unit
+// sets it before its first include; the two variants live in different
+// inline namespaces, so the host functions of units built with different
+// choices do not collide at link time.  Both give the same bits.
+#ifndef CFD_XDIV_QPROD
+#define CFD_XDIV_QPROD 1
+#endif
+#if CFD_XDIV_QPROD
+#define CFD_XDIV_VARIANT qprod_int
+#else
+#define CFD_XDIV_VARIANT qprod_fp64
+#endif
+
 namespace cfd {
 namespace xdiv {
+inline namespace CFD_XDIV_VARIANT {
 
 CFD_XDIV_HD uint64_t bits(double v)
 {
@@ -103,35 +122,72 @@ static __host__ __device__ __noinline__ double ieee_div(double x, double b) { re
 static double ieee_div(double x, double b) { return x / b; }
 #endif
 
-// x / b given y = 1 / b (IEEE), with the rounding decided on the integer
-// pipe.  q0 = RN(x*y) lies within two ulps of x/b.  With significands X, B,
-// Q (53-bit integers, hidden bit set) and s = ex - eb - eq + 1075 (52 or 53
-// in the plain case), X*2^s and Q*B are the dividend and q0 times the
-// divisor on a common scale, so R = X*2^s - Q*B is the exact remainder
-// (|R| < 2^56: the low 64 bits of both products give it).  x/b is
-// (Q + R/B) ulps, never exactly halfway between two doubles, so the
-// correctly rounded quotient is q0 moved by the nearest integer to R/B,
-// found by comparing 2R with +-B and +-3B.  The plain case: x, q0 and
-// 1/b normal (b below 2^1022), the significand of q0 in
-// [2^52 + 3, 2^53 - 2] (a step of up to two ulps then rounds within the
-// binade, or lands exactly on its upper end) and |R/B| < 5/2 (it is at most
-// 3/2 when y = RN(1/b)); everything else takes div_rare.  One FP64
-// multiply instead of the four FP64 operations of quotient().
-CFD_XDIV_HD double quotient_int(double x, double b, double y, bool &ok)
+// The high 64 bits of the 128-bit product a*b.
+CFD_XDIV_HD uint64_t mul_hi64(uint64_t a, uint64_t b)
 {
-    const double q0 = mul_rn(x, y);
-    const uint64_t ux = bits(x), ub = bits(b), uq = bits(q0);
-    const int ex = (int)((ux >> 52) & 0x7ff), eb = (int)((ub >> 52) & 0x7ff), eq = (int)((uq >> 52) & 0x7ff);
-    const uint64_t X = (ux & 0x000fffffffffffffULL) | 0x0010000000000000ULL;
-    const uint64_t B = (ub & 0x000fffffffffffffULL) | 0x0010000000000000ULL;
-    const uint64_t F = uq & 0x000fffffffffffffULL;
+#if defined(__CUDA_ARCH__)
+    return __umul64hi(a, b);
+#else
+    return (uint64_t)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+
+// x / b given y = 1 / b (IEEE), with the rounding decided on the integer
+// pipe.  q0 lies within two ulps of x/b: either RN(x*y), or x*y truncated
+// to 53 bits, from the high word of the product of the significands
+// shifted to the top of their words (X*Y in [2^104, 2^106), so
+// H = floor(X*Y / 2^42) lies in [2^62, 2^64) and its top 53 bits are
+// floor(X*Y / 2^(52 + t)), t = 1 when X*Y >= 2^105) -- y = RN(1/b) is within
+// half an ulp of 1/b and the truncation drops less than one.  With
+// significands X, B, Q (53-bit integers, hidden bit set) and
+// s = ex - eb - eq + 1075 (52 or 53 in the plain case), X*2^s and Q*B are
+// the dividend and q0 times the divisor on a common scale, so
+// R = X*2^s - Q*B is the exact remainder (|R| < 2^56: the low 64 bits of
+// both products give it).  x/b is (Q + R/B) ulps, never exactly halfway
+// between two doubles, so the correctly rounded quotient is q0 moved by the
+// nearest integer to R/B, found by comparing 2R with +-B and +-3B.  The
+// plain case: x, y, q0 and 1/b normal (b below 2^1022), the significand of
+// q0 in [2^52 + 3, 2^53 - 2] (a step of up to two ulps then rounds within
+// the binade, or lands exactly on its upper end) and |R/B| < 5/2;
+// everything else takes div_rare.  No FP64 instruction (QP = 1; one FP64
+// multiply with QP = 0) instead of the four of quotient().
+template <int QP>
+CFD_XDIV_HD double quotient_int_v(double x, double b, double y, bool &ok)
+{
+    constexpr uint64_t kFrac = 0x000fffffffffffffULL, kHidden = 0x0010000000000000ULL;
+    const uint64_t ux = bits(x), ub = bits(b);
+    const int ex = (int)((ux >> 52) & 0x7ff), eb = (int)((ub >> 52) & 0x7ff);
+    const uint64_t X = (ux & kFrac) | kHidden;
+    const uint64_t B = (ub & kFrac) | kHidden;
+    uint64_t uq;
+    int eq;
+    bool y_ok = true;
+    if (QP) {
+        const uint64_t uy = bits(y);
+        const int ey = (int)((uy >> 52) & 0x7ff);
+        const uint64_t H = mul_hi64(X << 11, ((uy & kFrac) | kHidden) << 11);
+        const int t = (int)(H >> 63);
+        eq = ex + ey - 1023 + t;
+        uq = ((ux ^ uy) & 0x8000000000000000ULL) | ((uint64_t)(eq & 0x7ff) << 52) | ((H >> (10 + t)) & kFrac);
+        y_ok = (unsigned)(ey - 1) < 2046u;
+    } else {
+        uq = bits(mul_rn(x, y));
+        eq = (int)((uq >> 52) & 0x7ff);
+    }
+    const uint64_t F = uq & kFrac;
     const int s = ex - eb - eq + 1075;
-    const int64_t R = (int64_t)((X << (s & 63)) - (F | 0x0010000000000000ULL) * B);
+    const int64_t R = (int64_t)((X << (s & 63)) - (F | kHidden) * B);
     const int64_t R2 = R * 2, Bs = (int64_t)B, B3 = 3 * (int64_t)B;
     const int d = (int)(R2 > Bs) + (int)(R2 > B3) - (int)(R2 < -Bs) - (int)(R2 < -B3);
-    ok = (unsigned)(ex - 1) < 2046u && (unsigned)(eb - 1) < 2044u && (unsigned)(eq - 1) < 2045u
+    ok = y_ok && (unsigned)(ex - 1) < 2046u && (unsigned)(eb - 1) < 2044u && (unsigned)(eq - 1) < 2045u
          && (unsigned)(s - 52) < 2u && F - 3u < 0x000ffffffffffffcULL && R2 < 5 * Bs && R2 > -5 * Bs;
     return from_bits(uq + (uint64_t)(int64_t)d);
+}
+
+// quotient_int_v with this translation unit's CFD_XDIV_QPROD.
+CFD_XDIV_HD double quotient_int(double x, double b, double y, bool &ok)
+{
+    return quotient_int_v<CFD_XDIV_QPROD>(x, b, y, ok);
 }
 
 // x / b given y = 1 / b, outside quotient_int's plain case.
@@ -334,5 +390,6 @@ CFD_XDIV_HD double pow2_over(double x)
     return ieee_div(c, x);
 }
 
+}  // namespace CFD_XDIV_VARIANT
 }  // namespace xdiv
 }  // namespace cfd

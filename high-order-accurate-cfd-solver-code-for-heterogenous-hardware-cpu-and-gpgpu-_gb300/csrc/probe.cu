@@ -70,8 +70,9 @@ __device__ __forceinline__ bool same32(float x, float y)
 
 // per thread `per` operand pairs of class cls; bad[0..4] count the
 // mismatches of f2d, d2f (and the hi/lo split), add/sub, mul and the
-// division from a shared reciprocal (xdiv::quotient_int where it accepts the
-// operands, and xdiv::div)
+// division from a shared reciprocal (xdiv::quotient_int_v, both ways of
+// forming its first quotient, where it accepts the operands; xdiv::div) and
+// the reciprocal (rcp_int, rcp, divide)
 __global__ void k_emu_check(int cls, uint64_t seed, int per, unsigned long long *bad)
 {
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -95,8 +96,10 @@ __global__ void k_emu_check(int cls, uint64_t seed, int per, unsigned long long 
         {
             const double y = 1.0 / b;
             bool ok;
-            const double q = xdiv::quotient_int(a, b, y, ok);
+            const double q = xdiv::quotient_int_v<1>(a, b, y, ok);   // first quotient: integer product
             nb[4] += ok && !same64(q, a / b);
+            const double qf = xdiv::quotient_int_v<0>(a, b, y, ok);  // first quotient: FP64 product
+            nb[4] += ok && !same64(qf, a / b);
             nb[4] += !same64(xdiv::div(a, b, y), a / b);
             const double yi = xdiv::rcp_int(b, ok);
             nb[4] += ok && !same64(yi, y);
