@@ -280,6 +280,84 @@ __device__ __forceinline__ double rcp_int(double b, bool &ok)
     return from_bits(sign | ((uint64_t)(2045 - eb) << 52) | (Yn & 0x000fffffffffffffULL));
 }
 
+#endif
+
+// float <-> bits and the float reciprocal RN(1/x) (the host's IEEE division
+// stands in for __frcp_rn); the high 64 bits of a signed 128-bit product.
+CFD_XDIV_HD uint32_t bits32(float v)
+{
+#if defined(__CUDA_ARCH__)
+    return __float_as_uint(v);
+#else
+    uint32_t u;
+    __builtin_memcpy(&u, &v, 4);
+    return u;
+#endif
+}
+
+CFD_XDIV_HD float from_bits32(uint32_t u)
+{
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(u);
+#else
+    float v;
+    __builtin_memcpy(&v, &u, 4);
+    return v;
+#endif
+}
+
+CFD_XDIV_HD float frcp_rn(float x)
+{
+#if defined(__CUDA_ARCH__)
+    return __frcp_rn(x);
+#else
+    volatile float one = 1.0f;
+    return one / x;
+#endif
+}
+
+CFD_XDIV_HD int64_t mul_hi64s(int64_t a, int64_t b)
+{
+#if defined(__CUDA_ARCH__)
+    return __mul64hi(a, b);
+#else
+    return (int64_t)(((__int128)a * b) >> 64);
+#endif
+}
+
+// rcp_int's case (b's reciprocal normal, B not a power of two) with the
+// Newton step on the integer pipe too, no FP64 instruction at all.  With S0
+// the significand of the float seed y0 = RN(1/m), m = B's top 24 bits as a
+// float in [1, 2) (y0 = S0 2^-24), eps = 1 - (B / 2^52) y0 is exactly
+// E / 2^76 with E = 2^76 - S0*B, and |eps| < 2^-22.4 (the seed is within
+// 2^-24, the 29 dropped bits within 2^-23), so |E| < 2^54 and the low 64
+// bits of S0*B give it.  2^105 / B = S0 2^29 / (1 - eps), so
+//   Y = S0 2^29 + S0 (E + E^2 / 2^76) / 2^47
+// (two terms of the series; the next is below 2^-13, the two floors below 2)
+// is within 2 of 2^105 / B, and the exact remainder R = 2^105 - Y*B
+// (|R| < 2^55) decides the rounding: Y moves by the nearest integer to R/B,
+// found by comparing 2R with +-B and +-3B.  ok = false outside the plain
+// case (a step out of [2^52, 2^53) included).
+CFD_XDIV_HD double rcp_int_i(double b, bool &ok)
+{
+    constexpr uint64_t kFrac = 0x000fffffffffffffULL, kHidden = 0x0010000000000000ULL;
+    const uint64_t ub = bits(b);
+    const int eb = (int)((ub >> 52) & 0x7ff);
+    const uint64_t F = ub & kFrac, B = F | kHidden;
+    const uint32_t rb = bits32(frcp_rn(from_bits32(0x3f800000u | (uint32_t)(F >> 29))));   // y0 in (0.5, 1]
+    const uint64_t S0 = (uint64_t)((rb & 0x7fffffu) | 0x800000u) << ((rb >> 23) - 126u);   // 2^23 .. 2^24
+    const int64_t E = (int64_t)(0ULL - S0 * B);
+    const int64_t E2 = mul_hi64s(E, E) >> 12;                          // E^2 / 2^76
+    const uint64_t Y = (S0 << 29) + (uint64_t)mul_hi64s((int64_t)(S0 << 17), E + E2);
+    const int64_t R = (int64_t)(0ULL - Y * B);
+    const int64_t R2 = 2 * R, Bs = (int64_t)B, B3 = 3 * (int64_t)B;
+    const int64_t d = (int64_t)(R2 > Bs) + (int64_t)(R2 > B3) - (int64_t)(R2 < -Bs) - (int64_t)(R2 < -B3);
+    const uint64_t Yn = Y + (uint64_t)d;
+    ok = (unsigned)(eb - 1) < 2044u && F != 0 && R2 < 5 * Bs && R2 > -5 * Bs && (Yn >> 52) == 1u;
+    return from_bits((ub & 0x8000000000000000ULL) | ((uint64_t)(2045 - eb) << 52) | (Yn & kFrac));
+}
+
+#if defined(__CUDACC__)
 // 1 / b outside rcp_int's plain case: 1 / +-0 = +-Inf and 1 / +-Inf = +-0
 // (IEEE 754 7.3, 6.1); a power of two b = 2^(eb - 1023) has the exact
 // reciprocal 2^(1023 - eb), biased exponent 2046 - eb, normal for eb in
@@ -304,12 +382,17 @@ static __device__ __noinline__ double rcp_rare(double b)
 #ifndef CFD_XDIV_RCP
 #define CFD_XDIV_RCP 1
 #endif
+// Which Newton step rcp uses: 1 rcp_int_i (integer pipe; by default where
+// the first quotient is the integer product too), 0 rcp_int (two FP64 FMAs).
+#ifndef CFD_XDIV_RCPI
+#define CFD_XDIV_RCPI CFD_XDIV_QPROD
+#endif
 CFD_XDIV_HD double rcp(double b)
 {
 #if defined(__CUDA_ARCH__)
     if (CFD_XDIV_RCP) {
         bool ok;
-        const double y = rcp_int(b, ok);
+        const double y = CFD_XDIV_RCPI ? rcp_int_i(b, ok) : rcp_int(b, ok);
         if (__builtin_expect(ok, 1)) return y;
         return rcp_rare(b);
     }

@@ -72,7 +72,7 @@ __device__ __forceinline__ bool same32(float x, float y)
 // mismatches of f2d, d2f (and the hi/lo split), add/sub, mul and the
 // division from a shared reciprocal (xdiv::quotient_int_v, both ways of
 // forming its first quotient, where it accepts the operands; xdiv::div) and
-// the reciprocal (rcp_int, rcp, divide)
+// the reciprocal (rcp_int and rcp_int_i, rcp, divide)
 __global__ void k_emu_check(int cls, uint64_t seed, int per, unsigned long long *bad)
 {
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -101,8 +101,10 @@ __global__ void k_emu_check(int cls, uint64_t seed, int per, unsigned long long 
             const double qf = xdiv::quotient_int_v<0>(a, b, y, ok);  // first quotient: FP64 product
             nb[4] += ok && !same64(qf, a / b);
             nb[4] += !same64(xdiv::div(a, b, y), a / b);
-            const double yi = xdiv::rcp_int(b, ok);
+            const double yi = xdiv::rcp_int(b, ok);   // Newton step on the FP64 pipe
             nb[4] += ok && !same64(yi, y);
+            const double yj = xdiv::rcp_int_i(b, ok);   // on the integer pipe
+            nb[4] += ok && !same64(yj, y);
             nb[4] += !same64(xdiv::rcp(b), y) + !same64(xdiv::divide(a, b), a / b);
         }
     }

@@ -1,6 +1,7 @@
 // exact_div_check.cpp -- cfd::xdiv::div(x, b, 1/b) against the host's IEEE
 // division x / b, bit for bit, on the pairs of div_cases.h, and
-// cfd::xdiv::scale2<K>(x) against x * 2^K on every operand of those pairs.
+// cfd::xdiv::scale2<K>(x) against x * 2^K and the integer-pipe reciprocal
+// cfd::xdiv::rcp_int_i(x) against 1 / x on every operand of those pairs.
 // Prints the share of plain-case quotients (no fallback division).
 //
 //   exact_div_check <rounds> <seed>
@@ -78,5 +79,25 @@ int main(int argc, char **argv)
             pcheck(x, cfd::xdiv::pow2_over<3>(x), 8.0);
         }
     std::printf("pow2_over: %ld cases, %ld pow2_over mismatches\n", pcases, pfails);
-    return fails == 0 && sfails == 0 && pfails == 0 ? 0 : 1;
+    // the integer-pipe reciprocal (rcp_int_i) where it accepts the operand
+    long rfails = 0, rcases = 0, rplain = 0;
+    for (const std::vector<double> *V : {&X, &B})
+        for (double x : *V) {
+            volatile double one = 1.0, vx = x;
+            const double want = one / vx;
+            bool ok;
+            const double got = cfd::xdiv::rcp_int_i(x, ok);
+            ++rcases;
+            if (!ok) continue;
+            ++rplain;
+            if (divcases::to_bits(got) != divcases::to_bits(want)) {
+                if (rfails < 10)
+                    std::printf("RCP MISMATCH x=%016llx want %016llx got %016llx\n", (unsigned long long)divcases::to_bits(x),
+                                (unsigned long long)divcases::to_bits(want), (unsigned long long)divcases::to_bits(got));
+                ++rfails;
+            }
+        }
+    std::printf("rcp_int_i: %ld cases, plain case %.4f, %ld rcp mismatches\n", rcases, (double)rplain / (double)rcases,
+                rfails);
+    return fails == 0 && sfails == 0 && pfails == 0 && rfails == 0 ? 0 : 1;
 }

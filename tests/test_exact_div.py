@@ -29,6 +29,7 @@ def test_exact_division_on_host(tmp_path, qprod):
     r = subprocess.run([str(exe), "1000000", "11"], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     assert " 0 mismatches" in r.stdout and " 0 scale2 mismatches" in r.stdout and " 0 pow2_over mismatches" in r.stdout
+    assert " 0 rcp mismatches" in r.stdout
 
 
 @pytest.mark.gpu
