@@ -2,8 +2,10 @@
 // along D: Roe average, LLF face flux and the sixth-order correction of
 // lattice_fp64.cuh face_node) at a register budget MB, the blocks of 128
 // threads per SM its launch bounds request.  face_fp64_mb2.cu, _mb3.cu and
-// _mb4.cu each compile one budget (in parallel); the solver times the three
-// per direction when it is created and keeps the fastest (the arithmetic is
+// _mb4.cu each compile one budget (in parallel; the 2-block unit forms its
+// divisions' first quotient and reciprocal on the FP64 pipe, the others on
+// the integer pipe, exact_div.cuh); the solver times the three per
+// direction at its second stage and keeps the fastest (the arithmetic is
 // the same in each: the same bits).  Include only from translation units
 // compiled with --fmad=false.
 #pragma once
