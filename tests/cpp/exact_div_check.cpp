@@ -97,6 +97,21 @@ int main(int argc, char **argv)
                 ++rfails;
             }
         }
+    // and densely at both ends of the significand range (the reciprocal's
+    // significand next to 2^53 and to 2^52), at five exponents
+    for (uint64_t f = 1; f < 100000; ++f)
+        for (uint64_t e : {(uint64_t)1, (uint64_t)500, (uint64_t)1023, (uint64_t)1800, (uint64_t)2044})
+            for (uint64_t F : {f, (uint64_t)0x0010000000000000ULL - f, f << 20}) {
+                const double x = divcases::from_bits((e << 52) | F);
+                volatile double one = 1.0, vx = x;
+                const double want = one / vx;
+                bool ok;
+                const double got = cfd::xdiv::rcp_int_i(x, ok);
+                ++rcases;
+                if (!ok) continue;
+                ++rplain;
+                if (divcases::to_bits(got) != divcases::to_bits(want)) ++rfails;
+            }
     std::printf("rcp_int_i: %ld cases, plain case %.4f, %ld rcp mismatches\n", rcases, (double)rplain / (double)rcases,
                 rfails);
     return fails == 0 && sfails == 0 && pfails == 0 && rfails == 0 ? 0 : 1;
