@@ -82,3 +82,33 @@ def test_static_node_limit_comes_from_the_header(pkg):
     text = (ROOT / "include" / "cfd_rhs.h").read_text()
     m = re.search(r"^#define\s+CFD_STATIC_MAX_NODES\s+(\d+)", text, flags=re.M)
     assert m and int(m.group(1)) == abi.STATIC_MAX_NODES
+
+
+def test_ctypes_mirrors_match_the_header(pkg, tmp_path):
+    """The Python mirrors of the header's structs (abi.Params, Geometry,
+    KernelTime, SolverInfo, BatchInfo) have the C layout: size and every
+    field's offset, as a C compiler lays out include/cfd_rhs.h."""
+    import shutil
+    import subprocess
+    from cfd_gb300 import abi
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    mirrors = {"cfd_params_t": abi.Params, "cfd_geometry_t": abi.Geometry, "cfd_kernel_time_t": abi.KernelTime,
+               "cfd_solver_info_t": abi.SolverInfo, "cfd_batch_info_t": abi.BatchInfo}
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "cfd_rhs.h"', "int main(void) {"]
+    for cname, py in mirrors.items():
+        lines.append(f'    printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'    printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["    return 0;", "}"]
+    src, exe = tmp_path / "layout.c", tmp_path / "layout"
+    src.write_text("\n".join(lines) + "\n")
+    r = subprocess.run(["gcc", "-Wall", "-Werror", f"-I{ROOT / 'include'}", str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = dict(((ln.split()[0], ln.split()[1]), int(ln.split()[2]))
+               for ln in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines())
+    for cname, py in mirrors.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
